@@ -1,0 +1,397 @@
+"""Benchmark of the GB300 FLIP substep (one JSON line on stdout, rank 0).
+
+Workload (default): the 256^3 dam break + falling sphere (x<0.35, y<0.5 block plus a
+sphere at (0.7, 0.8, 0.5), r = 0.12; 24,564,400 particles at 8 per cell, jittered
+uniform, seeded), dt = 1/480, solid walls, pressure solved to ||b-Ap||/||b|| < 1e-6 and
+max|b-Ap|*dx < 1e-5. A step is one FLIPMethod::advanceOneStep over all particles.
+
+  value  = particle-steps/s with particles resident in HBM, device time of each step
+           from CUDA events on the simulation's stream (max over ranks);
+  e2e    = the same metric through the C ABI with host buffers: every step uploads the
+           particles from pinned host memory, steps, and reads them back;
+  roofline = the dominant kernel class: algorithmic bytes per launch / its average
+           event-timed launch duration, against the measured HBM copy bandwidth;
+  cpu_baseline = the reference's algorithm (oracle restatement, bit-exact with the
+           reference's host build) on this host's cores, on a bounded sample.
+
+Multi-GPU: replicas only - each rank advances its own independent simulation (weak
+scaling, no collective on the data path); value sums all ranks' particle-steps over the
+slowest rank's time.
+
+--impl reference times the reference algorithm's CPU implementation (the oracle port,
+all host threads) on the same workload, metric and unit.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s at 256^3 FLIP (plain FP32 block-MIC(0)-PCG, max|div u|*dx < 1e-5)"
+UNIT = "particle-steps/s"
+
+# Algorithmic bytes per launch of each kernel class: (bytes per active cell, bytes per particle).
+#   pcg_direction: read z, d (8) + stencil code (2); write d', q (8)            -> 18 B/cell
+#   pcg_update:    read e, d, r, q (16) + M^-1 (4) + code (2); write e, r, z (12) -> 34 B/cell
+#   p2g:           per particle read idx (4) + pos, vel (24); per cell read dual-cell
+#                  starts (4), write mass, count, velocity (20) + flag (1)      -> 25 B/cell, 28 B/particle
+#   g2p:           per particle idx (4), read pos, vel, id (28), write (28), adjacency (4);
+#                  per cell read velo, comp, count (28)                          -> 28 B/cell, 64 B/particle
+#   velocity:      read flag (1), pres (4), velo (12); write pres (4), comp (12)  -> 33 B/cell
+#   rhs:           read flag (1), velo (12); write b (4), code (2); MIC read code (2), write M (4) -> 25 B/cell
+#   refine:        per pass read x (8), e (4), b (4), code (2); write x (8), r (4) -> 30 B/cell
+#   sort:          per particle read vkey (4), write key (4), read key (4), write idx (4); per cell scan 12 B
+#   bin:           per particle read id + pos (16), write vkey (4)
+ALG_BYTES = {
+    "bin": (0, 20), "tiles": (0, 0), "sort": (12, 16), "p2g": (25, 28), "rhs": (25, 0),
+    "pcg_direction": (18, 0), "pcg_update": (34, 0), "refine": (30, 0), "velocity": (33, 0), "g2p": (28, 64),
+}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="dam_sphere_256", choices=["dam_sphere_256", "dam_break_64"])
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-steps", type=int, default=2)
+    return ap.parse_args()
+
+
+def make_scene(name):
+    from vare_gb300 import scenes
+    return scenes.config1() if name == "dam_sphere_256" else scenes.config0()
+
+
+def workload_config(sc, extra=None):
+    cfg = {"workload": f"{sc.name}: {sc.res[0]}x{sc.res[1]}x{sc.res[2]} virtual grid in 8^3 tiles, "
+                       f"{sc.num_particles} particles (8/cell jittered, seeded), dt={sc.dt:.6g}, solid walls",
+           "grid": list(sc.res), "particles": sc.num_particles, "dt": sc.dt, "tile": 8,
+           "solver": "plain: FP32 PCG + block-MIC(0), FP64 dots, FP64 iterative refinement",
+           "tolerance": {"rel": 1e-6, "max_div_dx": 1e-5},
+           "l2": "inputs larger than L2 (particles alone are 590 MB); no flush",
+           "parallelism": "replicas (one independent simulation per GPU)"}
+    if extra:
+        cfg.update(extra)
+    return cfg
+
+
+class ClockSampler:
+    """nvidia-smi SM clock / throttle sampling during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.samples = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+
+        def read():
+            for line in self.proc.stdout:
+                self.samples.append([v.strip() for v in line.split(",")])
+        self.thread = threading.Thread(target=read, daemon=True)
+        self.thread.start()
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for s in self.samples:
+            try:
+                sm.append(float(s[0]))
+                mx.append(float(s[1]))
+            except (ValueError, IndexError):
+                continue
+            for n, v in zip(names, s[3:7]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel_class: str):
+    """Per-launch DRAM bytes of a kernel class from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    if not os.path.exists(path):
+        return None, None
+    with open(path) as f:
+        d = json.load(f)
+    e = d.get(kernel_class)
+    if not e:
+        return None, None
+    return e.get("dram_bytes_per_launch_full_size"), e.get("note")
+
+
+def cpu_baseline(scene, steps: int, threads: int | None = None):
+    """The reference algorithm on the host cores: the oracle restatement in compat mode
+    (4^3 tiles, the reference's CG stop rule), bit-exact with the reference's code."""
+    from oracle import bindings as B
+    if not os.path.exists(B.ORACLE_SO):
+        B.build(ref=False)
+    threads = threads or os.cpu_count()
+    ora = B.Oracle(scene, block=4, compat=True, solver="reference", max_iter=200, threads=threads)
+    ora.step(scene.dt)  # from rest the first solve is trivial; it serves as warm-up
+    times, nps = [], []
+    for _ in range(steps):
+        n = ora.num_particles
+        t0 = time.perf_counter()
+        ora.step(scene.dt)
+        times.append(time.perf_counter() - t0)
+        nps.append(n)
+    return {"value": sum(nps) / sum(times), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{steps} steps of the full workload after 1 warm-up step, oracle restatement of the "
+                      f"reference step (4^3 tiles, reference CG rule: |r|<1e-3 or 201 iterations), "
+                      f"{threads} OpenMP threads; {sum(times):.1f} s",
+            "ms_per_step": 1e3 * sum(times) / len(times)}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+    return world, rank, local
+
+
+def allreduce_max(v: float, world: int) -> float:
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    dev = torch.device("cuda", torch.cuda.current_device()) if dist.get_backend() == "nccl" else torch.device("cpu")
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def allreduce_sum(v: float, world: int) -> float:
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    dev = torch.device("cuda", torch.cuda.current_device()) if dist.get_backend() == "nccl" else torch.device("cpu")
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def barrier(world: int):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    sc = make_scene(args.workload)
+    from oracle import bindings as B
+    if not os.path.exists(B.ORACLE_SO):
+        B.build(ref=False)
+    threads = os.cpu_count()
+    ora = B.Oracle(sc, block=4, compat=True, solver="reference", max_iter=200, threads=threads)
+    warm = max(1, min(args.warmup, 2))
+    steps = max(1, min(args.steps, 5))
+    for _ in range(warm):
+        ora.step(sc.dt)
+    times, nps = [], []
+    for _ in range(steps):
+        n = ora.num_particles
+        t0 = time.perf_counter()
+        ora.step(sc.dt)
+        times.append(time.perf_counter() - t0)
+        nps.append(n)
+    value = sum(nps) / sum(times)
+    ms = sorted(1e3 * t for t in times)
+    sample = (f"{steps} timed steps (of --steps {args.steps}) after {warm} warm-up steps of the full workload; "
+              f"oracle restatement of the reference FLIP step, bit-exact with the reference's host build "
+              f"(4^3 tiles, reference CG rule), {threads} OpenMP threads")
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": sum(ms) / len(ms), "p50_ms": ms[len(ms) // 2], "p99_ms": ms[-1],
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic (seeded jittered-uniform dam break + sphere)", "impl": "reference",
+           "config": workload_config(sc, {"solver": "reference CG (absolute 1e-3, 201 iterations), FP32"}),
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def run_ours(args, world, rank, local):
+    import numpy as np
+    import torch
+
+    from vare_gb300 import build, flip
+
+    build.build()
+    torch.cuda.set_device(local)
+    sc = make_scene(args.workload)
+    sim = flip.FlipSim.from_scene(sc)
+    # warm-up, with every kernel class timed to find the dominant one
+    sim.set_profiling(0xFFFF)
+    for _ in range(args.warmup):
+        sim.step(sc.dt)
+    ms, n = sim.kernel_times()
+    classes = flip.KERNEL_CLASSES
+    dom = int(np.argmax(ms[:len(classes)]))
+    share = {c: float(ms[i]) for i, c in enumerate(classes)}
+    sim.set_profiling(1 << dom)
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    launches0 = sim.stats()["kernel_launches"]
+    barrier(world)
+    torch.cuda.synchronize()
+    step_ms, particle_steps, iters, worst = [], 0, [], {"residual_rel": 0.0, "residual_max_dx": 0.0}
+    all_conv = True
+    for _ in range(args.steps):
+        n0 = sim.num_particles
+        status = sim.step(sc.dt)
+        st = sim.stats()
+        step_ms.append(st["gpu_ms"])
+        particle_steps += n0
+        iters.append(st["solver_iterations"])
+        worst["residual_rel"] = max(worst["residual_rel"], st["residual_rel"])
+        worst["residual_max_dx"] = max(worst["residual_max_dx"], st["residual_max_dx"])
+        all_conv = all_conv and status == 0 and st["converged"] == 1
+    torch.cuda.synchronize()
+    barrier(world)
+    clk = clocks.stop()
+    launches = sim.stats()["kernel_launches"] - launches0
+    kms, kn = sim.kernel_times()
+    my_time = sum(step_ms) / 1e3
+    t_max = allreduce_max(my_time, world)
+    total_ps = allreduce_sum(float(particle_steps), world)
+    value = total_ps / t_max
+
+    # roofline of the dominant kernel class, measured over the timed region
+    fi = sim.frame_info()
+    ncells = fi["ntiles"] * 512
+    cell_b, part_b = ALG_BYTES[classes[dom]]
+    avg_launch_ms = float(kms[dom] / max(1, kn[dom]))
+    launches_per_step = float(kn[dom]) / args.steps
+    bytes_per_launch = cell_b * ncells + part_b * sim.num_particles
+    if classes[dom] in ("pcg_direction", "pcg_update"):
+        bytes_per_launch = cell_b * ncells
+    peak, peak_kind = measured_peaks()
+    achieved = bytes_per_launch / (avg_launch_ms * 1e-3) / 1e9 if avg_launch_ms > 0 else 0.0
+    traffic, tnote = ncu_traffic(classes[dom])
+    roof = {"kernel": classes[dom], "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"
+            if peak_kind == "measured" else "fallback 6.8 TB/s",
+            "alg_bytes_per_launch": bytes_per_launch, "avg_launch_ms": avg_launch_ms,
+            "launches_per_step": launches_per_step, "active_cells": ncells,
+            "share_of_warmup_device_time": {c: round(v / max(1e-9, sum(share.values())), 4)
+                                            for c, v in share.items()}}
+    if tnote:
+        roof["traffic_note"] = tnote
+
+    # end to end through the C ABI with host buffers (pinned), rank-local
+    e2e = None
+    if args.e2e_steps > 0:
+        n = sim.num_particles
+        hp = torch.empty((n, 3), dtype=torch.float32, pin_memory=True)
+        hv = torch.empty((n, 3), dtype=torch.float32, pin_memory=True)
+        got = sim.get_particles_ptr(hp.data_ptr(), hv.data_ptr(), n)
+        e_times, e_ps, h2d, d2h = [], 0, 0, 0
+        for _ in range(args.e2e_steps):
+            t0 = time.perf_counter()
+            sim.set_particles_ptr(hp.data_ptr(), hv.data_ptr(), got)
+            sim.step(sc.dt)
+            m = sim.num_particles
+            if m > hp.shape[0]:
+                raise RuntimeError("particle count grew")
+            got2 = sim.get_particles_ptr(hp.data_ptr(), hv.data_ptr(), hp.shape[0])
+            e_times.append(time.perf_counter() - t0)
+            e_ps += got
+            h2d += got * 24
+            d2h += got2 * 24
+            got = got2
+        et = allreduce_max(sum(e_times), world)
+        eps = allreduce_sum(float(e_ps), world)
+        e2e = {"value": eps / et, "unit": UNIT, "h2d_bytes_per_step": h2d // args.e2e_steps,
+               "d2h_bytes_per_step": d2h // args.e2e_steps, "steps": args.e2e_steps,
+               "ms_per_step": 1e3 * sum(e_times) / len(e_times),
+               "how": "host wall time of bora_flip_set_particles (pinned host -> device) + bora_flip_step + "
+                      "bora_flip_get_particles (device -> pinned host) per step"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        del sim
+        torch.cuda.empty_cache()
+        cpu = cpu_baseline(sc, args.cpu_steps)
+
+    if rank != 0:
+        return
+    ms_sorted = sorted(step_ms)
+    p99 = ms_sorted[min(len(ms_sorted) - 1, int(round(0.99 * (len(ms_sorted) - 1))))]
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": t_max * 1e3 / args.steps, "p50_ms": ms_sorted[len(ms_sorted) // 2],
+           "p99_ms": p99, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic (seeded jittered-uniform dam break + sphere; no public data set exists for this path)",
+           "config": workload_config(sc), "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+           "gpu_launches": int(launches), "clocks": clk,
+           "solver": {"iterations_per_step": iters, "all_converged": all_conv, **worst,
+                      "active_tiles": fi["ntiles"]}}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_ours(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

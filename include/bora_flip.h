@@ -1,0 +1,205 @@
+/* bora_flip.h - C ABI of the GB300-native sparse-grid FLIP substep.
+ *
+ * Drop-in boundary for the one call the reference's Houdini node makes per frame:
+ * Bora::FLIPMethod (base/header/FLIPMethod.h:13-126, base/source/FLIPMethod.cu), used by
+ * SOP_FlipWater (houdini/source/SOP_FlipWater.cpp:122-137, 282-292, 315-323, 358, 362).
+ * The reference exposes a C++ class with unified-memory arrays and no error reporting;
+ * this header exposes the same operations as plain C functions over an opaque handle,
+ * host pointers and sizes, each returning a status code. include/BoraFLIPMethod.hpp
+ * wraps it back into a FLIPMethod-shaped C++ class.
+ *
+ * Coordinates: "world" space is the caller's (the SOP's), "voxel" space is the
+ * reference's internal cell space (dx = 1, Grid::voxelPoint, base/header/Grid.h:446).
+ * Particle arrays are interleaved x,y,z floats, like Bora::Vec3fArray.
+ *
+ * Threading: a handle may be used from one host thread at a time. All work runs on one
+ * CUDA stream owned by the handle, on the device that was current at creation.
+ */
+#ifndef BORA_FLIP_H
+#define BORA_FLIP_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BORA_FLIP_ABI_VERSION 1
+
+/* Status codes. 0 = success; negative = error; positive = completed with a warning. */
+#define BORA_OK 0
+#define BORA_ERR_INVALID_ARG -1
+#define BORA_ERR_OUT_OF_MEMORY -2
+#define BORA_ERR_CUDA -3
+#define BORA_ERR_NO_DEVICE -4
+#define BORA_ERR_INTERNAL -5
+#define BORA_ERR_CAPACITY -6
+#define BORA_WARN_NOT_CONVERGED 1
+
+/* Particle coordinate space of a call. */
+#define BORA_SPACE_WORLD 0
+#define BORA_SPACE_VOXEL 1
+
+/* Pressure-solver forms. */
+#define BORA_SOLVER_PLAIN 0 /* FP32 PCG, block-MIC(0) preconditioner, FP64 dots + refinement */
+#define BORA_SOLVER_MIXED 1 /* FP32 PCG, multigrid V-cycle (FP16 storage), FP64 dots + refinement */
+
+/* Grid description: nx*ny*nz cells over the world box [min, max]
+ * (Grid::initialize(Nx,Ny,Nz,min,max), base/header/Grid.h:124-141). The simulation grid
+ * is this grid padded to a multiple of 4 cells per axis and re-centred
+ * (SparseFrame::initialize, base/source/SparseFrame.cu:28-73). */
+typedef struct bora_grid_desc
+{
+    int nx, ny, nz;
+    float min[3];
+    float max[3];
+} bora_grid_desc;
+
+/* Parameters: the first block mirrors Bora::FLIPMethod::Params field for field
+ * (base/header/FLIPMethod.h:51-67) with the same defaults; the second block adds the
+ * solver controls the reference hard-codes (LinearSystemSolver.cpp:39,46). */
+typedef struct bora_flip_params
+{
+    float ext_force[3];      /* (0, -9.80665, 0) world units / s^2 */
+    int max_substeps;        /* 1 */
+    float dt;                /* 1/24 s */
+    float wall_level;        /* -1e30: world height below which walls are solid */
+    int enable_water_tank;   /* 0 */
+    int enable_curl;         /* 0 (curl noise is not implemented; must be 0) */
+    float damping_band;      /* 0 */
+    float voxel_size;        /* 0.1 */
+    float col_vel_scale;     /* 1 */
+    int pts_per_cell;        /* 8 */
+    float vort_pres_rate;    /* 0.2 (post-processing only) */
+    float adjacency_under;   /* 2 (curl only) */
+    int proj_iteration;      /* 200: cap on inner PCG iterations per refinement pass */
+    int redist_iteration;    /* 80 (post-processing only) */
+    /* additions */
+    int solver;              /* BORA_SOLVER_PLAIN */
+    double tolerance;        /* 1e-6: stop when ||b - A p||_2 / ||b||_2 < tolerance ... */
+    double div_tolerance;    /* 1e-5: ... and max_i |b - A p|_i * dx_world < div_tolerance */
+    double inner_tolerance;  /* 1e-4: relative residual reduction of each FP32 inner solve */
+    int max_refinements;     /* 8: outer FP64 refinement passes */
+    int check_every;         /* 8: inner iterations between convergence checks */
+} bora_flip_params;
+
+typedef struct bora_flip_stats
+{
+    uint64_t steps;               /* steps taken */
+    uint64_t num_particles;       /* live particles after the last step */
+    uint64_t killed_last_step;
+    int32_t active_tiles;         /* 8^3 tiles in the last rebuild */
+    int32_t fluid_cells;
+    int32_t solver_iterations;    /* inner PCG iterations, all refinement passes */
+    int32_t refinements;
+    double residual_rel;          /* ||b - A p||_2 / ||b||_2, FP64 */
+    double residual_max;          /* max_i |b - A p|_i (1/s) */
+    double residual_max_dx;       /* residual_max * dx_world */
+    int32_t converged;
+    int32_t reserved;
+    double stage_ms[8];           /* host wall time of the last step: rebuild, p2g, system, solve,
+                                     velocity, particles, -, total */
+    double gpu_ms;                /* device time of the last step (CUDA events on the handle's stream) */
+    uint64_t kernel_launches;     /* kernels launched by this handle since creation */
+} bora_flip_stats;
+
+/* Kernel classes for opt-in per-kernel device timing (bora_flip_set_profiling). */
+#define BORA_KERNEL_BIN 0
+#define BORA_KERNEL_TILES 1        /* activation, tile scan, tile table, neighbour table */
+#define BORA_KERNEL_SORT 2         /* dual-cell histogram, scan, scatter */
+#define BORA_KERNEL_P2G 3
+#define BORA_KERNEL_RHS 4          /* right-hand side, stencil code, preconditioner set-up */
+#define BORA_KERNEL_PCG_DIRECTION 5
+#define BORA_KERNEL_PCG_UPDATE 6
+#define BORA_KERNEL_REFINE 7       /* solver init, FP64 refinement, pressure write-back */
+#define BORA_KERNEL_VELOCITY 8
+#define BORA_KERNEL_G2P 9
+#define BORA_KERNEL_CLASSES 16
+
+/* Simulation frame description (after padding). */
+typedef struct bora_frame_info
+{
+    int nx, ny, nz;        /* simulation grid in cells */
+    int tx, ty, tz;        /* 8^3 tiles per axis */
+    int tile;              /* 8 */
+    int active_tiles;
+    float translate[3];    /* world position of voxel (0,0,0) */
+    float scale[3];        /* world size of a voxel */
+    float voxel_wall_level;
+    float voxel_gravity[3];
+} bora_frame_info;
+
+typedef struct bora_flip_sim* bora_flip_handle;
+
+/* Default parameters (FLIPMethod::Params defaults, FLIPMethod.h:51-67). */
+int bora_flip_default_params( bora_flip_params* out );
+
+/* FLIPMethod::initialize (FLIPMethod.cu:16-47). */
+int bora_flip_create( const bora_grid_desc* grid, const bora_flip_params* params, bora_flip_handle* out );
+int bora_flip_destroy( bora_flip_handle h );
+int bora_flip_set_params( bora_flip_handle h, const bora_flip_params* params );
+
+/* FLIPMethod::newParticle (FLIPMethod.h:75-99), batched: append n particles from host
+ * memory (pinned memory copies fastest). Velocities may be NULL (zero). */
+int bora_flip_add_particles( bora_flip_handle h, const float* pos, const float* vel, size_t n, int space );
+/* Replace all particles (ids restart at 0). */
+int bora_flip_set_particles( bora_flip_handle h, const float* pos, const float* vel, size_t n, int space );
+int bora_flip_clear_particles( bora_flip_handle h );
+
+/* CollisionSource (base/header/CollisionSource.h): up to 8 analytic boxes, 9 floats each
+ * (lo xyz, hi xyz, velocity xyz) in voxel space; samples are clamped to +-band. */
+int bora_flip_set_colliders( bora_flip_handle h, const float* boxes, int n, float band );
+
+/* FLIPMethod::advanceOneStep (FLIPMethod.cu:208-298) in voxel space. Returns
+ * BORA_WARN_NOT_CONVERGED when the pressure solve stopped on its iteration caps. */
+int bora_flip_step( bora_flip_handle h, float dt );
+/* FLIPMethod::advanceOneFrame (FLIPMethod.cu:177-206) without the post-processing
+ * surface pipeline: one step of params.dt. */
+int bora_flip_frame( bora_flip_handle h );
+
+/* The stages of one step, for callers that interleave their own work and for tests. */
+#define BORA_STAGE_REBUILD 0          /* SparseFrame::buildFromPoints */
+#define BORA_STAGE_P2G 1              /* P2G + count field + cell flags */
+#define BORA_STAGE_BUILD_SYSTEM 2     /* FluidProjection::buildLinearSystem */
+#define BORA_STAGE_SOLVE 3            /* pressure solve */
+#define BORA_STAGE_UPDATE_VELOCITY 4  /* FluidProjection::solve after the solver */
+#define BORA_STAGE_UPDATE_PARTICLES 5 /* FLIPMethod::updateParticles + compaction */
+int bora_flip_run_stage( bora_flip_handle h, int stage, float dt );
+
+int bora_flip_num_particles( bora_flip_handle h, size_t* n );
+/* Copy live particles to host memory (any pointer may be NULL). ids identify particles
+ * across steps (the order of particles changes every step). cap = capacity in particles. */
+int bora_flip_get_particles( bora_flip_handle h, float* pos, float* vel, float* adjacency, int32_t* ids, size_t cap,
+                             size_t* n, int space );
+
+int bora_flip_frame_info( bora_flip_handle h, bora_frame_info* out );
+/* Active tiles as (i,j,k) tile coordinates, in storage (slot) order. */
+int bora_flip_get_tiles( bora_flip_handle h, int32_t* ijk, size_t cap_tiles );
+
+/* Grid fields in tile storage order (active tiles x 512 cells, x fastest in a tile). */
+#define BORA_FIELD_MASS 0      /* float  (getDensityField) */
+#define BORA_FIELD_SURF 1      /* float  particle count per cell */
+#define BORA_FIELD_PRES 2      /* float  */
+#define BORA_FIELD_VELO 3      /* 3 float per cell (pre-projection grid velocity, getVelocityField) */
+#define BORA_FIELD_COMP 4      /* 3 float per cell (projected grid velocity) */
+#define BORA_FIELD_FLAG 5      /* uint8: 0 air, 1 solid, 4 fluid, 255 beyond the grid */
+#define BORA_FIELD_RHS 6       /* float  right-hand side b = -div (fluid cells) */
+#define BORA_FIELD_CODE 7      /* uint16 stencil code (bit 15 fluid, bits 8-11 diagonal, bits 0-5 fluid nbrs) */
+int bora_flip_get_field( bora_flip_handle h, int which, void* out, size_t bytes );
+int bora_flip_set_field( bora_flip_handle h, int which, const void* in, size_t bytes );
+
+int bora_flip_get_stats( bora_flip_handle h, bora_flip_stats* out );
+
+/* Record CUDA events around every launch of the kernel classes in `class_mask` (bit c =
+ * class c) and accumulate their device time; setting a mask resets the totals. */
+int bora_flip_set_profiling( bora_flip_handle h, uint32_t class_mask );
+/* Accumulated device milliseconds and launch counts per kernel class (n <= 16 entries). */
+int bora_flip_get_kernel_times( bora_flip_handle h, double* ms, uint64_t* launches, int n );
+const char* bora_flip_status_string( int status );
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BORA_FLIP_H */

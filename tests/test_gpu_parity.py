@@ -1,0 +1,314 @@
+"""Parity of the CUDA FLIP substep (through the C ABI) with the CPU oracle.
+
+Stage tests feed the device and the oracle identical inputs and require bit-exact
+results wherever the stage's arithmetic is order-independent (tile set, dual-cell
+binning via the count field, cell flags, right-hand side and stencil, velocity update,
+G2P/advection). P2G sums and the pressure solve differ in summation order, so they are
+compared with the relative tolerance max|gpu - ref| / max|ref| <= 1e-5.
+"""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, ROOT
+from vare_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-5  # relative tolerance for order-dependent float results
+
+
+def rel_err(a, b) -> float:
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    den = np.abs(b).max() if b.size else 0.0
+    return float(np.abs(a - b).max() / den) if den > 0 else float(np.abs(a - b).max())
+
+
+def real_cells(tiles, nx, ny, nz) -> np.ndarray:
+    """Storage-order mask of the cells of active tiles that lie inside the grid."""
+    l = np.arange(512)
+    li, lj, lk = l & 7, (l >> 3) & 7, l >> 6
+    i = tiles[:, 0:1] * 8 + li[None, :]
+    j = tiles[:, 1:2] * 8 + lj[None, :]
+    k = tiles[:, 2:3] * 8 + lk[None, :]
+    return ((i < nx) & (j < ny) & (k < nz)).reshape(-1)
+
+
+def tight(**kw):
+    d = dict(tolerance=1e-10, div_tolerance=1e-12, max_refinements=30, inner_tolerance=1e-4)
+    d.update(kw)
+    return d
+
+
+def by_id(pos, vel, adj, ids):
+    o = np.argsort(ids)
+    return pos[o], vel[o], adj[o], ids[o]
+
+
+def colliders_for(n):
+    return [((n * 0.45, -2.0, n * 0.3), (n * 0.6, n * 0.3, n * 0.7), (0.0, 0.0, 0.0)),
+            ((n * 0.8, n * 0.1, -1.0), (n * 0.95, n * 0.2, n * 0.4), (-3.0, 1.0, 0.0))]
+
+
+@pytest.fixture(params=["dam_sphere_24", "colliders_20", "padded_22", "slab_24x16x40"])
+def scene(request):
+    name = request.param
+    if name == "dam_sphere_24":
+        return scenes.small(24)
+    if name == "colliders_20":
+        sc = scenes.small(20, dt=1.0 / 60.0)
+        sc.colliders = colliders_for(20)
+        return sc
+    if name == "padded_22":
+        return scenes.small(22)
+    sc = scenes.small(16)
+    sc.res = (24, 16, 40)
+    sc.bmax = (1.0, 16 / 24, 40 / 24)
+    sc.pos = sc.pos[(sc.pos[:, 0] < 24) & (sc.pos[:, 1] < 16)]
+    sc.vel = np.zeros_like(sc.pos)
+    return sc
+
+
+def _pair(gpu, oracle_lib, sc, **kw):
+    sim = gpu.FlipSim.from_scene(sc, **tight(**kw))
+    ora = oracle_lib.Oracle(sc, block=8, solver="fp64", tol=1e-13, threads=1)
+    return sim, ora
+
+
+def test_frame_matches_oracle(gpu, oracle_lib, scene):
+    sim, ora = _pair(gpu, oracle_lib, scene)
+    fi, fo = sim.frame_info(), ora.frame_info()
+    assert (fi["nx"], fi["ny"], fi["nz"]) == (fo["nx"], fo["ny"], fo["nz"])
+    xo = ora.grid_xform()
+    np.testing.assert_array_equal(fi["translate"], xo["translate"])
+    np.testing.assert_array_equal(fi["scale"], xo["scale"])
+    assert fi["voxel_wall"] == xo["voxel_wall"]
+    np.testing.assert_array_equal(fi["voxel_gravity"], xo["voxel_gravity"])
+
+
+def test_stages_bit_exact(gpu, oracle_lib, scene):
+    B = oracle_lib
+    sc = scene
+    sim, ora = _pair(gpu, oracle_lib, sc)
+    # rebuild + P2G + flags
+    sim.run_stage(gpu.STAGE_REBUILD)
+    sim.run_stage(gpu.STAGE_P2G)
+    ora.rebuild(); ora.p2g(); ora.mark()
+    tiles = sim.tiles()
+    np.testing.assert_array_equal(tiles, ora.tiles())
+    fi = sim.frame_info()
+    real = real_cells(tiles, fi["nx"], fi["ny"], fi["nz"])
+    # dual-cell binning: particle count per cell is exact
+    np.testing.assert_array_equal(sim.field(gpu.FIELD_SURF)[real], ora.field(B.FIELD_SURF)[real])
+    np.testing.assert_array_equal(sim.field(gpu.FIELD_FLAG)[real], ora.field(B.FIELD_MARK)[real].astype(np.uint8))
+    assert rel_err(sim.field(gpu.FIELD_MASS)[real], ora.field(B.FIELD_MASS)[real]) <= 1e-6
+    assert rel_err(sim.field(gpu.FIELD_VELO)[real], ora.field(B.FIELD_VELO)[real]) <= 1e-5
+    # right-hand side and stencil from identical grid velocities
+    velo = ora.field(B.FIELD_VELO)
+    sim.set_field(gpu.FIELD_VELO, velo)
+    sim.run_stage(gpu.STAGE_BUILD_SYSTEM)
+    ora.build_system()
+    sysm = ora.system()
+    cells = sysm["cells"]
+    rhs = sim.field(gpu.FIELD_RHS)
+    np.testing.assert_array_equal(rhs[cells], sysm["b"])
+    code = sim.field(gpu.FIELD_CODE).astype(np.int64)
+    assert np.all(code[cells] & 0x8000)
+    np.testing.assert_array_equal((code[cells] >> 8) & 15, sysm["vals"][:, 0].astype(np.int64))
+    nbr_mask = np.zeros(len(cells), np.int64)
+    for q in range(6):
+        nbr_mask |= (sysm["cols"][:, 1 + q] >= 0).astype(np.int64) << q
+    np.testing.assert_array_equal(code[cells] & 63, nbr_mask)
+    others = np.ones(len(code), bool)
+    others[cells] = False
+    assert not np.any(code[others & real] & 0x8000)
+    # velocity update from an identical pressure solution
+    ora.solve()
+    x = ora.system()["x"]
+    pres = np.zeros(len(rhs), np.float32)
+    pres[cells] = x
+    sim.set_field(gpu.FIELD_PRES, pres)
+    sim.run_stage(gpu.STAGE_UPDATE_VELOCITY)
+    ora.update_velocity()
+    np.testing.assert_array_equal(sim.field(gpu.FIELD_PRES)[real], ora.field(B.FIELD_PRES)[real])
+    np.testing.assert_array_equal(sim.field(gpu.FIELD_COMP)[real], ora.field(B.FIELD_COMP)[real])
+    # G2P + advection + kill from identical fields
+    sim.run_stage(gpu.STAGE_UPDATE_PARTICLES, sc.dt)
+    ora.update_particles(sc.dt)
+    ora.compact()
+    g = by_id(*sim.particles())
+    o = by_id(*ora.particles())
+    np.testing.assert_array_equal(g[3], o[3])
+    for a, b, name in zip(g[:3], o[:3], ("pos", "vel", "adj")):
+        np.testing.assert_array_equal(a, b, err_msg=name)
+
+
+def test_solve_matches_fp64_oracle(gpu, oracle_lib, scene):
+    B = oracle_lib
+    sc = scene
+    sim, ora = _pair(gpu, oracle_lib, sc)
+    for st in (gpu.STAGE_REBUILD, gpu.STAGE_P2G, gpu.STAGE_BUILD_SYSTEM):
+        sim.run_stage(st)
+    ora.rebuild(); ora.p2g(); ora.mark()
+    sim.set_field(gpu.FIELD_VELO, ora.field(B.FIELD_VELO))
+    sim.run_stage(gpu.STAGE_BUILD_SYSTEM)
+    ora.build_system()
+    status = sim.run_stage(gpu.STAGE_SOLVE)
+    st = sim.stats()
+    assert status == 0 and st["converged"] == 1, st
+    assert st["residual_rel"] <= 1e-10
+    ora.solve()
+    sysm = ora.system()
+    p_gpu = sim.field(gpu.FIELD_PRES)[sysm["cells"]]
+    assert rel_err(p_gpu, sysm["x"]) <= TOL
+    # the device's own residual report agrees with the oracle's FP64 residual of its answer
+    ora.set_solution(p_gpu)
+    rmax = ora.residual_max()
+    assert rmax <= max(10 * st["residual_max"], 1e-6 * np.abs(sysm["b"]).max())
+
+
+def test_full_step_matches_oracle(gpu, oracle_lib, scene):
+    sc = scene
+    sim, ora = _pair(gpu, oracle_lib, sc)
+    for _ in range(2):
+        assert sim.step(sc.dt) == 0
+        ora.step(sc.dt)
+    g = by_id(*sim.particles())
+    o = by_id(*ora.particles())
+    np.testing.assert_array_equal(g[3], o[3])
+    assert rel_err(g[0], o[0]) <= TOL
+    assert rel_err(g[1], o[1]) <= TOL
+    assert np.abs(g[2] - o[2]).max() <= 1e-3  # adjacency = min of integer counts
+
+
+def test_step_matches_reference_golden(gpu):
+    """One device step against the reference's own converged step (tests/golden)."""
+    g = np.load(os.path.join(GOLDEN, "ref_cg64_small24.npz"))
+    sc = scenes.small(int(g["n"]))
+    sim = gpu.FlipSim.from_scene(sc, **tight())
+    assert sim.step(sc.dt) == 0
+    pos, vel, adj, ids = by_id(*sim.particles())
+    ref_ids = g["ids0"]
+    o = np.argsort(ref_ids)
+    np.testing.assert_array_equal(ids, ref_ids[o])
+    assert rel_err(pos, g["pos0"][o]) <= TOL
+    assert rel_err(vel, g["vel0"][o]) <= TOL
+    np.testing.assert_array_equal(adj, g["adj0"][o])
+
+
+def test_deterministic(gpu):
+    sc = scenes.small(24)
+    a = gpu.FlipSim.from_scene(sc)
+    b = gpu.FlipSim.from_scene(sc)
+    for _ in range(3):
+        a.step(sc.dt)
+        b.step(sc.dt)
+    for x, y in zip(by_id(*a.particles()), by_id(*b.particles())):
+        np.testing.assert_array_equal(x, y)
+
+
+def test_multistep_statistics(gpu, oracle_lib):
+    """Chaotic dynamics: after 20 steps compare conserved counts and bulk statistics."""
+    sc = scenes.small(24)
+    sim = gpu.FlipSim.from_scene(sc, tolerance=1e-8, div_tolerance=1e-9)
+    ora = oracle_lib.Oracle(sc, block=8, solver="fp64", tol=1e-10, threads=os.cpu_count())
+    for _ in range(20):
+        sim.step(sc.dt)
+        ora.step(sc.dt)
+    gp, gv, _, _ = sim.particles()
+    op, ov, _, _ = ora.particles()
+    assert len(gp) == len(op)
+    ke_g = 0.5 * np.sum(gv.astype(np.float64) ** 2)
+    ke_o = 0.5 * np.sum(ov.astype(np.float64) ** 2)
+    assert abs(ke_g - ke_o) <= 1e-3 * ke_o
+    assert np.abs(gp.mean(0) - op.mean(0)).max() <= 1e-3
+
+
+def test_edge_cases(gpu, oracle_lib):
+    sc = scenes.small(16)
+    # empty
+    sim = gpu.FlipSim(sc.res, sc.bmin, sc.bmax, gpu.scene_params(sc))
+    assert sim.step(sc.dt) == 0 and sim.num_particles == 0
+    # a single particle, particles on the upper boundary and outside the grid
+    pts = np.array([[3.3, 4.7, 5.1], [16.0, 16.0, 16.0], [15.99, 0.0, 8.0], [-0.5, 3.0, 3.0], [20.0, 3.0, 3.0],
+                    [8.0, -3.0, 8.0]], np.float32)
+    vel = np.array([[1, 2, 3], [0, 0, 0], [5, -5, 0], [0, 0, 0], [0, 0, 0], [0, -1, 0]], np.float32)
+    sc2 = scenes.Scene(name="edge", res=sc.res, bmin=sc.bmin, bmax=sc.bmax, dt=sc.dt, pos=pts, vel=vel)
+    sim.set_particles(pts, vel, space=gpu.SPACE_VOXEL)
+    ora = oracle_lib.Oracle(sc2, block=8, solver="fp64", tol=1e-13, threads=1)
+    for _ in range(2):
+        sim.step(sc.dt)
+        ora.step(sc.dt)
+    g = by_id(*sim.particles())
+    o = by_id(*ora.particles())
+    np.testing.assert_array_equal(g[3], o[3])
+    assert rel_err(g[0], o[0]) <= TOL and rel_err(g[1], o[1]) <= TOL
+
+
+def test_world_space_round_trip(gpu):
+    sc = scenes.small(16)
+    sim = gpu.FlipSim(sc.res, sc.bmin, sc.bmax, gpu.scene_params(sc))
+    fi = sim.frame_info()
+    world = sc.pos * fi["scale"] + fi["translate"]
+    sim.set_particles(world, sc.vel * fi["scale"], space=gpu.SPACE_WORLD)
+    pos, _, _, ids = sim.particles(space=gpu.SPACE_VOXEL)
+    np.testing.assert_allclose(pos[np.argsort(ids)], sc.pos, atol=2e-5 * 16)
+    posw, _, _, ids = sim.particles(space=gpu.SPACE_WORLD)
+    np.testing.assert_allclose(posw[np.argsort(ids)], world, atol=1e-6)
+
+
+def test_full_size_invariants(gpu):
+    """The 256^3 dam-break + sphere scene (24,564,400 particles): size-independent
+    properties after two steps - every particle kept once (solid walls), the count field
+    sums to the stencil contributions, the tile set follows the activation rule, and the
+    projection met max|b - Ap| * dx < 1e-5 with ||r||/||b|| < 1e-6."""
+    sc = scenes.config1()
+    assert sc.num_particles == 24564400
+    sim = gpu.FlipSim.from_scene(sc)
+    for _ in range(2):
+        status = sim.step(sc.dt)
+        st = sim.stats()
+        assert status == 0 and st["converged"] == 1, st
+        assert st["residual_rel"] < 1e-6 and st["residual_max_dx"] < 1e-5
+    pos, vel, adj, ids = sim.particles()
+    assert len(ids) == sc.num_particles
+    np.testing.assert_array_equal(np.sort(ids), np.arange(sc.num_particles, dtype=np.int32))
+    assert np.isfinite(pos).all() and np.isfinite(vel).all()
+    assert pos.min() >= 0.0 and pos.max() <= 256.0
+    # rebuild for the current positions and check the tile rule and the count field
+    sim.run_stage(gpu.STAGE_REBUILD)
+    sim.run_stage(gpu.STAGE_P2G)
+    fi = sim.frame_info()
+    f = np.array([fi["tx"], fi["ty"], fi["tz"]])
+    t = np.clip(np.maximum(np.trunc(pos).astype(np.int64) // 8, 0), 0, f - 1)
+    occ = np.zeros(f[::-1], bool)
+    occ[t[:, 2], t[:, 1], t[:, 0]] = True
+    pad = np.pad(occ, 1)
+    act = np.zeros_like(occ)
+    for dz in range(3):
+        for dy in range(3):
+            for dx in range(3):
+                act |= pad[dz:dz + f[2], dy:dy + f[1], dx:dx + f[0]]
+    kk, jj, ii = np.nonzero(act)
+    expect = np.stack([ii, jj, kk], 1)
+    np.testing.assert_array_equal(sim.tiles(), expect[np.lexsort((ii, jj, kk))])
+    # count field: each particle touches min(2, clipped) cells per axis
+    d = np.maximum(np.trunc(pos - 0.5).astype(np.int64), 0)
+    touched = np.prod(np.where(d + 1 <= 255, 2, 1), axis=1)
+    assert int(sim.field(gpu.FIELD_SURF).astype(np.int64).sum()) == int(touched.sum())
+
+
+def test_cpp_harness_runs(gpu):
+    """Houdini-free FLIPMethod harness linked against the C ABI library."""
+    from vare_gb300 import build
+    src = os.path.join(ROOT, "tests", "cpp", "flipmethod_harness.cpp")
+    exe = os.path.join(ROOT, "tests", "cpp", "_build", "harness")
+    os.makedirs(os.path.dirname(exe), exist_ok=True)
+    libdir = os.path.dirname(build.LIB)
+    subprocess.run(["g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"), src, "-o", exe,
+                    "-L", libdir, "-lbora_flip", f"-Wl,-rpath,{libdir}"], check=True)
+    r = subprocess.run([exe, "3"], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr

@@ -1,0 +1,112 @@
+// Internal host-side declarations of the GB300 FLIP substep library (not installed).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "flip_common.cuh"
+
+// ---- scan ---------------------------------------------------------------------------
+size_t bora_scan_scratch_elems( size_t n );
+void bora_scan_u32( const uint32_t* in, uint32_t* out, size_t n, uint32_t* scratch, uint32_t* total, cudaStream_t st );
+
+// ---- particle arrays (structure of arrays) -------------------------------------------
+struct BoraParticlesDev
+{
+    float* px;
+    float* py;
+    float* pz;
+    float* vx;
+    float* vy;
+    float* vz;
+    int32_t* id;  // < 0: killed in the last step
+};
+
+// ---- cell fields over active slots x 512 ----------------------------------------------
+struct BoraCellsDev
+{
+    float* mass;
+    float* surf;  // particle count touching the cell (PointsToCountField)
+    float* pres;
+    float* vx;    // grid velocity after P2G and collider velocity ("velo")
+    float* vy;
+    float* vz;
+    float* cx;    // projected grid velocity ("comp")
+    float* cy;
+    float* cz;
+    uint8_t* flag;
+    uint16_t* code;
+    float* b;
+};
+
+// Tile tables.
+struct BoraTilesDev
+{
+    const int32_t* slot_of;   // [virtual tiles] -> slot or -1
+    const int32_t* tile_of;   // [slots] -> virtual tile linear index
+    const int32_t* nbr;       // [slots * 27] -> neighbour slot or -1
+};
+
+// Scalars that the solver kernels exchange on the device (ring of FP64 reductions).
+#define BORA_RING 64
+struct BoraReduceDev
+{
+    double* ring;        // [BORA_RING * 4]: slot values
+    double* partials;    // [max blocks * 2]
+    uint32_t* done;      // [BORA_RING] block-arrival counters
+};
+
+// ---- launchers -----------------------------------------------------------------------
+void bora_launch_bin( const BoraGridDev& g, BoraParticlesDev p, size_t n, uint32_t* vkey, uint8_t* tile_flag, cudaStream_t st );
+void bora_launch_activate( const BoraGridDev& g, const uint8_t* tile_flag, uint32_t* act, cudaStream_t st );
+void bora_launch_tile_assign( const BoraGridDev& g, const uint32_t* act, const uint32_t* excl, int32_t* slot_of,
+                              int32_t* tile_of, cudaStream_t st );
+void bora_launch_tile_nbrs( const BoraGridDev& g, int ntiles, const int32_t* slot_of, const int32_t* tile_of,
+                            int32_t* nbr, cudaStream_t st );
+void bora_launch_hist( size_t n, const uint32_t* vkey, const int32_t* slot_of, uint32_t outside_key, uint32_t* key,
+                       uint32_t* count, uint32_t* err, cudaStream_t st );
+void bora_launch_scatter( size_t n, const uint32_t* key, const uint32_t* start, uint32_t* count, uint32_t* idx,
+                          cudaStream_t st );
+void bora_launch_p2g( const BoraGridDev& g, int ntiles, BoraTilesDev t, BoraParticlesDev p, const uint32_t* idx,
+                      const uint32_t* start, BoraCellsDev c, cudaStream_t st );
+void bora_launch_rhs( const BoraGridDev& g, int ntiles, BoraTilesDev t, BoraCellsDev c, cudaStream_t st );
+void bora_launch_vel_update( const BoraGridDev& g, int ntiles, BoraTilesDev t, BoraCellsDev c, cudaStream_t st );
+void bora_launch_g2p( const BoraGridDev& g, size_t n, const int32_t* slot_of, BoraCellsDev c, BoraParticlesDev src,
+                      const uint32_t* idx, BoraParticlesDev dst, float* adj, float dt, uint32_t* nkilled,
+                      cudaStream_t st );
+void bora_launch_to_soa( size_t n, const float* pos, const float* vel, int space, const float* translate,
+                         const float* scale, BoraParticlesDev p, size_t offset, int32_t first_id, cudaStream_t st );
+
+// ---- pressure solve -------------------------------------------------------------------
+struct BoraSolverDev
+{
+    double* x;      // FP64 pressure iterate (refinement)
+    float* e;       // inner correction
+    float* r;       // residual
+    float* d[2];    // search directions (ping-pong)
+    float* q;       // A d
+    float* z;       // preconditioned residual
+    float* minv;    // block-MIC(0) inverse pivots
+};
+
+void bora_launch_mic_factor( const BoraGridDev& g, int ntiles, const uint16_t* code, float* minv, cudaStream_t st );
+// r = b, x = 0, e = 0, d = 0, q = 0; partial sums of ||b||^2 and max|b| -> ring slots
+void bora_launch_solve_init( int ntiles, const float* b, const uint16_t* code, BoraSolverDev s, BoraReduceDev red,
+                             int slot_norm2, int slot_max, cudaStream_t st );
+// e += alpha d; r -= alpha q; z = M^-1 r; rz, rr -> ring slots (alpha = rz_in / dq_in, or 0 when slot_rz_in < 0)
+void bora_launch_pcg_update( int ntiles, const uint16_t* code, BoraSolverDev s, int dsel, BoraReduceDev red,
+                             int slot_rz_in, int slot_dq_in, int slot_rz_out, int slot_rr_out, cudaStream_t st );
+// d' = z + beta d; q = A d'; dq -> ring slot (beta = rz_new / rz_old, or 0 when slot_rz_old < 0)
+void bora_launch_pcg_direction( const BoraGridDev& g, int ntiles, BoraTilesDev t, const uint16_t* code, BoraSolverDev s,
+                                int dsel_in, BoraReduceDev red, int slot_rz_new, int slot_rz_old, int slot_dq_out,
+                                cudaStream_t st );
+// x += e (FP64); e = 0; d = 0; q = 0
+void bora_launch_refine_accumulate( int ntiles, const uint16_t* code, BoraSolverDev s, cudaStream_t st );
+// r = b - A x in FP64 (stored FP32); ||r||^2 and max|r| -> ring slots
+void bora_launch_refine_residual( const BoraGridDev& g, int ntiles, BoraTilesDev t, const float* b, const uint16_t* code,
+                                  BoraSolverDev s, BoraReduceDev red, int slot_norm2, int slot_max, cudaStream_t st );
+// pres = (float) x on fluid cells, 0 elsewhere
+void bora_launch_write_pressure( int ntiles, const uint16_t* code, const double* x, float* pres, cudaStream_t st );
+
+size_t bora_reduce_max_blocks();

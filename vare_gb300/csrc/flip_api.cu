@@ -1,0 +1,943 @@
+// C ABI of the GB300 FLIP substep: the simulation handle, buffer management and the
+// per-step orchestration of FLIPMethod::advanceOneStep (base/source/FLIPMethod.cu:208-298).
+//
+// One handle = one simulation on one device and one CUDA stream. Device buffers are
+// grown geometrically and reused across steps; nothing is allocated inside a step
+// unless the particle count or the active-tile count outgrows its capacity.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "bora_internal.h"
+#include "../../include/bora_flip.h"
+
+namespace {
+
+struct DevBuf
+{
+    void* p = nullptr;
+    size_t bytes = 0;
+};
+
+cudaError_t grow( DevBuf& b, size_t bytes, bool keep, cudaStream_t st )
+{
+    if( bytes <= b.bytes ) return cudaSuccess;
+    size_t nb = std::max( bytes, b.bytes + b.bytes / 2 );
+    nb = ( nb + 255 ) & ~(size_t)255;
+    void* np = nullptr;
+    cudaError_t e = cudaMalloc( &np, nb );
+    if( e != cudaSuccess ) return e;
+    if( keep && b.p && b.bytes ) e = cudaMemcpyAsync( np, b.p, b.bytes, cudaMemcpyDeviceToDevice, st );
+    if( e == cudaSuccess && b.p ) { cudaStreamSynchronize( st ); cudaFree( b.p ); }
+    b.p = np;
+    b.bytes = nb;
+    return e;
+}
+
+void release( DevBuf& b )
+{
+    if( b.p ) cudaFree( b.p );
+    b.p = nullptr;
+    b.bytes = 0;
+}
+
+template <class T> T* P( DevBuf& b ) { return reinterpret_cast<T*>( b.p ); }
+
+// Compact live particles (id >= 0) into interleaved host-layout staging arrays.
+__global__ void k_live_flags( size_t n, const int32_t* __restrict__ id, uint32_t* __restrict__ flag )
+{
+    for( size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x )
+        flag[i] = id[i] >= 0 ? 1u : 0u;
+}
+
+__global__ void k_gather_live( size_t n, BoraParticlesDev p, const float* __restrict__ adj, const uint32_t* __restrict__ excl,
+                               int space, float3 tr, float3 sc, float* __restrict__ pos, float* __restrict__ vel,
+                               float* __restrict__ adj_out, int32_t* __restrict__ ids )
+{
+    for( size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x )
+    {
+        if( p.id[i] < 0 ) continue;
+        const size_t o = excl[i];
+        float x = p.px[i], y = p.py[i], z = p.pz[i], u = p.vx[i], v = p.vy[i], w = p.vz[i];
+        if( space == BORA_SPACE_WORLD )
+        {
+            // Grid::worldPoint / worldVector (base/header/Grid.h:432-444)
+            x = x * sc.x + tr.x; y = y * sc.y + tr.y; z = z * sc.z + tr.z;
+            u = u * sc.x; v = v * sc.y; w = w * sc.z;
+        }
+        if( pos ) { pos[3 * o] = x; pos[3 * o + 1] = y; pos[3 * o + 2] = z; }
+        if( vel ) { vel[3 * o] = u; vel[3 * o + 1] = v; vel[3 * o + 2] = w; }
+        if( adj_out ) adj_out[o] = adj[i];
+        if( ids ) ids[o] = p.id[i];
+    }
+}
+
+int grid_blocks( size_t n )
+{
+    const size_t b = ( n + 255 ) / 256;
+    return (int)std::max<size_t>( 1, std::min<size_t>( b, 152 * 16 ) );
+}
+
+}  // namespace
+
+struct bora_flip_sim
+{
+    int device = 0;
+    cudaStream_t st = nullptr;
+    bora_grid_desc gdesc{};
+    bora_flip_params prm{};
+    BoraGridDev g{};
+    float translate[3] = { 0, 0, 0 }, scale[3] = { 1, 1, 1 };
+    size_t ntv = 0;
+
+    // tiles
+    DevBuf tile_flag, tile_act, tile_excl, slot_of, tile_of, nbr;
+    int ntiles = 0;
+    size_t cap_tiles = 0;
+
+    // cells
+    DevBuf mass, surf, pres, vx, vy, vz, cx, cy, cz, flag, code, rhs;
+    DevBuf sx, se, sr, sd0, sd1, sq, sz, sminv;
+    DevBuf cell_count, cell_start;
+
+    // reductions
+    DevBuf ring, partials, done;
+    int next_slot = 0;
+
+    // particles
+    DevBuf pbuf[2][7];  // px py pz vx vy vz id
+    DevBuf adj, vkey, key, idx;
+    size_t cap_p = 0;
+    size_t np = 0;      // particles in the current buffer (killed ones included until the next sort)
+    size_t nlive = 0;
+    size_t nsorted = 0; // live particles indexed by idx after the last rebuild
+    int cur = 0;
+    int32_t next_id = 0;
+    bool sorted = false;   // idx/cell_start describe the current buffer
+
+    // scratch and staging
+    DevBuf scan_scratch, counters, stage_in, stage_out, live_flag;
+    uint32_t* h_cnt = nullptr;  // pinned
+    double* h_ring = nullptr;   // pinned
+
+    bora_flip_stats stats{};
+    int last_status = BORA_OK;
+
+    // device timing: per-step events (always) and opt-in per-kernel-class events
+    cudaEvent_t ev_step[2] = { nullptr, nullptr };
+    uint32_t prof_mask = 0;
+    double kt_ms[BORA_KERNEL_CLASSES] = {};
+    uint64_t kt_n[BORA_KERNEL_CLASSES] = {};
+    struct Pending { int cls; cudaEvent_t a, b; };
+    std::vector<cudaEvent_t> evpool;
+    std::vector<Pending> pending;
+
+    cudaEvent_t take_event()
+    {
+        if( !evpool.empty() ) { cudaEvent_t e = evpool.back(); evpool.pop_back(); return e; }
+        cudaEvent_t e = nullptr;
+        cudaEventCreate( &e );
+        return e;
+    }
+    // resolve recorded kernel timings; the stream must have been synchronized
+    void prof_resolve()
+    {
+        for( const Pending& p : pending )
+        {
+            float ms = 0.f;
+            if( cudaEventElapsedTime( &ms, p.a, p.b ) == cudaSuccess ) { kt_ms[p.cls] += ms; kt_n[p.cls] += 1; }
+            evpool.push_back( p.a );
+            evpool.push_back( p.b );
+        }
+        pending.clear();
+    }
+
+    BoraParticlesDev parts( int b )
+    {
+        return BoraParticlesDev{ P<float>( pbuf[b][0] ), P<float>( pbuf[b][1] ), P<float>( pbuf[b][2] ),
+                                 P<float>( pbuf[b][3] ), P<float>( pbuf[b][4] ), P<float>( pbuf[b][5] ),
+                                 P<int32_t>( pbuf[b][6] ) };
+    }
+    BoraCellsDev cells()
+    {
+        return BoraCellsDev{ P<float>( mass ), P<float>( surf ), P<float>( pres ), P<float>( vx ), P<float>( vy ),
+                             P<float>( vz ), P<float>( cx ), P<float>( cy ), P<float>( cz ), P<uint8_t>( flag ),
+                             P<uint16_t>( code ), P<float>( rhs ) };
+    }
+    BoraTilesDev tiles() { return BoraTilesDev{ P<int32_t>( slot_of ), P<int32_t>( tile_of ), P<int32_t>( nbr ) }; }
+    BoraSolverDev solver()
+    {
+        BoraSolverDev s;
+        s.x = P<double>( sx ); s.e = P<float>( se ); s.r = P<float>( sr );
+        s.d[0] = P<float>( sd0 ); s.d[1] = P<float>( sd1 ); s.q = P<float>( sq ); s.z = P<float>( sz );
+        s.minv = P<float>( sminv );
+        return s;
+    }
+    BoraReduceDev reducer() { return BoraReduceDev{ P<double>( ring ), P<double>( partials ), P<uint32_t>( done ) }; }
+    int slot()
+    {
+        const int s = next_slot;
+        next_slot = ( next_slot + 1 ) % BORA_RING;
+        return s;
+    }
+};
+
+namespace {
+
+int cuda_status( cudaError_t e )
+{
+    if( e == cudaSuccess ) return BORA_OK;
+    if( e == cudaErrorMemoryAllocation ) return BORA_ERR_OUT_OF_MEMORY;
+    return BORA_ERR_CUDA;
+}
+
+#define BORA_TRY( expr )                                        \
+    do {                                                        \
+        const cudaError_t _e = ( expr );                        \
+        if( _e != cudaSuccess ) return cuda_status( _e );       \
+    } while( 0 )
+
+#define BORA_TRYS( expr )                                       \
+    do {                                                        \
+        const int _s = ( expr );                                \
+        if( _s < 0 ) return _s;                                 \
+    } while( 0 )
+
+// Counts the kernels of one launcher call and, when its class is being profiled,
+// brackets them with CUDA events on the handle's stream.
+struct KTimer
+{
+    bora_flip_sim* s;
+    int cls;
+    cudaEvent_t a = nullptr;
+    KTimer( bora_flip_sim* sim, int c, int nkernels ) : s( sim ), cls( c )
+    {
+        s->stats.kernel_launches += (uint64_t)nkernels;
+        if( ( s->prof_mask >> cls ) & 1u )
+        {
+            a = s->take_event();
+            cudaEventRecord( a, s->st );
+        }
+    }
+    ~KTimer()
+    {
+        if( a )
+        {
+            cudaEvent_t b = s->take_event();
+            cudaEventRecord( b, s->st );
+            s->pending.push_back( bora_flip_sim::Pending{ cls, a, b } );
+        }
+    }
+};
+
+int check_launch( bora_flip_sim* h )
+{
+    const cudaError_t e = cudaGetLastError();
+    (void)h;
+    return cuda_status( e );
+}
+
+// Frame set-up: SparseFrame::initialize (SparseFrame.cu:28-73) and FLIPMethod::initialize
+// (FLIPMethod.cu:41-46) - pad each axis to a multiple of 4 cells, re-centre the box with a
+// uniform spacing h = min(dx,dy,dz), convert gravity and the wall level to voxel units.
+void setup_frame( bora_flip_sim* s )
+{
+    const bora_grid_desc& d = s->gdesc;
+    const int gn[3] = { d.nx, d.ny, d.nz };
+    float gT[3], gS[3], minP[3], maxP[3], cen[3], dd[3];
+    for( int a = 0; a < 3; ++a )
+    {
+        gT[a] = d.min[a];
+        gS[a] = ( d.max[a] - d.min[a] ) / (float)gn[a];
+    }
+    int fn[3];
+    for( int a = 0; a < 3; ++a ) fn[a] = ( gn[a] / 4 + ( ( gn[a] % 4 ) ? 1 : 0 ) ) * 4;
+    for( int a = 0; a < 3; ++a )
+    {
+        const float e = gT[a] + (float)gn[a] * gS[a];
+        minP[a] = std::min( gT[a], e );
+        maxP[a] = std::max( gT[a], e );
+        cen[a] = ( minP[a] + maxP[a] ) * 0.5f;
+        dd[a] = ( maxP[a] - minP[a] ) / (float)gn[a];
+    }
+    const float h = std::min( std::min( dd[0], dd[1] ), dd[2] );
+    for( int a = 0; a < 3; ++a )
+    {
+        const float L = (float)fn[a] * h;
+        const float nmin = cen[a] - L * 0.5f;
+        const float nmax = nmin + L;
+        s->translate[a] = nmin;
+        s->scale[a] = ( nmax - nmin ) / (float)fn[a];
+    }
+    BoraGridDev& g = s->g;
+    g.nx = fn[0]; g.ny = fn[1]; g.nz = fn[2];
+    g.tx = ( g.nx + 7 ) / 8; g.ty = ( g.ny + 7 ) / 8; g.tz = ( g.nz + 7 ) / 8;
+    s->ntv = (size_t)g.tx * g.ty * g.tz;
+}
+
+void apply_params( bora_flip_sim* s )
+{
+    BoraGridDev& g = s->g;
+    const bora_flip_params& p = s->prm;
+    for( int a = 0; a < 3; ++a ) g.gravity[a] = p.ext_force[a] / s->scale[a];
+    g.voxel_wall = ( p.wall_level - s->translate[1] ) / s->scale[1];
+    g.col_vel_scale = p.col_vel_scale;
+    g.maxsubsteps = p.max_substeps;
+    g.enable_tank = p.enable_water_tank;
+    g.damping_band = p.damping_band / p.voxel_size;
+}
+
+int ensure_particles( bora_flip_sim* s, size_t n )
+{
+    if( n <= s->cap_p ) return BORA_OK;
+    const size_t cap = std::max( n, s->cap_p + s->cap_p / 2 );
+    for( int b = 0; b < 2; ++b )
+        for( int a = 0; a < 7; ++a ) BORA_TRY( grow( s->pbuf[b][a], cap * 4, b == s->cur, s->st ) );
+    BORA_TRY( grow( s->adj, cap * 4, true, s->st ) );
+    BORA_TRY( grow( s->vkey, cap * 4, false, s->st ) );
+    BORA_TRY( grow( s->key, cap * 4, false, s->st ) );
+    BORA_TRY( grow( s->idx, cap * 4, false, s->st ) );
+    BORA_TRY( grow( s->live_flag, ( cap + 1 ) * 4, false, s->st ) );
+    s->cap_p = cap;
+    return BORA_OK;
+}
+
+int ensure_scan_scratch( bora_flip_sim* s, size_t n )
+{
+    BORA_TRY( grow( s->scan_scratch, bora_scan_scratch_elems( n ) * 4 + 16, false, s->st ) );
+    return BORA_OK;
+}
+
+int ensure_cells( bora_flip_sim* s, int ntiles )
+{
+    if( (size_t)ntiles <= s->cap_tiles && s->cap_tiles ) return BORA_OK;
+    const size_t cap = std::max<size_t>( (size_t)ntiles, s->cap_tiles + s->cap_tiles / 2 );
+    const size_t nc = cap * BORA_TILE_CELLS;
+    DevBuf* f4[] = { &s->mass, &s->surf, &s->pres, &s->vx, &s->vy, &s->vz, &s->cx, &s->cy, &s->cz, &s->rhs,
+                     &s->se, &s->sr, &s->sd0, &s->sd1, &s->sq, &s->sz, &s->sminv };
+    for( DevBuf* b : f4 ) BORA_TRY( grow( *b, nc * 4, false, s->st ) );
+    BORA_TRY( grow( s->flag, nc, false, s->st ) );
+    BORA_TRY( grow( s->code, nc * 2, false, s->st ) );
+    BORA_TRY( grow( s->sx, nc * 8, false, s->st ) );
+    const size_t oldc = s->cell_count.bytes;
+    BORA_TRY( grow( s->cell_count, ( nc + 2 ) * 4, true, s->st ) );
+    if( s->cell_count.bytes > oldc )
+        BORA_TRY( cudaMemsetAsync( (char*)s->cell_count.p + oldc, 0, s->cell_count.bytes - oldc, s->st ) );
+    BORA_TRY( grow( s->cell_start, ( nc + 2 ) * 4, false, s->st ) );
+    BORA_TRY( grow( s->tile_of, cap * 4, false, s->st ) );
+    BORA_TRY( grow( s->nbr, cap * 27 * 4, false, s->st ) );
+    BORA_TRY( grow( s->partials, ( std::max<size_t>( cap, 152 * 16 ) + 16 ) * 2 * 8, false, s->st ) );
+    BORA_TRYS( ensure_scan_scratch( s, std::max( nc + 2, s->ntv ) ) );
+    s->cap_tiles = cap;
+    return BORA_OK;
+}
+
+int read_counters( bora_flip_sim* s, int first, int count )
+{
+    BORA_TRY( cudaMemcpyAsync( s->h_cnt + first, P<uint32_t>( s->counters ) + first, count * 4, cudaMemcpyDeviceToHost, s->st ) );
+    BORA_TRY( cudaStreamSynchronize( s->st ) );
+    return BORA_OK;
+}
+
+double read_ring( bora_flip_sim* s, int slot, int* status )
+{
+    cudaError_t e = cudaMemcpyAsync( s->h_ring, P<double>( s->ring ) + slot, 8, cudaMemcpyDeviceToHost, s->st );
+    if( e == cudaSuccess ) e = cudaStreamSynchronize( s->st );
+    if( e != cudaSuccess ) { *status = cuda_status( e ); return 0.0; }
+    return s->h_ring[0];
+}
+
+// ---- stages --------------------------------------------------------------------------
+
+// SparseFrame::buildFromPoints (SparseFrame.cu:83-155): bin, activate, number the active
+// tiles, then counting-sort the particles by dual cell.
+int stage_rebuild( bora_flip_sim* s )
+{
+    cudaStream_t st = s->st;
+    BORA_TRY( cudaMemsetAsync( s->tile_flag.p, 0, s->ntv, st ) );
+    BORA_TRY( cudaMemsetAsync( s->counters.p, 0, 8 * 4, st ) );
+    if( s->np ) { KTimer t( s, BORA_KERNEL_BIN, 1 ); bora_launch_bin( s->g, s->parts( s->cur ), s->np, P<uint32_t>( s->vkey ), P<uint8_t>( s->tile_flag ), st ); }
+    {
+        KTimer t( s, BORA_KERNEL_TILES, 4 );
+        bora_launch_activate( s->g, P<uint8_t>( s->tile_flag ), P<uint32_t>( s->tile_act ), st );
+        bora_scan_u32( P<uint32_t>( s->tile_act ), P<uint32_t>( s->tile_excl ), s->ntv, P<uint32_t>( s->scan_scratch ),
+                       P<uint32_t>( s->counters ) + 0, st );
+    }
+    BORA_TRYS( check_launch( s ) );
+    BORA_TRYS( read_counters( s, 0, 1 ) );
+    const int ntiles = (int)s->h_cnt[0];
+    BORA_TRYS( ensure_cells( s, std::max( ntiles, 1 ) ) );
+    s->ntiles = ntiles;
+    const uint32_t ncell = (uint32_t)ntiles * BORA_TILE_CELLS;
+    {
+        KTimer t( s, BORA_KERNEL_TILES, ntiles > 0 ? 2 : 1 );
+        bora_launch_tile_assign( s->g, P<uint32_t>( s->tile_act ), P<uint32_t>( s->tile_excl ), P<int32_t>( s->slot_of ),
+                                 P<int32_t>( s->tile_of ), st );
+        bora_launch_tile_nbrs( s->g, ntiles, P<int32_t>( s->slot_of ), P<int32_t>( s->tile_of ), P<int32_t>( s->nbr ), st );
+    }
+    {
+        KTimer t( s, BORA_KERNEL_SORT, s->np ? 5 : 3 );
+        bora_launch_hist( s->np, P<uint32_t>( s->vkey ), P<int32_t>( s->slot_of ), ncell, P<uint32_t>( s->key ),
+                          P<uint32_t>( s->cell_count ), P<uint32_t>( s->counters ) + 2, st );
+        bora_scan_u32( P<uint32_t>( s->cell_count ), P<uint32_t>( s->cell_start ), (size_t)ncell + 1,
+                       P<uint32_t>( s->scan_scratch ), P<uint32_t>( s->counters ) + 1, st );
+        bora_launch_scatter( s->np, P<uint32_t>( s->key ), P<uint32_t>( s->cell_start ), P<uint32_t>( s->cell_count ),
+                             P<uint32_t>( s->idx ), st );
+    }
+    BORA_TRYS( check_launch( s ) );
+    BORA_TRYS( read_counters( s, 1, 2 ) );
+    if( s->h_cnt[2] != 0 ) return BORA_ERR_INTERNAL;
+    s->nsorted = s->h_cnt[1];  // live particles, addressed through idx in dual-cell order
+    s->sorted = true;
+    s->stats.active_tiles = ntiles;
+    return BORA_OK;
+}
+
+int stage_p2g( bora_flip_sim* s )
+{
+    if( !s->sorted ) return BORA_ERR_INVALID_ARG;
+    KTimer t( s, BORA_KERNEL_P2G, s->ntiles > 0 );
+    bora_launch_p2g( s->g, s->ntiles, s->tiles(), s->parts( s->cur ), P<uint32_t>( s->idx ), P<uint32_t>( s->cell_start ),
+                     s->cells(), s->st );
+    return check_launch( s );
+}
+
+int stage_build_system( bora_flip_sim* s )
+{
+    KTimer t( s, BORA_KERNEL_RHS, s->ntiles > 0 ? 2 : 0 );
+    bora_launch_rhs( s->g, s->ntiles, s->tiles(), s->cells(), s->st );
+    bora_launch_mic_factor( s->g, s->ntiles, P<uint16_t>( s->code ), P<float>( s->sminv ), s->st );
+    return check_launch( s );
+}
+
+// Pressure solve: FP64 iterative refinement around FP32 PCG passes.
+int stage_solve( bora_flip_sim* s )
+{
+    const bora_flip_params& p = s->prm;
+    BoraSolverDev sv = s->solver();
+    BoraReduceDev red = s->reducer();
+    const uint16_t* code = P<uint16_t>( s->code );
+    const float* b = P<float>( s->rhs );
+    cudaStream_t st = s->st;
+    int status = BORA_OK;
+    const double dx = s->scale[0];
+
+    const int s_b2 = s->slot(), s_bmax = s->slot();
+    { KTimer t( s, BORA_KERNEL_REFINE, 1 ); bora_launch_solve_init( s->ntiles, b, code, sv, red, s_b2, s_bmax, st ); }
+    BORA_TRYS( check_launch( s ) );
+    const double bnorm = std::sqrt( read_ring( s, s_b2, &status ) );
+    BORA_TRYS( status );
+    double rnorm = bnorm, rmax = read_ring( s, s_bmax, &status );
+    BORA_TRYS( status );
+    int total_it = 0, passes = 0;
+    bool converged = false;
+    const int max_inner = std::max( 1, p.proj_iteration );
+    const int check = std::max( 1, p.check_every );
+    for( ;; )
+    {
+        const bool norm_ok = rnorm <= p.tolerance * bnorm;
+        const bool max_ok = rmax * dx <= p.div_tolerance;
+        if( bnorm == 0.0 || ( norm_ok && max_ok ) ) { converged = true; break; }
+        if( passes >= std::max( 1, p.max_refinements ) ) break;
+        // inner FP32 PCG on A e = r
+        const double target = norm_ok ? 0.1 * rnorm : std::max( p.inner_tolerance * rnorm, 0.25 * p.tolerance * bnorm );
+        int rz_cur = s->slot(), rr_cur = s->slot();
+        { KTimer t( s, BORA_KERNEL_PCG_UPDATE, 1 ); bora_launch_pcg_update( s->ntiles, code, sv, 0, red, -1, -1, rz_cur, rr_cur, st ); }
+        int rz_prev = -1, dsel = 0, it = 0;
+        while( it < max_inner )
+        {
+            const int s_dq = s->slot();
+            { KTimer t( s, BORA_KERNEL_PCG_DIRECTION, 1 ); bora_launch_pcg_direction( s->g, s->ntiles, s->tiles(), code, sv, dsel, red, rz_cur, rz_prev, s_dq, st ); }
+            dsel ^= 1;
+            const int rz_new = s->slot(), rr_new = s->slot();
+            { KTimer t( s, BORA_KERNEL_PCG_UPDATE, 1 ); bora_launch_pcg_update( s->ntiles, code, sv, dsel, red, rz_cur, s_dq, rz_new, rr_new, st ); }
+            rz_prev = rz_cur;
+            rz_cur = rz_new;
+            rr_cur = rr_new;
+            ++it;
+            if( it % check == 0 )
+            {
+                BORA_TRYS( check_launch( s ) );
+                const double rr = read_ring( s, rr_cur, &status );
+                BORA_TRYS( status );
+                if( !( rr > 0.0 ) || std::sqrt( rr ) <= target ) break;
+            }
+        }
+        total_it += it;
+        ++passes;
+        const int s_n2 = s->slot(), s_mx = s->slot();
+        {
+            KTimer t( s, BORA_KERNEL_REFINE, 2 );
+            bora_launch_refine_accumulate( s->ntiles, code, sv, st );
+            bora_launch_refine_residual( s->g, s->ntiles, s->tiles(), b, code, sv, red, s_n2, s_mx, st );
+        }
+        BORA_TRYS( check_launch( s ) );
+        rnorm = std::sqrt( read_ring( s, s_n2, &status ) );
+        BORA_TRYS( status );
+        rmax = read_ring( s, s_mx, &status );
+        BORA_TRYS( status );
+        if( !std::isfinite( rnorm ) ) break;
+    }
+    { KTimer t( s, BORA_KERNEL_REFINE, 1 ); bora_launch_write_pressure( s->ntiles, code, sv.x, P<float>( s->pres ), st ); }
+    BORA_TRYS( check_launch( s ) );
+    s->stats.solver_iterations = total_it;
+    s->stats.refinements = passes;
+    s->stats.residual_rel = bnorm > 0.0 ? rnorm / bnorm : 0.0;
+    s->stats.residual_max = rmax;
+    s->stats.residual_max_dx = rmax * dx;
+    s->stats.converged = converged ? 1 : 0;
+    return converged ? BORA_OK : BORA_WARN_NOT_CONVERGED;
+}
+
+int stage_update_velocity( bora_flip_sim* s )
+{
+    KTimer t( s, BORA_KERNEL_VELOCITY, s->ntiles > 0 );
+    bora_launch_vel_update( s->g, s->ntiles, s->tiles(), s->cells(), s->st );
+    return check_launch( s );
+}
+
+int stage_update_particles( bora_flip_sim* s, float dt )
+{
+    if( !s->sorted ) return BORA_ERR_INVALID_ARG;
+    cudaStream_t st = s->st;
+    BORA_TRY( cudaMemsetAsync( P<uint32_t>( s->counters ) + 3, 0, 4, st ) );
+    const int nxt = s->cur ^ 1;
+    {
+        KTimer t( s, BORA_KERNEL_G2P, s->nsorted > 0 );
+        bora_launch_g2p( s->g, s->nsorted, P<int32_t>( s->slot_of ), s->cells(), s->parts( s->cur ), P<uint32_t>( s->idx ),
+                         s->parts( nxt ), P<float>( s->adj ), dt, P<uint32_t>( s->counters ) + 3, st );
+    }
+    BORA_TRYS( check_launch( s ) );
+    BORA_TRYS( read_counters( s, 3, 1 ) );
+    s->cur = nxt;
+    s->np = s->nsorted;
+    s->sorted = false;
+    s->stats.killed_last_step = s->h_cnt[3];
+    s->nlive = s->np - s->h_cnt[3];
+    s->stats.num_particles = s->nlive;
+    return BORA_OK;
+}
+
+int add_particles( bora_flip_sim* s, const float* pos, const float* vel, size_t n, int space )
+{
+    if( n == 0 ) return BORA_OK;
+    if( !pos ) return BORA_ERR_INVALID_ARG;
+    if( s->np + n > (size_t)0x7FFFFFF0 ) return BORA_ERR_CAPACITY;
+    BORA_TRYS( ensure_particles( s, s->np + n ) );
+    BORA_TRY( grow( s->stage_in, n * 24, false, s->st ) );
+    float* dpos = P<float>( s->stage_in );
+    float* dvel = dpos + 3 * n;
+    BORA_TRY( cudaMemcpyAsync( dpos, pos, n * 12, cudaMemcpyHostToDevice, s->st ) );
+    if( vel ) BORA_TRY( cudaMemcpyAsync( dvel, vel, n * 12, cudaMemcpyHostToDevice, s->st ) );
+    s->stats.kernel_launches += 1;
+    bora_launch_to_soa( n, dpos, vel ? dvel : nullptr, space == BORA_SPACE_VOXEL ? 1 : 0, s->translate, s->scale,
+                        s->parts( s->cur ), s->np, s->next_id, s->st );
+    BORA_TRY( cudaMemsetAsync( P<float>( s->adj ) + s->np, 0, n * 4, s->st ) );
+    BORA_TRYS( check_launch( s ) );
+    BORA_TRY( cudaStreamSynchronize( s->st ) );  // the caller may free its buffers on return
+    s->np += n;
+    s->nlive += n;
+    s->next_id += (int32_t)n;
+    s->sorted = false;
+    s->stats.num_particles = s->nlive;
+    return BORA_OK;
+}
+
+}  // namespace
+
+// ======================================================================================
+extern "C" {
+
+int bora_flip_default_params( bora_flip_params* o )
+{
+    if( !o ) return BORA_ERR_INVALID_ARG;
+    std::memset( o, 0, sizeof( *o ) );
+    o->ext_force[0] = 0.f; o->ext_force[1] = -9.80665f; o->ext_force[2] = 0.f;
+    o->max_substeps = 1;
+    o->dt = 1.f / 24.f;
+    o->wall_level = -1e+30f;
+    o->enable_water_tank = 0;
+    o->enable_curl = 0;
+    o->damping_band = 0.f;
+    o->voxel_size = 0.1f;
+    o->col_vel_scale = 1.f;
+    o->pts_per_cell = 8;
+    o->vort_pres_rate = 0.2f;
+    o->adjacency_under = 2.f;
+    o->proj_iteration = 200;
+    o->redist_iteration = 80;
+    o->solver = BORA_SOLVER_PLAIN;
+    o->tolerance = 1e-6;
+    o->div_tolerance = 1e-5;
+    o->inner_tolerance = 1e-4;
+    o->max_refinements = 8;
+    o->check_every = 8;
+    return BORA_OK;
+}
+
+static int validate_params( const bora_flip_params* p )
+{
+    if( !p ) return BORA_ERR_INVALID_ARG;
+    if( p->enable_curl ) return BORA_ERR_INVALID_ARG;  // curl noise is outside this library
+    if( p->solver != BORA_SOLVER_PLAIN ) return BORA_ERR_INVALID_ARG;
+    if( !( p->voxel_size > 0.f ) || !( p->tolerance > 0.0 ) ) return BORA_ERR_INVALID_ARG;
+    return BORA_OK;
+}
+
+int bora_flip_create( const bora_grid_desc* grid, const bora_flip_params* params, bora_flip_handle* out )
+{
+    if( !grid || !out ) return BORA_ERR_INVALID_ARG;
+    *out = nullptr;
+    if( grid->nx <= 0 || grid->ny <= 0 || grid->nz <= 0 ) return BORA_ERR_INVALID_ARG;
+    if( (double)grid->nx * grid->ny * grid->nz > 4.0e9 ) return BORA_ERR_CAPACITY;
+    for( int a = 0; a < 3; ++a )
+        if( !( grid->max[a] > grid->min[a] ) ) return BORA_ERR_INVALID_ARG;
+    bora_flip_params defaults;
+    bora_flip_default_params( &defaults );
+    const bora_flip_params* p = params ? params : &defaults;
+    BORA_TRYS( validate_params( p ) );
+    int ndev = 0;
+    if( cudaGetDeviceCount( &ndev ) != cudaSuccess || ndev == 0 ) return BORA_ERR_NO_DEVICE;
+    bora_flip_sim* s = new( std::nothrow ) bora_flip_sim();
+    if( !s ) return BORA_ERR_OUT_OF_MEMORY;
+    cudaGetDevice( &s->device );
+    s->gdesc = *grid;
+    s->prm = *p;
+    setup_frame( s );
+    apply_params( s );
+    int st = cuda_status( cudaStreamCreateWithFlags( &s->st, cudaStreamNonBlocking ) );
+    if( st == BORA_OK ) st = cuda_status( cudaEventCreate( &s->ev_step[0] ) );
+    if( st == BORA_OK ) st = cuda_status( cudaEventCreate( &s->ev_step[1] ) );
+    if( st == BORA_OK ) st = cuda_status( cudaHostAlloc( (void**)&s->h_cnt, 64, cudaHostAllocDefault ) );
+    if( st == BORA_OK ) st = cuda_status( cudaHostAlloc( (void**)&s->h_ring, 64, cudaHostAllocDefault ) );
+    if( st == BORA_OK ) st = cuda_status( grow( s->tile_flag, s->ntv, false, s->st ) );
+    if( st == BORA_OK ) st = cuda_status( grow( s->tile_act, s->ntv * 4, false, s->st ) );
+    if( st == BORA_OK ) st = cuda_status( grow( s->tile_excl, s->ntv * 4, false, s->st ) );
+    if( st == BORA_OK ) st = cuda_status( grow( s->slot_of, s->ntv * 4, false, s->st ) );
+    if( st == BORA_OK ) st = cuda_status( grow( s->counters, 64, false, s->st ) );
+    if( st == BORA_OK ) st = cuda_status( grow( s->ring, BORA_RING * 8, false, s->st ) );
+    if( st == BORA_OK ) st = cuda_status( grow( s->done, BORA_RING * 4, false, s->st ) );
+    if( st == BORA_OK ) st = cuda_status( cudaMemsetAsync( s->done.p, 0, BORA_RING * 4, s->st ) );
+    if( st == BORA_OK ) st = cuda_status( cudaMemsetAsync( s->ring.p, 0, BORA_RING * 8, s->st ) );
+    if( st == BORA_OK ) st = ensure_cells( s, 1 );
+    if( st == BORA_OK ) st = ensure_scan_scratch( s, s->ntv + 2 );
+    if( st == BORA_OK ) st = cuda_status( cudaStreamSynchronize( s->st ) );
+    if( st != BORA_OK )
+    {
+        bora_flip_destroy( s );
+        return st;
+    }
+    *out = s;
+    return BORA_OK;
+}
+
+int bora_flip_destroy( bora_flip_handle s )
+{
+    if( !s ) return BORA_ERR_INVALID_ARG;
+    if( s->st ) cudaStreamSynchronize( s->st );
+    DevBuf* all[] = { &s->tile_flag, &s->tile_act, &s->tile_excl, &s->slot_of, &s->tile_of, &s->nbr, &s->mass, &s->surf,
+                      &s->pres, &s->vx, &s->vy, &s->vz, &s->cx, &s->cy, &s->cz, &s->flag, &s->code, &s->rhs, &s->sx,
+                      &s->se, &s->sr, &s->sd0, &s->sd1, &s->sq, &s->sz, &s->sminv, &s->cell_count, &s->cell_start,
+                      &s->ring, &s->partials, &s->done, &s->adj, &s->vkey, &s->key, &s->idx, &s->scan_scratch,
+                      &s->counters, &s->stage_in, &s->stage_out, &s->live_flag };
+    for( DevBuf* b : all ) release( *b );
+    for( int b = 0; b < 2; ++b )
+        for( int a = 0; a < 7; ++a ) release( s->pbuf[b][a] );
+    s->prof_resolve();
+    for( cudaEvent_t e : s->evpool ) cudaEventDestroy( e );
+    for( int q = 0; q < 2; ++q )
+        if( s->ev_step[q] ) cudaEventDestroy( s->ev_step[q] );
+    if( s->h_cnt ) cudaFreeHost( s->h_cnt );
+    if( s->h_ring ) cudaFreeHost( s->h_ring );
+    if( s->st ) cudaStreamDestroy( s->st );
+    delete s;
+    return BORA_OK;
+}
+
+int bora_flip_set_params( bora_flip_handle s, const bora_flip_params* p )
+{
+    if( !s ) return BORA_ERR_INVALID_ARG;
+    BORA_TRYS( validate_params( p ) );
+    s->prm = *p;
+    apply_params( s );
+    return BORA_OK;
+}
+
+int bora_flip_add_particles( bora_flip_handle s, const float* pos, const float* vel, size_t n, int space )
+{
+    if( !s ) return BORA_ERR_INVALID_ARG;
+    return add_particles( s, pos, vel, n, space );
+}
+
+int bora_flip_clear_particles( bora_flip_handle s )
+{
+    if( !s ) return BORA_ERR_INVALID_ARG;
+    s->np = 0;
+    s->nlive = 0;
+    s->next_id = 0;
+    s->sorted = false;
+    s->stats.num_particles = 0;
+    return BORA_OK;
+}
+
+int bora_flip_set_particles( bora_flip_handle s, const float* pos, const float* vel, size_t n, int space )
+{
+    BORA_TRYS( bora_flip_clear_particles( s ) );
+    return add_particles( s, pos, vel, n, space );
+}
+
+int bora_flip_set_colliders( bora_flip_handle s, const float* boxes, int n, float band )
+{
+    if( !s || n < 0 || n > BORA_MAX_COLLIDERS || ( n > 0 && !boxes ) || !( band > 0.f ) ) return BORA_ERR_INVALID_ARG;
+    BoraColliderDev& c = s->g.cols;
+    std::memset( &c, 0, sizeof( c ) );
+    c.count = n;
+    c.band = band;
+    for( int q = 0; q < n; ++q )
+        for( int a = 0; a < 3; ++a )
+        {
+            c.box[q].lo[a] = boxes[9 * q + a];
+            c.box[q].hi[a] = boxes[9 * q + 3 + a];
+            c.box[q].vel[a] = boxes[9 * q + 6 + a];
+        }
+    return BORA_OK;
+}
+
+int bora_flip_run_stage( bora_flip_handle s, int stage, float dt )
+{
+    if( !s ) return BORA_ERR_INVALID_ARG;
+    switch( stage )
+    {
+        case BORA_STAGE_REBUILD: return stage_rebuild( s );
+        case BORA_STAGE_P2G: return stage_p2g( s );
+        case BORA_STAGE_BUILD_SYSTEM: return stage_build_system( s );
+        case BORA_STAGE_SOLVE: return stage_solve( s );
+        case BORA_STAGE_UPDATE_VELOCITY: return stage_update_velocity( s );
+        case BORA_STAGE_UPDATE_PARTICLES: return stage_update_particles( s, dt );
+        default: return BORA_ERR_INVALID_ARG;
+    }
+}
+
+int bora_flip_step( bora_flip_handle s, float dt )
+{
+    if( !s ) return BORA_ERR_INVALID_ARG;
+    if( s->np == 0 ) return BORA_OK;  // FLIPMethod.cu:179
+    const auto t0 = std::chrono::steady_clock::now();
+    cudaEventRecord( s->ev_step[0], s->st );
+    BORA_TRYS( stage_rebuild( s ) );
+    BORA_TRYS( stage_p2g( s ) );
+    BORA_TRYS( stage_build_system( s ) );
+    const int solve = stage_solve( s );
+    BORA_TRYS( solve );
+    BORA_TRYS( stage_update_velocity( s ) );
+    BORA_TRYS( stage_update_particles( s, dt ) );
+    cudaEventRecord( s->ev_step[1], s->st );
+    BORA_TRY( cudaEventSynchronize( s->ev_step[1] ) );
+    float gms = 0.f;
+    cudaEventElapsedTime( &gms, s->ev_step[0], s->ev_step[1] );
+    s->stats.gpu_ms = gms;
+    s->prof_resolve();
+    s->stats.steps++;
+    s->stats.stage_ms[7] = std::chrono::duration<double, std::milli>( std::chrono::steady_clock::now() - t0 ).count();
+    return solve;
+}
+
+int bora_flip_frame( bora_flip_handle s )
+{
+    if( !s ) return BORA_ERR_INVALID_ARG;
+    return bora_flip_step( s, s->prm.dt );
+}
+
+int bora_flip_num_particles( bora_flip_handle s, size_t* n )
+{
+    if( !s || !n ) return BORA_ERR_INVALID_ARG;
+    *n = s->nlive;
+    return BORA_OK;
+}
+
+int bora_flip_get_particles( bora_flip_handle s, float* pos, float* vel, float* adjacency, int32_t* ids, size_t cap,
+                             size_t* n, int space )
+{
+    if( !s ) return BORA_ERR_INVALID_ARG;
+    if( cap < s->nlive && ( pos || vel || adjacency || ids ) ) return BORA_ERR_CAPACITY;
+    if( n ) *n = s->nlive;
+    if( s->np == 0 ) return BORA_OK;
+    cudaStream_t st = s->st;
+    const size_t np = s->np;
+    BORA_TRYS( ensure_scan_scratch( s, std::max( np + 1, std::max( s->ntv, s->cap_tiles * BORA_TILE_CELLS + 2 ) ) ) );
+    BORA_TRY( grow( s->stage_out, s->nlive * 32 + 64, false, st ) );
+    BoraParticlesDev p = s->parts( s->cur );
+    s->stats.kernel_launches += 5;
+    k_live_flags<<<grid_blocks( np ), 256, 0, st>>>( np, p.id, P<uint32_t>( s->live_flag ) );
+    bora_scan_u32( P<uint32_t>( s->live_flag ), P<uint32_t>( s->live_flag ), np, P<uint32_t>( s->scan_scratch ),
+                   P<uint32_t>( s->counters ) + 4, st );
+    const size_t nl = s->nlive;
+    float* opos = P<float>( s->stage_out );
+    float* ovel = opos + 3 * nl;
+    float* oadj = ovel + 3 * nl;
+    int32_t* oid = reinterpret_cast<int32_t*>( oadj + nl );
+    const float3 tr = make_float3( s->translate[0], s->translate[1], s->translate[2] );
+    const float3 sc = make_float3( s->scale[0], s->scale[1], s->scale[2] );
+    k_gather_live<<<grid_blocks( np ), 256, 0, st>>>( np, p, P<float>( s->adj ), P<uint32_t>( s->live_flag ), space, tr, sc,
+                                                      opos, ovel, oadj, oid );
+    BORA_TRYS( check_launch( s ) );
+    if( pos ) BORA_TRY( cudaMemcpyAsync( pos, opos, nl * 12, cudaMemcpyDeviceToHost, st ) );
+    if( vel ) BORA_TRY( cudaMemcpyAsync( vel, ovel, nl * 12, cudaMemcpyDeviceToHost, st ) );
+    if( adjacency ) BORA_TRY( cudaMemcpyAsync( adjacency, oadj, nl * 4, cudaMemcpyDeviceToHost, st ) );
+    if( ids ) BORA_TRY( cudaMemcpyAsync( ids, oid, nl * 4, cudaMemcpyDeviceToHost, st ) );
+    BORA_TRY( cudaStreamSynchronize( st ) );
+    return BORA_OK;
+}
+
+int bora_flip_frame_info( bora_flip_handle s, bora_frame_info* o )
+{
+    if( !s || !o ) return BORA_ERR_INVALID_ARG;
+    o->nx = s->g.nx; o->ny = s->g.ny; o->nz = s->g.nz;
+    o->tx = s->g.tx; o->ty = s->g.ty; o->tz = s->g.tz;
+    o->tile = BORA_TILE;
+    o->active_tiles = s->ntiles;
+    for( int a = 0; a < 3; ++a ) { o->translate[a] = s->translate[a]; o->scale[a] = s->scale[a]; o->voxel_gravity[a] = s->g.gravity[a]; }
+    o->voxel_wall_level = s->g.voxel_wall;
+    return BORA_OK;
+}
+
+int bora_flip_get_tiles( bora_flip_handle s, int32_t* ijk, size_t cap_tiles )
+{
+    if( !s || ( !ijk && s->ntiles ) ) return BORA_ERR_INVALID_ARG;
+    if( cap_tiles < (size_t)s->ntiles ) return BORA_ERR_CAPACITY;
+    std::vector<int32_t> lin( (size_t)s->ntiles );
+    if( s->ntiles )
+    {
+        BORA_TRY( cudaMemcpyAsync( lin.data(), s->tile_of.p, lin.size() * 4, cudaMemcpyDeviceToHost, s->st ) );
+        BORA_TRY( cudaStreamSynchronize( s->st ) );
+    }
+    for( size_t t = 0; t < lin.size(); ++t )
+    {
+        ijk[3 * t] = lin[t] % s->g.tx;
+        ijk[3 * t + 1] = ( lin[t] / s->g.tx ) % s->g.ty;
+        ijk[3 * t + 2] = lin[t] / ( s->g.tx * s->g.ty );
+    }
+    return BORA_OK;
+}
+
+static int field_bufs( bora_flip_handle s, int which, DevBuf** b, int* ncomp, size_t* esize )
+{
+    *ncomp = 1;
+    *esize = 4;
+    switch( which )
+    {
+        case BORA_FIELD_MASS: b[0] = &s->mass; return BORA_OK;
+        case BORA_FIELD_SURF: b[0] = &s->surf; return BORA_OK;
+        case BORA_FIELD_PRES: b[0] = &s->pres; return BORA_OK;
+        case BORA_FIELD_VELO: b[0] = &s->vx; b[1] = &s->vy; b[2] = &s->vz; *ncomp = 3; return BORA_OK;
+        case BORA_FIELD_COMP: b[0] = &s->cx; b[1] = &s->cy; b[2] = &s->cz; *ncomp = 3; return BORA_OK;
+        case BORA_FIELD_FLAG: b[0] = &s->flag; *esize = 1; return BORA_OK;
+        case BORA_FIELD_RHS: b[0] = &s->rhs; return BORA_OK;
+        case BORA_FIELD_CODE: b[0] = &s->code; *esize = 2; return BORA_OK;
+        default: return BORA_ERR_INVALID_ARG;
+    }
+}
+
+int bora_flip_get_field( bora_flip_handle s, int which, void* out, size_t bytes )
+{
+    if( !s || !out ) return BORA_ERR_INVALID_ARG;
+    DevBuf* b[3];
+    int nc;
+    size_t es;
+    BORA_TRYS( field_bufs( s, which, b, &nc, &es ) );
+    const size_t ncell = (size_t)s->ntiles * BORA_TILE_CELLS;
+    if( bytes < ncell * nc * es ) return BORA_ERR_CAPACITY;
+    if( nc == 1 )
+    {
+        BORA_TRY( cudaMemcpyAsync( out, b[0]->p, ncell * es, cudaMemcpyDeviceToHost, s->st ) );
+        BORA_TRY( cudaStreamSynchronize( s->st ) );
+        return BORA_OK;
+    }
+    std::vector<float> tmp( ncell );
+    float* o = (float*)out;
+    for( int c = 0; c < nc; ++c )
+    {
+        BORA_TRY( cudaMemcpyAsync( tmp.data(), b[c]->p, ncell * 4, cudaMemcpyDeviceToHost, s->st ) );
+        BORA_TRY( cudaStreamSynchronize( s->st ) );
+        for( size_t i = 0; i < ncell; ++i ) o[3 * i + c] = tmp[i];
+    }
+    return BORA_OK;
+}
+
+int bora_flip_set_field( bora_flip_handle s, int which, const void* in, size_t bytes )
+{
+    if( !s || !in ) return BORA_ERR_INVALID_ARG;
+    DevBuf* b[3];
+    int nc;
+    size_t es;
+    BORA_TRYS( field_bufs( s, which, b, &nc, &es ) );
+    const size_t ncell = (size_t)s->ntiles * BORA_TILE_CELLS;
+    if( bytes < ncell * nc * es ) return BORA_ERR_CAPACITY;
+    if( nc == 1 )
+    {
+        BORA_TRY( cudaMemcpyAsync( b[0]->p, in, ncell * es, cudaMemcpyHostToDevice, s->st ) );
+        BORA_TRY( cudaStreamSynchronize( s->st ) );
+        return BORA_OK;
+    }
+    std::vector<float> tmp( ncell );
+    const float* src = (const float*)in;
+    for( int c = 0; c < nc; ++c )
+    {
+        for( size_t i = 0; i < ncell; ++i ) tmp[i] = src[3 * i + c];
+        BORA_TRY( cudaMemcpyAsync( b[c]->p, tmp.data(), ncell * 4, cudaMemcpyHostToDevice, s->st ) );
+        BORA_TRY( cudaStreamSynchronize( s->st ) );
+    }
+    return BORA_OK;
+}
+
+int bora_flip_get_stats( bora_flip_handle s, bora_flip_stats* o )
+{
+    if( !s || !o ) return BORA_ERR_INVALID_ARG;
+    *o = s->stats;
+    o->num_particles = s->nlive;
+    return BORA_OK;
+}
+
+int bora_flip_set_profiling( bora_flip_handle s, uint32_t mask )
+{
+    if( !s ) return BORA_ERR_INVALID_ARG;
+    BORA_TRY( cudaStreamSynchronize( s->st ) );
+    s->prof_resolve();
+    s->prof_mask = mask;
+    for( int c = 0; c < BORA_KERNEL_CLASSES; ++c ) { s->kt_ms[c] = 0.0; s->kt_n[c] = 0; }
+    return BORA_OK;
+}
+
+int bora_flip_get_kernel_times( bora_flip_handle s, double* ms, uint64_t* launches, int n )
+{
+    if( !s || n < 0 || n > BORA_KERNEL_CLASSES ) return BORA_ERR_INVALID_ARG;
+    BORA_TRY( cudaStreamSynchronize( s->st ) );
+    s->prof_resolve();
+    for( int c = 0; c < n; ++c )
+    {
+        if( ms ) ms[c] = s->kt_ms[c];
+        if( launches ) launches[c] = s->kt_n[c];
+    }
+    return BORA_OK;
+}
+
+const char* bora_flip_status_string( int st )
+{
+    switch( st )
+    {
+        case BORA_OK: return "ok";
+        case BORA_ERR_INVALID_ARG: return "invalid argument";
+        case BORA_ERR_OUT_OF_MEMORY: return "out of device memory";
+        case BORA_ERR_CUDA: return "CUDA error";
+        case BORA_ERR_NO_DEVICE: return "no CUDA device";
+        case BORA_ERR_INTERNAL: return "internal consistency check failed";
+        case BORA_ERR_CAPACITY: return "buffer too small or size limit exceeded";
+        case BORA_WARN_NOT_CONVERGED: return "pressure solve stopped before reaching its tolerance";
+        default: return "unknown status";
+    }
+}
+
+}  // extern "C"

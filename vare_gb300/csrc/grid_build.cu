@@ -1,0 +1,239 @@
+// Sparse-grid rebuild on the device: particle binning, tile activation, the tile table
+// and the per-step counting sort of particles by dual cell.
+//
+// Replaces SparseFrame::buildFromPoints (base/source/SparseFrame.cu:83-155), whose
+// per-particle 27-way atomicAdd marks a dense tile-count table and whose serial host
+// loop compacts it, and SparseField::build (SparseField.h:221-226).
+//
+// Activation rule at the 8^3 tile edge: tile T is active iff some particle's tile
+// (max(int(p)/8, 0), clamped to the table) lies within one tile of T in every axis.
+// Active tiles take slots in linear tile order (x fastest), as the reference numbers
+// its active tiles. The reference's unclamped lower loop bound (SparseFrame.cu:105-107)
+// that wraps index -1 into the previous row is not reproduced.
+#include "bora_internal.h"
+
+namespace {
+
+constexpr int kThreads = 256;
+
+inline int grid_for( size_t n, int threads = kThreads )
+{
+    const size_t b = ( n + threads - 1 ) / threads;
+    return (int)( b < 152 * 16 ? ( b > 0 ? b : 1 ) : 152 * 16 );
+}
+
+// Grid::inside (base/header/Grid.h:408-417)
+__device__ inline bool inside_grid( const BoraGridDev& g, float x, float y, float z )
+{
+    return !( x < 0.f || x > (float)g.nx || y < 0.f || y > (float)g.ny || z < 0.f || z > (float)g.nz );
+}
+
+__global__ void k_bin( BoraGridDev g, BoraParticlesDev p, size_t n, uint32_t* __restrict__ vkey,
+                       uint8_t* __restrict__ tile_flag )
+{
+    for( size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x )
+    {
+        if( p.id[i] < 0 ) { vkey[i] = BORA_DEAD_KEY; continue; }
+        const float x = p.px[i], y = p.py[i], z = p.pz[i];
+        // activation tile: SparseFrame.cu:101-103 at tile edge 8, clamped to the table
+        const int ti = bora_imin( bora_imax( bora_trunc( x ) / BORA_TILE, 0 ), g.tx - 1 );
+        const int tj = bora_imin( bora_imax( bora_trunc( y ) / BORA_TILE, 0 ), g.ty - 1 );
+        const int tk = bora_imin( bora_imax( bora_trunc( z ) / BORA_TILE, 0 ), g.tz - 1 );
+        tile_flag[( (size_t)tk * g.ty + tj ) * g.tx + ti] = 1;
+        if( !inside_grid( g, x, y, z ) ) { vkey[i] = BORA_DEAD_KEY - 1; continue; }
+        // dual cell = base of the P2G stencil (Rasterization.cu:139-141); <= n-1 inside
+        const int di = bora_imax( bora_trunc( x - 0.5f ), 0 );
+        const int dj = bora_imax( bora_trunc( y - 0.5f ), 0 );
+        const int dk = bora_imax( bora_trunc( z - 0.5f ), 0 );
+        const uint32_t vt = (uint32_t)( ( (size_t)( dk >> 3 ) * g.ty + ( dj >> 3 ) ) * g.tx + ( di >> 3 ) );
+        vkey[i] = vt * BORA_TILE_CELLS + (uint32_t)bora_local( di, dj, dk );
+    }
+}
+
+__global__ void k_activate( BoraGridDev g, const uint8_t* __restrict__ tile_flag, uint32_t* __restrict__ act )
+{
+    const size_t ntv = (size_t)g.tx * g.ty * g.tz;
+    for( size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < ntv; t += (size_t)gridDim.x * blockDim.x )
+    {
+        const int ti = (int)( t % g.tx ), tj = (int)( ( t / g.tx ) % g.ty ), tk = (int)( t / ( (size_t)g.tx * g.ty ) );
+        uint32_t a = 0;
+        for( int dk = -1; dk <= 1 && !a; ++dk )
+        {
+            const int k = tk + dk;
+            if( k < 0 || k >= g.tz ) continue;
+            for( int dj = -1; dj <= 1 && !a; ++dj )
+            {
+                const int j = tj + dj;
+                if( j < 0 || j >= g.ty ) continue;
+                for( int di = -1; di <= 1; ++di )
+                {
+                    const int i = ti + di;
+                    if( i < 0 || i >= g.tx ) continue;
+                    if( tile_flag[( (size_t)k * g.ty + j ) * g.tx + i] ) { a = 1; break; }
+                }
+            }
+        }
+        act[t] = a;
+    }
+}
+
+__global__ void k_tile_assign( size_t ntv, const uint32_t* __restrict__ act, const uint32_t* __restrict__ excl,
+                               int32_t* __restrict__ slot_of, int32_t* __restrict__ tile_of )
+{
+    for( size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < ntv; t += (size_t)gridDim.x * blockDim.x )
+    {
+        if( act[t] )
+        {
+            const int32_t s = (int32_t)excl[t];
+            slot_of[t] = s;
+            tile_of[s] = (int32_t)t;
+        }
+        else
+        {
+            slot_of[t] = -1;
+        }
+    }
+}
+
+__global__ void k_tile_nbrs( BoraGridDev g, int ntiles, const int32_t* __restrict__ slot_of,
+                             const int32_t* __restrict__ tile_of, int32_t* __restrict__ nbr )
+{
+    const size_t total = (size_t)ntiles * 27;
+    for( size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < total; q += (size_t)gridDim.x * blockDim.x )
+    {
+        const int s = (int)( q / 27 ), d = (int)( q % 27 );
+        const int t = tile_of[s];
+        const int ti = t % g.tx, tj = ( t / g.tx ) % g.ty, tk = t / ( g.tx * g.ty );
+        const int i = ti + d % 3 - 1, j = tj + ( d / 3 ) % 3 - 1, k = tk + d / 9 - 1;
+        int32_t v = -1;
+        if( i >= 0 && i < g.tx && j >= 0 && j < g.ty && k >= 0 && k < g.tz )
+            v = slot_of[( (size_t)k * g.ty + j ) * g.tx + i];
+        nbr[q] = v;
+    }
+}
+
+// Per-dual-cell particle histogram; one atomic per distinct key per warp.
+__global__ void k_hist( size_t n, const uint32_t* __restrict__ vkey, const int32_t* __restrict__ slot_of,
+                        uint32_t outside_key, uint32_t* __restrict__ key, uint32_t* __restrict__ count,
+                        uint32_t* __restrict__ err )
+{
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    const size_t nround = ( n + 31 ) & ~(size_t)31;
+    for( size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < nround; i += stride )
+    {
+        uint32_t k = BORA_DEAD_KEY;
+        if( i < n )
+        {
+            const uint32_t v = vkey[i];
+            if( v == BORA_DEAD_KEY - 1 ) k = outside_key;
+            else if( v != BORA_DEAD_KEY )
+            {
+                const int32_t s = slot_of[v / BORA_TILE_CELLS];
+                if( s >= 0 ) k = (uint32_t)s * BORA_TILE_CELLS + ( v % BORA_TILE_CELLS );
+                else { k = outside_key; atomicAdd( err, 1u ); }  // cannot happen: dual cells lie in active tiles
+            }
+            key[i] = k;
+        }
+        const uint32_t peers = __match_any_sync( 0xffffffffu, k );
+        const int lane = threadIdx.x & 31;
+        if( k != BORA_DEAD_KEY && lane == __ffs( peers ) - 1 ) atomicAdd( &count[k], (uint32_t)__popc( peers ) );
+    }
+}
+
+// Counting-sort scatter: every live particle gets a slot inside its dual cell's range.
+// The per-key counters are consumed (they are all zero afterwards, ready for the next
+// histogram).
+__global__ void k_scatter( size_t n, const uint32_t* __restrict__ key, const uint32_t* __restrict__ start,
+                           uint32_t* __restrict__ count, uint32_t* __restrict__ idx )
+{
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    const size_t nround = ( n + 31 ) & ~(size_t)31;
+    for( size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < nround; i += stride )
+    {
+        const uint32_t k = i < n ? key[i] : BORA_DEAD_KEY;
+        const uint32_t peers = __match_any_sync( 0xffffffffu, k );
+        const int lane = threadIdx.x & 31;
+        const int leader = __ffs( peers ) - 1;
+        uint32_t top = 0;
+        if( k != BORA_DEAD_KEY && lane == leader ) top = atomicSub( &count[k], (uint32_t)__popc( peers ) );
+        top = __shfl_sync( 0xffffffffu, top, leader );
+        if( k != BORA_DEAD_KEY )
+        {
+            const uint32_t rank = (uint32_t)__popc( peers & ( ( 1u << lane ) - 1u ) );
+            const uint32_t dst = start[k] + top - (uint32_t)__popc( peers ) + rank;
+            idx[dst] = (uint32_t)i;
+        }
+    }
+}
+
+// Host AoS (x,y,z) particles -> device SoA, with the world->voxel transform
+// (Grid::voxelPoint / voxelVector, base/header/Grid.h:446-458) when space == 0.
+__global__ void k_to_soa( size_t n, const float* __restrict__ pos, const float* __restrict__ vel, int space,
+                          float3 tr, float3 sc, BoraParticlesDev p, size_t offset, int32_t first_id )
+{
+    for( size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x )
+    {
+        float x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
+        float u = vel ? vel[3 * i] : 0.f, v = vel ? vel[3 * i + 1] : 0.f, w = vel ? vel[3 * i + 2] : 0.f;
+        if( space == 0 )
+        {
+            x = ( x - tr.x ) / sc.x; y = ( y - tr.y ) / sc.y; z = ( z - tr.z ) / sc.z;
+            u = u / sc.x; v = v / sc.y; w = w / sc.z;
+        }
+        const size_t o = offset + i;
+        p.px[o] = x; p.py[o] = y; p.pz[o] = z;
+        p.vx[o] = u; p.vy[o] = v; p.vz[o] = w;
+        p.id[o] = first_id + (int32_t)i;
+    }
+}
+
+}  // namespace
+
+void bora_launch_bin( const BoraGridDev& g, BoraParticlesDev p, size_t n, uint32_t* vkey, uint8_t* tile_flag, cudaStream_t st )
+{
+    if( n == 0 ) return;
+    k_bin<<<grid_for( n ), kThreads, 0, st>>>( g, p, n, vkey, tile_flag );
+}
+
+void bora_launch_activate( const BoraGridDev& g, const uint8_t* tile_flag, uint32_t* act, cudaStream_t st )
+{
+    const size_t ntv = (size_t)g.tx * g.ty * g.tz;
+    k_activate<<<grid_for( ntv ), kThreads, 0, st>>>( g, tile_flag, act );
+}
+
+void bora_launch_tile_assign( const BoraGridDev& g, const uint32_t* act, const uint32_t* excl, int32_t* slot_of,
+                              int32_t* tile_of, cudaStream_t st )
+{
+    const size_t ntv = (size_t)g.tx * g.ty * g.tz;
+    k_tile_assign<<<grid_for( ntv ), kThreads, 0, st>>>( ntv, act, excl, slot_of, tile_of );
+}
+
+void bora_launch_tile_nbrs( const BoraGridDev& g, int ntiles, const int32_t* slot_of, const int32_t* tile_of,
+                            int32_t* nbr, cudaStream_t st )
+{
+    if( ntiles <= 0 ) return;
+    k_tile_nbrs<<<grid_for( (size_t)ntiles * 27 ), kThreads, 0, st>>>( g, ntiles, slot_of, tile_of, nbr );
+}
+
+void bora_launch_hist( size_t n, const uint32_t* vkey, const int32_t* slot_of, uint32_t outside_key, uint32_t* key,
+                       uint32_t* count, uint32_t* err, cudaStream_t st )
+{
+    if( n == 0 ) return;
+    k_hist<<<grid_for( n ), kThreads, 0, st>>>( n, vkey, slot_of, outside_key, key, count, err );
+}
+
+void bora_launch_scatter( size_t n, const uint32_t* key, const uint32_t* start, uint32_t* count, uint32_t* idx,
+                          cudaStream_t st )
+{
+    if( n == 0 ) return;
+    k_scatter<<<grid_for( n ), kThreads, 0, st>>>( n, key, start, count, idx );
+}
+
+void bora_launch_to_soa( size_t n, const float* pos, const float* vel, int space, const float* translate,
+                         const float* scale, BoraParticlesDev p, size_t offset, int32_t first_id, cudaStream_t st )
+{
+    if( n == 0 ) return;
+    const float3 tr = make_float3( translate[0], translate[1], translate[2] );
+    const float3 sc = make_float3( scale[0], scale[1], scale[2] );
+    k_to_soa<<<grid_for( n ), kThreads, 0, st>>>( n, pos, vel, space, tr, sc, p, offset, first_id );
+}

@@ -1,0 +1,321 @@
+"""Python binding of the C ABI in include/bora_flip.h (ctypes, no torch types).
+
+`FlipSim` mirrors the reference's Bora::FLIPMethod (base/header/FLIPMethod.h:13-126):
+`initialize` is the constructor, `new_particles` batches FLIPMethod::newParticle,
+`advance_one_step` / `advance_one_frame` are advanceOneStep / advanceOneFrame, and the
+`field` / `tiles` accessors replace getVelocityField / getDensityField and the
+SparseFrame internals. Errors raise `BoraError` with the library's status code.
+
+The CUDA library must be built (vare_gb300.build.build()); there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_vp = ctypes.c_void_p
+
+BORA_OK = 0
+BORA_WARN_NOT_CONVERGED = 1
+SPACE_WORLD, SPACE_VOXEL = 0, 1
+SOLVER_PLAIN, SOLVER_MIXED = 0, 1
+STAGE_REBUILD, STAGE_P2G, STAGE_BUILD_SYSTEM, STAGE_SOLVE, STAGE_UPDATE_VELOCITY, STAGE_UPDATE_PARTICLES = range(6)
+FIELD_MASS, FIELD_SURF, FIELD_PRES, FIELD_VELO, FIELD_COMP, FIELD_FLAG, FIELD_RHS, FIELD_CODE = range(8)
+KERNEL_CLASSES = ["bin", "tiles", "sort", "p2g", "rhs", "pcg_direction", "pcg_update", "refine", "velocity", "g2p"]
+_FIELD_DTYPE = {FIELD_MASS: (np.float32, 1), FIELD_SURF: (np.float32, 1), FIELD_PRES: (np.float32, 1),
+                FIELD_VELO: (np.float32, 3), FIELD_COMP: (np.float32, 3), FIELD_FLAG: (np.uint8, 1),
+                FIELD_RHS: (np.float32, 1), FIELD_CODE: (np.uint16, 1)}
+
+
+class BoraError(RuntimeError):
+    def __init__(self, status: int, what: str):
+        self.status = status
+        super().__init__(f"{what}: status {status} ({status_string(status)})")
+
+
+class GridDesc(ctypes.Structure):
+    _fields_ = [("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int),
+                ("min", ctypes.c_float * 3), ("max", ctypes.c_float * 3)]
+
+
+class Params(ctypes.Structure):
+    _fields_ = [("ext_force", ctypes.c_float * 3), ("max_substeps", ctypes.c_int), ("dt", ctypes.c_float),
+                ("wall_level", ctypes.c_float), ("enable_water_tank", ctypes.c_int), ("enable_curl", ctypes.c_int),
+                ("damping_band", ctypes.c_float), ("voxel_size", ctypes.c_float), ("col_vel_scale", ctypes.c_float),
+                ("pts_per_cell", ctypes.c_int), ("vort_pres_rate", ctypes.c_float),
+                ("adjacency_under", ctypes.c_float), ("proj_iteration", ctypes.c_int),
+                ("redist_iteration", ctypes.c_int), ("solver", ctypes.c_int), ("tolerance", ctypes.c_double),
+                ("div_tolerance", ctypes.c_double), ("inner_tolerance", ctypes.c_double),
+                ("max_refinements", ctypes.c_int), ("check_every", ctypes.c_int)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("steps", ctypes.c_uint64), ("num_particles", ctypes.c_uint64), ("killed_last_step", ctypes.c_uint64),
+                ("active_tiles", ctypes.c_int32), ("fluid_cells", ctypes.c_int32),
+                ("solver_iterations", ctypes.c_int32), ("refinements", ctypes.c_int32),
+                ("residual_rel", ctypes.c_double), ("residual_max", ctypes.c_double),
+                ("residual_max_dx", ctypes.c_double), ("converged", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("stage_ms", ctypes.c_double * 8), ("gpu_ms", ctypes.c_double),
+                ("kernel_launches", ctypes.c_uint64)]
+
+    def as_dict(self) -> dict:
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k not in ("reserved", "stage_ms")}
+        d["stage_ms"] = list(self.stage_ms)
+        return d
+
+
+class FrameInfo(ctypes.Structure):
+    _fields_ = [("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int),
+                ("tx", ctypes.c_int), ("ty", ctypes.c_int), ("tz", ctypes.c_int), ("tile", ctypes.c_int),
+                ("active_tiles", ctypes.c_int), ("translate", ctypes.c_float * 3), ("scale", ctypes.c_float * 3),
+                ("voxel_wall_level", ctypes.c_float), ("voxel_gravity", ctypes.c_float * 3)]
+
+
+# name -> (restype, argtypes)
+_SIGS = {
+    "bora_flip_default_params": (ctypes.c_int, [ctypes.POINTER(Params)]),
+    "bora_flip_create": (ctypes.c_int, [ctypes.POINTER(GridDesc), ctypes.POINTER(Params), ctypes.POINTER(_vp)]),
+    "bora_flip_destroy": (ctypes.c_int, [_vp]),
+    "bora_flip_set_params": (ctypes.c_int, [_vp, ctypes.POINTER(Params)]),
+    "bora_flip_add_particles": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_size_t, ctypes.c_int]),
+    "bora_flip_set_particles": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_size_t, ctypes.c_int]),
+    "bora_flip_clear_particles": (ctypes.c_int, [_vp]),
+    "bora_flip_set_colliders": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_float]),
+    "bora_flip_step": (ctypes.c_int, [_vp, ctypes.c_float]),
+    "bora_flip_frame": (ctypes.c_int, [_vp]),
+    "bora_flip_run_stage": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_float]),
+    "bora_flip_num_particles": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_size_t)]),
+    "bora_flip_get_particles": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, ctypes.c_size_t,
+                                               ctypes.POINTER(ctypes.c_size_t), ctypes.c_int]),
+    "bora_flip_frame_info": (ctypes.c_int, [_vp, ctypes.POINTER(FrameInfo)]),
+    "bora_flip_get_tiles": (ctypes.c_int, [_vp, _vp, ctypes.c_size_t]),
+    "bora_flip_get_field": (ctypes.c_int, [_vp, ctypes.c_int, _vp, ctypes.c_size_t]),
+    "bora_flip_set_field": (ctypes.c_int, [_vp, ctypes.c_int, _vp, ctypes.c_size_t]),
+    "bora_flip_get_stats": (ctypes.c_int, [_vp, ctypes.POINTER(Stats)]),
+    "bora_flip_status_string": (ctypes.c_char_p, [ctypes.c_int]),
+    "bora_flip_set_profiling": (ctypes.c_int, [_vp, ctypes.c_uint32]),
+    "bora_flip_get_kernel_times": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int]),
+}
+
+_LIB: ctypes.CDLL | None = None
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load() -> ctypes.CDLL:
+    """Load the in-tree CUDA library; raises if it has not been built."""
+    global _LIB
+    if _LIB is None:
+        path = library_path()
+        if not os.path.exists(path):
+            raise RuntimeError(f"CUDA library {path} is missing: run vare_gb300.build.build() "
+                               "(this package has no CPU fallback)")
+        lib = ctypes.CDLL(path)
+        for name, (res, args) in _SIGS.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _LIB = lib
+    return _LIB
+
+
+def exported_symbols() -> list[str]:
+    return list(_SIGS)
+
+
+def status_string(status: int) -> str:
+    try:
+        return load().bora_flip_status_string(status).decode()
+    except Exception:  # pragma: no cover - only when the library is absent
+        return "?"
+
+
+def _check(status: int, what: str, allow_warn: bool = True) -> int:
+    if status < 0 or (status > 0 and not allow_warn):
+        raise BoraError(status, what)
+    return status
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    if isinstance(a, int):
+        return _vp(a)
+    return a.ctypes.data_as(_vp)
+
+
+def default_params(**overrides) -> Params:
+    p = Params()
+    _check(load().bora_flip_default_params(ctypes.byref(p)), "default_params")
+    for k, v in overrides.items():
+        if k == "ext_force":
+            p.ext_force = (ctypes.c_float * 3)(*v)
+        else:
+            setattr(p, k, v)
+    return p
+
+
+def scene_params(scene, **overrides) -> Params:
+    """Parameters of a generated scene (vare_gb300.scenes.Scene)."""
+    kw = dict(ext_force=scene.gravity, dt=scene.dt, wall_level=scene.wall_level, voxel_size=scene.voxel_size,
+              proj_iteration=10000)
+    kw.update(overrides)
+    return default_params(**kw)
+
+
+class FlipSim:
+    """One simulation on the current CUDA device (Bora::FLIPMethod over the C ABI)."""
+
+    def __init__(self, res, bmin, bmax, params: Params | None = None):
+        lib = load()
+        g = GridDesc()
+        g.nx, g.ny, g.nz = (int(v) for v in res)
+        g.min = (ctypes.c_float * 3)(*bmin)
+        g.max = (ctypes.c_float * 3)(*bmax)
+        h = _vp()
+        _check(lib.bora_flip_create(ctypes.byref(g), ctypes.byref(params) if params is not None else None,
+                                    ctypes.byref(h)), "bora_flip_create")
+        self.lib = lib
+        self.h = h
+        self.params = params
+
+    @classmethod
+    def from_scene(cls, scene, **overrides) -> "FlipSim":
+        sim = cls(scene.res, scene.bmin, scene.bmax, scene_params(scene, **overrides))
+        if scene.colliders:
+            sim.set_colliders(scene.colliders, scene.collider_band)
+        sim.set_particles(scene.pos, scene.vel, space=SPACE_VOXEL)
+        return sim
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.bora_flip_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_params(self, params: Params) -> None:
+        _check(self.lib.bora_flip_set_params(self.h, ctypes.byref(params)), "set_params")
+        self.params = params
+
+    def set_colliders(self, boxes, band: float) -> None:
+        arr = np.ascontiguousarray(np.array([np.concatenate([lo, hi, v]) for lo, hi, v in boxes],
+                                            np.float32).reshape(-1))
+        _check(self.lib.bora_flip_set_colliders(self.h, _ptr(arr), len(boxes), band), "set_colliders")
+
+    def add_particles(self, pos, vel=None, space: int = SPACE_WORLD) -> None:
+        pos = np.ascontiguousarray(pos, np.float32)
+        vel = None if vel is None else np.ascontiguousarray(vel, np.float32)
+        _check(self.lib.bora_flip_add_particles(self.h, _ptr(pos), _ptr(vel), pos.shape[0], space), "add_particles")
+
+    def set_particles(self, pos, vel=None, space: int = SPACE_WORLD) -> None:
+        pos = np.ascontiguousarray(pos, np.float32)
+        vel = None if vel is None else np.ascontiguousarray(vel, np.float32)
+        _check(self.lib.bora_flip_set_particles(self.h, _ptr(pos), _ptr(vel), pos.shape[0], space), "set_particles")
+
+    def set_particles_ptr(self, pos_ptr: int, vel_ptr: int, n: int, space: int = SPACE_VOXEL) -> None:
+        """Replace particles from raw host pointers (e.g. pinned torch buffers)."""
+        _check(self.lib.bora_flip_set_particles(self.h, _vp(pos_ptr), _vp(vel_ptr), n, space), "set_particles")
+
+    def step(self, dt: float) -> int:
+        return _check(self.lib.bora_flip_step(self.h, dt), "bora_flip_step")
+
+    advance_one_step = step
+
+    def advance_one_frame(self) -> int:
+        return _check(self.lib.bora_flip_frame(self.h), "bora_flip_frame")
+
+    def run_stage(self, stage: int, dt: float = 0.0) -> int:
+        return _check(self.lib.bora_flip_run_stage(self.h, stage, dt), f"run_stage({stage})")
+
+    @property
+    def num_particles(self) -> int:
+        n = ctypes.c_size_t()
+        _check(self.lib.bora_flip_num_particles(self.h, ctypes.byref(n)), "num_particles")
+        return int(n.value)
+
+    def particles(self, space: int = SPACE_VOXEL):
+        n = self.num_particles
+        pos = np.zeros((n, 3), np.float32)
+        vel = np.zeros((n, 3), np.float32)
+        adj = np.zeros(n, np.float32)
+        ids = np.zeros(n, np.int32)
+        out = ctypes.c_size_t()
+        _check(self.lib.bora_flip_get_particles(self.h, _ptr(pos), _ptr(vel), _ptr(adj), _ptr(ids), n,
+                                                ctypes.byref(out), space), "get_particles")
+        return pos, vel, adj, ids
+
+    def get_particles_ptr(self, pos_ptr: int, vel_ptr: int, cap: int, space: int = SPACE_VOXEL) -> int:
+        out = ctypes.c_size_t()
+        _check(self.lib.bora_flip_get_particles(self.h, _vp(pos_ptr), _vp(vel_ptr), None, None, cap,
+                                                ctypes.byref(out), space), "get_particles")
+        return int(out.value)
+
+    def frame_info(self) -> dict:
+        f = FrameInfo()
+        _check(self.lib.bora_flip_frame_info(self.h, ctypes.byref(f)), "frame_info")
+        return dict(nx=f.nx, ny=f.ny, nz=f.nz, tx=f.tx, ty=f.ty, tz=f.tz, tile=f.tile, ntiles=f.active_tiles,
+                    translate=np.array(f.translate[:], np.float32), scale=np.array(f.scale[:], np.float32),
+                    voxel_wall=f.voxel_wall_level, voxel_gravity=np.array(f.voxel_gravity[:], np.float32))
+
+    def tiles(self) -> np.ndarray:
+        n = self.frame_info()["ntiles"]
+        out = np.zeros((n, 3), np.int32)
+        _check(self.lib.bora_flip_get_tiles(self.h, _ptr(out), n), "get_tiles")
+        return out.astype(np.int64)
+
+    def field(self, which: int) -> np.ndarray:
+        n = self.frame_info()["ntiles"] * 512
+        dt, nc = _FIELD_DTYPE[which]
+        out = np.zeros((n, 3) if nc == 3 else n, dt)
+        _check(self.lib.bora_flip_get_field(self.h, which, _ptr(out), out.nbytes), "get_field")
+        return out
+
+    def set_field(self, which: int, data: np.ndarray) -> None:
+        dt, nc = _FIELD_DTYPE[which]
+        data = np.ascontiguousarray(data, dt)
+        _check(self.lib.bora_flip_set_field(self.h, which, _ptr(data), data.nbytes), "set_field")
+
+    def stats(self) -> dict:
+        s = Stats()
+        _check(self.lib.bora_flip_get_stats(self.h, ctypes.byref(s)), "get_stats")
+        return s.as_dict()
+
+    def set_profiling(self, class_mask: int) -> None:
+        _check(self.lib.bora_flip_set_profiling(self.h, class_mask), "set_profiling")
+
+    def kernel_times(self):
+        ms = np.zeros(16, np.float64)
+        n = np.zeros(16, np.uint64)
+        _check(self.lib.bora_flip_get_kernel_times(self.h, _ptr(ms), _ptr(n), 16), "get_kernel_times")
+        return ms, n
+
+    def dense(self, which: int, background=0.0) -> np.ndarray:
+        """Field scattered to a dense (nz, ny, nx[, 3]) array; inactive cells = background."""
+        fi = self.frame_info()
+        f = self.field(which)
+        t = self.tiles()
+        vec = f.ndim == 2
+        shape = (fi["tz"] * 8, fi["ty"] * 8, fi["tx"] * 8) + ((3,) if vec else ())
+        out = np.full(shape, background, dtype=f.dtype)
+        if len(t):
+            blk = f.reshape((len(t), 8, 8, 8) + ((3,) if vec else ()))
+            for n, (i, j, k) in enumerate(t):
+                out[k * 8:(k + 1) * 8, j * 8:(j + 1) * 8, i * 8:(i + 1) * 8] = blk[n]
+        return out[:fi["nz"], :fi["ny"], :fi["nx"]]
