@@ -53,23 +53,36 @@ def colliders_for(n):
             ((n * 0.8, n * 0.1, -1.0), (n * 0.95, n * 0.2, n * 0.4), (-3.0, 1.0, 0.0))]
 
 
+def moving(sc, oracle_lib, steps: int = 1):
+    """The scene after `steps` oracle steps from rest, as a new scene (ids renumbered in
+    id order): from rest the first pressure solve is trivial (b = 0), so stage tests
+    start from a moving state to exercise the solver."""
+    ora = oracle_lib.Oracle(sc, block=8, solver="fp64", tol=1e-13, threads=1)
+    for _ in range(steps):
+        ora.step(sc.dt)
+    pos, vel, _, ids = ora.particles()
+    o = np.argsort(ids)
+    import dataclasses
+    return dataclasses.replace(sc, pos=np.ascontiguousarray(pos[o]), vel=np.ascontiguousarray(vel[o]))
+
+
 @pytest.fixture(params=["dam_sphere_24", "colliders_20", "padded_22", "slab_24x16x40"])
-def scene(request):
+def scene(request, oracle_lib):
     name = request.param
     if name == "dam_sphere_24":
-        return scenes.small(24)
-    if name == "colliders_20":
+        sc = scenes.small(24)
+    elif name == "colliders_20":
         sc = scenes.small(20, dt=1.0 / 60.0)
         sc.colliders = colliders_for(20)
-        return sc
-    if name == "padded_22":
-        return scenes.small(22)
-    sc = scenes.small(16)
-    sc.res = (24, 16, 40)
-    sc.bmax = (1.0, 16 / 24, 40 / 24)
-    sc.pos = sc.pos[(sc.pos[:, 0] < 24) & (sc.pos[:, 1] < 16)]
-    sc.vel = np.zeros_like(sc.pos)
-    return sc
+    elif name == "padded_22":
+        sc = scenes.small(22)
+    else:
+        sc = scenes.small(16)
+        sc.res = (24, 16, 40)
+        sc.bmax = (1.0, 16 / 24, 40 / 24)
+        sc.pos = sc.pos[(sc.pos[:, 0] < 24) & (sc.pos[:, 1] < 16)]
+        sc.vel = np.zeros_like(sc.pos)
+    return moving(sc, oracle_lib, 2)
 
 
 def _pair(gpu, oracle_lib, sc, **kw):
@@ -156,18 +169,21 @@ def test_solve_matches_fp64_oracle(gpu, oracle_lib, scene):
     sim.set_field(gpu.FIELD_VELO, ora.field(B.FIELD_VELO))
     sim.run_stage(gpu.STAGE_BUILD_SYSTEM)
     ora.build_system()
+    assert np.abs(ora.system()["b"]).max() > 0, "trivial right-hand side"
     status = sim.run_stage(gpu.STAGE_SOLVE)
     st = sim.stats()
     assert status == 0 and st["converged"] == 1, st
+    assert st["solver_iterations"] > 0
     assert st["residual_rel"] <= 1e-10
     ora.solve()
     sysm = ora.system()
     p_gpu = sim.field(gpu.FIELD_PRES)[sysm["cells"]]
     assert rel_err(p_gpu, sysm["x"]) <= TOL
-    # the device's own residual report agrees with the oracle's FP64 residual of its answer
+    # the oracle's FP64 residual of the device answer (rounded to float32, which adds up
+    # to ~12 ulp(p) per row) agrees with the device's own FP64 residual report
     ora.set_solution(p_gpu)
     rmax = ora.residual_max()
-    assert rmax <= max(10 * st["residual_max"], 1e-6 * np.abs(sysm["b"]).max())
+    assert rmax <= 10 * st["residual_max"] + 16 * float(np.abs(sysm["x"]).max()) * 2.0 ** -24
 
 
 def test_full_step_matches_oracle(gpu, oracle_lib, scene):
@@ -197,6 +213,15 @@ def test_step_matches_reference_golden(gpu):
     assert rel_err(pos, g["pos0"][o]) <= TOL
     assert rel_err(vel, g["vel0"][o]) <= TOL
     np.testing.assert_array_equal(adj, g["adj0"][o])
+    # two more steps: chaotic amplification stays small over three steps
+    sim.step(sc.dt)
+    sim.step(sc.dt)
+    pos, vel, adj, ids = by_id(*sim.particles())
+    ref_ids = g["ids2"]
+    o = np.argsort(ref_ids)
+    np.testing.assert_array_equal(ids, ref_ids[o])
+    assert rel_err(pos, g["pos2"][o]) <= TOL
+    assert rel_err(vel, g["vel2"][o]) <= 1e-4
 
 
 def test_deterministic(gpu):

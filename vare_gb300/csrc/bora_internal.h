@@ -55,6 +55,7 @@ struct BoraReduceDev
     double* ring;        // [BORA_RING * 4]: slot values
     double* partials;    // [max blocks * 2]
     uint32_t* done;      // [BORA_RING] block-arrival counters
+    uint32_t* err;       // set non-zero by a kernel that met an inconsistent stencil code
 };
 
 // ---- launchers -----------------------------------------------------------------------
@@ -109,4 +110,3 @@ void bora_launch_refine_residual( const BoraGridDev& g, int ntiles, BoraTilesDev
 // pres = (float) x on fluid cells, 0 elsewhere
 void bora_launch_write_pressure( int ntiles, const uint16_t* code, const double* x, float* pres, cudaStream_t st );
 
-size_t bora_reduce_max_blocks();

@@ -176,7 +176,10 @@ struct bora_flip_sim
         s.minv = P<float>( sminv );
         return s;
     }
-    BoraReduceDev reducer() { return BoraReduceDev{ P<double>( ring ), P<double>( partials ), P<uint32_t>( done ) }; }
+    BoraReduceDev reducer()
+    {
+        return BoraReduceDev{ P<double>( ring ), P<double>( partials ), P<uint32_t>( done ), P<uint32_t>( counters ) + 5 };
+    }
     int slot()
     {
         const int s = next_slot;
@@ -425,6 +428,7 @@ int stage_solve( bora_flip_sim* s )
     int status = BORA_OK;
     const double dx = s->scale[0];
 
+    BORA_TRY( cudaMemsetAsync( P<uint32_t>( s->counters ) + 5, 0, 4, st ) );
     const int s_b2 = s->slot(), s_bmax = s->slot();
     { KTimer t( s, BORA_KERNEL_REFINE, 1 ); bora_launch_solve_init( s->ntiles, b, code, sv, red, s_b2, s_bmax, st ); }
     BORA_TRYS( check_launch( s ) );
@@ -483,6 +487,8 @@ int stage_solve( bora_flip_sim* s )
     }
     { KTimer t( s, BORA_KERNEL_REFINE, 1 ); bora_launch_write_pressure( s->ntiles, code, sv.x, P<float>( s->pres ), st ); }
     BORA_TRYS( check_launch( s ) );
+    BORA_TRYS( read_counters( s, 5, 1 ) );
+    if( s->h_cnt[5] != 0 ) return BORA_ERR_INTERNAL;
     s->stats.solver_iterations = total_it;
     s->stats.refinements = passes;
     s->stats.residual_rel = bnorm > 0.0 ? rnorm / bnorm : 0.0;

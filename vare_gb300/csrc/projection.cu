@@ -9,6 +9,8 @@
 // (float values + size_t columns, 84 B per row) after a serial host relabel of the
 // fluid cells; here the operator is applied from a 16-bit per-cell stencil code
 // (neighbour-is-fluid mask + integer diagonal), which encodes the same matrix.
+#include <algorithm>
+
 #include "bora_internal.h"
 
 namespace {
@@ -116,6 +118,49 @@ __global__ void __launch_bounds__( 512 ) k_rhs( BoraGridDev g, BoraTilesDev t, B
 }
 
 // ---------------------------------------------------------------------------------
+// Double-float accumulation: GB300's FP64 pipe is ~1/64 of its FP32 rate, so per-cell
+// dot-product terms are accumulated as unevaluated float pairs (hi + lo) with the
+// error-free TwoProd (fmaf) and TwoSum transformations (Dekker 1971, Knuth TAOCP 4.2.2),
+// giving ~48 significant bits from FP32 instructions; each warp converts its pair to
+// FP64 once. This relies on -fmad=false (no contraction inside TwoSum).
+struct DF
+{
+    float hi, lo;
+};
+__device__ inline DF df_prod( float a, float b )
+{
+    const float p = a * b;
+    return DF{ p, fmaf( a, b, -p ) };
+}
+__device__ inline DF df_add( DF a, DF b )
+{
+    const float s = a.hi + b.hi;
+    const float bb = s - a.hi;
+    float err = ( a.hi - ( s - bb ) ) + ( b.hi - bb );
+    err += a.lo + b.lo;
+    const float h = s + err;
+    return DF{ h, err - ( h - s ) };
+}
+__device__ inline double df_warp_sum( DF v )
+{
+#pragma unroll
+    for( int o = 16; o > 0; o >>= 1 )
+    {
+        DF w;
+        w.hi = __shfl_xor_sync( 0xffffffffu, v.hi, o );
+        w.lo = __shfl_xor_sync( 0xffffffffu, v.lo, o );
+        v = df_add( v, w );
+    }
+    return (double)v.hi + (double)v.lo;
+}
+__device__ inline float warp_maxf( float v )
+{
+#pragma unroll
+    for( int o = 16; o > 0; o >>= 1 ) v = fmaxf( v, __shfl_xor_sync( 0xffffffffu, v, o ) );
+    return v;
+}
+
+// ---------------------------------------------------------------------------------
 // Deterministic FP64 block reduction published through a ring slot: every block writes
 // its partial, the last block to arrive sums the partials in block order.
 __device__ inline double warp_sum( double v )
@@ -131,14 +176,13 @@ __device__ inline double warp_max( double v )
     return v;
 }
 
-// op1: 0 = sum, 1 = max for the second value. Slots < 0 are skipped.
-__device__ void reduce2_publish( double v0, double v1, int op1, BoraReduceDev red, int slot0, int slot1 )
+// op1: 0 = sum, 1 = max for the second value. Slots < 0 are skipped. Inputs are the
+// per-warp totals (already reduced across the warp, valid in every lane).
+__device__ void reduce2_publish_warp( double v0, double v1, int op1, BoraReduceDev red, int slot0, int slot1 )
 {
     __shared__ double w0[32], w1[32];
     __shared__ bool last;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = ( blockDim.x + 31 ) >> 5;
-    v0 = warp_sum( v0 );
-    v1 = op1 ? warp_max( v1 ) : warp_sum( v1 );
     if( lane == 0 ) { w0[wid] = v0; w1[wid] = v1; }
     __syncthreads();
     if( threadIdx.x == 0 )
@@ -155,33 +199,53 @@ __device__ void reduce2_publish( double v0, double v1, int op1, BoraReduceDev re
     __syncthreads();
     if( !last ) return;
     __threadfence();
+    // All threads of the last block: thread-strided partial sums in a fixed order
+    // (independent loads, unrolled so that many are in flight), then a fixed-shape tree.
     double a = 0.0, b = 0.0;
-    if( wid == 0 )
+    const unsigned nb = gridDim.x, stride = blockDim.x;
+#pragma unroll 4
+    for( unsigned q = threadIdx.x; q < nb; q += stride )
     {
-        // lane-strided partial sums in fixed order, then a fixed-shape warp tree
-        for( unsigned q = lane; q < gridDim.x; q += 32 )
-        {
-            a += __ldcg( &red.partials[2 * (size_t)q] );
-            const double pb = __ldcg( &red.partials[2 * (size_t)q + 1] );
-            b = op1 ? fmax( b, pb ) : b + pb;
-        }
-        a = warp_sum( a );
-        b = op1 ? warp_max( b ) : warp_sum( b );
-        if( lane == 0 )
-        {
-            if( slot0 >= 0 ) red.ring[slot0] = a;
-            if( slot1 >= 0 ) red.ring[slot1] = b;
-            const int key = slot0 >= 0 ? slot0 : slot1;
-            red.done[key % BORA_RING] = 0;
-            __threadfence();
-        }
+        const double2 pq = __ldcg( reinterpret_cast<const double2*>( red.partials ) + q );
+        a += pq.x;
+        b = op1 ? fmax( b, pq.y ) : b + pq.y;
+    }
+    a = warp_sum( a );
+    b = op1 ? warp_max( b ) : warp_sum( b );
+    if( lane == 0 ) { w0[wid] = a; w1[wid] = b; }
+    __syncthreads();
+    if( threadIdx.x == 0 )
+    {
+        double ta = 0.0, tb = 0.0;
+        for( int q = 0; q < nw; ++q ) { ta += w0[q]; tb = op1 ? fmax( tb, w1[q] ) : tb + w1[q]; }
+        if( slot0 >= 0 ) red.ring[slot0] = ta;
+        if( slot1 >= 0 ) red.ring[slot1] = tb;
+        const int key = slot0 >= 0 ? slot0 : slot1;
+        red.done[key % BORA_RING] = 0;
+        __threadfence();
     }
 }
 
+// Per-thread double-float sums (op1 = 0) or a float max in v1 (op1 = 1).
+__device__ inline void reduce2_publish_df( DF v0, DF v1, BoraReduceDev red, int slot0, int slot1 )
+{
+    const double a = df_warp_sum( v0 );
+    const double b = df_warp_sum( v1 );
+    reduce2_publish_warp( a, b, 0, red, slot0, slot1 );
+}
+__device__ inline void reduce2_publish_dfmax( DF v0, float vmax, BoraReduceDev red, int slot0, int slot1 )
+{
+    const double a = df_warp_sum( v0 );
+    const double b = (double)warp_maxf( vmax );
+    reduce2_publish_warp( a, b, 1, red, slot0, slot1 );
+}
+
 // ---------------------------------------------------------------------------------
-// Wavefront tables of an 8^3 tile: cells ordered by plane i+j+k (0..21).
-__constant__ uint16_t c_plane_cells[512];
-__constant__ uint16_t c_plane_start[23];
+// Wavefront tables of an 8^3 tile: cells ordered by plane i+j+k (0..21). Kept in global
+// memory and copied to shared memory by every CTA that sweeps planes (lanes of a warp
+// read different entries, which a constant-memory table would serialise).
+__device__ uint16_t g_plane_cells[512];
+__device__ uint16_t g_plane_start[23];
 
 struct PlaneTables
 {
@@ -204,6 +268,7 @@ struct PlaneTables
 };
 
 bool g_tables_ready[64] = { false };
+int g_num_sms[64] = { 0 };
 
 void ensure_tables()
 {
@@ -211,15 +276,34 @@ void ensure_tables()
     cudaGetDevice( &dev );
     if( dev < 0 || dev >= 64 || g_tables_ready[dev] ) return;
     static const PlaneTables tbl;
-    cudaMemcpyToSymbol( c_plane_cells, tbl.cells, sizeof( tbl.cells ) );
-    cudaMemcpyToSymbol( c_plane_start, tbl.start, sizeof( tbl.start ) );
+    cudaMemcpyToSymbol( g_plane_cells, tbl.cells, sizeof( tbl.cells ) );
+    cudaMemcpyToSymbol( g_plane_start, tbl.start, sizeof( tbl.start ) );
     g_tables_ready[dev] = true;
+}
+
+int num_sms()
+{
+    int dev = 0;
+    cudaGetDevice( &dev );
+    if( dev >= 0 && dev < 64 && g_num_sms[dev] > 0 ) return g_num_sms[dev];
+    int n = 0;
+    cudaDeviceGetAttribute( &n, cudaDevAttrMultiProcessorCount, dev );
+    if( n <= 0 ) n = 152;
+    if( dev >= 0 && dev < 64 ) g_num_sms[dev] = n;
+    return n;
+}
+
+__device__ inline void load_plane_tables( uint16_t* pc, uint16_t* ps )
+{
+    for( int q = threadIdx.x; q < 512; q += blockDim.x ) pc[q] = g_plane_cells[q];
+    if( threadIdx.x < 23 ) ps[threadIdx.x] = g_plane_start[threadIdx.x];
 }
 
 __device__ inline int code_diag( uint16_t c ) { return ( c >> 8 ) & 15; }
 
 // Block-MIC(0) pivots (MIC(0) of BLAS.cu:211-262 with tau = 0.97, restricted to the
-// couplings inside each 8^3 tile so that tiles factor independently). One warp per tile.
+// couplings inside each 8^3 tile so that tiles factor independently). One warp per
+// tile, persistent over tiles.
 constexpr int kTilesPerCta = 4;
 
 __global__ void __launch_bounds__( 32 * kTilesPerCta ) k_mic_factor( int ntiles, const uint16_t* __restrict__ code,
@@ -227,82 +311,93 @@ __global__ void __launch_bounds__( 32 * kTilesPerCta ) k_mic_factor( int ntiles,
 {
     __shared__ float sm[kTilesPerCta][512];
     __shared__ uint16_t sc[kTilesPerCta][512];
+    __shared__ uint16_t pc[512], ps[23];
+    load_plane_tables( pc, ps );
+    __syncthreads();
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int s = blockIdx.x * kTilesPerCta + w;
-    if( s >= ntiles ) return;
-    const size_t base = (size_t)s * 512;
-    for( int l = lane; l < 512; l += 32 ) { sc[w][l] = code[base + l]; sm[w][l] = 0.f; }
-    __syncwarp();
     const float tau = 0.97f;
-    for( int p = 0; p <= 21; ++p )
+    for( int s = blockIdx.x * kTilesPerCta + w; s < ntiles; s += gridDim.x * kTilesPerCta )
     {
-        for( int q = c_plane_start[p] + lane; q < c_plane_start[p + 1]; q += 32 )
+        const size_t base = (size_t)s * 512;
+        for( int l = lane; l < 512; l += 32 ) { sc[w][l] = code[base + l]; sm[w][l] = 0.f; }
+        __syncwarp();
+        for( int p = 0; p <= 21; ++p )
         {
-            const int l = c_plane_cells[q];
-            const uint16_t cc = sc[w][l];
-            if( !( cc & BORA_CODE_FLUID ) ) continue;
-            const int li = l & 7, lj = ( l >> 3 ) & 7, lk = l >> 6;
-            const float diag = (float)code_diag( cc );
-            float e = diag, e2 = 0.f;
-            if( li > 0 && ( cc & 1u ) )
+            for( int q = ps[p] + lane; q < ps[p + 1]; q += 32 )
             {
-                const int m = l - 1;
-                const uint16_t cm = sc[w][m];
-                const float M = sm[w][m];
-                const float a = ( lj < 7 && ( cm & 8u ) ) ? 1.f : 0.f;    // m+y inside the tile and fluid
-                const float b = ( lk < 7 && ( cm & 32u ) ) ? 1.f : 0.f;   // m+z
-                e -= M * M;
-                e2 += ( a + b ) * ( M * M );
+                const int l = pc[q];
+                const uint16_t cc = sc[w][l];
+                if( !( cc & BORA_CODE_FLUID ) ) continue;
+                const int li = l & 7, lj = ( l >> 3 ) & 7, lk = l >> 6;
+                const float diag = (float)code_diag( cc );
+                float e = diag, e2 = 0.f;
+                if( li > 0 && ( cc & 1u ) )
+                {
+                    const int m = l - 1;
+                    const uint16_t cm = sc[w][m];
+                    const float M = sm[w][m];
+                    const float a = ( lj < 7 && ( cm & 8u ) ) ? 1.f : 0.f;    // m+y inside the tile and fluid
+                    const float b = ( lk < 7 && ( cm & 32u ) ) ? 1.f : 0.f;   // m+z
+                    e -= M * M;
+                    e2 += ( a + b ) * ( M * M );
+                }
+                if( lj > 0 && ( cc & 4u ) )
+                {
+                    const int m = l - 8;
+                    const uint16_t cm = sc[w][m];
+                    const float M = sm[w][m];
+                    const float a = ( li < 7 && ( cm & 2u ) ) ? 1.f : 0.f;    // m+x
+                    const float b = ( lk < 7 && ( cm & 32u ) ) ? 1.f : 0.f;   // m+z
+                    e -= M * M;
+                    e2 += ( a + b ) * ( M * M );
+                }
+                if( lk > 0 && ( cc & 16u ) )
+                {
+                    const int m = l - 64;
+                    const uint16_t cm = sc[w][m];
+                    const float M = sm[w][m];
+                    const float a = ( li < 7 && ( cm & 2u ) ) ? 1.f : 0.f;    // m+x
+                    const float b = ( lj < 7 && ( cm & 8u ) ) ? 1.f : 0.f;    // m+y
+                    e -= M * M;
+                    e2 += ( a + b ) * ( M * M );
+                }
+                e -= tau * e2;
+                if( e < diag * 0.25f ) e = diag;
+                sm[w][l] = 1.f / sqrtf( e + 1e-30f );
             }
-            if( lj > 0 && ( cc & 4u ) )
-            {
-                const int m = l - 8;
-                const uint16_t cm = sc[w][m];
-                const float M = sm[w][m];
-                const float a = ( li < 7 && ( cm & 2u ) ) ? 1.f : 0.f;    // m+x
-                const float b = ( lk < 7 && ( cm & 32u ) ) ? 1.f : 0.f;   // m+z
-                e -= M * M;
-                e2 += ( a + b ) * ( M * M );
-            }
-            if( lk > 0 && ( cc & 16u ) )
-            {
-                const int m = l - 64;
-                const uint16_t cm = sc[w][m];
-                const float M = sm[w][m];
-                const float a = ( li < 7 && ( cm & 2u ) ) ? 1.f : 0.f;    // m+x
-                const float b = ( lj < 7 && ( cm & 8u ) ) ? 1.f : 0.f;    // m+y
-                e -= M * M;
-                e2 += ( a + b ) * ( M * M );
-            }
-            e -= tau * e2;
-            if( e < diag * 0.25f ) e = diag;
-            sm[w][l] = 1.f / sqrtf( e + 1e-30f );
+            __syncwarp();
         }
+        for( int l = lane; l < 512; l += 32 ) minv[base + l] = sm[w][l];
         __syncwarp();
     }
-    for( int l = lane; l < 512; l += 32 ) minv[base + l] = sm[w][l];
 }
 
 // ---------------------------------------------------------------------------------
 // PCG update: e += alpha d; r -= alpha q; z = M^-1 r (block-MIC(0) forward and backward
-// sweeps in shared memory); rz = r.z and rr = r.r in FP64. One warp per tile.
+// sweeps in shared memory); rz = r.z and rr = r.r, FP64-accurate. One warp per tile,
+// persistent over tiles; alpha is formed once per CTA.
 __global__ void __launch_bounds__( 32 * kTilesPerCta ) k_pcg_update( int ntiles, const uint16_t* __restrict__ code,
                                                                      BoraSolverDev sv, int dsel, BoraReduceDev red,
                                                                      int slot_rz_in, int slot_dq_in, int slot_rz_out,
                                                                      int slot_rr_out )
 {
-    __shared__ float sr[kTilesPerCta][512];
-    __shared__ float sy[kTilesPerCta][512];
-    __shared__ float sm[kTilesPerCta][512];
-    __shared__ uint16_t sc[kTilesPerCta][512];
+    // vector (16-byte / 8-byte) shared-memory accesses below need explicit alignment
+    __shared__ __align__( 16 ) float sr[kTilesPerCta][512];
+    __shared__ __align__( 16 ) float sy[kTilesPerCta][512];
+    __shared__ __align__( 16 ) float sm[kTilesPerCta][512];
+    __shared__ __align__( 16 ) uint16_t sc[kTilesPerCta][512];
+    __shared__ uint16_t pc[512], ps[23];
+    __shared__ float s_alpha;
+    load_plane_tables( pc, ps );
+    if( threadIdx.x == 0 ) s_alpha = slot_rz_in < 0 ? 0.f : (float)( red.ring[slot_rz_in] / red.ring[slot_dq_in] );
+    __syncthreads();
+    const float alpha = s_alpha;
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int s = blockIdx.x * kTilesPerCta + w;
-    double prz = 0.0, prr = 0.0;
-    const float alpha = slot_rz_in < 0 ? 0.f : (float)( red.ring[slot_rz_in] / red.ring[slot_dq_in] );
-    if( s < ntiles )
+    DF prz{ 0.f, 0.f }, prr{ 0.f, 0.f };
+    const float* dvec = sv.d[dsel];
+    for( int s = blockIdx.x * kTilesPerCta + w; s < ntiles; s += gridDim.x * kTilesPerCta )
     {
         const size_t base = (size_t)s * 512;
-        const float* dvec = sv.d[dsel];
         for( int l4 = lane; l4 < 128; l4 += 32 )
         {
             const size_t o = base + 4 * (size_t)l4;
@@ -310,23 +405,23 @@ __global__ void __launch_bounds__( 32 * kTilesPerCta ) k_pcg_update( int ntiles,
             float4 r = *reinterpret_cast<const float4*>( sv.r + o );
             const float4 d = *reinterpret_cast<const float4*>( dvec + o );
             const float4 q = *reinterpret_cast<const float4*>( sv.q + o );
+            const float4 mv = *reinterpret_cast<const float4*>( sv.minv + o );
+            const ushort4 cv = *reinterpret_cast<const ushort4*>( code + o );
             e.x = fmaf( alpha, d.x, e.x ); e.y = fmaf( alpha, d.y, e.y ); e.z = fmaf( alpha, d.z, e.z ); e.w = fmaf( alpha, d.w, e.w );
             r.x = fmaf( -alpha, q.x, r.x ); r.y = fmaf( -alpha, q.y, r.y ); r.z = fmaf( -alpha, q.z, r.z ); r.w = fmaf( -alpha, q.w, r.w );
             *reinterpret_cast<float4*>( sv.e + o ) = e;
             *reinterpret_cast<float4*>( sv.r + o ) = r;
-            sr[w][4 * l4] = r.x; sr[w][4 * l4 + 1] = r.y; sr[w][4 * l4 + 2] = r.z; sr[w][4 * l4 + 3] = r.w;
-            const float4 mv = *reinterpret_cast<const float4*>( sv.minv + o );
-            sm[w][4 * l4] = mv.x; sm[w][4 * l4 + 1] = mv.y; sm[w][4 * l4 + 2] = mv.z; sm[w][4 * l4 + 3] = mv.w;
-            const ushort4 cv = *reinterpret_cast<const ushort4*>( code + o );
-            sc[w][4 * l4] = cv.x; sc[w][4 * l4 + 1] = cv.y; sc[w][4 * l4 + 2] = cv.z; sc[w][4 * l4 + 3] = cv.w;
+            *reinterpret_cast<float4*>( &sr[w][4 * l4] ) = r;
+            *reinterpret_cast<float4*>( &sm[w][4 * l4] ) = mv;
+            *reinterpret_cast<ushort4*>( &sc[w][4 * l4] ) = cv;
         }
         __syncwarp();
         // forward: y_c = (r_c + sum_{lower m} M_m y_m) M_c   (A_mc = -1)
         for( int p = 0; p <= 21; ++p )
         {
-            for( int q = c_plane_start[p] + lane; q < c_plane_start[p + 1]; q += 32 )
+            for( int q = ps[p] + lane; q < ps[p + 1]; q += 32 )
             {
-                const int l = c_plane_cells[q];
+                const int l = pc[q];
                 const uint16_t cc = sc[w][l];
                 float y = 0.f;
                 if( cc & BORA_CODE_FLUID )
@@ -344,9 +439,9 @@ __global__ void __launch_bounds__( 32 * kTilesPerCta ) k_pcg_update( int ntiles,
         // backward: z_c = (y_c + M_c sum_{upper u} z_u) M_c ; z overwrites sy in place
         for( int p = 21; p >= 0; --p )
         {
-            for( int q = c_plane_start[p] + lane; q < c_plane_start[p + 1]; q += 32 )
+            for( int q = ps[p] + lane; q < ps[p + 1]; q += 32 )
             {
-                const int l = c_plane_cells[q];
+                const int l = pc[q];
                 const uint16_t cc = sc[w][l];
                 if( cc & BORA_CODE_FLUID )
                 {
@@ -363,73 +458,92 @@ __global__ void __launch_bounds__( 32 * kTilesPerCta ) k_pcg_update( int ntiles,
         for( int l4 = lane; l4 < 128; l4 += 32 )
         {
             const size_t o = base + 4 * (size_t)l4;
-            const float4 z = make_float4( sy[w][4 * l4], sy[w][4 * l4 + 1], sy[w][4 * l4 + 2], sy[w][4 * l4 + 3] );
+            const float4 z = *reinterpret_cast<const float4*>( &sy[w][4 * l4] );
+            const float4 r = *reinterpret_cast<const float4*>( &sr[w][4 * l4] );
             *reinterpret_cast<float4*>( sv.z + o ) = z;
-            const float r0 = sr[w][4 * l4], r1 = sr[w][4 * l4 + 1], r2 = sr[w][4 * l4 + 2], r3 = sr[w][4 * l4 + 3];
-            prz += (double)r0 * z.x + (double)r1 * z.y + (double)r2 * z.z + (double)r3 * z.w;
-            prr += (double)r0 * r0 + (double)r1 * r1 + (double)r2 * r2 + (double)r3 * r3;
+            prz = df_add( prz, df_prod( r.x, z.x ) ); prz = df_add( prz, df_prod( r.y, z.y ) );
+            prz = df_add( prz, df_prod( r.z, z.z ) ); prz = df_add( prz, df_prod( r.w, z.w ) );
+            prr = df_add( prr, df_prod( r.x, r.x ) ); prr = df_add( prr, df_prod( r.y, r.y ) );
+            prr = df_add( prr, df_prod( r.z, r.z ) ); prr = df_add( prr, df_prod( r.w, r.w ) );
         }
+        __syncwarp();
     }
-    reduce2_publish( prz, prr, 0, red, slot_rz_out, slot_rr_out );
+    reduce2_publish_df( prz, prr, red, slot_rz_out, slot_rr_out );
+}
+
+// Global index of the face neighbour of cell (slot s, local l) in direction q
+// (0:-x 1:+x 2:-y 3:+y 4:-z 5:+z), or SIZE_MAX when the neighbour tile is not active
+// (a stencil code that names a fluid neighbour there is inconsistent; callers record
+// it and skip the access).
+__device__ inline size_t face_nbr( const int32_t* __restrict__ nbr, size_t cell, int s, int l, int q )
+{
+    const int li = l & 7, lj = ( l >> 3 ) & 7, lk = l >> 6;
+    int dir, ll;
+    switch( q )
+    {
+        case 0: if( li > 0 ) return cell - 1; dir = 12; ll = l + 7; break;
+        case 1: if( li < 7 ) return cell + 1; dir = 14; ll = l - 7; break;
+        case 2: if( lj > 0 ) return cell - 8; dir = 10; ll = l + 56; break;
+        case 3: if( lj < 7 ) return cell + 8; dir = 16; ll = l - 56; break;
+        case 4: if( lk > 0 ) return cell - 64; dir = 4; ll = l + 448; break;
+        default: if( lk < 7 ) return cell + 64; dir = 22; ll = l - 448; break;
+    }
+    const int ns = nbr[(size_t)s * 27 + dir];
+    return ns < 0 ? (size_t)-1 : (size_t)ns * 512 + ll;
 }
 
 // ---------------------------------------------------------------------------------
-// PCG direction: d' = z + beta d; q = A d'; dq = d'.q. One CTA (512 threads) per tile;
-// d is double-buffered so that neighbour tiles read the previous direction.
-__global__ void __launch_bounds__( 512 ) k_pcg_direction( BoraGridDev g, BoraTilesDev t, const uint16_t* __restrict__ code,
-                                                          BoraSolverDev sv, int dsel_in, BoraReduceDev red,
-                                                          int slot_rz_new, int slot_rz_old, int slot_dq_out )
+// PCG direction: d' = z + beta d; q = A d'; dq = d'.q. Streaming, one thread per cell
+// (grid-stride): a neighbour's d' is recomputed from its z and previous d with the same
+// arithmetic as its own thread, so no tile barrier is needed; d is double-buffered.
+__global__ void __launch_bounds__( 256 ) k_pcg_direction( size_t ncells, const int32_t* __restrict__ nbr,
+                                                          const uint16_t* __restrict__ code, BoraSolverDev sv,
+                                                          int dsel_in, BoraReduceDev red, int slot_rz_new,
+                                                          int slot_rz_old, int slot_dq_out )
 {
-    __shared__ int32_t nb[27];
-    __shared__ float sd[512];
-    const int s = blockIdx.x;
-    if( threadIdx.x < 27 ) nb[threadIdx.x] = t.nbr[(size_t)s * 27 + threadIdx.x];
-    const float beta = slot_rz_old < 0 ? 0.f : (float)( red.ring[slot_rz_new] / red.ring[slot_rz_old] );
-    const float* dold = sv.d[dsel_in];
-    float* dnew = sv.d[dsel_in ^ 1];
-    const int l = threadIdx.x;
-    const size_t cell = (size_t)s * 512 + l;
-    const float dn = fmaf( beta, dold[cell], sv.z[cell] );
-    sd[l] = dn;
-    dnew[cell] = dn;
+    __shared__ float s_beta;
+    if( threadIdx.x == 0 ) s_beta = slot_rz_old < 0 ? 0.f : (float)( red.ring[slot_rz_new] / red.ring[slot_rz_old] );
     __syncthreads();
-    const uint16_t cc = code[cell];
-    double pdq = 0.0;
-    if( cc & BORA_CODE_FLUID )
+    const float beta = s_beta;
+    const float* __restrict__ dold = sv.d[dsel_in];
+    float* __restrict__ dnew = sv.d[dsel_in ^ 1];
+    const float* __restrict__ z = sv.z;
+    DF pdq{ 0.f, 0.f };
+    for( size_t cell = blockIdx.x * (size_t)blockDim.x + threadIdx.x; cell < ncells; cell += (size_t)gridDim.x * blockDim.x )
     {
-        const int li = l & 7, lj = ( l >> 3 ) & 7, lk = l >> 6;
-        float acc = 0.f;
-        // neighbour value: inside the tile from shared memory, else recomputed from the
-        // neighbour tile's z and previous d (identical arithmetic to its own CTA)
-        auto nbv = [&]( int q, int inside_off, int dx, int dy, int dz, int lo ) -> float {
-            if( inside_off ) return sd[l + lo];
-            const int ns = nb[bora_dir( dx, dy, dz )];
-            const int ll = bora_local( li + dx, lj + dy, lk + dz );
-            const size_t nc = (size_t)ns * 512 + ll;
-            return fmaf( beta, dold[nc], sv.z[nc] );
-        };
-        if( cc & 1u ) acc += nbv( 0, li > 0, -1, 0, 0, -1 );
-        if( cc & 2u ) acc += nbv( 1, li < 7, 1, 0, 0, 1 );
-        if( cc & 4u ) acc += nbv( 2, lj > 0, 0, -1, 0, -8 );
-        if( cc & 8u ) acc += nbv( 3, lj < 7, 0, 1, 0, 8 );
-        if( cc & 16u ) acc += nbv( 4, lk > 0, 0, 0, -1, -64 );
-        if( cc & 32u ) acc += nbv( 5, lk < 7, 0, 0, 1, 64 );
-        const float qv = fmaf( (float)code_diag( cc ), dn, -acc );
+        const float dn = fmaf( beta, dold[cell], z[cell] );
+        dnew[cell] = dn;
+        const uint16_t cc = code[cell];
+        float qv = 0.f;
+        if( cc & BORA_CODE_FLUID )
+        {
+            const int s = (int)( cell >> 9 ), l = (int)( cell & 511 );
+            float acc = 0.f;
+#pragma unroll
+            for( int q = 0; q < 6; ++q )
+            {
+                if( cc & ( 1u << q ) )
+                {
+                    const size_t nc = face_nbr( nbr, cell, s, l, q );
+                    if( nc == (size_t)-1 ) { atomicOr( red.err, 1u ); continue; }
+                    acc += fmaf( beta, dold[nc], z[nc] );
+                }
+            }
+            qv = fmaf( (float)code_diag( cc ), dn, -acc );
+            pdq = df_add( pdq, df_prod( dn, qv ) );
+        }
         sv.q[cell] = qv;
-        pdq = (double)dn * (double)qv;
     }
-    else
-    {
-        sv.q[cell] = 0.f;
-    }
-    reduce2_publish( pdq, 0.0, 0, red, slot_dq_out, -1 );
+    const double a = df_warp_sum( pdq );
+    reduce2_publish_warp( a, 0.0, 0, red, slot_dq_out, -1 );
 }
 
 // ---------------------------------------------------------------------------------
 __global__ void k_solve_init( size_t ncells, const float* __restrict__ b, BoraSolverDev sv, BoraReduceDev red,
                               int slot_norm2, int slot_max )
 {
-    double n2 = 0.0, mx = 0.0;
+    DF n2{ 0.f, 0.f };
+    float mx = 0.f;
     for( size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < ncells; i += (size_t)gridDim.x * blockDim.x )
     {
         const float bv = b[i];
@@ -439,10 +553,10 @@ __global__ void k_solve_init( size_t ncells, const float* __restrict__ b, BoraSo
         sv.d[0][i] = 0.f;
         sv.d[1][i] = 0.f;
         sv.q[i] = 0.f;
-        n2 += (double)bv * bv;
-        mx = fmax( mx, (double)fabsf( bv ) );
+        n2 = df_add( n2, df_prod( bv, bv ) );
+        mx = fmaxf( mx, fabsf( bv ) );
     }
-    reduce2_publish( n2, mx, 1, red, slot_norm2, slot_max );
+    reduce2_publish_dfmax( n2, mx, red, slot_norm2, slot_max );
 }
 
 __global__ void k_refine_accumulate( size_t ncells, const uint16_t* __restrict__ code, BoraSolverDev sv )
@@ -457,46 +571,34 @@ __global__ void k_refine_accumulate( size_t ncells, const uint16_t* __restrict__
     }
 }
 
-// r = b - A x in FP64 (A from the stencil code); r stored in FP32.
-__global__ void __launch_bounds__( 512 ) k_refine_residual( BoraGridDev g, BoraTilesDev t, const float* __restrict__ b,
-                                                            const uint16_t* __restrict__ code, BoraSolverDev sv,
-                                                            BoraReduceDev red, int slot_norm2, int slot_max )
+// r = b - A x in FP64 (A from the stencil code); r stored in FP32. Streaming, one thread
+// per cell.
+__global__ void __launch_bounds__( 256 ) k_refine_residual( size_t ncells, const int32_t* __restrict__ nbr,
+                                                            const float* __restrict__ b, const uint16_t* __restrict__ code,
+                                                            BoraSolverDev sv, BoraReduceDev red, int slot_norm2,
+                                                            int slot_max )
 {
-    __shared__ int32_t nb[27];
-    __shared__ double sxv[512];
-    const int s = blockIdx.x;
-    if( threadIdx.x < 27 ) nb[threadIdx.x] = t.nbr[(size_t)s * 27 + threadIdx.x];
-    const int l = threadIdx.x;
-    const size_t cell = (size_t)s * 512 + l;
-    sxv[l] = sv.x[cell];
-    __syncthreads();
-    const uint16_t cc = code[cell];
     double n2 = 0.0, mx = 0.0;
-    if( cc & BORA_CODE_FLUID )
+    for( size_t cell = blockIdx.x * (size_t)blockDim.x + threadIdx.x; cell < ncells; cell += (size_t)gridDim.x * blockDim.x )
     {
-        const int li = l & 7, lj = ( l >> 3 ) & 7, lk = l >> 6;
-        auto nbv = [&]( int inside_off, int dx, int dy, int dz, int lo ) -> double {
-            if( inside_off ) return sxv[l + lo];
-            const int ns = nb[bora_dir( dx, dy, dz )];
-            return sv.x[(size_t)ns * 512 + bora_local( li + dx, lj + dy, lk + dz )];
-        };
+        const uint16_t cc = code[cell];
+        if( !( cc & BORA_CODE_FLUID ) ) { sv.r[cell] = 0.f; continue; }
+        const int s = (int)( cell >> 9 ), l = (int)( cell & 511 );
         double acc = 0.0;
-        if( cc & 1u ) acc += nbv( li > 0, -1, 0, 0, -1 );
-        if( cc & 2u ) acc += nbv( li < 7, 1, 0, 0, 1 );
-        if( cc & 4u ) acc += nbv( lj > 0, 0, -1, 0, -8 );
-        if( cc & 8u ) acc += nbv( lj < 7, 0, 1, 0, 8 );
-        if( cc & 16u ) acc += nbv( lk > 0, 0, 0, -1, -64 );
-        if( cc & 32u ) acc += nbv( lk < 7, 0, 0, 1, 64 );
-        const double rv = (double)b[cell] - ( (double)code_diag( cc ) * sxv[l] - acc );
+#pragma unroll
+        for( int q = 0; q < 6; ++q )
+        {
+            if( !( cc & ( 1u << q ) ) ) continue;
+            const size_t nc = face_nbr( nbr, cell, s, l, q );
+            if( nc == (size_t)-1 ) { atomicOr( red.err, 2u ); continue; }
+            acc += sv.x[nc];
+        }
+        const double rv = (double)b[cell] - ( (double)code_diag( cc ) * sv.x[cell] - acc );
         sv.r[cell] = (float)rv;
-        n2 = rv * rv;
-        mx = fabs( rv );
+        n2 += rv * rv;
+        mx = fmax( mx, fabs( rv ) );
     }
-    else
-    {
-        sv.r[cell] = 0.f;
-    }
-    reduce2_publish( n2, mx, 1, red, slot_norm2, slot_max );
+    reduce2_publish_warp( warp_sum( n2 ), warp_max( mx ), 1, red, slot_norm2, slot_max );
 }
 
 __global__ void k_write_pressure( size_t ncells, const uint16_t* __restrict__ code, const double* __restrict__ x,
@@ -609,8 +711,6 @@ int grid_for( size_t n, int threads )
 
 }  // namespace
 
-size_t bora_reduce_max_blocks() { return 152 * 8 > 0 ? (size_t)1 << 22 : 0; }
-
 void bora_launch_rhs( const BoraGridDev& g, int ntiles, BoraTilesDev t, BoraCellsDev c, cudaStream_t st )
 {
     if( ntiles > 0 ) k_rhs<<<ntiles, 512, 0, st>>>( g, t, c );
@@ -624,7 +724,9 @@ void bora_launch_vel_update( const BoraGridDev& g, int ntiles, BoraTilesDev t, B
 void bora_launch_mic_factor( const BoraGridDev&, int ntiles, const uint16_t* code, float* minv, cudaStream_t st )
 {
     ensure_tables();
-    if( ntiles > 0 ) k_mic_factor<<<( ntiles + kTilesPerCta - 1 ) / kTilesPerCta, 32 * kTilesPerCta, 0, st>>>( ntiles, code, minv );
+    if( ntiles <= 0 ) return;
+    const int nb = std::min( ( ntiles + kTilesPerCta - 1 ) / kTilesPerCta, num_sms() * 8 );
+    k_mic_factor<<<nb, 32 * kTilesPerCta, 0, st>>>( ntiles, code, minv );
 }
 
 void bora_launch_solve_init( int ntiles, const float* b, const uint16_t*, BoraSolverDev s, BoraReduceDev red,
@@ -638,17 +740,18 @@ void bora_launch_pcg_update( int ntiles, const uint16_t* code, BoraSolverDev s, 
                              int slot_rz_in, int slot_dq_in, int slot_rz_out, int slot_rr_out, cudaStream_t st )
 {
     ensure_tables();
-    const int nb = ( ntiles + kTilesPerCta - 1 ) / kTilesPerCta;
-    k_pcg_update<<<nb > 0 ? nb : 1, 32 * kTilesPerCta, 0, st>>>( ntiles, code, s, dsel, red, slot_rz_in, slot_dq_in,
-                                                                   slot_rz_out, slot_rr_out );
+    const int nb = std::max( 1, std::min( ( ntiles + kTilesPerCta - 1 ) / kTilesPerCta, num_sms() * 7 ) );
+    k_pcg_update<<<nb, 32 * kTilesPerCta, 0, st>>>( ntiles, code, s, dsel, red, slot_rz_in, slot_dq_in, slot_rz_out,
+                                                    slot_rr_out );
 }
 
-void bora_launch_pcg_direction( const BoraGridDev& g, int ntiles, BoraTilesDev t, const uint16_t* code, BoraSolverDev s,
+void bora_launch_pcg_direction( const BoraGridDev&, int ntiles, BoraTilesDev t, const uint16_t* code, BoraSolverDev s,
                                 int dsel_in, BoraReduceDev red, int slot_rz_new, int slot_rz_old, int slot_dq_out,
                                 cudaStream_t st )
 {
-    if( ntiles > 0 )
-        k_pcg_direction<<<ntiles, 512, 0, st>>>( g, t, code, s, dsel_in, red, slot_rz_new, slot_rz_old, slot_dq_out );
+    const size_t nc = (size_t)ntiles * 512;
+    const int nb = (int)std::max<size_t>( 1, std::min<size_t>( ( nc + 255 ) / 256, (size_t)num_sms() * 8 ) );
+    k_pcg_direction<<<nb, 256, 0, st>>>( nc, t.nbr, code, s, dsel_in, red, slot_rz_new, slot_rz_old, slot_dq_out );
 }
 
 void bora_launch_refine_accumulate( int ntiles, const uint16_t* code, BoraSolverDev s, cudaStream_t st )
@@ -657,10 +760,12 @@ void bora_launch_refine_accumulate( int ntiles, const uint16_t* code, BoraSolver
     if( nc ) k_refine_accumulate<<<grid_for( nc, 256 ), 256, 0, st>>>( nc, code, s );
 }
 
-void bora_launch_refine_residual( const BoraGridDev& g, int ntiles, BoraTilesDev t, const float* b, const uint16_t* code,
+void bora_launch_refine_residual( const BoraGridDev&, int ntiles, BoraTilesDev t, const float* b, const uint16_t* code,
                                   BoraSolverDev s, BoraReduceDev red, int slot_norm2, int slot_max, cudaStream_t st )
 {
-    if( ntiles > 0 ) k_refine_residual<<<ntiles, 512, 0, st>>>( g, t, b, code, s, red, slot_norm2, slot_max );
+    const size_t nc = (size_t)ntiles * 512;
+    const int nb = (int)std::max<size_t>( 1, std::min<size_t>( ( nc + 255 ) / 256, (size_t)num_sms() * 8 ) );
+    k_refine_residual<<<nb, 256, 0, st>>>( nc, t.nbr, b, code, s, red, slot_norm2, slot_max );
 }
 
 void bora_launch_write_pressure( int ntiles, const uint16_t* code, const double* x, float* pres, cudaStream_t st )
