@@ -198,6 +198,16 @@ int bora_flip_set_profiling( bora_flip_handle h, uint32_t class_mask );
 int bora_flip_get_kernel_times( bora_flip_handle h, double* ms, uint64_t* launches, int n );
 const char* bora_flip_status_string( int status );
 
+/* ---- device building blocks ------------------------------------------------------- */
+
+/* Exclusive prefix sum of n uint32 counts in device memory: d_out[i] = sum_{j<i} d_in[j];
+ * *d_total (device pointer, may be NULL) = sum of all. d_in and d_out may alias. Runs on
+ * `stream` (a cudaStream_t; NULL = the legacy default stream) and returns without
+ * waiting. This is the compaction step of the sparse-frame rebuild: the reference
+ * numbers its active tiles with a serial host loop over the tile-marker table
+ * (base/source/SparseFrame.cu:131-152). Block sums go to stream-ordered scratch memory. */
+int bora_scan_u32( const uint32_t* d_in, uint32_t* d_out, size_t n, uint32_t* d_total, void* stream );
+
 #ifdef __cplusplus
 }
 #endif

@@ -15,7 +15,7 @@ HEADER = os.path.join(ROOT, "include", "bora_flip.h")
 
 def declared_functions():
     text = open(HEADER).read()
-    return sorted(set(re.findall(r"^\s*(?:int|const char\*)\s+(bora_flip_\w+)\s*\(", text, re.M)))
+    return sorted(set(re.findall(r"^\s*(?:int|const char\*)\s+(bora_\w+)\s*\(", text, re.M)))
 
 
 def test_header_declarations_are_bound(flip_lib):

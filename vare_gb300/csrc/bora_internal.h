@@ -9,7 +9,7 @@
 
 // ---- scan ---------------------------------------------------------------------------
 size_t bora_scan_scratch_elems( size_t n );
-void bora_scan_u32( const uint32_t* in, uint32_t* out, size_t n, uint32_t* scratch, uint32_t* total, cudaStream_t st );
+void bora_device_scan( const uint32_t* in, uint32_t* out, size_t n, uint32_t* scratch, uint32_t* total, cudaStream_t st );
 
 // ---- particle arrays (structure of arrays) -------------------------------------------
 struct BoraParticlesDev

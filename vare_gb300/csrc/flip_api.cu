@@ -366,7 +366,7 @@ int stage_rebuild( bora_flip_sim* s )
     {
         KTimer t( s, BORA_KERNEL_TILES, 4 );
         bora_launch_activate( s->g, P<uint8_t>( s->tile_flag ), P<uint32_t>( s->tile_act ), st );
-        bora_scan_u32( P<uint32_t>( s->tile_act ), P<uint32_t>( s->tile_excl ), s->ntv, P<uint32_t>( s->scan_scratch ),
+        bora_device_scan( P<uint32_t>( s->tile_act ), P<uint32_t>( s->tile_excl ), s->ntv, P<uint32_t>( s->scan_scratch ),
                        P<uint32_t>( s->counters ) + 0, st );
     }
     BORA_TRYS( check_launch( s ) );
@@ -385,7 +385,7 @@ int stage_rebuild( bora_flip_sim* s )
         KTimer t( s, BORA_KERNEL_SORT, s->np ? 5 : 3 );
         bora_launch_hist( s->np, P<uint32_t>( s->vkey ), P<int32_t>( s->slot_of ), ncell, P<uint32_t>( s->key ),
                           P<uint32_t>( s->cell_count ), P<uint32_t>( s->counters ) + 2, st );
-        bora_scan_u32( P<uint32_t>( s->cell_count ), P<uint32_t>( s->cell_start ), (size_t)ncell + 1,
+        bora_device_scan( P<uint32_t>( s->cell_count ), P<uint32_t>( s->cell_start ), (size_t)ncell + 1,
                        P<uint32_t>( s->scan_scratch ), P<uint32_t>( s->counters ) + 1, st );
         bora_launch_scatter( s->np, P<uint32_t>( s->key ), P<uint32_t>( s->cell_start ), P<uint32_t>( s->cell_count ),
                              P<uint32_t>( s->idx ), st );
@@ -778,7 +778,7 @@ int bora_flip_get_particles( bora_flip_handle s, float* pos, float* vel, float* 
     BoraParticlesDev p = s->parts( s->cur );
     s->stats.kernel_launches += 5;
     k_live_flags<<<grid_blocks( np ), 256, 0, st>>>( np, p.id, P<uint32_t>( s->live_flag ) );
-    bora_scan_u32( P<uint32_t>( s->live_flag ), P<uint32_t>( s->live_flag ), np, P<uint32_t>( s->scan_scratch ),
+    bora_device_scan( P<uint32_t>( s->live_flag ), P<uint32_t>( s->live_flag ), np, P<uint32_t>( s->scan_scratch ),
                    P<uint32_t>( s->counters ) + 4, st );
     const size_t nl = s->nlive;
     float* opos = P<float>( s->stage_out );

@@ -123,7 +123,7 @@ size_t bora_scan_scratch_elems( size_t n ) { return ( n + kScanChunk - 1 ) / kSc
 
 // out[i] = sum_{j<i} in[i]; *total = sum of all (device pointer, may be null).
 // in and out may alias. scratch holds bora_scan_scratch_elems(n) uint32.
-void bora_scan_u32( const uint32_t* in, uint32_t* out, size_t n, uint32_t* scratch, uint32_t* total, cudaStream_t st )
+void bora_device_scan( const uint32_t* in, uint32_t* out, size_t n, uint32_t* scratch, uint32_t* total, cudaStream_t st )
 {
     if( n == 0 )
     {
@@ -134,4 +134,29 @@ void bora_scan_u32( const uint32_t* in, uint32_t* out, size_t n, uint32_t* scrat
     k_scan_reduce<<<nb, kScanThreads, 0, st>>>( in, n, scratch );
     k_scan_blocks<<<1, kScanThreads, 0, st>>>( scratch, nb, total );
     k_scan_down<<<nb, kScanThreads, 0, st>>>( in, n, scratch, out );
+}
+
+// ---- public C ABI: device exclusive prefix sum -------------------------------------
+#include "../../include/bora_flip.h"
+
+extern "C" int bora_scan_u32( const uint32_t* d_in, uint32_t* d_out, size_t n, uint32_t* d_total, void* stream )
+{
+    if( n > 0 && ( !d_in || !d_out ) ) return BORA_ERR_INVALID_ARG;
+    if( n > (size_t)0xFFFFFFFFu ) return BORA_ERR_CAPACITY;
+    cudaStream_t st = (cudaStream_t)stream;
+    uint32_t* scratch = nullptr;
+    if( n > 0 )
+    {
+        // stream-ordered scratch for the per-block sums, released on the same stream
+        const cudaError_t e = cudaMallocAsync( (void**)&scratch, bora_scan_scratch_elems( n ) * sizeof( uint32_t ), st );
+        if( e != cudaSuccess ) return e == cudaErrorMemoryAllocation ? BORA_ERR_OUT_OF_MEMORY : BORA_ERR_CUDA;
+    }
+    bora_device_scan( d_in, d_out, n, scratch, d_total, st );
+    cudaError_t e = cudaGetLastError();
+    if( scratch )
+    {
+        const cudaError_t f = cudaFreeAsync( scratch, st );
+        if( e == cudaSuccess ) e = f;
+    }
+    return e == cudaSuccess ? BORA_OK : BORA_ERR_CUDA;
 }

@@ -99,6 +99,7 @@ _SIGS = {
     "bora_flip_status_string": (ctypes.c_char_p, [ctypes.c_int]),
     "bora_flip_set_profiling": (ctypes.c_int, [_vp, ctypes.c_uint32]),
     "bora_flip_get_kernel_times": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int]),
+    "bora_scan_u32": (ctypes.c_int, [_vp, _vp, ctypes.c_size_t, _vp, _vp]),
 }
 
 _LIB: ctypes.CDLL | None = None
