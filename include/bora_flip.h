@@ -208,6 +208,20 @@ const char* bora_flip_status_string( int status );
  * (base/source/SparseFrame.cu:131-152). Block sums go to stream-ordered scratch memory. */
 int bora_scan_u32( const uint32_t* d_in, uint32_t* d_out, size_t n, uint32_t* d_total, void* stream );
 
+/* bora_scan_u32 without any device allocation (this entry point has no counterpart in
+ * the reference). For callers that cannot call cudaMalloc or the stream-ordered
+ * allocator: a host plugin running under a fixed device-memory budget, code recorded
+ * into a CUDA graph where allocation calls are not allowed, or real-time callbacks that
+ * must not block on the allocator. The per-block sums go to a static device array of
+ * 512 KiB that every device using the library keeps until the process exits, so
+ * n <= 2^28 (268,435,456); larger n returns BORA_ERR_CAPACITY. The first call on a
+ * device looks up the array's device address (a runtime call that does not allocate);
+ * make that first call before any stream capture. All calls share the one array: two
+ * calls whose work overlaps on the GPU (different streams, or different host threads)
+ * race and must be serialised by the caller. Same arguments and results as
+ * bora_scan_u32; returns without waiting for the GPU. */
+int bora_scan_u32_noalloc( const uint32_t* d_in, uint32_t* d_out, size_t n, uint32_t* d_total, void* stream );
+
 #ifdef __cplusplus
 }
 #endif

@@ -160,3 +160,43 @@ extern "C" int bora_scan_u32( const uint32_t* d_in, uint32_t* d_out, size_t n, u
     }
     return e == cudaSuccess ? BORA_OK : BORA_ERR_CUDA;
 }
+
+// ---- no-allocation variant ---------------------------------------------------------
+// For callers that must not allocate device memory (see bora_scan_u32_noalloc in
+// include/bora_flip.h). The per-block sums live in this file-scope array: 2048 input
+// counts per block, so 2^28 counts need 131,073 sums (512 KiB + 4 B). Every device that
+// loads the library holds the array until the process exits.
+#include <mutex>
+
+#define BORA_SCAN_NOALLOC_MAX ( (size_t)1 << 28 )
+static __device__ __align__( 256 ) uint32_t g_noalloc_block_sums[BORA_SCAN_NOALLOC_MAX / kScanChunk + 1];
+
+namespace {
+std::mutex g_noalloc_mutex;
+uint32_t* g_noalloc_addr[64] = {};  // device address of g_noalloc_block_sums, per device ordinal
+}  // namespace
+
+extern "C" int bora_scan_u32_noalloc( const uint32_t* d_in, uint32_t* d_out, size_t n, uint32_t* d_total, void* stream )
+{
+    if( n > 0 && ( !d_in || !d_out ) ) return BORA_ERR_INVALID_ARG;
+    if( n > BORA_SCAN_NOALLOC_MAX ) return BORA_ERR_CAPACITY;
+    int dev = -1;
+    if( cudaGetDevice( &dev ) != cudaSuccess || dev < 0 || dev >= 64 ) return BORA_ERR_CUDA;
+    uint32_t* scratch = nullptr;
+    {
+        // First call on this device: the host-side name of the array is not a device
+        // address, so ask the runtime for the address on the current device.
+        std::lock_guard<std::mutex> lock( g_noalloc_mutex );
+        if( !g_noalloc_addr[dev] )
+        {
+            void* p = nullptr;
+            if( cudaGetSymbolAddress( &p, g_noalloc_block_sums ) != cudaSuccess || !p ) return BORA_ERR_CUDA;
+            g_noalloc_addr[dev] = static_cast<uint32_t*>( p );
+        }
+        scratch = g_noalloc_addr[dev];
+    }
+    // Each call writes every block sum before reading it, so the array's previous
+    // contents never matter and nothing needs clearing.
+    bora_device_scan( d_in, d_out, n, scratch, d_total, (cudaStream_t)stream );
+    return cudaGetLastError() == cudaSuccess ? BORA_OK : BORA_ERR_CUDA;
+}

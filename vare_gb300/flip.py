@@ -100,6 +100,7 @@ _SIGS = {
     "bora_flip_set_profiling": (ctypes.c_int, [_vp, ctypes.c_uint32]),
     "bora_flip_get_kernel_times": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int]),
     "bora_scan_u32": (ctypes.c_int, [_vp, _vp, ctypes.c_size_t, _vp, _vp]),
+    "bora_scan_u32_noalloc": (ctypes.c_int, [_vp, _vp, ctypes.c_size_t, _vp, _vp]),
 }
 
 _LIB: ctypes.CDLL | None = None
