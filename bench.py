@@ -52,7 +52,12 @@ UNIT = "particle-steps/s"
 ALG_BYTES = {
     "bin": (0, 20), "tiles": (0, 0), "sort": (12, 16), "p2g": (25, 28), "rhs": (25, 0),
     "pcg_direction": (18, 0), "pcg_update": (34, 0), "refine": (30, 0), "velocity": (33, 0), "g2p": (28, 64),
+    "mg_vcycle": (43, 0),
 }
+# Mixed form: the PCG update has no preconditioner sweep (read e, d, r, q; write e, r: 24 B/cell);
+# one V-cycle moves ~38 B per fine cell (FP16 level vectors, FP32 residual in, FP32 z out)
+# plus ~1/7 of that on the coarse levels -> 43 B/cell.
+ALG_BYTES_MIXED = dict(ALG_BYTES, pcg_update=(24, 0))
 
 
 def parse():
@@ -65,6 +70,9 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-steps", type=int, default=2)
+    ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--solver", default="both", choices=["both", "plain", "mixed"],
+                    help="plain only / mixed only (profiling runs); the default times both")
     return ap.parse_args()
 
 
@@ -262,17 +270,12 @@ def run_reference(args, world, rank):
     print(json.dumps(out), flush=True)
 
 
-def run_ours(args, world, rank, local):
+def timed_steps(sim, sc, args, world, flip, local, sample_clocks, alg=ALG_BYTES):
+    """W warm-up steps (every kernel class timed, to find the dominant one), then K timed
+    steps with only the dominant class bracketed by events. Returns the measurements."""
     import numpy as np
     import torch
 
-    from vare_gb300 import build, flip
-
-    build.build()
-    torch.cuda.set_device(local)
-    sc = make_scene(args.workload)
-    sim = flip.FlipSim.from_scene(sc)
-    # warm-up, with every kernel class timed to find the dominant one
     sim.set_profiling(0xFFFF)
     for _ in range(args.warmup):
         sim.step(sc.dt)
@@ -281,9 +284,9 @@ def run_ours(args, world, rank, local):
     dom = int(np.argmax(ms[:len(classes)]))
     share = {c: float(ms[i]) for i, c in enumerate(classes)}
     sim.set_profiling(1 << dom)
-
-    clocks = ClockSampler(local)
-    clocks.start()
+    clocks = ClockSampler(local) if sample_clocks else None
+    if clocks:
+        clocks.start()
     launches0 = sim.stats()["kernel_launches"]
     barrier(world)
     torch.cuda.synchronize()
@@ -301,35 +304,57 @@ def run_ours(args, world, rank, local):
         all_conv = all_conv and status == 0 and st["converged"] == 1
     torch.cuda.synchronize()
     barrier(world)
-    clk = clocks.stop()
+    clk = clocks.stop() if clocks else None
     launches = sim.stats()["kernel_launches"] - launches0
     kms, kn = sim.kernel_times()
     my_time = sum(step_ms) / 1e3
     t_max = allreduce_max(my_time, world)
     total_ps = allreduce_sum(float(particle_steps), world)
-    value = total_ps / t_max
 
     # roofline of the dominant kernel class, measured over the timed region
     fi = sim.frame_info()
     ncells = fi["ntiles"] * 512
-    cell_b, part_b = ALG_BYTES[classes[dom]]
+    name = classes[dom]
+    cell_b, part_b = alg.get(name, (0, 0))
     avg_launch_ms = float(kms[dom] / max(1, kn[dom]))
-    launches_per_step = float(kn[dom]) / args.steps
     bytes_per_launch = cell_b * ncells + part_b * sim.num_particles
-    if classes[dom] in ("pcg_direction", "pcg_update"):
-        bytes_per_launch = cell_b * ncells
     peak, peak_kind = measured_peaks()
     achieved = bytes_per_launch / (avg_launch_ms * 1e-3) / 1e9 if avg_launch_ms > 0 else 0.0
-    traffic, tnote = ncu_traffic(classes[dom])
-    roof = {"kernel": classes[dom], "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"
-            if peak_kind == "measured" else "fallback 6.8 TB/s",
+    traffic, tnote = ncu_traffic(name)
+    roof = {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "traffic": traffic,
+            "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
+            else "fallback 6.8 TB/s",
             "alg_bytes_per_launch": bytes_per_launch, "avg_launch_ms": avg_launch_ms,
-            "launches_per_step": launches_per_step, "active_cells": ncells,
+            "launches_per_step": float(kn[dom]) / args.steps, "active_cells": ncells,
             "share_of_warmup_device_time": {c: round(v / max(1e-9, sum(share.values())), 4)
                                             for c, v in share.items()}}
     if tnote:
         roof["traffic_note"] = tnote
+    ms_sorted = sorted(step_ms)
+    p99 = ms_sorted[min(len(ms_sorted) - 1, int(round(0.99 * (len(ms_sorted) - 1))))]
+    return {"value": total_ps / t_max, "t_max": t_max, "ms_per_step": t_max * 1e3 / args.steps,
+            "p50_ms": ms_sorted[len(ms_sorted) // 2], "p99_ms": p99, "roofline": roof, "clocks": clk,
+            "launches": int(launches),
+            "solver": {"iterations_per_step": iters, "all_converged": all_conv, **worst,
+                       "active_tiles": fi["ntiles"]}}
+
+
+def run_ours(args, world, rank, local):
+    import torch
+
+    from vare_gb300 import build, flip
+
+    build.build()
+    torch.cuda.set_device(local)
+    sc = make_scene(args.workload)
+    if args.solver == "mixed":
+        args.no_mixed = True
+    sim = flip.FlipSim.from_scene(sc, solver=flip.SOLVER_MIXED if args.solver == "mixed" else flip.SOLVER_PLAIN)
+    meas = timed_steps(sim, sc, args, world, flip, local, True)
+    if args.solver == "plain":
+        args.no_mixed = True
+    value, roof, clk, launches = meas["value"], meas["roofline"], meas["clocks"], meas["launches"]
 
     # end to end through the C ABI with host buffers (pinned), rank-local
     e2e = None
@@ -360,6 +385,19 @@ def run_ours(args, world, rank, local):
                "how": "host wall time of bora_flip_set_particles (pinned host -> device) + bora_flip_step + "
                       "bora_flip_get_particles (device -> pinned host) per step"}
 
+    # mixed-precision form on the same scene: MG-preconditioned CG, FP16 V-cycle storage
+    mixed = None
+    if not args.no_mixed:
+        del sim
+        torch.cuda.empty_cache()
+        sim = flip.FlipSim.from_scene(sc, solver=flip.SOLVER_MIXED)
+        mm = timed_steps(sim, sc, args, world, flip, local, False, ALG_BYTES_MIXED)
+        mixed = {"value": mm["value"], "unit": UNIT, "ms_per_step": mm["ms_per_step"], "p50_ms": mm["p50_ms"],
+                 "p99_ms": mm["p99_ms"], "roofline": mm["roofline"], "gpu_launches": mm["launches"],
+                 "solver": mm["solver"], "speedup_over_plain": mm["value"] / value,
+                 "config": "same scene; geometric-multigrid-preconditioned CG, V(2,2) damped Jacobi, FP16 level "
+                           "storage with FP32 arithmetic, FP64-accurate dots and norms, FP64 iterative refinement"}
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         del sim
@@ -368,16 +406,12 @@ def run_ours(args, world, rank, local):
 
     if rank != 0:
         return
-    ms_sorted = sorted(step_ms)
-    p99 = ms_sorted[min(len(ms_sorted) - 1, int(round(0.99 * (len(ms_sorted) - 1))))]
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-           "warmup": args.warmup, "ms_per_step": t_max * 1e3 / args.steps, "p50_ms": ms_sorted[len(ms_sorted) // 2],
-           "p99_ms": p99, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "warmup": args.warmup, "ms_per_step": meas["ms_per_step"], "p50_ms": meas["p50_ms"],
+           "p99_ms": meas["p99_ms"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
            "data": "synthetic (seeded jittered-uniform dam break + sphere; no public data set exists for this path)",
            "config": workload_config(sc), "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
-           "gpu_launches": int(launches), "clocks": clk,
-           "solver": {"iterations_per_step": iters, "all_converged": all_conv, **worst,
-                      "active_tiles": fi["ntiles"]}}
+           "gpu_launches": int(launches), "clocks": clk, "solver": meas["solver"], "mixed": mixed}
     print(json.dumps(out), flush=True)
 
 

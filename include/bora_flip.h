@@ -115,6 +115,7 @@ typedef struct bora_flip_stats
 #define BORA_KERNEL_REFINE 7       /* solver init, FP64 refinement, pressure write-back */
 #define BORA_KERNEL_VELOCITY 8
 #define BORA_KERNEL_G2P 9
+#define BORA_KERNEL_MG 10          /* multigrid V-cycle (mixed solver) */
 #define BORA_KERNEL_CLASSES 16
 
 /* Simulation frame description (after padding). */

@@ -159,10 +159,11 @@ def test_stages_bit_exact(gpu, oracle_lib, scene):
         np.testing.assert_array_equal(a, b, err_msg=name)
 
 
-def test_solve_matches_fp64_oracle(gpu, oracle_lib, scene):
+@pytest.mark.parametrize("solver", ["plain", "mixed"])
+def test_solve_matches_fp64_oracle(gpu, oracle_lib, scene, solver):
     B = oracle_lib
     sc = scene
-    sim, ora = _pair(gpu, oracle_lib, sc)
+    sim, ora = _pair(gpu, oracle_lib, sc, solver=gpu.SOLVER_MIXED if solver == "mixed" else gpu.SOLVER_PLAIN)
     for st in (gpu.STAGE_REBUILD, gpu.STAGE_P2G, gpu.STAGE_BUILD_SYSTEM):
         sim.run_stage(st)
     ora.rebuild(); ora.p2g(); ora.mark()
@@ -186,9 +187,10 @@ def test_solve_matches_fp64_oracle(gpu, oracle_lib, scene):
     assert rmax <= 10 * st["residual_max"] + 16 * float(np.abs(sysm["x"]).max()) * 2.0 ** -24
 
 
-def test_full_step_matches_oracle(gpu, oracle_lib, scene):
+@pytest.mark.parametrize("solver", ["plain", "mixed"])
+def test_full_step_matches_oracle(gpu, oracle_lib, scene, solver):
     sc = scene
-    sim, ora = _pair(gpu, oracle_lib, sc)
+    sim, ora = _pair(gpu, oracle_lib, sc, solver=gpu.SOLVER_MIXED if solver == "mixed" else gpu.SOLVER_PLAIN)
     for _ in range(2):
         assert sim.step(sc.dt) == 0
         ora.step(sc.dt)
@@ -224,10 +226,12 @@ def test_step_matches_reference_golden(gpu):
     assert rel_err(vel, g["vel2"][o]) <= 1e-4
 
 
-def test_deterministic(gpu):
+@pytest.mark.parametrize("solver", ["plain", "mixed"])
+def test_deterministic(gpu, solver):
     sc = scenes.small(24)
-    a = gpu.FlipSim.from_scene(sc)
-    b = gpu.FlipSim.from_scene(sc)
+    sv = gpu.SOLVER_MIXED if solver == "mixed" else gpu.SOLVER_PLAIN
+    a = gpu.FlipSim.from_scene(sc, solver=sv)
+    b = gpu.FlipSim.from_scene(sc, solver=sv)
     for _ in range(3):
         a.step(sc.dt)
         b.step(sc.dt)
@@ -285,14 +289,15 @@ def test_world_space_round_trip(gpu):
     np.testing.assert_allclose(posw[np.argsort(ids)], world, atol=1e-6)
 
 
-def test_full_size_invariants(gpu):
+@pytest.mark.parametrize("solver", ["plain", "mixed"])
+def test_full_size_invariants(gpu, solver):
     """The 256^3 dam-break + sphere scene (24,564,400 particles): size-independent
     properties after two steps - every particle kept once (solid walls), the count field
     sums to the stencil contributions, the tile set follows the activation rule, and the
     projection met max|b - Ap| * dx < 1e-5 with ||r||/||b|| < 1e-6."""
     sc = scenes.config1()
     assert sc.num_particles == 24564400
-    sim = gpu.FlipSim.from_scene(sc)
+    sim = gpu.FlipSim.from_scene(sc, solver=gpu.SOLVER_MIXED if solver == "mixed" else gpu.SOLVER_PLAIN)
     for _ in range(2):
         status = sim.step(sc.dt)
         st = sim.stats()

@@ -3,6 +3,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include "flip_common.cuh"
@@ -110,3 +111,28 @@ void bora_launch_refine_residual( const BoraGridDev& g, int ntiles, BoraTilesDev
 // pres = (float) x on fluid cells, 0 elsewhere
 void bora_launch_write_pressure( int ntiles, const uint16_t* code, const double* x, float* pres, cudaStream_t st );
 
+
+// ---- multigrid preconditioner (mixed form) ----------------------------------------------
+struct BoraLevelDev
+{
+    int kind;          // 0 = tiled (E cells per tile edge), 1 = dense grid
+    int E;             // tiled levels: 8, 4, 2, 1
+    int level;         // 0 = fine grid
+    int nx, ny, nz;    // cells of this level inside the domain
+    int dx, dy, dz;    // dense storage extent (dense levels)
+    size_t ncells;     // stored cells
+    uint8_t* type;     // BORA_FLUID / BORA_AIR / BORA_SOLID / BORA_MASKED
+    uint16_t* code;    // stencil code (fine-code layout)
+    __half* r;         // level residual (levels >= 1), stencil units
+    __half* z0;        // correction (pre-smoothed, then final)
+    __half* z1;        // correction after prolongation + one sweep
+};
+
+// Cell types and stencil codes of level c from level c-1 (levels[0] = fine, given).
+void bora_mg_setup( const BoraGridDev& g, BoraLevelDev* levels, int nlevels, BoraTilesDev t, uint32_t* err, cudaStream_t st );
+// One V-cycle: z = M^-1 r (FP32 in and out, FP16 inside); r.z -> ring slot (FP64-accurate).
+void bora_mg_vcycle( const BoraGridDev& g, const BoraLevelDev* levels, int nlevels, BoraTilesDev t, const float* r,
+                     float* z, BoraReduceDev red, int slot_rr, int slot_rz, int coarse_sweeps, cudaStream_t st );
+// e += alpha d; r -= alpha q; r.r -> ring slot (alpha = rz / dq, or 0 when slot_rz < 0)
+void bora_launch_pcg_update_noprec( int ntiles, BoraSolverDev s, int dsel, BoraReduceDev red, int slot_rz, int slot_dq,
+                                    int slot_rr_out, cudaStream_t st );

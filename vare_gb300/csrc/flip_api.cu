@@ -103,6 +103,12 @@ struct bora_flip_sim
     DevBuf sx, se, sr, sd0, sd1, sq, sz, sminv;
     DevBuf cell_count, cell_start;
 
+    // multigrid hierarchy (mixed solver): per level type, code, r, z0, z1
+    static constexpr int kMaxLevels = 16;
+    DevBuf mg_type[kMaxLevels], mg_code[kMaxLevels], mg_r[kMaxLevels], mg_z0[kMaxLevels], mg_z1[kMaxLevels];
+    BoraLevelDev levels[kMaxLevels] = {};
+    int nlevels = 0;
+
     // reductions
     DevBuf ring, partials, done;
     int next_slot = 0;
@@ -408,11 +414,78 @@ int stage_p2g( bora_flip_sim* s )
     return check_launch( s );
 }
 
+// Multigrid hierarchy for the current tiles: levels 0..3 tiled (8^3, 4^3, 2^3, 1 cell per
+// tile), then dense grids halved per level until a level has at most 512 cells.
+int build_hierarchy( bora_flip_sim* s )
+{
+    const BoraGridDev& g = s->g;
+    const size_t nt = (size_t)s->ntiles;
+    int n = 0;
+    int ex = g.nx, ey = g.ny, ez = g.nz;
+    auto add = [&]( int kind, int E, size_t ncells, int dx, int dy, int dz ) -> int {
+        if( n >= bora_flip_sim::kMaxLevels ) return BORA_ERR_INTERNAL;
+        BoraLevelDev& L = s->levels[n];
+        L.kind = kind; L.E = E; L.level = n;
+        L.nx = ex; L.ny = ey; L.nz = ez;
+        L.dx = dx; L.dy = dy; L.dz = dz;
+        L.ncells = ncells;
+        if( n == 0 )
+        {
+            L.type = P<uint8_t>( s->flag );
+            L.code = P<uint16_t>( s->code );
+            L.r = nullptr;
+        }
+        else
+        {
+            BORA_TRY( grow( s->mg_type[n], ncells + 16, false, s->st ) );
+            BORA_TRY( grow( s->mg_code[n], ncells * 2 + 16, false, s->st ) );
+            BORA_TRY( grow( s->mg_r[n], ncells * 2 + 16, false, s->st ) );
+            L.type = P<uint8_t>( s->mg_type[n] );
+            L.code = P<uint16_t>( s->mg_code[n] );
+            L.r = P<__half>( s->mg_r[n] );
+        }
+        BORA_TRY( grow( s->mg_z0[n], ncells * 2 + 16, false, s->st ) );
+        BORA_TRY( grow( s->mg_z1[n], ncells * 2 + 16, false, s->st ) );
+        L.z0 = P<__half>( s->mg_z0[n] );
+        L.z1 = P<__half>( s->mg_z1[n] );
+        ++n;
+        return BORA_OK;
+    };
+    auto half_up = []( int v ) { return ( v + 1 ) / 2; };
+    BORA_TRYS( add( 0, 8, nt * 512, 0, 0, 0 ) );
+    for( int E = 4; E >= 1; E /= 2 )
+    {
+        ex = half_up( ex ); ey = half_up( ey ); ez = half_up( ez );
+        BORA_TRYS( add( 0, E, nt * (size_t)E * E * E, 0, 0, 0 ) );
+        if( s->levels[n - 1].ncells <= 512 ) { s->nlevels = n; return BORA_OK; }
+    }
+    // level 3 has one cell per tile; its extent is the tile grid
+    while( true )
+    {
+        ex = half_up( ex ); ey = half_up( ey ); ez = half_up( ez );
+        BORA_TRYS( add( 1, 0, (size_t)ex * ey * ez, ex, ey, ez ) );
+        if( s->levels[n - 1].ncells <= 512 ) break;
+    }
+    s->nlevels = n;
+    return BORA_OK;
+}
+
 int stage_build_system( bora_flip_sim* s )
 {
-    KTimer t( s, BORA_KERNEL_RHS, s->ntiles > 0 ? 2 : 0 );
+    KTimer t( s, BORA_KERNEL_RHS, s->ntiles > 0 ? 1 : 0 );
     bora_launch_rhs( s->g, s->ntiles, s->tiles(), s->cells(), s->st );
-    bora_launch_mic_factor( s->g, s->ntiles, P<uint16_t>( s->code ), P<float>( s->sminv ), s->st );
+    if( s->ntiles <= 0 ) return check_launch( s );
+    if( s->prm.solver == BORA_SOLVER_MIXED )
+    {
+        BORA_TRYS( build_hierarchy( s ) );
+        s->stats.kernel_launches += 2 * (uint64_t)( s->nlevels - 1 );
+        bora_mg_setup( s->g, s->levels, s->nlevels, s->tiles(), P<uint32_t>( s->counters ) + 5, s->st );
+    }
+    else
+    {
+        s->stats.kernel_launches += 1;
+        bora_launch_mic_factor( s->g, s->ntiles, P<uint16_t>( s->code ), P<float>( s->sminv ), s->st );
+    }
     return check_launch( s );
 }
 
@@ -448,8 +521,23 @@ int stage_solve( bora_flip_sim* s )
         if( passes >= std::max( 1, p.max_refinements ) ) break;
         // inner FP32 PCG on A e = r
         const double target = norm_ok ? 0.1 * rnorm : std::max( p.inner_tolerance * rnorm, 0.25 * p.tolerance * bnorm );
+        const bool mixed = p.solver == BORA_SOLVER_MIXED;
+        const int vlaunch = 4 * ( s->nlevels - 1 ) + 1;
+        auto precondition = [&]( int rr_slot, int rz_slot ) {
+            KTimer t( s, BORA_KERNEL_MG, vlaunch );
+            bora_mg_vcycle( s->g, s->levels, s->nlevels, s->tiles(), sv.r, sv.z, red, rr_slot, rz_slot, 64, st );
+        };
         int rz_cur = s->slot(), rr_cur = s->slot();
-        { KTimer t( s, BORA_KERNEL_PCG_UPDATE, 1 ); bora_launch_pcg_update( s->ntiles, code, sv, 0, red, -1, -1, rz_cur, rr_cur, st ); }
+        if( mixed )
+        {
+            { KTimer t( s, BORA_KERNEL_PCG_UPDATE, 1 ); bora_launch_pcg_update_noprec( s->ntiles, sv, 0, red, -1, -1, rr_cur, st ); }
+            precondition( rr_cur, rz_cur );
+        }
+        else
+        {
+            KTimer t( s, BORA_KERNEL_PCG_UPDATE, 1 );
+            bora_launch_pcg_update( s->ntiles, code, sv, 0, red, -1, -1, rz_cur, rr_cur, st );
+        }
         int rz_prev = -1, dsel = 0, it = 0;
         while( it < max_inner )
         {
@@ -457,7 +545,16 @@ int stage_solve( bora_flip_sim* s )
             { KTimer t( s, BORA_KERNEL_PCG_DIRECTION, 1 ); bora_launch_pcg_direction( s->g, s->ntiles, s->tiles(), code, sv, dsel, red, rz_cur, rz_prev, s_dq, st ); }
             dsel ^= 1;
             const int rz_new = s->slot(), rr_new = s->slot();
-            { KTimer t( s, BORA_KERNEL_PCG_UPDATE, 1 ); bora_launch_pcg_update( s->ntiles, code, sv, dsel, red, rz_cur, s_dq, rz_new, rr_new, st ); }
+            if( mixed )
+            {
+                { KTimer t( s, BORA_KERNEL_PCG_UPDATE, 1 ); bora_launch_pcg_update_noprec( s->ntiles, sv, dsel, red, rz_cur, s_dq, rr_new, st ); }
+                precondition( rr_new, rz_new );
+            }
+            else
+            {
+                KTimer t( s, BORA_KERNEL_PCG_UPDATE, 1 );
+                bora_launch_pcg_update( s->ntiles, code, sv, dsel, red, rz_cur, s_dq, rz_new, rr_new, st );
+            }
             rz_prev = rz_cur;
             rz_cur = rz_new;
             rr_cur = rr_new;
@@ -588,7 +685,7 @@ static int validate_params( const bora_flip_params* p )
 {
     if( !p ) return BORA_ERR_INVALID_ARG;
     if( p->enable_curl ) return BORA_ERR_INVALID_ARG;  // curl noise is outside this library
-    if( p->solver != BORA_SOLVER_PLAIN ) return BORA_ERR_INVALID_ARG;
+    if( p->solver != BORA_SOLVER_PLAIN && p->solver != BORA_SOLVER_MIXED ) return BORA_ERR_INVALID_ARG;
     if( !( p->voxel_size > 0.f ) || !( p->tolerance > 0.0 ) ) return BORA_ERR_INVALID_ARG;
     return BORA_OK;
 }
@@ -652,6 +749,11 @@ int bora_flip_destroy( bora_flip_handle s )
     for( DevBuf* b : all ) release( *b );
     for( int b = 0; b < 2; ++b )
         for( int a = 0; a < 7; ++a ) release( s->pbuf[b][a] );
+    for( int l = 0; l < bora_flip_sim::kMaxLevels; ++l )
+    {
+        release( s->mg_type[l] ); release( s->mg_code[l] ); release( s->mg_r[l] );
+        release( s->mg_z0[l] ); release( s->mg_z1[l] );
+    }
     s->prof_resolve();
     for( cudaEvent_t e : s->evpool ) cudaEventDestroy( e );
     for( int q = 0; q < 2; ++q )

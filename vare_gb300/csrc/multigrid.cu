@@ -1,0 +1,644 @@
+// Geometric multigrid V-cycle preconditioner for the pressure PCG, with FP16 storage
+// and FP32 arithmetic (the mixed-precision form of the projection).
+//
+// The reference's pressure solve is unpreconditioned FP32 CG
+// (base/source/LinearSystemSolver.cpp:12-50); its only preconditioner is a serial MIC(0)
+// (base/source/BLAS.cu:211-331). This V-cycle replaces both for the mixed form.
+//
+// Hierarchy: level 0 is the fine grid of active 8^3 tiles; levels 1..3 keep the tile
+// layout with 4^3, 2^3 and 1 cell per tile (neighbours across tiles through the tile
+// neighbour table); levels >= 4 are small dense grids over the tile grid halved per
+// level. A coarse cell is fluid if any child is fluid, else air if any child is air
+// (inactive tiles count as air), else solid. Every level applies the reference's
+// 7-point rule (diagonal 6 + #air - #solid/wall, -1 per fluid neighbour,
+// FluidProjection.cu:234-244) to its own cell types; coarse operators are the
+// rediscretisation with spacing 2^l, i.e. the same stencil divided by 4^l.
+//
+// All quantities are kept in "stencil units" (the level equation S z = r' with
+// S = diag*z - sum of fluid neighbours): restriction averages the children's residuals
+// and multiplies by 4, prolongation injects the coarse correction. Smoothing is damped
+// Jacobi (omega = 0.8), two sweeps before and after; the coarsest level (<= 512 cells)
+// is smoothed in one CTA. Level residuals and corrections are stored as FP16: the fine
+// residual is scaled by 1/||r||_2 on entry so every stored value is O(1).
+#include <algorithm>
+
+#include <cuda_fp16.h>
+
+#include "bora_internal.h"
+#include "reduce.cuh"
+
+namespace {
+
+constexpr float kOmega = 0.8f;
+
+__device__ inline int code_diag( uint16_t c ) { return ( c >> 8 ) & 15; }
+
+// Index of the face neighbour q (0:-x 1:+x 2:-y 3:+y 4:-z 5:+z) of a cell on level L,
+// or -1 when it lies in an inactive tile / beyond the stored grid.
+struct LevelNav
+{
+    BoraLevelDev L;
+    const int32_t* nbr;      // tile neighbour table (tiled levels)
+    const int32_t* tile_of;  // slot -> virtual tile (tiled levels)
+    int tx, ty;              // tile grid (tiled levels)
+
+    __device__ inline void coords( long long cell, int& i, int& j, int& k ) const
+    {
+        if( L.kind == 1 )
+        {
+            i = (int)( cell % L.dx );
+            j = (int)( ( cell / L.dx ) % L.dy );
+            k = (int)( cell / ( (long long)L.dx * L.dy ) );
+            return;
+        }
+        const int E = L.E, E3 = E * E * E;
+        const int s = (int)( cell / E3 ), loc = (int)( cell % E3 );
+        const int vt = tile_of[s];
+        i = ( vt % tx ) * E + loc % E;
+        j = ( ( vt / tx ) % ty ) * E + ( loc / E ) % E;
+        k = ( vt / ( tx * ty ) ) * E + loc / ( E * E );
+    }
+    __device__ inline bool real( int i, int j, int k ) const { return i < L.nx && j < L.ny && k < L.nz; }
+
+    // neighbour cell index, -1 inactive/outside storage; *edge = true beyond the domain
+    __device__ inline long long nbr_index( long long cell, int i, int j, int k, int q, bool* edge ) const
+    {
+        const int di = q == 0 ? -1 : ( q == 1 ? 1 : 0 );
+        const int dj = q == 2 ? -1 : ( q == 3 ? 1 : 0 );
+        const int dk = q == 4 ? -1 : ( q == 5 ? 1 : 0 );
+        const int a = i + di, b = j + dj, c = k + dk;
+        *edge = ( a < 0 || b < 0 || c < 0 || a >= L.nx || b >= L.ny || c >= L.nz );
+        if( *edge ) return -1;
+        if( L.kind == 1 ) return (long long)a + (long long)L.dx * ( b + (long long)L.dy * c );
+        const int E = L.E, E3 = E * E * E;
+        const int s = (int)( cell / E3 );
+        const int la = ( ( i % E ) + di ), lb = ( ( j % E ) + dj ), lc = ( ( k % E ) + dk );
+        if( la >= 0 && la < E && lb >= 0 && lb < E && lc >= 0 && lc < E )
+            return (long long)s * E3 + la + E * ( lb + E * lc );
+        const int ox = la < 0 ? -1 : ( la >= E ? 1 : 0 );
+        const int oy = lb < 0 ? -1 : ( lb >= E ? 1 : 0 );
+        const int oz = lc < 0 ? -1 : ( lc >= E ? 1 : 0 );
+        const int ns = nbr[(size_t)s * 27 + bora_dir( ox, oy, oz )];
+        if( ns < 0 ) return -1;
+        const int wa = ( la + E ) % E, wb = ( lb + E ) % E, wc = ( lc + E ) % E;
+        return (long long)ns * E3 + wa + E * ( wb + E * wc );
+    }
+};
+
+// ---- set-up: cell types and stencil codes of coarse levels ---------------------------
+
+// Types of level `C` from level `F` (one finer). C tiled with E_C = E_F / 2 (children in
+// the same tile), or C dense: children are the finer level's cells (dense) or tiles
+// (F tiled with E = 1, through slot_of).
+__global__ void k_mg_types( BoraLevelDev F, BoraLevelDev C, const int32_t* __restrict__ slot_of,
+                            const int32_t* __restrict__ tile_of, int tx, int ty, int tz )
+{
+    for( long long cell = blockIdx.x * (long long)blockDim.x + threadIdx.x; cell < (long long)C.ncells;
+         cell += (long long)gridDim.x * blockDim.x )
+    {
+        int i, j, k;
+        if( C.kind == 1 )
+        {
+            i = (int)( cell % C.dx ); j = (int)( ( cell / C.dx ) % C.dy ); k = (int)( cell / ( (long long)C.dx * C.dy ) );
+        }
+        else
+        {
+            const int E = C.E, E3 = E * E * E;
+            const int s = (int)( cell / E3 ), loc = (int)( cell % E3 );
+            const int vt = tile_of[s];
+            i = ( vt % tx ) * E + loc % E;
+            j = ( ( vt / tx ) % ty ) * E + ( loc / E ) % E;
+            k = ( vt / ( tx * ty ) ) * E + loc / ( E * E );
+        }
+        if( i >= C.nx || j >= C.ny || k >= C.nz ) { C.type[cell] = BORA_MASKED; continue; }
+        bool anyF = false, anyA = false;
+        for( int o = 0; o < 8; ++o )
+        {
+            const int a = 2 * i + ( o & 1 ), b = 2 * j + ( ( o >> 1 ) & 1 ), c = 2 * k + ( o >> 2 );
+            if( a >= F.nx || b >= F.ny || c >= F.nz ) continue;  // beyond the finer grid: wall-like
+            uint8_t t;
+            if( C.kind == 0 )
+            {
+                const int E = F.E;
+                const int s = (int)( cell / ( C.E * C.E * C.E ) );
+                t = F.type[(long long)s * E * E * E + ( a % E ) + E * ( ( b % E ) + E * ( c % E ) )];
+            }
+            else if( F.kind == 1 )
+            {
+                t = F.type[(long long)a + (long long)F.dx * ( b + (long long)F.dy * c )];
+            }
+            else  // F tiled with one cell per tile: children are tiles
+            {
+                if( a >= tx || b >= ty || c >= tz ) continue;
+                const int s = slot_of[( (size_t)c * ty + b ) * tx + a];
+                t = s < 0 ? (uint8_t)BORA_AIR : F.type[s];
+            }
+            if( t == BORA_FLUID ) anyF = true;
+            else if( t == BORA_AIR ) anyA = true;
+        }
+        C.type[cell] = anyF ? BORA_FLUID : ( anyA ? BORA_AIR : BORA_SOLID );
+    }
+}
+
+// Stencil codes of level L from its types (same bit layout as the fine code).
+__global__ void k_mg_codes( LevelNav nav, float voxel_wall )
+{
+    const BoraLevelDev& L = nav.L;
+    for( long long cell = blockIdx.x * (long long)blockDim.x + threadIdx.x; cell < (long long)L.ncells;
+         cell += (long long)gridDim.x * blockDim.x )
+    {
+        if( L.type[cell] != BORA_FLUID ) { L.code[cell] = 0; continue; }
+        int i, j, k;
+        nav.coords( cell, i, j, k );
+        // FluidProjection.cu:208 evaluated at the cell's lowest fine row
+        const int wall = (float)( j << L.level ) + 0.5f <= voxel_wall + 1.f ? BORA_WALL : BORA_AIR;
+        int diag = 6;
+        uint32_t mask = 0;
+        for( int q = 0; q < 6; ++q )
+        {
+            bool edge;
+            const long long n = nav.nbr_index( cell, i, j, k, q, &edge );
+            int t = edge ? wall : ( n < 0 ? BORA_AIR : (int)L.type[n] );
+            if( t == BORA_MASKED ) t = BORA_SOLID;
+            if( t == BORA_AIR ) diag += 1;
+            else if( t == BORA_SOLID || t == BORA_WALL ) diag -= 1;
+            else if( t == BORA_FLUID ) mask |= 1u << q;
+        }
+        L.code[cell] = (uint16_t)( BORA_CODE_FLUID | ( (uint32_t)diag << 8 ) | mask );
+    }
+}
+
+// ---- V-cycle -----------------------------------------------------------------------
+//
+// Navigation is specialised per level kind: tiled levels use the tile edge E as a
+// compile-time constant (bit arithmetic, neighbours across tiles through the tile
+// neighbour table), dense levels use their small extents. Kernels only visit the
+// neighbours that the stencil code marks as fluid, which always exist.
+
+__device__ inline float scale_of( const double* ring, int slot )
+{
+    const double rr = ring[slot];
+    return rr > 0.0 ? (float)( 1.0 / sqrt( rr ) ) : 1.f;
+}
+
+template <int E>
+struct TiledNav
+{
+    static constexpr int LE = E == 8 ? 3 : ( E == 4 ? 2 : ( E == 2 ? 1 : 0 ) );
+    static constexpr int E3 = E * E * E;
+    const int32_t* nbr;
+    // dense parent level (E == 1 only)
+    const int32_t* tile_of;
+    int tx, ty, cdx, cdy;
+
+    __device__ inline long long nb( long long cell, int q ) const
+    {
+        const long long s = cell >> ( 3 * LE );
+        const int l = (int)( cell & ( E3 - 1 ) );
+        const int li = l & ( E - 1 ), lj = ( l >> LE ) & ( E - 1 ), lk = l >> ( 2 * LE );
+        int dir, ll;
+        switch( q )
+        {
+            case 0: if( li > 0 ) return cell - 1; dir = 12; ll = l + ( E - 1 ); break;
+            case 1: if( li < E - 1 ) return cell + 1; dir = 14; ll = l - ( E - 1 ); break;
+            case 2: if( lj > 0 ) return cell - E; dir = 10; ll = l + E * ( E - 1 ); break;
+            case 3: if( lj < E - 1 ) return cell + E; dir = 16; ll = l - E * ( E - 1 ); break;
+            case 4: if( lk > 0 ) return cell - E * E; dir = 4; ll = l + E * E * ( E - 1 ); break;
+            default: if( lk < E - 1 ) return cell + E * E; dir = 22; ll = l - E * E * ( E - 1 ); break;
+        }
+        const int ns = nbr[s * 27 + dir];
+        return ns < 0 ? -1 : (long long)ns * E3 + ll;
+    }
+    // parent on the next coarser level: same tile with edge E/2, or (E == 1) a dense cell
+    __device__ inline long long parent( long long cell ) const
+    {
+        const long long s = cell >> ( 3 * LE );
+        const int l = (int)( cell & ( E3 - 1 ) );
+        if( E > 1 )
+        {
+            constexpr int H = E > 1 ? E / 2 : 1;
+            const int li = l & ( E - 1 ), lj = ( l >> LE ) & ( E - 1 ), lk = l >> ( 2 * LE );
+            return s * ( H * H * H ) + ( li >> 1 ) + H * ( ( lj >> 1 ) + H * ( lk >> 1 ) );
+        }
+        const int vt = tile_of[s];
+        const int ti = vt % tx, tj = ( vt / tx ) % ty, tk = vt / ( tx * ty );
+        return (long long)( ti >> 1 ) + (long long)cdx * ( ( tj >> 1 ) + (long long)cdy * ( tk >> 1 ) );
+    }
+};
+
+struct DenseNav
+{
+    int dx, dy, dz;   // storage extent = cells inside the domain
+    int cdx, cdy;     // coarser dense level
+    __device__ inline long long nb( long long cell, int q ) const
+    {
+        const int i = (int)( cell % dx ), j = (int)( ( cell / dx ) % dy ), k = (int)( cell / ( (long long)dx * dy ) );
+        switch( q )
+        {
+            case 0: return i > 0 ? cell - 1 : -1;
+            case 1: return i < dx - 1 ? cell + 1 : -1;
+            case 2: return j > 0 ? cell - dx : -1;
+            case 3: return j < dy - 1 ? cell + dx : -1;
+            case 4: return k > 0 ? cell - (long long)dx * dy : -1;
+            default: return k < dz - 1 ? cell + (long long)dx * dy : -1;
+        }
+    }
+    __device__ inline long long parent( long long cell ) const
+    {
+        const int i = (int)( cell % dx ), j = (int)( ( cell / dx ) % dy ), k = (int)( cell / ( (long long)dx * dy ) );
+        return (long long)( i >> 1 ) + (long long)cdx * ( ( j >> 1 ) + (long long)cdy * ( k >> 1 ) );
+    }
+};
+
+// Level residual r' of a cell: level 0 reads the PCG residual (FP32) times the scale,
+// coarser levels read their FP16 residual.
+struct RIn
+{
+    const float* r0;
+    float s;
+    const __half* rh;
+    __device__ inline float operator()( long long c ) const { return r0 ? r0[c] * s : __half2float( rh[c] ); }
+};
+
+__device__ inline float ldh( const __half* z, long long c ) { return __half2float( z[c] ); }
+
+// z = two damped-Jacobi sweeps from zero: z1 = w r'/d, z2 = z1 + w (r' - S z1)/d, with
+// each neighbour's z1 recomputed from its own r' and diagonal.
+template <class Nav>
+__global__ void __launch_bounds__( 256 ) k_mg_smooth0( Nav nav, BoraLevelDev L, const float* __restrict__ r0,
+                                                       int slot_rr, const double* __restrict__ ring, uint32_t* err )
+{
+    __shared__ float s_scale;
+    if( threadIdx.x == 0 ) s_scale = r0 ? scale_of( ring, slot_rr ) : 1.f;
+    __syncthreads();
+    const RIn R{ r0, s_scale, L.r };
+    for( long long cell = blockIdx.x * (long long)blockDim.x + threadIdx.x; cell < (long long)L.ncells;
+         cell += (long long)gridDim.x * blockDim.x )
+    {
+        const uint16_t cc = L.code[cell];
+        float z2 = 0.f;
+        const int dg = code_diag( cc );
+        if( ( cc & BORA_CODE_FLUID ) && dg > 0 )
+        {
+            const float rc = R( cell );
+            const float z1 = kOmega * rc / (float)dg;
+            float sum = 0.f;
+#pragma unroll
+            for( int q = 0; q < 6; ++q )
+            {
+                if( !( cc & ( 1u << q ) ) ) continue;
+                const long long n = nav.nb( cell, q );
+                if( n < 0 ) { atomicOr( err, 4u ); continue; }
+                const int dn = code_diag( L.code[n] );
+                if( dn > 0 ) sum += kOmega * R( n ) / (float)dn;
+            }
+            z2 = z1 + kOmega * ( rc - ( (float)dg * z1 - sum ) ) / (float)dg;
+        }
+        L.z0[cell] = __float2half_rn( z2 );
+    }
+}
+
+// Restriction, one thread per (coarse cell, child): each thread forms its child's
+// residual r' - S z (z = the pre-smoothed z0), the 8 lanes of a coarse cell add up by
+// shuffles, and r'_C = 4 * mean = 0.5 * sum. Child enumeration:
+//   mode 0: C tiled (edge EC), F tiled (edge 2 EC) in the same tile;
+//   mode 1: C dense, F tiled with one cell per tile (children are tiles, via slot_of);
+//   mode 2: C dense, F dense.
+template <class FNav, int MODE, int EC>
+__global__ void __launch_bounds__( 256 ) k_mg_restrict( FNav fnav, BoraLevelDev F, BoraLevelDev C,
+                                                        const float* __restrict__ r0, int slot_rr,
+                                                        const double* __restrict__ ring,
+                                                        const int32_t* __restrict__ slot_of, int tx, int ty, int tz,
+                                                        uint32_t* err )
+{
+    __shared__ float s_scale;
+    if( threadIdx.x == 0 ) s_scale = r0 ? scale_of( ring, slot_rr ) : 1.f;
+    __syncthreads();
+    const RIn R{ r0, s_scale, F.r };
+    const long long total = (long long)C.ncells * 8;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    // every lane of a warp runs the same number of iterations (total and stride are multiples of 8 / 32)
+    const long long tround = ( total + 31 ) & ~31LL;
+    for( long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tround; t += stride )
+    {
+        const long long pc = t >> 3;
+        const int o = (int)( t & 7 );
+        float res = 0.f;
+        if( t < total && ( C.code[pc] & BORA_CODE_FLUID ) )
+        {
+            long long fc = -1;
+            if( MODE == 0 )
+            {
+                constexpr int LC = EC == 4 ? 2 : ( EC == 2 ? 1 : 0 );
+                constexpr int EF = 2 * EC;
+                const long long s = pc >> ( 3 * LC );
+                const int l = (int)( pc & ( EC * EC * EC - 1 ) );
+                const int ci = l & ( EC - 1 ), cj = ( l >> LC ) & ( EC - 1 ), ck = l >> ( 2 * LC );
+                fc = s * ( EF * EF * EF ) + ( 2 * ci + ( o & 1 ) ) + EF * ( ( 2 * cj + ( ( o >> 1 ) & 1 ) ) +
+                                                                           EF * ( 2 * ck + ( o >> 2 ) ) );
+                int a = 0;  // children beyond the domain are masked cells: their code is 0
+                (void)a;
+            }
+            else
+            {
+                const int I = (int)( pc % C.dx ), J = (int)( ( pc / C.dx ) % C.dy ), K = (int)( pc / ( (long long)C.dx * C.dy ) );
+                const int a = 2 * I + ( o & 1 ), b = 2 * J + ( ( o >> 1 ) & 1 ), c = 2 * K + ( o >> 2 );
+                if( MODE == 1 )
+                {
+                    if( a < tx && b < ty && c < tz ) fc = slot_of[( (size_t)c * ty + b ) * tx + a];
+                }
+                else if( a < F.dx && b < F.dy && c < F.dz )
+                {
+                    fc = (long long)a + (long long)F.dx * ( b + (long long)F.dy * c );
+                }
+            }
+            if( fc >= 0 )
+            {
+                const uint16_t cf = F.code[fc];
+                if( cf & BORA_CODE_FLUID )
+                {
+                    float sum = 0.f;
+#pragma unroll
+                    for( int q = 0; q < 6; ++q )
+                    {
+                        if( !( cf & ( 1u << q ) ) ) continue;
+                        const long long n = fnav.nb( fc, q );
+                        if( n < 0 ) { atomicOr( err, 8u ); continue; }
+                        sum += ldh( F.z0, n );
+                    }
+                    res = R( fc ) - ( (float)code_diag( cf ) * ldh( F.z0, fc ) - sum );
+                }
+            }
+        }
+        res += __shfl_xor_sync( 0xffffffffu, res, 1 );
+        res += __shfl_xor_sync( 0xffffffffu, res, 2 );
+        res += __shfl_xor_sync( 0xffffffffu, res, 4 );
+        if( t < total && o == 0 ) C.r[pc] = __float2half_rn( 0.5f * res );
+    }
+}
+
+// Coarsest level (<= 512 cells): Jacobi sweeps from zero in one CTA, in shared memory.
+template <class Nav>
+__global__ void __launch_bounds__( 512 ) k_mg_coarsest( Nav nav, BoraLevelDev L, int sweeps, uint32_t* err )
+{
+    __shared__ float zs[2][512], rs[512];
+    __shared__ int16_t nbs[512][6];
+    const int c = threadIdx.x;
+    const bool valid = c < (int)L.ncells;
+    uint16_t cc = 0;
+    if( valid )
+    {
+        cc = L.code[c];
+        rs[c] = __half2float( L.r[c] );
+        for( int q = 0; q < 6; ++q )
+        {
+            long long n = -1;
+            if( cc & ( 1u << q ) )
+            {
+                n = nav.nb( c, q );
+                if( n < 0 || n >= (long long)L.ncells ) { atomicOr( err, 16u ); n = -1; }
+            }
+            nbs[c][q] = (int16_t)n;
+        }
+    }
+    zs[0][c] = 0.f;
+    zs[1][c] = 0.f;
+    __syncthreads();
+    int cur = 0;
+    const int dg = code_diag( cc );
+    const bool act = valid && ( cc & BORA_CODE_FLUID ) && dg > 0;
+    for( int it = 0; it < sweeps; ++it )
+    {
+        float zn = 0.f;
+        if( act )
+        {
+            float sum = 0.f;
+            for( int q = 0; q < 6; ++q )
+                if( nbs[c][q] >= 0 ) sum += zs[cur][nbs[c][q]];
+            const float z = zs[cur][c];
+            zn = z + kOmega * ( rs[c] - ( (float)dg * z - sum ) ) / (float)dg;
+        }
+        zs[cur ^ 1][c] = zn;
+        __syncthreads();
+        cur ^= 1;
+    }
+    if( valid ) L.z0[c] = __float2half_rn( zs[cur][c] );
+}
+
+// z_a = z0 + P e (injection of the coarse correction C.z0), then one Jacobi sweep;
+// neighbours' z_a are formed the same way. Writes z1.
+template <class Nav>
+__global__ void __launch_bounds__( 256 ) k_mg_prolong_smooth( Nav nav, BoraLevelDev F, const __half* __restrict__ ec,
+                                                              const float* __restrict__ r0, int slot_rr,
+                                                              const double* __restrict__ ring, uint32_t* err )
+{
+    __shared__ float s_scale;
+    if( threadIdx.x == 0 ) s_scale = r0 ? scale_of( ring, slot_rr ) : 1.f;
+    __syncthreads();
+    const RIn R{ r0, s_scale, F.r };
+    for( long long cell = blockIdx.x * (long long)blockDim.x + threadIdx.x; cell < (long long)F.ncells;
+         cell += (long long)gridDim.x * blockDim.x )
+    {
+        const uint16_t cc = F.code[cell];
+        float zb = 0.f;
+        const int dg = code_diag( cc );
+        if( ( cc & BORA_CODE_FLUID ) && dg > 0 )
+        {
+            const float za = ldh( F.z0, cell ) + ldh( ec, nav.parent( cell ) );
+            float sum = 0.f;
+#pragma unroll
+            for( int q = 0; q < 6; ++q )
+            {
+                if( !( cc & ( 1u << q ) ) ) continue;
+                const long long n = nav.nb( cell, q );
+                if( n < 0 ) { atomicOr( err, 32u ); continue; }
+                sum += ldh( F.z0, n ) + ldh( ec, nav.parent( n ) );
+            }
+            zb = za + kOmega * ( R( cell ) - ( (float)dg * za - sum ) ) / (float)dg;
+        }
+        F.z1[cell] = __float2half_rn( zb );
+    }
+}
+
+// Final Jacobi sweep of a level: z = z1 + w (r' - S z1)/d, written to z0. On level 0 the
+// result is unscaled to FP32 into zout and r.z is accumulated (double-float, FP64 per warp).
+template <class Nav>
+__global__ void __launch_bounds__( 256 ) k_mg_smooth_last( Nav nav, BoraLevelDev L, const float* __restrict__ r0,
+                                                           int slot_rr, BoraReduceDev red, float* __restrict__ zout,
+                                                           int slot_rz )
+{
+    __shared__ float s_scale;
+    if( threadIdx.x == 0 ) s_scale = r0 ? scale_of( red.ring, slot_rr ) : 1.f;
+    __syncthreads();
+    const float sc = s_scale;
+    const RIn R{ r0, sc, L.r };
+    DF rz{ 0.f, 0.f };
+    for( long long cell = blockIdx.x * (long long)blockDim.x + threadIdx.x; cell < (long long)L.ncells;
+         cell += (long long)gridDim.x * blockDim.x )
+    {
+        const uint16_t cc = L.code[cell];
+        float zc = 0.f;
+        const int dg = code_diag( cc );
+        if( ( cc & BORA_CODE_FLUID ) && dg > 0 )
+        {
+            const float zb = ldh( L.z1, cell );
+            float sum = 0.f;
+#pragma unroll
+            for( int q = 0; q < 6; ++q )
+            {
+                if( !( cc & ( 1u << q ) ) ) continue;
+                const long long n = nav.nb( cell, q );
+                if( n < 0 ) { atomicOr( red.err, 64u ); continue; }
+                sum += ldh( L.z1, n );
+            }
+            zc = zb + kOmega * ( R( cell ) - ( (float)dg * zb - sum ) ) / (float)dg;
+        }
+        if( zout )
+        {
+            const float zf = zc / sc;  // undo the FP16 scaling of the residual
+            zout[cell] = zf;
+            if( cc & BORA_CODE_FLUID ) rz = df_add( rz, df_prod( r0[cell], zf ) );
+        }
+        else
+        {
+            L.z0[cell] = __float2half_rn( zc );
+        }
+    }
+    if( zout ) reduce2_publish_warp( df_warp_sum( rz ), 0.0, 0, red, slot_rz, -1 );
+}
+
+// PCG update without a preconditioner sweep: e += alpha d; r -= alpha q; r.r.
+__global__ void __launch_bounds__( 256 ) k_pcg_update_noprec( size_t ncells, BoraSolverDev sv, int dsel, BoraReduceDev red,
+                                                              int slot_rz, int slot_dq, int slot_rr_out )
+{
+    __shared__ float s_alpha;
+    if( threadIdx.x == 0 ) s_alpha = slot_rz < 0 ? 0.f : (float)( red.ring[slot_rz] / red.ring[slot_dq] );
+    __syncthreads();
+    const float alpha = s_alpha;
+    const float* __restrict__ d = sv.d[dsel];
+    DF rr{ 0.f, 0.f };
+    const size_t n4 = ncells / 4;
+    for( size_t v = blockIdx.x * (size_t)blockDim.x + threadIdx.x; v < n4; v += (size_t)gridDim.x * blockDim.x )
+    {
+        float4 e = reinterpret_cast<const float4*>( sv.e )[v];
+        float4 r = reinterpret_cast<const float4*>( sv.r )[v];
+        const float4 dv = reinterpret_cast<const float4*>( d )[v];
+        const float4 q = reinterpret_cast<const float4*>( sv.q )[v];
+        e.x = fmaf( alpha, dv.x, e.x ); e.y = fmaf( alpha, dv.y, e.y ); e.z = fmaf( alpha, dv.z, e.z ); e.w = fmaf( alpha, dv.w, e.w );
+        r.x = fmaf( -alpha, q.x, r.x ); r.y = fmaf( -alpha, q.y, r.y ); r.z = fmaf( -alpha, q.z, r.z ); r.w = fmaf( -alpha, q.w, r.w );
+        reinterpret_cast<float4*>( sv.e )[v] = e;
+        reinterpret_cast<float4*>( sv.r )[v] = r;
+        rr = df_add( rr, df_prod( r.x, r.x ) ); rr = df_add( rr, df_prod( r.y, r.y ) );
+        rr = df_add( rr, df_prod( r.z, r.z ) ); rr = df_add( rr, df_prod( r.w, r.w ) );
+    }
+    reduce2_publish_warp( df_warp_sum( rr ), 0.0, 0, red, slot_rr_out, -1 );
+}
+
+int g_sms = 0;
+int blocks_for( size_t n )
+{
+    if( g_sms <= 0 )
+    {
+        int dev = 0;
+        cudaGetDevice( &dev );
+        cudaDeviceGetAttribute( &g_sms, cudaDevAttrMultiProcessorCount, dev );
+        if( g_sms <= 0 ) g_sms = 152;
+    }
+    return (int)std::max<size_t>( 1, std::min<size_t>( ( n + 255 ) / 256, (size_t)g_sms * 8 ) );
+}
+
+LevelNav nav_of( const BoraGridDev& g, const BoraLevelDev& L, BoraTilesDev t )
+{
+    return LevelNav{ L, t.nbr, t.tile_of, g.tx, g.ty };
+}
+
+}  // namespace
+
+void bora_mg_setup( const BoraGridDev& g, BoraLevelDev* levels, int nlevels, BoraTilesDev t, uint32_t* err, cudaStream_t st )
+{
+    (void)err;
+    for( int l = 1; l < nlevels; ++l )
+    {
+        const BoraLevelDev& F = levels[l - 1];
+        const BoraLevelDev& C = levels[l];
+        k_mg_types<<<blocks_for( C.ncells ), 256, 0, st>>>( F, C, t.slot_of, t.tile_of, g.tx, g.ty, g.tz );
+        k_mg_codes<<<blocks_for( C.ncells ), 256, 0, st>>>( nav_of( g, C, t ), g.voxel_wall );
+    }
+}
+
+namespace {
+
+TiledNav<8> tnav8( BoraTilesDev t ) { return TiledNav<8>{ t.nbr, t.tile_of, 0, 0, 0, 0 }; }
+
+// Launch a level-templated kernel with the navigation of level l.
+template <class F>
+void with_nav( const BoraGridDev& g, const BoraLevelDev* levels, int nlevels, int l, BoraTilesDev t, F&& f )
+{
+    const BoraLevelDev& L = levels[l];
+    const int cdx = l + 1 < nlevels ? levels[l + 1].dx : 0;
+    const int cdy = l + 1 < nlevels ? levels[l + 1].dy : 0;
+    if( L.kind == 1 ) { f( DenseNav{ L.dx, L.dy, L.dz, cdx, cdy } ); return; }
+    switch( L.E )
+    {
+        case 8: f( TiledNav<8>{ t.nbr, t.tile_of, g.tx, g.ty, cdx, cdy } ); break;
+        case 4: f( TiledNav<4>{ t.nbr, t.tile_of, g.tx, g.ty, cdx, cdy } ); break;
+        case 2: f( TiledNav<2>{ t.nbr, t.tile_of, g.tx, g.ty, cdx, cdy } ); break;
+        default: f( TiledNav<1>{ t.nbr, t.tile_of, g.tx, g.ty, cdx, cdy } ); break;
+    }
+}
+
+}  // namespace
+
+void bora_mg_vcycle( const BoraGridDev& g, const BoraLevelDev* levels, int nlevels, BoraTilesDev t, const float* r,
+                     float* z, BoraReduceDev red, int slot_rr, int slot_rz, int coarse_sweeps, cudaStream_t st )
+{
+    if( nlevels < 2 ) return;  // the caller always builds at least two levels
+    const int last = nlevels - 1;
+    // down: pre-smooth and restrict
+    for( int l = 0; l < last; ++l )
+    {
+        const BoraLevelDev& F = levels[l];
+        const BoraLevelDev& C = levels[l + 1];
+        const float* r0 = l == 0 ? r : nullptr;
+        with_nav( g, levels, nlevels, l, t, [&]( auto nav ) {
+            k_mg_smooth0<<<blocks_for( F.ncells ), 256, 0, st>>>( nav, F, r0, slot_rr, red.ring, red.err );
+            const int nb = blocks_for( C.ncells * 8 );
+            using N = decltype( nav );
+            if( C.kind == 1 )
+            {
+                if( F.kind == 1 )
+                    k_mg_restrict<N, 2, 1><<<nb, 256, 0, st>>>( nav, F, C, r0, slot_rr, red.ring, t.slot_of, g.tx, g.ty, g.tz, red.err );
+                else
+                    k_mg_restrict<N, 1, 1><<<nb, 256, 0, st>>>( nav, F, C, r0, slot_rr, red.ring, t.slot_of, g.tx, g.ty, g.tz, red.err );
+            }
+            else if( C.E == 4 )
+                k_mg_restrict<N, 0, 4><<<nb, 256, 0, st>>>( nav, F, C, r0, slot_rr, red.ring, t.slot_of, g.tx, g.ty, g.tz, red.err );
+            else if( C.E == 2 )
+                k_mg_restrict<N, 0, 2><<<nb, 256, 0, st>>>( nav, F, C, r0, slot_rr, red.ring, t.slot_of, g.tx, g.ty, g.tz, red.err );
+            else
+                k_mg_restrict<N, 0, 1><<<nb, 256, 0, st>>>( nav, F, C, r0, slot_rr, red.ring, t.slot_of, g.tx, g.ty, g.tz, red.err );
+        } );
+    }
+    with_nav( g, levels, nlevels, last, t, [&]( auto nav ) {
+        k_mg_coarsest<<<1, 512, 0, st>>>( nav, levels[last], coarse_sweeps, red.err );
+    } );
+    // up: prolong + smooth, then a last sweep
+    for( int l = last - 1; l >= 0; --l )
+    {
+        const BoraLevelDev& F = levels[l];
+        const float* r0 = l == 0 ? r : nullptr;
+        with_nav( g, levels, nlevels, l, t, [&]( auto nav ) {
+            k_mg_prolong_smooth<<<blocks_for( F.ncells ), 256, 0, st>>>( nav, F, levels[l + 1].z0, r0, slot_rr, red.ring,
+                                                                         red.err );
+            k_mg_smooth_last<<<blocks_for( F.ncells ), 256, 0, st>>>( nav, F, r0, slot_rr, red, l == 0 ? z : nullptr,
+                                                                      slot_rz );
+        } );
+    }
+}
+
+void bora_launch_pcg_update_noprec( int ntiles, BoraSolverDev s, int dsel, BoraReduceDev red, int slot_rz, int slot_dq,
+                                    int slot_rr_out, cudaStream_t st )
+{
+    const size_t nc = (size_t)ntiles * 512;
+    k_pcg_update_noprec<<<blocks_for( nc / 4 ), 256, 0, st>>>( nc, s, dsel, red, slot_rz, slot_dq, slot_rr_out );
+}

@@ -1,0 +1,134 @@
+// FP64-accurate, deterministic reductions shared by the solver kernels.
+#pragma once
+
+#include "bora_internal.h"
+
+namespace bora_reduce {
+
+// ---------------------------------------------------------------------------------
+// Double-float accumulation: GB300's FP64 pipe is ~1/64 of its FP32 rate, so per-cell
+// dot-product terms are accumulated as unevaluated float pairs (hi + lo) with the
+// error-free TwoProd (fmaf) and TwoSum transformations (Dekker 1971, Knuth TAOCP 4.2.2),
+// giving ~48 significant bits from FP32 instructions; each warp converts its pair to
+// FP64 once. This relies on -fmad=false (no contraction inside TwoSum).
+struct DF
+{
+    float hi, lo;
+};
+__device__ __forceinline__ DF df_prod( float a, float b )
+{
+    const float p = a * b;
+    return DF{ p, fmaf( a, b, -p ) };
+}
+__device__ __forceinline__ DF df_add( DF a, DF b )
+{
+    const float s = a.hi + b.hi;
+    const float bb = s - a.hi;
+    float err = ( a.hi - ( s - bb ) ) + ( b.hi - bb );
+    err += a.lo + b.lo;
+    const float h = s + err;
+    return DF{ h, err - ( h - s ) };
+}
+__device__ __forceinline__ double df_warp_sum( DF v )
+{
+#pragma unroll
+    for( int o = 16; o > 0; o >>= 1 )
+    {
+        DF w;
+        w.hi = __shfl_xor_sync( 0xffffffffu, v.hi, o );
+        w.lo = __shfl_xor_sync( 0xffffffffu, v.lo, o );
+        v = df_add( v, w );
+    }
+    return (double)v.hi + (double)v.lo;
+}
+__device__ __forceinline__ float warp_maxf( float v )
+{
+#pragma unroll
+    for( int o = 16; o > 0; o >>= 1 ) v = fmaxf( v, __shfl_xor_sync( 0xffffffffu, v, o ) );
+    return v;
+}
+
+// ---------------------------------------------------------------------------------
+// Deterministic FP64 block reduction published through a ring slot: every block writes
+// its partial, the last block to arrive sums the partials in block order.
+__device__ __forceinline__ double warp_sum( double v )
+{
+#pragma unroll
+    for( int o = 16; o > 0; o >>= 1 ) v += __shfl_xor_sync( 0xffffffffu, v, o );
+    return v;
+}
+__device__ __forceinline__ double warp_max( double v )
+{
+#pragma unroll
+    for( int o = 16; o > 0; o >>= 1 ) v = fmax( v, __shfl_xor_sync( 0xffffffffu, v, o ) );
+    return v;
+}
+
+// op1: 0 = sum, 1 = max for the second value. Slots < 0 are skipped. Inputs are the
+// per-warp totals (already reduced across the warp, valid in every lane).
+__device__ __forceinline__ void reduce2_publish_warp( double v0, double v1, int op1, BoraReduceDev red, int slot0, int slot1 )
+{
+    __shared__ double w0[32], w1[32];
+    __shared__ bool last;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = ( blockDim.x + 31 ) >> 5;
+    if( lane == 0 ) { w0[wid] = v0; w1[wid] = v1; }
+    __syncthreads();
+    if( threadIdx.x == 0 )
+    {
+        double a = 0.0, b = 0.0;
+        for( int q = 0; q < nw; ++q ) { a += w0[q]; b = op1 ? fmax( b, w1[q] ) : b + w1[q]; }
+        red.partials[2 * (size_t)blockIdx.x] = a;
+        red.partials[2 * (size_t)blockIdx.x + 1] = b;
+        __threadfence();
+        const int key = slot0 >= 0 ? slot0 : slot1;
+        const unsigned prev = atomicAdd( &red.done[key % BORA_RING], 1u );
+        last = ( prev == gridDim.x - 1 );
+    }
+    __syncthreads();
+    if( !last ) return;
+    __threadfence();
+    // All threads of the last block: thread-strided partial sums in a fixed order
+    // (independent loads, unrolled so that many are in flight), then a fixed-shape tree.
+    double a = 0.0, b = 0.0;
+    const unsigned nb = gridDim.x, stride = blockDim.x;
+#pragma unroll 4
+    for( unsigned q = threadIdx.x; q < nb; q += stride )
+    {
+        const double2 pq = __ldcg( reinterpret_cast<const double2*>( red.partials ) + q );
+        a += pq.x;
+        b = op1 ? fmax( b, pq.y ) : b + pq.y;
+    }
+    a = warp_sum( a );
+    b = op1 ? warp_max( b ) : warp_sum( b );
+    if( lane == 0 ) { w0[wid] = a; w1[wid] = b; }
+    __syncthreads();
+    if( threadIdx.x == 0 )
+    {
+        double ta = 0.0, tb = 0.0;
+        for( int q = 0; q < nw; ++q ) { ta += w0[q]; tb = op1 ? fmax( tb, w1[q] ) : tb + w1[q]; }
+        if( slot0 >= 0 ) red.ring[slot0] = ta;
+        if( slot1 >= 0 ) red.ring[slot1] = tb;
+        const int key = slot0 >= 0 ? slot0 : slot1;
+        red.done[key % BORA_RING] = 0;
+        __threadfence();
+    }
+}
+
+// Per-thread double-float sums (op1 = 0) or a float max in v1 (op1 = 1).
+__device__ __forceinline__ void reduce2_publish_df( DF v0, DF v1, BoraReduceDev red, int slot0, int slot1 )
+{
+    const double a = df_warp_sum( v0 );
+    const double b = df_warp_sum( v1 );
+    reduce2_publish_warp( a, b, 0, red, slot0, slot1 );
+}
+__device__ __forceinline__ void reduce2_publish_dfmax( DF v0, float vmax, BoraReduceDev red, int slot0, int slot1 )
+{
+    const double a = df_warp_sum( v0 );
+    const double b = (double)warp_maxf( vmax );
+    reduce2_publish_warp( a, b, 1, red, slot0, slot1 );
+}
+
+
+}  // namespace bora_reduce
+
+using namespace bora_reduce;

@@ -25,7 +25,8 @@ SPACE_WORLD, SPACE_VOXEL = 0, 1
 SOLVER_PLAIN, SOLVER_MIXED = 0, 1
 STAGE_REBUILD, STAGE_P2G, STAGE_BUILD_SYSTEM, STAGE_SOLVE, STAGE_UPDATE_VELOCITY, STAGE_UPDATE_PARTICLES = range(6)
 FIELD_MASS, FIELD_SURF, FIELD_PRES, FIELD_VELO, FIELD_COMP, FIELD_FLAG, FIELD_RHS, FIELD_CODE = range(8)
-KERNEL_CLASSES = ["bin", "tiles", "sort", "p2g", "rhs", "pcg_direction", "pcg_update", "refine", "velocity", "g2p"]
+KERNEL_CLASSES = ["bin", "tiles", "sort", "p2g", "rhs", "pcg_direction", "pcg_update", "refine", "velocity", "g2p",
+                  "mg_vcycle"]
 _FIELD_DTYPE = {FIELD_MASS: (np.float32, 1), FIELD_SURF: (np.float32, 1), FIELD_PRES: (np.float32, 1),
                 FIELD_VELO: (np.float32, 3), FIELD_COMP: (np.float32, 3), FIELD_FLAG: (np.uint8, 1),
                 FIELD_RHS: (np.float32, 1), FIELD_CODE: (np.uint16, 1)}
