@@ -70,6 +70,7 @@ void bora_launch_hist( size_t n, const uint32_t* vkey, const int32_t* slot_of, u
                        uint32_t* count, uint32_t* err, cudaStream_t st );
 void bora_launch_scatter( size_t n, const uint32_t* key, const uint32_t* start, uint32_t* count, uint32_t* idx,
                           cudaStream_t st );
+void bora_launch_order_bins( size_t nbins, const uint32_t* start, uint32_t* idx, cudaStream_t st );
 void bora_launch_p2g( const BoraGridDev& g, int ntiles, BoraTilesDev t, BoraParticlesDev p, const uint32_t* idx,
                       const uint32_t* start, BoraCellsDev c, cudaStream_t st );
 void bora_launch_rhs( const BoraGridDev& g, int ntiles, BoraTilesDev t, BoraCellsDev c, cudaStream_t st );

@@ -388,13 +388,14 @@ int stage_rebuild( bora_flip_sim* s )
         bora_launch_tile_nbrs( s->g, ntiles, P<int32_t>( s->slot_of ), P<int32_t>( s->tile_of ), P<int32_t>( s->nbr ), st );
     }
     {
-        KTimer t( s, BORA_KERNEL_SORT, s->np ? 5 : 3 );
+        KTimer t( s, BORA_KERNEL_SORT, s->np ? 6 : 3 );
         bora_launch_hist( s->np, P<uint32_t>( s->vkey ), P<int32_t>( s->slot_of ), ncell, P<uint32_t>( s->key ),
                           P<uint32_t>( s->cell_count ), P<uint32_t>( s->counters ) + 2, st );
         bora_device_scan( P<uint32_t>( s->cell_count ), P<uint32_t>( s->cell_start ), (size_t)ncell + 1,
                        P<uint32_t>( s->scan_scratch ), P<uint32_t>( s->counters ) + 1, st );
         bora_launch_scatter( s->np, P<uint32_t>( s->key ), P<uint32_t>( s->cell_start ), P<uint32_t>( s->cell_count ),
                              P<uint32_t>( s->idx ), st );
+        if( s->np ) bora_launch_order_bins( (size_t)ncell + 1, P<uint32_t>( s->cell_start ), P<uint32_t>( s->idx ), st );
     }
     BORA_TRYS( check_launch( s ) );
     BORA_TRYS( read_counters( s, 1, 2 ) );

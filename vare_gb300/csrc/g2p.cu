@@ -15,19 +15,20 @@ struct CellLookup
 {
     const BoraGridDev& g;
     const int32_t* slot_of;
-    __device__ inline long long index( int i, int j, int k ) const
+    __device__ inline int index( int i, int j, int k ) const
     {
         const int s = slot_of[( (size_t)( k >> 3 ) * g.ty + ( j >> 3 ) ) * g.tx + ( i >> 3 )];
         if( s < 0 ) return -1;
-        return (long long)s * BORA_TILE_CELLS + bora_local( i, j, k );
+        return s * BORA_TILE_CELLS + bora_local( i, j, k );
     }
 };
 
 // SparseField::lerp over a vector field (base/header/SparseField.h:150-173) and
-// SparseField::lerpMin over a scalar field (SparseField.h:176-196).
+// SparseField::lerpMin over a scalar field (SparseField.h:176-196). Corner order:
+// (i,j,k),(i+1,j,k),(i,j,k+1),(i+1,j,k+1),(i,j+1,k),(i+1,j+1,k),(i,j+1,k+1),(i+1,j+1,k+1).
 struct Lerp8
 {
-    long long idx[8];  // (i,j,k),(i+1,j,k),(i,j,k+1),(i+1,j,k+1),(i,j+1,k),(i+1,j+1,k),(i,j+1,k+1),(i+1,j+1,k+1)
+    int idx[8];  // cell index, -1 = background (inactive tile)
     float x, y, z;
     __device__ inline void setup( const CellLookup& L, float px, float py, float pz )
     {
@@ -37,7 +38,15 @@ struct Lerp8
         x = bora_clampf( px - ( (float)i + .5f ), 0.f, 1.f );
         y = bora_clampf( py - ( (float)j + .5f ), 0.f, 1.f );
         z = bora_clampf( pz - ( (float)k + .5f ), 0.f, 1.f );
-        idx[0] = L.index( i, j, k );
+        const int b = L.index( i, j, k );
+        if( b >= 0 && ( i & 7 ) < 7 && ( j & 7 ) < 7 && ( k & 7 ) < 7 )
+        {
+            // the 2x2x2 block lies inside one tile
+            idx[0] = b; idx[1] = b + 1; idx[2] = b + 64; idx[3] = b + 65;
+            idx[4] = b + 8; idx[5] = b + 9; idx[6] = b + 72; idx[7] = b + 73;
+            return;
+        }
+        idx[0] = b;
         idx[1] = L.index( i + 1, j, k );
         idx[2] = L.index( i, j, k + 1 );
         idx[3] = L.index( i + 1, j, k + 1 );
@@ -46,8 +55,8 @@ struct Lerp8
         idx[6] = L.index( i, j + 1, k + 1 );
         idx[7] = L.index( i + 1, j + 1, k + 1 );
     }
-    __device__ inline float get( const float* f, int q, float bg ) const { return idx[q] < 0 ? bg : f[idx[q]]; }
-    __device__ inline float lerp( const float* f ) const
+    __device__ inline float get( const float* __restrict__ f, int q, float bg ) const { return idx[q] < 0 ? bg : __ldg( f + idx[q] ); }
+    __device__ inline float lerp( const float* __restrict__ f ) const
     {
         const float c00 = get( f, 0, 0.f ) * ( 1.f - x ) + get( f, 1, 0.f ) * x;
         const float c01 = get( f, 2, 0.f ) * ( 1.f - x ) + get( f, 3, 0.f ) * x;
@@ -57,7 +66,7 @@ struct Lerp8
         const float c1 = c01 * ( 1.f - y ) + c11 * y;
         return c0 * ( 1.f - z ) + c1 * z;
     }
-    __device__ inline float lerp_min( const float* f, float bg ) const
+    __device__ inline float lerp_min( const float* __restrict__ f, float bg ) const
     {
         float v = fminf_ref( get( f, 0, bg ), get( f, 1, bg ) );
         v = fminf_ref( v, fminf_ref( get( f, 2, bg ), get( f, 3, bg ) ) );
@@ -73,7 +82,39 @@ __device__ inline bool inside_grid( const BoraGridDev& g, float x, float y, floa
     return !( x < 0.f || x > (float)g.nx || y < 0.f || y > (float)g.ny || z < 0.f || z > (float)g.nz );
 }
 
-__global__ void __launch_bounds__( 256 ) k_g2p( BoraGridDev g, size_t n, const int32_t* __restrict__ slot_of,
+// Collider interactions of FLIPMethod::updateParticles, kept out of line: they are rare,
+// and their corner arrays would otherwise spill the common path's registers.
+__device__ __noinline__ float3 col_carry( const BoraGridDev* g, float3 p, float dt )
+{
+    if( bora_col_phi( *g, p.x, p.y, p.z ) < 0.f )  // FLIPMethod.cu:116-119
+    {
+        float cv[3];
+        bora_col_lerp( g->cols, g->nx, g->ny, g->nz, p.x, p.y, p.z, 2, cv );
+        p.x += cv[0] * dt; p.y += cv[1] * dt; p.z += cv[2] * dt;
+    }
+    return p;
+}
+
+// push-out along the collider normal (FLIPMethod.cu:146-157); w = 1 when it collided
+__device__ __noinline__ float4 col_push( const BoraGridDev* g, float3 p )
+{
+    const float phi = bora_col_phi( *g, p.x, p.y, p.z );
+    if( !( phi < 0.f ) ) return make_float4( p.x, p.y, p.z, 0.f );
+    float nr[3];
+    bora_col_lerp( g->cols, g->nx, g->ny, g->nz, p.x, p.y, p.z, 1, nr );
+    // Vec3f::normalized (base/header/Vector3.h:350-354)
+    const double dn = 1.0f / sqrtf( nr[0] * nr[0] + nr[1] * nr[1] + nr[2] * nr[2] + 1e-30f );
+    const float ux = (float)( nr[0] * dn ), uy = (float)( nr[1] * dn ), uz = (float)( nr[2] * dn );
+    return make_float4( p.x - ux * phi, p.y - uy * phi, p.z - uz * phi, 1.f );
+}
+
+__device__ __noinline__ bool col_kill( const BoraGridDev* g, float3 p )
+{
+    const float phi = bora_col_phi( *g, p.x, p.y, p.z );  // FLIPMethod.cu:161-165
+    return phi > 3.f || phi < 0.f;
+}
+
+__global__ void __launch_bounds__( 256 ) k_g2p( const __grid_constant__ BoraGridDev g, size_t n, const int32_t* __restrict__ slot_of,
                                                 BoraCellsDev c, BoraParticlesDev src, const uint32_t* __restrict__ idx,
                                                 BoraParticlesDev dst, float* __restrict__ adj, float dt,
                                                 uint32_t* __restrict__ nkilled )
@@ -110,11 +151,10 @@ __global__ void __launch_bounds__( 256 ) k_g2p( BoraGridDev g, size_t n, const i
             vx *= w; vy *= w; vz *= w;
         }
         const bool hasCols = g.cols.count > 0;
-        if( hasCols && bora_col_phi( g, px, py, pz ) < 0.f )
+        if( hasCols )
         {
-            float cv[3];
-            bora_col_lerp( g.cols, g.nx, g.ny, g.nz, px, py, pz, 2, cv );
-            px += cv[0] * dt; py += cv[1] * dt; pz += cv[2] * dt;
+            const float3 p = col_carry( &g, make_float3( px, py, pz ), dt );
+            px = p.x; py = p.y; pz = p.z;
         }
         bool kill = false;
         {
@@ -136,23 +176,12 @@ __global__ void __launch_bounds__( 256 ) k_g2p( BoraGridDev g, size_t n, const i
                 }
                 if( hasCols )
                 {
-                    const float phi = bora_col_phi( g, px, py, pz );
-                    if( phi < 0.f )
-                    {
-                        float nr[3];
-                        bora_col_lerp( g.cols, g.nx, g.ny, g.nz, px, py, pz, 1, nr );
-                        const double dn = 1.0f / sqrtf( nr[0] * nr[0] + nr[1] * nr[1] + nr[2] * nr[2] + 1e-30f );
-                        const float ux = (float)( nr[0] * dn ), uy = (float)( nr[1] * dn ), uz = (float)( nr[2] * dn );
-                        px -= ux * phi; py -= uy * phi; pz -= uz * phi;
-                        col = true;
-                    }
+                    const float4 r = col_push( &g, make_float3( px, py, pz ) );
+                    px = r.x; py = r.y; pz = r.z;
+                    if( r.w != 0.f ) col = true;
                 }
             }
-            if( col )
-            {
-                const float phi = bora_col_phi( g, px, py, pz );
-                if( phi > 3.f || phi < 0.f ) kill = true;
-            }
+            if( col && col_kill( &g, make_float3( px, py, pz ) ) ) kill = true;
             if( !inside_grid( g, px, py, pz ) ) kill = true;
         }
         vx += g.gravity[0] * dt; vy += g.gravity[1] * dt; vz += g.gravity[2] * dt;

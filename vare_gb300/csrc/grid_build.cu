@@ -166,6 +166,28 @@ __global__ void k_scatter( size_t n, const uint32_t* __restrict__ key, const uin
     }
 }
 
+// Order the particles of every dual cell by their source index (insertion sort of each
+// bin of the permutation, in place). The counting-sort scatter fills a bin in atomic
+// arrival order; this makes the order - and so every floating-point sum over a bin - a
+// function of the input only. Bins larger than `max_bin` (possible only for the bin of
+// particles outside the grid) keep their arrival order.
+__global__ void k_order_bins( size_t nbins, const uint32_t* __restrict__ start, uint32_t* __restrict__ idx,
+                              uint32_t max_bin )
+{
+    for( size_t b = blockIdx.x * (size_t)blockDim.x + threadIdx.x; b < nbins; b += (size_t)gridDim.x * blockDim.x )
+    {
+        const uint32_t q0 = start[b], q1 = start[b + 1];
+        if( q1 - q0 < 2 || q1 - q0 > max_bin ) continue;
+        for( uint32_t q = q0 + 1; q < q1; ++q )
+        {
+            const uint32_t v = idx[q];
+            uint32_t r = q;
+            while( r > q0 && idx[r - 1] > v ) { idx[r] = idx[r - 1]; --r; }
+            idx[r] = v;
+        }
+    }
+}
+
 // Host AoS (x,y,z) particles -> device SoA, with the world->voxel transform
 // (Grid::voxelPoint / voxelVector, base/header/Grid.h:446-458) when space == 0.
 __global__ void k_to_soa( size_t n, const float* __restrict__ pos, const float* __restrict__ vel, int space,
@@ -227,6 +249,12 @@ void bora_launch_scatter( size_t n, const uint32_t* key, const uint32_t* start, 
 {
     if( n == 0 ) return;
     k_scatter<<<grid_for( n ), kThreads, 0, st>>>( n, key, start, count, idx );
+}
+
+void bora_launch_order_bins( size_t nbins, const uint32_t* start, uint32_t* idx, cudaStream_t st )
+{
+    if( nbins == 0 ) return;
+    k_order_bins<<<grid_for( nbins ), kThreads, 0, st>>>( nbins, start, idx, 4096u );
 }
 
 void bora_launch_to_soa( size_t n, const float* pos, const float* vel, int space, const float* translate,
