@@ -523,10 +523,11 @@ int stage_solve( bora_flip_sim* s )
         // inner FP32 PCG on A e = r
         const double target = norm_ok ? 0.1 * rnorm : std::max( p.inner_tolerance * rnorm, 0.25 * p.tolerance * bnorm );
         const bool mixed = p.solver == BORA_SOLVER_MIXED;
-        const int vlaunch = 4 * ( s->nlevels - 1 ) + 1;
+        int vlaunch = 1;  // coarsest
+        for( int l = 0; l + 1 < s->nlevels; ++l ) vlaunch += ( s->levels[l].kind == 0 && s->levels[l].E >= 2 ) ? 2 : 4;
         auto precondition = [&]( int rr_slot, int rz_slot ) {
             KTimer t( s, BORA_KERNEL_MG, vlaunch );
-            bora_mg_vcycle( s->g, s->levels, s->nlevels, s->tiles(), sv.r, sv.z, red, rr_slot, rz_slot, 64, st );
+            bora_mg_vcycle( s->g, s->levels, s->nlevels, s->tiles(), sv.r, sv.z, red, rr_slot, rz_slot, 32, st );
         };
         int rz_cur = s->slot(), rr_cur = s->slot();
         if( mixed )

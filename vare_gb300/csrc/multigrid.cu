@@ -507,6 +507,312 @@ __global__ void __launch_bounds__( 256 ) k_mg_smooth_last( Nav nav, BoraLevelDev
     if( zout ) reduce2_publish_warp( df_warp_sum( rz ), 0.0, 0, red, slot_rz, -1 );
 }
 
+// ---- fused per-tile kernels for tiled levels with E >= 2 ------------------------------
+//
+// Persistent CTAs walk the tiles; for each tile the CTA works on the tile plus a 2-cell
+// halo of its level, (E+4)^3 cells, staged in shared memory (cells in inactive tiles or
+// beyond the tile grid read as non-fluid, and non-fluid cells hold z = 0, so stencil sums
+// run over all six neighbours without branches). Every thread visits the same region
+// cells for every tile, so their tile direction and local index are computed once per
+// launch. The loads of the next tile are issued before the current tile's shared-memory
+// sweeps, and the neighbour table two tiles ahead, so that global latency stays off the
+// per-tile critical path. Down: two Jacobi sweeps from zero, the residual, and its
+// restriction to the tile's (E/2)^3 coarse cells. Up: prolongation of the coarse
+// correction, then two sweeps; on level 0 the result is unscaled into the FP32 z and r.z
+// is accumulated, coarser levels write their result to z1 (neighbouring CTAs still read
+// z0).
+
+template <int E>
+struct TileRegion
+{
+    static constexpr int LE = E == 8 ? 3 : ( E == 4 ? 2 : 1 );
+    static constexpr int R = E + 4;  // region edge (2-cell halo)
+    static constexpr int N = R * R * R;
+    static constexpr int Q = E + 2;  // inner region edge (1-cell halo)
+    static constexpr int NQ = Q * Q * Q;
+    static constexpr int E3 = E * E * E;
+    static constexpr int H = E / 2;
+    static constexpr int NT = E == 8 ? 512 : ( E == 4 ? 128 : 64 );  // threads per CTA
+    static constexpr int MINB = 1024 / NT;                             // resident CTAs per SM
+    static constexpr int IA = ( N + NT - 1 ) / NT;
+    static constexpr int IB = ( NQ + NT - 1 ) / NT;
+    static constexpr int IC = ( E3 + NT - 1 ) / NT;
+    static constexpr uint32_t kValid = 1u << 31, kInner = 1u << 30;
+    static constexpr uint32_t kCentre = 13;  // bora_dir( 0, 0, 0 )
+    // Region cell h: bits 0-8 local index in its tile, 9-14 parent's local index on the
+    // coarser level, 16-20 tile direction, kInner when inside the 1-cell-halo region.
+    __device__ static inline uint32_t region_map( int h )
+    {
+        if( h >= N ) return 0;
+        const int x = h % R, y = ( h / R ) % R, z = h / ( R * R );
+        const int a = x + E - 2, b = y + E - 2, c = z + E - 2;  // >= 0
+        const int la = a & ( E - 1 ), lb = b & ( E - 1 ), lc = c & ( E - 1 );
+        const uint32_t local = (uint32_t)( la + E * ( lb + E * lc ) );
+        const uint32_t parent = (uint32_t)( ( la >> 1 ) + H * ( ( lb >> 1 ) + H * ( lc >> 1 ) ) );
+        const uint32_t dir = (uint32_t)bora_dir( ( a >> LE ) - 1, ( b >> LE ) - 1, ( c >> LE ) - 1 );
+        const bool inner = x >= 1 && x <= R - 2 && y >= 1 && y <= R - 2 && z >= 1 && z <= R - 2;
+        return kValid | ( inner ? kInner : 0u ) | ( dir << 16 ) | ( parent << 9 ) | local;
+    }
+    __device__ static inline int qh( int h2 )  // region index of inner-region cell h2, or -1
+    {
+        if( h2 >= NQ ) return -1;
+        return ( h2 % Q + 1 ) + R * ( ( ( h2 / Q ) % Q + 1 ) + R * ( h2 / ( Q * Q ) + 1 ) );
+    }
+    __device__ static inline int th( int l )  // region index of tile cell l, or -1
+    {
+        if( l >= E3 ) return -1;
+        return ( l % E + 2 ) + R * ( ( ( l / E ) % E + 2 ) + R * ( l / ( E * E ) + 2 ) );
+    }
+    __device__ static inline int th2( int l )  // inner-region index of tile cell l
+    {
+        return ( l % E + 1 ) + Q * ( ( ( l / E ) % E + 1 ) + Q * ( l / ( E * E ) + 1 ) );
+    }
+    // slot of the region cell's tile for neighbour table nb, or -1
+    __device__ static inline int slot( const int32_t* nb, uint32_t m ) { return ( m & kValid ) ? nb[( m >> 16 ) & 31] : -1; }
+};
+
+// omega / diag for diag 0..15 (0 for diag 0: such cells keep z = 0)
+__device__ inline void init_wd( float* wd )
+{
+    if( threadIdx.x < 16 ) wd[threadIdx.x] = threadIdx.x ? kOmega / (float)threadIdx.x : 0.f;
+}
+
+// One damped Jacobi update of a cell from its six neighbours in the same array.
+template <int STRIDE_Y>
+__device__ inline float jacobi( const float* z, int h, uint16_t cc, float r, const float* wd )
+{
+    const float zc = z[h];
+    const float sum = ( z[h - 1] + z[h + 1] ) + ( z[h - STRIDE_Y] + z[h + STRIDE_Y] ) +
+                      ( z[h - STRIDE_Y * STRIDE_Y] + z[h + STRIDE_Y * STRIDE_Y] );
+    return ( cc & BORA_CODE_FLUID ) ? zc + wd[code_diag( cc )] * ( r - ( (float)code_diag( cc ) * zc - sum ) ) : 0.f;
+}
+
+// neighbour table entry tid (< 27) of tile s, or -1 past the last tile
+__device__ inline int32_t nbr_entry( const BoraTilesDev& t, int s, int ntiles, int tid )
+{
+    return s < ntiles ? t.nbr[(size_t)s * 27 + tid] : -1;
+}
+
+template <int E, bool L0>
+__global__ void __launch_bounds__( TileRegion<E>::NT, TileRegion<E>::MINB ) k_mg_down_fused( BoraLevelDev F, BoraLevelDev C,
+                                                                           BoraTilesDev t, int ntiles,
+                                                                           const float* __restrict__ r0, int slot_rr,
+                                                                           const double* __restrict__ ring )
+{
+    using TR = TileRegion<E>;
+    constexpr int R = TR::R, Q = TR::Q, H = TR::H, NT = TR::NT, E3 = TR::E3;
+    __shared__ float rs[TR::N], z1[TR::N];
+    __shared__ uint16_t cs[TR::N];
+    __shared__ float z2[TR::NQ];
+    __shared__ float res[E3];
+    __shared__ int32_t nbb[2][27];
+    __shared__ float wd[16];
+    __shared__ float s_scale;
+    const int tid = threadIdx.x, G = gridDim.x;
+    init_wd( wd );
+    if( tid == 0 ) s_scale = L0 ? scale_of( ring, slot_rr ) : 1.f;
+    if( tid < 27 )
+    {
+        nbb[0][tid] = nbr_entry( t, blockIdx.x, ntiles, tid );
+        nbb[1][tid] = nbr_entry( t, blockIdx.x + G, ntiles, tid );
+    }
+    uint32_t am[TR::IA];
+    int bh[TR::IB], ch[TR::IC], ch2[TR::IC];
+#pragma unroll
+    for( int it = 0; it < TR::IA; ++it ) am[it] = TR::region_map( tid + it * NT );
+#pragma unroll
+    for( int it = 0; it < TR::IB; ++it ) bh[it] = TR::qh( tid + it * NT );
+#pragma unroll
+    for( int it = 0; it < TR::IC; ++it ) { ch[it] = TR::th( tid + it * NT ); ch2[it] = TR::th2( tid + it * NT ); }
+    __syncthreads();
+    const float sc = s_scale;
+    uint16_t cv[TR::IA];
+    float rv[TR::IA];
+    auto issue = [&]( const int32_t* nb ) {
+#pragma unroll
+        for( int it = 0; it < TR::IA; ++it )
+        {
+            const int sl = TR::slot( nb, am[it] );
+            cv[it] = 0;
+            rv[it] = 0.f;
+            if( sl >= 0 )
+            {
+                const uint32_t g = (uint32_t)sl * E3 + ( am[it] & 511u );
+                cv[it] = F.code[g];
+                rv[it] = L0 ? __ldg( r0 + g ) : __half2float( F.r[g] );
+            }
+        }
+    };
+    issue( nbb[0] );
+    int n = 0;
+    for( int s = blockIdx.x; s < ntiles; s += G, ++n )
+    {
+        // stage tile s; the first sweep from zero is pointwise z1 = w r'/d
+#pragma unroll
+        for( int it = 0; it < TR::IA; ++it )
+        {
+            const int h = tid + it * NT;
+            if( h < TR::N )
+            {
+                const uint16_t cc = cv[it];
+                const bool fl = cc & BORA_CODE_FLUID;
+                const float r = fl ? ( L0 ? rv[it] * sc : rv[it] ) : 0.f;
+                cs[h] = cc;
+                rs[h] = r;
+                z1[h] = fl ? r * wd[code_diag( cc )] : 0.f;
+            }
+        }
+        const int32_t nb2 = tid < 27 ? nbr_entry( t, s + 2 * G, ntiles, tid ) : -1;
+        __syncthreads();
+        if( s + G < ntiles ) issue( nbb[( n + 1 ) & 1] );
+        // second sweep on the inner region
+#pragma unroll
+        for( int it = 0; it < TR::IB; ++it )
+        {
+            const int h = bh[it];
+            if( h >= 0 ) z2[tid + it * NT] = jacobi<R>( z1, h, cs[h], rs[h], wd );
+        }
+        __syncthreads();
+        // residual on the tile
+#pragma unroll
+        for( int it = 0; it < TR::IC; ++it )
+        {
+            const int h = ch[it];
+            if( h < 0 ) continue;
+            const int h2 = ch2[it], l = tid + it * NT;
+            const uint16_t cc = cs[h];
+            const float zc = z2[h2];
+            const float sum = ( z2[h2 - 1] + z2[h2 + 1] ) + ( z2[h2 - Q] + z2[h2 + Q] ) + ( z2[h2 - Q * Q] + z2[h2 + Q * Q] );
+            res[l] = ( cc & BORA_CODE_FLUID ) ? rs[h] - ( (float)code_diag( cc ) * zc - sum ) : 0.f;
+            F.z0[(size_t)s * E3 + l] = __float2half_rn( zc );
+        }
+        __syncthreads();
+        // restriction, r'_C = 4 * mean of the 8 children = 0.5 * sum (non-fluid children
+        // hold 0, and a coarse cell is fluid exactly when one of its children is)
+        if( tid < H * H * H )
+        {
+            const int a = tid % H, b = ( tid / H ) % H, c = tid / ( H * H );
+            const int l = 2 * a + E * ( 2 * b + E * 2 * c );
+            const float sum = ( ( res[l] + res[l + 1] ) + ( res[l + E] + res[l + E + 1] ) ) +
+                              ( ( res[l + E * E] + res[l + E * E + 1] ) + ( res[l + E * E + E] + res[l + E * E + E + 1] ) );
+            C.r[(size_t)s * ( H * H * H ) + tid] = __float2half_rn( 0.5f * sum );
+        }
+        if( tid < 27 ) nbb[n & 1][tid] = nb2;  // tile s's table is no longer read
+        __syncthreads();
+    }
+}
+
+template <int E, bool L0>
+__global__ void __launch_bounds__( TileRegion<E>::NT, TileRegion<E>::MINB ) k_mg_up_fused( BoraLevelDev F, const __half* __restrict__ ec,
+                                                                         BoraTilesDev t, int ntiles,
+                                                                         const float* __restrict__ r0, int slot_rr,
+                                                                         BoraReduceDev red, float* __restrict__ zout,
+                                                                         int slot_rz )
+{
+    using TR = TileRegion<E>;
+    constexpr int R = TR::R, Q = TR::Q, H = TR::H, NT = TR::NT, E3 = TR::E3;
+    __shared__ float rs[TR::N], za[TR::N];
+    __shared__ uint16_t cs[TR::N];
+    __shared__ float zb[TR::NQ];
+    __shared__ float rraw[L0 ? E3 : 1];
+    __shared__ int32_t nbb[2][27];
+    __shared__ float wd[16];
+    __shared__ float s_scale;
+    const int tid = threadIdx.x, G = gridDim.x;
+    init_wd( wd );
+    if( tid == 0 ) s_scale = L0 ? scale_of( red.ring, slot_rr ) : 1.f;
+    if( tid < 27 )
+    {
+        nbb[0][tid] = nbr_entry( t, blockIdx.x, ntiles, tid );
+        nbb[1][tid] = nbr_entry( t, blockIdx.x + G, ntiles, tid );
+    }
+    uint32_t am[TR::IA];
+    int bh[TR::IB], ch[TR::IC], ch2[TR::IC];
+#pragma unroll
+    for( int it = 0; it < TR::IA; ++it ) am[it] = TR::region_map( tid + it * NT );
+#pragma unroll
+    for( int it = 0; it < TR::IB; ++it ) bh[it] = TR::qh( tid + it * NT );
+#pragma unroll
+    for( int it = 0; it < TR::IC; ++it ) { ch[it] = TR::th( tid + it * NT ); ch2[it] = TR::th2( tid + it * NT ); }
+    __syncthreads();
+    const float sc = s_scale;
+    uint16_t cv[TR::IA];
+    float rv[TR::IA], zv[TR::IA];
+    auto issue = [&]( const int32_t* nb ) {
+#pragma unroll
+        for( int it = 0; it < TR::IA; ++it )
+        {
+            const uint32_t m = am[it];
+            const int sl = TR::slot( nb, m );
+            cv[it] = 0;
+            rv[it] = 0.f;
+            zv[it] = 0.f;
+            if( sl >= 0 )
+            {
+                const uint32_t g = (uint32_t)sl * E3 + ( m & 511u );
+                cv[it] = F.code[g];
+                // za = z0 + P e: the parent is the same tile's cell on the coarser level
+                zv[it] = __half2float( F.z0[g] ) + __half2float( ec[(uint32_t)sl * ( H * H * H ) + ( ( m >> 9 ) & 63u )] );
+                if( m & TR::kInner ) rv[it] = L0 ? __ldg( r0 + g ) : __half2float( F.r[g] );
+            }
+        }
+    };
+    issue( nbb[0] );
+    DF rz{ 0.f, 0.f };
+    int n = 0;
+    for( int s = blockIdx.x; s < ntiles; s += G, ++n )
+    {
+#pragma unroll
+        for( int it = 0; it < TR::IA; ++it )
+        {
+            const int h = tid + it * NT;
+            if( h < TR::N )
+            {
+                const uint16_t cc = cv[it];
+                const bool fl = cc & BORA_CODE_FLUID;
+                cs[h] = cc;
+                rs[h] = fl ? ( L0 ? rv[it] * sc : rv[it] ) : 0.f;
+                za[h] = fl ? zv[it] : 0.f;
+                if( L0 && ( ( am[it] >> 16 ) & 31u ) == TR::kCentre ) rraw[am[it] & 511u] = rv[it];
+            }
+        }
+        const int32_t nb2 = tid < 27 ? nbr_entry( t, s + 2 * G, ntiles, tid ) : -1;
+        __syncthreads();
+        if( s + G < ntiles ) issue( nbb[( n + 1 ) & 1] );
+#pragma unroll
+        for( int it = 0; it < TR::IB; ++it )
+        {
+            const int h = bh[it];
+            if( h >= 0 ) zb[tid + it * NT] = jacobi<R>( za, h, cs[h], rs[h], wd );
+        }
+        __syncthreads();
+#pragma unroll
+        for( int it = 0; it < TR::IC; ++it )
+        {
+            const int h = ch[it];
+            if( h < 0 ) continue;
+            const int h2 = ch2[it], l = tid + it * NT;
+            const uint16_t cc = cs[h];
+            const float zc = jacobi<Q>( zb, h2, cc, rs[h], wd );
+            const size_t g = (size_t)s * E3 + l;
+            if( L0 )
+            {
+                const float zf = zc / sc;  // undo the FP16 scaling of the residual
+                zout[g] = zf;
+                if( cc & BORA_CODE_FLUID ) rz = df_add( rz, df_prod( rraw[l], zf ) );
+            }
+            else
+            {
+                F.z1[g] = __float2half_rn( zc );
+            }
+        }
+        if( tid < 27 ) nbb[n & 1][tid] = nb2;
+        __syncthreads();  // the next tile's staging overwrites the shared arrays
+    }
+    if( L0 ) reduce2_publish_warp( df_warp_sum( rz ), 0.0, 0, red, slot_rz, -1 );
+}
+
+
 // PCG update without a preconditioner sweep: e += alpha d; r -= alpha q; r.r.
 __global__ void __launch_bounds__( 256 ) k_pcg_update_noprec( size_t ncells, BoraSolverDev sv, int dsel, BoraReduceDev red,
                                                               int slot_rz, int slot_dq, int slot_rr_out )
@@ -545,6 +851,43 @@ int blocks_for( size_t n )
         if( g_sms <= 0 ) g_sms = 152;
     }
     return (int)std::max<size_t>( 1, std::min<size_t>( ( n + 255 ) / 256, (size_t)g_sms * 8 ) );
+}
+
+// Persistent grid for a fused kernel: as many CTAs as can be resident at once.
+template <class K>
+int fused_grid( K kernel, int nt, int ntiles, int* per_sm )
+{
+    int dev = 0;
+    cudaGetDevice( &dev );
+    int b = dev >= 0 && dev < 64 ? per_sm[dev] : 0;
+    if( b <= 0 )
+    {
+        if( cudaOccupancyMaxActiveBlocksPerMultiprocessor( &b, kernel, nt, 0 ) != cudaSuccess || b <= 0 ) b = 1;
+        if( dev >= 0 && dev < 64 ) per_sm[dev] = b;
+    }
+    blocks_for( 1 );  // sets g_sms
+    return std::max( 1, std::min( ntiles, b * g_sms ) );
+}
+
+template <int E, bool L0>
+void launch_down_fused( const BoraLevelDev& F, const BoraLevelDev& C, BoraTilesDev t, int ntiles, const float* r0,
+                        int slot_rr, const double* ring, cudaStream_t st )
+{
+    static int per_sm[64] = { 0 };
+    constexpr int NT = TileRegion<E>::NT;
+    const int grid = fused_grid( k_mg_down_fused<E, L0>, NT, ntiles, per_sm );
+    k_mg_down_fused<E, L0><<<grid, NT, 0, st>>>( F, C, t, ntiles, r0, slot_rr, ring );
+}
+
+template <int E, bool L0>
+void launch_up_fused( const BoraLevelDev& F, const __half* ec, BoraTilesDev t, int ntiles, const float* r0,
+                      int slot_rr, BoraReduceDev red, float* zout, int slot_rz, cudaStream_t st )
+{
+    static int per_sm[64] = { 0 };
+    constexpr int NT = TileRegion<E>::NT;
+    int grid = fused_grid( k_mg_up_fused<E, L0>, NT, ntiles, per_sm );
+    if( L0 ) grid = std::min( grid, 152 * 16 );  // partial sums capacity of the reduction
+    k_mg_up_fused<E, L0><<<grid, NT, 0, st>>>( F, ec, t, ntiles, r0, slot_rr, red, zout, slot_rz );
 }
 
 LevelNav nav_of( const BoraGridDev& g, const BoraLevelDev& L, BoraTilesDev t )
@@ -593,13 +936,22 @@ void bora_mg_vcycle( const BoraGridDev& g, const BoraLevelDev* levels, int nleve
                      float* z, BoraReduceDev red, int slot_rr, int slot_rz, int coarse_sweeps, cudaStream_t st )
 {
     if( nlevels < 2 ) return;  // the caller always builds at least two levels
+    if( levels[0].ncells == 0 ) return;
     const int last = nlevels - 1;
+    const int ntiles = levels[0].kind == 0 ? (int)( levels[0].ncells / 512 ) : 0;
     // down: pre-smooth and restrict
     for( int l = 0; l < last; ++l )
     {
         const BoraLevelDev& F = levels[l];
         const BoraLevelDev& C = levels[l + 1];
         const float* r0 = l == 0 ? r : nullptr;
+        if( F.kind == 0 && F.E >= 2 )
+        {
+            if( F.E == 8 ) launch_down_fused<8, true>( F, C, t, ntiles, r0, slot_rr, red.ring, st );
+            else if( F.E == 4 ) launch_down_fused<4, false>( F, C, t, ntiles, r0, slot_rr, red.ring, st );
+            else launch_down_fused<2, false>( F, C, t, ntiles, r0, slot_rr, red.ring, st );
+            continue;
+        }
         with_nav( g, levels, nlevels, l, t, [&]( auto nav ) {
             k_mg_smooth0<<<blocks_for( F.ncells ), 256, 0, st>>>( nav, F, r0, slot_rr, red.ring, red.err );
             const int nb = blocks_for( C.ncells * 8 );
@@ -611,10 +963,6 @@ void bora_mg_vcycle( const BoraGridDev& g, const BoraLevelDev* levels, int nleve
                 else
                     k_mg_restrict<N, 1, 1><<<nb, 256, 0, st>>>( nav, F, C, r0, slot_rr, red.ring, t.slot_of, g.tx, g.ty, g.tz, red.err );
             }
-            else if( C.E == 4 )
-                k_mg_restrict<N, 0, 4><<<nb, 256, 0, st>>>( nav, F, C, r0, slot_rr, red.ring, t.slot_of, g.tx, g.ty, g.tz, red.err );
-            else if( C.E == 2 )
-                k_mg_restrict<N, 0, 2><<<nb, 256, 0, st>>>( nav, F, C, r0, slot_rr, red.ring, t.slot_of, g.tx, g.ty, g.tz, red.err );
             else
                 k_mg_restrict<N, 0, 1><<<nb, 256, 0, st>>>( nav, F, C, r0, slot_rr, red.ring, t.slot_of, g.tx, g.ty, g.tz, red.err );
         } );
@@ -622,11 +970,21 @@ void bora_mg_vcycle( const BoraGridDev& g, const BoraLevelDev* levels, int nleve
     with_nav( g, levels, nlevels, last, t, [&]( auto nav ) {
         k_mg_coarsest<<<1, 512, 0, st>>>( nav, levels[last], coarse_sweeps, red.err );
     } );
-    // up: prolong + smooth, then a last sweep
+    // up: prolong + two sweeps
     for( int l = last - 1; l >= 0; --l )
     {
         const BoraLevelDev& F = levels[l];
         const float* r0 = l == 0 ? r : nullptr;
+        if( F.kind == 0 && F.E >= 2 )
+        {
+            // a coarser level that went through this fused path left its result in z1
+            const bool cf = l + 1 < last && levels[l + 1].kind == 0 && levels[l + 1].E >= 2;
+            const __half* ec = cf ? levels[l + 1].z1 : levels[l + 1].z0;
+            if( F.E == 8 ) launch_up_fused<8, true>( F, ec, t, ntiles, r0, slot_rr, red, z, slot_rz, st );
+            else if( F.E == 4 ) launch_up_fused<4, false>( F, ec, t, ntiles, r0, slot_rr, red, nullptr, slot_rz, st );
+            else launch_up_fused<2, false>( F, ec, t, ntiles, r0, slot_rr, red, nullptr, slot_rz, st );
+            continue;
+        }
         with_nav( g, levels, nlevels, l, t, [&]( auto nav ) {
             k_mg_prolong_smooth<<<blocks_for( F.ncells ), 256, 0, st>>>( nav, F, levels[l + 1].z0, r0, slot_rr, red.ring,
                                                                          red.err );
