@@ -532,8 +532,8 @@ struct TileRegion
     static constexpr int NQ = Q * Q * Q;
     static constexpr int E3 = E * E * E;
     static constexpr int H = E / 2;
-    static constexpr int NT = E == 8 ? 512 : ( E == 4 ? 128 : 64 );  // threads per CTA
-    static constexpr int MINB = 1024 / NT;                             // resident CTAs per SM
+    static constexpr int NT = E == 8 ? 256 : ( E == 4 ? 128 : 64 );  // threads per CTA
+    static constexpr int MINB = E == 8 ? 4 : 1024 / NT;                // resident CTAs per SM
     static constexpr int IA = ( N + NT - 1 ) / NT;
     static constexpr int IB = ( NQ + NT - 1 ) / NT;
     static constexpr int IC = ( E3 + NT - 1 ) / NT;

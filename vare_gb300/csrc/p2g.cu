@@ -7,8 +7,8 @@
 //
 // Particles arrive sorted by dual cell (the base cell of the reference's 2x2x2 stencil,
 // max(int(p-0.5),0) per axis), so the particles that touch cell c are exactly those of
-// the 8 dual cells {c-1, c}^3: each cell gathers from its 8 dual cells (one thread per
-// dual cell, combined by shuffles) - no atomics, one store per field.
+// the 8 dual cells {c-1, c}^3. Each dual cell's particles are read once and summed per
+// stencil corner, and each cell adds its 8 corner sums - no atomics, one store per field.
 // Weights follow the reference (w = prod max(0, 1-|p-c|) + 1e-5); sums are FP32 in a
 // fixed order (particles of a dual cell by source index, then a fixed tree over the 8
 // dual cells), so the result is bit-reproducible.
@@ -25,97 +25,141 @@ __device__ __noinline__ float3 col_velocity( const BoraGridDev* g, float x, floa
     return make_float3( cv[0], cv[1], cv[2] );
 }
 
-// One thread per (cell, dual cell): 8 consecutive lanes own the 8 dual cells {c-1, c}^3
-// of one cell, each sums its particles in bin order (fixed by k_order_bins), and the lanes
-// combine their sums with a fixed shuffle tree, so the result is reproducible.
-__global__ void __launch_bounds__( 256, 5 ) k_p2g( const __grid_constant__ BoraGridDev g, BoraTilesDev t, BoraParticlesDev p,
-                                                const uint32_t* __restrict__ idx, const uint32_t* __restrict__ start,
-                                                BoraCellsDev c, size_t ncells )
+// One CTA per tile. Each thread owns a dual cell of the tile (then, in a second round, of
+// the tile's low-side halo), reads its particles once in bin order (fixed by k_order_bins)
+// and keeps the 8 corner sums of m, m*v in registers. Every (cell, source dual cell) pair of
+// the tile is produced by exactly one thread and parked in shared memory; each cell then
+// adds its 8 sources with a fixed tree, so the result is reproducible. Halo dual cells
+// are recomputed by every tile that needs them instead of being exchanged.
+constexpr int kP2GThreads = 512;
+constexpr int kP2GHalo = 217;  // 9^3 - 8^3 dual cells with a -1 tile-local coordinate
+constexpr size_t kP2GSmem = 8 * 4 * 512 * sizeof( float ) + 8 * 512 * sizeof( uint32_t );
+
+__global__ void __launch_bounds__( kP2GThreads, 2 ) k_p2g( const __grid_constant__ BoraGridDev g, BoraTilesDev t,
+                                                           BoraParticlesDev p, const uint32_t* __restrict__ idx,
+                                                           const uint32_t* __restrict__ start, BoraCellsDev c )
 {
-    const size_t total = ncells * 8;  // a multiple of 32: every lane of a warp runs the same iterations
-    for( size_t tid = blockIdx.x * (size_t)blockDim.x + threadIdx.x; tid < total; tid += (size_t)gridDim.x * blockDim.x )
+    extern __shared__ float p2g_smem[];
+    float* part = p2g_smem;                                         // [o][m, mx, my, mz][cell]
+    uint32_t* pcnt = reinterpret_cast<uint32_t*>( p2g_smem + 8 * 4 * 512 );  // [o][cell]
+    __shared__ int32_t nb[27];
+    const int s = blockIdx.x, tid = threadIdx.x;
+    if( tid < 27 ) nb[tid] = t.nbr[(size_t)s * 27 + tid];
+    const int vt = t.tile_of[s];
+    const int ti = vt % g.tx, tj = ( vt / g.tx ) % g.ty, tk = vt / ( g.tx * g.ty );
+    __syncthreads();
+    for( int round = 0; round < 2; ++round )
     {
-        const size_t cell = tid >> 3;
-        const int o = (int)( tid & 7 );
-        const int s = (int)( cell >> 9 ), l = (int)( cell & 511 );
-        const int vt = t.tile_of[s];
-        const int ti = vt % g.tx, tj = ( vt / g.tx ) % g.ty, tk = vt / ( g.tx * g.ty );
-        const int i = ti * BORA_TILE + ( l & 7 ), j = tj * BORA_TILE + ( ( l >> 3 ) & 7 ), k = tk * BORA_TILE + ( l >> 6 );
-        const bool real = i < g.nx && j < g.ny && k < g.nz;
-        const float ccx = (float)i + .5f, ccy = (float)j + .5f, ccz = (float)k + .5f;
-        float m = 0.f, mx = 0.f, my = 0.f, mz = 0.f;
-        uint32_t cnt = 0;
-        const int di = i - 1 + ( o & 1 ), dj = j - 1 + ( ( o >> 1 ) & 1 ), dk = k - 1 + ( o >> 2 );
-        if( real && di >= 0 && dj >= 0 && dk >= 0 )
+        int di, dj, dk;  // tile-local dual-cell coordinates in [-1, 7]
+        if( round == 0 )
         {
-            const int ns = t.nbr[(size_t)s * 27 + bora_dir( ( di >> 3 ) - ti, ( dj >> 3 ) - tj, ( dk >> 3 ) - tk )];
-            if( ns >= 0 )
+            di = tid & 7; dj = ( tid >> 3 ) & 7; dk = tid >> 6;
+        }
+        else
+        {
+            if( tid >= kP2GHalo ) break;
+            if( tid < 81 ) { di = tid % 9 - 1; dj = tid / 9 - 1; dk = -1; }
+            else if( tid < 153 ) { const int u = tid - 81; di = u % 9 - 1; dj = -1; dk = u / 9; }
+            else { const int u = tid - 153; di = -1; dj = u & 7; dk = u >> 3; }
+        }
+        const int ns = nb[bora_dir( di < 0 ? -1 : 0, dj < 0 ? -1 : 0, dk < 0 ? -1 : 0 )];
+        uint32_t q0 = 0, q1 = 0;
+        if( ns >= 0 )
+        {
+            const uint32_t key = (uint32_t)ns * BORA_TILE_CELLS + (uint32_t)bora_local( di, dj, dk );
+            q0 = start[key];
+            q1 = start[key + 1];
+        }
+        // centres of the two cells per axis that the dual cell's particles touch
+        const int gi = ti * BORA_TILE + di, gj = tj * BORA_TILE + dj, gk = tk * BORA_TILE + dk;
+        const float cx0 = (float)gi + .5f, cx1 = (float)( gi + 1 ) + .5f;
+        const float cy0 = (float)gj + .5f, cy1 = (float)( gj + 1 ) + .5f;
+        const float cz0 = (float)gk + .5f, cz1 = (float)( gk + 1 ) + .5f;
+        float acc[8][4];
+#pragma unroll
+        for( int o = 0; o < 8; ++o ) acc[o][0] = acc[o][1] = acc[o][2] = acc[o][3] = 0.f;
+        for( uint32_t q = q0; q < q1; ++q )
+        {
+            const uint32_t pi = idx[q];
+            const float x = p.px[pi], y = p.py[pi], z = p.pz[pi];
+            const float vx = p.vx[pi], vy = p.vy[pi], vz = p.vz[pi];
+            const float wx[2] = { fmaxf( 0.f, 1.f - fabsf( x - cx0 ) ), fmaxf( 0.f, 1.f - fabsf( x - cx1 ) ) };
+            const float wy[2] = { fmaxf( 0.f, 1.f - fabsf( y - cy0 ) ), fmaxf( 0.f, 1.f - fabsf( y - cy1 ) ) };
+            const float wz[2] = { fmaxf( 0.f, 1.f - fabsf( z - cz0 ) ), fmaxf( 0.f, 1.f - fabsf( z - cz1 ) ) };
+#pragma unroll
+            for( int cr = 0; cr < 8; ++cr )  // corner (a, b, c) = bits of cr
             {
-                const uint32_t key = (uint32_t)ns * BORA_TILE_CELLS + (uint32_t)bora_local( di, dj, dk );
-                const uint32_t q0 = start[key], q1 = start[key + 1];
-                cnt = q1 - q0;
-                for( uint32_t q = q0; q < q1; ++q )
-                {
-                    const uint32_t pi = idx[q];
-                    const float x = p.px[pi], y = p.py[pi], z = p.pz[pi];
-                    const float dx = x - ccx, dy = y - ccy, dz = z - ccz;
-                    const float xw = fmaxf( 0.f, 1.f - fabsf( dx ) );
-                    const float yw = fmaxf( 0.f, 1.f - fabsf( dy ) );
-                    const float zw = fmaxf( 0.f, 1.f - fabsf( dz ) );
-                    const float w = xw * yw * zw + 1e-05f;
-                    m += w;
-                    mx += w * p.vx[pi];
-                    my += w * p.vy[pi];
-                    mz += w * p.vz[pi];
-                }
+                const float w = wx[cr & 1] * wy[( cr >> 1 ) & 1] * wz[cr >> 2] + 1e-05f;
+                acc[cr][0] += w;
+                acc[cr][1] += w * vx;
+                acc[cr][2] += w * vy;
+                acc[cr][3] += w * vz;
             }
         }
-        // fixed butterfly over the 8 dual cells (float addition is commutative, so every
-        // lane ends with the same, order-independent value)
+        const uint32_t n = q1 - q0;
 #pragma unroll
-        for( int sh = 1; sh < 8; sh <<= 1 )
+        for( int cr = 0; cr < 8; ++cr )
         {
-            m += __shfl_xor_sync( 0xffffffffu, m, sh );
-            mx += __shfl_xor_sync( 0xffffffffu, mx, sh );
-            my += __shfl_xor_sync( 0xffffffffu, my, sh );
-            mz += __shfl_xor_sync( 0xffffffffu, mz, sh );
-            cnt += __shfl_xor_sync( 0xffffffffu, cnt, sh );
+            const int a = cr & 1, b = ( cr >> 1 ) & 1, cc = cr >> 2;
+            const int li = di + a, lj = dj + b, lk = dk + cc;
+            if( li < 0 || lj < 0 || lk < 0 || li > 7 || lj > 7 || lk > 7 ) continue;
+            const int cell = li | ( lj << 3 ) | ( lk << 6 );
+            const int o = 7 - cr;  // the dual cell is cell - 1 + bits(o)
+            part[( o * 4 + 0 ) * 512 + cell] = acc[cr][0];
+            part[( o * 4 + 1 ) * 512 + cell] = acc[cr][1];
+            part[( o * 4 + 2 ) * 512 + cell] = acc[cr][2];
+            part[( o * 4 + 3 ) * 512 + cell] = acc[cr][3];
+            pcnt[o * 512 + cell] = n;
         }
-        if( o != 0 ) continue;
-        if( !real )
-        {
-            c.flag[cell] = BORA_MASKED;
-            c.mass[cell] = 0.f; c.surf[cell] = 0.f;
-            c.vx[cell] = 0.f; c.vy[cell] = 0.f; c.vz[cell] = 0.f;
-            continue;
-        }
-        float vx = 0.f, vy = 0.f, vz = 0.f, mass = 0.f;
-        if( m > 0.f )
-        {
-            mass = m;
-            vx = mx / m;
-            vy = my / m;
-            vz = mz / m;
-        }
-        // flags and collider velocity (FLIPMethod.cu:244-260)
-        uint8_t f;
-        const float phi = bora_col_phi( g, ccx, ccy, ccz );
-        if( m > 0.f ) f = BORA_FLUID;
-        else f = phi < 0.f ? BORA_SOLID : BORA_AIR;
-        if( phi < 0.f )
-        {
-            const float3 cv = col_velocity( &g, ccx, ccy, ccz );
-            vx += cv.x * g.col_vel_scale;
-            vy += cv.y * g.col_vel_scale;
-            vz += cv.z * g.col_vel_scale;
-        }
-        c.flag[cell] = f;
-        c.mass[cell] = mass;
-        c.surf[cell] = (float)cnt;
-        c.vx[cell] = vx;
-        c.vy[cell] = vy;
-        c.vz[cell] = vz;
     }
+    __syncthreads();
+    // per cell: fixed tree over the 8 source dual cells
+    const int l = tid;
+    auto tree = [&]( int v ) {
+        const float* q = part + v * 512 + l;
+        return ( ( q[0 * 2048] + q[1 * 2048] ) + ( q[2 * 2048] + q[3 * 2048] ) ) +
+               ( ( q[4 * 2048] + q[5 * 2048] ) + ( q[6 * 2048] + q[7 * 2048] ) );
+    };
+    const float m = tree( 0 ), mx = tree( 1 ), my = tree( 2 ), mz = tree( 3 );
+    uint32_t cnt = 0;
+#pragma unroll
+    for( int o = 0; o < 8; ++o ) cnt += pcnt[o * 512 + l];
+    const size_t cell = (size_t)s * BORA_TILE_CELLS + l;
+    const int i = ti * BORA_TILE + ( l & 7 ), j = tj * BORA_TILE + ( ( l >> 3 ) & 7 ), k = tk * BORA_TILE + ( l >> 6 );
+    if( !( i < g.nx && j < g.ny && k < g.nz ) )
+    {
+        c.flag[cell] = BORA_MASKED;
+        c.mass[cell] = 0.f; c.surf[cell] = 0.f;
+        c.vx[cell] = 0.f; c.vy[cell] = 0.f; c.vz[cell] = 0.f;
+        return;
+    }
+    const float ccx = (float)i + .5f, ccy = (float)j + .5f, ccz = (float)k + .5f;
+    float vx = 0.f, vy = 0.f, vz = 0.f, mass = 0.f;
+    if( m > 0.f )
+    {
+        mass = m;
+        vx = mx / m;
+        vy = my / m;
+        vz = mz / m;
+    }
+    // flags and collider velocity (FLIPMethod.cu:244-260)
+    uint8_t f;
+    const float phi = bora_col_phi( g, ccx, ccy, ccz );
+    if( m > 0.f ) f = BORA_FLUID;
+    else f = phi < 0.f ? BORA_SOLID : BORA_AIR;
+    if( phi < 0.f )
+    {
+        const float3 cv = col_velocity( &g, ccx, ccy, ccz );
+        vx += cv.x * g.col_vel_scale;
+        vy += cv.y * g.col_vel_scale;
+        vz += cv.z * g.col_vel_scale;
+    }
+    c.flag[cell] = f;
+    c.mass[cell] = mass;
+    c.surf[cell] = (float)cnt;
+    c.vx[cell] = vx;
+    c.vy[cell] = vy;
+    c.vz[cell] = vz;
 }
 
 }  // namespace
@@ -124,10 +168,13 @@ void bora_launch_p2g( const BoraGridDev& g, int ntiles, BoraTilesDev t, BoraPart
                       const uint32_t* start, BoraCellsDev c, cudaStream_t st )
 {
     if( ntiles <= 0 ) return;
-    const size_t ncells = (size_t)ntiles * BORA_TILE_CELLS;
-    int dev = 0, sms = 0;
+    static bool attr_set[64] = { false };
+    int dev = 0;
     cudaGetDevice( &dev );
-    cudaDeviceGetAttribute( &sms, cudaDevAttrMultiProcessorCount, dev );
-    const size_t want = ( ncells * 8 + 255 ) / 256, cap = (size_t)( sms > 0 ? sms : 152 ) * 16;
-    k_p2g<<<(int)( want < cap ? want : cap ), 256, 0, st>>>( g, t, p, idx, start, c, ncells );
+    if( dev >= 0 && dev < 64 && !attr_set[dev] )
+    {
+        cudaFuncSetAttribute( k_p2g, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kP2GSmem );
+        attr_set[dev] = true;
+    }
+    k_p2g<<<ntiles, kP2GThreads, kP2GSmem, st>>>( g, t, p, idx, start, c );
 }
