@@ -75,9 +75,9 @@ void bora_launch_p2g( const BoraGridDev& g, int ntiles, BoraTilesDev t, BoraPart
                       const uint32_t* start, BoraCellsDev c, cudaStream_t st );
 void bora_launch_rhs( const BoraGridDev& g, int ntiles, BoraTilesDev t, BoraCellsDev c, cudaStream_t st );
 void bora_launch_vel_update( const BoraGridDev& g, int ntiles, BoraTilesDev t, BoraCellsDev c, cudaStream_t st );
-void bora_launch_g2p( const BoraGridDev& g, size_t n, const int32_t* slot_of, BoraCellsDev c, BoraParticlesDev src,
-                      const uint32_t* idx, BoraParticlesDev dst, float* adj, float dt, uint32_t* nkilled,
-                      cudaStream_t st );
+void bora_launch_g2p( const BoraGridDev& g, int ntiles, size_t nsorted, BoraTilesDev t, const uint32_t* start, BoraCellsDev c,
+                      BoraParticlesDev src, const uint32_t* idx, BoraParticlesDev dst, float* adj, float dt,
+                      uint32_t* nkilled, cudaStream_t st );
 void bora_launch_to_soa( size_t n, const float* pos, const float* vel, int space, const float* translate,
                          const float* scale, BoraParticlesDev p, size_t offset, int32_t first_id, cudaStream_t st );
 

@@ -612,8 +612,8 @@ int stage_update_particles( bora_flip_sim* s, float dt )
     const int nxt = s->cur ^ 1;
     {
         KTimer t( s, BORA_KERNEL_G2P, s->nsorted > 0 );
-        bora_launch_g2p( s->g, s->nsorted, P<int32_t>( s->slot_of ), s->cells(), s->parts( s->cur ), P<uint32_t>( s->idx ),
-                         s->parts( nxt ), P<float>( s->adj ), dt, P<uint32_t>( s->counters ) + 3, st );
+        bora_launch_g2p( s->g, s->ntiles, s->nsorted, s->tiles(), P<uint32_t>( s->cell_start ), s->cells(), s->parts( s->cur ),
+                         P<uint32_t>( s->idx ), s->parts( nxt ), P<float>( s->adj ), dt, P<uint32_t>( s->counters ) + 3, st );
     }
     BORA_TRYS( check_launch( s ) );
     BORA_TRYS( read_counters( s, 3, 1 ) );

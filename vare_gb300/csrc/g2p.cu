@@ -11,70 +11,113 @@
 
 namespace {
 
-struct CellLookup
-{
-    const BoraGridDev& g;
-    const int32_t* slot_of;
-    __device__ inline int index( int i, int j, int k ) const
-    {
-        const int s = slot_of[( (size_t)( k >> 3 ) * g.ty + ( j >> 3 ) ) * g.tx + ( i >> 3 )];
-        if( s < 0 ) return -1;
-        return s * BORA_TILE_CELLS + bora_local( i, j, k );
-    }
-};
+// Grid values of a tile and its high-side halo layer, (8+1)^3 cells, staged in shared
+// memory as two float4 per cell: (comp, surf) and (velo, 0). Cells of inactive tiles hold
+// the field backgrounds (0, and 10 for surf: FLIPMethod.cu:30).
+constexpr int kG2PThreads = 256;
+constexpr int kStageEdge = BORA_TILE + 1;
+constexpr int kStageCells = kStageEdge * kStageEdge * kStageEdge;
 
 // SparseField::lerp over a vector field (base/header/SparseField.h:150-173) and
-// SparseField::lerpMin over a scalar field (SparseField.h:176-196). Corner order:
-// (i,j,k),(i+1,j,k),(i,j,k+1),(i+1,j,k+1),(i,j+1,k),(i+1,j+1,k),(i,j+1,k+1),(i+1,j+1,k+1).
-struct Lerp8
+// SparseField::lerpMin over a scalar field (SparseField.h:176-196), from the staged tile.
+// Corner order: (i,j,k),(i+1,j,k),(i,j,k+1),(i+1,j,k+1),(i,j+1,k),(i+1,j+1,k),(i,j+1,k+1),
+// (i+1,j+1,k+1).
+struct StagedLerp
 {
-    int idx[8];  // cell index, -1 = background (inactive tile)
+    int base;  // staged index of corner (i,j,k)
     float x, y, z;
-    __device__ inline void setup( const CellLookup& L, float px, float py, float pz )
+    __device__ inline void setup( const BoraGridDev& g, int ti, int tj, int tk, float px, float py, float pz )
     {
-        const int i = bora_clampi( bora_trunc( px - 0.5f ), 0, L.g.nx - 2 );
-        const int j = bora_clampi( bora_trunc( py - 0.5f ), 0, L.g.ny - 2 );
-        const int k = bora_clampi( bora_trunc( pz - 0.5f ), 0, L.g.nz - 2 );
+        const int i = bora_clampi( bora_trunc( px - 0.5f ), 0, g.nx - 2 );
+        const int j = bora_clampi( bora_trunc( py - 0.5f ), 0, g.ny - 2 );
+        const int k = bora_clampi( bora_trunc( pz - 0.5f ), 0, g.nz - 2 );
         x = bora_clampf( px - ( (float)i + .5f ), 0.f, 1.f );
         y = bora_clampf( py - ( (float)j + .5f ), 0.f, 1.f );
         z = bora_clampf( pz - ( (float)k + .5f ), 0.f, 1.f );
-        const int b = L.index( i, j, k );
-        if( b >= 0 && ( i & 7 ) < 7 && ( j & 7 ) < 7 && ( k & 7 ) < 7 )
-        {
-            // the 2x2x2 block lies inside one tile
-            idx[0] = b; idx[1] = b + 1; idx[2] = b + 64; idx[3] = b + 65;
-            idx[4] = b + 8; idx[5] = b + 9; idx[6] = b + 72; idx[7] = b + 73;
-            return;
-        }
-        idx[0] = b;
-        idx[1] = L.index( i + 1, j, k );
-        idx[2] = L.index( i, j, k + 1 );
-        idx[3] = L.index( i + 1, j, k + 1 );
-        idx[4] = L.index( i, j + 1, k );
-        idx[5] = L.index( i + 1, j + 1, k );
-        idx[6] = L.index( i, j + 1, k + 1 );
-        idx[7] = L.index( i + 1, j + 1, k + 1 );
+        base = ( i - ti * BORA_TILE ) + kStageEdge * ( ( j - tj * BORA_TILE ) + kStageEdge * ( k - tk * BORA_TILE ) );
     }
-    __device__ inline float get( const float* __restrict__ f, int q, float bg ) const { return idx[q] < 0 ? bg : __ldg( f + idx[q] ); }
-    __device__ inline float lerp( const float* __restrict__ f ) const
+    __device__ static inline int off( int q )
     {
-        const float c00 = get( f, 0, 0.f ) * ( 1.f - x ) + get( f, 1, 0.f ) * x;
-        const float c01 = get( f, 2, 0.f ) * ( 1.f - x ) + get( f, 3, 0.f ) * x;
-        const float c10 = get( f, 4, 0.f ) * ( 1.f - x ) + get( f, 5, 0.f ) * x;
-        const float c11 = get( f, 6, 0.f ) * ( 1.f - x ) + get( f, 7, 0.f ) * x;
-        const float c0 = c00 * ( 1.f - y ) + c10 * y;
-        const float c1 = c01 * ( 1.f - y ) + c11 * y;
-        return c0 * ( 1.f - z ) + c1 * z;
+        return ( q & 1 ) + kStageEdge * kStageEdge * ( ( q >> 1 ) & 1 ) + kStageEdge * ( q >> 2 );
     }
-    __device__ inline float lerp_min( const float* __restrict__ f, float bg ) const
+    __device__ static inline float4 mix( float4 a, float4 b, float t )
     {
-        float v = fminf_ref( get( f, 0, bg ), get( f, 1, bg ) );
-        v = fminf_ref( v, fminf_ref( get( f, 2, bg ), get( f, 3, bg ) ) );
-        v = fminf_ref( v, fminf_ref( get( f, 4, bg ), get( f, 5, bg ) ) );
-        v = fminf_ref( v, fminf_ref( get( f, 6, bg ), get( f, 7, bg ) ) );
-        return v;
+        return make_float4( a.x * ( 1.f - t ) + b.x * t, a.y * ( 1.f - t ) + b.y * t, a.z * ( 1.f - t ) + b.z * t,
+                            a.w * ( 1.f - t ) + b.w * t );
+    }
+    __device__ inline float4 lerp( const float4* f ) const
+    {
+        const float4 c00 = mix( f[base + off( 0 )], f[base + off( 1 )], x );
+        const float4 c01 = mix( f[base + off( 2 )], f[base + off( 3 )], x );
+        const float4 c10 = mix( f[base + off( 4 )], f[base + off( 5 )], x );
+        const float4 c11 = mix( f[base + off( 6 )], f[base + off( 7 )], x );
+        return mix( mix( c00, c10, y ), mix( c01, c11, y ), z );
     }
     __device__ static inline float fminf_ref( float a, float b ) { return a < b ? a : b; }  // MathUtils.h:174
+    __device__ inline float lerp_min_w( const float4* f ) const
+    {
+        float v = fminf_ref( f[base + off( 0 )].w, f[base + off( 1 )].w );
+        v = fminf_ref( v, fminf_ref( f[base + off( 2 )].w, f[base + off( 3 )].w ) );
+        v = fminf_ref( v, fminf_ref( f[base + off( 4 )].w, f[base + off( 5 )].w ) );
+        v = fminf_ref( v, fminf_ref( f[base + off( 6 )].w, f[base + off( 7 )].w ) );
+        return v;
+    }
+};
+
+// The same lerps through the tile table, for the rare particles outside every tile (the
+// sort's last bin: particles added outside the grid, killed by this step's bounds check).
+struct GlobalLerp
+{
+    const BoraGridDev& g;
+    const int32_t* slot_of;
+    const BoraCellsDev& c;
+    int idx[8];  // cell index, -1 = background (inactive tile)
+    float x, y, z;
+    __device__ inline int index( int i, int j, int k ) const
+    {
+        const int s = slot_of[( (size_t)( k >> 3 ) * g.ty + ( j >> 3 ) ) * g.tx + ( i >> 3 )];
+        return s < 0 ? -1 : s * BORA_TILE_CELLS + bora_local( i, j, k );
+    }
+    __device__ inline void setup( float px, float py, float pz )
+    {
+        const int i = bora_clampi( bora_trunc( px - 0.5f ), 0, g.nx - 2 );
+        const int j = bora_clampi( bora_trunc( py - 0.5f ), 0, g.ny - 2 );
+        const int k = bora_clampi( bora_trunc( pz - 0.5f ), 0, g.nz - 2 );
+        x = bora_clampf( px - ( (float)i + .5f ), 0.f, 1.f );
+        y = bora_clampf( py - ( (float)j + .5f ), 0.f, 1.f );
+        z = bora_clampf( pz - ( (float)k + .5f ), 0.f, 1.f );
+        for( int q = 0; q < 8; ++q ) idx[q] = index( i + ( q & 1 ), j + ( q >> 2 ), k + ( ( q >> 1 ) & 1 ) );
+    }
+    __device__ inline float4 fa( int q ) const
+    {
+        return idx[q] < 0 ? make_float4( 0.f, 0.f, 0.f, 10.f )
+                          : make_float4( c.cx[idx[q]], c.cy[idx[q]], c.cz[idx[q]], c.surf[idx[q]] );
+    }
+    __device__ inline float4 fb( int q ) const
+    {
+        return idx[q] < 0 ? make_float4( 0.f, 0.f, 0.f, 0.f ) : make_float4( c.vx[idx[q]], c.vy[idx[q]], c.vz[idx[q]], 0.f );
+    }
+    template <bool A>
+    __device__ inline float4 lerp() const
+    {
+        auto f = [&]( int q ) { return A ? fa( q ) : fb( q ); };
+        const float4 c00 = StagedLerp::mix( f( 0 ), f( 1 ), x );
+        const float4 c01 = StagedLerp::mix( f( 2 ), f( 3 ), x );
+        const float4 c10 = StagedLerp::mix( f( 4 ), f( 5 ), x );
+        const float4 c11 = StagedLerp::mix( f( 6 ), f( 7 ), x );
+        return StagedLerp::mix( StagedLerp::mix( c00, c10, y ), StagedLerp::mix( c01, c11, y ), z );
+    }
+    __device__ inline float surf_min() const
+    {
+        auto w = [&]( int q ) { return fa( q ).w; };
+        float v = StagedLerp::fminf_ref( w( 0 ), w( 1 ) );
+        v = StagedLerp::fminf_ref( v, StagedLerp::fminf_ref( w( 2 ), w( 3 ) ) );
+        v = StagedLerp::fminf_ref( v, StagedLerp::fminf_ref( w( 4 ), w( 5 ) ) );
+        v = StagedLerp::fminf_ref( v, StagedLerp::fminf_ref( w( 6 ), w( 7 ) ) );
+        return v;
+    }
+    __device__ inline float4 comp() const { return lerp<true>(); }
+    __device__ inline float4 velo() const { return lerp<false>(); }
 };
 
 __device__ inline bool inside_grid( const BoraGridDev& g, float x, float y, float z )
@@ -114,81 +157,147 @@ __device__ __noinline__ bool col_kill( const BoraGridDev* g, float3 p )
     return phi > 3.f || phi < 0.f;
 }
 
-__global__ void __launch_bounds__( 256 ) k_g2p( const __grid_constant__ BoraGridDev g, size_t n, const int32_t* __restrict__ slot_of,
-                                                BoraCellsDev c, BoraParticlesDev src, const uint32_t* __restrict__ idx,
-                                                BoraParticlesDev dst, float* __restrict__ adj, float dt,
-                                                uint32_t* __restrict__ nkilled )
+// FLIPMethod::updateParticles for one particle (FLIPMethod.cu:60-170); `smp` has been set
+// up at the particle's position and gives the interpolated grid values.
+template <class Sampler>
+__device__ inline bool advance_particle( const BoraGridDev& g, const Sampler& smp, float& px, float& py, float& pz,
+                                         float& vx, float& vy, float& vz, float dt )
 {
-    const CellLookup L{ g, slot_of };
     const float lx = (float)g.nx + 0.5f, lz = (float)g.nz + 0.5f;
     const float wall = g.voxel_wall;
-    uint32_t kills = 0;
-    for( size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x )
     {
-        const uint32_t pi = idx[q];
-        float px = src.px[pi], py = src.py[pi], pz = src.pz[pi];
-        float vx = src.vx[pi], vy = src.vy[pi], vz = src.vz[pi];
-        int32_t id = src.id[pi];
-        Lerp8 lp;
-        lp.setup( L, px, py, pz );
-        adj[q] = lp.lerp_min( c.surf, 10.f );  // surf background 10 (FLIPMethod.cu:30)
+        const float4 gn = smp.comp(), go = smp.velo();
+        vx += gn.x - go.x; vy += gn.y - go.y; vz += gn.z - go.z;
+        vx = vx * 0.95f + gn.x * 0.05f;
+        vy = vy * 0.95f + gn.y * 0.05f;
+        vz = vz * 0.95f + gn.z * 0.05f;
+    }
+    if( g.enable_tank && py <= wall )
+    {
+        const float band = g.damping_band;
+        float w = 1.f;
+        if( px < band ) w = fminf( w, bora_clampf( ( px - 0.f ) / band, 0.f, 1.f ) );
+        if( px > lx - band ) w = fminf( w, bora_clampf( ( lx - px ) / band, 0.f, 1.f ) );
+        if( pz < band ) w = fminf( w, bora_clampf( ( pz - 0.f ) / band, 0.f, 1.f ) );
+        if( pz > lz - band ) w = fminf( w, bora_clampf( ( lz - pz ) / band, 0.f, 1.f ) );
+        vx *= w; vy *= w; vz *= w;
+    }
+    const bool hasCols = g.cols.count > 0;
+    if( hasCols )
+    {
+        const float3 p = col_carry( &g, make_float3( px, py, pz ), dt );
+        px = p.x; py = p.y; pz = p.z;
+    }
+    bool kill = false;
+    {
+        const float len = sqrtf( vx * vx + vy * vy + vz * vz );
+        const int iter = 1 + bora_imin( bora_trunc( len * dt * 1.5f ), bora_imax( g.maxsubsteps, 1 ) );
+        const float sub_dt = dt / (float)iter;
+        bool col = false;
+        for( int it = 0; it < iter; ++it )
         {
-            const float gx = lp.lerp( c.cx ), gy = lp.lerp( c.cy ), gz = lp.lerp( c.cz );
-            const float ox = lp.lerp( c.vx ), oy = lp.lerp( c.vy ), oz = lp.lerp( c.vz );
-            vx += gx - ox; vy += gy - oy; vz += gz - oz;
-            vx = vx * 0.95f + gx * 0.05f;
-            vy = vy * 0.95f + gy * 0.05f;
-            vz = vz * 0.95f + gz * 0.05f;
-        }
-        if( g.enable_tank && py <= wall )
-        {
-            const float band = g.damping_band;
-            float w = 1.f;
-            if( px < band ) w = fminf( w, bora_clampf( ( px - 0.f ) / band, 0.f, 1.f ) );
-            if( px > lx - band ) w = fminf( w, bora_clampf( ( lx - px ) / band, 0.f, 1.f ) );
-            if( pz < band ) w = fminf( w, bora_clampf( ( pz - 0.f ) / band, 0.f, 1.f ) );
-            if( pz > lz - band ) w = fminf( w, bora_clampf( ( lz - pz ) / band, 0.f, 1.f ) );
-            vx *= w; vy *= w; vz *= w;
-        }
-        const bool hasCols = g.cols.count > 0;
-        if( hasCols )
-        {
-            const float3 p = col_carry( &g, make_float3( px, py, pz ), dt );
-            px = p.x; py = p.y; pz = p.z;
-        }
-        bool kill = false;
-        {
-            const float len = sqrtf( vx * vx + vy * vy + vz * vz );
-            const int iter = 1 + bora_imin( bora_trunc( len * dt * 1.5f ), bora_imax( g.maxsubsteps, 1 ) );
-            const float sub_dt = dt / (float)iter;
-            bool col = false;
-            for( int it = 0; it < iter; ++it )
+            px += vx * sub_dt; py += vy * sub_dt; pz += vz * sub_dt;
+            if( py <= wall )
             {
-                px += vx * sub_dt; py += vy * sub_dt; pz += vz * sub_dt;
-                if( py <= wall )
-                {
-                    if( px < 0.f ) { px = 0.f; if( vx < 0.f ) vx = 0.f; }
-                    if( py < 0.f ) { py = 0.f; if( vy < 0.f ) vy = 0.f; }
-                    if( pz < 0.f ) { pz = 0.f; if( vz < 0.f ) vz = 0.f; }
-                    if( px > (float)g.nx ) { px = (float)g.nx; if( vx > 0.f ) vx = 0.f; }
-                    if( py > (float)g.ny ) { py = (float)g.ny; if( vy > 0.f ) vy = 0.f; }
-                    if( pz > (float)g.nz ) { pz = (float)g.nz; if( vz > 0.f ) vz = 0.f; }
-                }
-                if( hasCols )
-                {
-                    const float4 r = col_push( &g, make_float3( px, py, pz ) );
-                    px = r.x; py = r.y; pz = r.z;
-                    if( r.w != 0.f ) col = true;
-                }
+                if( px < 0.f ) { px = 0.f; if( vx < 0.f ) vx = 0.f; }
+                if( py < 0.f ) { py = 0.f; if( vy < 0.f ) vy = 0.f; }
+                if( pz < 0.f ) { pz = 0.f; if( vz < 0.f ) vz = 0.f; }
+                if( px > (float)g.nx ) { px = (float)g.nx; if( vx > 0.f ) vx = 0.f; }
+                if( py > (float)g.ny ) { py = (float)g.ny; if( vy > 0.f ) vy = 0.f; }
+                if( pz > (float)g.nz ) { pz = (float)g.nz; if( vz > 0.f ) vz = 0.f; }
             }
-            if( col && col_kill( &g, make_float3( px, py, pz ) ) ) kill = true;
-            if( !inside_grid( g, px, py, pz ) ) kill = true;
+            if( hasCols )
+            {
+                const float4 r = col_push( &g, make_float3( px, py, pz ) );
+                px = r.x; py = r.y; pz = r.z;
+                if( r.w != 0.f ) col = true;
+            }
         }
-        vx += g.gravity[0] * dt; vy += g.gravity[1] * dt; vz += g.gravity[2] * dt;
+        if( col && col_kill( &g, make_float3( px, py, pz ) ) ) kill = true;
+        if( !inside_grid( g, px, py, pz ) ) kill = true;
+    }
+    vx += g.gravity[0] * dt; vy += g.gravity[1] * dt; vz += g.gravity[2] * dt;
+    return kill;
+}
+
+struct StagedSampler
+{
+    StagedLerp l;
+    const float4* fa;
+    const float4* fb;
+    __device__ inline float4 comp() const { return l.lerp( fa ); }
+    __device__ inline float4 velo() const { return l.lerp( fb ); }
+    __device__ inline float surf_min() const { return l.lerp_min_w( fa ); }
+};
+
+// One CTA per tile: stage the tile's grid values, then advance the particles of the
+// tile's dual cells (a contiguous range of the sorted order). The CTA after the last tile
+// advances the sort's outside bin through the tile table.
+__global__ void __launch_bounds__( kG2PThreads ) k_g2p( const __grid_constant__ BoraGridDev g, BoraTilesDev t, int ntiles,
+                                                       uint32_t nsorted, const uint32_t* __restrict__ start, BoraCellsDev c,
+                                                       BoraParticlesDev src, const uint32_t* __restrict__ idx,
+                                                       BoraParticlesDev dst, float* __restrict__ adj, float dt,
+                                                       uint32_t* __restrict__ nkilled )
+{
+    __shared__ float4 fa[kStageCells];  // comp, surf
+    __shared__ float4 fb[kStageCells];  // velo, 0
+    __shared__ int32_t nb[27];
+    const int s = blockIdx.x, tid = threadIdx.x;
+    uint32_t kills = 0;
+    auto finish = [&]( uint32_t q, uint32_t pi, float px, float py, float pz, float vx, float vy, float vz, bool kill ) {
         dst.px[q] = px; dst.py[q] = py; dst.pz[q] = pz;
         dst.vx[q] = vx; dst.vy[q] = vy; dst.vz[q] = vz;
-        dst.id[q] = kill ? -1 : id;
+        dst.id[q] = kill ? -1 : src.id[pi];
         kills += kill ? 1u : 0u;
+    };
+    if( s == ntiles )
+    {
+        const uint32_t q0 = start[(size_t)ntiles * BORA_TILE_CELLS], q1 = nsorted;
+        for( uint32_t q = q0 + tid; q < q1; q += kG2PThreads )
+        {
+            const uint32_t pi = idx[q];
+            float px = src.px[pi], py = src.py[pi], pz = src.pz[pi];
+            float vx = src.vx[pi], vy = src.vy[pi], vz = src.vz[pi];
+            GlobalLerp smp{ g, t.slot_of, c };
+            smp.setup( px, py, pz );
+            adj[q] = smp.surf_min();
+            const bool kill = advance_particle( g, smp, px, py, pz, vx, vy, vz, dt );
+            finish( q, pi, px, py, pz, vx, vy, vz, kill );
+        }
+    }
+    else
+    {
+        if( tid < 27 ) nb[tid] = t.nbr[(size_t)s * 27 + tid];
+        const int vt = t.tile_of[s];
+        const int ti = vt % g.tx, tj = ( vt / g.tx ) % g.ty, tk = vt / ( g.tx * g.ty );
+        __syncthreads();
+        for( int h = tid; h < kStageCells; h += kG2PThreads )
+        {
+            const int a = h % kStageEdge, b = ( h / kStageEdge ) % kStageEdge, cz = h / ( kStageEdge * kStageEdge );
+            const int ns = nb[bora_dir( a >> 3, b >> 3, cz >> 3 )];
+            float4 va = make_float4( 0.f, 0.f, 0.f, 10.f ), vb = make_float4( 0.f, 0.f, 0.f, 0.f );
+            if( ns >= 0 )
+            {
+                const size_t q = (size_t)ns * BORA_TILE_CELLS + (size_t)bora_local( a, b, cz );
+                va = make_float4( c.cx[q], c.cy[q], c.cz[q], c.surf[q] );
+                vb = make_float4( c.vx[q], c.vy[q], c.vz[q], 0.f );
+            }
+            fa[h] = va;
+            fb[h] = vb;
+        }
+        __syncthreads();
+        const uint32_t q0 = start[(size_t)s * BORA_TILE_CELLS], q1 = start[(size_t)( s + 1 ) * BORA_TILE_CELLS];
+        for( uint32_t q = q0 + tid; q < q1; q += kG2PThreads )
+        {
+            const uint32_t pi = idx[q];
+            float px = src.px[pi], py = src.py[pi], pz = src.pz[pi];
+            float vx = src.vx[pi], vy = src.vy[pi], vz = src.vz[pi];
+            StagedSampler smp{ {}, fa, fb };
+            smp.l.setup( g, ti, tj, tk, px, py, pz );
+            adj[q] = smp.surf_min();  // surf background 10 (FLIPMethod.cu:30)
+            const bool kill = advance_particle( g, smp, px, py, pz, vx, vy, vz, dt );
+            finish( q, pi, px, py, pz, vx, vy, vz, kill );
+        }
     }
     // one atomic per warp
     for( int o = 16; o > 0; o >>= 1 ) kills += __shfl_xor_sync( 0xffffffffu, kills, o );
@@ -197,11 +306,10 @@ __global__ void __launch_bounds__( 256 ) k_g2p( const __grid_constant__ BoraGrid
 
 }  // namespace
 
-void bora_launch_g2p( const BoraGridDev& g, size_t n, const int32_t* slot_of, BoraCellsDev c, BoraParticlesDev src,
-                      const uint32_t* idx, BoraParticlesDev dst, float* adj, float dt, uint32_t* nkilled, cudaStream_t st )
+void bora_launch_g2p( const BoraGridDev& g, int ntiles, size_t nsorted, BoraTilesDev t, const uint32_t* start, BoraCellsDev c,
+                      BoraParticlesDev src, const uint32_t* idx, BoraParticlesDev dst, float* adj, float dt,
+                      uint32_t* nkilled, cudaStream_t st )
 {
-    if( n == 0 ) return;
-    size_t b = ( n + 255 ) / 256;
-    if( b > 152 * 16 ) b = 152 * 16;
-    k_g2p<<<(int)b, 256, 0, st>>>( g, n, slot_of, c, src, idx, dst, adj, dt, nkilled );
+    if( nsorted == 0 ) return;
+    k_g2p<<<ntiles + 1, kG2PThreads, 0, st>>>( g, t, ntiles, (uint32_t)nsorted, start, c, src, idx, dst, adj, dt, nkilled );
 }
