@@ -81,7 +81,7 @@ typedef struct bora_flip_params
     double div_tolerance;    /* 1e-5: ... and max_i |b - A p|_i * dx_world < div_tolerance */
     double inner_tolerance;  /* 1e-4: relative residual reduction of each FP32 inner solve */
     int max_refinements;     /* 8: outer FP64 refinement passes */
-    int check_every;         /* 8: inner iterations between convergence checks */
+    int check_every;         /* 1: inner iterations between convergence checks (read back one iteration late) */
 } bora_flip_params;
 
 typedef struct bora_flip_stats

@@ -57,6 +57,7 @@ struct BoraReduceDev
     double* partials;    // [max blocks * 2]
     uint32_t* done;      // [BORA_RING] block-arrival counters
     uint32_t* err;       // set non-zero by a kernel that met an inconsistent stencil code
+    double* mirror;      // [BORA_RING] host-mapped copy of the slot values, or null
 };
 
 // ---- launchers -----------------------------------------------------------------------

@@ -128,6 +128,10 @@ struct bora_flip_sim
     DevBuf scan_scratch, counters, stage_in, stage_out, live_flag;
     uint32_t* h_cnt = nullptr;  // pinned
     double* h_ring = nullptr;   // pinned
+    double* h_mirror = nullptr;  // pinned, mapped: reductions' slot values as the host sees them
+    double* d_mirror = nullptr;  // its device address
+    static constexpr int kChecks = 8;
+    cudaEvent_t ev_chk[kChecks] = {};
 
     bora_flip_stats stats{};
     int last_status = BORA_OK;
@@ -184,7 +188,8 @@ struct bora_flip_sim
     }
     BoraReduceDev reducer()
     {
-        return BoraReduceDev{ P<double>( ring ), P<double>( partials ), P<uint32_t>( done ), P<uint32_t>( counters ) + 5 };
+        return BoraReduceDev{ P<double>( ring ), P<double>( partials ), P<uint32_t>( done ), P<uint32_t>( counters ) + 5,
+                              d_mirror };
     }
     int slot()
     {
@@ -527,7 +532,7 @@ int stage_solve( bora_flip_sim* s )
         for( int l = 0; l + 1 < s->nlevels; ++l ) vlaunch += ( s->levels[l].kind == 0 && s->levels[l].E >= 2 ) ? 2 : 4;
         auto precondition = [&]( int rr_slot, int rz_slot ) {
             KTimer t( s, BORA_KERNEL_MG, vlaunch );
-            bora_mg_vcycle( s->g, s->levels, s->nlevels, s->tiles(), sv.r, sv.z, red, rr_slot, rz_slot, 32, st );
+            bora_mg_vcycle( s->g, s->levels, s->nlevels, s->tiles(), sv.r, sv.z, red, rr_slot, rz_slot, 16, st );
         };
         int rz_cur = s->slot(), rr_cur = s->slot();
         if( mixed )
@@ -540,8 +545,16 @@ int stage_solve( bora_flip_sim* s )
             KTimer t( s, BORA_KERNEL_PCG_UPDATE, 1 );
             bora_launch_pcg_update( s->ntiles, code, sv, 0, red, -1, -1, rz_cur, rr_cur, st );
         }
+        // Convergence checks do not stall the device: the reductions also write their
+        // results to mapped host memory, an event marks the end of iteration i, and the
+        // host waits for it only once iteration i + 1 is queued (a converged solve runs one
+        // extra iteration, which only lowers the residual further).
+        struct Check { int it, q, slot; };
+        Check pend[bora_flip_sim::kChecks];
+        int npend = 0, nchk = 0;
+        bool done = false;
         int rz_prev = -1, dsel = 0, it = 0;
-        while( it < max_inner )
+        while( it < max_inner && !done )
         {
             const int s_dq = s->slot();
             { KTimer t( s, BORA_KERNEL_PCG_DIRECTION, 1 ); bora_launch_pcg_direction( s->g, s->ntiles, s->tiles(), code, sv, dsel, red, rz_cur, rz_prev, s_dq, st ); }
@@ -564,9 +577,17 @@ int stage_solve( bora_flip_sim* s )
             if( it % check == 0 )
             {
                 BORA_TRYS( check_launch( s ) );
-                const double rr = read_ring( s, rr_cur, &status );
-                BORA_TRYS( status );
-                if( !( rr > 0.0 ) || std::sqrt( rr ) <= target ) break;
+                const int q = nchk++ % bora_flip_sim::kChecks;
+                BORA_TRY( cudaEventRecord( s->ev_chk[q], st ) );
+                pend[npend++] = Check{ it, q, rr_cur };
+            }
+            while( npend > 0 && ( it - pend[0].it >= 1 || npend == bora_flip_sim::kChecks || it >= max_inner ) )
+            {
+                BORA_TRY( cudaEventSynchronize( s->ev_chk[pend[0].q] ) );
+                const double rr = ( (volatile double*)s->h_mirror )[pend[0].slot];
+                for( int k = 1; k < npend; ++k ) pend[k - 1] = pend[k];
+                --npend;
+                if( !( rr > 0.0 ) || std::sqrt( rr ) <= target ) { done = true; break; }
             }
         }
         total_it += it;
@@ -679,7 +700,7 @@ int bora_flip_default_params( bora_flip_params* o )
     o->div_tolerance = 1e-5;
     o->inner_tolerance = 1e-4;
     o->max_refinements = 8;
-    o->check_every = 8;
+    o->check_every = 1;
     return BORA_OK;
 }
 
@@ -718,6 +739,10 @@ int bora_flip_create( const bora_grid_desc* grid, const bora_flip_params* params
     if( st == BORA_OK ) st = cuda_status( cudaEventCreate( &s->ev_step[1] ) );
     if( st == BORA_OK ) st = cuda_status( cudaHostAlloc( (void**)&s->h_cnt, 64, cudaHostAllocDefault ) );
     if( st == BORA_OK ) st = cuda_status( cudaHostAlloc( (void**)&s->h_ring, 64, cudaHostAllocDefault ) );
+    if( st == BORA_OK ) st = cuda_status( cudaHostAlloc( (void**)&s->h_mirror, BORA_RING * 8, cudaHostAllocMapped ) );
+    if( st == BORA_OK ) st = cuda_status( cudaHostGetDevicePointer( (void**)&s->d_mirror, s->h_mirror, 0 ) );
+    for( int q = 0; q < bora_flip_sim::kChecks && st == BORA_OK; ++q )
+        st = cuda_status( cudaEventCreateWithFlags( &s->ev_chk[q], cudaEventDisableTiming ) );
     if( st == BORA_OK ) st = cuda_status( grow( s->tile_flag, s->ntv, false, s->st ) );
     if( st == BORA_OK ) st = cuda_status( grow( s->tile_act, s->ntv * 4, false, s->st ) );
     if( st == BORA_OK ) st = cuda_status( grow( s->tile_excl, s->ntv * 4, false, s->st ) );
@@ -760,8 +785,11 @@ int bora_flip_destroy( bora_flip_handle s )
     for( cudaEvent_t e : s->evpool ) cudaEventDestroy( e );
     for( int q = 0; q < 2; ++q )
         if( s->ev_step[q] ) cudaEventDestroy( s->ev_step[q] );
+    for( cudaEvent_t e : s->ev_chk )
+        if( e ) cudaEventDestroy( e );
     if( s->h_cnt ) cudaFreeHost( s->h_cnt );
     if( s->h_ring ) cudaFreeHost( s->h_ring );
+    if( s->h_mirror ) cudaFreeHost( s->h_mirror );
     if( s->st ) cudaStreamDestroy( s->st );
     delete s;
     return BORA_OK;

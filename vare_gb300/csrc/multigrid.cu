@@ -29,7 +29,7 @@
 
 namespace {
 
-constexpr float kOmega = 0.8f;
+constexpr float kOmega = 6.f / 7.f;  // damped Jacobi weight for the 7-point operator
 
 __device__ inline int code_diag( uint16_t c ) { return ( c >> 8 ) & 15; }
 

@@ -108,6 +108,11 @@ __device__ __forceinline__ void reduce2_publish_warp( double v0, double v1, int 
         for( int q = 0; q < nw; ++q ) { ta += w0[q]; tb = op1 ? fmax( tb, w1[q] ) : tb + w1[q]; }
         if( slot0 >= 0 ) red.ring[slot0] = ta;
         if( slot1 >= 0 ) red.ring[slot1] = tb;
+        if( red.mirror )  // host-visible once the kernel has completed
+        {
+            if( slot0 >= 0 ) red.mirror[slot0] = ta;
+            if( slot1 >= 0 ) red.mirror[slot1] = tb;
+        }
         const int key = slot0 >= 0 ? slot0 : slot1;
         red.done[key % BORA_RING] = 0;
         __threadfence();
