@@ -133,6 +133,8 @@ struct BoraLevelDev
 // Cell types and stencil codes of level c from level c-1 (levels[0] = fine, given).
 void bora_mg_setup( const BoraGridDev& g, BoraLevelDev* levels, int nlevels, BoraTilesDev t, uint32_t* err, cudaStream_t st );
 // One V-cycle: z = M^-1 r (FP32 in and out, FP16 inside); r.z -> ring slot (FP64-accurate).
+// Kernel launches of one bora_mg_vcycle call for this hierarchy.
+int bora_mg_vcycle_launches( const BoraLevelDev* levels, int nlevels );
 void bora_mg_vcycle( const BoraGridDev& g, const BoraLevelDev* levels, int nlevels, BoraTilesDev t, const float* r,
                      float* z, BoraReduceDev red, int slot_rr, int slot_rz, int coarse_sweeps, cudaStream_t st );
 // e += alpha d; r -= alpha q; r.r -> ring slot (alpha = rz / dq, or 0 when slot_rz < 0)

@@ -528,8 +528,7 @@ int stage_solve( bora_flip_sim* s )
         // inner FP32 PCG on A e = r
         const double target = norm_ok ? 0.1 * rnorm : std::max( p.inner_tolerance * rnorm, 0.25 * p.tolerance * bnorm );
         const bool mixed = p.solver == BORA_SOLVER_MIXED;
-        int vlaunch = 1;  // coarsest
-        for( int l = 0; l + 1 < s->nlevels; ++l ) vlaunch += ( s->levels[l].kind == 0 && s->levels[l].E >= 2 ) ? 2 : 4;
+        const int vlaunch = bora_mg_vcycle_launches( s->levels, s->nlevels );
         auto precondition = [&]( int rr_slot, int rz_slot ) {
             KTimer t( s, BORA_KERNEL_MG, vlaunch );
             bora_mg_vcycle( s->g, s->levels, s->nlevels, s->tiles(), sv.r, sv.z, red, rr_slot, rz_slot, 16, st );

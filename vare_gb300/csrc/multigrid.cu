@@ -262,18 +262,18 @@ struct RIn
 
 __device__ inline float ldh( const __half* z, long long c ) { return __half2float( z[c] ); }
 
+// The per-level operations below are written as device functions over a strided cell
+// range, so that the same code runs as one grid-wide kernel per operation (large levels)
+// or, for the small tail of the hierarchy, inside one CTA that walks several levels with
+// CTA barriers in between (k_mg_tail).
+
 // z = two damped-Jacobi sweeps from zero: z1 = w r'/d, z2 = z1 + w (r' - S z1)/d, with
 // each neighbour's z1 recomputed from its own r' and diagonal.
 template <class Nav>
-__global__ void __launch_bounds__( 256 ) k_mg_smooth0( Nav nav, BoraLevelDev L, const float* __restrict__ r0,
-                                                       int slot_rr, const double* __restrict__ ring, uint32_t* err )
+__device__ inline void smooth0_cells( const Nav& nav, const BoraLevelDev& L, const RIn& R, uint32_t* err, long long i0,
+                                      long long stride )
 {
-    __shared__ float s_scale;
-    if( threadIdx.x == 0 ) s_scale = r0 ? scale_of( ring, slot_rr ) : 1.f;
-    __syncthreads();
-    const RIn R{ r0, s_scale, L.r };
-    for( long long cell = blockIdx.x * (long long)blockDim.x + threadIdx.x; cell < (long long)L.ncells;
-         cell += (long long)gridDim.x * blockDim.x )
+    for( long long cell = i0; cell < (long long)L.ncells; cell += stride )
     {
         const uint16_t cc = L.code[cell];
         float z2 = 0.f;
@@ -304,22 +304,16 @@ __global__ void __launch_bounds__( 256 ) k_mg_smooth0( Nav nav, BoraLevelDev L, 
 //   mode 0: C tiled (edge EC), F tiled (edge 2 EC) in the same tile;
 //   mode 1: C dense, F tiled with one cell per tile (children are tiles, via slot_of);
 //   mode 2: C dense, F dense.
+// i0 and stride are multiples of 8 apart within a warp (every lane of a warp runs the
+// same number of iterations).
 template <class FNav, int MODE, int EC>
-__global__ void __launch_bounds__( 256 ) k_mg_restrict( FNav fnav, BoraLevelDev F, BoraLevelDev C,
-                                                        const float* __restrict__ r0, int slot_rr,
-                                                        const double* __restrict__ ring,
-                                                        const int32_t* __restrict__ slot_of, int tx, int ty, int tz,
-                                                        uint32_t* err )
+__device__ inline void restrict_cells( const FNav& fnav, const BoraLevelDev& F, const BoraLevelDev& C, const RIn& R,
+                                       const int32_t* __restrict__ slot_of, int tx, int ty, int tz, uint32_t* err,
+                                       long long i0, long long stride )
 {
-    __shared__ float s_scale;
-    if( threadIdx.x == 0 ) s_scale = r0 ? scale_of( ring, slot_rr ) : 1.f;
-    __syncthreads();
-    const RIn R{ r0, s_scale, F.r };
     const long long total = (long long)C.ncells * 8;
-    const long long stride = (long long)gridDim.x * blockDim.x;
-    // every lane of a warp runs the same number of iterations (total and stride are multiples of 8 / 32)
     const long long tround = ( total + 31 ) & ~31LL;
-    for( long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tround; t += stride )
+    for( long long t = i0; t < tround; t += stride )
     {
         const long long pc = t >> 3;
         const int o = (int)( t & 7 );
@@ -336,8 +330,6 @@ __global__ void __launch_bounds__( 256 ) k_mg_restrict( FNav fnav, BoraLevelDev 
                 const int ci = l & ( EC - 1 ), cj = ( l >> LC ) & ( EC - 1 ), ck = l >> ( 2 * LC );
                 fc = s * ( EF * EF * EF ) + ( 2 * ci + ( o & 1 ) ) + EF * ( ( 2 * cj + ( ( o >> 1 ) & 1 ) ) +
                                                                            EF * ( 2 * ck + ( o >> 2 ) ) );
-                int a = 0;  // children beyond the domain are masked cells: their code is 0
-                (void)a;
             }
             else
             {
@@ -352,7 +344,7 @@ __global__ void __launch_bounds__( 256 ) k_mg_restrict( FNav fnav, BoraLevelDev 
                     fc = (long long)a + (long long)F.dx * ( b + (long long)F.dy * c );
                 }
             }
-            if( fc >= 0 )
+            if( fc >= 0 )  // children beyond the domain are masked cells: their code is 0
             {
                 const uint16_t cf = F.code[fc];
                 if( cf & BORA_CODE_FLUID )
@@ -377,19 +369,25 @@ __global__ void __launch_bounds__( 256 ) k_mg_restrict( FNav fnav, BoraLevelDev 
     }
 }
 
-// Coarsest level (<= 512 cells): Jacobi sweeps from zero in one CTA, in shared memory.
-template <class Nav>
-__global__ void __launch_bounds__( 512 ) k_mg_coarsest( Nav nav, BoraLevelDev L, int sweeps, uint32_t* err )
+// Coarsest level (<= 512 cells): Jacobi sweeps from zero in shared memory; threads 0..511
+// of the CTA own one cell each, every thread of the CTA takes part in the barriers.
+struct CoarsestSmem
 {
-    __shared__ float zs[2][512], rs[512];
-    __shared__ int16_t nbs[512][6];
+    float zs[2][512], rs[512];
+    int16_t nbs[512][6];
+};
+
+template <class Nav>
+__device__ inline void coarsest_cells( const Nav& nav, const BoraLevelDev& L, int sweeps, uint32_t* err, CoarsestSmem& sm )
+{
     const int c = threadIdx.x;
+    const bool mine = c < 512;
     const bool valid = c < (int)L.ncells;
     uint16_t cc = 0;
     if( valid )
     {
         cc = L.code[c];
-        rs[c] = __half2float( L.r[c] );
+        sm.rs[c] = __half2float( L.r[c] );
         for( int q = 0; q < 6; ++q )
         {
             long long n = -1;
@@ -398,11 +396,10 @@ __global__ void __launch_bounds__( 512 ) k_mg_coarsest( Nav nav, BoraLevelDev L,
                 n = nav.nb( c, q );
                 if( n < 0 || n >= (long long)L.ncells ) { atomicOr( err, 16u ); n = -1; }
             }
-            nbs[c][q] = (int16_t)n;
+            sm.nbs[c][q] = (int16_t)n;
         }
     }
-    zs[0][c] = 0.f;
-    zs[1][c] = 0.f;
+    if( mine ) { sm.zs[0][c] = 0.f; sm.zs[1][c] = 0.f; }
     __syncthreads();
     int cur = 0;
     const int dg = code_diag( cc );
@@ -414,30 +411,24 @@ __global__ void __launch_bounds__( 512 ) k_mg_coarsest( Nav nav, BoraLevelDev L,
         {
             float sum = 0.f;
             for( int q = 0; q < 6; ++q )
-                if( nbs[c][q] >= 0 ) sum += zs[cur][nbs[c][q]];
-            const float z = zs[cur][c];
-            zn = z + kOmega * ( rs[c] - ( (float)dg * z - sum ) ) / (float)dg;
+                if( sm.nbs[c][q] >= 0 ) sum += sm.zs[cur][sm.nbs[c][q]];
+            const float z = sm.zs[cur][c];
+            zn = z + kOmega * ( sm.rs[c] - ( (float)dg * z - sum ) ) / (float)dg;
         }
-        zs[cur ^ 1][c] = zn;
+        if( mine ) sm.zs[cur ^ 1][c] = zn;
         __syncthreads();
         cur ^= 1;
     }
-    if( valid ) L.z0[c] = __float2half_rn( zs[cur][c] );
+    if( valid ) L.z0[c] = __float2half_rn( sm.zs[cur][c] );
 }
 
 // z_a = z0 + P e (injection of the coarse correction C.z0), then one Jacobi sweep;
 // neighbours' z_a are formed the same way. Writes z1.
 template <class Nav>
-__global__ void __launch_bounds__( 256 ) k_mg_prolong_smooth( Nav nav, BoraLevelDev F, const __half* __restrict__ ec,
-                                                              const float* __restrict__ r0, int slot_rr,
-                                                              const double* __restrict__ ring, uint32_t* err )
+__device__ inline void prolong_smooth_cells( const Nav& nav, const BoraLevelDev& F, const __half* __restrict__ ec,
+                                             const RIn& R, uint32_t* err, long long i0, long long stride )
 {
-    __shared__ float s_scale;
-    if( threadIdx.x == 0 ) s_scale = r0 ? scale_of( ring, slot_rr ) : 1.f;
-    __syncthreads();
-    const RIn R{ r0, s_scale, F.r };
-    for( long long cell = blockIdx.x * (long long)blockDim.x + threadIdx.x; cell < (long long)F.ncells;
-         cell += (long long)gridDim.x * blockDim.x )
+    for( long long cell = i0; cell < (long long)F.ncells; cell += stride )
     {
         const uint16_t cc = F.code[cell];
         float zb = 0.f;
@@ -461,20 +452,13 @@ __global__ void __launch_bounds__( 256 ) k_mg_prolong_smooth( Nav nav, BoraLevel
 }
 
 // Final Jacobi sweep of a level: z = z1 + w (r' - S z1)/d, written to z0. On level 0 the
-// result is unscaled to FP32 into zout and r.z is accumulated (double-float, FP64 per warp).
+// result is unscaled to FP32 into zout and r.z is accumulated (double-float).
 template <class Nav>
-__global__ void __launch_bounds__( 256 ) k_mg_smooth_last( Nav nav, BoraLevelDev L, const float* __restrict__ r0,
-                                                           int slot_rr, BoraReduceDev red, float* __restrict__ zout,
-                                                           int slot_rz )
+__device__ inline DF smooth_last_cells( const Nav& nav, const BoraLevelDev& L, const RIn& R, float* __restrict__ zout,
+                                        uint32_t* err, long long i0, long long stride )
 {
-    __shared__ float s_scale;
-    if( threadIdx.x == 0 ) s_scale = r0 ? scale_of( red.ring, slot_rr ) : 1.f;
-    __syncthreads();
-    const float sc = s_scale;
-    const RIn R{ r0, sc, L.r };
     DF rz{ 0.f, 0.f };
-    for( long long cell = blockIdx.x * (long long)blockDim.x + threadIdx.x; cell < (long long)L.ncells;
-         cell += (long long)gridDim.x * blockDim.x )
+    for( long long cell = i0; cell < (long long)L.ncells; cell += stride )
     {
         const uint16_t cc = L.code[cell];
         float zc = 0.f;
@@ -488,23 +472,141 @@ __global__ void __launch_bounds__( 256 ) k_mg_smooth_last( Nav nav, BoraLevelDev
             {
                 if( !( cc & ( 1u << q ) ) ) continue;
                 const long long n = nav.nb( cell, q );
-                if( n < 0 ) { atomicOr( red.err, 64u ); continue; }
+                if( n < 0 ) { atomicOr( err, 64u ); continue; }
                 sum += ldh( L.z1, n );
             }
             zc = zb + kOmega * ( R( cell ) - ( (float)dg * zb - sum ) ) / (float)dg;
         }
         if( zout )
         {
-            const float zf = zc / sc;  // undo the FP16 scaling of the residual
+            const float zf = zc / R.s;  // undo the FP16 scaling of the residual
             zout[cell] = zf;
-            if( cc & BORA_CODE_FLUID ) rz = df_add( rz, df_prod( r0[cell], zf ) );
+            if( cc & BORA_CODE_FLUID ) rz = df_add( rz, df_prod( R.r0[cell], zf ) );
         }
         else
         {
             L.z0[cell] = __float2half_rn( zc );
         }
     }
+    return rz;
+}
+
+// Grid-wide kernels, one per operation.
+__device__ inline long long gtid() { return blockIdx.x * (long long)blockDim.x + threadIdx.x; }
+__device__ inline long long gstride() { return (long long)gridDim.x * blockDim.x; }
+
+template <class Nav>
+__global__ void __launch_bounds__( 256 ) k_mg_smooth0( Nav nav, BoraLevelDev L, const float* __restrict__ r0,
+                                                       int slot_rr, const double* __restrict__ ring, uint32_t* err )
+{
+    __shared__ float s_scale;
+    if( threadIdx.x == 0 ) s_scale = r0 ? scale_of( ring, slot_rr ) : 1.f;
+    __syncthreads();
+    smooth0_cells( nav, L, RIn{ r0, s_scale, L.r }, err, gtid(), gstride() );
+}
+
+template <class FNav, int MODE, int EC>
+__global__ void __launch_bounds__( 256 ) k_mg_restrict( FNav fnav, BoraLevelDev F, BoraLevelDev C,
+                                                        const float* __restrict__ r0, int slot_rr,
+                                                        const double* __restrict__ ring,
+                                                        const int32_t* __restrict__ slot_of, int tx, int ty, int tz,
+                                                        uint32_t* err )
+{
+    __shared__ float s_scale;
+    if( threadIdx.x == 0 ) s_scale = r0 ? scale_of( ring, slot_rr ) : 1.f;
+    __syncthreads();
+    restrict_cells<FNav, MODE, EC>( fnav, F, C, RIn{ r0, s_scale, F.r }, slot_of, tx, ty, tz, err, gtid(), gstride() );
+}
+
+template <class Nav>
+__global__ void __launch_bounds__( 512 ) k_mg_coarsest( Nav nav, BoraLevelDev L, int sweeps, uint32_t* err )
+{
+    __shared__ CoarsestSmem sm;
+    coarsest_cells( nav, L, sweeps, err, sm );
+}
+
+template <class Nav>
+__global__ void __launch_bounds__( 256 ) k_mg_prolong_smooth( Nav nav, BoraLevelDev F, const __half* __restrict__ ec,
+                                                              const float* __restrict__ r0, int slot_rr,
+                                                              const double* __restrict__ ring, uint32_t* err )
+{
+    __shared__ float s_scale;
+    if( threadIdx.x == 0 ) s_scale = r0 ? scale_of( ring, slot_rr ) : 1.f;
+    __syncthreads();
+    prolong_smooth_cells( nav, F, ec, RIn{ r0, s_scale, F.r }, err, gtid(), gstride() );
+}
+
+template <class Nav>
+__global__ void __launch_bounds__( 256 ) k_mg_smooth_last( Nav nav, BoraLevelDev L, const float* __restrict__ r0,
+                                                           int slot_rr, BoraReduceDev red, float* __restrict__ zout,
+                                                           int slot_rz )
+{
+    __shared__ float s_scale;
+    if( threadIdx.x == 0 ) s_scale = r0 ? scale_of( red.ring, slot_rr ) : 1.f;
+    __syncthreads();
+    const DF rz = smooth_last_cells( nav, L, RIn{ r0, s_scale, L.r }, zout, red.err, gtid(), gstride() );
     if( zout ) reduce2_publish_warp( df_warp_sum( rz ), 0.0, 0, red, slot_rz, -1 );
+}
+
+// The small tail of the hierarchy in one thread-block cluster: levels that are dense or
+// tiled with one cell per tile (only the first), down to the coarsest and back up, with a
+// cluster barrier between the operations (the cluster's CTAs are co-scheduled, and the
+// barrier orders their global-memory writes at cluster scope). The coarsest level runs
+// in the cluster's first CTA.
+constexpr int kTailLevels = 8;
+constexpr int kTailThreads = 1024;
+constexpr int kTailCtas = 8;  // portable cluster size
+constexpr size_t kTailMaxCells = 32768;
+
+__device__ inline void cluster_barrier()
+{
+    asm volatile( "barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory" );
+}
+
+struct TailDesc
+{
+    BoraLevelDev L[kTailLevels];
+    int n;            // tail levels; the last is the coarsest of the hierarchy
+    int first_tiled;  // L[0] is tiled with one cell per tile
+    const int32_t* nbr;
+    const int32_t* tile_of;
+    const int32_t* slot_of;
+    int tx, ty, tz;
+    int sweeps;       // coarsest sweeps
+};
+
+__global__ void __launch_bounds__( kTailThreads ) k_mg_tail( const __grid_constant__ TailDesc d, uint32_t* err )
+{
+    __shared__ CoarsestSmem sm;
+    const long long i0 = blockIdx.x * (long long)blockDim.x + threadIdx.x, st = (long long)gridDim.x * blockDim.x;
+    auto with_level = [&]( int t, auto&& f ) {
+        const int cdx = t + 1 < d.n ? d.L[t + 1].dx : 0, cdy = t + 1 < d.n ? d.L[t + 1].dy : 0;
+        if( t == 0 && d.first_tiled ) f( TiledNav<1>{ d.nbr, d.tile_of, d.tx, d.ty, cdx, cdy } );
+        else f( DenseNav{ d.L[t].dx, d.L[t].dy, d.L[t].dz, cdx, cdy } );
+    };
+    for( int t = 0; t + 1 < d.n; ++t )
+    {
+        const RIn R{ nullptr, 1.f, d.L[t].r };
+        with_level( t, [&]( auto nav ) { smooth0_cells( nav, d.L[t], R, err, i0, st ); } );
+        cluster_barrier();
+        with_level( t, [&]( auto nav ) {
+            if( t == 0 && d.first_tiled )
+                restrict_cells<decltype( nav ), 1, 1>( nav, d.L[t], d.L[t + 1], R, d.slot_of, d.tx, d.ty, d.tz, err, i0, st );
+            else
+                restrict_cells<decltype( nav ), 2, 1>( nav, d.L[t], d.L[t + 1], R, d.slot_of, d.tx, d.ty, d.tz, err, i0, st );
+        } );
+        cluster_barrier();
+    }
+    if( blockIdx.x == 0 ) with_level( d.n - 1, [&]( auto nav ) { coarsest_cells( nav, d.L[d.n - 1], d.sweeps, err, sm ); } );
+    cluster_barrier();
+    for( int t = d.n - 2; t >= 0; --t )
+    {
+        const RIn R{ nullptr, 1.f, d.L[t].r };
+        with_level( t, [&]( auto nav ) { prolong_smooth_cells( nav, d.L[t], d.L[t + 1].z0, R, err, i0, st ); } );
+        cluster_barrier();
+        with_level( t, [&]( auto nav ) { (void)smooth_last_cells( nav, d.L[t], R, nullptr, err, i0, st ); } );
+        cluster_barrier();
+    }
 }
 
 // ---- fused per-tile kernels for tiled levels with E >= 2 ------------------------------
@@ -932,20 +1034,51 @@ void with_nav( const BoraGridDev& g, const BoraLevelDev* levels, int nlevels, in
 
 }  // namespace
 
+namespace {
+
+// First level of the one-CTA tail: the longest suffix of levels that are dense (or, first
+// only, tiled with one cell per tile) with at most kTailMaxCells cells; nlevels when the
+// coarsest level does not qualify (tiny scenes whose coarsest level is still tiled).
+int tail_start( const BoraLevelDev* levels, int nlevels )
+{
+    auto eligible = []( const BoraLevelDev& L ) { return L.ncells <= kTailMaxCells && ( L.kind == 1 || L.E == 1 ); };
+    const int last = nlevels - 1;
+    if( !eligible( levels[last] ) ) return nlevels;
+    int first = last;
+    while( first > 0 && eligible( levels[first - 1] ) && levels[first].kind == 1 && last - first + 2 <= kTailLevels ) --first;
+    return first;
+}
+
+bool fused_level( const BoraLevelDev& L ) { return L.kind == 0 && L.E >= 2; }
+
+}  // namespace
+
+int bora_mg_vcycle_launches( const BoraLevelDev* levels, int nlevels )
+{
+    if( nlevels < 2 ) return 0;
+    const int first = tail_start( levels, nlevels );
+    const int stop = std::min( first, nlevels - 1 );
+    int n = 1;  // the tail kernel, or the coarsest-level kernel
+    for( int l = 0; l < stop; ++l ) n += fused_level( levels[l] ) ? 2 : 4;
+    return n;
+}
+
 void bora_mg_vcycle( const BoraGridDev& g, const BoraLevelDev* levels, int nlevels, BoraTilesDev t, const float* r,
                      float* z, BoraReduceDev red, int slot_rr, int slot_rz, int coarse_sweeps, cudaStream_t st )
 {
     if( nlevels < 2 ) return;  // the caller always builds at least two levels
     if( levels[0].ncells == 0 ) return;
     const int last = nlevels - 1;
+    const int first = tail_start( levels, nlevels );  // levels [first, last] run in one CTA
+    const int stop = std::min( first, last );          // levels [0, stop) restrict/prolong here
     const int ntiles = levels[0].kind == 0 ? (int)( levels[0].ncells / 512 ) : 0;
     // down: pre-smooth and restrict
-    for( int l = 0; l < last; ++l )
+    for( int l = 0; l < stop; ++l )
     {
         const BoraLevelDev& F = levels[l];
         const BoraLevelDev& C = levels[l + 1];
         const float* r0 = l == 0 ? r : nullptr;
-        if( F.kind == 0 && F.E >= 2 )
+        if( fused_level( F ) )
         {
             if( F.E == 8 ) launch_down_fused<8, true>( F, C, t, ntiles, r0, slot_rr, red.ring, st );
             else if( F.E == 4 ) launch_down_fused<4, false>( F, C, t, ntiles, r0, slot_rr, red.ring, st );
@@ -967,18 +1100,43 @@ void bora_mg_vcycle( const BoraGridDev& g, const BoraLevelDev* levels, int nleve
                 k_mg_restrict<N, 0, 1><<<nb, 256, 0, st>>>( nav, F, C, r0, slot_rr, red.ring, t.slot_of, g.tx, g.ty, g.tz, red.err );
         } );
     }
-    with_nav( g, levels, nlevels, last, t, [&]( auto nav ) {
-        k_mg_coarsest<<<1, 512, 0, st>>>( nav, levels[last], coarse_sweeps, red.err );
-    } );
+    if( first <= last )
+    {
+        TailDesc d{};
+        d.n = last - first + 1;
+        for( int q = 0; q < d.n; ++q ) d.L[q] = levels[first + q];
+        d.first_tiled = levels[first].kind == 0;
+        d.nbr = t.nbr; d.tile_of = t.tile_of; d.slot_of = t.slot_of;
+        d.tx = g.tx; d.ty = g.ty; d.tz = g.tz;
+        d.sweeps = coarse_sweeps;
+        cudaLaunchConfig_t cfg{};
+        cfg.gridDim = dim3( kTailCtas );
+        cfg.blockDim = dim3( kTailThreads );
+        cfg.stream = st;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = kTailCtas;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        cudaLaunchKernelEx( &cfg, k_mg_tail, d, red.err );
+    }
+    else
+    {
+        with_nav( g, levels, nlevels, last, t, [&]( auto nav ) {
+            k_mg_coarsest<<<1, 512, 0, st>>>( nav, levels[last], coarse_sweeps, red.err );
+        } );
+    }
     // up: prolong + two sweeps
-    for( int l = last - 1; l >= 0; --l )
+    for( int l = stop - 1; l >= 0; --l )
     {
         const BoraLevelDev& F = levels[l];
         const float* r0 = l == 0 ? r : nullptr;
-        if( F.kind == 0 && F.E >= 2 )
+        if( fused_level( F ) )
         {
-            // a coarser level that went through this fused path left its result in z1
-            const bool cf = l + 1 < last && levels[l + 1].kind == 0 && levels[l + 1].E >= 2;
+            // a coarser level that went through the fused path left its result in z1
+            const bool cf = l + 1 < stop && fused_level( levels[l + 1] );
             const __half* ec = cf ? levels[l + 1].z1 : levels[l + 1].z0;
             if( F.E == 8 ) launch_up_fused<8, true>( F, ec, t, ntiles, r0, slot_rr, red, z, slot_rz, st );
             else if( F.E == 4 ) launch_up_fused<4, false>( F, ec, t, ntiles, r0, slot_rr, red, nullptr, slot_rz, st );

@@ -371,49 +371,110 @@ __device__ inline size_t face_nbr( const int32_t* __restrict__ nbr, size_t cell,
 }
 
 // ---------------------------------------------------------------------------------
-// PCG direction: d' = z + beta d; q = A d'; dq = d'.q. Streaming, one thread per cell
-// (grid-stride): a neighbour's d' is recomputed from its z and previous d with the same
-// arithmetic as its own thread, so no tile barrier is needed; d is double-buffered.
-__global__ void __launch_bounds__( 256 ) k_pcg_direction( size_t ncells, const int32_t* __restrict__ nbr,
-                                                          const uint16_t* __restrict__ code, BoraSolverDev sv,
-                                                          int dsel_in, BoraReduceDev red, int slot_rz_new,
-                                                          int slot_rz_old, int slot_dq_out )
+// PCG direction: d' = z + beta d; q = A d'; dq = d'.q (d double-buffered). Persistent CTAs
+// walk the tiles; each tile's d' is formed on the tile plus a 1-cell halo in shared memory
+// (non-fluid cells hold d = z = 0, so the stencil sum runs over all six neighbours in the
+// fixed order -x, +x, -y, +y, -z, +z without branches). The next tile's loads are issued
+// before the current tile's stencil, and the neighbour table two tiles ahead.
+namespace dirtile {
+constexpr int R = 10, N = R * R * R, NT = 256;
+constexpr int IA = ( N + NT - 1 ) / NT, IC = 512 / NT;
+constexpr uint32_t kValid = 1u << 31;
+__device__ inline uint32_t region_map( int h )  // bits 0-8 local index, 16-20 tile direction
 {
+    if( h >= N ) return 0;
+    const int a = h % R + 7, b = ( h / R ) % R + 7, c = h / ( R * R ) + 7;  // tile-local + 8, >= 0
+    return kValid | ( (uint32_t)bora_dir( ( a >> 3 ) - 1, ( b >> 3 ) - 1, ( c >> 3 ) - 1 ) << 16 ) |
+           (uint32_t)bora_local( a, b, c );
+}
+}  // namespace dirtile
+
+__global__ void __launch_bounds__( dirtile::NT ) k_pcg_direction_tiles( int ntiles, const int32_t* __restrict__ nbr,
+                                                                        const uint16_t* __restrict__ code, BoraSolverDev sv,
+                                                                        int dsel_in, BoraReduceDev red, int slot_rz_new,
+                                                                        int slot_rz_old, int slot_dq_out )
+{
+    using namespace dirtile;
+    __shared__ float dn_s[N];
+    __shared__ int32_t nbb[2][27];
     __shared__ float s_beta;
-    if( threadIdx.x == 0 ) s_beta = slot_rz_old < 0 ? 0.f : (float)( red.ring[slot_rz_new] / red.ring[slot_rz_old] );
+    const int tid = threadIdx.x, G = gridDim.x;
+    if( tid == 0 ) s_beta = slot_rz_old < 0 ? 0.f : (float)( red.ring[slot_rz_new] / red.ring[slot_rz_old] );
+    auto nbr_entry = [&]( int s ) { return s < ntiles ? nbr[(size_t)s * 27 + tid] : -1; };
+    if( tid < 27 )
+    {
+        nbb[0][tid] = nbr_entry( blockIdx.x );
+        nbb[1][tid] = nbr_entry( blockIdx.x + G );
+    }
+    uint32_t am[IA];
+#pragma unroll
+    for( int it = 0; it < IA; ++it ) am[it] = region_map( tid + it * NT );
     __syncthreads();
     const float beta = s_beta;
-    const float* __restrict__ dold = sv.d[dsel_in];
-    float* __restrict__ dnew = sv.d[dsel_in ^ 1];
-    const float* __restrict__ z = sv.z;
+    const float* __restrict__ dold = dsel_in ? sv.d[1] : sv.d[0];  // selects keep sv out of local memory
+    float* __restrict__ dnew = dsel_in ? sv.d[0] : sv.d[1];
+    float dv[IA], zv[IA];
+    uint32_t cv[IC];
+#define BORA_DIR_ISSUE( NB, S )                                                      \
+    _Pragma( "unroll" ) for( int it = 0; it < IA; ++it )                             \
+    {                                                                                \
+        const uint32_t m = am[it];                                                   \
+        const int sl = ( m & kValid ) ? ( NB )[( m >> 16 ) & 31] : -1;               \
+        dv[it] = 0.f;                                                                \
+        zv[it] = 0.f;                                                                \
+        if( sl >= 0 )                                                                \
+        {                                                                            \
+            const size_t g = (size_t)sl * 512 + ( m & 511u );                        \
+            dv[it] = dold[g];                                                        \
+            zv[it] = sv.z[g];                                                        \
+        }                                                                            \
+    }                                                                                \
+    _Pragma( "unroll" ) for( int it = 0; it < IC; ++it ) cv[it] = code[(size_t)( S ) * 512 + tid + it * NT];
+    BORA_DIR_ISSUE( nbb[0], blockIdx.x );
     DF pdq{ 0.f, 0.f };
-    for( size_t cell = blockIdx.x * (size_t)blockDim.x + threadIdx.x; cell < ncells; cell += (size_t)gridDim.x * blockDim.x )
+    int n = 0;
+    for( int s = blockIdx.x; s < ntiles; s += G, ++n )
     {
-        const float dn = fmaf( beta, dold[cell], z[cell] );
-        dnew[cell] = dn;
-        const uint16_t cc = code[cell];
-        float qv = 0.f;
-        if( cc & BORA_CODE_FLUID )
-        {
-            const int s = (int)( cell >> 9 ), l = (int)( cell & 511 );
-            float acc = 0.f;
 #pragma unroll
-            for( int q = 0; q < 6; ++q )
-            {
-                if( cc & ( 1u << q ) )
-                {
-                    const size_t nc = face_nbr( nbr, cell, s, l, q );
-                    if( nc == (size_t)-1 ) { atomicOr( red.err, 1u ); continue; }
-                    acc += fmaf( beta, dold[nc], z[nc] );
-                }
-            }
-            qv = fmaf( (float)code_diag( cc ), dn, -acc );
-            pdq = df_add( pdq, df_prod( dn, qv ) );
+        for( int it = 0; it < IA; ++it )
+        {
+            const int h = tid + it * NT;
+            if( h < N ) dn_s[h] = fmaf( beta, dv[it], zv[it] );
         }
-        sv.q[cell] = qv;
+        uint32_t cc[IC];
+#pragma unroll
+        for( int it = 0; it < IC; ++it ) cc[it] = cv[it];
+        const int32_t nb2 = tid < 27 ? nbr_entry( s + 2 * G ) : -1;
+        __syncthreads();
+        if( s + G < ntiles ) { BORA_DIR_ISSUE( nbb[( n + 1 ) & 1], s + G ); }
+#pragma unroll
+        for( int it = 0; it < IC; ++it )
+        {
+            const int l = tid + it * NT;
+            const int h = ( l & 7 ) + 1 + R * ( ( ( l >> 3 ) & 7 ) + 1 + R * ( ( l >> 6 ) + 1 ) );
+            const float dn = dn_s[h];
+            float qv = 0.f;
+            if( cc[it] & BORA_CODE_FLUID )
+            {
+                float acc = 0.f;
+                acc += dn_s[h - 1];
+                acc += dn_s[h + 1];
+                acc += dn_s[h - R];
+                acc += dn_s[h + R];
+                acc += dn_s[h - R * R];
+                acc += dn_s[h + R * R];
+                qv = fmaf( (float)code_diag( (uint16_t)cc[it] ), dn, -acc );
+                pdq = df_add( pdq, df_prod( dn, qv ) );
+            }
+            const size_t g = (size_t)s * 512 + l;
+            dnew[g] = dn;
+            sv.q[g] = qv;
+        }
+        if( tid < 27 ) nbb[n & 1][tid] = nb2;
+        __syncthreads();
     }
-    const double a = df_warp_sum( pdq );
-    reduce2_publish_warp( a, 0.0, 0, red, slot_dq_out, -1 );
+    reduce2_publish_warp( df_warp_sum( pdq ), 0.0, 0, red, slot_dq_out, -1 );
+#undef BORA_DIR_ISSUE
 }
 
 // ---------------------------------------------------------------------------------
@@ -627,9 +688,19 @@ void bora_launch_pcg_direction( const BoraGridDev&, int ntiles, BoraTilesDev t, 
                                 int dsel_in, BoraReduceDev red, int slot_rz_new, int slot_rz_old, int slot_dq_out,
                                 cudaStream_t st )
 {
-    const size_t nc = (size_t)ntiles * 512;
-    const int nb = (int)std::max<size_t>( 1, std::min<size_t>( ( nc + 255 ) / 256, (size_t)num_sms() * 8 ) );
-    k_pcg_direction<<<nb, 256, 0, st>>>( nc, t.nbr, code, s, dsel_in, red, slot_rz_new, slot_rz_old, slot_dq_out );
+    if( ntiles <= 0 ) return;
+    static int per_sm[64] = { 0 };
+    int dev = 0;
+    cudaGetDevice( &dev );
+    int b = dev >= 0 && dev < 64 ? per_sm[dev] : 0;
+    if( b <= 0 )
+    {
+        if( cudaOccupancyMaxActiveBlocksPerMultiprocessor( &b, k_pcg_direction_tiles, dirtile::NT, 0 ) != cudaSuccess || b <= 0 ) b = 1;
+        if( dev >= 0 && dev < 64 ) per_sm[dev] = b;
+    }
+    const int grid = std::max( 1, std::min( { ntiles, b * num_sms(), 152 * 16 } ) );  // partial sums capacity
+    k_pcg_direction_tiles<<<grid, dirtile::NT, 0, st>>>( ntiles, t.nbr, code, s, dsel_in, red, slot_rz_new, slot_rz_old,
+                                                         slot_dq_out );
 }
 
 void bora_launch_refine_accumulate( int ntiles, const uint16_t* code, BoraSolverDev s, cudaStream_t st )
