@@ -99,14 +99,15 @@ void bora_launch_mic_factor( const BoraGridDev& g, int ntiles, const uint16_t* c
 void bora_launch_solve_init( int ntiles, const float* b, const uint16_t* code, BoraSolverDev s, BoraReduceDev red,
                              int slot_norm2, int slot_max, cudaStream_t st );
 // e += alpha d; r -= alpha q; z = M^-1 r; rz, rr -> ring slots (alpha = rz_in / dq_in, or 0 when slot_rz_in < 0)
-void bora_launch_pcg_update( int ntiles, const uint16_t* code, BoraSolverDev s, int dsel, BoraReduceDev red,
-                             int slot_rz_in, int slot_dq_in, int slot_rz_out, int slot_rr_out, cudaStream_t st );
+void bora_launch_pcg_update( int ntiles, const uint16_t* code, BoraSolverDev s, BoraReduceDev red, int slot_rz_in,
+                             int slot_dq_in, int slot_rz_out, int slot_rr_out, cudaStream_t st );
 // d' = z + beta d; q = A d'; dq -> ring slot (beta = rz_new / rz_old, or 0 when slot_rz_old < 0)
 void bora_launch_pcg_direction( const BoraGridDev& g, int ntiles, BoraTilesDev t, const uint16_t* code, BoraSolverDev s,
                                 int dsel_in, BoraReduceDev red, int slot_rz_new, int slot_rz_old, int slot_dq_out,
-                                cudaStream_t st );
+                                int slot_a_rz, int slot_a_dq, cudaStream_t st );
 // x += e (FP64); e = 0; d = 0; q = 0
-void bora_launch_refine_accumulate( int ntiles, const uint16_t* code, BoraSolverDev s, cudaStream_t st );
+void bora_launch_refine_accumulate( int ntiles, const uint16_t* code, BoraSolverDev s, int dsel, const double* ring,
+                                    int slot_a_rz, int slot_a_dq, cudaStream_t st );
 // r = b - A x in FP64 (stored FP32); ||r||^2 and max|r| -> ring slots
 void bora_launch_refine_residual( const BoraGridDev& g, int ntiles, BoraTilesDev t, const float* b, const uint16_t* code,
                                   BoraSolverDev s, BoraReduceDev red, int slot_norm2, int slot_max, cudaStream_t st );
@@ -138,5 +139,5 @@ int bora_mg_vcycle_launches( const BoraLevelDev* levels, int nlevels );
 void bora_mg_vcycle( const BoraGridDev& g, const BoraLevelDev* levels, int nlevels, BoraTilesDev t, const float* r,
                      float* z, BoraReduceDev red, int slot_rr, int slot_rz, int coarse_sweeps, cudaStream_t st );
 // e += alpha d; r -= alpha q; r.r -> ring slot (alpha = rz / dq, or 0 when slot_rz < 0)
-void bora_launch_pcg_update_noprec( int ntiles, BoraSolverDev s, int dsel, BoraReduceDev red, int slot_rz, int slot_dq,
+void bora_launch_pcg_update_noprec( int ntiles, BoraSolverDev s, BoraReduceDev red, int slot_rz, int slot_dq,
                                     int slot_rr_out, cudaStream_t st );

@@ -536,13 +536,13 @@ int stage_solve( bora_flip_sim* s )
         int rz_cur = s->slot(), rr_cur = s->slot();
         if( mixed )
         {
-            { KTimer t( s, BORA_KERNEL_PCG_UPDATE, 1 ); bora_launch_pcg_update_noprec( s->ntiles, sv, 0, red, -1, -1, rr_cur, st ); }
+            { KTimer t( s, BORA_KERNEL_PCG_UPDATE, 1 ); bora_launch_pcg_update_noprec( s->ntiles, sv, red, -1, -1, rr_cur, st ); }
             precondition( rr_cur, rz_cur );
         }
         else
         {
             KTimer t( s, BORA_KERNEL_PCG_UPDATE, 1 );
-            bora_launch_pcg_update( s->ntiles, code, sv, 0, red, -1, -1, rz_cur, rr_cur, st );
+            bora_launch_pcg_update( s->ntiles, code, sv, red, -1, -1, rz_cur, rr_cur, st );
         }
         // Convergence checks do not stall the device: the reductions also write their
         // results to mapped host memory, an event marks the end of iteration i, and the
@@ -553,22 +553,28 @@ int stage_solve( bora_flip_sim* s )
         int npend = 0, nchk = 0;
         bool done = false;
         int rz_prev = -1, dsel = 0, it = 0;
+        int a_rz = -1, a_dq = -1;  // alpha of the last update, whose e += alpha d is still pending
         while( it < max_inner && !done )
         {
             const int s_dq = s->slot();
-            { KTimer t( s, BORA_KERNEL_PCG_DIRECTION, 1 ); bora_launch_pcg_direction( s->g, s->ntiles, s->tiles(), code, sv, dsel, red, rz_cur, rz_prev, s_dq, st ); }
+            {
+                KTimer t( s, BORA_KERNEL_PCG_DIRECTION, 1 );
+                bora_launch_pcg_direction( s->g, s->ntiles, s->tiles(), code, sv, dsel, red, rz_cur, rz_prev, s_dq, a_rz, a_dq, st );
+            }
             dsel ^= 1;
             const int rz_new = s->slot(), rr_new = s->slot();
             if( mixed )
             {
-                { KTimer t( s, BORA_KERNEL_PCG_UPDATE, 1 ); bora_launch_pcg_update_noprec( s->ntiles, sv, dsel, red, rz_cur, s_dq, rr_new, st ); }
+                { KTimer t( s, BORA_KERNEL_PCG_UPDATE, 1 ); bora_launch_pcg_update_noprec( s->ntiles, sv, red, rz_cur, s_dq, rr_new, st ); }
                 precondition( rr_new, rz_new );
             }
             else
             {
                 KTimer t( s, BORA_KERNEL_PCG_UPDATE, 1 );
-                bora_launch_pcg_update( s->ntiles, code, sv, dsel, red, rz_cur, s_dq, rz_new, rr_new, st );
+                bora_launch_pcg_update( s->ntiles, code, sv, red, rz_cur, s_dq, rz_new, rr_new, st );
             }
+            a_rz = rz_cur;
+            a_dq = s_dq;
             rz_prev = rz_cur;
             rz_cur = rz_new;
             rr_cur = rr_new;
@@ -594,7 +600,7 @@ int stage_solve( bora_flip_sim* s )
         const int s_n2 = s->slot(), s_mx = s->slot();
         {
             KTimer t( s, BORA_KERNEL_REFINE, 2 );
-            bora_launch_refine_accumulate( s->ntiles, code, sv, st );
+            bora_launch_refine_accumulate( s->ntiles, code, sv, dsel, P<double>( s->ring ), a_rz, a_dq, st );
             bora_launch_refine_residual( s->g, s->ntiles, s->tiles(), b, code, sv, red, s_n2, s_mx, st );
         }
         BORA_TRYS( check_launch( s ) );

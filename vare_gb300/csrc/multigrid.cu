@@ -915,27 +915,25 @@ __global__ void __launch_bounds__( TileRegion<E>::NT, TileRegion<E>::MINB ) k_mg
 }
 
 
-// PCG update without a preconditioner sweep: e += alpha d; r -= alpha q; r.r.
-__global__ void __launch_bounds__( 256 ) k_pcg_update_noprec( size_t ncells, BoraSolverDev sv, int dsel, BoraReduceDev red,
+// PCG update without a preconditioner sweep: r -= alpha q; r.r (e += alpha d is applied by
+// the next direction kernel or the refinement step).
+__global__ void __launch_bounds__( 256 ) k_pcg_update_noprec( size_t ncells, BoraSolverDev sv, BoraReduceDev red,
                                                               int slot_rz, int slot_dq, int slot_rr_out )
 {
     __shared__ float s_alpha;
     if( threadIdx.x == 0 ) s_alpha = slot_rz < 0 ? 0.f : (float)( red.ring[slot_rz] / red.ring[slot_dq] );
     __syncthreads();
     const float alpha = s_alpha;
-    const float* __restrict__ d = sv.d[dsel];
     DF rr{ 0.f, 0.f };
     const size_t n4 = ncells / 4;
+    float4* __restrict__ r4 = reinterpret_cast<float4*>( sv.r );
+    const float4* __restrict__ q4 = reinterpret_cast<const float4*>( sv.q );
     for( size_t v = blockIdx.x * (size_t)blockDim.x + threadIdx.x; v < n4; v += (size_t)gridDim.x * blockDim.x )
     {
-        float4 e = reinterpret_cast<const float4*>( sv.e )[v];
-        float4 r = reinterpret_cast<const float4*>( sv.r )[v];
-        const float4 dv = reinterpret_cast<const float4*>( d )[v];
-        const float4 q = reinterpret_cast<const float4*>( sv.q )[v];
-        e.x = fmaf( alpha, dv.x, e.x ); e.y = fmaf( alpha, dv.y, e.y ); e.z = fmaf( alpha, dv.z, e.z ); e.w = fmaf( alpha, dv.w, e.w );
+        float4 r = r4[v];
+        const float4 q = q4[v];
         r.x = fmaf( -alpha, q.x, r.x ); r.y = fmaf( -alpha, q.y, r.y ); r.z = fmaf( -alpha, q.z, r.z ); r.w = fmaf( -alpha, q.w, r.w );
-        reinterpret_cast<float4*>( sv.e )[v] = e;
-        reinterpret_cast<float4*>( sv.r )[v] = r;
+        r4[v] = r;
         rr = df_add( rr, df_prod( r.x, r.x ) ); rr = df_add( rr, df_prod( r.y, r.y ) );
         rr = df_add( rr, df_prod( r.z, r.z ) ); rr = df_add( rr, df_prod( r.w, r.w ) );
     }
@@ -1152,9 +1150,9 @@ void bora_mg_vcycle( const BoraGridDev& g, const BoraLevelDev* levels, int nleve
     }
 }
 
-void bora_launch_pcg_update_noprec( int ntiles, BoraSolverDev s, int dsel, BoraReduceDev red, int slot_rz, int slot_dq,
+void bora_launch_pcg_update_noprec( int ntiles, BoraSolverDev s, BoraReduceDev red, int slot_rz, int slot_dq,
                                     int slot_rr_out, cudaStream_t st )
 {
     const size_t nc = (size_t)ntiles * 512;
-    k_pcg_update_noprec<<<blocks_for( nc / 4 ), 256, 0, st>>>( nc, s, dsel, red, slot_rz, slot_dq, slot_rr_out );
+    k_pcg_update_noprec<<<blocks_for( nc / 4 ), 256, 0, st>>>( nc, s, red, slot_rz, slot_dq, slot_rr_out );
 }

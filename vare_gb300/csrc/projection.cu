@@ -251,19 +251,22 @@ __global__ void __launch_bounds__( 32 * kTilesPerCta ) k_mic_factor( int ntiles,
 }
 
 // ---------------------------------------------------------------------------------
-// PCG update: e += alpha d; r -= alpha q; z = M^-1 r (block-MIC(0) forward and backward
-// sweeps in shared memory); rz = r.z and rr = r.r, FP64-accurate. One warp per tile,
-// persistent over tiles; alpha is formed once per CTA.
-__global__ void __launch_bounds__( 32 * kTilesPerCta ) k_pcg_update( int ntiles, const uint16_t* __restrict__ code,
-                                                                     BoraSolverDev sv, int dsel, BoraReduceDev red,
-                                                                     int slot_rz_in, int slot_dq_in, int slot_rz_out,
-                                                                     int slot_rr_out )
+// PCG update: r -= alpha q; z = M^-1 r (block-MIC(0) forward and backward sweeps over the
+// tile's 22 wavefront planes i+j+k = p in shared memory); rz = r.z and rr = r.r,
+// FP64-accurate. The matching e += alpha d is applied by the next direction kernel (which
+// reads d anyway) or by the refinement step. One warp per tile, persistent over tiles;
+// all of a tile's loads are issued before its first store; alpha is formed once per CTA.
+// The sweeps run in place (y over r, then z over y) and need no cell types: non-fluid
+// cells have M = 0 (k_mic_factor) and r = 0, so their y and z vanish, and a neighbour
+// outside the tile is skipped by its tile-local coordinate.
+constexpr int kUpdWarps = 4;
+
+__global__ void __launch_bounds__( 32 * kUpdWarps ) k_pcg_update( int ntiles, BoraSolverDev sv, BoraReduceDev red,
+                                                                  int slot_rz_in, int slot_dq_in, int slot_rz_out,
+                                                                  int slot_rr_out )
 {
-    // vector (16-byte / 8-byte) shared-memory accesses below need explicit alignment
-    __shared__ __align__( 16 ) float sr[kTilesPerCta][512];
-    __shared__ __align__( 16 ) float sy[kTilesPerCta][512];
-    __shared__ __align__( 16 ) float sm[kTilesPerCta][512];
-    __shared__ __align__( 16 ) uint16_t sc[kTilesPerCta][512];
+    __shared__ __align__( 16 ) float sy[kUpdWarps][512];
+    __shared__ __align__( 16 ) float sm[kUpdWarps][512];
     __shared__ uint16_t pc[512], ps[23];
     __shared__ float s_alpha;
     load_plane_tables( pc, ps );
@@ -271,78 +274,71 @@ __global__ void __launch_bounds__( 32 * kTilesPerCta ) k_pcg_update( int ntiles,
     __syncthreads();
     const float alpha = s_alpha;
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float* __restrict__ y = sy[w];
+    float* __restrict__ M = sm[w];
+    const float4* __restrict__ r4 = reinterpret_cast<const float4*>( sv.r );
+    const float4* __restrict__ q4 = reinterpret_cast<const float4*>( sv.q );
+    const float4* __restrict__ m4 = reinterpret_cast<const float4*>( sv.minv );
     DF prz{ 0.f, 0.f }, prr{ 0.f, 0.f };
-    const float* dvec = sv.d[dsel];
-    for( int s = blockIdx.x * kTilesPerCta + w; s < ntiles; s += gridDim.x * kTilesPerCta )
+    for( int s = blockIdx.x * kUpdWarps + w; s < ntiles; s += gridDim.x * kUpdWarps )
     {
-        const size_t base = (size_t)s * 512;
-        for( int l4 = lane; l4 < 128; l4 += 32 )
+        const size_t b4 = (size_t)s * 128;
+        float4 r[4], q[4], mv[4];
+#pragma unroll
+        for( int k = 0; k < 4; ++k )
         {
-            const size_t o = base + 4 * (size_t)l4;
-            float4 e = *reinterpret_cast<const float4*>( sv.e + o );
-            float4 r = *reinterpret_cast<const float4*>( sv.r + o );
-            const float4 d = *reinterpret_cast<const float4*>( dvec + o );
-            const float4 q = *reinterpret_cast<const float4*>( sv.q + o );
-            const float4 mv = *reinterpret_cast<const float4*>( sv.minv + o );
-            const ushort4 cv = *reinterpret_cast<const ushort4*>( code + o );
-            e.x = fmaf( alpha, d.x, e.x ); e.y = fmaf( alpha, d.y, e.y ); e.z = fmaf( alpha, d.z, e.z ); e.w = fmaf( alpha, d.w, e.w );
-            r.x = fmaf( -alpha, q.x, r.x ); r.y = fmaf( -alpha, q.y, r.y ); r.z = fmaf( -alpha, q.z, r.z ); r.w = fmaf( -alpha, q.w, r.w );
-            *reinterpret_cast<float4*>( sv.e + o ) = e;
-            *reinterpret_cast<float4*>( sv.r + o ) = r;
-            *reinterpret_cast<float4*>( &sr[w][4 * l4] ) = r;
-            *reinterpret_cast<float4*>( &sm[w][4 * l4] ) = mv;
-            *reinterpret_cast<ushort4*>( &sc[w][4 * l4] ) = cv;
+            r[k] = r4[b4 + lane + 32 * k];
+            q[k] = q4[b4 + lane + 32 * k];
+            mv[k] = m4[b4 + lane + 32 * k];
+        }
+#pragma unroll
+        for( int k = 0; k < 4; ++k )
+        {
+            r[k].x = fmaf( -alpha, q[k].x, r[k].x ); r[k].y = fmaf( -alpha, q[k].y, r[k].y );
+            r[k].z = fmaf( -alpha, q[k].z, r[k].z ); r[k].w = fmaf( -alpha, q[k].w, r[k].w );
+            reinterpret_cast<float4*>( sv.r )[b4 + lane + 32 * k] = r[k];
+            reinterpret_cast<float4*>( y )[lane + 32 * k] = r[k];
+            reinterpret_cast<float4*>( M )[lane + 32 * k] = mv[k];
+            prr = df_add( prr, df_prod( r[k].x, r[k].x ) ); prr = df_add( prr, df_prod( r[k].y, r[k].y ) );
+            prr = df_add( prr, df_prod( r[k].z, r[k].z ) ); prr = df_add( prr, df_prod( r[k].w, r[k].w ) );
         }
         __syncwarp();
         // forward: y_c = (r_c + sum_{lower m} M_m y_m) M_c   (A_mc = -1)
         for( int p = 0; p <= 21; ++p )
         {
-            for( int q = ps[p] + lane; q < ps[p + 1]; q += 32 )
+            for( int qq = ps[p] + lane; qq < ps[p + 1]; qq += 32 )
             {
-                const int l = pc[q];
-                const uint16_t cc = sc[w][l];
-                float y = 0.f;
-                if( cc & BORA_CODE_FLUID )
-                {
-                    float t = sr[w][l];
-                    if( ( l & 7 ) > 0 && ( cc & 1u ) ) t = fmaf( sm[w][l - 1], sy[w][l - 1], t );
-                    if( ( ( l >> 3 ) & 7 ) > 0 && ( cc & 4u ) ) t = fmaf( sm[w][l - 8], sy[w][l - 8], t );
-                    if( ( l >> 6 ) > 0 && ( cc & 16u ) ) t = fmaf( sm[w][l - 64], sy[w][l - 64], t );
-                    y = t * sm[w][l];
-                }
-                sy[w][l] = y;
+                const int l = pc[qq];
+                float t = y[l];
+                if( l & 7 ) t = fmaf( M[l - 1], y[l - 1], t );
+                if( l & 56 ) t = fmaf( M[l - 8], y[l - 8], t );
+                if( l & 448 ) t = fmaf( M[l - 64], y[l - 64], t );
+                y[l] = t * M[l];
             }
             __syncwarp();
         }
-        // backward: z_c = (y_c + M_c sum_{upper u} z_u) M_c ; z overwrites sy in place
+        // backward: z_c = (y_c + M_c sum_{upper u} z_u) M_c
         for( int p = 21; p >= 0; --p )
         {
-            for( int q = ps[p] + lane; q < ps[p + 1]; q += 32 )
+            for( int qq = ps[p] + lane; qq < ps[p + 1]; qq += 32 )
             {
-                const int l = pc[q];
-                const uint16_t cc = sc[w][l];
-                if( cc & BORA_CODE_FLUID )
-                {
-                    float acc = 0.f;
-                    if( ( l & 7 ) < 7 && ( cc & 2u ) ) acc += sy[w][l + 1];
-                    if( ( ( l >> 3 ) & 7 ) < 7 && ( cc & 8u ) ) acc += sy[w][l + 8];
-                    if( ( l >> 6 ) < 7 && ( cc & 32u ) ) acc += sy[w][l + 64];
-                    const float M = sm[w][l];
-                    sy[w][l] = fmaf( M, acc, sy[w][l] ) * M;
-                }
+                const int l = pc[qq];
+                float acc = 0.f;
+                if( ( l & 7 ) != 7 ) acc += y[l + 1];
+                if( ( l & 56 ) != 56 ) acc += y[l + 8];
+                if( ( l & 448 ) != 448 ) acc += y[l + 64];
+                const float Ml = M[l];
+                y[l] = fmaf( Ml, acc, y[l] ) * Ml;
             }
             __syncwarp();
         }
-        for( int l4 = lane; l4 < 128; l4 += 32 )
+#pragma unroll
+        for( int k = 0; k < 4; ++k )
         {
-            const size_t o = base + 4 * (size_t)l4;
-            const float4 z = *reinterpret_cast<const float4*>( &sy[w][4 * l4] );
-            const float4 r = *reinterpret_cast<const float4*>( &sr[w][4 * l4] );
-            *reinterpret_cast<float4*>( sv.z + o ) = z;
-            prz = df_add( prz, df_prod( r.x, z.x ) ); prz = df_add( prz, df_prod( r.y, z.y ) );
-            prz = df_add( prz, df_prod( r.z, z.z ) ); prz = df_add( prz, df_prod( r.w, z.w ) );
-            prr = df_add( prr, df_prod( r.x, r.x ) ); prr = df_add( prr, df_prod( r.y, r.y ) );
-            prr = df_add( prr, df_prod( r.z, r.z ) ); prr = df_add( prr, df_prod( r.w, r.w ) );
+            const float4 z = reinterpret_cast<const float4*>( y )[lane + 32 * k];
+            reinterpret_cast<float4*>( sv.z )[b4 + lane + 32 * k] = z;
+            prz = df_add( prz, df_prod( r[k].x, z.x ) ); prz = df_add( prz, df_prod( r[k].y, z.y ) );
+            prz = df_add( prz, df_prod( r[k].z, z.z ) ); prz = df_add( prz, df_prod( r[k].w, z.w ) );
         }
         __syncwarp();
     }
@@ -371,7 +367,8 @@ __device__ inline size_t face_nbr( const int32_t* __restrict__ nbr, size_t cell,
 }
 
 // ---------------------------------------------------------------------------------
-// PCG direction: d' = z + beta d; q = A d'; dq = d'.q (d double-buffered). Persistent CTAs
+// PCG direction: e += alpha d (the previous update's step, pending); d' = z + beta d;
+// q = A d'; dq = d'.q (d double-buffered). Persistent CTAs
 // walk the tiles; each tile's d' is formed on the tile plus a 1-cell halo in shared memory
 // (non-fluid cells hold d = z = 0, so the stencil sum runs over all six neighbours in the
 // fixed order -x, +x, -y, +y, -z, +z without branches). The next tile's loads are issued
@@ -392,14 +389,21 @@ __device__ inline uint32_t region_map( int h )  // bits 0-8 local index, 16-20 t
 __global__ void __launch_bounds__( dirtile::NT ) k_pcg_direction_tiles( int ntiles, const int32_t* __restrict__ nbr,
                                                                         const uint16_t* __restrict__ code, BoraSolverDev sv,
                                                                         int dsel_in, BoraReduceDev red, int slot_rz_new,
-                                                                        int slot_rz_old, int slot_dq_out )
+                                                                        int slot_rz_old, int slot_dq_out, int slot_a_rz,
+                                                                        int slot_a_dq )
 {
     using namespace dirtile;
     __shared__ float dn_s[N];
+    __shared__ float do_s[512];  // d_old on the tile
     __shared__ int32_t nbb[2][27];
-    __shared__ float s_beta;
+    __shared__ float s_beta, s_alpha;
     const int tid = threadIdx.x, G = gridDim.x;
-    if( tid == 0 ) s_beta = slot_rz_old < 0 ? 0.f : (float)( red.ring[slot_rz_new] / red.ring[slot_rz_old] );
+    if( tid == 0 )
+    {
+        s_beta = slot_rz_old < 0 ? 0.f : (float)( red.ring[slot_rz_new] / red.ring[slot_rz_old] );
+        s_alpha = slot_a_rz < 0 ? 0.f : (float)( red.ring[slot_a_rz] / red.ring[slot_a_dq] );
+    }
+    const bool upd_e = slot_a_rz >= 0;  // the previous update's e += alpha d is still pending
     auto nbr_entry = [&]( int s ) { return s < ntiles ? nbr[(size_t)s * 27 + tid] : -1; };
     if( tid < 27 )
     {
@@ -410,10 +414,10 @@ __global__ void __launch_bounds__( dirtile::NT ) k_pcg_direction_tiles( int ntil
 #pragma unroll
     for( int it = 0; it < IA; ++it ) am[it] = region_map( tid + it * NT );
     __syncthreads();
-    const float beta = s_beta;
+    const float beta = s_beta, alpha = s_alpha;
     const float* __restrict__ dold = dsel_in ? sv.d[1] : sv.d[0];  // selects keep sv out of local memory
     float* __restrict__ dnew = dsel_in ? sv.d[0] : sv.d[1];
-    float dv[IA], zv[IA];
+    float dv[IA], zv[IA], ev[IC];
     uint32_t cv[IC];
 #define BORA_DIR_ISSUE( NB, S )                                                      \
     _Pragma( "unroll" ) for( int it = 0; it < IA; ++it )                             \
@@ -429,7 +433,11 @@ __global__ void __launch_bounds__( dirtile::NT ) k_pcg_direction_tiles( int ntil
             zv[it] = sv.z[g];                                                        \
         }                                                                            \
     }                                                                                \
-    _Pragma( "unroll" ) for( int it = 0; it < IC; ++it ) cv[it] = code[(size_t)( S ) * 512 + tid + it * NT];
+    _Pragma( "unroll" ) for( int it = 0; it < IC; ++it )                             \
+    {                                                                                \
+        cv[it] = code[(size_t)( S ) * 512 + tid + it * NT];                          \
+        if( upd_e ) ev[it] = sv.e[(size_t)( S ) * 512 + tid + it * NT];              \
+    }
     BORA_DIR_ISSUE( nbb[0], blockIdx.x );
     DF pdq{ 0.f, 0.f };
     int n = 0;
@@ -439,8 +447,15 @@ __global__ void __launch_bounds__( dirtile::NT ) k_pcg_direction_tiles( int ntil
         for( int it = 0; it < IA; ++it )
         {
             const int h = tid + it * NT;
-            if( h < N ) dn_s[h] = fmaf( beta, dv[it], zv[it] );
+            if( h < N )
+            {
+                dn_s[h] = fmaf( beta, dv[it], zv[it] );
+                if( ( ( am[it] >> 16 ) & 31u ) == 13u ) do_s[am[it] & 511u] = dv[it];  // tile cell
+            }
         }
+        float ee[IC];
+#pragma unroll
+        for( int it = 0; it < IC; ++it ) ee[it] = ev[it];
         uint32_t cc[IC];
 #pragma unroll
         for( int it = 0; it < IC; ++it ) cc[it] = cv[it];
@@ -469,6 +484,7 @@ __global__ void __launch_bounds__( dirtile::NT ) k_pcg_direction_tiles( int ntil
             const size_t g = (size_t)s * 512 + l;
             dnew[g] = dn;
             sv.q[g] = qv;
+            if( upd_e ) sv.e[g] = fmaf( alpha, do_s[l], ee[it] );
         }
         if( tid < 27 ) nbb[n & 1][tid] = nb2;
         __syncthreads();
@@ -498,11 +514,19 @@ __global__ void k_solve_init( size_t ncells, const float* __restrict__ b, BoraSo
     reduce2_publish_dfmax( n2, mx, red, slot_norm2, slot_max );
 }
 
-__global__ void k_refine_accumulate( size_t ncells, const uint16_t* __restrict__ code, BoraSolverDev sv )
+// x += e (+ the last update's pending alpha d), then clear the inner solve's vectors.
+__global__ void k_refine_accumulate( size_t ncells, const uint16_t* __restrict__ code, BoraSolverDev sv, int dsel,
+                                     const double* __restrict__ ring, int slot_a_rz, int slot_a_dq )
 {
+    __shared__ float s_alpha;
+    if( threadIdx.x == 0 ) s_alpha = slot_a_rz < 0 ? 0.f : (float)( ring[slot_a_rz] / ring[slot_a_dq] );
+    __syncthreads();
+    const float alpha = s_alpha;
+    const float* __restrict__ d = dsel ? sv.d[1] : sv.d[0];
     for( size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < ncells; i += (size_t)gridDim.x * blockDim.x )
     {
-        if( code[i] & BORA_CODE_FLUID ) sv.x[i] += (double)sv.e[i];
+        const float e = slot_a_rz < 0 ? sv.e[i] : fmaf( alpha, d[i], sv.e[i] );
+        if( code[i] & BORA_CODE_FLUID ) sv.x[i] += (double)e;
         sv.e[i] = 0.f;
         sv.d[0][i] = 0.f;
         sv.d[1][i] = 0.f;
@@ -675,18 +699,27 @@ void bora_launch_solve_init( int ntiles, const float* b, const uint16_t*, BoraSo
     k_solve_init<<<grid_for( nc, 256 ), 256, 0, st>>>( nc, b, s, red, slot_norm2, slot_max );
 }
 
-void bora_launch_pcg_update( int ntiles, const uint16_t* code, BoraSolverDev s, int dsel, BoraReduceDev red,
-                             int slot_rz_in, int slot_dq_in, int slot_rz_out, int slot_rr_out, cudaStream_t st )
+void bora_launch_pcg_update( int ntiles, const uint16_t* code, BoraSolverDev s, BoraReduceDev red, int slot_rz_in,
+                             int slot_dq_in, int slot_rz_out, int slot_rr_out, cudaStream_t st )
 {
+    (void)code;
     ensure_tables();
-    const int nb = std::max( 1, std::min( ( ntiles + kTilesPerCta - 1 ) / kTilesPerCta, num_sms() * 7 ) );
-    k_pcg_update<<<nb, 32 * kTilesPerCta, 0, st>>>( ntiles, code, s, dsel, red, slot_rz_in, slot_dq_in, slot_rz_out,
-                                                    slot_rr_out );
+    static int per_sm[64] = { 0 };
+    int dev = 0;
+    cudaGetDevice( &dev );
+    int bps = dev >= 0 && dev < 64 ? per_sm[dev] : 0;
+    if( bps <= 0 )
+    {
+        if( cudaOccupancyMaxActiveBlocksPerMultiprocessor( &bps, k_pcg_update, 32 * kUpdWarps, 0 ) != cudaSuccess || bps <= 0 ) bps = 1;
+        if( dev >= 0 && dev < 64 ) per_sm[dev] = bps;
+    }
+    const int nb = std::max( 1, std::min( { ( ntiles + kUpdWarps - 1 ) / kUpdWarps, bps * num_sms(), 152 * 16 } ) );
+    k_pcg_update<<<nb, 32 * kUpdWarps, 0, st>>>( ntiles, s, red, slot_rz_in, slot_dq_in, slot_rz_out, slot_rr_out );
 }
 
 void bora_launch_pcg_direction( const BoraGridDev&, int ntiles, BoraTilesDev t, const uint16_t* code, BoraSolverDev s,
                                 int dsel_in, BoraReduceDev red, int slot_rz_new, int slot_rz_old, int slot_dq_out,
-                                cudaStream_t st )
+                                int slot_a_rz, int slot_a_dq, cudaStream_t st )
 {
     if( ntiles <= 0 ) return;
     static int per_sm[64] = { 0 };
@@ -700,13 +733,14 @@ void bora_launch_pcg_direction( const BoraGridDev&, int ntiles, BoraTilesDev t, 
     }
     const int grid = std::max( 1, std::min( { ntiles, b * num_sms(), 152 * 16 } ) );  // partial sums capacity
     k_pcg_direction_tiles<<<grid, dirtile::NT, 0, st>>>( ntiles, t.nbr, code, s, dsel_in, red, slot_rz_new, slot_rz_old,
-                                                         slot_dq_out );
+                                                         slot_dq_out, slot_a_rz, slot_a_dq );
 }
 
-void bora_launch_refine_accumulate( int ntiles, const uint16_t* code, BoraSolverDev s, cudaStream_t st )
+void bora_launch_refine_accumulate( int ntiles, const uint16_t* code, BoraSolverDev s, int dsel, const double* ring,
+                                    int slot_a_rz, int slot_a_dq, cudaStream_t st )
 {
     const size_t nc = (size_t)ntiles * 512;
-    if( nc ) k_refine_accumulate<<<grid_for( nc, 256 ), 256, 0, st>>>( nc, code, s );
+    if( nc ) k_refine_accumulate<<<grid_for( nc, 256 ), 256, 0, st>>>( nc, code, s, dsel, ring, slot_a_rz, slot_a_dq );
 }
 
 void bora_launch_refine_residual( const BoraGridDev&, int ntiles, BoraTilesDev t, const float* b, const uint16_t* code,
