@@ -66,7 +66,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="dam_sphere_256", choices=["dam_sphere_256", "dam_break_64"])
+    ap.add_argument("--workload", default="dam_sphere_256", choices=["dam_sphere_256", "dam_break_64", "tank_1024"])
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-steps", type=int, default=2)
@@ -78,16 +78,24 @@ def parse():
 
 def make_scene(name):
     from vare_gb300 import scenes
+    if name == "tank_1024":
+        return scenes.config3()
     return scenes.config1() if name == "dam_sphere_256" else scenes.config0()
 
 
-def workload_config(sc, extra=None):
+SOLVER_DESC = {"plain": "plain: FP32 PCG + block-MIC(0), FP64 dots, FP64 iterative refinement",
+               "mixed": "mixed: FP32 PCG + geometric multigrid V(2,2) (FP16 level storage, FP32 arithmetic), "
+                        "FP64 dots, FP64 iterative refinement"}
+
+
+def workload_config(sc, extra=None, solver="plain"):
     cfg = {"workload": f"{sc.name}: {sc.res[0]}x{sc.res[1]}x{sc.res[2]} virtual grid in 8^3 tiles, "
-                       f"{sc.num_particles} particles (8/cell jittered, seeded), dt={sc.dt:.6g}, solid walls",
+                       f"{sc.num_particles} particles (8/cell jittered, seeded), dt={sc.dt:.6g}, solid walls"
+                       + (", static box obstacle" if sc.colliders else ""),
            "grid": list(sc.res), "particles": sc.num_particles, "dt": sc.dt, "tile": 8,
-           "solver": "plain: FP32 PCG + block-MIC(0), FP64 dots, FP64 iterative refinement",
+           "solver": SOLVER_DESC.get(solver, solver),
            "tolerance": {"rel": 1e-6, "max_div_dx": 1e-5},
-           "l2": "inputs larger than L2 (particles alone are 590 MB); no flush",
+           "l2": f"inputs larger than L2 (particles alone are {sc.num_particles * 24 // 1000000} MB); no flush",
            "parallelism": "replicas (one independent simulation per GPU)"}
     if extra:
         cfg.update(extra)
@@ -260,7 +268,10 @@ def run_reference(args, world, rank):
     sample = (f"{steps} timed steps (of --steps {args.steps}) after {warm} warm-up steps of the full workload; "
               f"oracle restatement of the reference FLIP step, bit-exact with the reference's host build "
               f"(4^3 tiles, reference CG rule), {threads} OpenMP threads")
-    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+    metric = METRIC if args.solver != "mixed" else METRIC.replace("plain FP32 block-MIC(0)-PCG", "mixed-precision MG-PCG")
+    if args.workload != "dam_sphere_256":
+        metric = metric.replace("at 256^3 FLIP", f"at {sc.res[0]}x{sc.res[1]}x{sc.res[2]} FLIP")
+    out = {"metric": metric, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": sum(ms) / len(ms), "p50_ms": ms[len(ms) // 2], "p99_ms": ms[-1],
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
            "data": "synthetic (seeded jittered-uniform dam break + sphere)", "impl": "reference",
@@ -406,11 +417,16 @@ def run_ours(args, world, rank, local):
 
     if rank != 0:
         return
-    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+    metric = METRIC if args.solver != "mixed" else METRIC.replace("plain FP32 block-MIC(0)-PCG", "mixed-precision MG-PCG")
+    if args.workload != "dam_sphere_256":
+        metric = metric.replace("at 256^3 FLIP", f"at {sc.res[0]}x{sc.res[1]}x{sc.res[2]} FLIP")
+    out = {"metric": metric, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": meas["ms_per_step"], "p50_ms": meas["p50_ms"],
            "p99_ms": meas["p99_ms"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-           "data": "synthetic (seeded jittered-uniform dam break + sphere; no public data set exists for this path)",
-           "config": workload_config(sc), "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+           "data": f"synthetic (seeded jittered-uniform {'tank + wave column' if sc.name.startswith('tank') else 'dam break + sphere'}; "
+                   "no public data set exists for this path)",
+           "config": workload_config(sc, solver=args.solver if args.solver != "both" else "plain"), "roofline": roof,
+           "cpu_baseline": cpu, "e2e": e2e,
            "gpu_launches": int(launches), "clocks": clk, "solver": meas["solver"], "mixed": mixed}
     print(json.dumps(out), flush=True)
 

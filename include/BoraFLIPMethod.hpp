@@ -85,6 +85,7 @@ class FLIPMethod
         int solver = BORA_SOLVER_PLAIN;
         double tolerance = 1e-6;
         double divTolerance = 1e-5;
+        int advection = BORA_ADVECT_EULER;
     } params;
 
     FLIPMethod() = default;
@@ -197,6 +198,7 @@ class FLIPMethod
         p.solver = params.solver;
         p.tolerance = params.tolerance;
         p.div_tolerance = params.divTolerance;
+        p.advection = params.advection;
         return p;
     }
 

@@ -45,6 +45,10 @@ extern "C" {
 #define BORA_SOLVER_PLAIN 0 /* FP32 PCG, block-MIC(0) preconditioner, FP64 dots + refinement */
 #define BORA_SOLVER_MIXED 1 /* FP32 PCG, multigrid V-cycle (FP16 storage), FP64 dots + refinement */
 
+/* particle advection (bora_flip_params.advection) */
+#define BORA_ADVECT_EULER 0
+#define BORA_ADVECT_RK2 1
+
 /* Grid description: nx*ny*nz cells over the world box [min, max]
  * (Grid::initialize(Nx,Ny,Nz,min,max), base/header/Grid.h:124-141). The simulation grid
  * is this grid padded to a multiple of 4 cells per axis and re-centred
@@ -82,6 +86,9 @@ typedef struct bora_flip_params
     double inner_tolerance;  /* 1e-4: relative residual reduction of each FP32 inner solve */
     int max_refinements;     /* 8: outer FP64 refinement passes */
     int check_every;         /* 1: inner iterations between convergence checks (read back one iteration late) */
+    int advection;           /* BORA_ADVECT_EULER: particle positions follow the particle velocity
+                                (FLIPMethod.cu:124-145); BORA_ADVECT_RK2: midpoint rule in the grid
+                                velocity field, per substep */
 } bora_flip_params;
 
 typedef struct bora_flip_stats

@@ -51,7 +51,7 @@ class OracleConfig(ctypes.Structure):
                 ("gravity", ctypes.c_float * 3), ("wall_level", ctypes.c_float),
                 ("maxsubsteps", ctypes.c_int), ("col_vel_scale", ctypes.c_float),
                 ("enable_tank", ctypes.c_int), ("damping_band", ctypes.c_float),
-                ("voxel_size", ctypes.c_float)]
+                ("voxel_size", ctypes.c_float), ("advection", ctypes.c_int)]
 
 
 class RefParams(ctypes.Structure):
@@ -188,7 +188,7 @@ class Oracle(_SimBase):
     _p = "ora_"
 
     def __init__(self, scene, block: int = 8, compat: bool = False, solver: str = "fp64",
-                 tol: float = 1e-12, max_iter: int = 100000, threads: int | None = None):
+                 tol: float = 1e-12, max_iter: int = 100000, threads: int | None = None, advection: int = 0):
         self.lib = _oracle_lib()
         if threads is not None:
             self.lib.ora_set_threads(int(threads))
@@ -208,6 +208,7 @@ class Oracle(_SimBase):
         c.enable_tank = 0
         c.damping_band = 0.0
         c.voxel_size = scene.voxel_size
+        c.advection = advection
         self.cfg = c
         self.h = _vp(self.lib.ora_create(ctypes.byref(c)))
         if scene.colliders:

@@ -60,6 +60,7 @@ typedef struct OracleConfig
     int enable_tank;
     float damping_band;    // world units
     float voxel_size;      // FLIPMethod::Params::voxelSize
+    int advection;         // 0: the reference's Euler substeps; 1: RK2 midpoint in the grid velocity
 } OracleConfig;
 
 }
@@ -740,7 +741,19 @@ struct Oracle
                 bool col = false;
                 for( int s = 0; s < iter; ++s )
                 {
-                    p.x += v.x * sub_dt; p.y += v.y * sub_dt; p.z += v.z * sub_dt;
+                    if( cfg.advection == 1 )
+                    {
+                        // RK2 (midpoint) in the projected grid velocity: an option of this
+                        // build, not of the reference, restated here with the same lerp.
+                        const float h = 0.5f * sub_dt;
+                        const V3 k1 = lerpV( comp, p.x, p.y, p.z );
+                        const V3 k2 = lerpV( comp, p.x + k1.x * h, p.y + k1.y * h, p.z + k1.z * h );
+                        p.x += k2.x * sub_dt; p.y += k2.y * sub_dt; p.z += k2.z * sub_dt;
+                    }
+                    else
+                    {
+                        p.x += v.x * sub_dt; p.y += v.y * sub_dt; p.z += v.z * sub_dt;
+                    }
                     if( p.y <= wall )
                     {
                         if( p.x < 0.f ) { p.x = 0.f; if( v.x < 0.f ) v.x = 0.f; }

@@ -302,6 +302,7 @@ void apply_params( bora_flip_sim* s )
     g.maxsubsteps = p.max_substeps;
     g.enable_tank = p.enable_water_tank;
     g.damping_band = p.damping_band / p.voxel_size;
+    g.advection = p.advection;
 }
 
 int ensure_particles( bora_flip_sim* s, size_t n )
@@ -706,6 +707,7 @@ int bora_flip_default_params( bora_flip_params* o )
     o->inner_tolerance = 1e-4;
     o->max_refinements = 8;
     o->check_every = 1;
+    o->advection = BORA_ADVECT_EULER;
     return BORA_OK;
 }
 
@@ -714,6 +716,7 @@ static int validate_params( const bora_flip_params* p )
     if( !p ) return BORA_ERR_INVALID_ARG;
     if( p->enable_curl ) return BORA_ERR_INVALID_ARG;  // curl noise is outside this library
     if( p->solver != BORA_SOLVER_PLAIN && p->solver != BORA_SOLVER_MIXED ) return BORA_ERR_INVALID_ARG;
+    if( p->advection != BORA_ADVECT_EULER && p->advection != BORA_ADVECT_RK2 ) return BORA_ERR_INVALID_ARG;
     if( !( p->voxel_size > 0.f ) || !( p->tolerance > 0.0 ) ) return BORA_ERR_INVALID_ARG;
     return BORA_OK;
 }

@@ -58,6 +58,7 @@ struct BoraGridDev
     int maxsubsteps;
     int enable_tank;
     float damping_band;  // voxel units
+    int advection;       // BORA_ADVECT_EULER / BORA_ADVECT_RK2
     BoraColliderDev cols;
 };
 

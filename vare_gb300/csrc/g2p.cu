@@ -8,6 +8,7 @@
 // sorted and each warp's trilinear reads hit the same few cells. Killed particles are
 // written with id -1 and dropped by the next step's counting sort.
 #include "bora_internal.h"
+#include "../../include/bora_flip.h"
 
 namespace {
 
@@ -157,11 +158,23 @@ __device__ __noinline__ bool col_kill( const BoraGridDev* g, float3 p )
     return phi > 3.f || phi < 0.f;
 }
 
+// Grid velocity ("comp") at an arbitrary point, for the RK2 option.
+__device__ inline float4 comp_at( const BoraGridDev& g, const int32_t* slot_of, const BoraCellsDev& c, float x, float y,
+                                  float z )
+{
+    GlobalLerp l{ g, slot_of, c };
+    l.setup( x, y, z );
+    return l.comp();
+}
+
 // FLIPMethod::updateParticles for one particle (FLIPMethod.cu:60-170); `smp` has been set
-// up at the particle's position and gives the interpolated grid values.
+// up at the particle's position and gives the interpolated grid values. With the RK2
+// option each substep moves the particle by the midpoint rule in the grid velocity field
+// instead of by its own velocity; everything else is unchanged.
 template <class Sampler>
-__device__ inline bool advance_particle( const BoraGridDev& g, const Sampler& smp, float& px, float& py, float& pz,
-                                         float& vx, float& vy, float& vz, float dt )
+__device__ inline bool advance_particle( const BoraGridDev& g, const Sampler& smp, const int32_t* slot_of,
+                                         const BoraCellsDev& c, float& px, float& py, float& pz, float& vx, float& vy,
+                                         float& vz, float dt )
 {
     const float lx = (float)g.nx + 0.5f, lz = (float)g.nz + 0.5f;
     const float wall = g.voxel_wall;
@@ -196,7 +209,17 @@ __device__ inline bool advance_particle( const BoraGridDev& g, const Sampler& sm
         bool col = false;
         for( int it = 0; it < iter; ++it )
         {
-            px += vx * sub_dt; py += vy * sub_dt; pz += vz * sub_dt;
+            if( g.advection == BORA_ADVECT_RK2 )
+            {
+                const float h = 0.5f * sub_dt;
+                const float4 k1 = comp_at( g, slot_of, c, px, py, pz );
+                const float4 k2 = comp_at( g, slot_of, c, px + k1.x * h, py + k1.y * h, pz + k1.z * h );
+                px += k2.x * sub_dt; py += k2.y * sub_dt; pz += k2.z * sub_dt;
+            }
+            else
+            {
+                px += vx * sub_dt; py += vy * sub_dt; pz += vz * sub_dt;
+            }
             if( py <= wall )
             {
                 if( px < 0.f ) { px = 0.f; if( vx < 0.f ) vx = 0.f; }
@@ -261,7 +284,7 @@ __global__ void __launch_bounds__( kG2PThreads ) k_g2p( const __grid_constant__ 
             GlobalLerp smp{ g, t.slot_of, c };
             smp.setup( px, py, pz );
             adj[q] = smp.surf_min();
-            const bool kill = advance_particle( g, smp, px, py, pz, vx, vy, vz, dt );
+            const bool kill = advance_particle( g, smp, t.slot_of, c, px, py, pz, vx, vy, vz, dt );
             finish( q, pi, px, py, pz, vx, vy, vz, kill );
         }
     }
@@ -295,7 +318,7 @@ __global__ void __launch_bounds__( kG2PThreads ) k_g2p( const __grid_constant__ 
             StagedSampler smp{ {}, fa, fb };
             smp.l.setup( g, ti, tj, tk, px, py, pz );
             adj[q] = smp.surf_min();  // surf background 10 (FLIPMethod.cu:30)
-            const bool kill = advance_particle( g, smp, px, py, pz, vx, vy, vz, dt );
+            const bool kill = advance_particle( g, smp, t.slot_of, c, px, py, pz, vx, vy, vz, dt );
             finish( q, pi, px, py, pz, vx, vy, vz, kill );
         }
     }

@@ -276,7 +276,7 @@ __global__ void __launch_bounds__( 32 * kUpdWarps ) k_pcg_update( int ntiles, Bo
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     float* __restrict__ y = sy[w];
     float* __restrict__ M = sm[w];
-    const float4* __restrict__ r4 = reinterpret_cast<const float4*>( sv.r );
+    const float4* r4 = reinterpret_cast<const float4*>( sv.r );  // also written below
     const float4* __restrict__ q4 = reinterpret_cast<const float4*>( sv.q );
     const float4* __restrict__ m4 = reinterpret_cast<const float4*>( sv.minv );
     DF prz{ 0.f, 0.f }, prr{ 0.f, 0.f };

@@ -23,6 +23,7 @@ BORA_OK = 0
 BORA_WARN_NOT_CONVERGED = 1
 SPACE_WORLD, SPACE_VOXEL = 0, 1
 SOLVER_PLAIN, SOLVER_MIXED = 0, 1
+ADVECT_EULER, ADVECT_RK2 = 0, 1
 STAGE_REBUILD, STAGE_P2G, STAGE_BUILD_SYSTEM, STAGE_SOLVE, STAGE_UPDATE_VELOCITY, STAGE_UPDATE_PARTICLES = range(6)
 FIELD_MASS, FIELD_SURF, FIELD_PRES, FIELD_VELO, FIELD_COMP, FIELD_FLAG, FIELD_RHS, FIELD_CODE = range(8)
 KERNEL_CLASSES = ["bin", "tiles", "sort", "p2g", "rhs", "pcg_direction", "pcg_update", "refine", "velocity", "g2p",
@@ -51,7 +52,7 @@ class Params(ctypes.Structure):
                 ("adjacency_under", ctypes.c_float), ("proj_iteration", ctypes.c_int),
                 ("redist_iteration", ctypes.c_int), ("solver", ctypes.c_int), ("tolerance", ctypes.c_double),
                 ("div_tolerance", ctypes.c_double), ("inner_tolerance", ctypes.c_double),
-                ("max_refinements", ctypes.c_int), ("check_every", ctypes.c_int)]
+                ("max_refinements", ctypes.c_int), ("check_every", ctypes.c_int), ("advection", ctypes.c_int)]
 
 
 class Stats(ctypes.Structure):

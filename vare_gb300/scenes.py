@@ -135,6 +135,32 @@ def config1() -> Scene:
                      sphere=(0.7, 0.8, 0.5, 0.12), name="dam_sphere_256")
 
 
+def config3(scale: int = 1) -> Scene:
+    """Large sparse domain: 1024x512x1024 cells (unit-wide box, 0.5 tall), a shallow tank
+    8 cells deep over the whole floor, a wave column (x < 0.04, lower 30% of the height,
+    all z) released at one end, and a static box obstacle at mid-span; dt = 1/960,
+    seed 0x5EED0003. About 119 M particles at 8 per cell, about 6% of the 1,048,576
+    tiles active. `scale` divides the resolution (8 gives a 128x64x128 copy with a
+    1-cell tank for parity tests)."""
+    nx, ny, nz = 1024 // scale, 512 // scale, 1024 // scale
+    res = (nx, ny, nz)
+    bmin = (0.0, 0.0, 0.0)
+    bmax = (1.0, 0.5, 1.0)
+    depth = 0.5 * 8.0 / 512.0
+
+    def inside(x, y, z):
+        return (y < depth) | ((x < 0.04) & (y < 0.15))
+
+    seed = 0x5EED0003
+    pos = _fill(res, bmin, bmax, inside, seed, 8, chunk_k=max(1, 16 // scale))
+    vel = np.zeros_like(pos)
+    sc = Scene(name="tank_1024" if scale == 1 else f"tank_{nx}", res=res, bmin=bmin, bmax=bmax, dt=1.0 / 960.0,
+               pos=pos, vel=vel, seed=seed)
+    # static box obstacle at mid-span (voxel space), below the column's release height
+    sc.colliders = [((0.45 * nx, -2.0, 0.3 * nz), (0.55 * nx, 0.06 * ny, 0.7 * nz), (0.0, 0.0, 0.0))]
+    return sc
+
+
 def small(n: int = 24, seed: int = 7, sphere: bool = True, dt: float = 1.0 / 120.0) -> Scene:
     """Small dam break + sphere scene for parity tests."""
     return dam_break(n, (0.4, 0.55), seed=seed, dt=dt,
