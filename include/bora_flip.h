@@ -109,6 +109,7 @@ typedef struct bora_flip_stats
                                      velocity, particles, -, total */
     double gpu_ms;                /* device time of the last step (CUDA events on the handle's stream) */
     uint64_t kernel_launches;     /* kernels launched by this handle since creation */
+    uint64_t device_bytes;        /* device memory the handle holds */
 } bora_flip_stats;
 
 /* Kernel classes for opt-in per-kernel device timing (bora_flip_set_profiling). */

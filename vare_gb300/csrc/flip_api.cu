@@ -681,6 +681,25 @@ int add_particles( bora_flip_sim* s, const float* pos, const float* vel, size_t 
 }  // namespace
 
 // ======================================================================================
+// Every device buffer of a handle.
+template <class F>
+void for_each_buffer( bora_flip_sim* s, F&& f )
+{
+    DevBuf* all[] = { &s->tile_flag, &s->tile_act, &s->tile_excl, &s->slot_of, &s->tile_of, &s->nbr, &s->mass, &s->surf,
+                      &s->pres, &s->vx, &s->vy, &s->vz, &s->cx, &s->cy, &s->cz, &s->flag, &s->code, &s->rhs, &s->sx,
+                      &s->se, &s->sr, &s->sd0, &s->sd1, &s->sq, &s->sz, &s->sminv, &s->cell_count, &s->cell_start,
+                      &s->ring, &s->partials, &s->done, &s->adj, &s->vkey, &s->key, &s->idx, &s->scan_scratch,
+                      &s->counters, &s->stage_in, &s->stage_out, &s->live_flag };
+    for( DevBuf* b : all ) f( *b );
+    for( int q = 0; q < 2; ++q )
+        for( int a = 0; a < 7; ++a ) f( s->pbuf[q][a] );
+    for( int l = 0; l < bora_flip_sim::kMaxLevels; ++l )
+    {
+        f( s->mg_type[l] ); f( s->mg_code[l] ); f( s->mg_r[l] );
+        f( s->mg_z0[l] ); f( s->mg_z1[l] );
+    }
+}
+
 extern "C" {
 
 int bora_flip_default_params( bora_flip_params* o )
@@ -776,19 +795,7 @@ int bora_flip_destroy( bora_flip_handle s )
 {
     if( !s ) return BORA_ERR_INVALID_ARG;
     if( s->st ) cudaStreamSynchronize( s->st );
-    DevBuf* all[] = { &s->tile_flag, &s->tile_act, &s->tile_excl, &s->slot_of, &s->tile_of, &s->nbr, &s->mass, &s->surf,
-                      &s->pres, &s->vx, &s->vy, &s->vz, &s->cx, &s->cy, &s->cz, &s->flag, &s->code, &s->rhs, &s->sx,
-                      &s->se, &s->sr, &s->sd0, &s->sd1, &s->sq, &s->sz, &s->sminv, &s->cell_count, &s->cell_start,
-                      &s->ring, &s->partials, &s->done, &s->adj, &s->vkey, &s->key, &s->idx, &s->scan_scratch,
-                      &s->counters, &s->stage_in, &s->stage_out, &s->live_flag };
-    for( DevBuf* b : all ) release( *b );
-    for( int b = 0; b < 2; ++b )
-        for( int a = 0; a < 7; ++a ) release( s->pbuf[b][a] );
-    for( int l = 0; l < bora_flip_sim::kMaxLevels; ++l )
-    {
-        release( s->mg_type[l] ); release( s->mg_code[l] ); release( s->mg_r[l] );
-        release( s->mg_z0[l] ); release( s->mg_z1[l] );
-    }
+    for_each_buffer( s, []( DevBuf& b ) { release( b ); } );
     s->prof_resolve();
     for( cudaEvent_t e : s->evpool ) cudaEventDestroy( e );
     for( int q = 0; q < 2; ++q )
@@ -1044,6 +1051,9 @@ int bora_flip_get_stats( bora_flip_handle s, bora_flip_stats* o )
     if( !s || !o ) return BORA_ERR_INVALID_ARG;
     *o = s->stats;
     o->num_particles = s->nlive;
+    uint64_t bytes = 0;
+    for_each_buffer( s, [&]( DevBuf& b ) { bytes += b.bytes; } );
+    o->device_bytes = bytes;
     return BORA_OK;
 }
 

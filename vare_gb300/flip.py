@@ -62,7 +62,7 @@ class Stats(ctypes.Structure):
                 ("residual_rel", ctypes.c_double), ("residual_max", ctypes.c_double),
                 ("residual_max_dx", ctypes.c_double), ("converged", ctypes.c_int32), ("reserved", ctypes.c_int32),
                 ("stage_ms", ctypes.c_double * 8), ("gpu_ms", ctypes.c_double),
-                ("kernel_launches", ctypes.c_uint64)]
+                ("kernel_launches", ctypes.c_uint64), ("device_bytes", ctypes.c_uint64)]
 
     def as_dict(self) -> dict:
         d = {k: getattr(self, k) for k, _ in self._fields_ if k not in ("reserved", "stage_ms")}

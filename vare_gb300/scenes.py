@@ -184,3 +184,21 @@ def serving_request(r: int, rng: np.random.Generator | None = None) -> tuple[Sce
         sc = dam_break(edge, (1.0, 0.25 * h), seed=seed, dt=1.0 / 240.0,
                        sphere=(0.5, 0.7, 0.5, 0.25 * h + 0.05), name=f"req{r}_drop_{edge}")
     return sc, steps
+
+
+def serving_arrivals(n: int = 64, rate: float = 20.0, seed: int = 0x5EED1000) -> np.ndarray:
+    """Poisson arrival times (s) of the serving stream: exponential gaps at `rate`/s."""
+    rng = np.random.default_rng(seed)
+    return np.cumsum(rng.exponential(1.0 / rate, size=n))
+
+
+def serving_plan(n: int = 64) -> list[tuple[int, int, float]]:
+    """(edge, steps, fill) of each request of the stream, without generating particles."""
+    out = []
+    for r in range(n):
+        rng = np.random.default_rng(0x5EED1000 + r)
+        edge = int(round(math.exp(rng.uniform(math.log(32), math.log(192)))))
+        fill = float(rng.uniform(0.2, 0.5))
+        steps = int(rng.integers(50, 401))
+        out.append((edge, steps, fill))
+    return out
