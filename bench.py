@@ -38,8 +38,9 @@ METRIC = "particle-steps/s at 256^3 FLIP (plain FP32 block-MIC(0)-PCG, max|div u
 UNIT = "particle-steps/s"
 
 # Algorithmic bytes per launch of each kernel class: (bytes per active cell, bytes per particle).
-#   pcg_direction: read z, d (8) + stencil code (2); write d', q (8)            -> 18 B/cell
-#   pcg_update:    read e, d, r, q (16) + M^-1 (4) + code (2); write e, r, z (12) -> 34 B/cell
+#   pcg_direction: read z, d (8) + stencil code (2) + e (4); write d', q (8) + e (4) -> 26 B/cell
+#                  (the previous update's e += alpha d is applied here)
+#   pcg_update:    read r, q (8) + M^-1 (4); write r, z (8)                   -> 20 B/cell
 #   p2g:           per particle read idx (4) + pos, vel (24); per cell read dual-cell
 #                  starts (4), write mass, count, velocity (20) + flag (1)      -> 25 B/cell, 28 B/particle
 #   g2p:           per particle idx (4), read pos, vel, id (28), write (28), adjacency (4);
@@ -49,15 +50,16 @@ UNIT = "particle-steps/s"
 #   refine:        per pass read x (8), e (4), b (4), code (2); write x (8), r (4) -> 30 B/cell
 #   sort:          per particle read vkey (4), write key (4), read key (4), write idx (4); per cell scan 12 B
 #   bin:           per particle read id + pos (16), write vkey (4)
+#   mg_vcycle:     level 0 down: read r (4), code (2); write z0 (2), coarse r (0.25); level 0 up:
+#                  read r (4), code (2), z0 (2), coarse z (0.25); write z (4) -> 20.5 B per fine
+#                  cell, plus the coarser levels (1/8 of that per level)       -> 23 B/cell
 ALG_BYTES = {
     "bin": (0, 20), "tiles": (0, 0), "sort": (12, 16), "p2g": (25, 28), "rhs": (25, 0),
-    "pcg_direction": (18, 0), "pcg_update": (34, 0), "refine": (30, 0), "velocity": (33, 0), "g2p": (28, 64),
-    "mg_vcycle": (43, 0),
+    "pcg_direction": (26, 0), "pcg_update": (20, 0), "refine": (30, 0), "velocity": (33, 0), "g2p": (28, 64),
+    "mg_vcycle": (23, 0),
 }
-# Mixed form: the PCG update has no preconditioner sweep (read e, d, r, q; write e, r: 24 B/cell);
-# one V-cycle moves ~38 B per fine cell (FP16 level vectors, FP32 residual in, FP32 z out)
-# plus ~1/7 of that on the coarse levels -> 43 B/cell.
-ALG_BYTES_MIXED = dict(ALG_BYTES, pcg_update=(24, 0))
+# Mixed form: the PCG update has no preconditioner sweep (read r, q; write r: 12 B/cell).
+ALG_BYTES_MIXED = dict(ALG_BYTES, pcg_update=(12, 0))
 
 
 def parse():
