@@ -520,6 +520,10 @@ int stage_solve( bora_flip_sim* s )
     bool converged = false;
     const int max_inner = std::max( 1, p.proj_iteration );
     const int check = std::max( 1, p.check_every );
+    // The Krylov recurrence continues across refinement passes (residual replacement): a
+    // pass ends by replacing the recursive FP32 residual with the FP64 one, keeps the last
+    // direction d and r.z, and the next pass carries on from them instead of restarting.
+    int rz_prev = -1, dsel = 0;
     for( ;; )
     {
         const bool norm_ok = rnorm <= p.tolerance * bnorm;
@@ -553,7 +557,7 @@ int stage_solve( bora_flip_sim* s )
         Check pend[bora_flip_sim::kChecks];
         int npend = 0, nchk = 0;
         bool done = false;
-        int rz_prev = -1, dsel = 0, it = 0;
+        int it = 0;
         int a_rz = -1, a_dq = -1;  // alpha of the last update, whose e += alpha d is still pending
         while( it < max_inner && !done )
         {
@@ -610,6 +614,12 @@ int stage_solve( bora_flip_sim* s )
         rmax = read_ring( s, s_mx, &status );
         BORA_TRYS( status );
         if( !std::isfinite( rnorm ) ) break;
+        // Continue the recurrence only while the FP64 residual still agrees with the
+        // recursive one (the device finished the pass, so its last r.r is in mapped memory);
+        // a larger drift would break conjugacy, so the next pass restarts (beta = 0).
+        const double rr_rec = ( (volatile double*)s->h_mirror )[rr_cur];
+        const double rec = rr_rec > 0.0 ? std::sqrt( rr_rec ) : 0.0;
+        if( !( rec > 0.0 ) || rnorm > 1.5 * rec ) rz_prev = -1;
     }
     { KTimer t( s, BORA_KERNEL_REFINE, 1 ); bora_launch_write_pressure( s->ntiles, code, sv.x, P<float>( s->pres ), st ); }
     BORA_TRYS( check_launch( s ) );
@@ -723,7 +733,7 @@ int bora_flip_default_params( bora_flip_params* o )
     o->solver = BORA_SOLVER_PLAIN;
     o->tolerance = 1e-6;
     o->div_tolerance = 1e-5;
-    o->inner_tolerance = 1e-4;
+    o->inner_tolerance = 1e-3;
     o->max_refinements = 8;
     o->check_every = 1;
     o->advection = BORA_ADVECT_EULER;

@@ -514,7 +514,8 @@ __global__ void k_solve_init( size_t ncells, const float* __restrict__ b, BoraSo
     reduce2_publish_dfmax( n2, mx, red, slot_norm2, slot_max );
 }
 
-// x += e (+ the last update's pending alpha d), then clear the inner solve's vectors.
+// x += e (+ the last update's pending alpha d), then clear e and q; the direction d is kept
+// (the next refinement pass continues the recurrence from it).
 __global__ void k_refine_accumulate( size_t ncells, const uint16_t* __restrict__ code, BoraSolverDev sv, int dsel,
                                      const double* __restrict__ ring, int slot_a_rz, int slot_a_dq )
 {
@@ -528,8 +529,6 @@ __global__ void k_refine_accumulate( size_t ncells, const uint16_t* __restrict__
         const float e = slot_a_rz < 0 ? sv.e[i] : fmaf( alpha, d[i], sv.e[i] );
         if( code[i] & BORA_CODE_FLUID ) sv.x[i] += (double)e;
         sv.e[i] = 0.f;
-        sv.d[0][i] = 0.f;
-        sv.d[1][i] = 0.f;
         sv.q[i] = 0.f;
     }
 }
