@@ -318,7 +318,7 @@ __device__ inline void restrict_cells( const FNav& fnav, const BoraLevelDev& F, 
         const long long pc = t >> 3;
         const int o = (int)( t & 7 );
         float res = 0.f;
-        if( t < total && ( C.code[pc] & BORA_CODE_FLUID ) )
+        if( t < total )  // a coarse cell is fluid exactly when a child is; others sum zeros
         {
             long long fc = -1;
             if( MODE == 0 )
@@ -555,7 +555,7 @@ __global__ void __launch_bounds__( 256 ) k_mg_smooth_last( Nav nav, BoraLevelDev
 // in the cluster's first CTA.
 constexpr int kTailLevels = 8;
 constexpr int kTailThreads = 1024;
-constexpr int kTailCtas = 8;  // portable cluster size
+constexpr int kTailCtasMax = 16;  // non-portable cluster size, where the device supports it
 constexpr size_t kTailMaxCells = 32768;
 
 __device__ inline void cluster_barrier()
@@ -1049,6 +1049,35 @@ int tail_start( const BoraLevelDev* levels, int nlevels )
 
 bool fused_level( const BoraLevelDev& L ) { return L.kind == 0 && L.E >= 2; }
 
+// CTAs of the tail cluster: 16 where the device can co-schedule such a cluster of this
+// kernel, else the portable 8.
+int tail_cluster_size()
+{
+    static int size[64] = { 0 };
+    int dev = 0;
+    cudaGetDevice( &dev );
+    if( dev >= 0 && dev < 64 && size[dev] > 0 ) return size[dev];
+    int n = 8;
+    if( cudaFuncSetAttribute( k_mg_tail, cudaFuncAttributeNonPortableClusterSizeAllowed, 1 ) == cudaSuccess )
+    {
+        cudaLaunchConfig_t cfg{};
+        cfg.gridDim = dim3( kTailCtasMax );
+        cfg.blockDim = dim3( kTailThreads );
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = kTailCtasMax;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        int clusters = 0;
+        if( cudaOccupancyMaxActiveClusters( &clusters, k_mg_tail, &cfg ) == cudaSuccess && clusters > 0 ) n = kTailCtasMax;
+    }
+    cudaGetLastError();  // a refused query leaves no error behind
+    if( dev >= 0 && dev < 64 ) size[dev] = n;
+    return n;
+}
+
 }  // namespace
 
 int bora_mg_vcycle_launches( const BoraLevelDev* levels, int nlevels )
@@ -1107,13 +1136,14 @@ void bora_mg_vcycle( const BoraGridDev& g, const BoraLevelDev* levels, int nleve
         d.nbr = t.nbr; d.tile_of = t.tile_of; d.slot_of = t.slot_of;
         d.tx = g.tx; d.ty = g.ty; d.tz = g.tz;
         d.sweeps = coarse_sweeps;
+        const int ctas = tail_cluster_size();
         cudaLaunchConfig_t cfg{};
-        cfg.gridDim = dim3( kTailCtas );
+        cfg.gridDim = dim3( ctas );
         cfg.blockDim = dim3( kTailThreads );
         cfg.stream = st;
         cudaLaunchAttribute attr[1];
         attr[0].id = cudaLaunchAttributeClusterDimension;
-        attr[0].val.clusterDim.x = kTailCtas;
+        attr[0].val.clusterDim.x = ctas;
         attr[0].val.clusterDim.y = 1;
         attr[0].val.clusterDim.z = 1;
         cfg.attrs = attr;
