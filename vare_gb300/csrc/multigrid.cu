@@ -866,6 +866,7 @@ __global__ void __launch_bounds__( TileRegion<E>::NT, TileRegion<E>::MINB ) k_mg
     int n = 0;
     for( int s = blockIdx.x; s < ntiles; s += G, ++n )
     {
+        float trz = 0.f;  // this thread's r.z over its cells of the tile
 #pragma unroll
         for( int it = 0; it < TR::IA; ++it )
         {
@@ -903,13 +904,14 @@ __global__ void __launch_bounds__( TileRegion<E>::NT, TileRegion<E>::MINB ) k_mg
             {
                 const float zf = zc / sc;  // undo the FP16 scaling of the residual
                 zout[g] = zf;
-                if( cc & BORA_CODE_FLUID ) rz = df_add( rz, df_prod( rraw[l], zf ) );
+                if( cc & BORA_CODE_FLUID ) trz = fmaf( rraw[l], zf, trz );
             }
             else
             {
                 F.z1[g] = __float2half_rn( zc );
             }
         }
+        if( L0 ) rz = df_add_f( rz, trz );
         if( tid < 27 ) nbb[n & 1][tid] = nb2;
         __syncthreads();  // the next tile's staging overwrites the shared arrays
     }
@@ -936,8 +938,7 @@ __global__ void __launch_bounds__( 256 ) k_pcg_update_noprec( size_t ncells, Bor
         const float4 q = q4[v];
         r.x = fmaf( -alpha, q.x, r.x ); r.y = fmaf( -alpha, q.y, r.y ); r.z = fmaf( -alpha, q.z, r.z ); r.w = fmaf( -alpha, q.w, r.w );
         r4[v] = r;
-        rr = df_add( rr, df_prod( r.x, r.x ) ); rr = df_add( rr, df_prod( r.y, r.y ) );
-        rr = df_add( rr, df_prod( r.z, r.z ) ); rr = df_add( rr, df_prod( r.w, r.w ) );
+        rr = df_add_f( rr, dot4( r, r ) );
     }
     reduce2_publish_warp( df_warp_sum( rr ), 0.0, 0, red, slot_rr_out, -1 );
 }

@@ -299,8 +299,7 @@ __global__ void __launch_bounds__( 32 * kUpdWarps ) k_pcg_update( int ntiles, Bo
             reinterpret_cast<float4*>( sv.r )[b4 + lane + 32 * k] = r[k];
             reinterpret_cast<float4*>( y )[lane + 32 * k] = r[k];
             reinterpret_cast<float4*>( M )[lane + 32 * k] = mv[k];
-            prr = df_add( prr, df_prod( r[k].x, r[k].x ) ); prr = df_add( prr, df_prod( r[k].y, r[k].y ) );
-            prr = df_add( prr, df_prod( r[k].z, r[k].z ) ); prr = df_add( prr, df_prod( r[k].w, r[k].w ) );
+            prr = df_add_f( prr, dot4( r[k], r[k] ) );
         }
         __syncwarp();
         // forward: y_c = (r_c + sum_{lower m} M_m y_m) M_c   (A_mc = -1)
@@ -337,8 +336,7 @@ __global__ void __launch_bounds__( 32 * kUpdWarps ) k_pcg_update( int ntiles, Bo
         {
             const float4 z = reinterpret_cast<const float4*>( y )[lane + 32 * k];
             reinterpret_cast<float4*>( sv.z )[b4 + lane + 32 * k] = z;
-            prz = df_add( prz, df_prod( r[k].x, z.x ) ); prz = df_add( prz, df_prod( r[k].y, z.y ) );
-            prz = df_add( prz, df_prod( r[k].z, z.z ) ); prz = df_add( prz, df_prod( r[k].w, z.w ) );
+            prz = df_add_f( prz, dot4( r[k], z ) );
         }
         __syncwarp();
     }
@@ -462,6 +460,7 @@ __global__ void __launch_bounds__( dirtile::NT ) k_pcg_direction_tiles( int ntil
         const int32_t nb2 = tid < 27 ? nbr_entry( s + 2 * G ) : -1;
         __syncthreads();
         if( s + G < ntiles ) { BORA_DIR_ISSUE( nbb[( n + 1 ) & 1], s + G ); }
+        float tdq = 0.f;  // this thread's d'.q over its cells of the tile
 #pragma unroll
         for( int it = 0; it < IC; ++it )
         {
@@ -479,13 +478,14 @@ __global__ void __launch_bounds__( dirtile::NT ) k_pcg_direction_tiles( int ntil
                 acc += dn_s[h - R * R];
                 acc += dn_s[h + R * R];
                 qv = fmaf( (float)code_diag( (uint16_t)cc[it] ), dn, -acc );
-                pdq = df_add( pdq, df_prod( dn, qv ) );
+                tdq = fmaf( dn, qv, tdq );
             }
             const size_t g = (size_t)s * 512 + l;
             dnew[g] = dn;
             sv.q[g] = qv;
             if( upd_e ) sv.e[g] = fmaf( alpha, do_s[l], ee[it] );
         }
+        pdq = df_add_f( pdq, tdq );
         if( tid < 27 ) nbb[n & 1][tid] = nb2;
         __syncthreads();
     }

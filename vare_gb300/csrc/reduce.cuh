@@ -29,6 +29,23 @@ __device__ __forceinline__ DF df_add( DF a, DF b )
     const float h = s + err;
     return DF{ h, err - ( h - s ) };
 }
+// DF + float (TwoSum with a zero low part).
+__device__ __forceinline__ DF df_add_f( DF a, float b )
+{
+    const float s = a.hi + b;
+    const float bb = s - a.hi;
+    const float err = ( ( a.hi - ( s - bb ) ) + ( b - bb ) ) + a.lo;
+    const float h = s + err;
+    return DF{ h, err - ( h - s ) };
+}
+// FP32 dot product of two float4 (fused multiply-adds). Short FP32 partial sums like this
+// one (4 terms, relative error ~2^-22) feed the double-float accumulators: that keeps the
+// totals accurate to ~1e-7 relative, far more than the FP32 alpha and beta of PCG need,
+// at a quarter of the double-float operations.
+__device__ __forceinline__ float dot4( float4 a, float4 b )
+{
+    return fmaf( a.w, b.w, fmaf( a.z, b.z, fmaf( a.y, b.y, a.x * b.x ) ) );
+}
 __device__ __forceinline__ double df_warp_sum( DF v )
 {
 #pragma unroll
