@@ -105,7 +105,7 @@ typedef struct bora_flip_stats
     double residual_max;          /* max_i |b - A p|_i (1/s) */
     double residual_max_dx;       /* residual_max * dx_world */
     int32_t converged;
-    int32_t reserved;
+    int32_t mg_vcycle_launches;   /* kernel launches per V-cycle in the last solve (mixed form), else 0 */
     double stage_ms[8];           /* host wall time of the last step: rebuild, p2g, system, solve,
                                      velocity, particles, -, total */
     double gpu_ms;                /* device time of the last step (CUDA events on the handle's stream) */

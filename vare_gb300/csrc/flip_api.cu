@@ -534,6 +534,7 @@ int stage_solve( bora_flip_sim* s )
         const double target = norm_ok ? 0.1 * rnorm : std::max( p.inner_tolerance * rnorm, 0.25 * p.tolerance * bnorm );
         const bool mixed = p.solver == BORA_SOLVER_MIXED;
         const int vlaunch = bora_mg_vcycle_launches( s->levels, s->nlevels );
+        s->stats.mg_vcycle_launches = mixed ? vlaunch : 0;
         auto precondition = [&]( int rr_slot, int rz_slot ) {
             KTimer t( s, BORA_KERNEL_MG, vlaunch );
             bora_mg_vcycle( s->g, s->levels, s->nlevels, s->tiles(), sv.r, sv.z, red, rr_slot, rz_slot, 16, st );

@@ -60,7 +60,7 @@ class Stats(ctypes.Structure):
                 ("active_tiles", ctypes.c_int32), ("fluid_cells", ctypes.c_int32),
                 ("solver_iterations", ctypes.c_int32), ("refinements", ctypes.c_int32),
                 ("residual_rel", ctypes.c_double), ("residual_max", ctypes.c_double),
-                ("residual_max_dx", ctypes.c_double), ("converged", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("residual_max_dx", ctypes.c_double), ("converged", ctypes.c_int32), ("mg_vcycle_launches", ctypes.c_int32),
                 ("stage_ms", ctypes.c_double * 8), ("gpu_ms", ctypes.c_double),
                 ("kernel_launches", ctypes.c_uint64), ("device_bytes", ctypes.c_uint64)]
 
