@@ -8,6 +8,36 @@
 
 #include "flip_common.cuh"
 
+#include <utility>
+
+// ---- programmatic dependent launch ---------------------------------------------------
+// The kernels of a solver iteration form a chain in which each one reads what the one
+// before wrote. They are launched with programmatic stream serialisation: a kernel may
+// start while its predecessor is finishing, runs the part of its prologue that touches
+// only data no kernel of the chain writes (tile tables, stencil codes, index set-up), and
+// then waits for the predecessor's completion (griddepcontrol.wait) before anything else.
+// Each kernel of the chain allows its successor to launch as soon as all of its own CTAs
+// have started (griddepcontrol.launch_dependents), so earlier kernels are never starved.
+__device__ __forceinline__ void bora_pdl_trigger() { asm volatile( "griddepcontrol.launch_dependents;" ::: "memory" ); }
+__device__ __forceinline__ void bora_pdl_wait() { asm volatile( "griddepcontrol.wait;" ::: "memory" ); }
+
+template <typename... KArgs, typename... Args>
+cudaError_t bora_launch_pdl( void ( *kernel )( KArgs... ), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                             Args&&... args )
+{
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx( &cfg, kernel, std::forward<Args>( args )... );
+}
+
 // ---- scan ---------------------------------------------------------------------------
 size_t bora_scan_scratch_elems( size_t n );
 void bora_device_scan( const uint32_t* in, uint32_t* out, size_t n, uint32_t* scratch, uint32_t* total, cudaStream_t st );

@@ -580,6 +580,8 @@ struct TailDesc
 __global__ void __launch_bounds__( kTailThreads ) k_mg_tail( const __grid_constant__ TailDesc d, uint32_t* err )
 {
     __shared__ CoarsestSmem sm;
+    bora_pdl_trigger();
+    bora_pdl_wait();
     const long long i0 = blockIdx.x * (long long)blockDim.x + threadIdx.x, st = (long long)gridDim.x * blockDim.x;
     auto with_level = [&]( int t, auto&& f ) {
         const int cdx = t + 1 < d.n ? d.L[t + 1].dx : 0, cdy = t + 1 < d.n ? d.L[t + 1].dy : 0;
@@ -713,8 +715,8 @@ __global__ void __launch_bounds__( TileRegion<E>::NT, TileRegion<E>::MINB ) k_mg
     __shared__ float wd[16];
     __shared__ float s_scale;
     const int tid = threadIdx.x, G = gridDim.x;
+    bora_pdl_trigger();
     init_wd( wd );
-    if( tid == 0 ) s_scale = L0 ? scale_of( ring, slot_rr ) : 1.f;
     if( tid < 27 )
     {
         nbb[0][tid] = nbr_entry( t, blockIdx.x, ntiles, tid );
@@ -728,6 +730,8 @@ __global__ void __launch_bounds__( TileRegion<E>::NT, TileRegion<E>::MINB ) k_mg
     for( int it = 0; it < TR::IB; ++it ) bh[it] = TR::qh( tid + it * NT );
 #pragma unroll
     for( int it = 0; it < TR::IC; ++it ) { ch[it] = TR::th( tid + it * NT ); ch2[it] = TR::th2( tid + it * NT ); }
+    bora_pdl_wait();  // the previous kernel's results are complete from here
+    if( tid == 0 ) s_scale = L0 ? scale_of( ring, slot_rr ) : 1.f;
     __syncthreads();
     const float sc = s_scale;
     uint16_t cv[TR::IA];
@@ -823,8 +827,8 @@ __global__ void __launch_bounds__( TileRegion<E>::NT, TileRegion<E>::MINB ) k_mg
     __shared__ float wd[16];
     __shared__ float s_scale;
     const int tid = threadIdx.x, G = gridDim.x;
+    bora_pdl_trigger();
     init_wd( wd );
-    if( tid == 0 ) s_scale = L0 ? scale_of( red.ring, slot_rr ) : 1.f;
     if( tid < 27 )
     {
         nbb[0][tid] = nbr_entry( t, blockIdx.x, ntiles, tid );
@@ -838,6 +842,8 @@ __global__ void __launch_bounds__( TileRegion<E>::NT, TileRegion<E>::MINB ) k_mg
     for( int it = 0; it < TR::IB; ++it ) bh[it] = TR::qh( tid + it * NT );
 #pragma unroll
     for( int it = 0; it < TR::IC; ++it ) { ch[it] = TR::th( tid + it * NT ); ch2[it] = TR::th2( tid + it * NT ); }
+    bora_pdl_wait();  // the previous kernel's results are complete from here
+    if( tid == 0 ) s_scale = L0 ? scale_of( red.ring, slot_rr ) : 1.f;
     __syncthreads();
     const float sc = s_scale;
     uint16_t cv[TR::IA];
@@ -925,6 +931,8 @@ __global__ void __launch_bounds__( 256 ) k_pcg_update_noprec( size_t ncells, Bor
                                                               int slot_rz, int slot_dq, int slot_rr_out )
 {
     __shared__ float s_alpha;
+    bora_pdl_trigger();
+    bora_pdl_wait();
     if( threadIdx.x == 0 ) s_alpha = slot_rz < 0 ? 0.f : (float)( red.ring[slot_rz] / red.ring[slot_dq] );
     __syncthreads();
     const float alpha = s_alpha;
@@ -979,7 +987,7 @@ void launch_down_fused( const BoraLevelDev& F, const BoraLevelDev& C, BoraTilesD
     static int per_sm[64] = { 0 };
     constexpr int NT = TileRegion<E>::NT;
     const int grid = fused_grid( k_mg_down_fused<E, L0>, NT, ntiles, per_sm );
-    k_mg_down_fused<E, L0><<<grid, NT, 0, st>>>( F, C, t, ntiles, r0, slot_rr, ring );
+    bora_launch_pdl( k_mg_down_fused<E, L0>, grid, NT, 0, st, F, C, t, ntiles, r0, slot_rr, ring );
 }
 
 template <int E, bool L0>
@@ -990,7 +998,7 @@ void launch_up_fused( const BoraLevelDev& F, const __half* ec, BoraTilesDev t, i
     constexpr int NT = TileRegion<E>::NT;
     int grid = fused_grid( k_mg_up_fused<E, L0>, NT, ntiles, per_sm );
     if( L0 ) grid = std::min( grid, 152 * 16 );  // partial sums capacity of the reduction
-    k_mg_up_fused<E, L0><<<grid, NT, 0, st>>>( F, ec, t, ntiles, r0, slot_rr, red, zout, slot_rz );
+    bora_launch_pdl( k_mg_up_fused<E, L0>, grid, NT, 0, st, F, ec, t, ntiles, r0, slot_rr, red, zout, slot_rz );
 }
 
 LevelNav nav_of( const BoraGridDev& g, const BoraLevelDev& L, BoraTilesDev t )
@@ -1144,13 +1152,15 @@ void bora_mg_vcycle( const BoraGridDev& g, const BoraLevelDev* levels, int nleve
         cfg.gridDim = dim3( ctas );
         cfg.blockDim = dim3( kTailThreads );
         cfg.stream = st;
-        cudaLaunchAttribute attr[1];
+        cudaLaunchAttribute attr[2];
         attr[0].id = cudaLaunchAttributeClusterDimension;
         attr[0].val.clusterDim.x = ctas;
         attr[0].val.clusterDim.y = 1;
         attr[0].val.clusterDim.z = 1;
+        attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[1].val.programmaticStreamSerializationAllowed = 1;
         cfg.attrs = attr;
-        cfg.numAttrs = 1;
+        cfg.numAttrs = 2;
         cudaLaunchKernelEx( &cfg, k_mg_tail, d, red.err );
     }
     else
@@ -1187,5 +1197,5 @@ void bora_launch_pcg_update_noprec( int ntiles, BoraSolverDev s, BoraReduceDev r
                                     int slot_rr_out, cudaStream_t st )
 {
     const size_t nc = (size_t)ntiles * 512;
-    k_pcg_update_noprec<<<blocks_for( nc / 4 ), 256, 0, st>>>( nc, s, red, slot_rz, slot_dq, slot_rr_out );
+    bora_launch_pdl( k_pcg_update_noprec, blocks_for( nc / 4 ), 256, 0, st, nc, s, red, slot_rz, slot_dq, slot_rr_out );
 }

@@ -269,7 +269,9 @@ __global__ void __launch_bounds__( 32 * kUpdWarps ) k_pcg_update( int ntiles, Bo
     __shared__ __align__( 16 ) float sm[kUpdWarps][512];
     __shared__ uint16_t pc[512], ps[23];
     __shared__ float s_alpha;
+    bora_pdl_trigger();
     load_plane_tables( pc, ps );
+    bora_pdl_wait();  // the previous kernel's results are complete from here
     if( threadIdx.x == 0 ) s_alpha = slot_rz_in < 0 ? 0.f : (float)( red.ring[slot_rz_in] / red.ring[slot_dq_in] );
     __syncthreads();
     const float alpha = s_alpha;
@@ -396,14 +398,10 @@ __global__ void __launch_bounds__( dirtile::NT ) k_pcg_direction_tiles( int ntil
     __shared__ int32_t nbb[2][27];
     __shared__ float s_beta, s_alpha;
     const int tid = threadIdx.x, G = gridDim.x;
-    if( tid == 0 )
-    {
-        s_beta = slot_rz_old < 0 ? 0.f : (float)( red.ring[slot_rz_new] / red.ring[slot_rz_old] );
-        s_alpha = slot_a_rz < 0 ? 0.f : (float)( red.ring[slot_a_rz] / red.ring[slot_a_dq] );
-    }
+    bora_pdl_trigger();
     const bool upd_e = slot_a_rz >= 0;  // the previous update's e += alpha d is still pending
     auto nbr_entry = [&]( int s ) { return s < ntiles ? nbr[(size_t)s * 27 + tid] : -1; };
-    if( tid < 27 )
+    if( tid < 27 )  // tile tables: not written by the solver chain
     {
         nbb[0][tid] = nbr_entry( blockIdx.x );
         nbb[1][tid] = nbr_entry( blockIdx.x + G );
@@ -411,6 +409,12 @@ __global__ void __launch_bounds__( dirtile::NT ) k_pcg_direction_tiles( int ntil
     uint32_t am[IA];
 #pragma unroll
     for( int it = 0; it < IA; ++it ) am[it] = region_map( tid + it * NT );
+    bora_pdl_wait();  // the previous kernel's results (ring, z, d, e) are complete from here
+    if( tid == 0 )
+    {
+        s_beta = slot_rz_old < 0 ? 0.f : (float)( red.ring[slot_rz_new] / red.ring[slot_rz_old] );
+        s_alpha = slot_a_rz < 0 ? 0.f : (float)( red.ring[slot_a_rz] / red.ring[slot_a_dq] );
+    }
     __syncthreads();
     const float beta = s_beta, alpha = s_alpha;
     const float* __restrict__ dold = dsel_in ? sv.d[1] : sv.d[0];  // selects keep sv out of local memory
@@ -713,7 +717,8 @@ void bora_launch_pcg_update( int ntiles, const uint16_t* code, BoraSolverDev s, 
         if( dev >= 0 && dev < 64 ) per_sm[dev] = bps;
     }
     const int nb = std::max( 1, std::min( { ( ntiles + kUpdWarps - 1 ) / kUpdWarps, bps * num_sms(), 152 * 16 } ) );
-    k_pcg_update<<<nb, 32 * kUpdWarps, 0, st>>>( ntiles, s, red, slot_rz_in, slot_dq_in, slot_rz_out, slot_rr_out );
+    bora_launch_pdl( k_pcg_update, nb, 32 * kUpdWarps, 0, st, ntiles, s, red, slot_rz_in, slot_dq_in, slot_rz_out,
+                     slot_rr_out );
 }
 
 void bora_launch_pcg_direction( const BoraGridDev&, int ntiles, BoraTilesDev t, const uint16_t* code, BoraSolverDev s,
@@ -731,8 +736,8 @@ void bora_launch_pcg_direction( const BoraGridDev&, int ntiles, BoraTilesDev t, 
         if( dev >= 0 && dev < 64 ) per_sm[dev] = b;
     }
     const int grid = std::max( 1, std::min( { ntiles, b * num_sms(), 152 * 16 } ) );  // partial sums capacity
-    k_pcg_direction_tiles<<<grid, dirtile::NT, 0, st>>>( ntiles, t.nbr, code, s, dsel_in, red, slot_rz_new, slot_rz_old,
-                                                         slot_dq_out, slot_a_rz, slot_a_dq );
+    bora_launch_pdl( k_pcg_direction_tiles, grid, dirtile::NT, 0, st, ntiles, (const int32_t*)t.nbr, code, s, dsel_in, red,
+                     slot_rz_new, slot_rz_old, slot_dq_out, slot_a_rz, slot_a_dq );
 }
 
 void bora_launch_refine_accumulate( int ntiles, const uint16_t* code, BoraSolverDev s, int dsel, const double* ring,
