@@ -334,18 +334,15 @@ def timed_steps(sim, sc, args, world, flip, local, sample_clocks, alg=ALG_BYTES)
     cell_b, part_b = alg.get(name, (0, 0))
     avg_launch_ms = float(kms[dom] / max(1, kn[dom]))
     bytes_per_launch = cell_b * ncells + part_b * sim.num_particles
-    if name == "mg_vcycle":  # the model is per V-cycle; the class counts its kernel launches
-        bytes_per_launch /= max(1, sim.stats()["mg_vcycle_launches"])
     peak, peak_kind = measured_peaks()
     achieved = bytes_per_launch / (avg_launch_ms * 1e-3) / 1e9 if avg_launch_ms > 0 else 0.0
     traffic, tnote = ncu_traffic(name)
-    if name == "mg_vcycle" and traffic:  # committed per V-cycle; report per launch like the bytes
-        traffic /= max(1, sim.stats()["mg_vcycle_launches"])
     roof = {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "traffic": traffic,
             "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
             else "fallback 6.8 TB/s",
             "alg_bytes_per_launch": bytes_per_launch, "avg_launch_ms": avg_launch_ms,
+            "kernels_per_launch": (sim.stats()["mg_vcycle_launches"] if name == "mg_vcycle" else 1),
             "launches_per_step": float(kn[dom]) / args.steps, "active_cells": ncells,
             "share_of_warmup_device_time": {c: round(v / max(1e-9, sum(share.values())), 4)
                                             for c, v in share.items()}}
