@@ -350,8 +350,18 @@ def timed_steps(sim, sc, args, world, flip, local, sample_clocks, alg=ALG_BYTES)
         roof["traffic_note"] = tnote
     ms_sorted = sorted(step_ms)
     p99 = ms_sorted[min(len(ms_sorted) - 1, int(round(0.99 * (len(ms_sorted) - 1))))]
+    # whole-step compulsory traffic (per particle, per active cell, per unknown and PCG
+    # iteration, per refinement sweep) against the measured HBM bandwidth
+    nu = int(np.count_nonzero(sim.field(flip.FIELD_FLAG) == 4))  # fluid cells = unknowns
+    b_it = 87 if alg is ALG_BYTES_MIXED else 69
+    passes = sim.stats()["refinements"]
+    b_step = (92 * sim.num_particles + 90 * ncells + b_it * nu * float(np.mean(iters)) + 13 * nu * passes)
+    step_roof = {"bytes_per_step": b_step, "achieved": b_step / (t_max / args.steps) / 1e9, "peak": peak,
+                 "unit": "GB/s", "frac": b_step / (t_max / args.steps) / 1e9 / peak,
+                 "model": f"92 B/particle + 90 B/active cell + {b_it} B/unknown/PCG iteration + 13 B/unknown/refinement"}
     return {"value": total_ps / t_max, "t_max": t_max, "ms_per_step": t_max * 1e3 / args.steps,
-            "p50_ms": ms_sorted[len(ms_sorted) // 2], "p99_ms": p99, "roofline": roof, "clocks": clk,
+            "p50_ms": ms_sorted[len(ms_sorted) // 2], "p99_ms": p99, "roofline": roof, "step_roofline": step_roof,
+            "clocks": clk,
             "launches": int(launches),
             "solver": {"iterations_per_step": iters, "all_converged": all_conv, **worst,
                        "active_tiles": fi["ntiles"]}}
@@ -410,7 +420,8 @@ def run_ours(args, world, rank, local):
         sim = flip.FlipSim.from_scene(sc, solver=flip.SOLVER_MIXED)
         mm = timed_steps(sim, sc, args, world, flip, local, False, ALG_BYTES_MIXED)
         mixed = {"value": mm["value"], "unit": UNIT, "ms_per_step": mm["ms_per_step"], "p50_ms": mm["p50_ms"],
-                 "p99_ms": mm["p99_ms"], "roofline": mm["roofline"], "gpu_launches": mm["launches"],
+                 "p99_ms": mm["p99_ms"], "roofline": mm["roofline"], "step_roofline": mm["step_roofline"],
+                 "gpu_launches": mm["launches"],
                  "solver": mm["solver"], "speedup_over_plain": mm["value"] / value,
                  "config": "same scene; geometric-multigrid-preconditioned CG, V(2,2) damped Jacobi, FP16 level "
                            "storage with FP32 arithmetic, FP64-accurate dots and norms, FP64 iterative refinement"}
@@ -433,7 +444,8 @@ def run_ours(args, world, rank, local):
                    "no public data set exists for this path)",
            "config": workload_config(sc, solver=args.solver if args.solver != "both" else "plain"), "roofline": roof,
            "cpu_baseline": cpu, "e2e": e2e,
-           "gpu_launches": int(launches), "clocks": clk, "solver": meas["solver"], "mixed": mixed}
+           "gpu_launches": int(launches), "clocks": clk, "solver": meas["solver"], "step_roofline": meas["step_roofline"],
+           "mixed": mixed}
     print(json.dumps(out), flush=True)
 
 

@@ -104,7 +104,7 @@ void bora_launch_scatter( size_t n, const uint32_t* key, const uint32_t* start, 
 void bora_launch_order_bins( size_t nbins, const uint32_t* start, uint32_t* idx, cudaStream_t st );
 void bora_launch_p2g( const BoraGridDev& g, int ntiles, BoraTilesDev t, BoraParticlesDev p, const uint32_t* idx,
                       const uint32_t* start, BoraCellsDev c, cudaStream_t st );
-void bora_launch_rhs( const BoraGridDev& g, int ntiles, BoraTilesDev t, BoraCellsDev c, cudaStream_t st );
+void bora_launch_rhs( const BoraGridDev& g, int ntiles, BoraTilesDev t, BoraCellsDev c, uint32_t* nfluid, cudaStream_t st );
 void bora_launch_vel_update( const BoraGridDev& g, int ntiles, BoraTilesDev t, BoraCellsDev c, cudaStream_t st );
 void bora_launch_g2p( const BoraGridDev& g, int ntiles, size_t nsorted, BoraTilesDev t, const uint32_t* start, BoraCellsDev c,
                       BoraParticlesDev src, const uint32_t* idx, BoraParticlesDev dst, float* adj, float dt,

@@ -480,7 +480,8 @@ int build_hierarchy( bora_flip_sim* s )
 int stage_build_system( bora_flip_sim* s )
 {
     KTimer t( s, BORA_KERNEL_RHS, s->ntiles > 0 ? 1 : 0 );
-    bora_launch_rhs( s->g, s->ntiles, s->tiles(), s->cells(), s->st );
+    BORA_TRY( cudaMemsetAsync( P<uint32_t>( s->counters ) + 6, 0, 4, s->st ) );
+    bora_launch_rhs( s->g, s->ntiles, s->tiles(), s->cells(), P<uint32_t>( s->counters ) + 6, s->st );
     if( s->ntiles <= 0 ) return check_launch( s );
     if( s->prm.solver == BORA_SOLVER_MIXED )
     {
@@ -624,8 +625,9 @@ int stage_solve( bora_flip_sim* s )
     }
     { KTimer t( s, BORA_KERNEL_REFINE, 1 ); bora_launch_write_pressure( s->ntiles, code, sv.x, P<float>( s->pres ), st ); }
     BORA_TRYS( check_launch( s ) );
-    BORA_TRYS( read_counters( s, 5, 1 ) );
+    BORA_TRYS( read_counters( s, 5, 2 ) );
     if( s->h_cnt[5] != 0 ) return BORA_ERR_INTERNAL;
+    s->stats.fluid_cells = (int32_t)s->h_cnt[6];
     s->stats.solver_iterations = total_it;
     s->stats.refinements = passes;
     s->stats.residual_rel = bnorm > 0.0 ? rnorm / bnorm : 0.0;

@@ -195,7 +195,20 @@ __device__ inline bool advance_particle( const BoraGridDev& g, const Sampler& sm
         if( pz > lz - band ) w = fminf( w, bora_clampf( ( lz - pz ) / band, 0.f, 1.f ) );
         vx *= w; vy *= w; vz *= w;
     }
-    const bool hasCols = g.cols.count > 0;
+    // Collider work only where a collider can be met this step: the substep positions stay
+    // within |v| dt of the start (the box clamp only shortens moves of particles that start
+    // inside the grid), a sampled collider value is a lerp of box distances at cell centres
+    // within sqrt(3) cells, and a box distance changes by at most the distance moved. So a
+    // particle whose start is farther than 2 |v| dt + 2 cells from every box sees positive
+    // collider values all step long. (RK2 moves with the grid velocity: no cull.)
+    bool hasCols = g.cols.count > 0;
+    if( hasCols && g.advection != BORA_ADVECT_RK2 && inside_grid( g, px, py, pz ) )
+    {
+        const float reach = 2.f * sqrtf( vx * vx + vy * vy + vz * vz ) * dt + 2.f;
+        hasCols = false;
+        for( int n = 0; n < g.cols.count; ++n )
+            if( !( bora_box_sdf( g.cols.box[n], px, py, pz ) > reach ) ) hasCols = true;
+    }
     if( hasCols )
     {
         const float3 p = col_carry( &g, make_float3( px, py, pz ), dt );

@@ -52,7 +52,7 @@ __device__ inline float absr( float x ) { return x < 0.f ? -x : x; }  // MathUti
 
 // ---------------------------------------------------------------------------------
 // Right-hand side and stencil code (FluidProjection.cu:203-266).
-__global__ void __launch_bounds__( 512 ) k_rhs( BoraGridDev g, BoraTilesDev t, BoraCellsDev c )
+__global__ void __launch_bounds__( 512 ) k_rhs( BoraGridDev g, BoraTilesDev t, BoraCellsDev c, uint32_t* nfluid )
 {
     using HL = Halo<1>;
     __shared__ int32_t nb[27];
@@ -75,7 +75,10 @@ __global__ void __launch_bounds__( 512 ) k_rhs( BoraGridDev g, BoraTilesDev t, B
     const int i = ti * 8 + li, j = tj * 8 + lj, k = tk * 8 + lk;
     const size_t cell = (size_t)s * BORA_TILE_CELLS + l;
     const int h = HL::at( li + 1, lj + 1, lk + 1 );
-    if( sf[h] != BORA_FLUID )
+    const bool fluid = sf[h] == BORA_FLUID;
+    const unsigned fl = __ballot_sync( 0xffffffffu, fluid );  // unknowns of the system, counted per warp
+    if( ( threadIdx.x & 31 ) == 0 && fl ) atomicAdd( nfluid, (uint32_t)__popc( fl ) );
+    if( !fluid )
     {
         c.b[cell] = 0.f;
         c.code[cell] = 0;
@@ -677,9 +680,9 @@ int grid_for( size_t n, int threads )
 
 }  // namespace
 
-void bora_launch_rhs( const BoraGridDev& g, int ntiles, BoraTilesDev t, BoraCellsDev c, cudaStream_t st )
+void bora_launch_rhs( const BoraGridDev& g, int ntiles, BoraTilesDev t, BoraCellsDev c, uint32_t* nfluid, cudaStream_t st )
 {
-    if( ntiles > 0 ) k_rhs<<<ntiles, 512, 0, st>>>( g, t, c );
+    if( ntiles > 0 ) k_rhs<<<ntiles, 512, 0, st>>>( g, t, c, nfluid );
 }
 
 void bora_launch_vel_update( const BoraGridDev& g, int ntiles, BoraTilesDev t, BoraCellsDev c, cudaStream_t st )
