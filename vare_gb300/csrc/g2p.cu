@@ -269,7 +269,7 @@ struct StagedSampler
 // One CTA per tile: stage the tile's grid values, then advance the particles of the
 // tile's dual cells (a contiguous range of the sorted order). The CTA after the last tile
 // advances the sort's outside bin through the tile table.
-__global__ void __launch_bounds__( kG2PThreads ) k_g2p( const __grid_constant__ BoraGridDev g, BoraTilesDev t, int ntiles,
+__global__ void __launch_bounds__( kG2PThreads, 4 ) k_g2p( const __grid_constant__ BoraGridDev g, BoraTilesDev t, int ntiles,
                                                        uint32_t nsorted, const uint32_t* __restrict__ start, BoraCellsDev c,
                                                        BoraParticlesDev src, const uint32_t* __restrict__ idx,
                                                        BoraParticlesDev dst, float* __restrict__ adj, float dt,
