@@ -127,6 +127,29 @@ class FLIPMethod
         pts.id.push_back( -1 );
     }
 
+    // FLIPMethod::fillWaterTank (FLIPMethod.cu:407-478): append the tank's particles (world
+    // space, zero velocity) below params.wallLevel to the host store.
+    void fillWaterTank( Particles& pts )
+    {
+        requireInit();
+        const bora_flip_params p = toC();
+        check( bora_flip_set_params( _h, &p ), "bora_flip_set_params" );
+        const size_t n = pts.size();
+        if( pts.velocity.size() != 3 * n ) pts.velocity.resize( 3 * n, 0.f );
+        check( bora_flip_set_particles( _h, pts.position.data(), pts.velocity.data(), n, BORA_SPACE_WORLD ),
+               "bora_flip_set_particles" );
+        check( bora_flip_fill_water_tank( _h, nullptr ), "bora_flip_fill_water_tank" );
+        size_t m = 0;
+        check( bora_flip_num_particles( _h, &m ), "bora_flip_num_particles" );
+        pts.position.resize( 3 * m );
+        pts.velocity.resize( 3 * m );
+        pts.adjacency.resize( m );
+        pts.id.resize( m );
+        check( bora_flip_get_particles( _h, pts.position.data(), pts.velocity.data(), pts.adjacency.data(),
+                                        pts.id.data(), m, &m, BORA_SPACE_WORLD ),
+               "bora_flip_get_particles" );
+    }
+
     // CollisionSource replacement: analytic boxes (lo xyz, hi xyz, velocity xyz; voxel units).
     void setColliders( const std::vector<float>& boxes, float band = 3.f )
     {

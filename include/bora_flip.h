@@ -156,6 +156,12 @@ int bora_flip_add_particles( bora_flip_handle h, const float* pos, const float* 
 /* Replace all particles (ids restart at 0). */
 int bora_flip_set_particles( bora_flip_handle h, const float* pos, const float* vel, size_t n, int space );
 int bora_flip_clear_particles( bora_flip_handle h );
+/* FLIPMethod::fillWaterTank (FLIPMethod.cu:407-478): append the water tank's particles
+ * below the wall level (params.wall_level) with zero velocity, in the reference's order and
+ * at its positions; params.pts_per_cell extra particles per cell fill the 4-cell band under
+ * the wall. *added (may be NULL) receives the count. With params.enable_water_tank the tile
+ * rows below the wall stay active every step (SparseFrame.cu:119-129). */
+int bora_flip_fill_water_tank( bora_flip_handle h, size_t* added );
 
 /* CollisionSource (base/header/CollisionSource.h): up to 8 analytic boxes, 9 floats each
  * (lo xyz, hi xyz, velocity xyz) in voxel space; samples are clamped to +-band. */

@@ -113,6 +113,8 @@ def _oracle_lib() -> ctypes.CDLL:
         lib.ora_residual_max.restype = ctypes.c_double
         lib.ora_last_rel.argtypes = [_vp]
         lib.ora_last_rel.restype = ctypes.c_double
+        lib.ora_fill_water_tank.argtypes = [_vp, ctypes.c_int]
+        lib.ora_fill_water_tank.restype = ctypes.c_size_t
         lib._typed = True
     return lib
 
@@ -188,7 +190,8 @@ class Oracle(_SimBase):
     _p = "ora_"
 
     def __init__(self, scene, block: int = 8, compat: bool = False, solver: str = "fp64",
-                 tol: float = 1e-12, max_iter: int = 100000, threads: int | None = None, advection: int = 0):
+                 tol: float = 1e-12, max_iter: int = 100000, threads: int | None = None, advection: int = 0,
+                 tank: bool = False, damping_band: float = 0.0):
         self.lib = _oracle_lib()
         if threads is not None:
             self.lib.ora_set_threads(int(threads))
@@ -205,8 +208,8 @@ class Oracle(_SimBase):
         c.wall_level = scene.wall_level
         c.maxsubsteps = 1
         c.col_vel_scale = 1.0
-        c.enable_tank = 0
-        c.damping_band = 0.0
+        c.enable_tank = 1 if tank else 0
+        c.damping_band = damping_band
         c.voxel_size = scene.voxel_size
         c.advection = advection
         self.cfg = c
@@ -225,6 +228,10 @@ class Oracle(_SimBase):
         arr = np.ascontiguousarray(np.array([np.concatenate([lo, hi, v]) for lo, hi, v in boxes],
                                             np.float32).reshape(-1))
         self.lib.ora_set_colliders(self.h, len(boxes), _ptr(arr), band)
+
+    def fill_water_tank(self, per_cell: int = 8) -> int:
+        """FLIPMethod::fillWaterTank restated (particles appended in voxel space)."""
+        return int(self.lib.ora_fill_water_tank(self.h, per_cell))
 
     def set_particles(self, pos, vel, ids=None) -> None:
         pos = np.ascontiguousarray(pos, np.float32)
@@ -313,6 +320,8 @@ def _ref_lib(path: str) -> ctypes.CDLL:
         lib.ref_num_unknowns.argtypes = [_vp]
         lib.ref_num_unknowns.restype = ctypes.c_size_t
         lib.ref_get_system.argtypes = [_vp, _vp, _vp, _vp]
+        lib.ref_fill_water_tank.argtypes = [_vp]
+        lib.ref_fill_water_tank.restype = ctypes.c_size_t
         if hasattr(lib, "ref_cg64_set"):
             lib.ref_cg64_set.argtypes = [ctypes.c_double, ctypes.c_int]
             lib.ref_cg64_last_iters.restype = ctypes.c_int
@@ -329,7 +338,8 @@ class RefSim(_SimBase):
 
     _p = "ref_"
 
-    def __init__(self, scene, converged: bool = False, tol: float = 1e-12, proj_iteration: int = 200):
+    def __init__(self, scene, converged: bool = False, tol: float = 1e-12, proj_iteration: int = 200,
+                 tank: bool = False, damping_band: float = 0.0):
         self.lib = _ref_lib(REF64_SO if converged else REF_SO)
         if converged:
             self.lib.ref_cg64_set(tol, 100000)
@@ -338,9 +348,9 @@ class RefSim(_SimBase):
         p.maxsubsteps = 1
         p.dt = scene.dt
         p.wallLevel = scene.wall_level
-        p.enableWaterTank = 0
+        p.enableWaterTank = 1 if tank else 0
         p.enableCurl = 0
-        p.dampingBand = 0.0
+        p.dampingBand = damping_band
         p.voxelSize = scene.voxel_size
         p.colVelScale = 1.0
         p.ptsPerCell = 8
@@ -364,6 +374,10 @@ class RefSim(_SimBase):
         if h:
             self.lib.ref_destroy(h)
             self.h = None
+
+    def fill_water_tank(self) -> int:
+        """The reference's own FLIPMethod::fillWaterTank (new particles brought to voxel space)."""
+        return int(self.lib.ref_fill_water_tank(self.h))
 
     @property
     def num_particles(self) -> int:

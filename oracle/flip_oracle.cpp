@@ -13,6 +13,7 @@
 // multiply-add changes the rounding that this file restates.
 #include <cmath>
 #include <cstdint>
+#include <climits>
 #include <cstring>
 #include <cstdlib>
 #include <vector>
@@ -871,6 +872,71 @@ void ora_set_particles( void* h, const float* pos, const float* vel, const int32
         o->vel[i] = V3{ vel[3 * i], vel[3 * i + 1], vel[3 * i + 2] };
         o->pid[i] = id ? id[i] : (int32_t)i;
     }
+}
+
+// Random.h:30-38, Rand( seed, 0, 1 ): an integer hash of the seed scaled to [0, 1].
+static float bora_rand01( unsigned int seed )
+{
+    unsigned int i = ( seed ^ 12345391u ) * 2654435769u;
+    i ^= ( i << 6 ) ^ ( i >> 26 );
+    i *= 2654435769u;
+    i += ( i << 5 ) ^ ( i >> 12 );
+    return ( 1.0f - 0.0f ) * (float)i / (float)( UINT_MAX ) + 0.0f;
+}
+
+// FLIPMethod::fillWaterTank (base/source/FLIPMethod.cu:407-478): per cell below the wall
+// level two jittered particles, the cell centre, and `per_cell` more in the 4-cell band
+// under the wall, appended in (k, j, i) order; their world positions (Grid::worldPoint)
+// come back to voxel space as particlesToVoxel does (FLIPMethod.cu:499-514). Returns the
+// number of particles added (ids continue after the largest id).
+size_t ora_fill_water_tank( void* h, int per_cell )
+{
+    Oracle* o = (Oracle*)h;
+    const float wall = o->voxelWall;
+    if( wall <= 0.f ) return 0;
+    int32_t next = 0;
+    for( int32_t q : o->pid ) next = q + 1 > next ? q + 1 : next;
+    const size_t n0 = o->pos.size();
+    const int nx = o->nx, ny = o->ny, nz = o->nz;
+    const int hh = clampi( (int)wall + 1, 0, ny );
+    auto add = [&]( V3 p ) {
+        V3 w{ p.x * o->scale[0] + o->translate[0], p.y * o->scale[1] + o->translate[1], p.z * o->scale[2] + o->translate[2] };
+        V3 v{ ( w.x - o->translate[0] ) / o->scale[0], ( w.y - o->translate[1] ) / o->scale[1], ( w.z - o->translate[2] ) / o->scale[2] };
+        o->pos.push_back( v );
+        o->vel.push_back( V3{ 0.f, 0.f, 0.f } );
+        o->adj.push_back( 0.f );
+        o->pid.push_back( next++ );
+    };
+    for( int k = 0; k < nz; ++k )
+        for( int j = 0; j < hh; ++j )
+            for( int i = 0; i < nx; ++i )
+            {
+                const unsigned ui = (unsigned)i, uj = (unsigned)j, uk = (unsigned)k;
+                const V3 cen{ i + .5f, j + .5f, k + .5f };
+                const float band = wall - cen.y;
+                const float dx0 = bora_rand01( ui * 45651u + uk * 75561u + uj * 65551u );
+                const float dy0 = bora_rand01( ui * 51221u + uk * 99331u + uj * 11221u );
+                const float dz0 = bora_rand01( ui * 81221u + uk * 45331u + uj * 66551u );
+                const float dx1 = bora_rand01( ui * 53454u + uk * 12234u + uj * 23853u );
+                const float dy1 = bora_rand01( ui * 76335u + uk * 94762u + uj * 93654u );
+                const float dz1 = bora_rand01( ui * 98547u + uk * 23443u + uj * 53218u );
+                const V3 p0{ ( cen.x - 0.5f ) + dx0, ( cen.y - 0.5f ) + dy0, ( cen.z - 0.5f ) + dz0 };
+                const V3 p1{ ( cen.x - 0.5f ) + dx1, ( cen.y - 0.5f ) + dy1, ( cen.z - 0.5f ) + dz1 };
+                if( p0.y <= wall ) add( p0 );
+                if( p1.y <= wall ) add( p1 );
+                if( cen.y <= wall ) add( cen );
+                if( band > 0.f && band < 4.f )
+                    for( int n = 0; n < per_cell; ++n )
+                    {
+                        const unsigned un = (unsigned)n;
+                        const float dx = bora_rand01( ui * 45651u + uk * 75561u + uj * 65551u + un * 44222u );
+                        const float dy = bora_rand01( ui * 51221u + uk * 99331u + uj * 11221u + un * 59374u );
+                        const float dz = bora_rand01( ui * 81221u + uk * 45331u + uj * 66551u + un * 12333u );
+                        const V3 pp{ ( cen.x - 0.5f ) + dx, ( cen.y - 0.5f ) + dy, ( cen.z - 0.5f ) + dz };
+                        if( pp.y <= wall ) add( pp );
+                    }
+            }
+    return o->pos.size() - n0;
 }
 
 size_t ora_num_particles( void* h ) { return ( (Oracle*)h )->pos.size(); }

@@ -126,6 +126,22 @@ void ref_add_particles( void* h, const float* pos, const float* vel, size_t n )
                              Bora::Vec3f( vel[3 * i], vel[3 * i + 1], vel[3 * i + 2] ) );
 }
 
+// FLIPMethod::fillWaterTank (FLIPMethod.cu:407-478) on the reference's own code; the new
+// particles are brought to voxel space as particlesToVoxel would (FLIPMethod.cu:499-514).
+size_t ref_fill_water_tank( void* h )
+{
+    RefSim* s = (RefSim*)h;
+    const size_t n0 = s->pts.position.size();
+    s->flip.fillWaterTank( s->pts );
+    const size_t n1 = s->pts.position.size();
+    for( size_t i = n0; i < n1; ++i )
+    {
+        s->pts.position[i] = s->flip._grid.voxelPoint( s->pts.position[i] );
+        s->pts.velocity[i] = s->flip._grid.voxelVector( s->pts.velocity[i] );
+    }
+    return n1 - n0;
+}
+
 void ref_step( void* h, float dt )
 {
     RefSim* s = (RefSim*)h;

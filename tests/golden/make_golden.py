@@ -15,6 +15,9 @@ Fixtures:
                           3 steps: particle arrays after steps 1 and 3.
   ref_dam64.npz           64^3 dam break (505,856 particles), reference CG rule,
                           2 steps: SHA-256 of the particle arrays and summaries.
+  ref_tank24.npz          24^3 dam break + sphere with the water tank on (wall level 0.25,
+                          damping band 0.1): FLIPMethod::fillWaterTank's particles, then 3
+                          steps with the reference CG rule: per-step SHA-256 and counts.
 
 Usage: OMP_NUM_THREADS=1 python tests/golden/make_golden.py
 """
@@ -127,9 +130,35 @@ def dam64():
     print("dam64", counts, ke)
 
 
+def tank_scene():
+    sc = scenes.small(24, seed=11)
+    sc.wall_level = 0.25  # world units: the tank is 6 cells deep
+    return sc
+
+
+def tank24():
+    sc = tank_scene()
+    ref = B.RefSim(sc, tank=True, damping_band=0.1)
+    added = ref.fill_water_tank()
+    pos0, vel0, _ = ref.particles()
+    ids = np.arange(ref.num_particles, dtype=np.int64)
+    hashes, counts, ntiles = [], [], []
+    for s in range(3):
+        ref.step(sc.dt)
+        pos, vel, adj = ref.particles()
+        ids = remove_order(ids, ref.removed())
+        hashes.append(sha(pos, vel, adj))
+        counts.append(ref.num_particles)
+        ntiles.append(ref.frame_info()["ntiles"])
+    np.savez_compressed(os.path.join(HERE, "ref_tank24.npz"), added=added, pos0=pos0, vel0=vel0,
+                        hashes=np.array(hashes), counts=np.array(counts), ntiles=np.array(ntiles), ids=ids,
+                        wall_level=sc.wall_level, damping_band=0.1)
+    print("tank24", added, counts, ntiles)
+
+
 if __name__ == "__main__":
     if not B.reference_available():
         B.build(ref=True)
-    small20()
-    small24_cg64()
-    dam64()
+    which = sys.argv[1:] or ["small20", "small24_cg64", "dam64", "tank24"]
+    for name in which:
+        globals()[name]()

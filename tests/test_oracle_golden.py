@@ -159,3 +159,25 @@ def test_reference_build_matches_oracle_live():
     po, vo, ao, _ = ora.particles()
     np.testing.assert_array_equal(pr, po)
     np.testing.assert_array_equal(vr, vo)
+
+
+def test_compat_tank24_bit_exact(oracle_lib):
+    """Water tank (FLIPMethod::fillWaterTank, the tank's always-active tile rows, damping
+    band): the restatement reproduces the reference's own fill and three steps bit for bit."""
+    B = oracle_lib
+    g = np.load(os.path.join(GOLDEN, "ref_tank24.npz"))
+    sc = scenes.small(24, seed=11)
+    sc.wall_level = float(g["wall_level"])
+    ora = B.Oracle(sc, block=4, compat=True, solver="reference", max_iter=200, threads=1, tank=True,
+                   damping_band=float(g["damping_band"]))
+    assert ora.fill_water_tank(8) == int(g["added"])
+    pos0, vel0, _, _ = ora.particles()
+    np.testing.assert_array_equal(pos0, g["pos0"])
+    np.testing.assert_array_equal(vel0, g["vel0"])
+    for s in range(len(g["hashes"])):
+        ora.step(sc.dt)
+        pos, vel, adj, ids = ora.particles()
+        assert ora.num_particles == g["counts"][s], f"particle count, step {s}"
+        assert ora.frame_info()["ntiles"] == g["ntiles"][s], f"active tiles, step {s}"
+        assert sha(pos, vel, adj) == g["hashes"][s], f"particle arrays differ at step {s}"
+    np.testing.assert_array_equal(ids, g["ids"])

@@ -93,6 +93,10 @@ struct BoraReduceDev
 // ---- launchers -----------------------------------------------------------------------
 void bora_launch_bin( const BoraGridDev& g, BoraParticlesDev p, size_t n, uint32_t* vkey, uint8_t* tile_flag, cudaStream_t st );
 void bora_launch_activate( const BoraGridDev& g, const uint8_t* tile_flag, uint32_t* act, cudaStream_t st );
+// FLIPMethod::fillWaterTank: count (write = false) or write the tank's particles.
+void bora_launch_tank( const BoraGridDev& g, int hh, int per_cell, float3 tr, float3 sc, uint32_t* count,
+                       const uint32_t* offset, BoraParticlesDev p, size_t base, int32_t first_id, bool write,
+                       cudaStream_t st );
 void bora_launch_tile_assign( const BoraGridDev& g, const uint32_t* act, const uint32_t* excl, int32_t* slot_of,
                               int32_t* tile_of, cudaStream_t st );
 void bora_launch_tile_nbrs( const BoraGridDev& g, int ntiles, const int32_t* slot_of, const int32_t* tile_of,

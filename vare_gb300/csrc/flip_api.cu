@@ -838,6 +838,46 @@ int bora_flip_add_particles( bora_flip_handle s, const float* pos, const float* 
     return add_particles( s, pos, vel, n, space );
 }
 
+int bora_flip_fill_water_tank( bora_flip_handle s, size_t* added )
+{
+    if( !s ) return BORA_ERR_INVALID_ARG;
+    if( added ) *added = 0;
+    const float wall = s->g.voxel_wall;
+    if( wall <= 0.f ) return BORA_OK;  // FLIPMethod.cu:409
+    const int hh = std::max( 0, std::min( (int)wall + 1, s->g.ny ) );
+    const size_t ncell = (size_t)s->g.nx * hh * s->g.nz;
+    if( ncell == 0 ) return BORA_OK;
+    cudaStream_t st = s->st;
+    BORA_TRY( grow( s->stage_in, ( 2 * ncell + 2 ) * 4, false, st ) );
+    uint32_t* count = P<uint32_t>( s->stage_in );
+    uint32_t* offset = count + ncell + 1;
+    BORA_TRYS( ensure_scan_scratch( s, ncell + 1 ) );
+    const float3 tr = make_float3( s->translate[0], s->translate[1], s->translate[2] );
+    const float3 sc = make_float3( s->scale[0], s->scale[1], s->scale[2] );
+    const int per_cell = std::max( 0, s->prm.pts_per_cell );
+    s->stats.kernel_launches += 2;
+    bora_launch_tank( s->g, hh, per_cell, tr, sc, count, nullptr, s->parts( s->cur ), 0, 0, false, st );
+    bora_device_scan( count, offset, ncell, P<uint32_t>( s->scan_scratch ), P<uint32_t>( s->counters ) + 7, st );
+    BORA_TRYS( check_launch( s ) );
+    BORA_TRYS( read_counters( s, 7, 1 ) );
+    const size_t n = s->h_cnt[7];
+    if( n == 0 ) return BORA_OK;
+    if( s->np + n > (size_t)0x7FFFFFF0 ) return BORA_ERR_CAPACITY;
+    BORA_TRYS( ensure_particles( s, s->np + n ) );
+    s->stats.kernel_launches += 1;
+    bora_launch_tank( s->g, hh, per_cell, tr, sc, count, offset, s->parts( s->cur ), s->np, s->next_id, true, st );
+    BORA_TRY( cudaMemsetAsync( P<float>( s->adj ) + s->np, 0, n * 4, st ) );
+    BORA_TRYS( check_launch( s ) );
+    BORA_TRY( cudaStreamSynchronize( st ) );
+    s->np += n;
+    s->nlive += n;
+    s->next_id += (int32_t)n;
+    s->sorted = false;
+    s->stats.num_particles = s->nlive;
+    if( added ) *added = n;
+    return BORA_OK;
+}
+
 int bora_flip_clear_particles( bora_flip_handle s )
 {
     if( !s ) return BORA_ERR_INVALID_ARG;

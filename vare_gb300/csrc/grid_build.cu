@@ -50,13 +50,13 @@ __global__ void k_bin( BoraGridDev g, BoraParticlesDev p, size_t n, uint32_t* __
     }
 }
 
-__global__ void k_activate( BoraGridDev g, const uint8_t* __restrict__ tile_flag, uint32_t* __restrict__ act )
+__global__ void k_activate( BoraGridDev g, const uint8_t* __restrict__ tile_flag, uint32_t* __restrict__ act, int tank_rows )
 {
     const size_t ntv = (size_t)g.tx * g.ty * g.tz;
     for( size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < ntv; t += (size_t)gridDim.x * blockDim.x )
     {
         const int ti = (int)( t % g.tx ), tj = (int)( ( t / g.tx ) % g.ty ), tk = (int)( t / ( (size_t)g.tx * g.ty ) );
-        uint32_t a = 0;
+        uint32_t a = tj < tank_rows ? 1u : 0u;  // the water tank keeps its rows active (SparseFrame.cu:119-129)
         for( int dk = -1; dk <= 1 && !a; ++dk )
         {
             const int k = tk + dk;
@@ -209,7 +209,77 @@ __global__ void k_to_soa( size_t n, const float* __restrict__ pos, const float* 
     }
 }
 
+// Random.h:30-38, Rand( seed, 0, 1 ): an integer hash of the seed scaled to [0, 1].
+__device__ inline float bora_rand01( unsigned int seed )
+{
+    unsigned int i = ( seed ^ 12345391u ) * 2654435769u;
+    i ^= ( i << 6 ) ^ ( i >> 26 );
+    i *= 2654435769u;
+    i += ( i << 5 ) ^ ( i >> 12 );
+    return ( 1.0f - 0.0f ) * (float)i / 4294967296.0f + 0.0f;  // (float)UINT_MAX rounds to 2^32
+}
+
+// FLIPMethod::fillWaterTank (FLIPMethod.cu:407-478), one thread per cell below the wall
+// level: two jittered particles, the cell centre, and `per_cell` more in the 4-cell band
+// under the wall. COUNT pass: particles per cell; write pass: each cell's particles at its
+// prefix offset, so the order is the reference's (k, j, i) loop order. Positions take the
+// reference's round trip through world space (Grid::worldPoint, then particlesToVoxel).
+template <bool WRITE>
+__global__ void k_tank( BoraGridDev g, int hh, float wall, int per_cell, float3 tr, float3 sc, uint32_t* count,
+                        const uint32_t* __restrict__ offset, BoraParticlesDev p, size_t base, int32_t first_id )
+{
+    const size_t ncell = (size_t)g.nx * hh * g.nz;
+    for( size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < ncell; c += (size_t)gridDim.x * blockDim.x )
+    {
+        const int i = (int)( c % g.nx ), j = (int)( ( c / g.nx ) % hh ), k = (int)( c / ( (size_t)g.nx * hh ) );
+        const unsigned ui = (unsigned)i, uj = (unsigned)j, uk = (unsigned)k;
+        const float cx = i + .5f, cy = j + .5f, cz = k + .5f;
+        uint32_t m = 0;
+        const size_t o = WRITE ? base + offset[c] : 0;
+        auto emit = [&]( float x, float y, float z ) {
+            if( !( y <= wall ) ) return;
+            if( WRITE )
+            {
+                const float wx = x * sc.x + tr.x, wy = y * sc.y + tr.y, wz = z * sc.z + tr.z;
+                p.px[o + m] = ( wx - tr.x ) / sc.x;
+                p.py[o + m] = ( wy - tr.y ) / sc.y;
+                p.pz[o + m] = ( wz - tr.z ) / sc.z;
+                p.vx[o + m] = 0.f; p.vy[o + m] = 0.f; p.vz[o + m] = 0.f;
+                p.id[o + m] = first_id + (int32_t)( offset[c] + m );
+            }
+            ++m;
+        };
+        emit( ( cx - 0.5f ) + bora_rand01( ui * 45651u + uk * 75561u + uj * 65551u ),
+              ( cy - 0.5f ) + bora_rand01( ui * 51221u + uk * 99331u + uj * 11221u ),
+              ( cz - 0.5f ) + bora_rand01( ui * 81221u + uk * 45331u + uj * 66551u ) );
+        emit( ( cx - 0.5f ) + bora_rand01( ui * 53454u + uk * 12234u + uj * 23853u ),
+              ( cy - 0.5f ) + bora_rand01( ui * 76335u + uk * 94762u + uj * 93654u ),
+              ( cz - 0.5f ) + bora_rand01( ui * 98547u + uk * 23443u + uj * 53218u ) );
+        emit( cx, cy, cz );
+        const float band = wall - cy;
+        if( band > 0.f && band < 4.f )
+            for( int n = 0; n < per_cell; ++n )
+            {
+                const unsigned un = (unsigned)n;
+                emit( ( cx - 0.5f ) + bora_rand01( ui * 45651u + uk * 75561u + uj * 65551u + un * 44222u ),
+                      ( cy - 0.5f ) + bora_rand01( ui * 51221u + uk * 99331u + uj * 11221u + un * 59374u ),
+                      ( cz - 0.5f ) + bora_rand01( ui * 81221u + uk * 45331u + uj * 66551u + un * 12333u ) );
+            }
+        if( !WRITE ) count[c] = m;
+    }
+}
+
 }  // namespace
+
+void bora_launch_tank( const BoraGridDev& g, int hh, int per_cell, float3 tr, float3 sc, uint32_t* count,
+                       const uint32_t* offset, BoraParticlesDev p, size_t base, int32_t first_id, bool write,
+                       cudaStream_t st )
+{
+    const size_t ncell = (size_t)g.nx * hh * g.nz;
+    if( ncell == 0 ) return;
+    if( write ) k_tank<true><<<grid_for( ncell ), kThreads, 0, st>>>( g, hh, g.voxel_wall, per_cell, tr, sc, count, offset, p, base, first_id );
+    else k_tank<false><<<grid_for( ncell ), kThreads, 0, st>>>( g, hh, g.voxel_wall, per_cell, tr, sc, count, offset, p, base, first_id );
+}
 
 void bora_launch_bin( const BoraGridDev& g, BoraParticlesDev p, size_t n, uint32_t* vkey, uint8_t* tile_flag, cudaStream_t st )
 {
@@ -220,7 +290,14 @@ void bora_launch_bin( const BoraGridDev& g, BoraParticlesDev p, size_t n, uint32
 void bora_launch_activate( const BoraGridDev& g, const uint8_t* tile_flag, uint32_t* act, cudaStream_t st )
 {
     const size_t ntv = (size_t)g.tx * g.ty * g.tz;
-    k_activate<<<grid_for( ntv ), kThreads, 0, st>>>( g, tile_flag, act );
+    // tile rows wholly below the wall level stay active with the tank on (build tile edge 8)
+    int tank_rows = 0;
+    if( g.enable_tank )
+    {
+        tank_rows = (int)g.voxel_wall / BORA_TILE;
+        tank_rows = tank_rows < 0 ? 0 : ( tank_rows > g.ty ? g.ty : tank_rows );
+    }
+    k_activate<<<grid_for( ntv ), kThreads, 0, st>>>( g, tile_flag, act, tank_rows );
 }
 
 void bora_launch_tile_assign( const BoraGridDev& g, const uint32_t* act, const uint32_t* excl, int32_t* slot_of,

@@ -86,6 +86,7 @@ _SIGS = {
     "bora_flip_add_particles": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_size_t, ctypes.c_int]),
     "bora_flip_set_particles": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_size_t, ctypes.c_int]),
     "bora_flip_clear_particles": (ctypes.c_int, [_vp]),
+    "bora_flip_fill_water_tank": (ctypes.c_int, [_vp, _vp]),
     "bora_flip_set_colliders": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_float]),
     "bora_flip_step": (ctypes.c_int, [_vp, ctypes.c_float]),
     "bora_flip_frame": (ctypes.c_int, [_vp]),
@@ -232,6 +233,12 @@ class FlipSim:
         pos = np.ascontiguousarray(pos, np.float32)
         vel = None if vel is None else np.ascontiguousarray(vel, np.float32)
         _check(self.lib.bora_flip_set_particles(self.h, _ptr(pos), _ptr(vel), pos.shape[0], space), "set_particles")
+
+    def fill_water_tank(self) -> int:
+        """FLIPMethod::fillWaterTank: append the tank's particles; returns how many."""
+        n = ctypes.c_size_t()
+        _check(self.lib.bora_flip_fill_water_tank(self.h, ctypes.byref(n)), "fill_water_tank")
+        return n.value
 
     def set_particles_ptr(self, pos_ptr: int, vel_ptr: int, n: int, space: int = SPACE_VOXEL) -> None:
         """Replace particles from raw host pointers (e.g. pinned torch buffers)."""
