@@ -166,6 +166,12 @@ int bora_flip_fill_water_tank( bora_flip_handle h, size_t* added );
 /* CollisionSource (base/header/CollisionSource.h): up to 8 analytic boxes, 9 floats each
  * (lo xyz, hi xyz, velocity xyz) in voxel space; samples are clamped to +-band. */
 int bora_flip_set_colliders( bora_flip_handle h, const float* boxes, int n, float band );
+/* CollisionSource::update (CollisionSource.h:66-126) from raw buffers instead of OpenVDB
+ * grids: the collider's signed distance (voxel units, negative inside) and velocity (voxel
+ * units per second; NULL = at rest) at the cell centres of the frame grid (bora_frame_info
+ * nx, ny, nz; x fastest), ncells = nx*ny*nz. Normals are central differences of the
+ * distances, as for boxes. Replaces any boxes; phi = NULL removes the collider. */
+int bora_flip_set_collider_field( bora_flip_handle h, const float* phi, const float* vel, size_t ncells );
 
 /* FLIPMethod::advanceOneStep (FLIPMethod.cu:208-298) in voxel space. Returns
  * BORA_WARN_NOT_CONVERGED when the pressure solve stopped on its iteration caps. */

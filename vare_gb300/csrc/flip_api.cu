@@ -102,6 +102,7 @@ struct bora_flip_sim
     DevBuf mass, surf, pres, vx, vy, vz, cx, cy, cz, flag, code, rhs;
     DevBuf sx, se, sr, sd0, sd1, sq, sz, sminv;
     DevBuf cell_count, cell_start;
+    DevBuf col_phi, col_vel;  // collider signed distance / velocity per frame cell
 
     // multigrid hierarchy (mixed solver): per level type, code, r, z0, z1
     static constexpr int kMaxLevels = 16;
@@ -702,7 +703,7 @@ void for_each_buffer( bora_flip_sim* s, F&& f )
                       &s->pres, &s->vx, &s->vy, &s->vz, &s->cx, &s->cy, &s->cz, &s->flag, &s->code, &s->rhs, &s->sx,
                       &s->se, &s->sr, &s->sd0, &s->sd1, &s->sq, &s->sz, &s->sminv, &s->cell_count, &s->cell_start,
                       &s->ring, &s->partials, &s->done, &s->adj, &s->vkey, &s->key, &s->idx, &s->scan_scratch,
-                      &s->counters, &s->stage_in, &s->stage_out, &s->live_flag };
+                      &s->counters, &s->stage_in, &s->stage_out, &s->live_flag, &s->col_phi, &s->col_vel };
     for( DevBuf* b : all ) f( *b );
     for( int q = 0; q < 2; ++q )
         for( int a = 0; a < 7; ++a ) f( s->pbuf[q][a] );
@@ -909,6 +910,32 @@ int bora_flip_set_colliders( bora_flip_handle s, const float* boxes, int n, floa
             c.box[q].hi[a] = boxes[9 * q + 3 + a];
             c.box[q].vel[a] = boxes[9 * q + 6 + a];
         }
+    return BORA_OK;
+}
+
+int bora_flip_set_collider_field( bora_flip_handle s, const float* phi, const float* vel, size_t ncells )
+{
+    if( !s ) return BORA_ERR_INVALID_ARG;
+    BoraColliderDev& c = s->g.cols;
+    if( !phi )
+    {
+        c.fphi = nullptr;
+        c.fvel = nullptr;
+        return BORA_OK;
+    }
+    const size_t n = (size_t)s->g.nx * s->g.ny * s->g.nz;
+    if( ncells != n ) return BORA_ERR_INVALID_ARG;
+    BORA_TRY( grow( s->col_phi, n * 4, false, s->st ) );
+    BORA_TRY( cudaMemcpyAsync( s->col_phi.p, phi, n * 4, cudaMemcpyHostToDevice, s->st ) );
+    if( vel )
+    {
+        BORA_TRY( grow( s->col_vel, n * 12, false, s->st ) );
+        BORA_TRY( cudaMemcpyAsync( s->col_vel.p, vel, n * 12, cudaMemcpyHostToDevice, s->st ) );
+    }
+    BORA_TRY( cudaStreamSynchronize( s->st ) );  // the caller may free its buffers on return
+    c.count = 0;  // replaces any boxes
+    c.fphi = P<float>( s->col_phi );
+    c.fvel = vel ? P<float>( s->col_vel ) : nullptr;
     return BORA_OK;
 }
 

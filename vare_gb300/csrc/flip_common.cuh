@@ -40,12 +40,19 @@ struct BoraBoxDev
     float lo[3], hi[3], vel[3];
 };
 
+// Colliders: analytic boxes sampled at cell centres, or (fphi != null) signed distances
+// and velocities given per cell of the frame grid (x fastest), as CollisionSource samples
+// its SDF and velocity grids at cell centres (CollisionSource.h:66-126).
 struct BoraColliderDev
 {
     int count;
     float band;
     BoraBoxDev box[BORA_MAX_COLLIDERS];
+    const float* fphi;  // [nx*ny*nz] voxel units, or null
+    const float* fvel;  // [3*nx*ny*nz] voxel units per second, or null (zero)
 };
+
+__host__ __device__ inline bool bora_col_active( const BoraColliderDev& s ) { return s.count > 0 || s.fphi != nullptr; }
 
 // Grid constants shared by every kernel of one simulation.
 struct BoraGridDev
@@ -103,8 +110,13 @@ __device__ inline float bora_box_sdf( const BoraBoxDev& b, float px, float py, f
     return outside + inside;
 }
 
-__device__ inline float bora_col_phi_cell( const BoraColliderDev& s, int i, int j, int k, int* arg )
+__device__ inline float bora_col_phi_cell( const BoraColliderDev& s, int nx, int ny, int i, int j, int k, int* arg )
 {
+    if( s.fphi )
+    {
+        if( arg ) *arg = 0;
+        return s.fphi[(size_t)i + (size_t)nx * ( (size_t)j + (size_t)ny * k )];
+    }
     const float px = (float)i + 0.5f, py = (float)j + 0.5f, pz = (float)k + 0.5f;
     float best = s.band;
     int a = -1;
@@ -126,13 +138,21 @@ __device__ inline void bora_col_sample( const BoraColliderDev& s, int nx, int ny
     int a;
     if( which == 0 )
     {
-        out[0] = bora_col_phi_cell( s, i, j, k, &a );
+        out[0] = bora_col_phi_cell( s, nx, ny, i, j, k, &a );
         out[1] = out[2] = 0.f;
+        return;
+    }
+    if( which == 2 && s.fphi )
+    {
+        const size_t c = (size_t)i + (size_t)nx * ( (size_t)j + (size_t)ny * k );
+        out[0] = s.fvel ? s.fvel[3 * c] : 0.f;
+        out[1] = s.fvel ? s.fvel[3 * c + 1] : 0.f;
+        out[2] = s.fvel ? s.fvel[3 * c + 2] : 0.f;
         return;
     }
     if( which == 2 )
     {
-        const float phi = bora_col_phi_cell( s, i, j, k, &a );
+        const float phi = bora_col_phi_cell( s, nx, ny, i, j, k, &a );
         if( a >= 0 && phi < s.band )
         {
             out[0] = s.box[a].vel[0]; out[1] = s.box[a].vel[1]; out[2] = s.box[a].vel[2];
@@ -146,9 +166,9 @@ __device__ inline void bora_col_sample( const BoraColliderDev& s, int nx, int ny
     const int i0 = i > 0 ? i - 1 : 0, i1 = i < nx - 1 ? i + 1 : nx - 1;
     const int j0 = j > 0 ? j - 1 : 0, j1 = j < ny - 1 ? j + 1 : ny - 1;
     const int k0 = k > 0 ? k - 1 : 0, k1 = k < nz - 1 ? k + 1 : nz - 1;
-    const float gx = ( bora_col_phi_cell( s, i1, j, k, 0 ) - bora_col_phi_cell( s, i0, j, k, 0 ) ) * 0.5f;
-    const float gy = ( bora_col_phi_cell( s, i, j1, k, 0 ) - bora_col_phi_cell( s, i, j0, k, 0 ) ) * 0.5f;
-    const float gz = ( bora_col_phi_cell( s, i, j, k1, 0 ) - bora_col_phi_cell( s, i, j, k0, 0 ) ) * 0.5f;
+    const float gx = ( bora_col_phi_cell( s, nx, ny, i1, j, k, 0 ) - bora_col_phi_cell( s, nx, ny, i0, j, k, 0 ) ) * 0.5f;
+    const float gy = ( bora_col_phi_cell( s, nx, ny, i, j1, k, 0 ) - bora_col_phi_cell( s, nx, ny, i, j0, k, 0 ) ) * 0.5f;
+    const float gz = ( bora_col_phi_cell( s, nx, ny, i, j, k1, 0 ) - bora_col_phi_cell( s, nx, ny, i, j, k0, 0 ) ) * 0.5f;
     const double d = 1.0f / sqrtf( gx * gx + gy * gy + gz * gz + 1e-30f );
     out[0] = (float)( gx * d );
     out[1] = (float)( gy * d );
@@ -188,7 +208,7 @@ __device__ inline void bora_col_lerp( const BoraColliderDev& s, int nx, int ny, 
 
 __device__ inline float bora_col_phi( const BoraGridDev& g, float px, float py, float pz )
 {
-    if( g.cols.count == 0 ) return 5.f;  // reference background without a collider (CollisionSource.h:56,130)
+    if( !bora_col_active( g.cols ) ) return 5.f;  // reference background without a collider (CollisionSource.h:56,130)
     float v[3];
     bora_col_lerp( g.cols, g.nx, g.ny, g.nz, px, py, pz, 0, v );
     return v[0];

@@ -201,8 +201,8 @@ __device__ inline bool advance_particle( const BoraGridDev& g, const Sampler& sm
     // within sqrt(3) cells, and a box distance changes by at most the distance moved. So a
     // particle whose start is farther than 2 |v| dt + 2 cells from every box sees positive
     // collider values all step long. (RK2 moves with the grid velocity: no cull.)
-    bool hasCols = g.cols.count > 0;
-    if( hasCols && g.advection != BORA_ADVECT_RK2 && inside_grid( g, px, py, pz ) )
+    bool hasCols = bora_col_active( g.cols );
+    if( hasCols && !g.cols.fphi && g.advection != BORA_ADVECT_RK2 && inside_grid( g, px, py, pz ) )
     {
         const float reach = 2.f * sqrtf( vx * vx + vy * vy + vz * vz ) * dt + 2.f;
         hasCols = false;

@@ -87,6 +87,7 @@ _SIGS = {
     "bora_flip_set_particles": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_size_t, ctypes.c_int]),
     "bora_flip_clear_particles": (ctypes.c_int, [_vp]),
     "bora_flip_fill_water_tank": (ctypes.c_int, [_vp, _vp]),
+    "bora_flip_set_collider_field": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_size_t]),
     "bora_flip_set_colliders": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_float]),
     "bora_flip_step": (ctypes.c_int, [_vp, ctypes.c_float]),
     "bora_flip_frame": (ctypes.c_int, [_vp]),
@@ -233,6 +234,15 @@ class FlipSim:
         pos = np.ascontiguousarray(pos, np.float32)
         vel = None if vel is None else np.ascontiguousarray(vel, np.float32)
         _check(self.lib.bora_flip_set_particles(self.h, _ptr(pos), _ptr(vel), pos.shape[0], space), "set_particles")
+
+    def set_collider_field(self, phi, vel=None) -> None:
+        """Collider signed distance (and velocity) per frame cell, voxel units, x fastest."""
+        if phi is None:
+            _check(self.lib.bora_flip_set_collider_field(self.h, None, None, 0), "set_collider_field")
+            return
+        phi = np.ascontiguousarray(phi, np.float32).reshape(-1)
+        vel = None if vel is None else np.ascontiguousarray(vel, np.float32).reshape(-1)
+        _check(self.lib.bora_flip_set_collider_field(self.h, _ptr(phi), _ptr(vel), phi.size), "set_collider_field")
 
     def fill_water_tank(self) -> int:
         """FLIPMethod::fillWaterTank: append the tank's particles; returns how many."""
