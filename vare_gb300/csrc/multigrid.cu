@@ -699,6 +699,128 @@ __device__ inline int32_t nbr_entry( const BoraTilesDev& t, int s, int ntiles, i
     return s < ntiles ? t.nbr[(size_t)s * 27 + tid] : -1;
 }
 
+// Row-wise staging of the level-0 region (E = 8, 12^3 cells): one thread per region row
+// (12 cells along x: 2 from the -x neighbour tile, 8 from the middle tile, 2 from the +x
+// neighbour), loaded with vector loads (8 cells of a tile row are 16 B of codes and 32 B of
+// FP32 values, aligned) instead of one scalar load per cell.
+struct Row8
+{
+    int dl, dc, dr;  // tile directions of the row's three segments
+    uint32_t off;    // local index of the row's x = 0 cell in its tiles
+    uint32_t poff;   // local index of its parent on the 4^3 level
+    int h0;          // region index of the row's first cell
+    __device__ inline void init( int row )
+    {
+        const int b = row % 12, c = row / 12;
+        const int dy = b < 2 ? -1 : ( b >= 10 ? 1 : 0 ), dz = c < 2 ? -1 : ( c >= 10 ? 1 : 0 );
+        const int ly = ( b + 6 ) & 7, lz = ( c + 6 ) & 7;
+        dl = bora_dir( -1, dy, dz );
+        dc = bora_dir( 0, dy, dz );
+        dr = bora_dir( 1, dy, dz );
+        off = (uint32_t)( 8 * ly + 64 * lz );
+        poff = (uint32_t)( 4 * ( ly >> 1 ) + 16 * ( lz >> 1 ) );
+        h0 = 12 * row;
+    }
+};
+
+// The 12 codes and values of a row (segments left 2, middle 8, right 2 cells).
+struct RowData
+{
+    uint4 cm;          // middle codes
+    uint32_t cl, cr;   // left / right codes
+    float4 v0, v1;     // middle values
+    float2 vl, vr;     // left / right values
+    __device__ inline uint16_t code( int a ) const
+    {
+        if( a < 2 ) return (uint16_t)( cl >> ( 16 * a ) );
+        if( a >= 10 ) return (uint16_t)( cr >> ( 16 * ( a - 10 ) ) );
+        const int m = a - 2;
+        const uint32_t w = m < 2 ? cm.x : ( m < 4 ? cm.y : ( m < 6 ? cm.z : cm.w ) );
+        return (uint16_t)( w >> ( 16 * ( m & 1 ) ) );
+    }
+    __device__ inline float value( int a ) const
+    {
+        if( a < 2 ) return a == 0 ? vl.x : vl.y;
+        if( a >= 10 ) return a == 10 ? vr.x : vr.y;
+        const int m = a - 2;
+        const float4 v = m < 4 ? v0 : v1;
+        const int q = m & 3;
+        return q == 0 ? v.x : ( q == 1 ? v.y : ( q == 2 ? v.z : v.w ) );
+    }
+    // codes always; values only when with_val (zero otherwise)
+    __device__ inline void load( const int32_t* nb, const Row8& rw, const uint16_t* __restrict__ code,
+                                 const float* __restrict__ val, bool with_val )
+    {
+        const int sl = nb[rw.dl], sc = nb[rw.dc], sr = nb[rw.dr];
+        cm = make_uint4( 0u, 0u, 0u, 0u ); cl = cr = 0u;
+        v0 = v1 = make_float4( 0.f, 0.f, 0.f, 0.f ); vl = vr = make_float2( 0.f, 0.f );
+        if( sc >= 0 )
+        {
+            const size_t g = (size_t)sc * 512 + rw.off;
+            cm = *reinterpret_cast<const uint4*>( code + g );
+            if( with_val )
+            {
+                v0 = __ldg( reinterpret_cast<const float4*>( val + g ) );
+                v1 = __ldg( reinterpret_cast<const float4*>( val + g + 4 ) );
+            }
+        }
+        if( sl >= 0 )
+        {
+            const size_t g = (size_t)sl * 512 + rw.off + 6;
+            cl = *reinterpret_cast<const uint32_t*>( code + g );
+            if( with_val ) vl = __ldg( reinterpret_cast<const float2*>( val + g ) );
+        }
+        if( sr >= 0 )
+        {
+            const size_t g = (size_t)sr * 512 + rw.off;
+            cr = *reinterpret_cast<const uint32_t*>( code + g );
+            if( with_val ) vr = __ldg( reinterpret_cast<const float2*>( val + g ) );
+        }
+    }
+};
+
+// The FP16 correction z0 + P e of a level-0 row: z0 of the 12 cells and the parent value on
+// the 4^3 level (left cells have parent x 3, middle cells x / 2, right cells x 0).
+struct RowZ
+{
+    uint4 zm;
+    uint32_t zl, zr;
+    uint2 em;
+    uint32_t el, er;
+    __device__ inline void load( const int32_t* nb, const Row8& rw, const __half* __restrict__ z0,
+                                 const __half* __restrict__ ec )
+    {
+        const int sl = nb[rw.dl], sc = nb[rw.dc], sr = nb[rw.dr];
+        zm = make_uint4( 0u, 0u, 0u, 0u ); zl = zr = 0u;
+        em = make_uint2( 0u, 0u ); el = er = 0u;
+        if( sc >= 0 )
+        {
+            zm = *reinterpret_cast<const uint4*>( z0 + (size_t)sc * 512 + rw.off );
+            em = *reinterpret_cast<const uint2*>( ec + (size_t)sc * 64 + rw.poff );
+        }
+        if( sl >= 0 )
+        {
+            zl = *reinterpret_cast<const uint32_t*>( z0 + (size_t)sl * 512 + rw.off + 6 );
+            el = *reinterpret_cast<const uint16_t*>( ec + (size_t)sl * 64 + rw.poff + 3 );
+        }
+        if( sr >= 0 )
+        {
+            zr = *reinterpret_cast<const uint32_t*>( z0 + (size_t)sr * 512 + rw.off );
+            er = *reinterpret_cast<const uint16_t*>( ec + (size_t)sr * 64 + rw.poff );
+        }
+    }
+    __device__ static inline float h2f( uint32_t bits ) { return __half2float( __ushort_as_half( (unsigned short)bits ) ); }
+    __device__ inline float value( int a ) const  // z0 + P e of cell a
+    {
+        if( a < 2 ) return h2f( zl >> ( 16 * a ) ) + h2f( el );
+        if( a >= 10 ) return h2f( zr >> ( 16 * ( a - 10 ) ) ) + h2f( er );
+        const int m = a - 2;
+        const uint32_t w = m < 2 ? zm.x : ( m < 4 ? zm.y : ( m < 6 ? zm.z : zm.w ) );
+        const uint32_t e = m < 4 ? em.x : em.y;
+        return h2f( w >> ( 16 * ( m & 1 ) ) ) + h2f( e >> ( 16 * ( ( m >> 1 ) & 1 ) ) );
+    }
+};
+
 template <int E, bool L0>
 __global__ void __launch_bounds__( TileRegion<E>::NT, TileRegion<E>::MINB ) k_mg_down_fused( BoraLevelDev F, BoraLevelDev C,
                                                                            BoraTilesDev t, int ntiles,
@@ -707,8 +829,9 @@ __global__ void __launch_bounds__( TileRegion<E>::NT, TileRegion<E>::MINB ) k_mg
 {
     using TR = TileRegion<E>;
     constexpr int R = TR::R, Q = TR::Q, H = TR::H, NT = TR::NT, E3 = TR::E3;
-    __shared__ float rs[TR::N], z1[TR::N];
-    __shared__ uint16_t cs[TR::N];
+    __shared__ __align__( 16 ) float rs[TR::N];
+    __shared__ __align__( 16 ) float z1[TR::N];
+    __shared__ __align__( 16 ) uint16_t cs[TR::N];
     __shared__ float z2[TR::NQ];
     __shared__ float res[E3];
     __shared__ int32_t nbb[2][27];
@@ -734,20 +857,32 @@ __global__ void __launch_bounds__( TileRegion<E>::NT, TileRegion<E>::MINB ) k_mg
     if( tid == 0 ) s_scale = L0 ? scale_of( ring, slot_rr ) : 1.f;
     __syncthreads();
     const float sc = s_scale;
-    uint16_t cv[TR::IA];
-    float rv[TR::IA];
+    constexpr bool kRows = E == 8 && L0;  // row-wise vector staging of the level-0 region
+    uint16_t cv[kRows ? 1 : TR::IA];
+    float rv[kRows ? 1 : TR::IA];
+    Row8 rw;
+    RowData rd;
+    const bool has_row = kRows && tid < 144;
+    if( has_row ) rw.init( tid );
     auto issue = [&]( const int32_t* nb ) {
-#pragma unroll
-        for( int it = 0; it < TR::IA; ++it )
+        if constexpr( kRows )
         {
-            const int sl = TR::slot( nb, am[it] );
-            cv[it] = 0;
-            rv[it] = 0.f;
-            if( sl >= 0 )
+            if( has_row ) rd.load( nb, rw, F.code, r0, true );
+        }
+        else
+        {
+#pragma unroll
+            for( int it = 0; it < TR::IA; ++it )
             {
-                const uint32_t g = (uint32_t)sl * E3 + ( am[it] & 511u );
-                cv[it] = F.code[g];
-                rv[it] = L0 ? __ldg( r0 + g ) : __half2float( F.r[g] );
+                const int sl = TR::slot( nb, am[it] );
+                cv[it] = 0;
+                rv[it] = 0.f;
+                if( sl >= 0 )
+                {
+                    const uint32_t g = (uint32_t)sl * E3 + ( am[it] & 511u );
+                    cv[it] = F.code[g];
+                    rv[it] = L0 ? __ldg( r0 + g ) : __half2float( F.r[g] );
+                }
             }
         }
     };
@@ -756,18 +891,39 @@ __global__ void __launch_bounds__( TileRegion<E>::NT, TileRegion<E>::MINB ) k_mg
     for( int s = blockIdx.x; s < ntiles; s += G, ++n )
     {
         // stage tile s; the first sweep from zero is pointwise z1 = w r'/d
-#pragma unroll
-        for( int it = 0; it < TR::IA; ++it )
+        if constexpr( kRows )
         {
-            const int h = tid + it * NT;
-            if( h < TR::N )
+            if( has_row )
             {
-                const uint16_t cc = cv[it];
-                const bool fl = cc & BORA_CODE_FLUID;
-                const float r = fl ? ( L0 ? rv[it] * sc : rv[it] ) : 0.f;
-                cs[h] = cc;
-                rs[h] = r;
-                z1[h] = fl ? r * wd[code_diag( cc )] : 0.f;
+#pragma unroll
+                for( int a = 0; a < 12; a += 2 )
+                {
+                    const uint16_t c0 = rd.code( a ), c1 = rd.code( a + 1 );
+                    const bool f0 = c0 & BORA_CODE_FLUID, f1 = c1 & BORA_CODE_FLUID;
+                    const float q0 = f0 ? rd.value( a ) * sc : 0.f, q1 = f1 ? rd.value( a + 1 ) * sc : 0.f;
+                    const int h = rw.h0 + a;
+                    *reinterpret_cast<uint32_t*>( &cs[h] ) = (uint32_t)c0 | ( (uint32_t)c1 << 16 );
+                    *reinterpret_cast<float2*>( &rs[h] ) = make_float2( q0, q1 );
+                    *reinterpret_cast<float2*>( &z1[h] ) =
+                        make_float2( f0 ? q0 * wd[code_diag( c0 )] : 0.f, f1 ? q1 * wd[code_diag( c1 )] : 0.f );
+                }
+            }
+        }
+        else
+        {
+#pragma unroll
+            for( int it = 0; it < TR::IA; ++it )
+            {
+                const int h = tid + it * NT;
+                if( h < TR::N )
+                {
+                    const uint16_t cc = cv[it];
+                    const bool fl = cc & BORA_CODE_FLUID;
+                    const float r = fl ? ( L0 ? rv[it] * sc : rv[it] ) : 0.f;
+                    cs[h] = cc;
+                    rs[h] = r;
+                    z1[h] = fl ? r * wd[code_diag( cc )] : 0.f;
+                }
             }
         }
         const int32_t nb2 = tid < 27 ? nbr_entry( t, s + 2 * G, ntiles, tid ) : -1;
@@ -819,10 +975,11 @@ __global__ void __launch_bounds__( TileRegion<E>::NT, TileRegion<E>::MINB ) k_mg
 {
     using TR = TileRegion<E>;
     constexpr int R = TR::R, Q = TR::Q, H = TR::H, NT = TR::NT, E3 = TR::E3;
-    __shared__ float rs[TR::N], za[TR::N];
-    __shared__ uint16_t cs[TR::N];
+    __shared__ __align__( 16 ) float rs[TR::N];
+    __shared__ __align__( 16 ) float za[TR::N];
+    __shared__ __align__( 16 ) uint16_t cs[TR::N];
     __shared__ float zb[TR::NQ];
-    __shared__ float rraw[L0 ? E3 : 1];
+    __shared__ __align__( 16 ) float rraw[L0 ? E3 : 1];
     __shared__ int32_t nbb[2][27];
     __shared__ float wd[16];
     __shared__ float s_scale;
@@ -846,24 +1003,48 @@ __global__ void __launch_bounds__( TileRegion<E>::NT, TileRegion<E>::MINB ) k_mg
     if( tid == 0 ) s_scale = L0 ? scale_of( red.ring, slot_rr ) : 1.f;
     __syncthreads();
     const float sc = s_scale;
-    uint16_t cv[TR::IA];
-    float rv[TR::IA], zv[TR::IA];
+    constexpr bool kRows = E == 8 && L0;  // row-wise vector staging of the level-0 region
+    uint16_t cv[kRows ? 1 : TR::IA];
+    float rv[kRows ? 1 : TR::IA], zv[kRows ? 1 : TR::IA];
+    Row8 rw;
+    RowData rd;
+    RowZ rzv;
+    const bool has_row = kRows && tid < 144;
+    bool inner_row = false, centre_row = false;
+    if( has_row )
+    {
+        rw.init( tid );
+        const int b = tid % 12, c = tid / 12;
+        inner_row = b >= 1 && b <= 10 && c >= 1 && c <= 10;
+        centre_row = b >= 2 && b <= 9 && c >= 2 && c <= 9;
+    }
     auto issue = [&]( const int32_t* nb ) {
-#pragma unroll
-        for( int it = 0; it < TR::IA; ++it )
+        if constexpr( kRows )
         {
-            const uint32_t m = am[it];
-            const int sl = TR::slot( nb, m );
-            cv[it] = 0;
-            rv[it] = 0.f;
-            zv[it] = 0.f;
-            if( sl >= 0 )
+            if( has_row )
             {
-                const uint32_t g = (uint32_t)sl * E3 + ( m & 511u );
-                cv[it] = F.code[g];
-                // za = z0 + P e: the parent is the same tile's cell on the coarser level
-                zv[it] = __half2float( F.z0[g] ) + __half2float( ec[(uint32_t)sl * ( H * H * H ) + ( ( m >> 9 ) & 63u )] );
-                if( m & TR::kInner ) rv[it] = L0 ? __ldg( r0 + g ) : __half2float( F.r[g] );
+                rd.load( nb, rw, F.code, r0, inner_row );
+                rzv.load( nb, rw, F.z0, ec );
+            }
+        }
+        else
+        {
+#pragma unroll
+            for( int it = 0; it < TR::IA; ++it )
+            {
+                const uint32_t m = am[it];
+                const int sl = TR::slot( nb, m );
+                cv[it] = 0;
+                rv[it] = 0.f;
+                zv[it] = 0.f;
+                if( sl >= 0 )
+                {
+                    const uint32_t g = (uint32_t)sl * E3 + ( m & 511u );
+                    cv[it] = F.code[g];
+                    // za = z0 + P e: the parent is the same tile's cell on the coarser level
+                    zv[it] = __half2float( F.z0[g] ) + __half2float( ec[(uint32_t)sl * ( H * H * H ) + ( ( m >> 9 ) & 63u )] );
+                    if( m & TR::kInner ) rv[it] = L0 ? __ldg( r0 + g ) : __half2float( F.r[g] );
+                }
             }
         }
     };
@@ -873,18 +1054,40 @@ __global__ void __launch_bounds__( TileRegion<E>::NT, TileRegion<E>::MINB ) k_mg
     for( int s = blockIdx.x; s < ntiles; s += G, ++n )
     {
         float trz = 0.f;  // this thread's r.z over its cells of the tile
-#pragma unroll
-        for( int it = 0; it < TR::IA; ++it )
+        if constexpr( kRows )
         {
-            const int h = tid + it * NT;
-            if( h < TR::N )
+            if( has_row )
             {
-                const uint16_t cc = cv[it];
-                const bool fl = cc & BORA_CODE_FLUID;
-                cs[h] = cc;
-                rs[h] = fl ? ( L0 ? rv[it] * sc : rv[it] ) : 0.f;
-                za[h] = fl ? zv[it] : 0.f;
-                if( L0 && ( ( am[it] >> 16 ) & 31u ) == TR::kCentre ) rraw[am[it] & 511u] = rv[it];
+#pragma unroll
+                for( int a = 0; a < 12; a += 2 )
+                {
+                    const uint16_t c0 = rd.code( a ), c1 = rd.code( a + 1 );
+                    const bool f0 = c0 & BORA_CODE_FLUID, f1 = c1 & BORA_CODE_FLUID;
+                    const float v0 = rd.value( a ), v1 = rd.value( a + 1 );
+                    const int h = rw.h0 + a;
+                    *reinterpret_cast<uint32_t*>( &cs[h] ) = (uint32_t)c0 | ( (uint32_t)c1 << 16 );
+                    *reinterpret_cast<float2*>( &rs[h] ) = make_float2( f0 ? v0 * sc : 0.f, f1 ? v1 * sc : 0.f );
+                    *reinterpret_cast<float2*>( &za[h] ) = make_float2( f0 ? rzv.value( a ) : 0.f, f1 ? rzv.value( a + 1 ) : 0.f );
+                    if( centre_row && a >= 2 && a < 10 )
+                        *reinterpret_cast<float2*>( &rraw[rw.off + a - 2] ) = make_float2( v0, v1 );
+                }
+            }
+        }
+        else
+        {
+#pragma unroll
+            for( int it = 0; it < TR::IA; ++it )
+            {
+                const int h = tid + it * NT;
+                if( h < TR::N )
+                {
+                    const uint16_t cc = cv[it];
+                    const bool fl = cc & BORA_CODE_FLUID;
+                    cs[h] = cc;
+                    rs[h] = fl ? ( L0 ? rv[it] * sc : rv[it] ) : 0.f;
+                    za[h] = fl ? zv[it] : 0.f;
+                    if( L0 && ( ( am[it] >> 16 ) & 31u ) == TR::kCentre ) rraw[am[it] & 511u] = rv[it];
+                }
             }
         }
         const int32_t nb2 = tid < 27 ? nbr_entry( t, s + 2 * G, ntiles, tid ) : -1;
