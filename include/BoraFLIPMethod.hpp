@@ -7,7 +7,8 @@
 //   Bora::FLIPMethod::Params params            BoraGB300::FLIPMethod::Params params (same fields)
 //   initialize( const Grid& )                  initialize( grid ) / initialize( nx,ny,nz,min,max )
 //   newParticle( Particles&, p, v )            newParticle( Particles&, p, v )
-//   advanceOneFrame( Particles& )              advanceOneFrame( Particles& )
+//   advanceOneFrame( Particles& )              advanceOneFrame( Particles& )   (step + postProcess)
+//   postProcess( Particles& )                  postProcess( Particles& )       (voxel space)
 //   advanceOneStep( Particles&, dt )           advanceOneStep( Particles&, dt )   (voxel space)
 //   particlesToVoxel / particlesToWorld        particlesToVoxel / particlesToWorld
 //   updateCollisionSource( vdb, vdb )          setColliders( boxes )  (analytic boxes; no OpenVDB)
@@ -47,17 +48,20 @@ inline int check( int st, const char* what )
 }
 
 // Host particle store: the attributes FLIPMethod reads and writes
-// (Bora::Particles position, velocity, adjacency; FLIPMethod.h:75-99) plus an id.
+// (Bora::Particles position, velocity, adjacency, vorticity, curvature; FLIPMethod.h:75-99)
+// plus an id.
 struct Particles
 {
     std::vector<float> position;   // x,y,z per particle
     std::vector<float> velocity;   // x,y,z per particle
     std::vector<float> adjacency;  // one per particle
+    std::vector<float> vorticity;  // one per particle (postProcess)
+    std::vector<float> curvature;  // one per particle (postProcess)
     std::vector<int32_t> id;
     size_t size() const { return position.size() / 3; }
     void clear()
     {
-        position.clear(); velocity.clear(); adjacency.clear(); id.clear();
+        position.clear(); velocity.clear(); adjacency.clear(); vorticity.clear(); curvature.clear(); id.clear();
     }
 };
 
@@ -124,6 +128,8 @@ class FLIPMethod
     {
         for( int a = 0; a < 3; ++a ) { pts.position.push_back( p[a] ); pts.velocity.push_back( v[a] ); }
         pts.adjacency.push_back( 0.f );
+        pts.vorticity.push_back( 0.f );
+        pts.curvature.push_back( 0.f );
         pts.id.push_back( -1 );
     }
 
@@ -157,18 +163,23 @@ class FLIPMethod
         check( bora_flip_set_colliders( _h, boxes.data(), (int)( boxes.size() / 9 ), band ), "bora_flip_set_colliders" );
     }
 
-    // FLIPMethod::advanceOneFrame (FLIPMethod.cu:177-206) without postProcess: world-space
-    // particles in, one step of params.dt, world-space particles out.
+    // FLIPMethod::advanceOneFrame (FLIPMethod.cu:177-206): world-space particles in, one
+    // step of params.dt and postProcess, world-space particles out.
     int advanceOneFrame( Particles& pts )
     {
         if( pts.size() == 0 ) return BORA_OK;  // FLIPMethod.cu:179
-        const int st = run( pts, params.dt, BORA_SPACE_WORLD );
+        const int st = run( pts, params.dt, BORA_SPACE_WORLD, true, true );
         ++_frameCount;
         return st;
     }
 
     // FLIPMethod::advanceOneStep (FLIPMethod.cu:208-298): voxel-space particles.
-    int advanceOneStep( Particles& pts, float dt ) { return run( pts, dt, BORA_SPACE_VOXEL ); }
+    int advanceOneStep( Particles& pts, float dt ) { return run( pts, dt, BORA_SPACE_VOXEL, true, false ); }
+
+    // FLIPMethod::postProcess (FLIPMethod.cu:300-405) on voxel-space particles: updates
+    // their vorticity and curvature; the surface is then in the handle's fields
+    // (BORA_FIELD_SURF over the active tiles, bora_flip_get_field).
+    void postProcess( Particles& pts ) { run( pts, 0.f, BORA_SPACE_VOXEL, false, true ); }
 
     // FLIPMethod::particlesToVoxel / particlesToWorld (FLIPMethod.cu:481-513).
     void particlesToVoxel( Particles& pts ) const { transform( pts, true ); }
@@ -225,7 +236,7 @@ class FLIPMethod
         return p;
     }
 
-    int run( Particles& pts, float dt, int space )
+    int run( Particles& pts, float dt, int space, bool step, bool post )
     {
         requireInit();
         const bora_flip_params p = toC();
@@ -233,7 +244,12 @@ class FLIPMethod
         const size_t n = pts.size();
         if( pts.velocity.size() != 3 * n ) pts.velocity.resize( 3 * n, 0.f );
         check( bora_flip_set_particles( _h, pts.position.data(), pts.velocity.data(), n, space ), "bora_flip_set_particles" );
-        const int st = check( bora_flip_step( _h, dt ), "bora_flip_step" );
+        const bool attrs = pts.vorticity.size() == n && pts.curvature.size() == n;
+        if( attrs && n )
+            check( bora_flip_set_particle_attributes( _h, pts.vorticity.data(), pts.curvature.data(), n ),
+                   "bora_flip_set_particle_attributes" );
+        const int st = step ? check( bora_flip_step( _h, dt ), "bora_flip_step" ) : BORA_OK;
+        if( post ) check( bora_flip_post_process( _h ), "bora_flip_post_process" );
         size_t m = 0;
         check( bora_flip_num_particles( _h, &m ), "bora_flip_num_particles" );
         pts.position.resize( 3 * m );
@@ -243,6 +259,13 @@ class FLIPMethod
         check( bora_flip_get_particles( _h, pts.position.data(), pts.velocity.data(), pts.adjacency.data(),
                                         pts.id.data(), m, &m, space ),
                "bora_flip_get_particles" );
+        if( attrs || post )
+        {
+            pts.vorticity.resize( m );
+            pts.curvature.resize( m );
+            check( bora_flip_get_particle_attributes( _h, pts.vorticity.data(), pts.curvature.data(), nullptr, m, &m ),
+                   "bora_flip_get_particle_attributes" );
+        }
         return st;
     }
 

@@ -90,6 +90,8 @@ typedef struct bora_flip_params
     int advection;           /* BORA_ADVECT_EULER: particle positions follow the particle velocity
                                 (FLIPMethod.cu:124-145); BORA_ADVECT_RK2: midpoint rule in the grid
                                 velocity field, per substep */
+    int post_process;        /* 1: bora_flip_frame post-processes after the step, as
+                                FLIPMethod::advanceOneFrame does (FLIPMethod.cu:177-206) */
 } bora_flip_params;
 
 typedef struct bora_flip_stats
@@ -125,6 +127,7 @@ typedef struct bora_flip_stats
 #define BORA_KERNEL_VELOCITY 8
 #define BORA_KERNEL_G2P 9
 #define BORA_KERNEL_MG 10          /* multigrid V-cycle (mixed solver) */
+#define BORA_KERNEL_POST 11        /* post-processing: splat, tank scan, redistancing, attributes */
 #define BORA_KERNEL_CLASSES 16
 
 /* Simulation frame description (after padding). */
@@ -176,9 +179,42 @@ int bora_flip_set_collider_field( bora_flip_handle h, const float* phi, const fl
 /* FLIPMethod::advanceOneStep (FLIPMethod.cu:208-298) in voxel space. Returns
  * BORA_WARN_NOT_CONVERGED when the pressure solve stopped on its iteration caps. */
 int bora_flip_step( bora_flip_handle h, float dt );
-/* FLIPMethod::advanceOneFrame (FLIPMethod.cu:177-206) without the post-processing
- * surface pipeline: one step of params.dt. */
+/* FLIPMethod::advanceOneFrame (FLIPMethod.cu:177-206): one step of params.dt, then (with
+ * params.post_process) bora_flip_post_process. */
 int bora_flip_frame( bora_flip_handle h );
+
+/* FLIPMethod::postProcess (FLIPMethod.cu:300-405), the surface pipeline that follows the
+ * step in a frame: rebuild the tiles from the current particles (prepareNextStep; the
+ * next step reuses them), splat the surface and velocity
+ * (Rasterization::ParticlesToSurfaceAndVelocity, Rasterization.cu:311-398; influence 1.5,
+ * droplet 0.5), with the water tank turn enclosed air below the wall level into liquid
+ * (surf = -5), params.redist_iteration redistancing steps
+ * (Rasterization::ReinitializeSurface, Rasterization.cu:400-486), then update the
+ * particles' vorticity (decay (1 - params.vort_pres_rate)^params.dt) and curvature.
+ * Afterwards BORA_FIELD_SURF holds the signed distance (voxel units, negative in the
+ * liquid), BORA_FIELD_VELO the splatted velocity, BORA_FIELD_COMP the surface normals and
+ * BORA_FIELD_PRES zero. The splat's sums are added in no fixed order (as the reference's
+ * atomics). The tank's scan is the 6-connected fill of air from the wall layer and the
+ * far corner; the reference's host loop reads its popped cell through a reference that
+ * the loop's first push overwrites (FLIPMethod.cu:335-337), which can leave air cells of
+ * one-cell-wide passages unreached that are reached here. */
+int bora_flip_post_process( bora_flip_handle h );
+
+/* The parts of bora_flip_post_process, for tests and callers that interleave their own
+ * work. All need the tiles of a rebuild (BORA_STAGE_REBUILD, or a post-processing);
+ * BORA_POST_SPLAT also needs the particles unchanged since. */
+#define BORA_POST_SPLAT 0        /* zero the fields, splat, normalise (surf, pres = weight sum, velo, comp = mean position) */
+#define BORA_POST_TANK_SCAN 1    /* water tank only: enclosed air below the wall -> surf = -5 */
+#define BORA_POST_REDISTANCE 2   /* params.redist_iteration steps on surf (pres is the scratch field) */
+#define BORA_POST_ATTRIBUTES 3   /* curl -> vorticity, normals -> comp, curvature -> particles, pres = 0 */
+int bora_flip_run_post_stage( bora_flip_handle h, int stage );
+
+/* Particles::vorticity / ::curvature of the live particles, in bora_flip_get_particles'
+ * order (ids as there; any pointer may be NULL; zero before the first post-processing). */
+int bora_flip_get_particle_attributes( bora_flip_handle h, float* vorticity, float* curvature, int32_t* ids,
+                                       size_t cap, size_t* n );
+/* Replace them (n = live particles, in bora_flip_get_particles' order; NULL = zeros). */
+int bora_flip_set_particle_attributes( bora_flip_handle h, const float* vorticity, const float* curvature, size_t n );
 
 /* The stages of one step, for callers that interleave their own work and for tests. */
 #define BORA_STAGE_REBUILD 0          /* SparseFrame::buildFromPoints */

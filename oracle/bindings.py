@@ -115,6 +115,13 @@ def _oracle_lib() -> ctypes.CDLL:
         lib.ora_last_rel.restype = ctypes.c_double
         lib.ora_fill_water_tank.argtypes = [_vp, ctypes.c_int]
         lib.ora_fill_water_tank.restype = ctypes.c_size_t
+        lib.ora_post_process.argtypes = [_vp, ctypes.c_float, ctypes.c_float, ctypes.c_int, ctypes.c_int]
+        lib.ora_post_splat.argtypes = [_vp]
+        lib.ora_post_tank_scan.argtypes = [_vp, ctypes.c_int]
+        lib.ora_post_redistance.argtypes = [_vp, ctypes.c_int]
+        lib.ora_post_attributes.argtypes = [_vp, ctypes.c_float, ctypes.c_float]
+        lib.ora_get_attributes.argtypes = [_vp, _vp, _vp]
+        lib.ora_set_attributes.argtypes = [_vp, _vp, _vp]
         lib._typed = True
     return lib
 
@@ -295,6 +302,34 @@ class Oracle(_SimBase):
     def last_rel(self) -> float:
         return float(self.lib.ora_last_rel(self.h))
 
+    # FLIPMethod::postProcess restated
+    def post_process(self, dt: float, vort_pres_rate: float = 0.2, redist_iteration: int = 80,
+                     literal_scan: bool = False) -> None:
+        """literal_scan reproduces the reference's tank scan as it executes; the default is
+        the 6-connected fill of the device path."""
+        self.lib.ora_post_process(self.h, dt, vort_pres_rate, redist_iteration, 1 if literal_scan else 0)
+
+    def post_splat(self): self.lib.ora_post_splat(self.h)
+    def post_tank_scan(self, literal: bool = False): self.lib.ora_post_tank_scan(self.h, 1 if literal else 0)
+
+    def post_redistance(self, iters: int = 80):
+        self.lib.ora_post_redistance(self.h, iters)
+
+    def post_attributes(self, dt: float, vort_pres_rate: float = 0.2):
+        self.lib.ora_post_attributes(self.h, dt, vort_pres_rate)
+
+    def attributes(self):
+        n = self.num_particles
+        vort = np.zeros(n, np.float32)
+        curv = np.zeros(n, np.float32)
+        self.lib.ora_get_attributes(self.h, _ptr(vort), _ptr(curv))
+        return vort, curv
+
+    def set_attributes(self, vort, curv) -> None:
+        vort = np.ascontiguousarray(vort, np.float32)
+        curv = np.ascontiguousarray(curv, np.float32)
+        self.lib.ora_set_attributes(self.h, _ptr(vort), _ptr(curv))
+
 
 def _ref_lib(path: str) -> ctypes.CDLL:
     lib = _load(path)
@@ -322,6 +357,8 @@ def _ref_lib(path: str) -> ctypes.CDLL:
         lib.ref_get_system.argtypes = [_vp, _vp, _vp, _vp]
         lib.ref_fill_water_tank.argtypes = [_vp]
         lib.ref_fill_water_tank.restype = ctypes.c_size_t
+        lib.ref_post_process.argtypes = [_vp]
+        lib.ref_get_attributes.argtypes = [_vp, _vp, _vp]
         if hasattr(lib, "ref_cg64_set"):
             lib.ref_cg64_set.argtypes = [ctypes.c_double, ctypes.c_int]
             lib.ref_cg64_last_iters.restype = ctypes.c_int
@@ -399,6 +436,18 @@ class RefSim(_SimBase):
 
     def step(self, dt: float) -> None:
         self.lib.ref_step(self.h, dt)
+
+    def post_process(self) -> None:
+        """The reference's own FLIPMethod::postProcess (params.dt, vortPresRate 0.2,
+        redistIteration 80)."""
+        self.lib.ref_post_process(self.h)
+
+    def attributes(self):
+        n = self.num_particles
+        vort = np.zeros(n, np.float32)
+        curv = np.zeros(n, np.float32)
+        self.lib.ref_get_attributes(self.h, _ptr(vort), _ptr(curv))
+        return vort, curv
 
     def system(self):
         n = int(self.lib.ref_num_unknowns(self.h))

@@ -816,6 +816,320 @@ struct Oracle
         removeMasked( vel, removed );
         removeMasked( adj, removed );
         removeMasked( pid, removed );
+        removeMasked( vort, removed );
+        removeMasked( curv, removed );
+    }
+
+    // =================================================================================
+    // FLIPMethod::postProcess (base/source/FLIPMethod.cu:300-405): the surface pipeline
+    // that follows the step in FLIPMethod::advanceOneFrame. The particle attributes
+    // Particles::vorticity / ::curvature (base/header/Particles.h:28) ride along with the
+    // particles through compact(). Cells of an 8^3 tile beyond the grid are skipped (the
+    // reference's 4^3 tiles never extend past its grid).
+    std::vector<float> vort, curv;
+    float presBackground = 0.f;
+
+    // Rasterization::ParticlesToSurfaceAndVelocity (base/source/Rasterization.cu:311-398)
+    // with influence 1.5 and droplet radius 0.5 (FLIPMethod.cu:320): weights
+    // max(0, (1 - (d/1.5)^2)^3) over the 3^3 cells around the particle's cell
+    // (Grid::neighborCells, base/header/Grid.h:353-370), accumulated in particle order
+    // into pres/velo (FLIPMethod.cu:320 passes _sPresField as the mass field) and
+    // surf/comp (the weighted position); then surf = distance from the weighted mean
+    // position to the cell centre - 0.5 (5 where nothing landed) and velo = weighted mean
+    // velocity.
+    void splatSurface()
+    {
+        std::fill( surf.begin(), surf.end(), 0.f );
+        std::fill( pres.begin(), pres.end(), 0.f );
+        std::fill( comp.begin(), comp.end(), V3{ 0.f, 0.f, 0.f } );
+        std::fill( velo.begin(), velo.end(), V3{ 0.f, 0.f, 0.f } );
+        const float h = 1.5f, r = 0.5f;
+        for( size_t n = 0; n < pos.size(); ++n )
+        {
+            const V3 p = pos[n], v = vel[n];
+            if( !inside( p ) ) continue;
+            const int i0 = clampi( (int)p.x - 1, 0, nx - 1 ), i1 = clampi( (int)p.x + 1, 0, nx - 1 );
+            const int j0 = clampi( (int)p.y - 1, 0, ny - 1 ), j1 = clampi( (int)p.y + 1, 0, ny - 1 );
+            const int k0 = clampi( (int)p.z - 1, 0, nz - 1 ), k1 = clampi( (int)p.z + 1, 0, nz - 1 );
+            for( int k = k0; k <= k1; ++k )
+                for( int j = j0; j <= j1; ++j )
+                    for( int i = i0; i <= i1; ++i )
+                    {
+                        const float dx = p.x - ( (float)i + .5f ), dy = p.y - ( (float)j + .5f ), dz = p.z - ( (float)k + .5f );
+                        const float dist = std::sqrt( dx * dx + dy * dy + dz * dz );  // Vec3f::length (Vector3.h:328-331)
+                        const float s = dist / h;
+                        const float t = 1.f - s * s;
+                        const float w = fmaxr( 0.f, t * t * t );
+                        const int64_t q = findIndex( i, j, k );
+                        if( q == kNull ) continue;
+                        pres[(size_t)q] += w;
+                        velo[(size_t)q].x += w * v.x; velo[(size_t)q].y += w * v.y; velo[(size_t)q].z += w * v.z;
+                        surf[(size_t)q] += w;
+                        comp[(size_t)q].x += w * p.x; comp[(size_t)q].y += w * p.y; comp[(size_t)q].z += w * p.z;
+                    }
+        }
+        surfBackground = 10.f;
+        for( size_t n = 0; n < surf.size(); ++n )
+        {
+            int i, j, k;
+            findIndices( n, i, j, k );
+            if( surf[n] > 1e-30f )
+            {
+                comp[n].x /= surf[n]; comp[n].y /= surf[n]; comp[n].z /= surf[n];
+                const float dx = comp[n].x - ( (float)i + .5f ), dy = comp[n].y - ( (float)j + .5f ),
+                            dz = comp[n].z - ( (float)k + .5f );
+                surf[n] = std::sqrt( dx * dx + dy * dy + dz * dz ) - r;  // Vec3f::distanceTo (Vector3.h:364-367)
+            }
+            else
+            {
+                surf[n] = 5.f;
+            }
+            if( pres[n] > 1e-30f )
+            {
+                velo[n].x /= pres[n]; velo[n].y /= pres[n]; velo[n].z /= pres[n];
+            }
+            else
+            {
+                velo[n] = V3{ 0.f, 0.f, 0.f };
+            }
+        }
+    }
+
+    // The water-tank scan (FLIPMethod.cu:322-366): a depth-first fill from the corner
+    // cell (nx-1, ny-1, nz-1) and from every air cell (surf > 0; inactive tiles read the
+    // background 10) of the layer j = wall, through air cells, expanding only cells at or
+    // below the wall; air cells at or below the wall that it does not reach become liquid
+    // (surf = -5). literal = true restates the loop as the reference executes it: the
+    // popped cell is read through a reference to the stack's last element
+    // (FLIPMethod.cu:335-337), and the iteration's first push_back constructs the new cell
+    // in that same slot, so the remaining neighbour tests of the iteration are made around
+    // the first pushed cell instead. literal = false is the 6-connected fill that the loop
+    // describes (the device path's rule). A negative wall level skips the scan (the
+    // reference converts it to size_t, which is undefined), and with the wall at or above
+    // the grid top only the corner seeds it (the reference would read past its tile table).
+    void tankScan( bool literal )
+    {
+        if( !cfg.enable_tank || voxelWall < 0.f ) return;
+        const size_t wall = (size_t)voxelWall;
+        std::vector<uint8_t> scan( (size_t)nx * ny * nz, 0 );
+        auto S = [&]( int i, int j, int k ) { return at( surf, i, j, k, surfBackground ); };
+        auto sc = [&]( int i, int j, int k ) -> uint8_t& { return scan[( (size_t)k * ny + j ) * nx + i]; };
+        struct C3 { int i, j, k; };
+        std::vector<C3> cells;
+        cells.reserve( (size_t)nx * nz );
+        cells.push_back( C3{ nx - 1, ny - 1, nz - 1 } );
+        if( wall < (size_t)ny )
+            for( int k = 0; k < nz; ++k )
+                for( int i = 0; i < nx; ++i )
+                    if( S( i, (int)wall, k ) > 0.f ) cells.push_back( C3{ i, (int)wall, k } );
+        while( !cells.empty() )
+        {
+            C3 c = cells.back();
+            cells.pop_back();
+            sc( c.i, c.j, c.k ) = 1;
+            if( (size_t)c.j > wall ) continue;
+            bool first = true;
+            auto push = [&]( C3 q ) {
+                cells.push_back( q );
+                if( literal && first ) c = q;
+                first = false;
+            };
+            if( c.i - 1 >= 0 && S( c.i - 1, c.j, c.k ) > 0.f && sc( c.i - 1, c.j, c.k ) == 0 ) push( C3{ c.i - 1, c.j, c.k } );
+            if( c.i + 1 < nx && S( c.i + 1, c.j, c.k ) > 0.f && sc( c.i + 1, c.j, c.k ) == 0 ) push( C3{ c.i + 1, c.j, c.k } );
+            if( c.j - 1 >= 0 && S( c.i, c.j - 1, c.k ) > 0.f && sc( c.i, c.j - 1, c.k ) == 0 ) push( C3{ c.i, c.j - 1, c.k } );
+            if( c.j + 1 < ny && S( c.i, c.j + 1, c.k ) > 0.f && sc( c.i, c.j + 1, c.k ) == 0 ) push( C3{ c.i, c.j + 1, c.k } );
+            if( c.k - 1 >= 0 && S( c.i, c.j, c.k - 1 ) > 0.f && sc( c.i, c.j, c.k - 1 ) == 0 ) push( C3{ c.i, c.j, c.k - 1 } );
+            if( c.k + 1 < nz && S( c.i, c.j, c.k + 1 ) > 0.f && sc( c.i, c.j, c.k + 1 ) == 0 ) push( C3{ c.i, c.j, c.k + 1 } );
+        }
+        for( size_t n = 0; n < surf.size(); ++n )
+        {
+            int i, j, k;
+            findIndices( n, i, j, k );
+            if( !real( i, j, k ) || (size_t)j > wall ) continue;
+            if( surf[n] > 0.f && sc( i, j, k ) == 0 ) surf[n] = -5.f;
+        }
+    }
+
+    // Rasterization::ReinitializeSurface (base/source/Rasterization.cu:400-486): `iters`
+    // Godunov upwind steps (dt 0.3) of phi_t = sign(phi0)(1 - |grad phi|) with
+    // sign = phi / sqrt(phi^2 + 1); differences are mirrored at the grid faces, or, for
+    // the water tank, the faces read the level y - wall (-1 / +1 below / above). surf and
+    // pres swap after each step, as the reference swaps the two fields' storage.
+    void redistance( int iters )
+    {
+        const int I = nx - 1, J = ny - 1, K = nz - 1;
+        const float dt = 0.3f;
+        surfBackground = 10.f;
+        presBackground = 10.f;
+        const bool tank = cfg.enable_tank != 0;
+        const float level = voxelWall;
+        const long long nc = (long long)surf.size();
+        for( int it = 0; it < iters; ++it )
+        {
+#pragma omp parallel for schedule(static)
+            for( long long n = 0; n < nc; ++n )
+            {
+                int i, j, k;
+                findIndices( (size_t)n, i, j, k );
+                const float v = surf[(size_t)n];
+                if( !real( i, j, k ) ) { pres[(size_t)n] = v; continue; }
+                auto S = [&]( int a, int b, int c ) { return at( surf, a, b, c, 10.f ); };
+                float vi0, vi1, vj0, vj1, vk0, vk1;
+                if( tank )
+                {
+                    const float ll = ( (float)j + .5f ) - level;
+                    vj0 = j == 0 ? ll - 1.f : S( i, j - 1, k );
+                    vj1 = j == J ? ll + 1.f : S( i, j + 1, k );
+                    vi0 = i == 0 ? ll : S( i - 1, j, k );
+                    vi1 = i == I ? ll : S( i + 1, j, k );
+                    vk0 = k == 0 ? ll : S( i, j, k - 1 );
+                    vk1 = k == K ? ll : S( i, j, k + 1 );
+                }
+                else
+                {
+                    vi0 = i == 0 ? 2.f * v - S( i + 1, j, k ) : S( i - 1, j, k );
+                    vi1 = i == I ? 2.f * v - S( i - 1, j, k ) : S( i + 1, j, k );
+                    vj0 = j == 0 ? 2.f * v - S( i, j + 1, k ) : S( i, j - 1, k );
+                    vj1 = j == J ? 2.f * v - S( i, j - 1, k ) : S( i, j + 1, k );
+                    vk0 = k == 0 ? 2.f * v - S( i, j, k + 1 ) : S( i, j, k - 1 );
+                    vk1 = k == K ? 2.f * v - S( i, j, k - 1 ) : S( i, j, k + 1 );
+                }
+                const float dx0 = v - vi0, dx1 = vi1 - v, dy0 = v - vj0, dy1 = vj1 - v, dz0 = v - vk0, dz1 = vk1 - v;
+                auto sq = []( float x ) { return x * x; };
+                const float a = sq( fmaxr( dx0, 0.f ) ) + sq( fminr( dx1, 0.f ) ) + sq( fmaxr( dy0, 0.f ) ) +
+                                sq( fminr( dy1, 0.f ) ) + sq( fmaxr( dz0, 0.f ) ) + sq( fminr( dz1, 0.f ) );
+                const float b = sq( fminr( dx0, 0.f ) ) + sq( fmaxr( dx1, 0.f ) ) + sq( fminr( dy0, 0.f ) ) +
+                                sq( fmaxr( dy1, 0.f ) ) + sq( fminr( dz0, 0.f ) ) + sq( fmaxr( dz1, 0.f ) );
+                const float sign = v / std::sqrt( v * v + 1.f );
+                pres[(size_t)n] = ( v - dt * fmaxr( sign, 0.f ) * ( std::sqrt( a ) - 1.f ) ) -
+                                  dt * fminr( sign, 0.f ) * ( std::sqrt( b ) - 1.f );
+            }
+            std::swap( surf, pres );
+        }
+    }
+
+    // FieldOP::curl, sparse (base/source/FieldOP.cu:338-369): central differences of velo
+    // (background 0), mirrored at the grid faces, into comp.
+    void curlToComp()
+    {
+        const int I = nx - 1, J = ny - 1, K = nz - 1;
+        const V3 bg{ 0.f, 0.f, 0.f };
+        const long long nc = (long long)velo.size();
+#pragma omp parallel for schedule(static)
+        for( long long n = 0; n < nc; ++n )
+        {
+            int i, j, k;
+            findIndices( (size_t)n, i, j, k );
+            if( !real( i, j, k ) ) continue;
+            const V3 v = velo[(size_t)n];
+            auto F = [&]( int a, int b, int c ) { return at( velo, a, b, c, bg ); };
+            auto mir = [&]( V3 o ) { return V3{ v.x * 2.f - o.x, v.y * 2.f - o.y, v.z * 2.f - o.z }; };
+            const V3 x0 = i == 0 ? mir( F( i + 1, j, k ) ) : F( i - 1, j, k );
+            const V3 x1 = i == I ? mir( F( i - 1, j, k ) ) : F( i + 1, j, k );
+            const V3 y0 = j == 0 ? mir( F( i, j + 1, k ) ) : F( i, j - 1, k );
+            const V3 y1 = j == J ? mir( F( i, j - 1, k ) ) : F( i, j + 1, k );
+            const V3 z0 = k == 0 ? mir( F( i, j, k + 1 ) ) : F( i, j, k - 1 );
+            const V3 z1 = k == K ? mir( F( i, j, k - 1 ) ) : F( i, j, k + 1 );
+            comp[(size_t)n] = V3{ ( y1.z - y0.z ) * 0.5f - ( z1.y - z0.y ) * 0.5f, ( z1.x - z0.x ) * 0.5f - ( x1.z - x0.z ) * 0.5f,
+                                  ( x1.y - x0.y ) * 0.5f - ( y1.x - y0.x ) * 0.5f };
+        }
+    }
+
+    // FieldOP::normalGradient, sparse (FieldOP.cu:79-110): central differences of surf
+    // (background 10), mirrored at the faces, normalised (Vec3f::normalized,
+    // base/header/Vector3.h:350-354), into comp.
+    void normalToComp()
+    {
+        const int I = nx - 1, J = ny - 1, K = nz - 1;
+        const long long nc = (long long)surf.size();
+        const float bg = surfBackground;
+#pragma omp parallel for schedule(static)
+        for( long long n = 0; n < nc; ++n )
+        {
+            int i, j, k;
+            findIndices( (size_t)n, i, j, k );
+            if( !real( i, j, k ) ) continue;
+            const float v = surf[(size_t)n];
+            auto S = [&]( int a, int b, int c ) { return at( surf, a, b, c, bg ); };
+            const float vi0 = i == 0 ? 2.f * v - S( i + 1, j, k ) : S( i - 1, j, k );
+            const float vi1 = i == I ? 2.f * v - S( i - 1, j, k ) : S( i + 1, j, k );
+            const float vj0 = j == 0 ? 2.f * v - S( i, j + 1, k ) : S( i, j - 1, k );
+            const float vj1 = j == J ? 2.f * v - S( i, j - 1, k ) : S( i, j + 1, k );
+            const float vk0 = k == 0 ? 2.f * v - S( i, j, k + 1 ) : S( i, j, k - 1 );
+            const float vk1 = k == K ? 2.f * v - S( i, j, k - 1 ) : S( i, j, k + 1 );
+            const float gx = ( vi1 - vi0 ) * 0.5f, gy = ( vj1 - vj0 ) * 0.5f, gz = ( vk1 - vk0 ) * 0.5f;
+            const float d = 1.f / std::sqrt( gx * gx + gy * gy + gz * gz + 1e-30f );
+            comp[(size_t)n] = V3{ gx * d, gy * d, gz * d };
+        }
+    }
+
+    // FieldOP::curvature of a vector field, sparse (FieldOP.cu:273-301): divergence of
+    // comp (background 0) by central differences mirrored at the faces, into pres.
+    void curvatureToPres()
+    {
+        const int I = nx - 1, J = ny - 1, K = nz - 1;
+        const V3 bg{ 0.f, 0.f, 0.f };
+        const long long nc = (long long)comp.size();
+#pragma omp parallel for schedule(static)
+        for( long long n = 0; n < nc; ++n )
+        {
+            int i, j, k;
+            findIndices( (size_t)n, i, j, k );
+            if( !real( i, j, k ) ) continue;
+            const V3 s = comp[(size_t)n];
+            auto N = [&]( int a, int b, int c ) { return at( comp, a, b, c, bg ); };
+            const float si0 = i == 0 ? s.x * 2.f - N( i + 1, j, k ).x : N( i - 1, j, k ).x;
+            const float si1 = i == I ? s.x * 2.f - N( i - 1, j, k ).x : N( i + 1, j, k ).x;
+            const float sj0 = j == 0 ? s.y * 2.f - N( i, j + 1, k ).y : N( i, j - 1, k ).y;
+            const float sj1 = j == J ? s.y * 2.f - N( i, j - 1, k ).y : N( i, j + 1, k ).y;
+            const float sk0 = k == 0 ? s.z * 2.f - N( i, j, k + 1 ).z : N( i, j, k - 1 ).z;
+            const float sk1 = k == K ? s.z * 2.f - N( i, j, k - 1 ).z : N( i, j, k + 1 ).z;
+            pres[(size_t)n] = ( si1 - si0 ) * 0.5f + ( sj1 - sj0 ) * 0.5f + ( sk1 - sk0 ) * 0.5f;
+        }
+    }
+
+    // FLIPMethod.cu:370-404: curl -> per-particle vorticity (decayed by
+    // (1 - vortPresRate)^dt, the larger of that and |world curl| - 0.2 kept), normal
+    // gradient -> curvature -> per-particle curvature (pres background 10 here, as
+    // ReinitializeSurface left it), then pres cleared to 0 with background 0.
+    void particleAttributes( float dt, float vort_pres_rate )
+    {
+        if( vort.size() != pos.size() ) vort.resize( pos.size(), 0.f );
+        if( curv.size() != pos.size() ) curv.resize( pos.size(), 0.f );
+        curlToComp();
+        const float dis = powf( 1.f - vort_pres_rate, dt );
+        const long long np = (long long)pos.size();
+#pragma omp parallel for schedule(static)
+        for( long long n = 0; n < np; ++n )
+        {
+            const V3 p = pos[(size_t)n];
+            const V3 c = lerpV( comp, p.x, p.y, p.z );
+            const float wx = c.x * scale[0], wy = c.y * scale[1], wz = c.z * scale[2];  // Grid::worldVector
+            float v = std::sqrt( wx * wx + wy * wy + wz * wz );
+            v = fmaxr( 0.f, v - 0.2f );
+            float& q = vort[(size_t)n];
+            q -= q * dis;
+            q = fmaxr( v, q );
+        }
+        normalToComp();
+        curvatureToPres();
+#pragma omp parallel for schedule(static)
+        for( long long n = 0; n < np; ++n )
+        {
+            const V3 p = pos[(size_t)n];
+            curv[(size_t)n] = lerpS( pres, presBackground, p.x, p.y, p.z );
+        }
+        std::fill( pres.begin(), pres.end(), 0.f );
+        presBackground = 0.f;
+    }
+
+    void postProcess( float dt, float vort_pres_rate, int redist_iteration, bool literal_scan )
+    {
+        rebuild();  // FLIPMethod::prepareNextStep
+        splatSurface();
+        tankScan( literal_scan );
+        redistance( redist_iteration );
+        particleAttributes( dt, vort_pres_rate );
     }
 
     int step( float dt )
@@ -866,6 +1180,7 @@ void ora_set_particles( void* h, const float* pos, const float* vel, const int32
 {
     Oracle* o = (Oracle*)h;
     o->pos.resize( n ); o->vel.resize( n ); o->adj.assign( n, 0.f ); o->pid.resize( n );
+    o->vort.assign( n, 0.f ); o->curv.assign( n, 0.f );
     for( size_t i = 0; i < n; ++i )
     {
         o->pos[i] = V3{ pos[3 * i], pos[3 * i + 1], pos[3 * i + 2] };
@@ -906,6 +1221,8 @@ size_t ora_fill_water_tank( void* h, int per_cell )
         o->vel.push_back( V3{ 0.f, 0.f, 0.f } );
         o->adj.push_back( 0.f );
         o->pid.push_back( next++ );
+        o->vort.push_back( 0.f );
+        o->curv.push_back( 0.f );
     };
     for( int k = 0; k < nz; ++k )
         for( int j = 0; j < hh; ++j )
@@ -970,6 +1287,41 @@ void ora_update_particles( void* h, float dt ) { ( (Oracle*)h )->updateParticles
 void ora_compact( void* h ) { ( (Oracle*)h )->compact(); }
 int ora_step( void* h, float dt ) { return ( (Oracle*)h )->step( dt ); }
 double ora_last_rel( void* h ) { return ( (Oracle*)h )->lastRel; }
+
+// FLIPMethod::postProcess and its parts. flags: bit 0 = the reference's tank scan as
+// executed (see tankScan).
+void ora_post_process( void* h, float dt, float vort_pres_rate, int redist_iteration, int flags )
+{
+    ( (Oracle*)h )->postProcess( dt, vort_pres_rate, redist_iteration, flags & 1 );
+}
+void ora_post_splat( void* h ) { ( (Oracle*)h )->splatSurface(); }
+void ora_post_tank_scan( void* h, int literal ) { ( (Oracle*)h )->tankScan( literal != 0 ); }
+void ora_post_redistance( void* h, int iters ) { ( (Oracle*)h )->redistance( iters ); }
+void ora_post_attributes( void* h, float dt, float vort_pres_rate ) { ( (Oracle*)h )->particleAttributes( dt, vort_pres_rate ); }
+
+// Particle vorticity and curvature, in particle order (any pointer may be NULL).
+void ora_get_attributes( void* h, float* vort, float* curv )
+{
+    Oracle* o = (Oracle*)h;
+    const size_t n = o->pos.size();
+    for( size_t i = 0; i < n; ++i )
+    {
+        if( vort ) vort[i] = i < o->vort.size() ? o->vort[i] : 0.f;
+        if( curv ) curv[i] = i < o->curv.size() ? o->curv[i] : 0.f;
+    }
+}
+void ora_set_attributes( void* h, const float* vort, const float* curv )
+{
+    Oracle* o = (Oracle*)h;
+    const size_t n = o->pos.size();
+    o->vort.assign( n, 0.f );
+    o->curv.assign( n, 0.f );
+    for( size_t i = 0; i < n; ++i )
+    {
+        if( vort ) o->vort[i] = vort[i];
+        if( curv ) o->curv[i] = curv[i];
+    }
+}
 
 // out: fx, fy, fz, block, frame nx, ny, nz, active tiles
 void ora_frame_info( void* h, int64_t* out )

@@ -149,6 +149,27 @@ void ref_step( void* h, float dt )
     s->flip.advanceOneStep( s->pts, dt );
 }
 
+// FLIPMethod::postProcess (FLIPMethod.cu:300-405) on the reference's own code, in voxel
+// space (advanceOneFrame calls it before particlesToWorld).
+void ref_post_process( void* h )
+{
+    RefSim* s = (RefSim*)h;
+    if( s->pts.position.size() == 0 ) return;
+    s->flip.postProcess( s->pts );
+}
+
+// Particle vorticity and curvature (Particles::vorticity / ::curvature).
+void ref_get_attributes( void* h, float* vort, float* curv )
+{
+    RefSim* s = (RefSim*)h;
+    const size_t n = s->pts.position.size();
+    for( size_t i = 0; i < n; ++i )
+    {
+        if( vort ) vort[i] = s->pts.vorticity[i];
+        if( curv ) curv[i] = s->pts.curvature[i];
+    }
+}
+
 size_t ref_num_particles( void* h ) { return ((RefSim*)h)->pts.position.size(); }
 
 void ref_get_particles( void* h, float* pos, float* vel, float* adj )

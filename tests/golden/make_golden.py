@@ -19,7 +19,15 @@ Fixtures:
                           damping band 0.1): FLIPMethod::fillWaterTank's particles, then 3
                           steps with the reference CG rule: per-step SHA-256 and counts.
 
-Usage: OMP_NUM_THREADS=1 python tests/golden/make_golden.py
+  ref_post_small20.npz    20^3 dam break + sphere (dt 1/60) set swirling (6 rad/s about
+                          the vertical axis), two frames of step +
+                          FLIPMethod::postProcess (redistIteration 80, vortPresRate 0.2):
+                          per-frame SHA-256 of the surface, normal and velocity fields and
+                          the particles' vorticity and curvature; final arrays.
+  ref_post_bubble32.npz   32^3 water tank with an enclosed air bubble (vare_gb300.scenes.
+                          tank_bubble), one postProcess: the tank's scan fills the bubble.
+
+Usage: OMP_NUM_THREADS=1 python tests/golden/make_golden.py [fixture ...]
 """
 from __future__ import annotations
 
@@ -156,9 +164,55 @@ def tank24():
     print("tank24", added, counts, ntiles)
 
 
+def _post_record(ref):
+    surf = ref.field(B.FIELD_SURF)
+    comp = ref.field(B.FIELD_COMP)
+    velo = ref.field(B.FIELD_VELO)
+    vort, curv = ref.attributes()
+    return surf, comp, velo, vort, curv
+
+
+def swirl(sc, omega: float = 6.0):
+    """The scene with particles rotating about the vertical axis through the box centre
+    (omega rad/s, voxel units), so that the vorticity threshold (0.2 world units) is
+    exceeded."""
+    c = np.array(sc.res, np.float32) * 0.5
+    d = sc.pos - c
+    vel = np.zeros_like(sc.pos)
+    vel[:, 0] = -omega * d[:, 2]
+    vel[:, 2] = omega * d[:, 0]
+    sc.vel = vel.astype(np.float32)
+    return sc
+
+
+def post_small20():
+    sc = swirl(scenes.small(20, dt=1.0 / 60.0))
+    ref = B.RefSim(sc)
+    hashes = []
+    for f in range(2):
+        ref.step(sc.dt)
+        ref.post_process()
+        hashes.append(sha(*_post_record(ref)))
+    surf, comp, velo, vort, curv = _post_record(ref)
+    pos, vel, adj = ref.particles()
+    np.savez_compressed(os.path.join(HERE, "ref_post_small20.npz"), hashes=np.array(hashes), surf=surf, comp=comp,
+                        velo=velo, vort=vort, curv=curv, pos=pos, tiles=ref.tiles(), dt=sc.dt)
+    print("post_small20", hashes[-1][:16], float(np.abs(vort).max()), float(np.abs(curv).max()))
+
+
+def post_bubble32():
+    sc = scenes.tank_bubble(32)
+    ref = B.RefSim(sc, tank=True)
+    ref.post_process()
+    surf, comp, velo, vort, curv = _post_record(ref)
+    np.savez_compressed(os.path.join(HERE, "ref_post_bubble32.npz"), hash=sha(surf, comp, velo, vort, curv),
+                        surf=surf, vort=vort, curv=curv, tiles=ref.tiles(), wall_level=sc.wall_level, dt=sc.dt)
+    print("post_bubble32", int(np.sum(surf < 0)), float(np.abs(curv).max()))
+
+
 if __name__ == "__main__":
     if not B.reference_available():
         B.build(ref=True)
-    which = sys.argv[1:] or ["small20", "small24_cg64", "dam64", "tank24"]
+    which = sys.argv[1:] or ["small20", "small24_cg64", "dam64", "tank24", "post_small20", "post_bubble32"]
     for name in which:
         globals()[name]()

@@ -1,0 +1,247 @@
+"""Post-processing (FLIPMethod::postProcess) on the GPU against the CPU oracle, through
+the C ABI.
+
+Each stage gets identical inputs on both sides. The splat's sums are added in a
+different order (shared-memory and global atomics on the device, particle order in the
+oracle), so its fields are compared with a tolerance; the water tank's scan, the
+redistancing, the curl / normal / curvature fields and the particles' vorticity and
+curvature are order-independent and must agree bit for bit. The oracle restatement is
+pinned to the reference's own postProcess by tests/test_oracle_post.py.
+"""
+import numpy as np
+import pytest
+
+from test_oracle_post import swirl
+from vare_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-5
+
+
+def rel_err(a, b) -> float:
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    den = np.abs(b).max() if b.size else 0.0
+    return float(np.abs(a - b).max() / den) if den > 0 else float(np.abs(a - b).max())
+
+
+def real_cells(tiles, nx, ny, nz) -> np.ndarray:
+    l = np.arange(512)
+    i = tiles[:, 0:1] * 8 + (l & 7)[None, :]
+    j = tiles[:, 1:2] * 8 + ((l >> 3) & 7)[None, :]
+    k = tiles[:, 2:3] * 8 + (l >> 6)[None, :]
+    return ((i < nx) & (j < ny) & (k < nz)).reshape(-1)
+
+
+CASES = ["swirl_20", "swirl_padded_22", "bubble_32"]
+
+
+def make_case(name):
+    if name == "swirl_20":
+        return swirl(scenes.small(20, dt=1.0 / 60.0)), False
+    if name == "swirl_padded_22":
+        return swirl(scenes.small(22, seed=3), omega=4.0), False
+    return scenes.tank_bubble(32), True
+
+
+def pair(gpu, B, sc, tank, **kw):
+    if tank:
+        kw["enable_water_tank"] = 1
+    sim = gpu.FlipSim.from_scene(sc, **kw)
+    ora = B.Oracle(sc, block=8, threads=1, tank=tank)
+    return sim, ora
+
+
+def splat_both(gpu, sim, ora):
+    sim.run_stage(gpu.STAGE_REBUILD)
+    sim.run_post_stage(gpu.POST_SPLAT)
+    ora.rebuild()
+    ora.post_splat()
+    tiles = sim.tiles()
+    np.testing.assert_array_equal(tiles, ora.tiles())
+    fi = sim.frame_info()
+    return real_cells(tiles, fi["nx"], fi["ny"], fi["nz"])
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_splat_matches_oracle(gpu, oracle_lib, name):
+    B = oracle_lib
+    sc, tank = make_case(name)
+    sim, ora = pair(gpu, B, sc, tank)
+    real = splat_both(gpu, sim, ora)
+    wg, wo = sim.field(gpu.FIELD_PRES)[real], ora.field(B.FIELD_PRES)[real]
+    assert rel_err(wg, wo) <= TOL
+    sg, so = sim.field(gpu.FIELD_SURF)[real], ora.field(B.FIELD_SURF)[real]
+    np.testing.assert_array_equal(wg == 0, wo == 0)
+    assert np.all(sg[wo == 0] == 5.0)
+    # the mean position carries float rounding of coordinates up to the grid size
+    assert np.abs(sg - so).max() <= 2e-6 * max(sc.res)  # voxel units
+    assert rel_err(sim.field(gpu.FIELD_VELO)[real], ora.field(B.FIELD_VELO)[real]) <= TOL
+    assert rel_err(sim.field(gpu.FIELD_COMP)[real], ora.field(B.FIELD_COMP)[real]) <= TOL
+
+
+def copy_fields(gpu, B, sim, ora, which):
+    names = {B.FIELD_SURF: gpu.FIELD_SURF, B.FIELD_VELO: gpu.FIELD_VELO, B.FIELD_PRES: gpu.FIELD_PRES,
+             B.FIELD_COMP: gpu.FIELD_COMP}
+    for w in which:
+        sim.set_field(names[w], ora.field(w))
+
+
+def test_tank_scan_bit_exact_bubble(gpu, oracle_lib):
+    B = oracle_lib
+    sc, _ = make_case("bubble_32")
+    sim, ora = pair(gpu, B, sc, True)
+    real = splat_both(gpu, sim, ora)
+    copy_fields(gpu, B, sim, ora, [B.FIELD_SURF])
+    before = ora.field(B.FIELD_SURF)
+    sim.run_post_stage(gpu.POST_TANK_SCAN)
+    ora.post_tank_scan(False)
+    after = ora.field(B.FIELD_SURF)
+    np.testing.assert_array_equal(sim.field(gpu.FIELD_SURF)[real], after[real])
+    assert np.sum((after == -5) & (before > 0)) > 100  # the bubble is filled
+
+
+@pytest.mark.parametrize("density", [0.3, 0.45, 0.6])
+def test_tank_scan_bit_exact_random_air(gpu, oracle_lib, density):
+    """Random air patterns (thin passages, many components) over a 32^3 grid whose slab
+    (rows 0..13) also holds inactive tiles, which the scan reads as air."""
+    B = oracle_lib
+    sc = scenes.dam_break(32, (0.25, 0.3), seed=5, ppc=1)
+    sc.wall_level = 13.5 / 32
+    sim, ora = pair(gpu, B, sc, True)
+    sim.run_stage(gpu.STAGE_REBUILD)
+    ora.rebuild()
+    tiles = sim.tiles()
+    np.testing.assert_array_equal(tiles, ora.tiles())
+    fi = sim.frame_info()
+    assert len(tiles) < fi["tx"] * fi["ty"] * fi["tz"]
+    real = real_cells(tiles, fi["nx"], fi["ny"], fi["nz"])
+    for seed in range(3):
+        rng = np.random.default_rng(1000 + seed)
+        surf = np.where(rng.random(len(real)) < density, 1.0, -1.0).astype(np.float32)
+        sim.set_field(gpu.FIELD_SURF, surf)
+        ora.set_field(B.FIELD_SURF, surf)
+        sim.run_post_stage(gpu.POST_TANK_SCAN)
+        ora.post_tank_scan(False)
+        got, want = sim.field(gpu.FIELD_SURF)[real], ora.field(B.FIELD_SURF)[real]
+        np.testing.assert_array_equal(got, want)
+        assert np.sum(want == -5) > 0
+
+
+@pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("iters", [80, 7])
+def test_redistance_bit_exact(gpu, oracle_lib, name, iters):
+    B = oracle_lib
+    sc, tank = make_case(name)
+    sim, ora = pair(gpu, B, sc, tank, redist_iteration=iters)
+    real = splat_both(gpu, sim, ora)
+    copy_fields(gpu, B, sim, ora, [B.FIELD_SURF])
+    sim.run_post_stage(gpu.POST_REDISTANCE)
+    ora.post_redistance(iters)
+    np.testing.assert_array_equal(sim.field(gpu.FIELD_SURF)[real], ora.field(B.FIELD_SURF)[real])
+    np.testing.assert_array_equal(sim.field(gpu.FIELD_PRES)[real], ora.field(B.FIELD_PRES)[real])
+
+
+def by_id(ids, *arrays):
+    o = np.argsort(ids)
+    return [a[o] for a in arrays]
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_attributes_bit_exact(gpu, oracle_lib, name):
+    B = oracle_lib
+    sc, tank = make_case(name)
+    sim, ora = pair(gpu, B, sc, tank)
+    real = splat_both(gpu, sim, ora)
+    ora.post_redistance(80)
+    copy_fields(gpu, B, sim, ora, [B.FIELD_SURF, B.FIELD_VELO])
+    # identical starting vorticity / curvature, matched by particle id
+    _, _, _, gid = sim.particles()
+    _, _, _, oid = ora.particles()
+    rng = np.random.default_rng(7)
+    v0 = rng.random(sc.num_particles).astype(np.float32)
+    c0 = rng.random(sc.num_particles).astype(np.float32)
+    sim.set_particle_attributes(v0[gid], c0[gid])
+    ora.set_attributes(v0[oid], c0[oid])
+    sim.run_post_stage(gpu.POST_ATTRIBUTES)
+    ora.post_attributes(sc.dt, 0.2)
+    np.testing.assert_array_equal(sim.field(gpu.FIELD_COMP)[real], ora.field(B.FIELD_COMP)[real])
+    assert not np.any(sim.field(gpu.FIELD_PRES))
+    gv, gc, gids = sim.particle_attributes()
+    ov, oc = ora.attributes()
+    gv, gc = by_id(gids, gv, gc)
+    ov, oc = by_id(oid, ov, oc)
+    np.testing.assert_array_equal(gv, ov)
+    np.testing.assert_array_equal(gc, oc)
+    assert np.any(gv != v0[np.sort(gids)])  # the stage changed something
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_post_process_matches_oracle(gpu, oracle_lib, name):
+    """The whole pipeline from identical particles. Only the splat's summation order
+    differs, and the redistancing amplifies that rounding near the surface (the update's
+    sign factor grows perturbations while |grad phi| is far from 1): the oracle run on the
+    same particles in permuted orders spreads by up to about 0.01 voxel in the distance and
+    0.01 in curvature (tests/test_oracle_post.py::test_post_order_spread), so the bounds
+    here are of that size. Vorticity comes from the smooth splatted velocity and agrees
+    closely."""
+    B = oracle_lib
+    sc, tank = make_case(name)
+    sim, ora = pair(gpu, B, sc, tank)
+    sim.post_process()
+    ora.post_process(sc.dt)
+    tiles = sim.tiles()
+    np.testing.assert_array_equal(tiles, ora.tiles())
+    fi = sim.frame_info()
+    real = real_cells(tiles, fi["nx"], fi["ny"], fi["nz"])
+    sg, so = sim.field(gpu.FIELD_SURF)[real], ora.field(B.FIELD_SURF)[real]
+    assert np.abs(sg - so).max() <= 0.05
+    assert np.mean(np.abs(sg - so) > 1e-2) <= 0.01
+    np.testing.assert_array_equal(sg < -4, so < -4)  # the same cells filled by the tank's scan
+    gv, gc, gids = sim.particle_attributes()
+    _, _, _, oid = ora.particles()
+    ov, oc = ora.attributes()
+    gv, gc = by_id(gids, gv, gc)
+    ov, oc = by_id(oid, ov, oc)
+    assert np.abs(gv - ov).max() <= 1e-4
+    assert np.abs(gc - oc).max() <= 0.05
+
+
+def test_frame_runs_post_process_and_carries_attributes(gpu, oracle_lib):
+    """bora_flip_frame = step + post-processing (FLIPMethod::advanceOneFrame); vorticity
+    and curvature stay with their particles through the steps' reordering."""
+    B = oracle_lib
+    sc = swirl(scenes.small(20, dt=1.0 / 60.0))
+    sim = gpu.FlipSim.from_scene(sc, tolerance=1e-10, div_tolerance=1e-12, max_refinements=30,
+                                 inner_tolerance=1e-4)
+    ora = B.Oracle(sc, block=8, solver="fp64", tol=1e-13, threads=1)
+    for _ in range(3):
+        assert sim.advance_one_frame() == 0
+        ora.step(sc.dt)
+        ora.post_process(sc.dt)
+    gv, gc, gids = sim.particle_attributes()
+    _, _, _, oid = ora.particles()
+    ov, oc = ora.attributes()
+    np.testing.assert_array_equal(np.sort(gids), np.sort(oid))
+    gv, gc = by_id(gids, gv, gc)
+    ov, oc = by_id(oid, ov, oc)
+    assert np.abs(ov).max() > 0.5
+    assert rel_err(gv, ov) <= 1e-3
+    # a plain step carries the attributes with the particles
+    rng = np.random.default_rng(3)
+    _, _, _, pid = sim.particles()
+    v = rng.random(len(pid)).astype(np.float32)
+    c = rng.random(len(pid)).astype(np.float32)
+    sim.set_particle_attributes(v, c)
+    want = dict(zip(pid.tolist(), zip(v.tolist(), c.tolist())))
+    assert sim.step(sc.dt) == 0
+    gv, gc, gids = sim.particle_attributes()
+    got = np.array([want[i] for i in gids.tolist()], np.float32)
+    np.testing.assert_array_equal(gv, got[:, 0])
+    np.testing.assert_array_equal(gc, got[:, 1])
+    # new particles start at zero
+    sim.add_particles(np.full((4, 3), 5.5, np.float32), space=gpu.SPACE_VOXEL)
+    gv, gc, gids = sim.particle_attributes()
+    newest = np.argsort(gids)[-4:]
+    assert not np.any(gv[newest]) and not np.any(gc[newest])

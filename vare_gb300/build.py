@@ -21,7 +21,8 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libbora_flip.so")
 
-SOURCES = ["scan.cu", "grid_build.cu", "p2g.cu", "projection.cu", "multigrid.cu", "g2p.cu", "flip_api.cu", "serve.cu"]
+SOURCES = ["scan.cu", "grid_build.cu", "p2g.cu", "projection.cu", "multigrid.cu", "g2p.cu", "surface.cu", "flip_api.cu",
+           "serve.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC",
               "--expt-relaxed-constexpr", "-Xcudafe", "--diag_suppress=177"]

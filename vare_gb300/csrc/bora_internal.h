@@ -52,6 +52,8 @@ struct BoraParticlesDev
     float* vy;
     float* vz;
     int32_t* id;  // < 0: killed in the last step
+    float* vort;  // Particles::vorticity / ::curvature (post-processing), or null while unused
+    float* curv;
 };
 
 // ---- cell fields over active slots x 512 ----------------------------------------------
@@ -113,6 +115,21 @@ void bora_launch_vel_update( const BoraGridDev& g, int ntiles, BoraTilesDev t, B
 void bora_launch_g2p( const BoraGridDev& g, int ntiles, size_t nsorted, BoraTilesDev t, const uint32_t* start, BoraCellsDev c,
                       BoraParticlesDev src, const uint32_t* idx, BoraParticlesDev dst, float* adj, float dt,
                       uint32_t* nkilled, cudaStream_t st );
+// ---- post-processing (FLIPMethod::postProcess) ------------------------------------------
+void bora_launch_splat( const BoraGridDev& g, int ntiles, BoraTilesDev t, const uint32_t* start, const uint32_t* idx,
+                        BoraParticlesDev p, BoraCellsDev c, cudaStream_t st );
+// labels: ntiles * 512 + tiles-table entries; returns the number of kernels launched
+int bora_tank_scan_launches( const BoraGridDev& g, int ntiles, BoraTilesDev t, float* surf, uint32_t* labels,
+                             uint32_t* err, cudaStream_t st );
+cudaError_t bora_launch_redistance( const BoraGridDev& g, int ntiles, BoraTilesDev t, const float* in, float* out,
+                                    cudaStream_t st );
+// curl of velo -> (wx, wy, wz); normals of surf -> comp; curvature of the normals -> pres
+void bora_launch_surface_fields( const BoraGridDev& g, int ntiles, BoraTilesDev t, BoraCellsDev c, float* wx, float* wy,
+                                 float* wz, cudaStream_t st );
+void bora_launch_particle_attributes( const BoraGridDev& g, const int32_t* slot_of, size_t np, BoraParticlesDev p,
+                                      const float* wx, const float* wy, const float* wz, const float* curvature,
+                                      float3 scale, float dis, cudaStream_t st );
+
 void bora_launch_to_soa( size_t n, const float* pos, const float* vel, int space, const float* translate,
                          const float* scale, BoraParticlesDev p, size_t offset, int32_t first_id, cudaStream_t st );
 

@@ -75,6 +75,31 @@ __global__ void k_gather_live( size_t n, BoraParticlesDev p, const float* __rest
     }
 }
 
+// Particle vorticity / curvature of live particles, in the same order.
+__global__ void k_gather_attrs( size_t n, BoraParticlesDev p, const uint32_t* __restrict__ excl, float* __restrict__ vort,
+                                float* __restrict__ curv, int32_t* __restrict__ ids )
+{
+    for( size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x )
+    {
+        if( p.id[i] < 0 ) continue;
+        const size_t o = excl[i];
+        vort[o] = p.vort ? p.vort[i] : 0.f;
+        curv[o] = p.curv ? p.curv[i] : 0.f;
+        ids[o] = p.id[i];
+    }
+}
+
+__global__ void k_scatter_attrs( size_t n, BoraParticlesDev p, const uint32_t* __restrict__ excl,
+                                 const float* __restrict__ vort, const float* __restrict__ curv )
+{
+    for( size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x )
+    {
+        if( p.id[i] < 0 ) continue;
+        p.vort[i] = vort[excl[i]];
+        p.curv[i] = curv[excl[i]];
+    }
+}
+
 int grid_blocks( size_t n )
 {
     const size_t b = ( n + 255 ) / 256;
@@ -116,6 +141,9 @@ struct bora_flip_sim
 
     // particles
     DevBuf pbuf[2][7];  // px py pz vx vy vz id
+    DevBuf pattr[2][2]; // vorticity, curvature (allocated by the first post-processing)
+    bool attrs = false;
+    DevBuf labels;      // post-processing: union-find labels of the water tank's scan
     DevBuf adj, vkey, key, idx;
     size_t cap_p = 0;
     size_t np = 0;      // particles in the current buffer (killed ones included until the next sort)
@@ -170,7 +198,8 @@ struct bora_flip_sim
     {
         return BoraParticlesDev{ P<float>( pbuf[b][0] ), P<float>( pbuf[b][1] ), P<float>( pbuf[b][2] ),
                                  P<float>( pbuf[b][3] ), P<float>( pbuf[b][4] ), P<float>( pbuf[b][5] ),
-                                 P<int32_t>( pbuf[b][6] ) };
+                                 P<int32_t>( pbuf[b][6] ), attrs ? P<float>( pattr[b][0] ) : nullptr,
+                                 attrs ? P<float>( pattr[b][1] ) : nullptr };
     }
     BoraCellsDev cells()
     {
@@ -312,6 +341,9 @@ int ensure_particles( bora_flip_sim* s, size_t n )
     const size_t cap = std::max( n, s->cap_p + s->cap_p / 2 );
     for( int b = 0; b < 2; ++b )
         for( int a = 0; a < 7; ++a ) BORA_TRY( grow( s->pbuf[b][a], cap * 4, b == s->cur, s->st ) );
+    if( s->attrs )
+        for( int b = 0; b < 2; ++b )
+            for( int a = 0; a < 2; ++a ) BORA_TRY( grow( s->pattr[b][a], cap * 4, b == s->cur, s->st ) );
     BORA_TRY( grow( s->adj, cap * 4, true, s->st ) );
     BORA_TRY( grow( s->vkey, cap * 4, false, s->st ) );
     BORA_TRY( grow( s->key, cap * 4, false, s->st ) );
@@ -667,6 +699,103 @@ int stage_update_particles( bora_flip_sim* s, float dt )
     return BORA_OK;
 }
 
+// ---- post-processing (FLIPMethod::postProcess, FLIPMethod.cu:300-405) --------------------
+
+// Particle vorticity and curvature start at 0 for every particle (FLIPMethod.h:94-96);
+// from the first post-processing on they are kept in both particle buffers.
+int ensure_attrs( bora_flip_sim* s )
+{
+    if( s->attrs ) return BORA_OK;
+    for( int b = 0; b < 2; ++b )
+        for( int a = 0; a < 2; ++a ) BORA_TRY( grow( s->pattr[b][a], std::max<size_t>( s->cap_p, 1 ) * 4, false, s->st ) );
+    for( int a = 0; a < 2; ++a )
+        if( s->np ) BORA_TRY( cudaMemsetAsync( s->pattr[s->cur][a].p, 0, s->np * 4, s->st ) );
+    s->attrs = true;
+    return BORA_OK;
+}
+
+// Rasterization::ParticlesToSurfaceAndVelocity (Rasterization.cu:311-398).
+int post_splat( bora_flip_sim* s )
+{
+    if( !s->sorted ) return BORA_ERR_INVALID_ARG;
+    cudaStream_t st = s->st;
+    const size_t nc = (size_t)s->ntiles * BORA_TILE_CELLS;
+    if( nc == 0 ) return BORA_OK;
+    DevBuf* zero[] = { &s->surf, &s->cx, &s->cy, &s->cz, &s->vx, &s->vy, &s->vz };
+    for( DevBuf* b : zero ) BORA_TRY( cudaMemsetAsync( b->p, 0, nc * 4, st ) );
+    KTimer t( s, BORA_KERNEL_POST, 2 );
+    bora_launch_splat( s->g, s->ntiles, s->tiles(), P<uint32_t>( s->cell_start ), P<uint32_t>( s->idx ), s->parts( s->cur ),
+                       s->cells(), st );
+    return check_launch( s );
+}
+
+// The water tank's fill of enclosed air pockets (FLIPMethod.cu:322-366).
+int post_tank_scan( bora_flip_sim* s )
+{
+    if( !s->prm.enable_water_tank || s->ntiles <= 0 || !( s->g.voxel_wall >= 0.f ) ) return BORA_OK;
+    const size_t nn = (size_t)s->ntiles * BORA_TILE_CELLS + s->ntv;
+    if( nn >= ( (size_t)1 << 31 ) ) return BORA_ERR_CAPACITY;
+    BORA_TRY( grow( s->labels, nn * 4, false, s->st ) );
+    BORA_TRY( cudaMemsetAsync( P<uint32_t>( s->counters ) + 8, 0, 4, s->st ) );
+    {
+        KTimer t( s, BORA_KERNEL_POST, 6 );
+        bora_tank_scan_launches( s->g, s->ntiles, s->tiles(), P<float>( s->surf ), P<uint32_t>( s->labels ),
+                                 P<uint32_t>( s->counters ) + 8, s->st );
+    }
+    BORA_TRYS( check_launch( s ) );
+    BORA_TRYS( read_counters( s, 8, 1 ) );
+    return s->h_cnt[8] ? BORA_ERR_INTERNAL : BORA_OK;
+}
+
+// Rasterization::ReinitializeSurface (Rasterization.cu:400-486): surf and pres swap
+// storage after every step, as the reference swaps the fields' pointers.
+int post_redistance( bora_flip_sim* s )
+{
+    if( s->ntiles <= 0 ) return BORA_OK;
+    const int iters = std::max( 0, s->prm.redist_iteration );
+    KTimer t( s, BORA_KERNEL_POST, iters );
+    for( int it = 0; it < iters; ++it )
+    {
+        BORA_TRY( bora_launch_redistance( s->g, s->ntiles, s->tiles(), P<float>( s->surf ), P<float>( s->pres ), s->st ) );
+        std::swap( s->surf, s->pres );
+    }
+    return check_launch( s );
+}
+
+// FLIPMethod.cu:370-404: curl, normals and curvature, the particles' vorticity and
+// curvature, then pres cleared.
+int post_attributes( bora_flip_sim* s )
+{
+    BORA_TRYS( ensure_attrs( s ) );
+    cudaStream_t st = s->st;
+    const size_t nc = (size_t)s->ntiles * BORA_TILE_CELLS;
+    float* wx = P<float>( s->sd0 );
+    float* wy = P<float>( s->sd1 );
+    float* wz = P<float>( s->sq );
+    // FLIPMethod.cu:376, on the host as the reference computes it
+    const float dis = powf( 1.f - s->prm.vort_pres_rate, s->prm.dt );
+    {
+        KTimer t( s, BORA_KERNEL_POST, ( s->ntiles > 0 ? 2 : 0 ) + ( s->np > 0 ? 1 : 0 ) );
+        bora_launch_surface_fields( s->g, s->ntiles, s->tiles(), s->cells(), wx, wy, wz, st );
+        if( s->ntiles > 0 )
+            bora_launch_particle_attributes( s->g, P<int32_t>( s->slot_of ), s->np, s->parts( s->cur ), wx, wy, wz,
+                                             P<float>( s->pres ), make_float3( s->scale[0], s->scale[1], s->scale[2] ),
+                                             dis, st );
+    }
+    if( nc ) BORA_TRY( cudaMemsetAsync( s->pres.p, 0, nc * 4, st ) );
+    return check_launch( s );
+}
+
+int post_process( bora_flip_sim* s )
+{
+    BORA_TRYS( stage_rebuild( s ) );  // FLIPMethod::prepareNextStep
+    BORA_TRYS( post_splat( s ) );
+    BORA_TRYS( post_tank_scan( s ) );
+    BORA_TRYS( post_redistance( s ) );
+    BORA_TRYS( post_attributes( s ) );
+    return BORA_OK;
+}
+
 int add_particles( bora_flip_sim* s, const float* pos, const float* vel, size_t n, int space )
 {
     if( n == 0 ) return BORA_OK;
@@ -682,6 +811,8 @@ int add_particles( bora_flip_sim* s, const float* pos, const float* vel, size_t 
     bora_launch_to_soa( n, dpos, vel ? dvel : nullptr, space == BORA_SPACE_VOXEL ? 1 : 0, s->translate, s->scale,
                         s->parts( s->cur ), s->np, s->next_id, s->st );
     BORA_TRY( cudaMemsetAsync( P<float>( s->adj ) + s->np, 0, n * 4, s->st ) );
+    if( s->attrs )  // FLIPMethod::newParticle appends vorticity and curvature 0 (FLIPMethod.h:94-96)
+        for( int a = 0; a < 2; ++a ) BORA_TRY( cudaMemsetAsync( P<float>( s->pattr[s->cur][a] ) + s->np, 0, n * 4, s->st ) );
     BORA_TRYS( check_launch( s ) );
     BORA_TRY( cudaStreamSynchronize( s->st ) );  // the caller may free its buffers on return
     s->np += n;
@@ -706,7 +837,11 @@ void for_each_buffer( bora_flip_sim* s, F&& f )
                       &s->counters, &s->stage_in, &s->stage_out, &s->live_flag, &s->col_phi, &s->col_vel };
     for( DevBuf* b : all ) f( *b );
     for( int q = 0; q < 2; ++q )
+    {
         for( int a = 0; a < 7; ++a ) f( s->pbuf[q][a] );
+        for( int a = 0; a < 2; ++a ) f( s->pattr[q][a] );
+    }
+    f( s->labels );
     for( int l = 0; l < bora_flip_sim::kMaxLevels; ++l )
     {
         f( s->mg_type[l] ); f( s->mg_code[l] ); f( s->mg_r[l] );
@@ -741,6 +876,7 @@ int bora_flip_default_params( bora_flip_params* o )
     o->max_refinements = 8;
     o->check_every = 1;
     o->advection = BORA_ADVECT_EULER;
+    o->post_process = 1;
     return BORA_OK;
 }
 
@@ -830,6 +966,7 @@ int bora_flip_set_params( bora_flip_handle s, const bora_flip_params* p )
     BORA_TRYS( validate_params( p ) );
     s->prm = *p;
     apply_params( s );
+    s->sorted = false;  // the water tank's rows change the activation
     return BORA_OK;
 }
 
@@ -868,6 +1005,8 @@ int bora_flip_fill_water_tank( bora_flip_handle s, size_t* added )
     s->stats.kernel_launches += 1;
     bora_launch_tank( s->g, hh, per_cell, tr, sc, count, offset, s->parts( s->cur ), s->np, s->next_id, true, st );
     BORA_TRY( cudaMemsetAsync( P<float>( s->adj ) + s->np, 0, n * 4, st ) );
+    if( s->attrs )
+        for( int a = 0; a < 2; ++a ) BORA_TRY( cudaMemsetAsync( P<float>( s->pattr[s->cur][a] ) + s->np, 0, n * 4, st ) );
     BORA_TRYS( check_launch( s ) );
     BORA_TRY( cudaStreamSynchronize( st ) );
     s->np += n;
@@ -886,6 +1025,7 @@ int bora_flip_clear_particles( bora_flip_handle s )
     s->nlive = 0;
     s->next_id = 0;
     s->sorted = false;
+    s->attrs = false;
     s->stats.num_particles = 0;
     return BORA_OK;
 }
@@ -960,7 +1100,9 @@ int bora_flip_step( bora_flip_handle s, float dt )
     if( s->np == 0 ) return BORA_OK;  // FLIPMethod.cu:179
     const auto t0 = std::chrono::steady_clock::now();
     cudaEventRecord( s->ev_step[0], s->st );
-    BORA_TRYS( stage_rebuild( s ) );
+    // FLIPMethod.cu:210: the frame is rebuilt unless post-processing has just built it
+    // from these particles (prepareNextStep)
+    if( !s->sorted ) BORA_TRYS( stage_rebuild( s ) );
     BORA_TRYS( stage_p2g( s ) );
     BORA_TRYS( stage_build_system( s ) );
     const int solve = stage_solve( s );
@@ -981,7 +1123,92 @@ int bora_flip_step( bora_flip_handle s, float dt )
 int bora_flip_frame( bora_flip_handle s )
 {
     if( !s ) return BORA_ERR_INVALID_ARG;
-    return bora_flip_step( s, s->prm.dt );
+    const int st = bora_flip_step( s, s->prm.dt );
+    if( st < 0 || !s->prm.post_process ) return st;
+    BORA_TRYS( bora_flip_post_process( s ) );
+    return st;
+}
+
+int bora_flip_post_process( bora_flip_handle s )
+{
+    if( !s ) return BORA_ERR_INVALID_ARG;
+    if( s->np == 0 ) return BORA_OK;
+    BORA_TRYS( post_process( s ) );
+    BORA_TRY( cudaStreamSynchronize( s->st ) );
+    s->prof_resolve();
+    return BORA_OK;
+}
+
+int bora_flip_run_post_stage( bora_flip_handle s, int stage )
+{
+    if( !s ) return BORA_ERR_INVALID_ARG;
+    int st = BORA_ERR_INVALID_ARG;
+    switch( stage )
+    {
+        case BORA_POST_SPLAT: st = post_splat( s ); break;
+        case BORA_POST_TANK_SCAN: st = post_tank_scan( s ); break;
+        case BORA_POST_REDISTANCE: st = post_redistance( s ); break;
+        case BORA_POST_ATTRIBUTES: st = post_attributes( s ); break;
+        default: return BORA_ERR_INVALID_ARG;
+    }
+    BORA_TRYS( st );
+    BORA_TRY( cudaStreamSynchronize( s->st ) );
+    s->prof_resolve();
+    return BORA_OK;
+}
+
+int bora_flip_get_particle_attributes( bora_flip_handle s, float* vorticity, float* curvature, int32_t* ids, size_t cap,
+                                       size_t* n )
+{
+    if( !s ) return BORA_ERR_INVALID_ARG;
+    if( cap < s->nlive && ( vorticity || curvature || ids ) ) return BORA_ERR_CAPACITY;
+    if( n ) *n = s->nlive;
+    if( s->np == 0 ) return BORA_OK;
+    cudaStream_t st = s->st;
+    const size_t np = s->np, nl = s->nlive;
+    BORA_TRYS( ensure_scan_scratch( s, std::max( np + 1, std::max( s->ntv, s->cap_tiles * BORA_TILE_CELLS + 2 ) ) ) );
+    BORA_TRY( grow( s->stage_out, nl * 12 + 64, false, st ) );
+    float* ov = P<float>( s->stage_out );
+    float* oc = ov + nl;
+    int32_t* oid = reinterpret_cast<int32_t*>( oc + nl );
+    BoraParticlesDev p = s->parts( s->cur );
+    s->stats.kernel_launches += 4;
+    k_live_flags<<<grid_blocks( np ), 256, 0, st>>>( np, p.id, P<uint32_t>( s->live_flag ) );
+    bora_device_scan( P<uint32_t>( s->live_flag ), P<uint32_t>( s->live_flag ), np, P<uint32_t>( s->scan_scratch ),
+                   P<uint32_t>( s->counters ) + 4, st );
+    k_gather_attrs<<<grid_blocks( np ), 256, 0, st>>>( np, p, P<uint32_t>( s->live_flag ), ov, oc, oid );
+    BORA_TRYS( check_launch( s ) );
+    if( vorticity ) BORA_TRY( cudaMemcpyAsync( vorticity, ov, nl * 4, cudaMemcpyDeviceToHost, st ) );
+    if( curvature ) BORA_TRY( cudaMemcpyAsync( curvature, oc, nl * 4, cudaMemcpyDeviceToHost, st ) );
+    if( ids ) BORA_TRY( cudaMemcpyAsync( ids, oid, nl * 4, cudaMemcpyDeviceToHost, st ) );
+    BORA_TRY( cudaStreamSynchronize( st ) );
+    return BORA_OK;
+}
+
+int bora_flip_set_particle_attributes( bora_flip_handle s, const float* vorticity, const float* curvature, size_t n )
+{
+    if( !s || n != s->nlive ) return BORA_ERR_INVALID_ARG;
+    BORA_TRYS( ensure_attrs( s ) );
+    if( s->np == 0 ) return BORA_OK;
+    cudaStream_t st = s->st;
+    const size_t np = s->np;
+    BORA_TRYS( ensure_scan_scratch( s, std::max( np + 1, std::max( s->ntv, s->cap_tiles * BORA_TILE_CELLS + 2 ) ) ) );
+    BORA_TRY( grow( s->stage_in, n * 8 + 64, false, st ) );
+    float* iv = P<float>( s->stage_in );
+    float* ic = iv + n;
+    if( vorticity ) BORA_TRY( cudaMemcpyAsync( iv, vorticity, n * 4, cudaMemcpyHostToDevice, st ) );
+    else BORA_TRY( cudaMemsetAsync( iv, 0, n * 4, st ) );
+    if( curvature ) BORA_TRY( cudaMemcpyAsync( ic, curvature, n * 4, cudaMemcpyHostToDevice, st ) );
+    else BORA_TRY( cudaMemsetAsync( ic, 0, n * 4, st ) );
+    BoraParticlesDev p = s->parts( s->cur );
+    s->stats.kernel_launches += 4;
+    k_live_flags<<<grid_blocks( np ), 256, 0, st>>>( np, p.id, P<uint32_t>( s->live_flag ) );
+    bora_device_scan( P<uint32_t>( s->live_flag ), P<uint32_t>( s->live_flag ), np, P<uint32_t>( s->scan_scratch ),
+                   P<uint32_t>( s->counters ) + 4, st );
+    k_scatter_attrs<<<grid_blocks( np ), 256, 0, st>>>( np, p, P<uint32_t>( s->live_flag ), iv, ic );
+    BORA_TRYS( check_launch( s ) );
+    BORA_TRY( cudaStreamSynchronize( st ) );  // the caller may free its buffers on return
+    return BORA_OK;
 }
 
 int bora_flip_num_particles( bora_flip_handle s, size_t* n )

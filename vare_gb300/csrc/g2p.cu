@@ -284,6 +284,11 @@ __global__ void __launch_bounds__( kG2PThreads, 4 ) k_g2p( const __grid_constant
         dst.px[q] = px; dst.py[q] = py; dst.pz[q] = pz;
         dst.vx[q] = vx; dst.vy[q] = vy; dst.vz[q] = vz;
         dst.id[q] = kill ? -1 : src.id[pi];
+        if( dst.vort )  // post-processing attributes ride along (FLIPMethod.cu:295-296)
+        {
+            dst.vort[q] = src.vort[pi];
+            dst.curv[q] = src.curv[pi];
+        }
         kills += kill ? 1u : 0u;
     };
     if( s == ntiles )

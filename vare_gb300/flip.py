@@ -25,9 +25,10 @@ SPACE_WORLD, SPACE_VOXEL = 0, 1
 SOLVER_PLAIN, SOLVER_MIXED = 0, 1
 ADVECT_EULER, ADVECT_RK2 = 0, 1
 STAGE_REBUILD, STAGE_P2G, STAGE_BUILD_SYSTEM, STAGE_SOLVE, STAGE_UPDATE_VELOCITY, STAGE_UPDATE_PARTICLES = range(6)
+POST_SPLAT, POST_TANK_SCAN, POST_REDISTANCE, POST_ATTRIBUTES = range(4)
 FIELD_MASS, FIELD_SURF, FIELD_PRES, FIELD_VELO, FIELD_COMP, FIELD_FLAG, FIELD_RHS, FIELD_CODE = range(8)
 KERNEL_CLASSES = ["bin", "tiles", "sort", "p2g", "rhs", "pcg_direction", "pcg_update", "refine", "velocity", "g2p",
-                  "mg_vcycle"]
+                  "mg_vcycle", "post"]
 _FIELD_DTYPE = {FIELD_MASS: (np.float32, 1), FIELD_SURF: (np.float32, 1), FIELD_PRES: (np.float32, 1),
                 FIELD_VELO: (np.float32, 3), FIELD_COMP: (np.float32, 3), FIELD_FLAG: (np.uint8, 1),
                 FIELD_RHS: (np.float32, 1), FIELD_CODE: (np.uint16, 1)}
@@ -52,7 +53,8 @@ class Params(ctypes.Structure):
                 ("adjacency_under", ctypes.c_float), ("proj_iteration", ctypes.c_int),
                 ("redist_iteration", ctypes.c_int), ("solver", ctypes.c_int), ("tolerance", ctypes.c_double),
                 ("div_tolerance", ctypes.c_double), ("inner_tolerance", ctypes.c_double),
-                ("max_refinements", ctypes.c_int), ("check_every", ctypes.c_int), ("advection", ctypes.c_int)]
+                ("max_refinements", ctypes.c_int), ("check_every", ctypes.c_int), ("advection", ctypes.c_int),
+                ("post_process", ctypes.c_int)]
 
 
 class Stats(ctypes.Structure):
@@ -92,6 +94,11 @@ _SIGS = {
     "bora_flip_step": (ctypes.c_int, [_vp, ctypes.c_float]),
     "bora_flip_frame": (ctypes.c_int, [_vp]),
     "bora_flip_run_stage": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_float]),
+    "bora_flip_post_process": (ctypes.c_int, [_vp]),
+    "bora_flip_run_post_stage": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "bora_flip_get_particle_attributes": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_size_t,
+                                                         ctypes.POINTER(ctypes.c_size_t)]),
+    "bora_flip_set_particle_attributes": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_size_t]),
     "bora_flip_num_particles": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_size_t)]),
     "bora_flip_get_particles": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, ctypes.c_size_t,
                                                ctypes.POINTER(ctypes.c_size_t), ctypes.c_int]),
@@ -264,6 +271,30 @@ class FlipSim:
 
     def run_stage(self, stage: int, dt: float = 0.0) -> int:
         return _check(self.lib.bora_flip_run_stage(self.h, stage, dt), f"run_stage({stage})")
+
+    def post_process(self) -> None:
+        """FLIPMethod::postProcess: surface splat, tank scan, redistancing, particle attributes."""
+        _check(self.lib.bora_flip_post_process(self.h), "bora_flip_post_process")
+
+    def run_post_stage(self, stage: int) -> None:
+        _check(self.lib.bora_flip_run_post_stage(self.h, stage), f"run_post_stage({stage})")
+
+    def particle_attributes(self):
+        """(vorticity, curvature, ids) of the live particles, in particles()' order."""
+        n = self.num_particles
+        vort = np.zeros(n, np.float32)
+        curv = np.zeros(n, np.float32)
+        ids = np.zeros(n, np.int32)
+        out = ctypes.c_size_t()
+        _check(self.lib.bora_flip_get_particle_attributes(self.h, _ptr(vort), _ptr(curv), _ptr(ids), n,
+                                                          ctypes.byref(out)), "get_particle_attributes")
+        return vort, curv, ids
+
+    def set_particle_attributes(self, vort, curv) -> None:
+        vort = np.ascontiguousarray(vort, np.float32)
+        curv = np.ascontiguousarray(curv, np.float32)
+        _check(self.lib.bora_flip_set_particle_attributes(self.h, _ptr(vort), _ptr(curv), vort.shape[0]),
+               "set_particle_attributes")
 
     @property
     def num_particles(self) -> int:

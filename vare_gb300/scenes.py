@@ -161,6 +161,26 @@ def config3(scale: int = 1) -> Scene:
     return sc
 
 
+def tank_bubble(n: int = 32, depth: float = 0.625, bubble=(0.5, 0.3, 0.5, 0.16), seed: int = 0x5EED0004,
+                dt: float = 1.0 / 120.0) -> Scene:
+    """Water tank with an air bubble: fluid below `depth` (unit box, world units) except a
+    sphere (cx, cy, cz, r); the wall level is the tank's depth, so the water tank's scan
+    fills the enclosed bubble. Run with the water tank enabled."""
+    res = (n, n, n)
+    bmin = (0.0, 0.0, 0.0)
+    bmax = (1.0, 1.0, 1.0)
+    cx, cy, cz, r = bubble
+
+    def inside(x, y, z):
+        return (y < depth) & ((x - cx) ** 2 + (y - cy) ** 2 + (z - cz) ** 2 >= r * r)
+
+    pos = _fill(res, bmin, bmax, inside, seed, 8)
+    sc = Scene(name=f"tank_bubble_{n}", res=res, bmin=bmin, bmax=bmax, dt=dt, pos=pos, vel=np.zeros_like(pos),
+               seed=seed)
+    sc.wall_level = depth
+    return sc
+
+
 def small(n: int = 24, seed: int = 7, sphere: bool = True, dt: float = 1.0 / 120.0) -> Scene:
     """Small dam break + sphere scene for parity tests."""
     return dam_break(n, (0.4, 0.55), seed=seed, dt=dt,
