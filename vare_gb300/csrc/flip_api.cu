@@ -719,11 +719,8 @@ int post_splat( bora_flip_sim* s )
 {
     if( !s->sorted ) return BORA_ERR_INVALID_ARG;
     cudaStream_t st = s->st;
-    const size_t nc = (size_t)s->ntiles * BORA_TILE_CELLS;
-    if( nc == 0 ) return BORA_OK;
-    DevBuf* zero[] = { &s->surf, &s->cx, &s->cy, &s->cz, &s->vx, &s->vy, &s->vz };
-    for( DevBuf* b : zero ) BORA_TRY( cudaMemsetAsync( b->p, 0, nc * 4, st ) );
-    KTimer t( s, BORA_KERNEL_POST, 2 );
+    if( s->ntiles <= 0 ) return BORA_OK;
+    KTimer t( s, BORA_KERNEL_POST, 1 );
     bora_launch_splat( s->g, s->ntiles, s->tiles(), P<uint32_t>( s->cell_start ), P<uint32_t>( s->idx ), s->parts( s->cur ),
                        s->cells(), st );
     return check_launch( s );

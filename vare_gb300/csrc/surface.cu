@@ -17,11 +17,6 @@ namespace {
 __device__ inline float maxr( float a, float b ) { return a > b ? a : b; }
 __device__ inline float minr( float a, float b ) { return a < b ? a : b; }
 
-__device__ inline bool inside_grid( const BoraGridDev& g, float x, float y, float z )  // Grid::inside, Grid.h:408-417
-{
-    return !( x < 0.f || x > (float)g.nx || y < 0.f || y > (float)g.ny || z < 0.f || z > (float)g.nz );
-}
-
 __device__ inline void tile_coords( const BoraGridDev& g, int vt, int& ti, int& tj, int& tk )
 {
     ti = vt % g.tx;
@@ -31,119 +26,174 @@ __device__ inline void tile_coords( const BoraGridDev& g, int vt, int& ti, int& 
 
 // ======================================================================================
 // Rasterization::ParticlesToSurfaceAndVelocity (base/source/Rasterization.cu:311-398),
-// influence 1.5, droplet 0.5 (FLIPMethod.cu:320). One CTA per tile takes the particles
-// of the tile's dual cells (a contiguous range of the sort) and adds their weights into
-// an 11^3 shared-memory region (tile cells -1..9: a particle in dual cell d reaches
-// cells (int)p-1..(int)p+1 within d-1..d+2), then adds the region to the grid. Cells
-// 2..6 of the tile are reached only from the tile's own dual cells and are stored; the
-// rest are added with atomics, in no fixed order, as the reference's atomics are.
-constexpr int kSplatEdge = 11;
-constexpr int kSplatCells = kSplatEdge * kSplatEdge * kSplatEdge;
+// influence 1.5, droplet 0.5 (FLIPMethod.cu:320), as a gather. A particle p adds to the
+// 3^3 cells around (int)p those within the kernel radius; a cell c is reached only from
+// particles of dual cells c-2 .. c+1 per axis (dual cell = max(int(p - 0.5), 0), the
+// sort's key). One CTA per tile owns the tile's 512 cells (two per thread, 7 sums each
+// in registers) and walks the 11 dual-cell layers z = -2 .. 8 of its region: each
+// layer's particles (11 x 11 dual cells, one contiguous sorted range per dual cell) are
+// staged in shared memory, and every cell whose z range includes the layer tests the
+// particles of its 4 x 4 dual cells there. Sums run in a fixed order (layers, dual cells,
+// the sort's particle order), so the result is reproducible; no atomics, and the
+// normalisation of Rasterization.cu:373-395 is applied on the way out.
 constexpr int kSplatThreads = 256;
+constexpr int kSplatCap = 1536;  // staged particles per pass (a layer with more takes several)
+constexpr int kLayerCells = 121;  // 11 x 11 dual cells
 
-// max(0, (1 - (d/1.5)^2)^3) at the centre of cell (i,j,k) (Rasterization.cu:343-349,
-// Vec3f::length, base/header/Vector3.h:328-331). d^2 >= 2.25 gives 0 without the
-// division: then d >= 1.5, s >= 1 and the cube is <= 0.
-__device__ inline float splat_weight( float px, float py, float pz, int i, int j, int k )
-{
-    const float dx = px - ( (float)i + .5f ), dy = py - ( (float)j + .5f ), dz = pz - ( (float)k + .5f );
-    const float d2 = dx * dx + dy * dy + dz * dz;
-    if( !( d2 < 2.25f ) ) return 0.f;
-    const float s = sqrtf( d2 ) / 1.5f;
-    const float t = 1.f - s * s;
-    return maxr( 0.f, t * t * t );
-}
-
+// Kernel weight of Rasterization.cu:343-349, max(0, (1 - (d/1.5)^2)^3), evaluated as
+// (1 - d^2 / 2.25)^3 with fused multiply-adds: the same function without the square root
+// and the division (one weight's rounding differs by an ulp or two; the sums' order, open
+// in the reference, moves them more). Zero for d^2 >= 2.25; a cell within that radius lies
+// in the reference's 3^3 box around (int)p.
 __global__ void __launch_bounds__( kSplatThreads ) k_splat( const __grid_constant__ BoraGridDev g, BoraTilesDev t,
                                                             const uint32_t* __restrict__ start,
                                                             const uint32_t* __restrict__ idx, BoraParticlesDev p,
                                                             BoraCellsDev c )
 {
-    __shared__ float acc[7][kSplatCells];  // w, w x, w y, w z, w u, w v, w w
+    __shared__ float4 sa[kSplatCap];  // x, y, z, u (x = -1e30: outside the grid)
+    __shared__ float2 sb[kSplatCap];  // v, w
+    __shared__ uint32_t q0s[kLayerCells];
+    __shared__ uint32_t off[kLayerCells + 1];
+    __shared__ uint32_t wsum[4];
     __shared__ int32_t nb[27];
     const int s = blockIdx.x, tid = threadIdx.x;
-    for( int h = tid; h < 7 * kSplatCells; h += kSplatThreads ) ( &acc[0][0] )[h] = 0.f;
     if( tid < 27 ) nb[tid] = t.nbr[(size_t)s * 27 + tid];
     int ti, tj, tk;
     tile_coords( g, t.tile_of[s], ti, tj, tk );
-    const int ox = ti * BORA_TILE - 1, oy = tj * BORA_TILE - 1, oz = tk * BORA_TILE - 1;
+    // this thread's two cells: (li, lj, 2m) and (li, lj, 2m + 1), which share each
+    // candidate's x and y distances
+    const int li = tid & 7, lj = ( tid >> 3 ) & 7, m2 = 2 * ( tid >> 6 );
+    const float cx = (float)( ti * BORA_TILE + li ) + .5f, cy = (float)( tj * BORA_TILE + lj ) + .5f;
+    const float cz0 = (float)( tk * BORA_TILE + m2 ) + .5f, cz1 = (float)( tk * BORA_TILE + m2 + 1 ) + .5f;
+    float acc[2][7];
+#pragma unroll
+    for( int m = 0; m < 2; ++m )
+#pragma unroll
+        for( int v = 0; v < 7; ++v ) acc[m][v] = 0.f;
+    const float fnx = (float)g.nx, fny = (float)g.ny, fnz = (float)g.nz;
     __syncthreads();
-    const uint32_t q0 = start[(size_t)s * BORA_TILE_CELLS], q1 = start[(size_t)( s + 1 ) * BORA_TILE_CELLS];
-    for( uint32_t q = q0 + tid; q < q1; q += kSplatThreads )
+    for( int zz = -2; zz <= 8; ++zz )
     {
-        const uint32_t pi = idx[q];
-        const float x = p.px[pi], y = p.py[pi], z = p.pz[pi];
-        if( !inside_grid( g, x, y, z ) ) continue;
-        const float u = p.vx[pi], v = p.vy[pi], w = p.vz[pi];
-        // Grid::neighborCells (base/header/Grid.h:353-370) with offset (int)1.5 = 1
-        const int xi = bora_trunc( x ), yi = bora_trunc( y ), zi = bora_trunc( z );
-        const int i0 = bora_clampi( xi - 1, 0, g.nx - 1 ), i1 = bora_clampi( xi + 1, 0, g.nx - 1 );
-        const int j0 = bora_clampi( yi - 1, 0, g.ny - 1 ), j1 = bora_clampi( yi + 1, 0, g.ny - 1 );
-        const int k0 = bora_clampi( zi - 1, 0, g.nz - 1 ), k1 = bora_clampi( zi + 1, 0, g.nz - 1 );
-        for( int k = k0; k <= k1; ++k )
-            for( int j = j0; j <= j1; ++j )
-                for( int i = i0; i <= i1; ++i )
+        // particle ranges of the layer's dual cells (xx, yy) in -2..8, and their prefix sums
+        uint32_t cnt = 0;
+        if( tid < kLayerCells )
+        {
+            const int xx = tid % 11 - 2, yy = tid / 11 - 2;
+            const int sl = nb[bora_dir( xx < 0 ? -1 : ( xx > 7 ? 1 : 0 ), yy < 0 ? -1 : ( yy > 7 ? 1 : 0 ),
+                                        zz < 0 ? -1 : ( zz > 7 ? 1 : 0 ) )];
+            uint32_t a = 0;
+            if( sl >= 0 )
+            {
+                const uint32_t key = (uint32_t)sl * BORA_TILE_CELLS + (uint32_t)bora_local( xx & 7, yy & 7, zz & 7 );
+                a = start[key];
+                cnt = start[key + 1] - a;
+            }
+            q0s[tid] = a;
+        }
+        // exclusive scan over the 121 counts (warps 0..3)
+        uint32_t inc = cnt;
+        const int lane = tid & 31, wp = tid >> 5;
+#pragma unroll
+        for( int o = 1; o < 32; o <<= 1 )
+        {
+            const uint32_t y = __shfl_up_sync( 0xffffffffu, inc, o );
+            if( lane >= o ) inc += y;
+        }
+        if( wp < 4 && lane == 31 ) wsum[wp] = inc;
+        __syncthreads();
+        if( tid < kLayerCells )
+        {
+            uint32_t base = 0;
+            for( int w = 0; w < wp; ++w ) base += wsum[w];
+            off[tid + 1] = base + inc;
+            if( tid == 0 ) off[0] = 0;
+        }
+        __syncthreads();
+        const uint32_t total = off[kLayerCells];
+        // a particle of dual layer zz reaches cells zz - 1 .. zz + 2 only
+        const bool live = zz >= m2 - 2 && zz <= m2 + 2;
+        for( uint32_t e0 = 0; e0 < total; e0 += kSplatCap )
+        {
+            const uint32_t e1 = min( total, e0 + kSplatCap );
+            for( uint32_t e = e0 + tid; e < e1; e += kSplatThreads )
+            {
+                int lo = 0, hi = kLayerCells;  // dual cell d with off[d] <= e < off[d + 1]
+                while( hi - lo > 1 )
                 {
-                    const float wt = splat_weight( x, y, z, i, j, k );
-                    if( wt == 0.f ) continue;  // adds nothing: every sum starts at +0
-                    const int h = ( i - ox ) + kSplatEdge * ( ( j - oy ) + kSplatEdge * ( k - oz ) );
-                    atomicAdd( &acc[0][h], wt );
-                    atomicAdd( &acc[1][h], wt * x );
-                    atomicAdd( &acc[2][h], wt * y );
-                    atomicAdd( &acc[3][h], wt * z );
-                    atomicAdd( &acc[4][h], wt * u );
-                    atomicAdd( &acc[5][h], wt * v );
-                    atomicAdd( &acc[6][h], wt * w );
+                    const int mid = ( lo + hi ) >> 1;
+                    if( off[mid] <= e ) lo = mid;
+                    else hi = mid;
                 }
-    }
-    __syncthreads();
-    for( int h = tid; h < kSplatCells; h += kSplatThreads )
-    {
-        const float ws = acc[0][h];
-        if( ws == 0.f ) continue;
-        const int a = h % kSplatEdge, b = ( h / kSplatEdge ) % kSplatEdge, cc = h / ( kSplatEdge * kSplatEdge );
-        const int sl = nb[bora_dir( a == 0 ? -1 : ( a >= 9 ? 1 : 0 ), b == 0 ? -1 : ( b >= 9 ? 1 : 0 ),
-                                    cc == 0 ? -1 : ( cc >= 9 ? 1 : 0 ) )];
-        if( sl < 0 ) continue;  // cannot happen: the tiles around a particle's tile are active
-        const size_t n = (size_t)sl * BORA_TILE_CELLS + (size_t)bora_local( ox + a, oy + b, oz + cc );
-        if( a >= 3 && a <= 7 && b >= 3 && b <= 7 && cc >= 3 && cc <= 7 )
-        {
-            c.surf[n] = ws;
-            c.cx[n] = acc[1][h]; c.cy[n] = acc[2][h]; c.cz[n] = acc[3][h];
-            c.vx[n] = acc[4][h]; c.vy[n] = acc[5][h]; c.vz[n] = acc[6][h];
+                const uint32_t pi = idx[q0s[lo] + ( e - off[lo] )];
+                float x = p.px[pi];
+                const float y = p.py[pi], z = p.pz[pi];
+                // Grid::inside (Grid.h:408-417): a particle outside is moved out of every
+                // cell's reach, so it adds weight 0 (and 0 * finite values) everywhere
+                if( x < 0.f || x > fnx || y < 0.f || y > fny || z < 0.f || z > fnz ) x = -1e30f;
+                sa[e - e0] = make_float4( x, y, z, p.vx[pi] );
+                sb[e - e0] = make_float2( p.vy[pi], p.vz[pi] );
+            }
+            __syncthreads();
+            if( live )
+            {
+                // the 4 dual cells xx = li-2 .. li+1 of a row are adjacent in the staging
+                for( int yy = lj - 2; yy <= lj + 1; ++yy )
+                {
+                    const int d = li + 11 * ( yy + 2 );
+                    // the row's part of this pass, as staging indices (empty when the row lies
+                    // wholly before or after the pass)
+                    const uint32_t ga = max( off[d], e0 ), gb = min( off[d + 4], e1 );
+                    const uint32_t a = ga - e0, b = gb > ga ? gb - e0 : a;
+                    // branch-free: a particle outside the radius (or the grid) adds weight 0
+                    auto add = [&]( uint32_t e ) {
+                        const float4 q = sa[e];
+                        const float2 r = sb[e];
+                        const float dx = q.x - cx, dy = q.y - cy, dz0 = q.z - cz0, dz1 = q.z - cz1;
+                        const float h2 = fmaf( dy, dy, dx * dx );
+                        const float t0 = fmaf( -fmaf( dz0, dz0, h2 ), 1.f / 2.25f, 1.f );
+                        const float t1 = fmaf( -fmaf( dz1, dz1, h2 ), 1.f / 2.25f, 1.f );
+                        const float w0 = t0 > 0.f ? t0 * t0 * t0 : 0.f, w1 = t1 > 0.f ? t1 * t1 * t1 : 0.f;
+                        acc[0][0] += w0; acc[1][0] += w1;
+                        acc[0][1] = fmaf( w0, q.x, acc[0][1] ); acc[1][1] = fmaf( w1, q.x, acc[1][1] );
+                        acc[0][2] = fmaf( w0, q.y, acc[0][2] ); acc[1][2] = fmaf( w1, q.y, acc[1][2] );
+                        acc[0][3] = fmaf( w0, q.z, acc[0][3] ); acc[1][3] = fmaf( w1, q.z, acc[1][3] );
+                        acc[0][4] = fmaf( w0, q.w, acc[0][4] ); acc[1][4] = fmaf( w1, q.w, acc[1][4] );
+                        acc[0][5] = fmaf( w0, r.x, acc[0][5] ); acc[1][5] = fmaf( w1, r.x, acc[1][5] );
+                        acc[0][6] = fmaf( w0, r.y, acc[0][6] ); acc[1][6] = fmaf( w1, r.y, acc[1][6] );
+                    };
+                    uint32_t e = a;
+                    for( ; e + 2 <= b; e += 2 )
+                    {
+                        add( e ); add( e + 1 );
+                    }
+                    if( e < b ) add( e );
+                }
+            }
+            __syncthreads();  // the staging buffer and the layer tables are reused
         }
-        else
-        {
-            atomicAdd( &c.surf[n], ws );
-            atomicAdd( &c.cx[n], acc[1][h] ); atomicAdd( &c.cy[n], acc[2][h] ); atomicAdd( &c.cz[n], acc[3][h] );
-            atomicAdd( &c.vx[n], acc[4][h] ); atomicAdd( &c.vy[n], acc[5][h] ); atomicAdd( &c.vz[n], acc[6][h] );
-        }
     }
-}
-
-// Rasterization.cu:373-395 per cell: the weighted mean position's distance to the cell
-// centre minus the droplet radius (5 where no weight landed), the weighted mean
-// velocity; the weight sum goes to pres, the field FLIPMethod.cu:320 passes as "mass".
-__global__ void k_splat_finish( const __grid_constant__ BoraGridDev g, BoraTilesDev t, size_t ncell, BoraCellsDev c )
-{
-    for( size_t n = blockIdx.x * (size_t)blockDim.x + threadIdx.x; n < ncell; n += (size_t)gridDim.x * blockDim.x )
+    // Rasterization.cu:373-395: mean position's distance to the centre - 0.5 (5 where no
+    // weight landed), mean velocity; the weight sum goes to pres ("mass", FLIPMethod.cu:320)
+#pragma unroll
+    for( int m = 0; m < 2; ++m )
     {
-        int ti, tj, tk;
-        tile_coords( g, t.tile_of[n / BORA_TILE_CELLS], ti, tj, tk );
-        const int l = (int)( n % BORA_TILE_CELLS );
-        const int i = ti * BORA_TILE + ( l & 7 ), j = tj * BORA_TILE + ( ( l >> 3 ) & 7 ), k = tk * BORA_TILE + ( l >> 6 );
-        const float w = c.surf[n];
+        const int lk = m2 + m;
+        const size_t n = (size_t)s * BORA_TILE_CELLS + (size_t)( li + 8 * lj + 64 * lk );
+        const int i = ti * BORA_TILE + li, j = tj * BORA_TILE + lj, k = tk * BORA_TILE + lk;
+        const bool real = i < g.nx && j < g.ny && k < g.nz;
+        const float w = real ? acc[m][0] : 0.f;
         c.pres[n] = w;
         if( w > 1e-30f )
         {
-            const float x = c.cx[n] / w, y = c.cy[n] / w, z = c.cz[n] / w;
+            const float x = acc[m][1] / w, y = acc[m][2] / w, z = acc[m][3] / w;
             c.cx[n] = x; c.cy[n] = y; c.cz[n] = z;
             const float dx = x - ( (float)i + .5f ), dy = y - ( (float)j + .5f ), dz = z - ( (float)k + .5f );
             c.surf[n] = sqrtf( dx * dx + dy * dy + dz * dz ) - 0.5f;  // Vec3f::distanceTo, Vector3.h:364-367
-            c.vx[n] = c.vx[n] / w; c.vy[n] = c.vy[n] / w; c.vz[n] = c.vz[n] / w;
+            c.vx[n] = acc[m][4] / w; c.vy[n] = acc[m][5] / w; c.vz[n] = acc[m][6] / w;
         }
         else
         {
+            c.cx[n] = real ? acc[m][1] : 0.f; c.cy[n] = real ? acc[m][2] : 0.f; c.cz[n] = real ? acc[m][3] : 0.f;
             c.surf[n] = 5.f;
             c.vx[n] = 0.f; c.vy[n] = 0.f; c.vz[n] = 0.f;
         }
@@ -360,61 +410,19 @@ __device__ inline size_t halo_index( const int32_t* nb, int h )  // storage inde
     return (size_t)ns * BORA_TILE_CELLS + (size_t)bora_local( a + 7, b + 7, cc + 7 );
 }
 
-// Rasterization::ReinitializeSurface (base/source/Rasterization.cu:400-486), one step:
-// Godunov upwind update of phi_t = sign(phi)(1 - |grad phi|), dt 0.3, sign =
-// phi / sqrt(phi^2 + 1); differences mirrored at the grid faces, or for the water tank
-// the faces read the level y - wall (minus / plus one below / above the grid).
-template <bool TANK>
-__global__ void __launch_bounds__( 512 ) k_redistance( const __grid_constant__ BoraGridDev g, BoraTilesDev t,
-                                                        const float* __restrict__ in, float* __restrict__ out )
+// One Godunov upwind step of Rasterization::ReinitializeSurface
+// (base/source/Rasterization.cu:400-486) at a cell with value v and neighbours
+// (i0, i1, j0, j1, k0, k1): phi_t = sign(phi)(1 - |grad phi|), dt 0.3,
+// sign = phi / sqrt(phi^2 + 1). Of the reference's two terms
+// dt max(sign,0)(sqrt(a) - 1) and dt min(sign,0)(sqrt(b) - 1) one has a zero factor; its
+// value is the signed zero (+0) * (sqrt(x) - 1), whose sign is that of x - 1, so only the
+// other square root is taken.
+__device__ inline float godunov_step( float v, float vi0, float vi1, float vj0, float vj1, float vk0, float vk1 )
 {
-    __shared__ float r[kQN];
-    __shared__ int32_t nb[27];
-    const int s = blockIdx.x, tid = threadIdx.x;
-    bora_pdl_trigger();
-    if( tid < 27 ) nb[tid] = t.nbr[(size_t)s * 27 + tid];
-    int ti, tj, tk;
-    tile_coords( g, t.tile_of[s], ti, tj, tk );
-    __syncthreads();
-    size_t src[2];
-    for( int u = 0; u < 2; ++u ) src[u] = tid + u * 512 < kQN ? halo_index( nb, tid + u * 512 ) : SIZE_MAX;
-    bora_pdl_wait();
-    for( int u = 0; u < 2; ++u )
-        if( tid + u * 512 < kQN ) r[tid + u * 512] = src[u] == SIZE_MAX ? 10.f : in[src[u]];
-    __syncthreads();
-    const int li = tid & 7, lj = ( tid >> 3 ) & 7, lk = tid >> 6;
-    const int i = ti * BORA_TILE + li, j = tj * BORA_TILE + lj, k = tk * BORA_TILE + lk;
-    const int h = ( li + 1 ) + kQ * ( ( lj + 1 ) + kQ * ( lk + 1 ) );
-    const float v = r[h];
-    const size_t n = (size_t)s * BORA_TILE_CELLS + tid;
-    if( i >= g.nx || j >= g.ny || k >= g.nz )
-    {
-        out[n] = v;
-        return;
-    }
-    const int I = g.nx - 1, J = g.ny - 1, K = g.nz - 1;
-    float vi0, vi1, vj0, vj1, vk0, vk1;
-    if( TANK )
-    {
-        const float ll = ( (float)j + .5f ) - g.voxel_wall;
-        vj0 = j == 0 ? ll - 1.f : r[h - kQ];
-        vj1 = j == J ? ll + 1.f : r[h + kQ];
-        vi0 = i == 0 ? ll : r[h - 1];
-        vi1 = i == I ? ll : r[h + 1];
-        vk0 = k == 0 ? ll : r[h - kQ * kQ];
-        vk1 = k == K ? ll : r[h + kQ * kQ];
-    }
-    else
-    {
-        vi0 = i == 0 ? 2.f * v - r[h + 1] : r[h - 1];
-        vi1 = i == I ? 2.f * v - r[h - 1] : r[h + 1];
-        vj0 = j == 0 ? 2.f * v - r[h + kQ] : r[h - kQ];
-        vj1 = j == J ? 2.f * v - r[h - kQ] : r[h + kQ];
-        vk0 = k == 0 ? 2.f * v - r[h + kQ * kQ] : r[h - kQ * kQ];
-        vk1 = k == K ? 2.f * v - r[h - kQ * kQ] : r[h + kQ * kQ];
-    }
     const float dx0 = v - vi0, dx1 = vi1 - v, dy0 = v - vj0, dy1 = vj1 - v, dz0 = v - vk0, dz1 = vk1 - v;
     const float sign = v / sqrtf( v * v + 1.f );
+    const float dt = 0.3f;
+    const float ps = maxr( sign, 0.f ), ns = minr( sign, 0.f );
     float a = maxr( dx0, 0.f ) * maxr( dx0, 0.f );
     a = a + minr( dx1, 0.f ) * minr( dx1, 0.f );
     a = a + maxr( dy0, 0.f ) * maxr( dy0, 0.f );
@@ -427,8 +435,100 @@ __global__ void __launch_bounds__( 512 ) k_redistance( const __grid_constant__ B
     b = b + maxr( dy1, 0.f ) * maxr( dy1, 0.f );
     b = b + minr( dz0, 0.f ) * minr( dz0, 0.f );
     b = b + maxr( dz1, 0.f ) * maxr( dz1, 0.f );
-    const float dt = 0.3f;
-    out[n] = ( v - dt * maxr( sign, 0.f ) * ( sqrtf( a ) - 1.f ) ) - dt * minr( sign, 0.f ) * ( sqrtf( b ) - 1.f );
+    const float zp = a < 1.f ? -0.f : 0.f, zn = b < 1.f ? -0.f : 0.f;
+    const bool pos = ps != 0.f;  // sign > 0: the first term is live
+    const bool neg = ns != 0.f;  // sign < 0: the second
+    const float t1 = pos ? dt * ps * ( sqrtf( a ) - 1.f ) : zp;
+    const float t2 = neg ? dt * ns * ( sqrtf( b ) - 1.f ) : zn;
+    return ( v - t1 ) - t2;
+}
+
+// Redistancing, one step over all tiles: a persistent grid walks the tiles; each tile's
+// 10^3 region (the tile and a one-cell halo, background 10 for inactive tiles) is read
+// into registers one tile ahead, so the loads of the next tile overlap the arithmetic of
+// the current one.
+constexpr int kRedistThreads = 512;
+
+template <bool TANK>
+__global__ void __launch_bounds__( kRedistThreads ) k_redistance( const __grid_constant__ BoraGridDev g, BoraTilesDev t,
+                                                                   int ntiles, const float* __restrict__ in,
+                                                                   float* __restrict__ out )
+{
+    __shared__ float r[kQN];
+    __shared__ int32_t nbb[2][27];
+    const int tid = threadIdx.x, G = gridDim.x;
+    bora_pdl_trigger();
+    if( tid < 27 )
+    {
+        nbb[0][tid] = blockIdx.x < ntiles ? t.nbr[(size_t)blockIdx.x * 27 + tid] : -1;
+        nbb[1][tid] = blockIdx.x + G < ntiles ? t.nbr[(size_t)( blockIdx.x + G ) * 27 + tid] : -1;
+    }
+    __syncthreads();
+    bora_pdl_wait();  // `in` is the previous step's output
+    // this thread's two region cells: tile direction and local index, the same for every tile
+    int rdir[2], rloc[2];
+    for( int u = 0; u < 2; ++u )
+    {
+        const int hh = tid + u * kRedistThreads;
+        const int a = hh % kQ, b = ( hh / kQ ) % kQ, c = hh / ( kQ * kQ );
+        rdir[u] = hh < kQN ? bora_dir( a == 0 ? -1 : ( a == 9 ? 1 : 0 ), b == 0 ? -1 : ( b == 9 ? 1 : 0 ),
+                                       c == 0 ? -1 : ( c == 9 ? 1 : 0 ) )
+                           : -1;
+        rloc[u] = bora_local( a + 7, b + 7, c + 7 );
+    }
+    float pf[2];
+    auto issue = [&]( const int32_t* nb ) {
+        for( int u = 0; u < 2; ++u )
+        {
+            const int ns = rdir[u] >= 0 ? nb[rdir[u]] : -1;
+            pf[u] = ns >= 0 ? in[(size_t)ns * BORA_TILE_CELLS + rloc[u]] : 10.f;
+        }
+    };
+    issue( nbb[0] );
+    const int li = tid & 7, lj = ( tid >> 3 ) & 7, lk = tid >> 6;
+    const int h = ( li + 1 ) + kQ * ( ( lj + 1 ) + kQ * ( lk + 1 ) );
+    const int I = g.nx - 1, J = g.ny - 1, K = g.nz - 1;
+    int n = 0;
+    for( int s = blockIdx.x; s < ntiles; s += G, ++n )
+    {
+        for( int u = 0; u < 2; ++u )
+            if( tid + u * kRedistThreads < kQN ) r[tid + u * kRedistThreads] = pf[u];
+        const int32_t nb2 = tid < 27 && s + 2 * G < ntiles ? t.nbr[(size_t)( s + 2 * G ) * 27 + tid] : -1;
+        __syncthreads();
+        if( s + G < ntiles ) issue( nbb[( n + 1 ) & 1] );
+        int ti, tj, tk;
+        tile_coords( g, t.tile_of[s], ti, tj, tk );
+        const int i = ti * BORA_TILE + li, j = tj * BORA_TILE + lj, k = tk * BORA_TILE + lk;
+        const float v = r[h];
+        float res = v;
+        if( i < g.nx && j < g.ny && k < g.nz )
+        {
+            float vi0, vi1, vj0, vj1, vk0, vk1;
+            if( TANK )
+            {
+                const float ll = ( (float)j + .5f ) - g.voxel_wall;
+                vj0 = j == 0 ? ll - 1.f : r[h - kQ];
+                vj1 = j == J ? ll + 1.f : r[h + kQ];
+                vi0 = i == 0 ? ll : r[h - 1];
+                vi1 = i == I ? ll : r[h + 1];
+                vk0 = k == 0 ? ll : r[h - kQ * kQ];
+                vk1 = k == K ? ll : r[h + kQ * kQ];
+            }
+            else
+            {
+                vi0 = i == 0 ? 2.f * v - r[h + 1] : r[h - 1];
+                vi1 = i == I ? 2.f * v - r[h - 1] : r[h + 1];
+                vj0 = j == 0 ? 2.f * v - r[h + kQ] : r[h - kQ];
+                vj1 = j == J ? 2.f * v - r[h - kQ] : r[h + kQ];
+                vk0 = k == 0 ? 2.f * v - r[h + kQ * kQ] : r[h - kQ * kQ];
+                vk1 = k == K ? 2.f * v - r[h - kQ * kQ] : r[h + kQ * kQ];
+            }
+            res = godunov_step( v, vi0, vi1, vj0, vj1, vk0, vk1 );
+        }
+        out[(size_t)s * BORA_TILE_CELLS + tid] = res;
+        if( tid < 27 ) nbb[n & 1][tid] = nb2;  // tile s's table is no longer read
+        __syncthreads();  // the next tile's staging overwrites r
+    }
 }
 
 // FieldOP::curl of the splatted velocity (base/source/FieldOP.cu:338-369; background 0)
@@ -590,8 +690,6 @@ void bora_launch_splat( const BoraGridDev& g, int ntiles, BoraTilesDev t, const 
 {
     if( ntiles <= 0 ) return;
     k_splat<<<ntiles, kSplatThreads, 0, st>>>( g, t, start, idx, p, c );
-    const size_t ncell = (size_t)ntiles * BORA_TILE_CELLS;
-    k_splat_finish<<<blocks_for_cells( ncell ), 256, 0, st>>>( g, t, ncell, c );
 }
 
 int bora_tank_scan_launches( const BoraGridDev& g, int ntiles, BoraTilesDev t, float* surf, uint32_t* labels,
@@ -616,12 +714,33 @@ int bora_tank_scan_launches( const BoraGridDev& g, int ntiles, BoraTilesDev t, f
     return 6;
 }
 
+template <bool TANK>
+int redistance_grid( int ntiles )
+{
+    static int per_sm[64] = { 0 };
+    int dev = 0;
+    cudaGetDevice( &dev );
+    int b = dev >= 0 && dev < 64 ? per_sm[dev] : 0;
+    if( b <= 0 )
+    {
+        if( cudaOccupancyMaxActiveBlocksPerMultiprocessor( &b, k_redistance<TANK>, kRedistThreads, 0 ) != cudaSuccess || b <= 0 )
+            b = 1;
+        if( dev >= 0 && dev < 64 ) per_sm[dev] = b;
+    }
+    int sms = 0;
+    cudaDeviceGetAttribute( &sms, cudaDevAttrMultiProcessorCount, dev );
+    return std::max( 1, std::min( ntiles, b * std::max( sms, 1 ) ) );
+}
+
 cudaError_t bora_launch_redistance( const BoraGridDev& g, int ntiles, BoraTilesDev t, const float* in, float* out,
                                     cudaStream_t st )
 {
     if( ntiles <= 0 ) return cudaSuccess;
-    if( g.enable_tank ) return bora_launch_pdl( k_redistance<true>, dim3( ntiles ), dim3( 512 ), 0, st, g, t, in, out );
-    return bora_launch_pdl( k_redistance<false>, dim3( ntiles ), dim3( 512 ), 0, st, g, t, in, out );
+    if( g.enable_tank )
+        return bora_launch_pdl( k_redistance<true>, dim3( redistance_grid<true>( ntiles ) ), dim3( kRedistThreads ), 0, st,
+                                g, t, ntiles, in, out );
+    return bora_launch_pdl( k_redistance<false>, dim3( redistance_grid<false>( ntiles ) ), dim3( kRedistThreads ), 0, st,
+                            g, t, ntiles, in, out );
 }
 
 void bora_launch_surface_fields( const BoraGridDev& g, int ntiles, BoraTilesDev t, BoraCellsDev c, float* wx, float* wy,
