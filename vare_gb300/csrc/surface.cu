@@ -456,12 +456,18 @@ __global__ void __launch_bounds__( kRedistThreads ) k_redistance( const __grid_c
 {
     __shared__ float r[kQN];
     __shared__ int32_t nbb[2][27];
+    __shared__ int tcb[2][3];  // tile coordinates, double-buffered like the neighbour tables
     const int tid = threadIdx.x, G = gridDim.x;
     bora_pdl_trigger();
     if( tid < 27 )
     {
         nbb[0][tid] = blockIdx.x < ntiles ? t.nbr[(size_t)blockIdx.x * 27 + tid] : -1;
         nbb[1][tid] = blockIdx.x + G < ntiles ? t.nbr[(size_t)( blockIdx.x + G ) * 27 + tid] : -1;
+    }
+    else if( tid == 32 || tid == 33 )
+    {
+        const int q = tid - 32, sq = blockIdx.x + q * G;
+        if( sq < ntiles ) tile_coords( g, t.tile_of[sq], tcb[q][0], tcb[q][1], tcb[q][2] );
     }
     __syncthreads();
     bora_pdl_wait();  // `in` is the previous step's output
@@ -494,10 +500,11 @@ __global__ void __launch_bounds__( kRedistThreads ) k_redistance( const __grid_c
         for( int u = 0; u < 2; ++u )
             if( tid + u * kRedistThreads < kQN ) r[tid + u * kRedistThreads] = pf[u];
         const int32_t nb2 = tid < 27 && s + 2 * G < ntiles ? t.nbr[(size_t)( s + 2 * G ) * 27 + tid] : -1;
+        int tc2[3] = { 0, 0, 0 };
+        if( tid == 32 && s + 2 * G < ntiles ) tile_coords( g, t.tile_of[s + 2 * G], tc2[0], tc2[1], tc2[2] );
         __syncthreads();
         if( s + G < ntiles ) issue( nbb[( n + 1 ) & 1] );
-        int ti, tj, tk;
-        tile_coords( g, t.tile_of[s], ti, tj, tk );
+        const int ti = tcb[n & 1][0], tj = tcb[n & 1][1], tk = tcb[n & 1][2];
         const int i = ti * BORA_TILE + li, j = tj * BORA_TILE + lj, k = tk * BORA_TILE + lk;
         const float v = r[h];
         float res = v;
@@ -526,8 +533,9 @@ __global__ void __launch_bounds__( kRedistThreads ) k_redistance( const __grid_c
             res = godunov_step( v, vi0, vi1, vj0, vj1, vk0, vk1 );
         }
         out[(size_t)s * BORA_TILE_CELLS + tid] = res;
-        if( tid < 27 ) nbb[n & 1][tid] = nb2;  // tile s's table is no longer read
-        __syncthreads();  // the next tile's staging overwrites r
+        __syncthreads();  // tile s's tables and region are no longer read
+        if( tid < 27 ) nbb[n & 1][tid] = nb2;
+        if( tid == 32 ) { tcb[n & 1][0] = tc2[0]; tcb[n & 1][1] = tc2[1]; tcb[n & 1][2] = tc2[2]; }
     }
 }
 
