@@ -29,15 +29,16 @@ __device__ inline void tile_coords( const BoraGridDev& g, int vt, int& ti, int& 
 // influence 1.5, droplet 0.5 (FLIPMethod.cu:320), as a gather. A particle p adds to the
 // 3^3 cells around (int)p those within the kernel radius; a cell c is reached only from
 // particles of dual cells c-2 .. c+1 per axis (dual cell = max(int(p - 0.5), 0), the
-// sort's key). One CTA per tile owns the tile's 512 cells (two per thread, 7 sums each
-// in registers) and walks the 11 dual-cell layers z = -2 .. 8 of its region: each
-// layer's particles (11 x 11 dual cells, one contiguous sorted range per dual cell) are
-// staged in shared memory, and every cell whose z range includes the layer tests the
-// particles of its 4 x 4 dual cells there. Sums run in a fixed order (layers, dual cells,
-// the sort's particle order), so the result is reproducible; no atomics, and the
-// normalisation of Rasterization.cu:373-395 is applied on the way out.
+// sort's key). One CTA per tile owns the tile's 512 cells and walks the 11 dual-cell
+// layers z = -2 .. 8 of its region: each layer's particles (11 x 11 dual cells, one
+// contiguous sorted range each) are staged in shared memory, and the 256 cells the layer
+// can reach (z - 1 .. z + 2) are worked on at once: a pair of z-adjacent cells per thread
+// pair (the pair shares each candidate's x and y distances), the two threads of a pair
+// taking two of the four candidate rows each. Layer sums go into per-cell shared sums in a
+// fixed order, so the result is reproducible; no atomics, and the normalisation of
+// Rasterization.cu:373-395 is applied on the way out.
 constexpr int kSplatThreads = 256;
-constexpr int kSplatCap = 1536;  // staged particles per pass (a layer with more takes several)
+constexpr int kSplatCap = 1024;  // staged particles per pass (a layer with more takes several)
 constexpr int kLayerCells = 121;  // 11 x 11 dual cells
 
 // Kernel weight of Rasterization.cu:343-349, max(0, (1 - (d/1.5)^2)^3), evaluated as
@@ -52,24 +53,22 @@ __global__ void __launch_bounds__( kSplatThreads ) k_splat( const __grid_constan
 {
     __shared__ float4 sa[kSplatCap];  // x, y, z, u (x = -1e30: outside the grid)
     __shared__ float2 sb[kSplatCap];  // v, w
+    __shared__ float accs[7][BORA_TILE_CELLS];  // per cell: w, w x, w y, w z, w u, w v, w w
     __shared__ uint32_t q0s[kLayerCells];
     __shared__ uint32_t off[kLayerCells + 1];
     __shared__ uint32_t wsum[4];
     __shared__ int32_t nb[27];
     const int s = blockIdx.x, tid = threadIdx.x;
     if( tid < 27 ) nb[tid] = t.nbr[(size_t)s * 27 + tid];
+    for( int h = tid; h < 7 * BORA_TILE_CELLS; h += kSplatThreads ) ( &accs[0][0] )[h] = 0.f;
     int ti, tj, tk;
     tile_coords( g, t.tile_of[s], ti, tj, tk );
-    // this thread's two cells: (li, lj, 2m) and (li, lj, 2m + 1), which share each
-    // candidate's x and y distances
-    const int li = tid & 7, lj = ( tid >> 3 ) & 7, m2 = 2 * ( tid >> 6 );
+    // work item: cells (li, lj, zz - 1 + 2 pr) and (li, lj, zz + 2 pr); lanes l and l ^ 16
+    // split its four candidate rows
+    const int half = ( tid >> 4 ) & 1;
+    const int item = ( tid & 15 ) | ( ( tid >> 5 ) << 4 );
+    const int li = item & 7, lj = ( item >> 3 ) & 7, pr = item >> 6;
     const float cx = (float)( ti * BORA_TILE + li ) + .5f, cy = (float)( tj * BORA_TILE + lj ) + .5f;
-    const float cz0 = (float)( tk * BORA_TILE + m2 ) + .5f, cz1 = (float)( tk * BORA_TILE + m2 + 1 ) + .5f;
-    float acc[2][7];
-#pragma unroll
-    for( int m = 0; m < 2; ++m )
-#pragma unroll
-        for( int v = 0; v < 7; ++v ) acc[m][v] = 0.f;
     const float fnx = (float)g.nx, fny = (float)g.ny, fnz = (float)g.nz;
     __syncthreads();
     for( int zz = -2; zz <= 8; ++zz )
@@ -110,8 +109,13 @@ __global__ void __launch_bounds__( kSplatThreads ) k_splat( const __grid_constan
         }
         __syncthreads();
         const uint32_t total = off[kLayerCells];
-        // a particle of dual layer zz reaches cells zz - 1 .. zz + 2 only
-        const bool live = zz >= m2 - 2 && zz <= m2 + 2;
+        const int z0 = zz - 1 + 2 * pr, z1 = z0 + 1;  // this item's cells
+        const float cz0 = (float)( tk * BORA_TILE + z0 ) + .5f, cz1 = (float)( tk * BORA_TILE + z1 ) + .5f;
+        float acc[2][7];
+#pragma unroll
+        for( int m = 0; m < 2; ++m )
+#pragma unroll
+            for( int v = 0; v < 7; ++v ) acc[m][v] = 0.f;
         for( uint32_t e0 = 0; e0 < total; e0 += kSplatCap )
         {
             const uint32_t e1 = min( total, e0 + kSplatCap );
@@ -134,66 +138,77 @@ __global__ void __launch_bounds__( kSplatThreads ) k_splat( const __grid_constan
                 sb[e - e0] = make_float2( p.vy[pi], p.vz[pi] );
             }
             __syncthreads();
-            if( live )
+            // the 4 dual cells xx = li-2 .. li+1 of a row are adjacent in the staging
+            for( int yy = lj - 2 + 2 * half; yy <= lj - 1 + 2 * half; ++yy )
             {
-                // the 4 dual cells xx = li-2 .. li+1 of a row are adjacent in the staging
-                for( int yy = lj - 2; yy <= lj + 1; ++yy )
+                const int d = li + 11 * ( yy + 2 );
+                // the row's part of this pass, as staging indices (empty when the row lies
+                // wholly before or after the pass)
+                const uint32_t ga = max( off[d], e0 ), gb = min( off[d + 4], e1 );
+                const uint32_t a = ga - e0, b = gb > ga ? gb - e0 : a;
+                // branch-free: a particle outside the radius (or the grid) adds weight 0
+                auto add = [&]( uint32_t e ) {
+                    const float4 q = sa[e];
+                    const float2 r = sb[e];
+                    const float dx = q.x - cx, dy = q.y - cy, dz0 = q.z - cz0, dz1 = q.z - cz1;
+                    const float h2 = fmaf( dy, dy, dx * dx );
+                    const float t0 = fmaf( -fmaf( dz0, dz0, h2 ), 1.f / 2.25f, 1.f );
+                    const float t1 = fmaf( -fmaf( dz1, dz1, h2 ), 1.f / 2.25f, 1.f );
+                    const float w0 = t0 > 0.f ? t0 * t0 * t0 : 0.f, w1 = t1 > 0.f ? t1 * t1 * t1 : 0.f;
+                    acc[0][0] += w0; acc[1][0] += w1;
+                    acc[0][1] = fmaf( w0, q.x, acc[0][1] ); acc[1][1] = fmaf( w1, q.x, acc[1][1] );
+                    acc[0][2] = fmaf( w0, q.y, acc[0][2] ); acc[1][2] = fmaf( w1, q.y, acc[1][2] );
+                    acc[0][3] = fmaf( w0, q.z, acc[0][3] ); acc[1][3] = fmaf( w1, q.z, acc[1][3] );
+                    acc[0][4] = fmaf( w0, q.w, acc[0][4] ); acc[1][4] = fmaf( w1, q.w, acc[1][4] );
+                    acc[0][5] = fmaf( w0, r.x, acc[0][5] ); acc[1][5] = fmaf( w1, r.x, acc[1][5] );
+                    acc[0][6] = fmaf( w0, r.y, acc[0][6] ); acc[1][6] = fmaf( w1, r.y, acc[1][6] );
+                };
+                uint32_t e = a;
+                for( ; e + 2 <= b; e += 2 )
                 {
-                    const int d = li + 11 * ( yy + 2 );
-                    // the row's part of this pass, as staging indices (empty when the row lies
-                    // wholly before or after the pass)
-                    const uint32_t ga = max( off[d], e0 ), gb = min( off[d + 4], e1 );
-                    const uint32_t a = ga - e0, b = gb > ga ? gb - e0 : a;
-                    // branch-free: a particle outside the radius (or the grid) adds weight 0
-                    auto add = [&]( uint32_t e ) {
-                        const float4 q = sa[e];
-                        const float2 r = sb[e];
-                        const float dx = q.x - cx, dy = q.y - cy, dz0 = q.z - cz0, dz1 = q.z - cz1;
-                        const float h2 = fmaf( dy, dy, dx * dx );
-                        const float t0 = fmaf( -fmaf( dz0, dz0, h2 ), 1.f / 2.25f, 1.f );
-                        const float t1 = fmaf( -fmaf( dz1, dz1, h2 ), 1.f / 2.25f, 1.f );
-                        const float w0 = t0 > 0.f ? t0 * t0 * t0 : 0.f, w1 = t1 > 0.f ? t1 * t1 * t1 : 0.f;
-                        acc[0][0] += w0; acc[1][0] += w1;
-                        acc[0][1] = fmaf( w0, q.x, acc[0][1] ); acc[1][1] = fmaf( w1, q.x, acc[1][1] );
-                        acc[0][2] = fmaf( w0, q.y, acc[0][2] ); acc[1][2] = fmaf( w1, q.y, acc[1][2] );
-                        acc[0][3] = fmaf( w0, q.z, acc[0][3] ); acc[1][3] = fmaf( w1, q.z, acc[1][3] );
-                        acc[0][4] = fmaf( w0, q.w, acc[0][4] ); acc[1][4] = fmaf( w1, q.w, acc[1][4] );
-                        acc[0][5] = fmaf( w0, r.x, acc[0][5] ); acc[1][5] = fmaf( w1, r.x, acc[1][5] );
-                        acc[0][6] = fmaf( w0, r.y, acc[0][6] ); acc[1][6] = fmaf( w1, r.y, acc[1][6] );
-                    };
-                    uint32_t e = a;
-                    for( ; e + 2 <= b; e += 2 )
-                    {
-                        add( e ); add( e + 1 );
-                    }
-                    if( e < b ) add( e );
+                    add( e ); add( e + 1 );
                 }
+                if( e < b ) add( e );
             }
-            __syncthreads();  // the staging buffer and the layer tables are reused
+            __syncthreads();  // the staging buffer is reused by the next pass
         }
+        // the two halves' sums, added in a fixed order into the cells' running sums (each
+        // cell is owned by one item in a layer)
+#pragma unroll
+        for( int m = 0; m < 2; ++m )
+        {
+            const int zc = m == 0 ? z0 : z1;
+#pragma unroll
+            for( int v = 0; v < 7; ++v )
+            {
+                const float other = __shfl_xor_sync( 0xffffffffu, acc[m][v], 16 );
+                if( half == 0 && zc >= 0 && zc <= 7 ) accs[v][li + 8 * lj + 64 * zc] += acc[m][v] + other;
+            }
+        }
+        __syncthreads();  // the layer tables are rewritten next
     }
     // Rasterization.cu:373-395: mean position's distance to the centre - 0.5 (5 where no
     // weight landed), mean velocity; the weight sum goes to pres ("mass", FLIPMethod.cu:320)
 #pragma unroll
     for( int m = 0; m < 2; ++m )
     {
-        const int lk = m2 + m;
-        const size_t n = (size_t)s * BORA_TILE_CELLS + (size_t)( li + 8 * lj + 64 * lk );
-        const int i = ti * BORA_TILE + li, j = tj * BORA_TILE + lj, k = tk * BORA_TILE + lk;
+        const int l = tid + 256 * m;
+        const int i = ti * BORA_TILE + ( l & 7 ), j = tj * BORA_TILE + ( ( l >> 3 ) & 7 ), k = tk * BORA_TILE + ( l >> 6 );
+        const size_t n = (size_t)s * BORA_TILE_CELLS + l;
         const bool real = i < g.nx && j < g.ny && k < g.nz;
-        const float w = real ? acc[m][0] : 0.f;
+        const float w = real ? accs[0][l] : 0.f;
         c.pres[n] = w;
         if( w > 1e-30f )
         {
-            const float x = acc[m][1] / w, y = acc[m][2] / w, z = acc[m][3] / w;
+            const float x = accs[1][l] / w, y = accs[2][l] / w, z = accs[3][l] / w;
             c.cx[n] = x; c.cy[n] = y; c.cz[n] = z;
             const float dx = x - ( (float)i + .5f ), dy = y - ( (float)j + .5f ), dz = z - ( (float)k + .5f );
             c.surf[n] = sqrtf( dx * dx + dy * dy + dz * dz ) - 0.5f;  // Vec3f::distanceTo, Vector3.h:364-367
-            c.vx[n] = acc[m][4] / w; c.vy[n] = acc[m][5] / w; c.vz[n] = acc[m][6] / w;
+            c.vx[n] = accs[4][l] / w; c.vy[n] = accs[5][l] / w; c.vz[n] = accs[6][l] / w;
         }
         else
         {
-            c.cx[n] = real ? acc[m][1] : 0.f; c.cy[n] = real ? acc[m][2] : 0.f; c.cz[n] = real ? acc[m][3] : 0.f;
+            c.cx[n] = real ? accs[1][l] : 0.f; c.cy[n] = real ? accs[2][l] : 0.f; c.cz[n] = real ? accs[3][l] : 0.f;
             c.surf[n] = 5.f;
             c.vx[n] = 0.f; c.vy[n] = 0.f; c.vz[n] = 0.f;
         }
