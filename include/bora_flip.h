@@ -231,6 +231,17 @@ int bora_flip_num_particles( bora_flip_handle h, size_t* n );
 int bora_flip_get_particles( bora_flip_handle h, float* pos, float* vel, float* adjacency, int32_t* ids, size_t cap,
                              size_t* n, int space );
 
+/* Asynchronous export of the current particles (the SOP's per-frame attribute export,
+ * SOP_FlipWater.cpp:205-248): the live particles, their adjacency-free attributes and ids are
+ * gathered on the handle's stream into a device export buffer (in bora_flip_get_particles'
+ * order) and copied to the given host buffers on a second stream; the call returns at once.
+ * A following bora_flip_step / frame runs while the copy is in flight (pinned host buffers
+ * give full overlap). The host buffers must stay valid until bora_flip_export_wait; a new
+ * export first waits for the previous one. *n = live particles. Any pointer may be NULL. */
+int bora_flip_export_begin( bora_flip_handle h, float* pos, float* vel, float* vorticity, float* curvature,
+                            int32_t* ids, size_t cap, int space, size_t* n );
+int bora_flip_export_wait( bora_flip_handle h );
+
 int bora_flip_frame_info( bora_flip_handle h, bora_frame_info* out );
 /* Active tiles as (i,j,k) tile coordinates, in storage (slot) order. */
 int bora_flip_get_tiles( bora_flip_handle h, int32_t* ijk, size_t cap_tiles );

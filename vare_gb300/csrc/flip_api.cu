@@ -100,6 +100,16 @@ __global__ void k_scatter_attrs( size_t n, BoraParticlesDev p, const uint32_t* _
     }
 }
 
+__global__ void k_to_host_u32( const uint32_t* __restrict__ src, uint32_t* dst, int n )
+{
+    for( int i = threadIdx.x; i < n; i += blockDim.x ) ( (volatile uint32_t*)dst )[i] = src[i];
+}
+
+__global__ void k_to_host_f64( const double* __restrict__ src, double* dst, int n )
+{
+    for( int i = threadIdx.x; i < n; i += blockDim.x ) ( (volatile double*)dst )[i] = src[i];
+}
+
 int grid_blocks( size_t n )
 {
     const size_t b = ( n + 255 ) / 256;
@@ -144,6 +154,12 @@ struct bora_flip_sim
     DevBuf pattr[2][2]; // vorticity, curvature (allocated by the first post-processing)
     bool attrs = false;
     DevBuf labels;      // post-processing: union-find labels of the water tank's scan
+    // asynchronous export: live particles gathered into exp_buf on the handle's stream, copied
+    // to the caller's host memory on a second stream while the next step runs
+    DevBuf exp_buf;
+    cudaStream_t st_copy = nullptr;
+    cudaEvent_t ev_gathered = nullptr, ev_copied = nullptr;
+    bool exporting = false;
     DevBuf adj, vkey, key, idx;
     size_t cap_p = 0;
     size_t np = 0;      // particles in the current buffer (killed ones included until the next sort)
@@ -155,8 +171,10 @@ struct bora_flip_sim
 
     // scratch and staging
     DevBuf scan_scratch, counters, stage_in, stage_out, live_flag;
-    uint32_t* h_cnt = nullptr;  // pinned
-    double* h_ring = nullptr;   // pinned
+    uint32_t* h_cnt = nullptr;  // pinned, mapped: counters as the host sees them
+    uint32_t* d_cnt = nullptr;  // its device address
+    double* h_ring = nullptr;   // pinned, mapped
+    double* d_hring = nullptr;  // its device address
     double* h_mirror = nullptr;  // pinned, mapped: reductions' slot values as the host sees them
     double* d_mirror = nullptr;  // its device address
     static constexpr int kChecks = 8;
@@ -383,19 +401,26 @@ int ensure_cells( bora_flip_sim* s, int ntiles )
     return BORA_OK;
 }
 
+// Scalars the host reads back are written into mapped host memory by a one-warp kernel
+// rather than copied: a copy would queue behind a large export on the copy engines
+// (bora_flip_export_begin) and stall the step it should overlap.
 int read_counters( bora_flip_sim* s, int first, int count )
 {
-    BORA_TRY( cudaMemcpyAsync( s->h_cnt + first, P<uint32_t>( s->counters ) + first, count * 4, cudaMemcpyDeviceToHost, s->st ) );
+    s->stats.kernel_launches += 1;
+    k_to_host_u32<<<1, 32, 0, s->st>>>( P<uint32_t>( s->counters ) + first, s->d_cnt + first, count );
+    BORA_TRY( cudaGetLastError() );
     BORA_TRY( cudaStreamSynchronize( s->st ) );
     return BORA_OK;
 }
 
 double read_ring( bora_flip_sim* s, int slot, int* status )
 {
-    cudaError_t e = cudaMemcpyAsync( s->h_ring, P<double>( s->ring ) + slot, 8, cudaMemcpyDeviceToHost, s->st );
+    s->stats.kernel_launches += 1;
+    k_to_host_f64<<<1, 32, 0, s->st>>>( P<double>( s->ring ) + slot, s->d_hring, 1 );
+    cudaError_t e = cudaGetLastError();
     if( e == cudaSuccess ) e = cudaStreamSynchronize( s->st );
     if( e != cudaSuccess ) { *status = cuda_status( e ); return 0.0; }
-    return s->h_ring[0];
+    return ( (volatile double*)s->h_ring )[0];
 }
 
 // ---- stages --------------------------------------------------------------------------
@@ -839,6 +864,7 @@ void for_each_buffer( bora_flip_sim* s, F&& f )
         for( int a = 0; a < 2; ++a ) f( s->pattr[q][a] );
     }
     f( s->labels );
+    f( s->exp_buf );
     for( int l = 0; l < bora_flip_sim::kMaxLevels; ++l )
     {
         f( s->mg_type[l] ); f( s->mg_code[l] ); f( s->mg_r[l] );
@@ -911,8 +937,10 @@ int bora_flip_create( const bora_grid_desc* grid, const bora_flip_params* params
     int st = cuda_status( cudaStreamCreateWithFlags( &s->st, cudaStreamNonBlocking ) );
     if( st == BORA_OK ) st = cuda_status( cudaEventCreate( &s->ev_step[0] ) );
     if( st == BORA_OK ) st = cuda_status( cudaEventCreate( &s->ev_step[1] ) );
-    if( st == BORA_OK ) st = cuda_status( cudaHostAlloc( (void**)&s->h_cnt, 64, cudaHostAllocDefault ) );
-    if( st == BORA_OK ) st = cuda_status( cudaHostAlloc( (void**)&s->h_ring, 64, cudaHostAllocDefault ) );
+    if( st == BORA_OK ) st = cuda_status( cudaHostAlloc( (void**)&s->h_cnt, 64, cudaHostAllocMapped ) );
+    if( st == BORA_OK ) st = cuda_status( cudaHostGetDevicePointer( (void**)&s->d_cnt, s->h_cnt, 0 ) );
+    if( st == BORA_OK ) st = cuda_status( cudaHostAlloc( (void**)&s->h_ring, 64, cudaHostAllocMapped ) );
+    if( st == BORA_OK ) st = cuda_status( cudaHostGetDevicePointer( (void**)&s->d_hring, s->h_ring, 0 ) );
     if( st == BORA_OK ) st = cuda_status( cudaHostAlloc( (void**)&s->h_mirror, BORA_RING * 8, cudaHostAllocMapped ) );
     if( st == BORA_OK ) st = cuda_status( cudaHostGetDevicePointer( (void**)&s->d_mirror, s->h_mirror, 0 ) );
     for( int q = 0; q < bora_flip_sim::kChecks && st == BORA_OK; ++q )
@@ -942,7 +970,11 @@ int bora_flip_destroy( bora_flip_handle s )
 {
     if( !s ) return BORA_ERR_INVALID_ARG;
     if( s->st ) cudaStreamSynchronize( s->st );
+    if( s->st_copy ) cudaStreamSynchronize( s->st_copy );
     for_each_buffer( s, []( DevBuf& b ) { release( b ); } );
+    if( s->ev_gathered ) cudaEventDestroy( s->ev_gathered );
+    if( s->ev_copied ) cudaEventDestroy( s->ev_copied );
+    if( s->st_copy ) cudaStreamDestroy( s->st_copy );
     s->prof_resolve();
     for( cudaEvent_t e : s->evpool ) cudaEventDestroy( e );
     for( int q = 0; q < 2; ++q )
@@ -1246,6 +1278,63 @@ int bora_flip_get_particles( bora_flip_handle s, float* pos, float* vel, float* 
     if( adjacency ) BORA_TRY( cudaMemcpyAsync( adjacency, oadj, nl * 4, cudaMemcpyDeviceToHost, st ) );
     if( ids ) BORA_TRY( cudaMemcpyAsync( ids, oid, nl * 4, cudaMemcpyDeviceToHost, st ) );
     BORA_TRY( cudaStreamSynchronize( st ) );
+    return BORA_OK;
+}
+
+int bora_flip_export_begin( bora_flip_handle s, float* pos, float* vel, float* vorticity, float* curvature, int32_t* ids,
+                            size_t cap, int space, size_t* n )
+{
+    if( !s ) return BORA_ERR_INVALID_ARG;
+    if( cap < s->nlive && ( pos || vel || vorticity || curvature || ids ) ) return BORA_ERR_CAPACITY;
+    if( n ) *n = s->nlive;
+    if( !s->st_copy )
+    {
+        BORA_TRY( cudaStreamCreateWithFlags( &s->st_copy, cudaStreamNonBlocking ) );
+        BORA_TRY( cudaEventCreateWithFlags( &s->ev_gathered, cudaEventDisableTiming ) );
+        BORA_TRY( cudaEventCreateWithFlags( &s->ev_copied, cudaEventDisableTiming ) );
+    }
+    if( s->exporting ) BORA_TRY( cudaEventSynchronize( s->ev_copied ) );  // one export at a time
+    s->exporting = false;
+    if( s->np == 0 || s->nlive == 0 ) return BORA_OK;
+    cudaStream_t st = s->st;
+    const size_t np = s->np, nl = s->nlive;
+    BORA_TRYS( ensure_scan_scratch( s, std::max( np + 1, std::max( s->ntv, s->cap_tiles * BORA_TILE_CELLS + 2 ) ) ) );
+    BORA_TRY( grow( s->exp_buf, nl * 40 + 64, false, st ) );
+    float* opos = P<float>( s->exp_buf );
+    float* ovel = opos + 3 * nl;
+    float* oadj = ovel + 3 * nl;
+    float* ovort = oadj + nl;
+    float* ocurv = ovort + nl;
+    int32_t* oid = reinterpret_cast<int32_t*>( ocurv + nl );
+    BoraParticlesDev p = s->parts( s->cur );
+    const float3 tr = make_float3( s->translate[0], s->translate[1], s->translate[2] );
+    const float3 sc = make_float3( s->scale[0], s->scale[1], s->scale[2] );
+    s->stats.kernel_launches += 5;
+    k_live_flags<<<grid_blocks( np ), 256, 0, st>>>( np, p.id, P<uint32_t>( s->live_flag ) );
+    bora_device_scan( P<uint32_t>( s->live_flag ), P<uint32_t>( s->live_flag ), np, P<uint32_t>( s->scan_scratch ),
+                   P<uint32_t>( s->counters ) + 4, st );
+    k_gather_live<<<grid_blocks( np ), 256, 0, st>>>( np, p, P<float>( s->adj ), P<uint32_t>( s->live_flag ), space, tr, sc,
+                                                      opos, ovel, oadj, oid );
+    k_gather_attrs<<<grid_blocks( np ), 256, 0, st>>>( np, p, P<uint32_t>( s->live_flag ), ovort, ocurv, oid );
+    BORA_TRYS( check_launch( s ) );
+    BORA_TRY( cudaEventRecord( s->ev_gathered, st ) );
+    cudaStream_t cs = s->st_copy;
+    BORA_TRY( cudaStreamWaitEvent( cs, s->ev_gathered, 0 ) );
+    if( pos ) BORA_TRY( cudaMemcpyAsync( pos, opos, nl * 12, cudaMemcpyDeviceToHost, cs ) );
+    if( vel ) BORA_TRY( cudaMemcpyAsync( vel, ovel, nl * 12, cudaMemcpyDeviceToHost, cs ) );
+    if( vorticity ) BORA_TRY( cudaMemcpyAsync( vorticity, ovort, nl * 4, cudaMemcpyDeviceToHost, cs ) );
+    if( curvature ) BORA_TRY( cudaMemcpyAsync( curvature, ocurv, nl * 4, cudaMemcpyDeviceToHost, cs ) );
+    if( ids ) BORA_TRY( cudaMemcpyAsync( ids, oid, nl * 4, cudaMemcpyDeviceToHost, cs ) );
+    BORA_TRY( cudaEventRecord( s->ev_copied, cs ) );
+    s->exporting = true;  // the next export waits for ev_copied before it gathers into exp_buf
+    return BORA_OK;
+}
+
+int bora_flip_export_wait( bora_flip_handle s )
+{
+    if( !s ) return BORA_ERR_INVALID_ARG;
+    if( s->exporting ) BORA_TRY( cudaEventSynchronize( s->ev_copied ) );
+    s->exporting = false;
     return BORA_OK;
 }
 

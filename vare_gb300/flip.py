@@ -99,6 +99,9 @@ _SIGS = {
     "bora_flip_get_particle_attributes": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_size_t,
                                                          ctypes.POINTER(ctypes.c_size_t)]),
     "bora_flip_set_particle_attributes": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_size_t]),
+    "bora_flip_export_begin": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_size_t, ctypes.c_int,
+                                              ctypes.POINTER(ctypes.c_size_t)]),
+    "bora_flip_export_wait": (ctypes.c_int, [_vp]),
     "bora_flip_num_particles": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_size_t)]),
     "bora_flip_get_particles": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, ctypes.c_size_t,
                                                ctypes.POINTER(ctypes.c_size_t), ctypes.c_int]),
@@ -289,6 +292,19 @@ class FlipSim:
         _check(self.lib.bora_flip_get_particle_attributes(self.h, _ptr(vort), _ptr(curv), _ptr(ids), n,
                                                           ctypes.byref(out)), "get_particle_attributes")
         return vort, curv, ids
+
+    def export_begin(self, pos_ptr: int, vel_ptr: int, vort_ptr: int = 0, curv_ptr: int = 0, ids_ptr: int = 0,
+                     cap: int = 0, space: int = SPACE_VOXEL) -> int:
+        """Start the asynchronous copy of the current particles to host memory (raw pointers,
+        pinned for overlap; 0 = skip); returns the live count. Call export_wait before reading."""
+        n = ctypes.c_size_t()
+        _check(self.lib.bora_flip_export_begin(self.h, _vp(pos_ptr or None), _vp(vel_ptr or None),
+                                               _vp(vort_ptr or None), _vp(curv_ptr or None), _vp(ids_ptr or None),
+                                               cap, space, ctypes.byref(n)), "export_begin")
+        return int(n.value)
+
+    def export_wait(self) -> None:
+        _check(self.lib.bora_flip_export_wait(self.h), "export_wait")
 
     def set_particle_attributes(self, vort, curv) -> None:
         vort = np.ascontiguousarray(vort, np.float32)
