@@ -234,7 +234,8 @@ struct DenseNav
     int cdx, cdy;     // coarser dense level
     __device__ inline long long nb( long long cell, int q ) const
     {
-        const int i = (int)( cell % dx ), j = (int)( ( cell / dx ) % dy ), k = (int)( cell / ( (long long)dx * dy ) );
+        const int c = (int)cell;  // dense levels hold far fewer than 2^31 cells
+        const int i = c % dx, j = ( c / dx ) % dy, k = c / ( dx * dy );
         switch( q )
         {
             case 0: return i > 0 ? cell - 1 : -1;
@@ -247,8 +248,9 @@ struct DenseNav
     }
     __device__ inline long long parent( long long cell ) const
     {
-        const int i = (int)( cell % dx ), j = (int)( ( cell / dx ) % dy ), k = (int)( cell / ( (long long)dx * dy ) );
-        return (long long)( i >> 1 ) + (long long)cdx * ( ( j >> 1 ) + (long long)cdy * ( k >> 1 ) );
+        const int c = (int)cell;
+        const int i = c % dx, j = ( c / dx ) % dy, k = c / ( dx * dy );
+        return (long long)( ( i >> 1 ) + cdx * ( ( j >> 1 ) + cdy * ( k >> 1 ) ) );
     }
 };
 
@@ -554,7 +556,8 @@ __global__ void __launch_bounds__( 256 ) k_mg_smooth_last( Nav nav, BoraLevelDev
 // tiled with one cell per tile (only the first), down to the coarsest and back up, with a
 // cluster barrier between the operations (the cluster's CTAs are co-scheduled, and the
 // barrier orders their global-memory writes at cluster scope). The coarsest level runs
-// in the cluster's first CTA.
+// in the cluster's first CTA. (Walking the levels below the first in one CTA's shared
+// memory was slower: a 4096-cell level then runs on one SM.)
 constexpr int kTailLevels = 8;
 constexpr int kTailThreads = 1024;
 constexpr int kTailCtasMax = 16;  // non-portable cluster size, where the device supports it
