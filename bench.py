@@ -24,6 +24,7 @@ all host threads) on the same workload, metric and unit.
 from __future__ import annotations
 
 import argparse
+import contextlib
 import json
 import os
 import subprocess
@@ -76,6 +77,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-post", action="store_true", help="skip the post-processing measurement")
     ap.add_argument("--post-reps", type=int, default=5)
+    ap.add_argument("--nvtx", action="store_true",
+                    help="mark the timed steps and one post-processing frame with NVTX ranges 'step' and 'post' "
+                         "(for a profiler's range filter)")
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--solver", default="both", choices=["both", "plain", "mixed"],
@@ -310,16 +314,17 @@ def timed_steps(sim, sc, args, world, flip, local, sample_clocks, alg=ALG_BYTES)
     torch.cuda.synchronize()
     step_ms, particle_steps, iters, worst = [], 0, [], {"residual_rel": 0.0, "residual_max_dx": 0.0}
     all_conv = True
-    for _ in range(args.steps):
-        n0 = sim.num_particles
-        status = sim.step(sc.dt)
-        st = sim.stats()
-        step_ms.append(st["gpu_ms"])
-        particle_steps += n0
-        iters.append(st["solver_iterations"])
-        worst["residual_rel"] = max(worst["residual_rel"], st["residual_rel"])
-        worst["residual_max_dx"] = max(worst["residual_max_dx"], st["residual_max_dx"])
-        all_conv = all_conv and status == 0 and st["converged"] == 1
+    with torch.cuda.nvtx.range("step") if getattr(args, "nvtx", False) else contextlib.nullcontext():
+        for _ in range(args.steps):
+            n0 = sim.num_particles
+            status = sim.step(sc.dt)
+            st = sim.stats()
+            step_ms.append(st["gpu_ms"])
+            particle_steps += n0
+            iters.append(st["solver_iterations"])
+            worst["residual_rel"] = max(worst["residual_rel"], st["residual_rel"])
+            worst["residual_max_dx"] = max(worst["residual_max_dx"], st["residual_max_dx"])
+            all_conv = all_conv and status == 0 and st["converged"] == 1
     torch.cuda.synchronize()
     barrier(world)
     clk = clocks.stop() if clocks else None
@@ -369,7 +374,7 @@ def timed_steps(sim, sc, args, world, flip, local, sample_clocks, alg=ALG_BYTES)
                        "active_tiles": fi["ntiles"]}}
 
 
-def post_measure(sim, sc, flip, reps: int = 5) -> dict:
+def post_measure(sim, sc, flip, reps: int = 5, nvtx: bool = False) -> dict:
     """FLIPMethod::postProcess on the state the timed steps left (one frame's surface
     pipeline): host wall time of bora_flip_post_process (synchronous; it includes the
     tile rebuild it starts with), then each stage on its own. The redistancing's
@@ -380,10 +385,11 @@ def post_measure(sim, sc, flip, reps: int = 5) -> dict:
     torch.cuda.synchronize()
     sim.post_process()  # warm-up (allocates the attribute buffers)
     times = []
-    for _ in range(max(1, reps)):
+    for r in range(max(1, reps)):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        sim.post_process()
+        with torch.cuda.nvtx.range("post") if nvtx and r == 0 else contextlib.nullcontext():
+            sim.post_process()
         torch.cuda.synchronize()
         times.append(time.perf_counter() - t0)
     stages = {}
@@ -470,7 +476,7 @@ def run_ours(args, world, rank, local):
                  "config": "same scene; geometric-multigrid-preconditioned CG, V(2,2) damped Jacobi, FP16 level "
                            "storage with FP32 arithmetic, FP64-accurate dots and norms, FP64 iterative refinement"}
 
-    post = None if args.no_post else post_measure(sim, sc, flip)
+    post = None if args.no_post else post_measure(sim, sc, flip, args.post_reps, args.nvtx)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
