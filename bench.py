@@ -212,6 +212,43 @@ def cpu_baseline(scene, steps: int, threads: int | None = None):
             "ms_per_step": 1e3 * sum(times) / len(times)}
 
 
+def post_cpu_baseline(flip, reps: int = 2) -> dict:
+    """FLIPMethod::postProcess on the host cores next to the device, both on the 64^3 dam
+    break after one step (505,856 particles): the oracle restatement in compat mode (4^3
+    tiles, the reference's rules; its splat adds in particle order on one thread, as the
+    reference's host build does with one thread), all other loops on all cores."""
+    import torch
+    from oracle import bindings as B
+    from vare_gb300 import scenes
+    if not os.path.exists(B.ORACLE_SO):
+        B.build(ref=False)
+    sc = scenes.config0()
+    sim = flip.FlipSim.from_scene(sc, solver=flip.SOLVER_MIXED)
+    sim.step(sc.dt)
+    sim.post_process()
+    gt = []
+    for _ in range(3):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sim.post_process()
+        torch.cuda.synchronize()
+        gt.append(time.perf_counter() - t0)
+    del sim
+    threads = os.cpu_count()
+    ora = B.Oracle(sc, block=4, compat=True, solver="reference", max_iter=200, threads=threads)
+    ora.step(sc.dt)
+    ct = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        ora.post_process(sc.dt, literal_scan=True)
+        ct.append(time.perf_counter() - t0)
+    gt.sort()
+    ct.sort()
+    return {"workload": "dam_break_64 after one step (505,856 particles)", "gpu_ms": 1e3 * gt[len(gt) // 2],
+            "cpu_ms": 1e3 * ct[len(ct) // 2], "cores": threads, "kind": "port",
+            "sample": f"{reps} post-processing frames of the oracle restatement in compat mode"}
+
+
 def dist_setup(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -483,6 +520,8 @@ def run_ours(args, world, rank, local):
         del sim
         torch.cuda.empty_cache()
         cpu = cpu_baseline(sc, args.cpu_steps)
+        if post is not None:
+            post["cpu_baseline"] = post_cpu_baseline(flip)
 
     if rank != 0:
         return

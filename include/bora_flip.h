@@ -248,10 +248,10 @@ int bora_flip_get_tiles( bora_flip_handle h, int32_t* ijk, size_t cap_tiles );
 
 /* Grid fields in tile storage order (active tiles x 512 cells, x fastest in a tile). */
 #define BORA_FIELD_MASS 0      /* float  (getDensityField) */
-#define BORA_FIELD_SURF 1      /* float  particle count per cell */
+#define BORA_FIELD_SURF 1      /* float  particle count per cell after a step; signed distance after post-processing */
 #define BORA_FIELD_PRES 2      /* float  */
-#define BORA_FIELD_VELO 3      /* 3 float per cell (pre-projection grid velocity, getVelocityField) */
-#define BORA_FIELD_COMP 4      /* 3 float per cell (projected grid velocity) */
+#define BORA_FIELD_VELO 3      /* 3 float per cell (pre-projection grid velocity, getVelocityField; splatted velocity after post-processing) */
+#define BORA_FIELD_COMP 4      /* 3 float per cell (projected grid velocity; surface normals after post-processing) */
 #define BORA_FIELD_FLAG 5      /* uint8: 0 air, 1 solid, 4 fluid, 255 beyond the grid */
 #define BORA_FIELD_RHS 6       /* float  right-hand side b = -div (fluid cells) */
 #define BORA_FIELD_CODE 7      /* uint16 stencil code (bit 15 fluid, bits 8-11 diagonal, bits 0-5 fluid nbrs) */
