@@ -94,9 +94,9 @@ def make_scene(name):
     return scenes.config1() if name == "dam_sphere_256" else scenes.config0()
 
 
-SOLVER_DESC = {"plain": "plain: FP32 PCG + block-MIC(0), FP64 dots, FP64 iterative refinement",
+SOLVER_DESC = {"plain": "plain: FP32 PCG + block-MIC(0), FP64-accurate dots, double-float iterative refinement",
                "mixed": "mixed: FP32 PCG + geometric multigrid V(2,2) (FP16 level storage, FP32 arithmetic), "
-                        "FP64 dots, FP64 iterative refinement"}
+                        "FP64-accurate dots, double-float iterative refinement"}
 
 
 def workload_config(sc, extra=None, solver="plain"):
@@ -511,7 +511,7 @@ def run_ours(args, world, rank, local):
                  "gpu_launches": mm["launches"],
                  "solver": mm["solver"], "speedup_over_plain": mm["value"] / value,
                  "config": "same scene; geometric-multigrid-preconditioned CG, V(2,2) damped Jacobi, FP16 level "
-                           "storage with FP32 arithmetic, FP64-accurate dots and norms, FP64 iterative refinement"}
+                           "storage with FP32 arithmetic, FP64-accurate dots and norms, double-float iterative refinement"}
 
     post = None if args.no_post else post_measure(sim, sc, flip, args.post_reps, args.nvtx)
 

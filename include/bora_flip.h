@@ -42,8 +42,8 @@ extern "C" {
 #define BORA_SPACE_VOXEL 1
 
 /* Pressure-solver forms. */
-#define BORA_SOLVER_PLAIN 0 /* FP32 PCG, block-MIC(0) preconditioner, FP64 dots + refinement */
-#define BORA_SOLVER_MIXED 1 /* FP32 PCG, multigrid V-cycle (FP16 storage), FP64 dots + refinement */
+#define BORA_SOLVER_PLAIN 0 /* FP32 PCG, block-MIC(0) preconditioner, FP64-accurate dots, double-float refinement */
+#define BORA_SOLVER_MIXED 1 /* FP32 PCG, multigrid V-cycle (FP16 storage), FP64-accurate dots, double-float refinement */
 
 /* particle advection (bora_flip_params.advection) */
 #define BORA_ADVECT_EULER 0
@@ -84,8 +84,8 @@ typedef struct bora_flip_params
     double tolerance;        /* 1e-6: stop when ||b - A p||_2 / ||b||_2 < tolerance ... */
     double div_tolerance;    /* 1e-5: ... and max_i |b - A p|_i * dx_world < div_tolerance */
     double inner_tolerance;  /* 1e-3: relative residual reduction of each FP32 inner solve (the
-                                recurrence continues across passes while FP64 and FP32 residuals agree) */
-    int max_refinements;     /* 8: outer FP64 refinement passes */
+                                recurrence continues across passes while the refined and FP32 residuals agree) */
+    int max_refinements;     /* 8: outer refinement passes (double-float iterate and residual) */
     int check_every;         /* 1: inner iterations between convergence checks (read back one iteration late) */
     int advection;           /* BORA_ADVECT_EULER: particle positions follow the particle velocity
                                 (FLIPMethod.cu:124-145); BORA_ADVECT_RK2: midpoint rule in the grid
@@ -123,7 +123,7 @@ typedef struct bora_flip_stats
 #define BORA_KERNEL_RHS 4          /* right-hand side, stencil code, preconditioner set-up */
 #define BORA_KERNEL_PCG_DIRECTION 5
 #define BORA_KERNEL_PCG_UPDATE 6
-#define BORA_KERNEL_REFINE 7       /* solver init, FP64 refinement, pressure write-back */
+#define BORA_KERNEL_REFINE 7       /* solver init, refinement, pressure write-back */
 #define BORA_KERNEL_VELOCITY 8
 #define BORA_KERNEL_G2P 9
 #define BORA_KERNEL_MG 10          /* multigrid V-cycle (mixed solver) */

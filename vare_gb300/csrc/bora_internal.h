@@ -136,7 +136,7 @@ void bora_launch_to_soa( size_t n, const float* pos, const float* vel, int space
 // ---- pressure solve -------------------------------------------------------------------
 struct BoraSolverDev
 {
-    double* x;      // FP64 pressure iterate (refinement)
+    float2* x;      // pressure iterate of the refinement as a double-float pair (hi, lo): ~48 bits
     float* e;       // inner correction
     float* r;       // residual
     float* d[2];    // search directions (ping-pong)
@@ -163,7 +163,7 @@ void bora_launch_refine_accumulate( int ntiles, const uint16_t* code, BoraSolver
 void bora_launch_refine_residual( const BoraGridDev& g, int ntiles, BoraTilesDev t, const float* b, const uint16_t* code,
                                   BoraSolverDev s, BoraReduceDev red, int slot_norm2, int slot_max, cudaStream_t st );
 // pres = (float) x on fluid cells, 0 elsewhere
-void bora_launch_write_pressure( int ntiles, const uint16_t* code, const double* x, float* pres, cudaStream_t st );
+void bora_launch_write_pressure( int ntiles, const uint16_t* code, const float2* x, float* pres, cudaStream_t st );
 
 
 // ---- multigrid preconditioner (mixed form) ----------------------------------------------

@@ -229,7 +229,7 @@ struct bora_flip_sim
     BoraSolverDev solver()
     {
         BoraSolverDev s;
-        s.x = P<double>( sx ); s.e = P<float>( se ); s.r = P<float>( sr );
+        s.x = P<float2>( sx ); s.e = P<float>( se ); s.r = P<float>( sr );
         s.d[0] = P<float>( sd0 ); s.d[1] = P<float>( sd1 ); s.q = P<float>( sq ); s.z = P<float>( sz );
         s.minv = P<float>( sminv );
         return s;
@@ -555,7 +555,7 @@ int stage_build_system( bora_flip_sim* s )
     return check_launch( s );
 }
 
-// Pressure solve: FP64 iterative refinement around FP32 PCG passes.
+// Pressure solve: double-float iterative refinement around FP32 PCG passes.
 int stage_solve( bora_flip_sim* s )
 {
     const bora_flip_params& p = s->prm;
@@ -580,7 +580,7 @@ int stage_solve( bora_flip_sim* s )
     const int max_inner = std::max( 1, p.proj_iteration );
     const int check = std::max( 1, p.check_every );
     // The Krylov recurrence continues across refinement passes (residual replacement): a
-    // pass ends by replacing the recursive FP32 residual with the FP64 one, keeps the last
+    // pass ends by replacing the recursive FP32 residual with the refined one, keeps the last
     // direction d and r.z, and the next pass carries on from them instead of restarting.
     int rz_prev = -1, dsel = 0;
     for( ;; )
@@ -674,7 +674,7 @@ int stage_solve( bora_flip_sim* s )
         rmax = read_ring( s, s_mx, &status );
         BORA_TRYS( status );
         if( !std::isfinite( rnorm ) ) break;
-        // Continue the recurrence only while the FP64 residual still agrees with the
+        // Continue the recurrence only while the refined residual still agrees with the
         // recursive one (the device finished the pass, so its last r.r is in mapped memory);
         // a larger drift would break conjugacy, so the next pass restarts (beta = 0).
         const double rr_rec = ( (volatile double*)s->h_mirror )[rr_cur];

@@ -1,6 +1,7 @@
 // Pressure projection over active 8^3 tiles: right-hand side and stencil build, a
-// matrix-free PCG with a block-MIC(0) preconditioner, FP64 reductions and FP64
-// iterative refinement, and the pressure-gradient velocity update.
+// matrix-free PCG with a block-MIC(0) preconditioner, FP64-accurate (double-float)
+// reductions and double-float iterative refinement, and the pressure-gradient velocity
+// update.
 //
 // Replaces FluidProjection::buildLinearSystem / solve (sparse,
 // base/source/FluidProjection.cu:165-381), LinearSystemSolver::cg/pcg
@@ -510,7 +511,7 @@ __global__ void k_solve_init( size_t ncells, const float* __restrict__ b, BoraSo
     {
         const float bv = b[i];
         sv.r[i] = bv;
-        sv.x[i] = 0.0;
+        sv.x[i] = make_float2( 0.f, 0.f );
         sv.e[i] = 0.f;
         sv.d[0][i] = 0.f;
         sv.d[1][i] = 0.f;
@@ -534,47 +535,60 @@ __global__ void k_refine_accumulate( size_t ncells, const uint16_t* __restrict__
     for( size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < ncells; i += (size_t)gridDim.x * blockDim.x )
     {
         const float e = slot_a_rz < 0 ? sv.e[i] : fmaf( alpha, d[i], sv.e[i] );
-        if( code[i] & BORA_CODE_FLUID ) sv.x[i] += (double)e;
+        if( code[i] & BORA_CODE_FLUID )
+        {
+            const float2 x = sv.x[i];
+            const DF y = df_add_f( DF{ x.x, x.y }, e );
+            sv.x[i] = make_float2( y.hi, y.lo );
+        }
         sv.e[i] = 0.f;
         sv.q[i] = 0.f;
     }
 }
 
-// r = b - A x in FP64 (A from the stencil code); r stored in FP32. Streaming, one thread
-// per cell.
+// r = b - A x in double-float arithmetic (A from the stencil code, x the double-float
+// iterate); r stored in FP32, ||r||^2 and max|r| reduced. Streaming, one thread per cell.
+// GB300's FP64 pipe is narrow: in FP64 this kernel and the accumulation were bound by it.
 __global__ void __launch_bounds__( 256 ) k_refine_residual( size_t ncells, const int32_t* __restrict__ nbr,
                                                             const float* __restrict__ b, const uint16_t* __restrict__ code,
                                                             BoraSolverDev sv, BoraReduceDev red, int slot_norm2,
                                                             int slot_max )
 {
-    double n2 = 0.0, mx = 0.0;
+    DF n2{ 0.f, 0.f };
+    float mx = 0.f;
     for( size_t cell = blockIdx.x * (size_t)blockDim.x + threadIdx.x; cell < ncells; cell += (size_t)gridDim.x * blockDim.x )
     {
         const uint16_t cc = code[cell];
         if( !( cc & BORA_CODE_FLUID ) ) { sv.r[cell] = 0.f; continue; }
         const int s = (int)( cell >> 9 ), l = (int)( cell & 511 );
-        double acc = 0.0;
+        DF acc{ 0.f, 0.f };
 #pragma unroll
         for( int q = 0; q < 6; ++q )
         {
             if( !( cc & ( 1u << q ) ) ) continue;
             const size_t nc = face_nbr( nbr, cell, s, l, q );
             if( nc == (size_t)-1 ) { atomicOr( red.err, 2u ); continue; }
-            acc += sv.x[nc];
+            const float2 xn = sv.x[nc];
+            acc = df_add( acc, DF{ xn.x, xn.y } );
         }
-        const double rv = (double)b[cell] - ( (double)code_diag( cc ) * sv.x[cell] - acc );
-        sv.r[cell] = (float)rv;
-        n2 += rv * rv;
-        mx = fmax( mx, fabs( rv ) );
+        const float2 xc = sv.x[cell];
+        const float dg = (float)code_diag( cc );
+        const DF ax = df_add_f( df_prod( xc.x, dg ), xc.y * dg );  // diag * x (diag <= 12)
+        const DF t = df_add( ax, DF{ -acc.hi, -acc.lo } );
+        const DF rv = df_add_f( DF{ -t.hi, -t.lo }, b[cell] );
+        const float rf = rv.hi + rv.lo;
+        sv.r[cell] = rf;
+        n2 = df_add( n2, df_prod( rf, rf ) );
+        mx = fmaxf( mx, fabsf( rf ) );
     }
-    reduce2_publish_warp( warp_sum( n2 ), warp_max( mx ), 1, red, slot_norm2, slot_max );
+    reduce2_publish_dfmax( n2, mx, red, slot_norm2, slot_max );
 }
 
-__global__ void k_write_pressure( size_t ncells, const uint16_t* __restrict__ code, const double* __restrict__ x,
+__global__ void k_write_pressure( size_t ncells, const uint16_t* __restrict__ code, const float2* __restrict__ x,
                                   float* __restrict__ pres )
 {
     for( size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < ncells; i += (size_t)gridDim.x * blockDim.x )
-        pres[i] = ( code[i] & BORA_CODE_FLUID ) ? (float)x[i] : 0.f;
+        pres[i] = ( code[i] & BORA_CODE_FLUID ) ? x[i].x + x[i].y : 0.f;
 }
 
 // ---------------------------------------------------------------------------------
@@ -758,7 +772,7 @@ void bora_launch_refine_residual( const BoraGridDev&, int ntiles, BoraTilesDev t
     k_refine_residual<<<nb, 256, 0, st>>>( nc, t.nbr, b, code, s, red, slot_norm2, slot_max );
 }
 
-void bora_launch_write_pressure( int ntiles, const uint16_t* code, const double* x, float* pres, cudaStream_t st )
+void bora_launch_write_pressure( int ntiles, const uint16_t* code, const float2* x, float* pres, cudaStream_t st )
 {
     const size_t nc = (size_t)ntiles * 512;
     if( nc ) k_write_pressure<<<grid_for( nc, 256 ), 256, 0, st>>>( nc, code, x, pres );
