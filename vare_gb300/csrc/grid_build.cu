@@ -174,10 +174,36 @@ __global__ void k_scatter( size_t n, const uint32_t* __restrict__ key, const uin
 __global__ void k_order_bins( size_t nbins, const uint32_t* __restrict__ start, uint32_t* __restrict__ idx,
                               uint32_t max_bin )
 {
+    constexpr int kReg = 16;  // bins up to this size are sorted in registers
     for( size_t b = blockIdx.x * (size_t)blockDim.x + threadIdx.x; b < nbins; b += (size_t)gridDim.x * blockDim.x )
     {
         const uint32_t q0 = start[b], q1 = start[b + 1];
-        if( q1 - q0 < 2 || q1 - q0 > max_bin ) continue;
+        const uint32_t n = q1 - q0;
+        if( n < 2 || n > max_bin ) continue;
+        if( n <= kReg )
+        {
+            uint32_t v[kReg];
+#pragma unroll
+            for( int a = 0; a < kReg; ++a ) v[a] = a < (int)n ? idx[q0 + a] : 0xFFFFFFFFu;
+            bool sorted = true;
+#pragma unroll
+            for( int a = 1; a < kReg; ++a ) sorted = sorted && v[a - 1] < v[a];  // padding sorts last
+            if( sorted ) continue;
+            // odd-even transposition network (indices are distinct)
+#pragma unroll
+            for( int pass = 0; pass < kReg; ++pass )
+#pragma unroll
+                for( int a = pass & 1; a + 1 < kReg; a += 2 )
+                {
+                    const uint32_t lo = min( v[a], v[a + 1] ), hi = max( v[a], v[a + 1] );
+                    v[a] = lo;
+                    v[a + 1] = hi;
+                }
+#pragma unroll
+            for( int a = 0; a < kReg; ++a )
+                if( a < (int)n ) idx[q0 + a] = v[a];
+            continue;
+        }
         for( uint32_t q = q0 + 1; q < q1; ++q )
         {
             const uint32_t v = idx[q];
