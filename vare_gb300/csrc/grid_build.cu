@@ -28,26 +28,46 @@ __device__ inline bool inside_grid( const BoraGridDev& g, float x, float y, floa
     return !( x < 0.f || x > (float)g.nx || y < 0.f || y > (float)g.ny || z < 0.f || z > (float)g.nz );
 }
 
+__device__ inline uint32_t bin_one( const BoraGridDev& g, int32_t id, float x, float y, float z,
+                                    uint8_t* __restrict__ tile_flag )
+{
+    if( id < 0 ) return BORA_DEAD_KEY;
+    // activation tile: SparseFrame.cu:101-103 at tile edge 8, clamped to the table
+    const int ti = bora_imin( bora_imax( bora_trunc( x ) / BORA_TILE, 0 ), g.tx - 1 );
+    const int tj = bora_imin( bora_imax( bora_trunc( y ) / BORA_TILE, 0 ), g.ty - 1 );
+    const int tk = bora_imin( bora_imax( bora_trunc( z ) / BORA_TILE, 0 ), g.tz - 1 );
+    tile_flag[( (size_t)tk * g.ty + tj ) * g.tx + ti] = 1;
+    if( !inside_grid( g, x, y, z ) ) return BORA_DEAD_KEY - 1;
+    // dual cell = base of the P2G stencil (Rasterization.cu:139-141); <= n-1 inside
+    const int di = bora_imax( bora_trunc( x - 0.5f ), 0 );
+    const int dj = bora_imax( bora_trunc( y - 0.5f ), 0 );
+    const int dk = bora_imax( bora_trunc( z - 0.5f ), 0 );
+    const uint32_t vt = (uint32_t)( ( (size_t)( dk >> 3 ) * g.ty + ( dj >> 3 ) ) * g.tx + ( di >> 3 ) );
+    return vt * BORA_TILE_CELLS + (uint32_t)bora_local( di, dj, dk );
+}
+
+// Four particles per thread with 16-byte loads and stores (the arrays are 256-byte
+// aligned), the last n % 4 one by one.
 __global__ void k_bin( BoraGridDev g, BoraParticlesDev p, size_t n, uint32_t* __restrict__ vkey,
                        uint8_t* __restrict__ tile_flag )
 {
-    for( size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x )
+    const size_t n4 = n / 4;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for( size_t v = blockIdx.x * (size_t)blockDim.x + threadIdx.x; v < n4; v += stride )
     {
-        if( p.id[i] < 0 ) { vkey[i] = BORA_DEAD_KEY; continue; }
-        const float x = p.px[i], y = p.py[i], z = p.pz[i];
-        // activation tile: SparseFrame.cu:101-103 at tile edge 8, clamped to the table
-        const int ti = bora_imin( bora_imax( bora_trunc( x ) / BORA_TILE, 0 ), g.tx - 1 );
-        const int tj = bora_imin( bora_imax( bora_trunc( y ) / BORA_TILE, 0 ), g.ty - 1 );
-        const int tk = bora_imin( bora_imax( bora_trunc( z ) / BORA_TILE, 0 ), g.tz - 1 );
-        tile_flag[( (size_t)tk * g.ty + tj ) * g.tx + ti] = 1;
-        if( !inside_grid( g, x, y, z ) ) { vkey[i] = BORA_DEAD_KEY - 1; continue; }
-        // dual cell = base of the P2G stencil (Rasterization.cu:139-141); <= n-1 inside
-        const int di = bora_imax( bora_trunc( x - 0.5f ), 0 );
-        const int dj = bora_imax( bora_trunc( y - 0.5f ), 0 );
-        const int dk = bora_imax( bora_trunc( z - 0.5f ), 0 );
-        const uint32_t vt = (uint32_t)( ( (size_t)( dk >> 3 ) * g.ty + ( dj >> 3 ) ) * g.tx + ( di >> 3 ) );
-        vkey[i] = vt * BORA_TILE_CELLS + (uint32_t)bora_local( di, dj, dk );
+        const int4 id = reinterpret_cast<const int4*>( p.id )[v];
+        const float4 x = reinterpret_cast<const float4*>( p.px )[v];
+        const float4 y = reinterpret_cast<const float4*>( p.py )[v];
+        const float4 z = reinterpret_cast<const float4*>( p.pz )[v];
+        uint4 k;
+        k.x = bin_one( g, id.x, x.x, y.x, z.x, tile_flag );
+        k.y = bin_one( g, id.y, x.y, y.y, z.y, tile_flag );
+        k.z = bin_one( g, id.z, x.z, y.z, z.z, tile_flag );
+        k.w = bin_one( g, id.w, x.w, y.w, z.w, tile_flag );
+        reinterpret_cast<uint4*>( vkey )[v] = k;
     }
+    for( size_t i = n4 * 4 + blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += stride )
+        vkey[i] = bin_one( g, p.id[i], p.px[i], p.py[i], p.pz[i], tile_flag );
 }
 
 __global__ void k_activate( BoraGridDev g, const uint8_t* __restrict__ tile_flag, uint32_t* __restrict__ act, int tank_rows )
@@ -310,7 +330,7 @@ void bora_launch_tank( const BoraGridDev& g, int hh, int per_cell, float3 tr, fl
 void bora_launch_bin( const BoraGridDev& g, BoraParticlesDev p, size_t n, uint32_t* vkey, uint8_t* tile_flag, cudaStream_t st )
 {
     if( n == 0 ) return;
-    k_bin<<<grid_for( n ), kThreads, 0, st>>>( g, p, n, vkey, tile_flag );
+    k_bin<<<grid_for( ( n + 3 ) / 4 ), kThreads, 0, st>>>( g, p, n, vkey, tile_flag );
 }
 
 void bora_launch_activate( const BoraGridDev& g, const uint8_t* tile_flag, uint32_t* act, cudaStream_t st )
