@@ -256,93 +256,178 @@ __global__ void __launch_bounds__( 32 * kTilesPerCta ) k_mic_factor( int ntiles,
 
 // ---------------------------------------------------------------------------------
 // PCG update: r -= alpha q; z = M^-1 r (block-MIC(0) forward and backward sweeps over the
-// tile's 22 wavefront planes i+j+k = p in shared memory); rz = r.z and rr = r.r,
-// FP64-accurate. The matching e += alpha d is applied by the next direction kernel (which
-// reads d anyway) or by the refinement step. One warp per tile, persistent over tiles;
-// all of a tile's loads are issued before its first store; alpha is formed once per CTA.
-// The sweeps run in place (y over r, then z over y) and need no cell types: non-fluid
-// cells have M = 0 (k_mic_factor) and r = 0, so their y and z vanish, and a neighbour
-// outside the tile is skipped by its tile-local coordinate.
-constexpr int kUpdWarps = 4;
+// tile's 22 wavefront planes i+j+k = p); rz = r.z and rr = r.r, FP64-accurate. The matching
+// e += alpha d is applied by the next direction kernel (which reads d anyway) or by the
+// refinement step. One warp per tile, persistent over tiles; alpha is formed once per CTA.
+//
+// Sweep schedule: each lane owns two x-rows of the tile, (j, kq) and (j, kq + 4) with
+// j = lane & 7, kq = lane >> 3, i.e. tile rows lane and lane + 32; the tile's values and
+// pivots are staged in shared memory at cell address i + 8 j + 73 k, where the plane pitch 73
+// makes every step's 32 accesses fall in distinct banks. Step u of a sweep handles cell i = u - (j + k) - 1 of
+// every row at once, so a lane's cell address is its own row offset plus the compile-time u,
+// and the -y, -z (+y, +z) neighbours sit 8 and 73 cells below (above) it, computed in the
+// previous step. The -x (+x) neighbour is the lane's own previous step, kept in registers.
+// Steps outside a row's eight cells compute with pivot 0 (so they yield 0 and feed the row's
+// first cell a zero neighbour) and store nothing; neighbours outside the tile (j = 0 / 7,
+// k = 0 / 7) are masked, and zeroed guard cells keep every read inside the warp's buffers and
+// finite. The floating-point operations per cell are those of
+// the wavefront form: forward y_c = (r_c + M_x y_x + M_y y_y + M_z y_z) M_c as three chained
+// FMAs in the order -x, -y, -z; backward z_c = (y_c + M_c (z_x + z_y + z_z)) M_c with the sum
+// in the order +x, +y, +z. Non-fluid cells have M = 0 (k_mic_factor) and r = 0.
+namespace micsweep {
+constexpr int kPlane = 73;                          // buffer pitch of a z-plane (64 cells + 9)
+constexpr int kGuard = 80;                          // cells before the tile (reads reach -73)
+constexpr int kBuf = kGuard + 7 * kPlane + 64 + kPlane + 7;  // reads reach 574 + 73
+constexpr int kWarps = 4;
+}  // namespace micsweep
+constexpr int kUpdWarps = micsweep::kWarps;
 
-__global__ void __launch_bounds__( 32 * kUpdWarps ) k_pcg_update( int ntiles, BoraSolverDev sv, BoraReduceDev red,
+__global__ void __launch_bounds__( 32 * kUpdWarps, 5 ) k_pcg_update( int ntiles, BoraSolverDev sv, BoraReduceDev red,
                                                                   int slot_rz_in, int slot_dq_in, int slot_rz_out,
                                                                   int slot_rr_out )
 {
-    __shared__ __align__( 16 ) float sy[kUpdWarps][512];
-    __shared__ __align__( 16 ) float sm[kUpdWarps][512];
-    __shared__ uint16_t pc[512], ps[23];
+    using namespace micsweep;
+    __shared__ __align__( 16 ) float sval[kUpdWarps][kBuf];
+    __shared__ __align__( 16 ) float spiv[kUpdWarps][kBuf];
     __shared__ float s_alpha;
     bora_pdl_trigger();
-    load_plane_tables( pc, ps );
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float* const V = sval[w] + kGuard;  // tile cell (i, j, k) at V[i + 8 j + kPlane k]
+    float* const P = spiv[w] + kGuard;
+    for( int q = lane; q < kBuf; q += 32 ) { sval[w][q] = 0.f; spiv[w][q] = 0.f; }
     bora_pdl_wait();  // the previous kernel's results are complete from here
     if( threadIdx.x == 0 ) s_alpha = slot_rz_in < 0 ? 0.f : (float)( red.ring[slot_rz_in] / red.ring[slot_dq_in] );
     __syncthreads();
     const float alpha = s_alpha;
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    float* __restrict__ y = sy[w];
-    float* __restrict__ M = sm[w];
-    const float4* r4 = reinterpret_cast<const float4*>( sv.r );  // also written below
+    const int j = lane & 7, kq = lane >> 3, sA = j + kq;  // plane offset of row A; row B: sA + 4
+    const bool has_ym = j > 0, has_yp = j < 7, has_zmA = kq > 0, has_zpB = kq < 3;
+    // cell of row A at step u: VA + u (row B: VB + u)
+    const int rA = 8 * j + kPlane * kq, rB = rA + 4 * kPlane;  // element 0 of rows A and B
+    const int oA = rA - sA - 1, oB = rB - ( sA + 4 ) - 1;
+    float4* const r4 = reinterpret_cast<float4*>( sv.r );
+    float4* const z4 = reinterpret_cast<float4*>( sv.z );
     const float4* __restrict__ q4 = reinterpret_cast<const float4*>( sv.q );
     const float4* __restrict__ m4 = reinterpret_cast<const float4*>( sv.minv );
+    // Step u of a row with plane offset s. The operands that do not depend on the previous
+    // step (the cell's own value and pivot, the neighbours' pivots) are read one step ahead,
+    // so that only the two neighbour values computed in the previous step are waited for.
+    struct FwdOps { float r, p, py, pz; };
+    auto fwd_load = [&]( int o, bool zm ) -> FwdOps {
+        return { V[o], P[o], has_ym ? P[o - 8] : 0.f, zm ? P[o - kPlane] : 0.f };
+    };
+    // y = (r + M_x y_x + M_y y_y + M_z y_z) M
+    auto fwd_step = [&]( int o, int u, int s, const FwdOps& c, float& y, float& m ) {
+        const bool act = (unsigned)( u - s - 1 ) < 8u;
+        const float vy = V[o - 8], vz = V[o - kPlane];
+        float t = fmaf( m, y, c.r );
+        t = fmaf( c.py, vy, t );
+        t = fmaf( c.pz, vz, t );
+        m = act ? c.p : 0.f;
+        y = t * m;
+        if( act ) V[o] = y;
+    };
+    struct BwdOps { float y, p; };
+    auto bwd_load = [&]( int o ) -> BwdOps { return { V[o], P[o] }; };
+    // z = (y + M (z_x + z_y + z_z)) M
+    auto bwd_step = [&]( int o, int u, int s, bool zp, const BwdOps& c, float& z ) {
+        const bool act = (unsigned)( u - s - 1 ) < 8u;
+        const float zy = has_yp ? V[o + 8] : 0.f, zz = zp ? V[o + kPlane] : 0.f;
+        float acc = 0.f;
+        acc += z;
+        acc += zy;
+        acc += zz;
+        const float m = act ? c.p : 0.f;
+        z = fmaf( m, acc, c.y ) * m;
+        if( act ) V[o] = z;
+    };
+    // global traffic in whole-warp 512-byte float4 runs: float4 c = lane + 32 m of a tile holds
+    // cells 4c .. 4c + 3, which sit at buffer address 4c + 9 k, k = c >> 4
+    const int cbase = 4 * lane + 9 * ( lane >> 4 );  // + 146 m
+    auto prefetch_tile = [&]( int s ) {  // the tile's r, q and pivots into L2
+        if( s < ntiles && lane < 3 )
+        {
+            const float* src = ( lane == 0 ? sv.r : lane == 1 ? sv.q : sv.minv ) + (size_t)s * 512;
+            asm volatile( "cp.async.bulk.prefetch.L2.global [%0], 2048;" ::"l"( src ) : "memory" );
+        }
+    };
     DF prz{ 0.f, 0.f }, prr{ 0.f, 0.f };
-    for( int s = blockIdx.x * kUpdWarps + w; s < ntiles; s += gridDim.x * kUpdWarps )
+    const int tstride = gridDim.x * kUpdWarps;
+    // the next tile's r, q and pivots are loaded into registers before this tile's sweeps
+    float4 rn[4], qn[4], mn[4];
+    auto load_tile = [&]( int s ) {
+        if( s >= ntiles ) return;
+#pragma unroll
+        for( int m = 0; m < 4; ++m )
+        {
+            const size_t o = (size_t)s * 128 + lane + 32 * m;
+            rn[m] = r4[o];
+            qn[m] = q4[o];
+            mn[m] = m4[o];
+        }
+    };
+    load_tile( blockIdx.x * kUpdWarps + w );
+    for( int s = blockIdx.x * kUpdWarps + w; s < ntiles; s += tstride )
     {
-        const size_t b4 = (size_t)s * 128;
-        float4 r[4], q[4], mv[4];
+        const size_t b4 = (size_t)s * 128 + lane;
+        float4 r[4];
 #pragma unroll
-        for( int k = 0; k < 4; ++k )
+        for( int m = 0; m < 4; ++m )
         {
-            r[k] = r4[b4 + lane + 32 * k];
-            q[k] = q4[b4 + lane + 32 * k];
-            mv[k] = m4[b4 + lane + 32 * k];
+            r[m] = rn[m];
+            const float4 q = qn[m];
+            const float4 mv = mn[m];
+            r[m].x = fmaf( -alpha, q.x, r[m].x ); r[m].y = fmaf( -alpha, q.y, r[m].y );
+            r[m].z = fmaf( -alpha, q.z, r[m].z ); r[m].w = fmaf( -alpha, q.w, r[m].w );
+            r4[b4 + 32 * m] = r[m];
+            const int c = cbase + 146 * m;
+            V[c] = r[m].x; V[c + 1] = r[m].y; V[c + 2] = r[m].z; V[c + 3] = r[m].w;
+            P[c] = mv.x; P[c + 1] = mv.y; P[c + 2] = mv.z; P[c + 3] = mv.w;
+            prr = df_add_f( prr, dot4( r[m], r[m] ) );
         }
-#pragma unroll
-        for( int k = 0; k < 4; ++k )
-        {
-            r[k].x = fmaf( -alpha, q[k].x, r[k].x ); r[k].y = fmaf( -alpha, q[k].y, r[k].y );
-            r[k].z = fmaf( -alpha, q[k].z, r[k].z ); r[k].w = fmaf( -alpha, q[k].w, r[k].w );
-            reinterpret_cast<float4*>( sv.r )[b4 + lane + 32 * k] = r[k];
-            reinterpret_cast<float4*>( y )[lane + 32 * k] = r[k];
-            reinterpret_cast<float4*>( M )[lane + 32 * k] = mv[k];
-            prr = df_add_f( prr, dot4( r[k], r[k] ) );
-        }
+        load_tile( s + tstride );
+        prefetch_tile( s + 2 * tstride );
         __syncwarp();
-        // forward: y_c = (r_c + sum_{lower m} M_m y_m) M_c   (A_mc = -1)
-        for( int p = 0; p <= 21; ++p )
+        // forward: row A holds cells at u = 1 .. 18, row B at u = 5 .. 22
         {
-            for( int qq = ps[p] + lane; qq < ps[p + 1]; qq += 32 )
+            float yA = 0.f, mA = 0.f, yB = 0.f, mB = 0.f;  // the -x neighbour (previous step)
+            FwdOps cA = fwd_load( oA + 1, has_zmA ), cB = { 0.f, 0.f, 0.f, 0.f };
+#pragma unroll
+            for( int u = 1; u <= 22; ++u )
             {
-                const int l = pc[qq];
-                float t = y[l];
-                if( l & 7 ) t = fmaf( M[l - 1], y[l - 1], t );
-                if( l & 56 ) t = fmaf( M[l - 8], y[l - 8], t );
-                if( l & 448 ) t = fmaf( M[l - 64], y[l - 64], t );
-                y[l] = t * M[l];
+                FwdOps nA = { 0.f, 0.f, 0.f, 0.f }, nB = { 0.f, 0.f, 0.f, 0.f };
+                if( u + 1 <= 18 ) nA = fwd_load( oA + u + 1, has_zmA );
+                if( u + 1 >= 5 && u + 1 <= 22 ) nB = fwd_load( oB + u + 1, true );
+                if( u <= 18 ) fwd_step( oA + u, u, sA, cA, yA, mA );
+                if( u >= 5 ) fwd_step( oB + u, u, sA + 4, cB, yB, mB );
+                cA = nA;
+                cB = nB;
+                __syncwarp();
             }
-            __syncwarp();
         }
-        // backward: z_c = (y_c + M_c sum_{upper u} z_u) M_c
-        for( int p = 21; p >= 0; --p )
+        // backward, in place over y
         {
-            for( int qq = ps[p] + lane; qq < ps[p + 1]; qq += 32 )
+            float zA = 0.f, zB = 0.f;  // the +x neighbour (previous step)
+            BwdOps cB = bwd_load( oB + 22 ), cA = { 0.f, 0.f };
+#pragma unroll
+            for( int u = 22; u >= 1; --u )
             {
-                const int l = pc[qq];
-                float acc = 0.f;
-                if( ( l & 7 ) != 7 ) acc += y[l + 1];
-                if( ( l & 56 ) != 56 ) acc += y[l + 8];
-                if( ( l & 448 ) != 448 ) acc += y[l + 64];
-                const float Ml = M[l];
-                y[l] = fmaf( Ml, acc, y[l] ) * Ml;
+                BwdOps nA = { 0.f, 0.f }, nB = { 0.f, 0.f };
+                if( u - 1 >= 5 ) nB = bwd_load( oB + u - 1 );
+                if( u - 1 >= 1 && u - 1 <= 18 ) nA = bwd_load( oA + u - 1 );
+                if( u >= 5 ) bwd_step( oB + u, u, sA + 4, has_zpB, cB, zB );
+                if( u <= 18 ) bwd_step( oA + u, u, sA, true, cA, zA );
+                cA = nA;
+                cB = nB;
+                __syncwarp();
             }
-            __syncwarp();
         }
 #pragma unroll
-        for( int k = 0; k < 4; ++k )
+        for( int m = 0; m < 4; ++m )
         {
-            const float4 z = reinterpret_cast<const float4*>( y )[lane + 32 * k];
-            reinterpret_cast<float4*>( sv.z )[b4 + lane + 32 * k] = z;
-            prz = df_add_f( prz, dot4( r[k], z ) );
+            const int c = cbase + 146 * m;
+            const float4 z = make_float4( V[c], V[c + 1], V[c + 2], V[c + 3] );
+            z4[b4 + 32 * m] = z;
+            prz = df_add_f( prz, dot4( r[m], z ) );
         }
         __syncwarp();
     }
@@ -733,7 +818,11 @@ void bora_launch_pcg_update( int ntiles, const uint16_t* code, BoraSolverDev s, 
         if( cudaOccupancyMaxActiveBlocksPerMultiprocessor( &bps, k_pcg_update, 32 * kUpdWarps, 0 ) != cudaSuccess || bps <= 0 ) bps = 1;
         if( dev >= 0 && dev < 64 ) per_sm[dev] = bps;
     }
-    const int nb = std::max( 1, std::min( { ( ntiles + kUpdWarps - 1 ) / kUpdWarps, bps * num_sms(), 152 * 16 } ) );
+    // as many rounds of one tile per warp as the resident warps need, and the grid sized so
+    // that every warp gets that many tiles (no warp waits in the reduction for a straggler)
+    const int cap = std::max( 1, std::min( bps * num_sms(), 152 * 16 ) ) * kUpdWarps;
+    const int rounds = ( ntiles + cap - 1 ) / cap;
+    const int nb = std::max( 1, ( ntiles + kUpdWarps * rounds - 1 ) / ( kUpdWarps * rounds ) );
     bora_launch_pdl( k_pcg_update, nb, 32 * kUpdWarps, 0, st, ntiles, s, red, slot_rz_in, slot_dq_in, slot_rz_out,
                      slot_rr_out );
 }
