@@ -258,19 +258,21 @@ __global__ void __launch_bounds__( 32 * kTilesPerCta ) k_mic_factor( int ntiles,
 // PCG update: r -= alpha q; z = M^-1 r (block-MIC(0) forward and backward sweeps over the
 // tile's 22 wavefront planes i+j+k = p); rz = r.z and rr = r.r, FP64-accurate. The matching
 // e += alpha d is applied by the next direction kernel (which reads d anyway) or by the
-// refinement step. One warp per tile, persistent over tiles; alpha is formed once per CTA.
+// refinement step. One warp per tile, persistent over tiles (every warp gets the same
+// number of tiles; the next tile's r, q and pivots are loaded into registers during the
+// current tile's sweeps, the one after into L2); alpha is formed once per CTA.
 //
 // Sweep schedule: each lane owns two x-rows of the tile, (j, kq) and (j, kq + 4) with
 // j = lane & 7, kq = lane >> 3, i.e. tile rows lane and lane + 32; the tile's values and
-// pivots are staged in shared memory at cell address i + 8 j + 73 k, where the plane pitch 73
-// makes every step's 32 accesses fall in distinct banks. Step u of a sweep handles cell i = u - (j + k) - 1 of
-// every row at once, so a lane's cell address is its own row offset plus the compile-time u,
-// and the -y, -z (+y, +z) neighbours sit 8 and 73 cells below (above) it, computed in the
-// previous step. The -x (+x) neighbour is the lane's own previous step, kept in registers.
-// Steps outside a row's eight cells compute with pivot 0 (so they yield 0 and feed the row's
-// first cell a zero neighbour) and store nothing; neighbours outside the tile (j = 0 / 7,
-// k = 0 / 7) are masked, and zeroed guard cells keep every read inside the warp's buffers and
-// finite. The floating-point operations per cell are those of
+// pivots are staged in shared memory at cell address i + 8 j + 73 k, where the plane pitch
+// 73 makes every step's 32 accesses fall in distinct banks. Step u of a sweep handles cell
+// i = u - (j + k) - 1 of every row at once, so a lane's cell address is its own row offset
+// plus the compile-time u, and the -y, -z (+y, +z) neighbours sit 8 and 73 cells below
+// (above) it, computed in the previous step. The -x (+x) neighbour is the lane's own previous
+// step, kept in registers. Steps outside a row's eight cells compute with pivot 0 (so they
+// yield 0 and feed the row's first cell a zero neighbour) and store nothing; neighbours
+// outside the tile (j = 0 / 7, k = 0 / 7) are masked, and zeroed guard cells keep every read
+// inside the warp's buffers and finite. The floating-point operations per cell are those of
 // the wavefront form: forward y_c = (r_c + M_x y_x + M_y y_y + M_z y_z) M_c as three chained
 // FMAs in the order -x, -y, -z; backward z_c = (y_c + M_c (z_x + z_y + z_z)) M_c with the sum
 // in the order +x, +y, +z. Non-fluid cells have M = 0 (k_mic_factor) and r = 0.
@@ -278,7 +280,7 @@ namespace micsweep {
 constexpr int kPlane = 73;                          // buffer pitch of a z-plane (64 cells + 9)
 constexpr int kGuard = 80;                          // cells before the tile (reads reach -73)
 constexpr int kBuf = kGuard + 7 * kPlane + 64 + kPlane + 7;  // reads reach 574 + 73
-constexpr int kWarps = 4;
+constexpr int kWarps = 4;  // 4 x 5.9 KB of buffers per CTA; five CTAs per SM at 96 registers
 }  // namespace micsweep
 constexpr int kUpdWarps = micsweep::kWarps;
 
