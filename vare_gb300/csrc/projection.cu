@@ -459,133 +459,142 @@ __device__ inline size_t face_nbr( const int32_t* __restrict__ nbr, size_t cell,
 
 // ---------------------------------------------------------------------------------
 // PCG direction: e += alpha d (the previous update's step, pending); d' = z + beta d;
-// q = A d'; dq = d'.q (d double-buffered). Persistent CTAs
-// walk the tiles; each tile's d' is formed on the tile plus a 1-cell halo in shared memory
-// (non-fluid cells hold d = z = 0, so the stencil sum runs over all six neighbours in the
-// fixed order -x, +x, -y, +y, -z, +z without branches). The next tile's loads are issued
-// before the current tile's stencil, and the neighbour table two tiles ahead.
-namespace dirtile {
-constexpr int R = 10, N = R * R * R, NT = 256;
-constexpr int IA = ( N + NT - 1 ) / NT, IC = 512 / NT;
-constexpr uint32_t kValid = 1u << 31;
-__device__ inline uint32_t region_map( int h )  // bits 0-8 local index, 16-20 tile direction
-{
-    if( h >= N ) return 0;
-    const int a = h % R + 7, b = ( h / R ) % R + 7, c = h / ( R * R ) + 7;  // tile-local + 8, >= 0
-    return kValid | ( (uint32_t)bora_dir( ( a >> 3 ) - 1, ( b >> 3 ) - 1, ( c >> 3 ) - 1 ) << 16 ) |
-           (uint32_t)bora_local( a, b, c );
-}
-}  // namespace dirtile
+// q = A d'; dq = d'.q (d double-buffered). One warp per tile, persistent over tiles. Each
+// lane owns two x-rows of the tile, (j, kq) and (j, kq + 4) with j = lane & 7, kq = lane >> 3
+// (tile rows lane and lane + 32), read and written as 16-byte vectors. The stencil's x
+// neighbours are the lane's own registers, its y and z neighbours inside the tile come from
+// other lanes by shuffles, and the cells of the six face-neighbour tiles that the tile's
+// boundary rows need are loaded by the lanes that own those rows (d' formed the same way;
+// an inactive neighbour tile contributes 0). Non-fluid cells hold d = z = 0, so the stencil
+// sum runs over all six neighbours in the fixed order -x, +x, -y, +y, -z, +z; the dot
+// product adds d'.q of cells (i, j, k) and (i, j, k + 4) in float, then into a double-float
+// sum.
+constexpr int kDirWarps = 4;
 
-__global__ void __launch_bounds__( dirtile::NT ) k_pcg_direction_tiles( int ntiles, const int32_t* __restrict__ nbr,
-                                                                        const uint16_t* __restrict__ code, BoraSolverDev sv,
-                                                                        int dsel_in, BoraReduceDev red, int slot_rz_new,
-                                                                        int slot_rz_old, int slot_dq_out, int slot_a_rz,
-                                                                        int slot_a_dq )
+__global__ void __launch_bounds__( 32 * kDirWarps ) k_pcg_direction( int ntiles, const int32_t* __restrict__ nbr,
+                                                                    const uint16_t* __restrict__ code, BoraSolverDev sv,
+                                                                    int dsel_in, BoraReduceDev red, int slot_rz_new,
+                                                                    int slot_rz_old, int slot_dq_out, int slot_a_rz,
+                                                                    int slot_a_dq )
 {
-    using namespace dirtile;
-    __shared__ float dn_s[N];
-    __shared__ float do_s[512];  // d_old on the tile
-    __shared__ int32_t nbb[2][27];
     __shared__ float s_beta, s_alpha;
-    const int tid = threadIdx.x, G = gridDim.x;
     bora_pdl_trigger();
-    const bool upd_e = slot_a_rz >= 0;  // the previous update's e += alpha d is still pending
-    auto nbr_entry = [&]( int s ) { return s < ntiles ? nbr[(size_t)s * 27 + tid] : -1; };
-    if( tid < 27 )  // tile tables: not written by the solver chain
-    {
-        nbb[0][tid] = nbr_entry( blockIdx.x );
-        nbb[1][tid] = nbr_entry( blockIdx.x + G );
-    }
-    uint32_t am[IA];
-#pragma unroll
-    for( int it = 0; it < IA; ++it ) am[it] = region_map( tid + it * NT );
     bora_pdl_wait();  // the previous kernel's results (ring, z, d, e) are complete from here
-    if( tid == 0 )
+    if( threadIdx.x == 0 )
     {
         s_beta = slot_rz_old < 0 ? 0.f : (float)( red.ring[slot_rz_new] / red.ring[slot_rz_old] );
         s_alpha = slot_a_rz < 0 ? 0.f : (float)( red.ring[slot_a_rz] / red.ring[slot_a_dq] );
     }
     __syncthreads();
     const float beta = s_beta, alpha = s_alpha;
+    const bool upd_e = slot_a_rz >= 0;  // the previous update's e += alpha d is still pending
     const float* __restrict__ dold = dsel_in ? sv.d[1] : sv.d[0];  // selects keep sv out of local memory
     float* __restrict__ dnew = dsel_in ? sv.d[0] : sv.d[1];
-    float dv[IA], zv[IA], ev[IC];
-    uint32_t cv[IC];
-#define BORA_DIR_ISSUE( NB, S )                                                      \
-    _Pragma( "unroll" ) for( int it = 0; it < IA; ++it )                             \
-    {                                                                                \
-        const uint32_t m = am[it];                                                   \
-        const int sl = ( m & kValid ) ? ( NB )[( m >> 16 ) & 31] : -1;               \
-        dv[it] = 0.f;                                                                \
-        zv[it] = 0.f;                                                                \
-        if( sl >= 0 )                                                                \
-        {                                                                            \
-            const size_t g = (size_t)sl * 512 + ( m & 511u );                        \
-            dv[it] = dold[g];                                                        \
-            zv[it] = sv.z[g];                                                        \
-        }                                                                            \
-    }                                                                                \
-    _Pragma( "unroll" ) for( int it = 0; it < IC; ++it )                             \
-    {                                                                                \
-        cv[it] = code[(size_t)( S ) * 512 + tid + it * NT];                          \
-        if( upd_e ) ev[it] = sv.e[(size_t)( S ) * 512 + tid + it * NT];              \
-    }
-    BORA_DIR_ISSUE( nbb[0], blockIdx.x );
+    const int lane = threadIdx.x & 31, j = lane & 7, kq = lane >> 3;
+    constexpr unsigned kAll = 0xffffffffu;
+    // d' of 8 consecutive cells starting at cell c of tile slot t (0 when t < 0)
+    auto halo8 = [&]( int t, int c, float* v ) {
+        if( t < 0 ) { for( int i = 0; i < 8; ++i ) v[i] = 0.f; return; }
+        const size_t g = (size_t)t * 512 + c;
+        const float4 d0 = *reinterpret_cast<const float4*>( dold + g ), d1 = *reinterpret_cast<const float4*>( dold + g + 4 );
+        const float4 z0 = *reinterpret_cast<const float4*>( sv.z + g ), z1 = *reinterpret_cast<const float4*>( sv.z + g + 4 );
+        v[0] = fmaf( beta, d0.x, z0.x ); v[1] = fmaf( beta, d0.y, z0.y ); v[2] = fmaf( beta, d0.z, z0.z ); v[3] = fmaf( beta, d0.w, z0.w );
+        v[4] = fmaf( beta, d1.x, z1.x ); v[5] = fmaf( beta, d1.y, z1.y ); v[6] = fmaf( beta, d1.z, z1.z ); v[7] = fmaf( beta, d1.w, z1.w );
+    };
+    auto halo1 = [&]( int t, int c ) { return t < 0 ? 0.f : fmaf( beta, dold[(size_t)t * 512 + c], sv.z[(size_t)t * 512 + c] ); };
     DF pdq{ 0.f, 0.f };
-    int n = 0;
-    for( int s = blockIdx.x; s < ntiles; s += G, ++n )
+    for( int s = blockIdx.x * kDirWarps + ( threadIdx.x >> 5 ); s < ntiles; s += gridDim.x * kDirWarps )
     {
+        const int32_t* __restrict__ nb = nbr + (size_t)s * 27;  // tile tables: not written by the solver chain
+        const int smx = nb[bora_dir( -1, 0, 0 )], spx = nb[bora_dir( 1, 0, 0 )];
+        const int smy = nb[bora_dir( 0, -1, 0 )], spy = nb[bora_dir( 0, 1, 0 )];
+        const int smz = nb[bora_dir( 0, 0, -1 )], spz = nb[bora_dir( 0, 0, 1 )];
+        const size_t gA = (size_t)s * 512 + 8 * lane, gB = gA + 256;
+        // own rows: d' = z + beta d and the pending e += alpha d, both stored right away
+        float dA[8], dB[8];
+        uint16_t cA[8], cB[8];
 #pragma unroll
-        for( int it = 0; it < IA; ++it )
+        for( int r = 0; r < 2; ++r )
         {
-            const int h = tid + it * NT;
-            if( h < N )
+            const size_t g = r ? gB : gA;
+            float* dn = r ? dB : dA;
+            uint16_t* cc = r ? cB : cA;
+            halo8( s, (int)( g - (size_t)s * 512 ), dn );
+            reinterpret_cast<float4*>( dnew + g )[0] = make_float4( dn[0], dn[1], dn[2], dn[3] );
+            reinterpret_cast<float4*>( dnew + g )[1] = make_float4( dn[4], dn[5], dn[6], dn[7] );
+            const uint4 cw = *reinterpret_cast<const uint4*>( code + g );
+            const uint32_t w4[4] = { cw.x, cw.y, cw.z, cw.w };
+#pragma unroll
+            for( int i = 0; i < 4; ++i ) { cc[2 * i] = (uint16_t)( w4[i] & 0xffffu ); cc[2 * i + 1] = (uint16_t)( w4[i] >> 16 ); }
+            if( upd_e )
             {
-                dn_s[h] = fmaf( beta, dv[it], zv[it] );
-                if( ( ( am[it] >> 16 ) & 31u ) == 13u ) do_s[am[it] & 511u] = dv[it];  // tile cell
+                const float4 d0 = *reinterpret_cast<const float4*>( dold + g ), d1 = *reinterpret_cast<const float4*>( dold + g + 4 );
+                float4 e0 = *reinterpret_cast<const float4*>( sv.e + g ), e1 = *reinterpret_cast<const float4*>( sv.e + g + 4 );
+                e0.x = fmaf( alpha, d0.x, e0.x ); e0.y = fmaf( alpha, d0.y, e0.y ); e0.z = fmaf( alpha, d0.z, e0.z ); e0.w = fmaf( alpha, d0.w, e0.w );
+                e1.x = fmaf( alpha, d1.x, e1.x ); e1.y = fmaf( alpha, d1.y, e1.y ); e1.z = fmaf( alpha, d1.z, e1.z ); e1.w = fmaf( alpha, d1.w, e1.w );
+                reinterpret_cast<float4*>( sv.e + g )[0] = e0;
+                reinterpret_cast<float4*>( sv.e + g )[1] = e1;
             }
         }
-        float ee[IC];
-#pragma unroll
-        for( int it = 0; it < IC; ++it ) ee[it] = ev[it];
-        uint32_t cc[IC];
-#pragma unroll
-        for( int it = 0; it < IC; ++it ) cc[it] = cv[it];
-        const int32_t nb2 = tid < 27 ? nbr_entry( s + 2 * G ) : -1;
-        __syncthreads();
-        if( s + G < ntiles ) { BORA_DIR_ISSUE( nbb[( n + 1 ) & 1], s + G ); }
-        float tdq = 0.f;  // this thread's d'.q over its cells of the tile
-#pragma unroll
-        for( int it = 0; it < IC; ++it )
+        // neighbour-tile cells: x ends of both rows; the y face row of lanes j = 0 / 7 (both
+        // rows); the z face row of row A at k = 0 (-z) and of row B at k = 7 (+z)
+        const float xmA = halo1( smx, 8 * lane + 7 ), xpA = halo1( spx, 8 * lane );
+        const float xmB = halo1( smx, 256 + 8 * lane + 7 ), xpB = halo1( spx, 256 + 8 * lane );
+        float yhA[8], yhB[8], zh[8];
         {
-            const int l = tid + it * NT;
-            const int h = ( l & 7 ) + 1 + R * ( ( ( l >> 3 ) & 7 ) + 1 + R * ( ( l >> 6 ) + 1 ) );
-            const float dn = dn_s[h];
-            float qv = 0.f;
-            if( cc[it] & BORA_CODE_FLUID )
+            const int yt = j == 0 ? smy : ( j == 7 ? spy : -1 );
+            const int yc = 8 * ( lane - j ) + ( j == 0 ? 56 : 0 );  // row (7 or 0, kq) of the neighbour tile
+            halo8( yt, yc, yhA );
+            halo8( yt, yc + 256, yhB );
+            const int zt = kq == 0 ? smz : ( kq == 3 ? spz : -1 );
+            const int zc = 8 * j + ( kq == 0 ? 448 : 0 );  // row (j, 7) or (j, 0) of the neighbour tile
+            halo8( zt, zc, zh );
+        }
+        float qA[8], qB[8];
+        float tdq[8];
+#pragma unroll
+        for( int i = 0; i < 8; ++i )
+        {
+            // y neighbours (lanes j -+ 1), z neighbours (lanes -+ 8, across the two rows)
+            float ymA = __shfl_up_sync( kAll, dA[i], 1 ), ypA = __shfl_down_sync( kAll, dA[i], 1 );
+            float ymB = __shfl_up_sync( kAll, dB[i], 1 ), ypB = __shfl_down_sync( kAll, dB[i], 1 );
+            if( j == 0 ) { ymA = yhA[i]; ymB = yhB[i]; }
+            if( j == 7 ) { ypA = yhA[i]; ypB = yhB[i]; }
+            float zmA = __shfl_up_sync( kAll, dA[i], 8 );
+            if( kq == 0 ) zmA = zh[i];
+            const float zpA = __shfl_sync( kAll, kq == 0 ? dB[i] : dA[i], ( lane + 8 ) & 31 );
+            const float zmB = __shfl_sync( kAll, kq == 3 ? dA[i] : dB[i], ( lane + 24 ) & 31 );
+            float zpB = __shfl_down_sync( kAll, dB[i], 8 );
+            if( kq == 3 ) zpB = zh[i];
+            const float xmA_ = i > 0 ? dA[i > 0 ? i - 1 : 0] : xmA, xpA_ = i < 7 ? dA[i < 7 ? i + 1 : 7] : xpA;
+            const float xmB_ = i > 0 ? dB[i > 0 ? i - 1 : 0] : xmB, xpB_ = i < 7 ? dB[i < 7 ? i + 1 : 7] : xpB;
+            qA[i] = 0.f;
+            qB[i] = 0.f;
+            float t = 0.f;
+            if( cA[i] & BORA_CODE_FLUID )
             {
                 float acc = 0.f;
-                acc += dn_s[h - 1];
-                acc += dn_s[h + 1];
-                acc += dn_s[h - R];
-                acc += dn_s[h + R];
-                acc += dn_s[h - R * R];
-                acc += dn_s[h + R * R];
-                qv = fmaf( (float)code_diag( (uint16_t)cc[it] ), dn, -acc );
-                tdq = fmaf( dn, qv, tdq );
+                acc += xmA_; acc += xpA_; acc += ymA; acc += ypA; acc += zmA; acc += zpA;
+                qA[i] = fmaf( (float)code_diag( cA[i] ), dA[i], -acc );
+                t = fmaf( dA[i], qA[i], t );
             }
-            const size_t g = (size_t)s * 512 + l;
-            dnew[g] = dn;
-            sv.q[g] = qv;
-            if( upd_e ) sv.e[g] = fmaf( alpha, do_s[l], ee[it] );
+            if( cB[i] & BORA_CODE_FLUID )
+            {
+                float acc = 0.f;
+                acc += xmB_; acc += xpB_; acc += ymB; acc += ypB; acc += zmB; acc += zpB;
+                qB[i] = fmaf( (float)code_diag( cB[i] ), dB[i], -acc );
+                t = fmaf( dB[i], qB[i], t );
+            }
+            tdq[i] = t;
         }
-        pdq = df_add_f( pdq, tdq );
-        if( tid < 27 ) nbb[n & 1][tid] = nb2;
-        __syncthreads();
+        reinterpret_cast<float4*>( sv.q + gA )[0] = make_float4( qA[0], qA[1], qA[2], qA[3] );
+        reinterpret_cast<float4*>( sv.q + gA )[1] = make_float4( qA[4], qA[5], qA[6], qA[7] );
+        reinterpret_cast<float4*>( sv.q + gB )[0] = make_float4( qB[0], qB[1], qB[2], qB[3] );
+        reinterpret_cast<float4*>( sv.q + gB )[1] = make_float4( qB[4], qB[5], qB[6], qB[7] );
+#pragma unroll
+        for( int i = 0; i < 8; ++i ) pdq = df_add_f( pdq, tdq[i] );
     }
     reduce2_publish_warp( df_warp_sum( pdq ), 0.0, 0, red, slot_dq_out, -1 );
-#undef BORA_DIR_ISSUE
 }
 
 // ---------------------------------------------------------------------------------
@@ -840,11 +849,14 @@ void bora_launch_pcg_direction( const BoraGridDev&, int ntiles, BoraTilesDev t, 
     int b = dev >= 0 && dev < 64 ? per_sm[dev] : 0;
     if( b <= 0 )
     {
-        if( cudaOccupancyMaxActiveBlocksPerMultiprocessor( &b, k_pcg_direction_tiles, dirtile::NT, 0 ) != cudaSuccess || b <= 0 ) b = 1;
+        if( cudaOccupancyMaxActiveBlocksPerMultiprocessor( &b, k_pcg_direction, 32 * kDirWarps, 0 ) != cudaSuccess || b <= 0 ) b = 1;
         if( dev >= 0 && dev < 64 ) per_sm[dev] = b;
     }
-    const int grid = std::max( 1, std::min( { ntiles, b * num_sms(), 152 * 16 } ) );  // partial sums capacity
-    bora_launch_pdl( k_pcg_direction_tiles, grid, dirtile::NT, 0, st, ntiles, (const int32_t*)t.nbr, code, s, dsel_in, red,
+    // every warp gets the same number of tiles; at most 152 x 16 CTAs (partial sums capacity)
+    const int cap = std::max( 1, std::min( b * num_sms(), 152 * 16 ) ) * kDirWarps;
+    const int rounds = ( ntiles + cap - 1 ) / cap;
+    const int grid = std::max( 1, ( ntiles + kDirWarps * rounds - 1 ) / ( kDirWarps * rounds ) );
+    bora_launch_pdl( k_pcg_direction, grid, 32 * kDirWarps, 0, st, ntiles, (const int32_t*)t.nbr, code, s, dsel_in, red,
                      slot_rz_new, slot_rz_old, slot_dq_out, slot_a_rz, slot_a_dq );
 }
 
