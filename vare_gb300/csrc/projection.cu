@@ -832,7 +832,7 @@ void bora_launch_pcg_update( int ntiles, const uint16_t* code, BoraSolverDev s, 
     // as many rounds of one tile per warp as the resident warps need, and the grid sized so
     // that every warp gets that many tiles (no warp waits in the reduction for a straggler)
     const int cap = std::max( 1, std::min( bps * num_sms(), 152 * 16 ) ) * kUpdWarps;
-    const int rounds = ( ntiles + cap - 1 ) / cap;
+    const int rounds = std::max( 1, ( ntiles + cap - 1 ) / cap );  // one block even for no tiles: it publishes the sums
     const int nb = std::max( 1, ( ntiles + kUpdWarps * rounds - 1 ) / ( kUpdWarps * rounds ) );
     bora_launch_pdl( k_pcg_update, nb, 32 * kUpdWarps, 0, st, ntiles, s, red, slot_rz_in, slot_dq_in, slot_rz_out,
                      slot_rr_out );
