@@ -8,7 +8,35 @@
 
 #include "flip_common.cuh"
 
+#include <atomic>
 #include <utility>
+
+// ---- per-device values computed on first use ------------------------------------------
+// Launch shapes and device attributes are queried once per device ordinal. Host threads
+// that drive different handles (the serving layer runs one per request) may race to fill an
+// entry: each computes the same value, and the entries are atomics. Declare instances with
+// static storage (zero-initialised).
+class BoraPerDevice
+{
+public:
+    template <class F>
+    int get( F compute )
+    {
+        int dev = 0;
+        if( cudaGetDevice( &dev ) != cudaSuccess || dev < 0 || dev >= kMaxDevices ) return compute();
+        int v = v_[dev].load( std::memory_order_acquire );
+        if( v <= 0 )
+        {
+            v = compute();
+            v_[dev].store( v, std::memory_order_release );
+        }
+        return v;
+    }
+
+private:
+    static constexpr int kMaxDevices = 64;
+    std::atomic<int> v_[kMaxDevices];
+};
 
 // ---- programmatic dependent launch ---------------------------------------------------
 // The kernels of a solver iteration form a chain in which each one reads what the one

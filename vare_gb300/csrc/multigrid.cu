@@ -1168,40 +1168,38 @@ __global__ void __launch_bounds__( 256 ) k_pcg_update_noprec( size_t ncells, Bor
     reduce2_publish_warp( df_warp_sum( rr ), 0.0, 0, red, slot_rr_out, -1 );
 }
 
-int g_sms = 0;
+int sm_count()
+{
+    static BoraPerDevice sms;
+    return sms.get( [] {
+        int dev = 0, n = 0;
+        cudaGetDevice( &dev );
+        cudaDeviceGetAttribute( &n, cudaDevAttrMultiProcessorCount, dev );
+        return n > 0 ? n : 152;
+    } );
+}
+
 int blocks_for( size_t n )
 {
-    if( g_sms <= 0 )
-    {
-        int dev = 0;
-        cudaGetDevice( &dev );
-        cudaDeviceGetAttribute( &g_sms, cudaDevAttrMultiProcessorCount, dev );
-        if( g_sms <= 0 ) g_sms = 152;
-    }
-    return (int)std::max<size_t>( 1, std::min<size_t>( ( n + 255 ) / 256, (size_t)g_sms * 8 ) );
+    return (int)std::max<size_t>( 1, std::min<size_t>( ( n + 255 ) / 256, (size_t)sm_count() * 8 ) );
 }
 
 // Persistent grid for a fused kernel: as many CTAs as can be resident at once.
 template <class K>
-int fused_grid( K kernel, int nt, int ntiles, int* per_sm )
+int fused_grid( K kernel, int nt, int ntiles, BoraPerDevice& per_sm )
 {
-    int dev = 0;
-    cudaGetDevice( &dev );
-    int b = dev >= 0 && dev < 64 ? per_sm[dev] : 0;
-    if( b <= 0 )
-    {
-        if( cudaOccupancyMaxActiveBlocksPerMultiprocessor( &b, kernel, nt, 0 ) != cudaSuccess || b <= 0 ) b = 1;
-        if( dev >= 0 && dev < 64 ) per_sm[dev] = b;
-    }
-    blocks_for( 1 );  // sets g_sms
-    return std::max( 1, std::min( ntiles, b * g_sms ) );
+    const int b = per_sm.get( [&] {
+        int v = 0;
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor( &v, kernel, nt, 0 ) == cudaSuccess && v > 0 ? v : 1;
+    } );
+    return std::max( 1, std::min( ntiles, b * sm_count() ) );
 }
 
 template <int E, bool L0>
 void launch_down_fused( const BoraLevelDev& F, const BoraLevelDev& C, BoraTilesDev t, int ntiles, const float* r0,
                         int slot_rr, const double* ring, cudaStream_t st )
 {
-    static int per_sm[64] = { 0 };
+    static BoraPerDevice per_sm;
     constexpr int NT = TileRegion<E>::NT;
     const int grid = fused_grid( k_mg_down_fused<E, L0>, NT, ntiles, per_sm );
     bora_launch_pdl( k_mg_down_fused<E, L0>, grid, NT, 0, st, F, C, t, ntiles, r0, slot_rr, ring );
@@ -1211,7 +1209,7 @@ template <int E, bool L0>
 void launch_up_fused( const BoraLevelDev& F, const __half* ec, BoraTilesDev t, int ntiles, const float* r0,
                       int slot_rr, BoraReduceDev red, float* zout, int slot_rz, cudaStream_t st )
 {
-    static int per_sm[64] = { 0 };
+    static BoraPerDevice per_sm;
     constexpr int NT = TileRegion<E>::NT;
     int grid = fused_grid( k_mg_up_fused<E, L0>, NT, ntiles, per_sm );
     if( L0 ) grid = std::min( grid, 152 * 16 );  // partial sums capacity of the reduction
@@ -1281,29 +1279,27 @@ bool fused_level( const BoraLevelDev& L ) { return L.kind == 0 && L.E >= 2; }
 // kernel, else the portable 8.
 int tail_cluster_size()
 {
-    static int size[64] = { 0 };
-    int dev = 0;
-    cudaGetDevice( &dev );
-    if( dev >= 0 && dev < 64 && size[dev] > 0 ) return size[dev];
-    int n = 8;
-    if( cudaFuncSetAttribute( k_mg_tail, cudaFuncAttributeNonPortableClusterSizeAllowed, 1 ) == cudaSuccess )
-    {
-        cudaLaunchConfig_t cfg{};
-        cfg.gridDim = dim3( kTailCtasMax );
-        cfg.blockDim = dim3( kTailThreads );
-        cudaLaunchAttribute attr[1];
-        attr[0].id = cudaLaunchAttributeClusterDimension;
-        attr[0].val.clusterDim.x = kTailCtasMax;
-        attr[0].val.clusterDim.y = 1;
-        attr[0].val.clusterDim.z = 1;
-        cfg.attrs = attr;
-        cfg.numAttrs = 1;
-        int clusters = 0;
-        if( cudaOccupancyMaxActiveClusters( &clusters, k_mg_tail, &cfg ) == cudaSuccess && clusters > 0 ) n = kTailCtasMax;
-    }
-    cudaGetLastError();  // a refused query leaves no error behind
-    if( dev >= 0 && dev < 64 ) size[dev] = n;
-    return n;
+    static BoraPerDevice size;
+    return size.get( [] {
+        int n = 8;
+        if( cudaFuncSetAttribute( k_mg_tail, cudaFuncAttributeNonPortableClusterSizeAllowed, 1 ) == cudaSuccess )
+        {
+            cudaLaunchConfig_t cfg{};
+            cfg.gridDim = dim3( kTailCtasMax );
+            cfg.blockDim = dim3( kTailThreads );
+            cudaLaunchAttribute attr[1];
+            attr[0].id = cudaLaunchAttributeClusterDimension;
+            attr[0].val.clusterDim.x = kTailCtasMax;
+            attr[0].val.clusterDim.y = 1;
+            attr[0].val.clusterDim.z = 1;
+            cfg.attrs = attr;
+            cfg.numAttrs = 1;
+            int clusters = 0;
+            if( cudaOccupancyMaxActiveClusters( &clusters, k_mg_tail, &cfg ) == cudaSuccess && clusters > 0 ) n = kTailCtasMax;
+        }
+        cudaGetLastError();  // a refused query leaves no error behind
+        return n;
+    } );
 }
 
 }  // namespace

@@ -168,13 +168,10 @@ void bora_launch_p2g( const BoraGridDev& g, int ntiles, BoraTilesDev t, BoraPart
                       const uint32_t* start, BoraCellsDev c, cudaStream_t st )
 {
     if( ntiles <= 0 ) return;
-    static bool attr_set[64] = { false };
-    int dev = 0;
-    cudaGetDevice( &dev );
-    if( dev >= 0 && dev < 64 && !attr_set[dev] )
-    {
+    static BoraPerDevice attr_set;
+    attr_set.get( [] {
         cudaFuncSetAttribute( k_p2g, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kP2GSmem );
-        attr_set[dev] = true;
-    }
+        return 1;
+    } );
     k_p2g<<<ntiles, kP2GThreads, kP2GSmem, st>>>( g, t, p, idx, start, c );
 }

@@ -149,30 +149,27 @@ struct PlaneTables
     }
 };
 
-bool g_tables_ready[64] = { false };
-int g_num_sms[64] = { 0 };
-
 void ensure_tables()
 {
-    int dev = 0;
-    cudaGetDevice( &dev );
-    if( dev < 0 || dev >= 64 || g_tables_ready[dev] ) return;
-    static const PlaneTables tbl;
-    cudaMemcpyToSymbol( g_plane_cells, tbl.cells, sizeof( tbl.cells ) );
-    cudaMemcpyToSymbol( g_plane_start, tbl.start, sizeof( tbl.start ) );
-    g_tables_ready[dev] = true;
+    static BoraPerDevice ready;
+    ready.get( [] {
+        static const PlaneTables tbl;
+        cudaMemcpyToSymbol( g_plane_cells, tbl.cells, sizeof( tbl.cells ) );
+        cudaMemcpyToSymbol( g_plane_start, tbl.start, sizeof( tbl.start ) );
+        cudaDeviceSynchronize();  // the tables are in place before any stream's kernel reads them
+        return 1;
+    } );
 }
 
 int num_sms()
 {
-    int dev = 0;
-    cudaGetDevice( &dev );
-    if( dev >= 0 && dev < 64 && g_num_sms[dev] > 0 ) return g_num_sms[dev];
-    int n = 0;
-    cudaDeviceGetAttribute( &n, cudaDevAttrMultiProcessorCount, dev );
-    if( n <= 0 ) n = 152;
-    if( dev >= 0 && dev < 64 ) g_num_sms[dev] = n;
-    return n;
+    static BoraPerDevice sms;
+    return sms.get( [] {
+        int dev = 0, n = 0;
+        cudaGetDevice( &dev );
+        cudaDeviceGetAttribute( &n, cudaDevAttrMultiProcessorCount, dev );
+        return n > 0 ? n : 152;
+    } );
 }
 
 __device__ inline void load_plane_tables( uint16_t* pc, uint16_t* ps )
@@ -819,16 +816,11 @@ void bora_launch_pcg_update( int ntiles, const uint16_t* code, BoraSolverDev s, 
                              int slot_dq_in, int slot_rz_out, int slot_rr_out, cudaStream_t st )
 {
     (void)code;
-    ensure_tables();
-    static int per_sm[64] = { 0 };
-    int dev = 0;
-    cudaGetDevice( &dev );
-    int bps = dev >= 0 && dev < 64 ? per_sm[dev] : 0;
-    if( bps <= 0 )
-    {
-        if( cudaOccupancyMaxActiveBlocksPerMultiprocessor( &bps, k_pcg_update, 32 * kUpdWarps, 0 ) != cudaSuccess || bps <= 0 ) bps = 1;
-        if( dev >= 0 && dev < 64 ) per_sm[dev] = bps;
-    }
+    static BoraPerDevice per_sm;
+    const int bps = per_sm.get( [] {
+        int v = 0;
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor( &v, k_pcg_update, 32 * kUpdWarps, 0 ) == cudaSuccess && v > 0 ? v : 1;
+    } );
     // as many rounds of one tile per warp as the resident warps need, and the grid sized so
     // that every warp gets that many tiles (no warp waits in the reduction for a straggler)
     const int cap = std::max( 1, std::min( bps * num_sms(), 152 * 16 ) ) * kUpdWarps;
@@ -843,15 +835,11 @@ void bora_launch_pcg_direction( const BoraGridDev&, int ntiles, BoraTilesDev t, 
                                 int slot_a_rz, int slot_a_dq, cudaStream_t st )
 {
     if( ntiles <= 0 ) return;
-    static int per_sm[64] = { 0 };
-    int dev = 0;
-    cudaGetDevice( &dev );
-    int b = dev >= 0 && dev < 64 ? per_sm[dev] : 0;
-    if( b <= 0 )
-    {
-        if( cudaOccupancyMaxActiveBlocksPerMultiprocessor( &b, k_pcg_direction, 32 * kDirWarps, 0 ) != cudaSuccess || b <= 0 ) b = 1;
-        if( dev >= 0 && dev < 64 ) per_sm[dev] = b;
-    }
+    static BoraPerDevice per_sm;
+    const int b = per_sm.get( [] {
+        int v = 0;
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor( &v, k_pcg_direction, 32 * kDirWarps, 0 ) == cudaSuccess && v > 0 ? v : 1;
+    } );
     // every warp gets the same number of tiles; at most 152 x 16 CTAs (partial sums capacity)
     const int cap = std::max( 1, std::min( b * num_sms(), 152 * 16 ) ) * kDirWarps;
     const int rounds = ( ntiles + cap - 1 ) / cap;

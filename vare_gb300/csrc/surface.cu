@@ -740,17 +740,13 @@ int bora_tank_scan_launches( const BoraGridDev& g, int ntiles, BoraTilesDev t, f
 template <bool TANK>
 int redistance_grid( int ntiles )
 {
-    static int per_sm[64] = { 0 };
-    int dev = 0;
+    static BoraPerDevice per_sm;
+    const int b = per_sm.get( [] {
+        int v = 0;
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor( &v, k_redistance<TANK>, kRedistThreads, 0 ) == cudaSuccess && v > 0 ? v : 1;
+    } );
+    int dev = 0, sms = 0;
     cudaGetDevice( &dev );
-    int b = dev >= 0 && dev < 64 ? per_sm[dev] : 0;
-    if( b <= 0 )
-    {
-        if( cudaOccupancyMaxActiveBlocksPerMultiprocessor( &b, k_redistance<TANK>, kRedistThreads, 0 ) != cudaSuccess || b <= 0 )
-            b = 1;
-        if( dev >= 0 && dev < 64 ) per_sm[dev] = b;
-    }
-    int sms = 0;
     cudaDeviceGetAttribute( &sms, cudaDevAttrMultiProcessorCount, dev );
     return std::max( 1, std::min( ntiles, b * std::max( sms, 1 ) ) );
 }
