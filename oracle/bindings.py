@@ -1,4 +1,4 @@
-"""ORACLE (test infrastructure only): ctypes bindings for the CPU checkers.
+"""ORACLE (test infrastructure only): ctypes bindings for the CPU oracles.
 
 * `Oracle` wraps oracle/_build/liboracle_flip.so, the CPU restatement of the
   reference's FLIP substep (flip_oracle.cpp), in "compat" mode (4^3 tiles, the

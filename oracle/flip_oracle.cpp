@@ -2,7 +2,7 @@
 // FLIP substep, FLIPMethod::advanceOneStep (base/source/FLIPMethod.cu:208-298).
 //
 // Only tests, __graft_entry__.smoke() and bench.py's CPU-baseline leg may load this
-// library, and only as the checker or the timed CPU baseline; the product path never
+// library, and only as the test oracle or the timed CPU baseline; the product path never
 // calls it.
 //
 // Each stage follows the reference's arithmetic in the same operation order, so that

@@ -3,7 +3,7 @@
 // ORACLE INFRASTRUCTURE. This header lets the reference's own FLIP sources
 // (base/source/{SparseFrame,Rasterization,FluidProjection,BLAS,FieldOP,FLIPMethod}.cu
 // and {ArrayUtils,LinearSystemSolver,Particles}.cpp) compile unmodified with g++ for
-// the host CPU, so that the reference itself can be run as a checker and as the
+// the host CPU, so that the reference itself can be run as a test oracle and as the
 // timed CPU baseline. It is never linked into the product library.
 //
 // What it provides in place of the reference's Foundation.h (base/header/Foundation.h:58-107):
