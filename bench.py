@@ -81,6 +81,9 @@ def parse():
                     help="mark the timed steps and one post-processing frame with NVTX ranges 'step' and 'post' "
                          "(for a profiler's range filter)")
     ap.add_argument("--cpu-steps", type=int, default=2)
+    ap.add_argument("--no-parity", action="store_true",
+                    help="skip the parity report (one step of each solver form against the oracle's FP64 "
+                         "projection from the state the timed steps left)")
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--solver", default="both", choices=["both", "plain", "mixed"],
                     help="plain only / mixed only (profiling runs); the default times both")
@@ -189,27 +192,96 @@ def ncu_traffic(kernel_class: str):
     return e.get("dram_bytes_per_launch_full_size"), e.get("note")
 
 
-def cpu_baseline(scene, steps: int, threads: int | None = None):
-    """The reference algorithm on the host cores: the oracle restatement in compat mode
-    (4^3 tiles, the reference's CG stop rule), bit-exact with the reference's code."""
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu), or the machine type."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    import platform
+    return platform.machine()
+
+
+PHASES = ("rebuild", "p2g", "mark", "build_system", "solve", "update_velocity", "update_particles", "compact")
+
+
+def _oracle_timed_step(ora, dt: float, phases: dict) -> float:
+    """One oracle step stage by stage (the same sequence as its step()), phase times added
+    into `phases`; returns the step's wall time."""
+    t_start = time.perf_counter()
+    iters = 0
+    for name in PHASES:
+        t0 = time.perf_counter()
+        if name == "update_particles":
+            ora.update_particles(dt)
+        elif name == "solve":
+            iters = ora.solve()
+        else:
+            getattr(ora, name)()
+        phases[name] = phases.get(name, 0.0) + (time.perf_counter() - t0)
+    phases.setdefault("_iterations", []).append(int(iters))
+    return time.perf_counter() - t_start
+
+
+def _oracle_leg(scene, steps: int, solver: str, threads: int, tol: float = 1e-6, timed_threads: int | None = None):
+    """`steps` timed oracle steps (compat mode: 4^3 tiles, the reference's rules) after one
+    warm-up step from rest on all `threads`; the timed steps run on `timed_threads`."""
     from oracle import bindings as B
     if not os.path.exists(B.ORACLE_SO):
         B.build(ref=False)
-    threads = threads or os.cpu_count()
-    ora = B.Oracle(scene, block=4, compat=True, solver="reference", max_iter=200, threads=threads)
+    ora = B.Oracle(scene, block=4, compat=True, solver=solver, tol=tol,
+                   max_iter=200 if solver == "reference" else 10**6, threads=threads)
     ora.step(scene.dt)  # from rest the first solve is trivial; it serves as warm-up
-    times, nps = [], []
+    if timed_threads:
+        ora.lib.ora_set_threads(int(timed_threads))
+    times, nps, phases = [], [], {}
     for _ in range(steps):
-        n = ora.num_particles
-        t0 = time.perf_counter()
-        ora.step(scene.dt)
-        times.append(time.perf_counter() - t0)
-        nps.append(n)
-    return {"value": sum(nps) / sum(times), "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{steps} steps of the full workload after 1 warm-up step, oracle restatement of the "
-                      f"reference step (4^3 tiles, reference CG rule: |r|<1e-3 or 201 iterations), "
-                      f"{threads} OpenMP threads; {sum(times):.1f} s",
-            "ms_per_step": 1e3 * sum(times) / len(times)}
+        nps.append(ora.num_particles)
+        times.append(_oracle_timed_step(ora, scene.dt, phases))
+    if timed_threads:
+        ora.lib.ora_set_threads(int(threads))
+    iters = phases.pop("_iterations")
+    tot = sum(times)
+    return {"value": sum(nps) / tot, "ms_per_step": 1e3 * tot / len(times), "seconds": tot, "iterations": iters,
+            "phase_ms_per_step": {k: round(1e3 * v / len(times), 1) for k, v in phases.items()}}
+
+
+def cpu_baseline(scene, steps: int, threads: int | None = None, one_thread: bool = True):
+    """The reference algorithm on the host cores: the oracle restatement in compat mode
+    (4^3 tiles), bit-exact with the reference's code under its own CG rule.
+
+    Variants: `o_ref` the reference's stop rule (|r| < 1e-3 absolute or 201 iterations,
+    FP32 dots; at 256^3 it stops on the cap, unconverged); `o_tol` the same FP32 CG
+    recurrence with FP64 dots run to ||r||/||b|| < 1e-6 with no cap - the like-for-like
+    baseline of the device's converged solve; `o_ref_1_thread` one step of o_ref on one
+    thread. The headline value is o_ref (the reference as shipped)."""
+    threads = threads or os.cpu_count()
+    model = cpu_model()
+    ref = _oracle_leg(scene, steps, "reference", threads)
+    tol = _oracle_leg(scene, steps, "tol", threads, tol=1e-6)
+    out = {"value": ref["value"], "unit": UNIT, "cores": threads, "kind": "port", "cpu_model": model,
+           "sample": f"{steps} steps of the full workload after 1 warm-up step, oracle restatement of the "
+                     f"reference step (4^3 tiles, reference CG rule: |r|<1e-3 or 201 iterations), "
+                     f"{threads} OpenMP threads on {model}; {ref['seconds']:.1f} s",
+           "ms_per_step": ref["ms_per_step"], "phase_ms_per_step": ref["phase_ms_per_step"],
+           "cg_iterations_per_step": ref["iterations"],
+           "variants": {"o_tol": {"value": tol["value"], "unit": UNIT, "cores": threads, "kind": "port",
+                                  "ms_per_step": tol["ms_per_step"], "phase_ms_per_step": tol["phase_ms_per_step"],
+                                  "cg_iterations_per_step": tol["iterations"],
+                                  "sample": f"{steps} steps after 1 warm-up step; the reference's FP32 CG "
+                                            f"recurrence with FP64 dots to ||r||/||b|| < 1e-6, no iteration cap "
+                                            f"(the device's convergence level); {tol['seconds']:.1f} s"}}}
+    if one_thread:
+        one = _oracle_leg(scene, 1, "reference", threads, timed_threads=1)
+        out["variants"]["o_ref_1_thread"] = {
+            "value": one["value"], "unit": UNIT, "cores": 1, "kind": "port", "ms_per_step": one["ms_per_step"],
+            "phase_ms_per_step": one["phase_ms_per_step"],
+            "sample": f"1 step after 1 warm-up step (warm-up on {threads} threads), reference CG rule, one thread; "
+                      f"{one['seconds']:.1f} s"}
+    return out
 
 
 def post_cpu_baseline(flip, reps: int = 2) -> dict:
@@ -292,6 +364,8 @@ def barrier(world: int):
 
 
 def run_reference(args, world, rank):
+    """The reference's algorithm on the host cores: every one of the --warmup and --steps
+    steps of the workload runs (the first warm-up step starts from rest), all host threads."""
     if rank != 0:
         return
     sc = make_scene(args.workload)
@@ -299,23 +373,20 @@ def run_reference(args, world, rank):
     if not os.path.exists(B.ORACLE_SO):
         B.build(ref=False)
     threads = os.cpu_count()
+    model = cpu_model()
     ora = B.Oracle(sc, block=4, compat=True, solver="reference", max_iter=200, threads=threads)
-    warm = max(1, min(args.warmup, 2))
-    steps = max(1, min(args.steps, 5))
-    for _ in range(warm):
+    for _ in range(args.warmup):
         ora.step(sc.dt)
-    times, nps = [], []
-    for _ in range(steps):
-        n = ora.num_particles
-        t0 = time.perf_counter()
-        ora.step(sc.dt)
-        times.append(time.perf_counter() - t0)
-        nps.append(n)
+    times, nps, phases = [], [], {}
+    for _ in range(args.steps):
+        nps.append(ora.num_particles)
+        times.append(_oracle_timed_step(ora, sc.dt, phases))
+    iters = phases.pop("_iterations")
     value = sum(nps) / sum(times)
     ms = sorted(1e3 * t for t in times)
-    sample = (f"{steps} timed steps (of --steps {args.steps}) after {warm} warm-up steps of the full workload; "
+    sample = (f"{args.steps} timed steps after {args.warmup} warm-up steps of the full workload; "
               f"oracle restatement of the reference FLIP step, bit-exact with the reference's host build "
-              f"(4^3 tiles, reference CG rule), {threads} OpenMP threads")
+              f"(4^3 tiles, reference CG rule), {threads} OpenMP threads on {model}")
     metric = METRIC if args.solver != "mixed" else METRIC.replace("plain FP32 block-MIC(0)-PCG", "mixed-precision MG-PCG")
     if args.workload != "dam_sphere_256":
         metric = metric.replace("at 256^3 FLIP", f"at {sc.res[0]}x{sc.res[1]}x{sc.res[2]} FLIP")
@@ -324,7 +395,9 @@ def run_reference(args, world, rank):
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
            "data": "synthetic (seeded jittered-uniform dam break + sphere)", "impl": "reference",
            "config": workload_config(sc, {"solver": "reference CG (absolute 1e-3, 201 iterations), FP32"}),
-           "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample,
+                            "cpu_model": model, "cg_iterations_per_step": iters,
+                            "phase_ms_per_step": {k: round(1e3 * v / len(times), 1) for k, v in phases.items()}},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
 
@@ -409,6 +482,30 @@ def timed_steps(sim, sc, args, world, flip, local, sample_clocks, alg=ALG_BYTES)
             "launches": int(launches),
             "solver": {"iterations_per_step": iters, "all_converged": all_conv, **worst,
                        "active_tiles": fi["ntiles"]}}
+
+
+def parity_report(flip, sc, sim, forms: dict) -> dict:
+    """One step from the simulation's current particles on the device (each solver form,
+    the library's default settings - the ones timed) and on the oracle (all host threads,
+    8^3 tiles, the reference's rules, FluidProjection's system solved in FP64 to 1e-12):
+    max|device - oracle| / max|oracle| of pressure, projected grid velocity and particle
+    velocity and position."""
+    import numpy as np
+
+    from oracle import parity as OP
+    pos, vel, _, ids = sim.particles()
+    o = np.argsort(ids)
+    state = OP.with_state(sc, pos[o], vel[o])
+    del pos, vel, ids
+    ora = OP.oracle_step(state)
+    out = {}
+    for name, solver in forms.items():
+        e = OP.compare(OP.device_step(flip, state, solver=solver), ora)
+        e["how"] = ("one step from the state after the timed steps; device at the timed settings vs the oracle's "
+                    f"FP64 projection (CG to 1e-12, {ora['seconds']:.0f} s on {os.cpu_count()} host threads); "
+                    "max|device - oracle| / max|oracle|")
+        out[name] = e
+    return out
 
 
 def post_measure(sim, sc, flip, reps: int = 5, nvtx: bool = False) -> dict:
@@ -512,6 +609,17 @@ def run_ours(args, world, rank, local):
                  "solver": mm["solver"], "speedup_over_plain": mm["value"] / value,
                  "config": "same scene; geometric-multigrid-preconditioned CG, V(2,2) damped Jacobi, FP16 level "
                            "storage with FP32 arithmetic, FP64-accurate dots and norms, double-float iterative refinement"}
+
+    # parity at the benchmarked settings (a checker, outside every timed region): one step
+    # of each solver form and of the oracle (FP64 projection) from the state left here
+    if not args.no_parity and args.workload != "tank_1024":
+        forms = {"plain": flip.SOLVER_PLAIN, "mixed": flip.SOLVER_MIXED}
+        if args.solver != "both":
+            forms = {args.solver: forms[args.solver]}
+        rep = parity_report(flip, sc, sim, forms)
+        meas["solver"]["parity"] = rep.get("plain") or rep.get("mixed")
+        if mixed is not None:
+            mixed["solver"]["parity"] = rep["mixed"]
 
     post = None if args.no_post else post_measure(sim, sc, flip, args.post_reps, args.nvtx)
 

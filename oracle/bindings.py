@@ -31,16 +31,28 @@ def _ptr(a: np.ndarray | None):
     return None if a is None else a.ctypes.data_as(_vp)
 
 
+def reference_dir() -> str | None:
+    """The reference checkout named by BORA_REFERENCE (the directory holding base/source),
+    or None when the variable is unset."""
+    d = os.environ.get("BORA_REFERENCE")
+    return d or None
+
+
 def build(ref: bool | None = None, quiet: bool = True) -> None:
-    """Compile the restatement (and the reference build when its sources exist)."""
+    """Compile the restatement, and the host build of the reference when BORA_REFERENCE
+    names a checkout (ref=None: when it is set and holds base/source; ref=True: required,
+    an error otherwise)."""
     targets = ["all"]
-    refdir = os.environ.get("BORA_REFERENCE", "/root/reference")
+    refdir = reference_dir()
+    has_ref = refdir is not None and os.path.isdir(os.path.join(refdir, "base", "source"))
     if ref is None:
-        ref = os.path.isdir(os.path.join(refdir, "base", "source"))
+        ref = has_ref
+    elif ref and not has_ref:
+        raise RuntimeError("building the reference needs BORA_REFERENCE set to a checkout holding base/source")
+    args = ["make", "-C", HERE, "-j8", *targets]
     if ref:
-        targets.append("ref")
-    subprocess.run(["make", "-C", HERE, "-j8", f"REF={refdir}", *targets], check=True,
-                   stdout=subprocess.DEVNULL if quiet else None)
+        args += [f"REF={refdir}", "ref"]
+    subprocess.run(args, check=True, stdout=subprocess.DEVNULL if quiet else None)
 
 
 class OracleConfig(ctypes.Structure):
@@ -208,7 +220,7 @@ class Oracle(_SimBase):
         c.bmax = (ctypes.c_float * 3)(*scene.bmax)
         c.block = block
         c.compat_wrap = 1 if compat else 0
-        c.solver = {"reference": 0, "fp64": 1}[solver]
+        c.solver = {"reference": 0, "fp64": 1, "tol": 2}[solver]
         c.tol = tol
         c.max_iter = max_iter
         c.gravity = (ctypes.c_float * 3)(*scene.gravity)

@@ -51,8 +51,9 @@ typedef struct OracleConfig
     float bmin[3], bmax[3];
     int block;             // tile edge in cells: 4 (reference) or 8 (build)
     int compat_wrap;       // 1: reproduce the reference's unclamped tile-neighbour loop
-    int solver;            // 0: reference CG rule (LinearSystemSolver.cpp:12-50), 1: FP64 CG to tol
-    double tol;            // relative tolerance of solver 1
+    int solver;            // 0: reference CG rule (LinearSystemSolver.cpp:12-50), 1: FP64 CG to tol,
+                           // 2: the reference's FP32 recurrence with FP64 dots to a relative tol
+    double tol;            // relative tolerance of solvers 1 and 2
     int max_iter;          // projIteration (solver 0) / iteration cap (solver 1)
     float gravity[3];      // world units (FLIPMethod::Params::extForce)
     float wall_level;      // world units (FLIPMethod::Params::wallLevel)
@@ -556,16 +557,62 @@ struct Oracle
         {
             spmvF( p, Ap, nullptr, false );
             const float alpha = rsold / dotF( p, Ap );
-            for( size_t q = 0; q < N; ++q ) x[q] = x[q] + ( alpha * p[q] );
-            for( size_t q = 0; q < N; ++q ) r[q] = r[q] - ( alpha * Ap[q] );
-            const float rsnew = dotF( r, r );
+            axpyF( x, alpha, p, x );   // BLAS::axpy (BLAS.cu:142-150) as a parallel loop, like
+            axpyF( r, -alpha, Ap, r ); // the reference's LaunchCudaDevice; element-wise, so the
+            const float rsnew = dotF( r, r );  // result does not depend on the thread count
             if( std::sqrt( rsnew ) < 1e-3f ) break;
             const float beta = rsnew / rsold;
-            for( size_t q = 0; q < N; ++q ) p[q] = r[q] + ( beta * p[q] );
+            axpyF( r, beta, p, p );
             rsold = rsnew;
             if( count > max ) break;
         }
         return count;
+    }
+    // out = a + s * c element-wise in float (r - alpha*Ap is written a + (-alpha)*c: IEEE
+    // negation is exact, so it rounds like a - alpha*c)
+    static void axpyF( const std::vector<float>& a, float s_, const std::vector<float>& c, std::vector<float>& out )
+    {
+        const long long n = (long long)a.size();
+#pragma omp parallel for schedule(static)
+        for( long long i = 0; i < n; ++i ) out[(size_t)i] = a[(size_t)i] + ( s_ * c[(size_t)i] );
+    }
+    static double dotFD( const std::vector<float>& a, const std::vector<float>& c )
+    {
+        double s_ = 0.0;
+        const long long n = (long long)a.size();
+#pragma omp parallel for reduction(+ : s_) schedule(static)
+        for( long long i = 0; i < n; ++i ) s_ += (double)a[(size_t)i] * (double)c[(size_t)i];
+        return s_;
+    }
+    // The like-for-like CPU baseline of a converged solve: LinearSystemSolver::cg's FP32
+    // recurrence (LinearSystemSolver.cpp:12-50) with its dots in FP64 and its stop rule
+    // replaced by ||r||/||b|| < tol on the recursive residual, no 201-iteration cap.
+    int solveTol( double tol, int maxit )
+    {
+        const size_t N = b.size();
+        std::vector<float> r( N ), p( N ), Ap( N );
+        spmvF( x, r, &b, true );
+        p = r;
+        const double bn = std::sqrt( dotFD( b, b ) );
+        double rsold = dotFD( r, r );
+        int it = 0;
+        if( bn > 0.0 )
+        {
+            while( std::sqrt( rsold ) > tol * bn && it < maxit )
+            {
+                spmvF( p, Ap, nullptr, false );
+                const float alpha = (float)( rsold / dotFD( p, Ap ) );
+                axpyF( x, alpha, p, x );
+                axpyF( r, -alpha, Ap, r );
+                const double rsnew = dotFD( r, r );
+                const float beta = (float)( rsnew / rsold );
+                axpyF( r, beta, p, p );
+                rsold = rsnew;
+                ++it;
+            }
+        }
+        lastRel = bn > 0.0 ? std::sqrt( rsold ) / bn : 0.0;
+        return it;
     }
     void spmvD( const std::vector<double>& p, std::vector<double>& out ) const
     {
@@ -608,10 +655,13 @@ struct Oracle
             {
                 spmvD( P, Q );
                 const double alpha = rs / dotD( P, Q );
-                for( size_t i = 0; i < N; ++i ) { X[i] += alpha * P[i]; R[i] -= alpha * Q[i]; }
+                const long long n = (long long)N;
+#pragma omp parallel for schedule(static)
+                for( long long i = 0; i < n; ++i ) { X[(size_t)i] += alpha * P[(size_t)i]; R[(size_t)i] -= alpha * Q[(size_t)i]; }
                 const double rn = dotD( R, R );
                 const double beta = rn / rs;
-                for( size_t i = 0; i < N; ++i ) P[i] = R[i] + beta * P[i];
+#pragma omp parallel for schedule(static)
+                for( long long i = 0; i < n; ++i ) P[(size_t)i] = R[(size_t)i] + beta * P[(size_t)i];
                 rs = rn;
                 ++it;
             }
@@ -623,6 +673,7 @@ struct Oracle
     int solve()
     {
         if( cfg.solver == 0 ) lastIters = solveRef( cfg.max_iter );
+        else if( cfg.solver == 2 ) lastIters = solveTol( cfg.tol, cfg.max_iter );
         else lastIters = solve64( cfg.tol, cfg.max_iter );
         return lastIters;
     }

@@ -111,6 +111,10 @@ struct BoraTilesDev
 
 // Scalars that the solver kernels exchange on the device (ring of FP64 reductions).
 #define BORA_RING 64
+// Largest grid of a kernel that reduces through BoraReduceDev::partials (one slot pair per
+// block). Every such launcher clamps its grid to this, and the handle sizes the partials
+// buffer for at least this many blocks.
+constexpr int kBoraMaxReduceBlocks = 152 * 16;
 struct BoraReduceDev
 {
     double* ring;        // [BORA_RING * 4]: slot values

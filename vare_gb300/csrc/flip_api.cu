@@ -395,7 +395,7 @@ int ensure_cells( bora_flip_sim* s, int ntiles )
     BORA_TRY( grow( s->cell_start, ( nc + 2 ) * 4, false, s->st ) );
     BORA_TRY( grow( s->tile_of, cap * 4, false, s->st ) );
     BORA_TRY( grow( s->nbr, cap * 27 * 4, false, s->st ) );
-    BORA_TRY( grow( s->partials, ( std::max<size_t>( cap, 152 * 16 ) + 16 ) * 2 * 8, false, s->st ) );
+    BORA_TRY( grow( s->partials, ( std::max<size_t>( cap, kBoraMaxReduceBlocks ) + 16 ) * 2 * 8, false, s->st ) );
     BORA_TRYS( ensure_scan_scratch( s, std::max( nc + 2, s->ntv ) ) );
     s->cap_tiles = cap;
     return BORA_OK;
@@ -1094,15 +1094,16 @@ int bora_flip_set_collider_field( bora_flip_handle s, const float* phi, const fl
     }
     const size_t n = (size_t)s->g.nx * s->g.ny * s->g.nz;
     if( ncells != n ) return BORA_ERR_INVALID_ARG;
+    // all allocations first; then the copies. A failure after the first copy leaves no
+    // collider at all rather than a mix of the old and the new one.
     BORA_TRY( grow( s->col_phi, n * 4, false, s->st ) );
-    BORA_TRY( cudaMemcpyAsync( s->col_phi.p, phi, n * 4, cudaMemcpyHostToDevice, s->st ) );
-    if( vel )
-    {
-        BORA_TRY( grow( s->col_vel, n * 12, false, s->st ) );
-        BORA_TRY( cudaMemcpyAsync( s->col_vel.p, vel, n * 12, cudaMemcpyHostToDevice, s->st ) );
-    }
-    BORA_TRY( cudaStreamSynchronize( s->st ) );  // the caller may free its buffers on return
+    if( vel ) BORA_TRY( grow( s->col_vel, n * 12, false, s->st ) );
+    c.fphi = nullptr;
+    c.fvel = nullptr;
     c.count = 0;  // replaces any boxes
+    BORA_TRY( cudaMemcpyAsync( s->col_phi.p, phi, n * 4, cudaMemcpyHostToDevice, s->st ) );
+    if( vel ) BORA_TRY( cudaMemcpyAsync( s->col_vel.p, vel, n * 12, cudaMemcpyHostToDevice, s->st ) );
+    BORA_TRY( cudaStreamSynchronize( s->st ) );  // the caller may free its buffers on return
     c.fphi = P<float>( s->col_phi );
     c.fvel = vel ? P<float>( s->col_vel ) : nullptr;
     return BORA_OK;

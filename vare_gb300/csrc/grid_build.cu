@@ -19,7 +19,7 @@ constexpr int kThreads = 256;
 inline int grid_for( size_t n, int threads = kThreads )
 {
     const size_t b = ( n + threads - 1 ) / threads;
-    return (int)( b < 152 * 16 ? ( b > 0 ? b : 1 ) : 152 * 16 );
+    return (int)( b < 152 * 16 ? ( b > 0 ? b : 1 ) : 152 * 16 );  // grid-stride loops: 16 blocks per SM
 }
 
 // Grid::inside (base/header/Grid.h:408-417)

@@ -1212,7 +1212,7 @@ void launch_up_fused( const BoraLevelDev& F, const __half* ec, BoraTilesDev t, i
     static BoraPerDevice per_sm;
     constexpr int NT = TileRegion<E>::NT;
     int grid = fused_grid( k_mg_up_fused<E, L0>, NT, ntiles, per_sm );
-    if( L0 ) grid = std::min( grid, 152 * 16 );  // partial sums capacity of the reduction
+    if( L0 ) grid = std::min( grid, kBoraMaxReduceBlocks );  // partial sums capacity of the reduction
     bora_launch_pdl( k_mg_up_fused<E, L0>, grid, NT, 0, st, F, ec, t, ntiles, r0, slot_rr, red, zout, slot_rz );
 }
 

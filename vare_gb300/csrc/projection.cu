@@ -823,7 +823,7 @@ void bora_launch_pcg_update( int ntiles, const uint16_t* code, BoraSolverDev s, 
     } );
     // as many rounds of one tile per warp as the resident warps need, and the grid sized so
     // that every warp gets that many tiles (no warp waits in the reduction for a straggler)
-    const int cap = std::max( 1, std::min( bps * num_sms(), 152 * 16 ) ) * kUpdWarps;
+    const int cap = std::max( 1, std::min( bps * num_sms(), kBoraMaxReduceBlocks ) ) * kUpdWarps;
     const int rounds = std::max( 1, ( ntiles + cap - 1 ) / cap );  // one block even for no tiles: it publishes the sums
     const int nb = std::max( 1, ( ntiles + kUpdWarps * rounds - 1 ) / ( kUpdWarps * rounds ) );
     bora_launch_pdl( k_pcg_update, nb, 32 * kUpdWarps, 0, st, ntiles, s, red, slot_rz_in, slot_dq_in, slot_rz_out,
@@ -841,7 +841,7 @@ void bora_launch_pcg_direction( const BoraGridDev&, int ntiles, BoraTilesDev t, 
         return cudaOccupancyMaxActiveBlocksPerMultiprocessor( &v, k_pcg_direction, 32 * kDirWarps, 0 ) == cudaSuccess && v > 0 ? v : 1;
     } );
     // every warp gets the same number of tiles; at most 152 x 16 CTAs (partial sums capacity)
-    const int cap = std::max( 1, std::min( b * num_sms(), 152 * 16 ) ) * kDirWarps;
+    const int cap = std::max( 1, std::min( b * num_sms(), kBoraMaxReduceBlocks ) ) * kDirWarps;
     const int rounds = ( ntiles + cap - 1 ) / cap;
     const int grid = std::max( 1, ( ntiles + kDirWarps * rounds - 1 ) / ( kDirWarps * rounds ) );
     bora_launch_pdl( k_pcg_direction, grid, 32 * kDirWarps, 0, st, ntiles, (const int32_t*)t.nbr, code, s, dsel_in, red,
