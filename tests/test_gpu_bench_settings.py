@@ -9,11 +9,13 @@ oracle's step, whose projection is solved by CG in FP64 to 1e-12 (FluidProjectio
 276-381, FLIPMethod.cu:208-298). The errors are max|device - oracle| / max|oracle| for
 the pressure field, the projected grid velocity and the particle velocities.
 
-Bounds. A relative residual of 1e-6 leaves a relative pressure error of at most
-cond(A) * 1e-6; for these Poisson systems the error that remains is carried by the
-smoothest modes, which the residual weighs by their small eigenvalues. The measured
-errors sit below the bounds written in each test (the measured values are in the test
-output, `-s`).
+Bound: 1e-5 relative for pressure, grid velocity and particle velocity (1e-6 for
+positions, which move by v*dt). A relative residual of 1e-6 bounds the relative pressure
+error only by cond(A) * 1e-6, but both solver forms iterate until max|b - A p|*dx < 1e-5
+as well, and on GB300 the errors measured against the FP64 projection are far inside
+the bound: at most 3e-7 (pressure), 1.5e-6 (grid velocity), 1.0e-6 (particle velocity)
+and 1.2e-7 (position) over the scenes below, 256^3 included (values in the test output,
+`-s`; the benchmark line repeats the 256^3 figures for each form).
 """
 import os
 
@@ -26,7 +28,7 @@ from vare_gb300 import scenes
 pytestmark = pytest.mark.gpu
 
 # bounds of max|device - oracle| / max|oracle| at the benchmarked stop rule
-BOUND = {"pressure": 1e-4, "grid_velocity": 1e-5, "particle_velocity": 1e-5, "particle_position": 1e-6}
+BOUND = {"pressure": 1e-5, "grid_velocity": 1e-5, "particle_velocity": 1e-5, "particle_position": 1e-6}
 
 
 def _moving(sc, oracle_lib, steps=2):

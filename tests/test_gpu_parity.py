@@ -331,8 +331,22 @@ def test_full_size_invariants(gpu, solver):
     assert int(sim.field(gpu.FIELD_SURF).astype(np.int64).sum()) == int(touched.sum())
 
 
-def test_cpp_harness_runs(gpu):
-    """Houdini-free FLIPMethod harness linked against the C ABI library."""
+def _read_store(f, with_origin):
+    n = int(np.fromfile(f, np.int64, 1)[0])
+    pos = np.fromfile(f, np.float32, 3 * n).reshape(n, 3)
+    vel = np.fromfile(f, np.float32, 3 * n).reshape(n, 3)
+    origin = np.fromfile(f, np.int32, n) if with_origin else None
+    return pos, vel, origin
+
+
+def test_cpp_harness_matches_oracle(gpu, oracle_lib, tmp_path):
+    """The header-only FLIPMethod wrapper (include/BoraFLIPMethod.hpp) driven the way the
+    Houdini node drives Bora::FLIPMethod - world-space particles, newParticle per point,
+    advanceOneFrame (step + postProcess) three times, the library's default solver
+    settings - against the oracle running the same frames: each frame's world -> voxel
+    upload and voxel -> world read-back (Grid::voxelPoint / worldPoint, FLIPMethod.cu:
+    481-513) restated in float32, one step with an FP64 projection in between; particles
+    matched by their index in the initial store."""
     from vare_gb300 import build
     src = os.path.join(ROOT, "tests", "cpp", "flipmethod_harness.cpp")
     exe = os.path.join(ROOT, "tests", "cpp", "_build", "harness")
@@ -340,8 +354,33 @@ def test_cpp_harness_runs(gpu):
     libdir = os.path.dirname(build.LIB)
     subprocess.run(["g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"), src, "-o", exe,
                     "-L", libdir, "-lbora_flip", f"-Wl,-rpath,{libdir}"], check=True)
-    r = subprocess.run([exe, "3"], capture_output=True, text=True, timeout=300)
+    out = str(tmp_path / "harness.bin")
+    frames = 3
+    r = subprocess.run([exe, str(frames), out], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
+    with open(out, "rb") as f:
+        pos0, vel0, _ = _read_store(f, False)
+        pos1, vel1, origin = _read_store(f, True)
+    f32 = np.float32
+    dt = f32(1.0) / f32(24.0) / f32(4.0)  # the harness's params.dt
+    sc = scenes.Scene(name="harness", res=(32, 32, 32), bmin=(0.0, 0.0, 0.0), bmax=(1.0, 1.0, 1.0), dt=float(dt),
+                      pos=np.zeros((0, 3), f32), vel=np.zeros((0, 3), f32), wall_level=2.0,
+                      gravity=(0.0, -9.80665, 0.0))
+    ora = oracle_lib.Oracle(sc, block=8, solver="fp64", tol=1e-12, threads=os.cpu_count())
+    xf = ora.grid_xform()
+    tr, scl = xf["translate"].astype(f32), xf["scale"].astype(f32)
+    wp, wv, ids = pos0, vel0, np.arange(len(pos0), dtype=np.int32)
+    for _ in range(frames):
+        ora.set_particles((wp - tr) / scl, wv / scl, ids)
+        ora.step(dt)
+        p, v, _, ids = ora.particles()
+        wp, wv = p * scl + tr, v * scl
+    o = np.argsort(ids)
+    g = np.argsort(origin)
+    np.testing.assert_array_equal(origin[g], ids[o])
+    ep, ev = rel_err(pos1[g], wp[o]), rel_err(vel1[g], wv[o])
+    print(f"\nC++ wrapper vs oracle after {frames} frames: position {ep:.3e}, velocity {ev:.3e}")
+    assert ep <= TOL and ev <= 1e-4
 
 
 def test_rk2_advection_matches_oracle(gpu, oracle_lib, scene):
