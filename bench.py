@@ -562,7 +562,8 @@ def run_ours(args, world, rank, local):
     if args.solver == "mixed":
         args.no_mixed = True
     sim = flip.FlipSim.from_scene(sc, solver=flip.SOLVER_MIXED if args.solver == "mixed" else flip.SOLVER_PLAIN)
-    meas = timed_steps(sim, sc, args, world, flip, local, True)
+    meas = timed_steps(sim, sc, args, world, flip, local, True,
+                       ALG_BYTES_MIXED if args.solver == "mixed" else ALG_BYTES)
     if args.solver == "plain":
         args.no_mixed = True
     value, roof, clk, launches = meas["value"], meas["roofline"], meas["clocks"], meas["launches"]

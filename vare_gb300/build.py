@@ -4,9 +4,12 @@ Each translation unit is compiled by nvcc for sm_103a in parallel, then linked i
 shared library with a plain C ABI (include/bora_flip.h). No torch types cross the
 boundary, so the library loads into any host process (ctypes, a C++ plugin, ...).
 
-Floating-point contraction is disabled (-fmad=false) so that kernels restating the
-reference's float arithmetic round exactly like it; kernels that want fused
-multiply-adds (the pressure solver) call fmaf explicitly.
+Floating-point contraction is disabled (-fmad=false) in the translation units whose
+kernels restate the reference's float arithmetic, so that they round exactly like it;
+their solver kernels call fmaf explicitly where they want fused multiply-adds. The
+multigrid preconditioner restates nothing of the reference and is compiled with
+contraction on (CONTRACT below); its double-float helpers multiply with __fmul_rn, which
+is never contracted.
 """
 from __future__ import annotations
 
@@ -21,11 +24,12 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libbora_flip.so")
 
-SOURCES = ["scan.cu", "grid_build.cu", "p2g.cu", "projection.cu", "multigrid.cu", "g2p.cu", "surface.cu", "flip_api.cu",
-           "serve.cu"]
+SOURCES = ["scan.cu", "grid_build.cu", "p2g.cu", "projection.cu", "multigrid.cu", "mg_mid.cu", "g2p.cu", "surface.cu",
+           "flip_api.cu", "serve.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC",
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
               "--expt-relaxed-constexpr", "-Xcudafe", "--diag_suppress=177"]
+CONTRACT = {"multigrid.cu", "mg_mid.cu"}  # translation units compiled with -fmad=true
 
 
 def nvcc() -> str:
@@ -42,7 +46,8 @@ def _compile(src: str, verbose: bool) -> str:
     deps.append(os.path.join(HERE, "..", "include", "bora_flip.h"))
     if os.path.exists(obj) and all(os.path.getmtime(obj) >= os.path.getmtime(d) for d in deps):
         return obj
-    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, "-I", CSRC, "-c", path, "-o", obj]
+    fmad = "-fmad=true" if src in CONTRACT else "-fmad=false"
+    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, fmad, "-I", CSRC, "-c", path, "-o", obj]
     if verbose:
         cmd.insert(1, "-Xptxas=-v")
     r = subprocess.run(cmd, capture_output=True, text=True)

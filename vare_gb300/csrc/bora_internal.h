@@ -215,12 +215,27 @@ struct BoraLevelDev
 };
 
 // Cell types and stencil codes of level c from level c-1 (levels[0] = fine, given).
-void bora_mg_setup( const BoraGridDev& g, BoraLevelDev* levels, int nlevels, BoraTilesDev t, uint32_t* err, cudaStream_t st );
+// mid_image: the buffer for the coarse levels' cluster image (bora_mg_mid_image_bytes), or null
+void bora_mg_setup( const BoraGridDev& g, BoraLevelDev* levels, int nlevels, BoraTilesDev t, void* mid_image,
+                    uint32_t* err, cudaStream_t st );
 // One V-cycle: z = M^-1 r (FP32 in and out, FP16 inside); r.z -> ring slot (FP64-accurate).
 // Kernel launches of one bora_mg_vcycle call for this hierarchy.
-int bora_mg_vcycle_launches( const BoraLevelDev* levels, int nlevels );
-void bora_mg_vcycle( const BoraGridDev& g, const BoraLevelDev* levels, int nlevels, BoraTilesDev t, const float* r,
-                     float* z, BoraReduceDev red, int slot_rr, int slot_rz, int coarse_sweeps, cudaStream_t st );
+int bora_mg_vcycle_launches( const BoraGridDev& g, const BoraLevelDev* levels, int nlevels, BoraTilesDev t,
+                             const void* mid_image );
+// Level 3 .. coarsest of a V-cycle in one thread-block cluster out of distributed shared
+// memory (mg_mid.cu). bora_mg_mid_image_bytes: the device buffer its per-step static image
+// needs, 0 when the hierarchy does not have the shape or size it handles;
+// bora_mg_mid_setup: lay the image out (once per step, after bora_mg_setup's codes);
+// bora_mg_mid_vcycle: 1 when it runs these levels (launching the kernel when `launch`), 0
+// when the caller must run them itself.
+size_t bora_mg_mid_image_bytes( const BoraGridDev& g, const BoraLevelDev* levels, int nlevels, BoraTilesDev t, int ntiles );
+void bora_mg_mid_setup( const BoraGridDev& g, const BoraLevelDev* levels, int nlevels, BoraTilesDev t, int ntiles,
+                        void* image, cudaStream_t st );
+int bora_mg_mid_vcycle( const BoraGridDev& g, const BoraLevelDev* levels, int nlevels, BoraTilesDev t, int ntiles,
+                        const void* image, uint32_t* err, int sweeps, cudaStream_t st, bool launch );
+void bora_mg_vcycle( const BoraGridDev& g, const BoraLevelDev* levels, int nlevels, BoraTilesDev t, const void* mid_image,
+                     const float* r, float* z, BoraReduceDev red, int slot_rr, int slot_rz, int coarse_sweeps,
+                     cudaStream_t st );
 // e += alpha d; r -= alpha q; r.r -> ring slot (alpha = rz / dq, or 0 when slot_rz < 0)
 void bora_launch_pcg_update_noprec( int ntiles, BoraSolverDev s, BoraReduceDev red, int slot_rz, int slot_dq,
                                     int slot_rr_out, cudaStream_t st );

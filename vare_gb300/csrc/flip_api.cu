@@ -142,6 +142,8 @@ struct bora_flip_sim
     // multigrid hierarchy (mixed solver): per level type, code, r, z0, z1
     static constexpr int kMaxLevels = 16;
     DevBuf mg_type[kMaxLevels], mg_code[kMaxLevels], mg_r[kMaxLevels], mg_z0[kMaxLevels], mg_z1[kMaxLevels];
+    DevBuf mg_mid;         // static image of the coarse levels' cluster kernel (mg_mid.cu), or empty
+    bool mg_mid_on = false;
     BoraLevelDev levels[kMaxLevels] = {};
     int nlevels = 0;
 
@@ -517,6 +519,7 @@ int build_hierarchy( bora_flip_sim* s )
         return BORA_OK;
     };
     auto half_up = []( int v ) { return ( v + 1 ) / 2; };
+    s->mg_mid_on = false;
     BORA_TRYS( add( 0, 8, nt * 512, 0, 0, 0 ) );
     for( int E = 4; E >= 1; E /= 2 )
     {
@@ -532,6 +535,13 @@ int build_hierarchy( bora_flip_sim* s )
         if( s->levels[n - 1].ncells <= 512 ) break;
     }
     s->nlevels = n;
+    // the coarse levels run in one cluster kernel when they fit it; its static image
+    const size_t img = bora_mg_mid_image_bytes( g, s->levels, n, s->tiles(), (int)nt );
+    if( img > 0 )
+    {
+        BORA_TRY( grow( s->mg_mid, img, false, s->st ) );
+        s->mg_mid_on = true;
+    }
     return BORA_OK;
 }
 
@@ -544,8 +554,9 @@ int stage_build_system( bora_flip_sim* s )
     if( s->prm.solver == BORA_SOLVER_MIXED )
     {
         BORA_TRYS( build_hierarchy( s ) );
-        s->stats.kernel_launches += 2 * (uint64_t)( s->nlevels - 1 );
-        bora_mg_setup( s->g, s->levels, s->nlevels, s->tiles(), P<uint32_t>( s->counters ) + 5, s->st );
+        s->stats.kernel_launches += 2 * (uint64_t)( s->nlevels - 1 ) + ( s->mg_mid_on ? 1 : 0 );
+        bora_mg_setup( s->g, s->levels, s->nlevels, s->tiles(), s->mg_mid_on ? s->mg_mid.p : nullptr,
+                       P<uint32_t>( s->counters ) + 5, s->st );
     }
     else
     {
@@ -592,11 +603,12 @@ int stage_solve( bora_flip_sim* s )
         // inner FP32 PCG on A e = r
         const double target = norm_ok ? 0.1 * rnorm : std::max( p.inner_tolerance * rnorm, 0.25 * p.tolerance * bnorm );
         const bool mixed = p.solver == BORA_SOLVER_MIXED;
-        const int vlaunch = bora_mg_vcycle_launches( s->levels, s->nlevels );
+        const void* mid_img = s->mg_mid_on ? s->mg_mid.p : nullptr;
+        const int vlaunch = mixed ? bora_mg_vcycle_launches( s->g, s->levels, s->nlevels, s->tiles(), mid_img ) : 0;
         s->stats.mg_vcycle_launches = mixed ? vlaunch : 0;
         auto precondition = [&]( int rr_slot, int rz_slot ) {
             KTimer t( s, BORA_KERNEL_MG, vlaunch );
-            bora_mg_vcycle( s->g, s->levels, s->nlevels, s->tiles(), sv.r, sv.z, red, rr_slot, rz_slot, 16, st );
+            bora_mg_vcycle( s->g, s->levels, s->nlevels, s->tiles(), mid_img, sv.r, sv.z, red, rr_slot, rz_slot, 16, st );
         };
         int rz_cur = s->slot(), rr_cur = s->slot();
         if( mixed )
@@ -870,6 +882,7 @@ void for_each_buffer( bora_flip_sim* s, F&& f )
         f( s->mg_type[l] ); f( s->mg_code[l] ); f( s->mg_r[l] );
         f( s->mg_z0[l] ); f( s->mg_z1[l] );
     }
+    f( s->mg_mid );
 }
 
 extern "C" {

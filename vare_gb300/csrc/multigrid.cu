@@ -1223,7 +1223,8 @@ LevelNav nav_of( const BoraGridDev& g, const BoraLevelDev& L, BoraTilesDev t )
 
 }  // namespace
 
-void bora_mg_setup( const BoraGridDev& g, BoraLevelDev* levels, int nlevels, BoraTilesDev t, uint32_t* err, cudaStream_t st )
+void bora_mg_setup( const BoraGridDev& g, BoraLevelDev* levels, int nlevels, BoraTilesDev t, void* mid_image,
+                    uint32_t* err, cudaStream_t st )
 {
     (void)err;
     for( int l = 1; l < nlevels; ++l )
@@ -1233,6 +1234,8 @@ void bora_mg_setup( const BoraGridDev& g, BoraLevelDev* levels, int nlevels, Bor
         k_mg_types<<<blocks_for( C.ncells ), 256, 0, st>>>( F, C, t.slot_of, t.tile_of, g.tx, g.ty, g.tz );
         k_mg_codes<<<blocks_for( C.ncells ), 256, 0, st>>>( nav_of( g, C, t ), g.voxel_wall );
     }
+    const int ntiles = levels[0].kind == 0 ? (int)( levels[0].ncells / 512 ) : 0;
+    bora_mg_mid_setup( g, levels, nlevels, t, ntiles, mid_image, st );
 }
 
 namespace {
@@ -1304,25 +1307,33 @@ int tail_cluster_size()
 
 }  // namespace
 
-int bora_mg_vcycle_launches( const BoraLevelDev* levels, int nlevels )
+int bora_mg_vcycle_launches( const BoraGridDev& g, const BoraLevelDev* levels, int nlevels, BoraTilesDev t,
+                             const void* mid_image )
 {
     if( nlevels < 2 ) return 0;
-    const int first = tail_start( levels, nlevels );
+    const int ntiles = levels[0].kind == 0 ? (int)( levels[0].ncells / 512 ) : 0;
+    const int first = bora_mg_mid_vcycle( g, levels, nlevels, t, ntiles, mid_image, nullptr, 16, nullptr, false )
+                          ? 3
+                          : tail_start( levels, nlevels );
     const int stop = std::min( first, nlevels - 1 );
     int n = 1;  // the tail kernel, or the coarsest-level kernel
     for( int l = 0; l < stop; ++l ) n += fused_level( levels[l] ) ? 2 : 4;
     return n;
 }
 
-void bora_mg_vcycle( const BoraGridDev& g, const BoraLevelDev* levels, int nlevels, BoraTilesDev t, const float* r,
-                     float* z, BoraReduceDev red, int slot_rr, int slot_rz, int coarse_sweeps, cudaStream_t st )
+void bora_mg_vcycle( const BoraGridDev& g, const BoraLevelDev* levels, int nlevels, BoraTilesDev t, const void* mid_image,
+                     const float* r, float* z, BoraReduceDev red, int slot_rr, int slot_rz, int coarse_sweeps,
+                     cudaStream_t st )
 {
     if( nlevels < 2 ) return;  // the caller always builds at least two levels
     if( levels[0].ncells == 0 ) return;
     const int last = nlevels - 1;
-    const int first = tail_start( levels, nlevels );  // levels [first, last] run in one CTA
-    const int stop = std::min( first, last );          // levels [0, stop) restrict/prolong here
     const int ntiles = levels[0].kind == 0 ? (int)( levels[0].ncells / 512 ) : 0;
+    // level 3 .. coarsest in one cluster out of distributed shared memory (mg_mid.cu) when
+    // the hierarchy fits it; otherwise the tail levels run from global memory (k_mg_tail)
+    const bool mid = bora_mg_mid_vcycle( g, levels, nlevels, t, ntiles, mid_image, red.err, coarse_sweeps, st, false ) != 0;
+    const int first = mid ? 3 : tail_start( levels, nlevels );  // levels [first, last] run in one kernel
+    const int stop = std::min( first, last );                     // levels [0, stop) restrict/prolong here
     // down: pre-smooth and restrict
     for( int l = 0; l < stop; ++l )
     {
@@ -1351,7 +1362,11 @@ void bora_mg_vcycle( const BoraGridDev& g, const BoraLevelDev* levels, int nleve
                 k_mg_restrict<N, 0, 1><<<nb, 256, 0, st>>>( nav, F, C, r0, slot_rr, red.ring, t.slot_of, g.tx, g.ty, g.tz, red.err );
         } );
     }
-    if( first <= last )
+    if( mid )
+    {
+        bora_mg_mid_vcycle( g, levels, nlevels, t, ntiles, mid_image, red.err, coarse_sweeps, st, true );
+    }
+    else if( first <= last )
     {
         TailDesc d{};
         d.n = last - first + 1;

@@ -10,14 +10,16 @@ namespace bora_reduce {
 // dot-product terms are accumulated as unevaluated float pairs (hi + lo) with the
 // error-free TwoProd (fmaf) and TwoSum transformations (Dekker 1971, Knuth TAOCP 4.2.2),
 // giving ~48 significant bits from FP32 instructions; each warp converts its pair to
-// FP64 once. This relies on -fmad=false (no contraction inside TwoSum).
+// FP64 once. The product is formed with __fmul_rn, which the compiler never fuses into a
+// following addition, so the transformations stay error-free under -fmad=true as well
+// (TwoSum has no multiplication to contract).
 struct DF
 {
     float hi, lo;
 };
 __device__ __forceinline__ DF df_prod( float a, float b )
 {
-    const float p = a * b;
+    const float p = __fmul_rn( a, b );
     return DF{ p, fmaf( a, b, -p ) };
 }
 __device__ __forceinline__ DF df_add( DF a, DF b )
