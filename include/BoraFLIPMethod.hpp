@@ -11,7 +11,8 @@
 //   postProcess( Particles& )                  postProcess( Particles& )       (voxel space)
 //   advanceOneStep( Particles&, dt )           advanceOneStep( Particles&, dt )   (voxel space)
 //   particlesToVoxel / particlesToWorld        particlesToVoxel / particlesToWorld
-//   updateCollisionSource( vdb, vdb )          setColliders( boxes )  (analytic boxes; no OpenVDB)
+//   updateCollisionSource( vdb, vdb )          updateCollisionSource( voxels, phi, vel, background )
+//                                              (the grids' active voxels) or setColliders( boxes )
 //   getGrid()                                  getGrid() -> bora_frame_info
 //
 // Differences a caller sees: particles live in a host store (BoraGB300::Particles) that
@@ -161,6 +162,23 @@ class FLIPMethod
     {
         requireInit();
         check( bora_flip_set_colliders( _h, boxes.data(), (int)( boxes.size() / 9 ), band ), "bora_flip_set_colliders" );
+    }
+
+    // FLIPMethod::updateCollisionSource (FLIPMethod.h:111-114 -> CollisionSource::update):
+    // the collider level set's active voxels (frame cells, 3 ints each), their signed
+    // distances (world units) and velocities (world units per second, may be empty), and
+    // the level set's background (world units) - what OpenVDB's active-value iterator
+    // yields after sampling the grids at the frame's cell centres.
+    void updateCollisionSource( const std::vector<int32_t>& ijk, const std::vector<float>& phi,
+                                const std::vector<float>& vel, float background )
+    {
+        requireInit();
+        const size_t n = phi.size();
+        if( ijk.size() != 3 * n || ( !vel.empty() && vel.size() != 3 * n ) )
+            throw Error( BORA_ERR_INVALID_ARG, "updateCollisionSource" );
+        check( bora_flip_set_collider_voxels( _h, ijk.data(), phi.data(), vel.empty() ? nullptr : vel.data(), n,
+                                              background ),
+               "bora_flip_set_collider_voxels" );
     }
 
     // FLIPMethod::advanceOneFrame (FLIPMethod.cu:177-206): world-space particles in, one

@@ -175,6 +175,19 @@ int bora_flip_set_colliders( bora_flip_handle h, const float* boxes, int n, floa
  * nx, ny, nz; x fastest), ncells = nx*ny*nz. Normals are central differences of the
  * distances, as for boxes. Replaces any boxes; phi = NULL removes the collider. */
 int bora_flip_set_collider_field( bora_flip_handle h, const float* phi, const float* vel, size_t ncells );
+/* CollisionSource::update (CollisionSource.h:66-126) from a level set's active voxels, the
+ * form OpenVDB's active-value iterator yields: count voxels at frame cells ijk (3 int32
+ * each; cells outside the frame grid are ignored) with the signed distance phi (world
+ * units, negative inside) and velocity vel (3 floats, world units per second; NULL = at
+ * rest) sampled at those cells' centres, and the level set's background (world units).
+ * As SparseFrame::buildFromPoints does for the reference's collider frame, every 8^3 tile
+ * that holds an active voxel or neighbours one becomes a collider tile; its cells store
+ * phi / dx and vel / dx (voxel units), cells without a voxel the background / dx, and every
+ * other cell reads the background with zero velocity and normal. Normals are normalised
+ * central differences of the stored distances. Memory follows the collider's tiles, not
+ * the frame. Replaces boxes or a per-cell field; count = 0 removes the collider. */
+int bora_flip_set_collider_voxels( bora_flip_handle h, const int32_t* ijk, const float* phi, const float* vel,
+                                   size_t count, float background );
 
 /* FLIPMethod::advanceOneStep (FLIPMethod.cu:208-298) in voxel space. Returns
  * BORA_WARN_NOT_CONVERGED when the pressure solve stopped on its iteration caps. */
@@ -256,6 +269,28 @@ int bora_flip_get_tiles( bora_flip_handle h, int32_t* ijk, size_t cap_tiles );
 #define BORA_FIELD_RHS 6       /* float  right-hand side b = -div (fluid cells) */
 #define BORA_FIELD_CODE 7      /* uint16 stencil code (bit 15 fluid, bits 8-11 diagonal, bits 0-5 fluid nbrs) */
 int bora_flip_get_field( bora_flip_handle h, int which, void* out, size_t bytes );
+
+/* The SOP's sparse -> VDB conversions after a frame (SOP_FlipWater.cpp:252-264):
+ * FieldCast's convertSurfaceVDB (base/header/FieldCast.h:362-440) and convertVelocityVDB
+ * (FieldCast.h:14-48), computed on the device and returned as OpenVDB leaf nodes: 8^3
+ * voxel blocks at multiples of 8 (VDB voxel (i,j,k) = the frame's cell (i,j,k); x fastest
+ * inside a leaf, bit l of the 512-bit mask = voxel l). Per leaf: origins 3 int32 (voxel
+ * coordinates, may be negative), masks 8 uint64 (active voxels), values 512 floats
+ * (BORA_VDB_SURFACE) or 512 x 3 floats (BORA_VDB_VELOCITY).
+ *   surface:  phi * dx (world units) on the cells of active tiles inside the grid, background
+ *             * dx on inactive voxels; with params.enable_water_tank, the 3-cell border band
+ *             around and below the grid up to 3 cells above params.wall_level becomes active
+ *             with min(cell centre y - wall_level, value). Call after post-processing (the
+ *             surface is then a signed distance with background 10 voxels).
+ *   velocity: the splatted velocity times dx (world units per second), active where its
+ *             length is not below 1e-30, 0 elsewhere.
+ * Leaves without an active voxel are omitted. transform (4 floats, may be NULL): voxel size
+ * dx and the translation min + dx/2 of the VDB linear transform; background (may be NULL).
+ * With origins == NULL only *nleaves is set; BORA_ERR_CAPACITY when cap_leaves is short. */
+#define BORA_VDB_SURFACE 0
+#define BORA_VDB_VELOCITY 1
+int bora_flip_export_vdb( bora_flip_handle h, int which, int32_t* origins, uint64_t* masks, float* values,
+                          size_t cap_leaves, size_t* nleaves, float* transform, float* background );
 int bora_flip_set_field( bora_flip_handle h, int which, const void* in, size_t bytes );
 
 int bora_flip_get_stats( bora_flip_handle h, bora_flip_stats* out );

@@ -103,6 +103,7 @@ def _oracle_lib() -> ctypes.CDLL:
         lib.ora_set_threads.argtypes = [ctypes.c_int]
         lib.ora_get_threads.restype = ctypes.c_int
         lib.ora_set_colliders.argtypes = [_vp, ctypes.c_int, _vp, ctypes.c_float]
+        lib.ora_set_collider_voxels.argtypes = [_vp, _vp, _vp, _vp, ctypes.c_size_t, ctypes.c_float]
         lib.ora_set_particles.argtypes = [_vp, _vp, _vp, _vp, ctypes.c_size_t]
         lib.ora_num_particles.argtypes = [_vp]
         lib.ora_num_particles.restype = ctypes.c_size_t
@@ -247,6 +248,14 @@ class Oracle(_SimBase):
         arr = np.ascontiguousarray(np.array([np.concatenate([lo, hi, v]) for lo, hi, v in boxes],
                                             np.float32).reshape(-1))
         self.lib.ora_set_colliders(self.h, len(boxes), _ptr(arr), band)
+
+    def set_collider_voxels(self, ijk, phi, vel=None, background: float = 0.0) -> None:
+        """Sparse collider from a level set's active voxels (world-unit phi and velocity)."""
+        self._col_keep = (np.ascontiguousarray(ijk, np.int32).reshape(-1, 3),
+                          np.ascontiguousarray(phi, np.float32).reshape(-1),
+                          None if vel is None else np.ascontiguousarray(vel, np.float32).reshape(-1, 3))
+        ijk, phi, vel = self._col_keep
+        self.lib.ora_set_collider_voxels(self.h, _ptr(ijk), _ptr(phi), _ptr(vel), len(phi), float(background))
 
     def fill_water_tank(self, per_cell: int = 8) -> int:
         """FLIPMethod::fillWaterTank restated (particles appended in voxel space)."""

@@ -12,6 +12,13 @@
  *             clamped to the grid), normalised like Vec3f::normalized()
  *             (base/header/Vector3.h:350-354).
  * Queries use SparseField::lerp's rule (base/header/SparseField.h:150-173).
+ *
+ * A sparse collider (CollisionSource::update, CollisionSource.h:66-126, from a level set's
+ * active voxels) replaces the boxes when tslot is set: the collider's 8^3 tiles over the
+ * frame's tile grid hold cell-centre samples (phi, velocity; voxel units); cells outside
+ * them read the background phi with zero velocity and zero normal (the reference's
+ * fields' backgrounds outside the collider frame); normals on the collider's tiles are the
+ * same normalised central differences of phi.
  * Shared by the CPU oracle restatement and the reference host shim so that both read
  * identical collider samples. Compile without floating-point contraction. */
 #ifndef BORA_COLLIDER_MATH_H
@@ -36,7 +43,25 @@ typedef struct BoraColliderSet
     int count;
     float band;
     BoraColliderBox box[BORA_MAX_COLLIDERS];
+    /* sparse collider: tile slot table over the frame's 8^3 tile grid (or NULL), samples */
+    const int* tslot;
+    const float* tphi;  /* [slots * 512] */
+    const float* tvel;  /* [slots * 512 * 3] or NULL (zero) */
+    float tbg;
+    int ttx, tty;
 } BoraColliderSet;
+
+static inline int bora_collider_active( const BoraColliderSet* s ) { return s->count > 0 || s->tslot != 0; }
+
+/* the sparse collider's slot of the tile holding cell (i,j,k), or -1 */
+static inline int bora_collider_tile_slot( const BoraColliderSet* s, int i, int j, int k )
+{
+    return s->tslot[(size_t)( i >> 3 ) + (size_t)s->ttx * ( (size_t)( j >> 3 ) + (size_t)s->tty * (size_t)( k >> 3 ) )];
+}
+static inline size_t bora_collider_local( int i, int j, int k )
+{
+    return (size_t)( ( i & 7 ) | ( ( j & 7 ) << 3 ) | ( ( k & 7 ) << 6 ) );
+}
 
 static inline float bora_box_sdf( const BoraColliderBox* b, float px, float py, float pz )
 {
@@ -62,6 +87,12 @@ static inline float bora_box_sdf( const BoraColliderBox* b, float px, float py, 
 /* Clamped phi sample at cell (i,j,k); *arg receives the index of the closest box. */
 static inline float bora_collider_phi_cell( const BoraColliderSet* s, int i, int j, int k, int* arg )
 {
+    if( s->tslot )
+    {
+        const int sl = bora_collider_tile_slot( s, i, j, k );
+        if( arg ) *arg = 0;
+        return sl < 0 ? s->tbg : s->tphi[(size_t)sl * 512 + bora_collider_local( i, j, k )];
+    }
     const float px = (float)i + 0.5f, py = (float)j + 0.5f, pz = (float)k + 0.5f;
     float best = s->band;
     int a = -1;
@@ -84,6 +115,21 @@ static inline void bora_collider_sample( const BoraColliderSet* s, int nx, int n
     {
         out[0] = bora_collider_phi_cell( s, i, j, k, &a );
         out[1] = out[2] = 0.f;
+        return;
+    }
+    if( s->tslot && which == BORA_COLLIDER_VELOCITY )
+    {
+        const int sl = bora_collider_tile_slot( s, i, j, k );
+        const size_t c = (size_t)sl * 512 + bora_collider_local( i, j, k );
+        const int have = sl >= 0 && s->tvel;
+        out[0] = have ? s->tvel[3 * c] : 0.f;
+        out[1] = have ? s->tvel[3 * c + 1] : 0.f;
+        out[2] = have ? s->tvel[3 * c + 2] : 0.f;
+        return;
+    }
+    if( s->tslot && bora_collider_tile_slot( s, i, j, k ) < 0 )
+    {
+        out[0] = out[1] = out[2] = 0.f;
         return;
     }
     if( which == BORA_COLLIDER_VELOCITY )

@@ -99,6 +99,8 @@ struct Oracle
     std::vector<uint8_t> removed;
     // colliders
     BoraColliderSet cols;
+    std::vector<int> col_tslot;        // sparse collider (ora_set_collider_voxels)
+    std::vector<float> col_tphi, col_tvel;
 
     size_t ncells() const { return coords.size() / 3 * (size_t)B * B * B; }
 
@@ -129,14 +131,14 @@ struct Oracle
     // Collider queries (CollisionSource.h:128-150, restated in collider_math.h)
     inline float colPhi( float px, float py, float pz ) const
     {
-        if( cols.count == 0 ) return 5.f;
+        if( !bora_collider_active( &cols ) ) return 5.f;
         float v[3];
         bora_collider_lerp( &cols, nx, ny, nz, px, py, pz, BORA_COLLIDER_PHI, v );
         return v[0];
     }
     inline V3 colVec( float px, float py, float pz, int which ) const
     {
-        if( cols.count == 0 ) return V3{ 0.f, 0.f, 0.f };
+        if( !bora_collider_active( &cols ) ) return V3{ 0.f, 0.f, 0.f };
         float v[3];
         bora_collider_lerp( &cols, nx, ny, nz, px, py, pz, which, v );
         return V3{ v[0], v[1], v[2] };
@@ -245,7 +247,7 @@ struct Oracle
         // Grid::voxelVector / voxelPoint (Grid.h:446-458)
         voxelForce = V3{ c.gravity[0] / scale[0], c.gravity[1] / scale[1], c.gravity[2] / scale[2] };
         voxelWall = ( c.wall_level - translate[1] ) / scale[1];
-        cols.count = 0;
+        std::memset( &cols, 0, sizeof( cols ) );
         cols.band = 5.f;
     }
 
@@ -1211,6 +1213,66 @@ void ora_destroy( void* h ) { delete (Oracle*)h; }
 
 void ora_set_threads( int n ) { if( n > 0 ) omp_set_num_threads( n ); }
 int ora_get_threads() { return omp_get_max_threads(); }
+
+// CollisionSource::update (CollisionSource.h:66-126) from a level set's active voxels
+// (frame cells ijk, phi in world units, velocities in world units per second or NULL, the
+// level set's background): SparseFrame::buildFromPoints's rule - a tile is the collider's
+// when an active voxel lies in it or in one of its 26 neighbours, here over 8^3 tiles - and
+// samples phi / h, v / scale at the voxels, background / h on the collider's other cells.
+void ora_set_collider_voxels( void* h, const int32_t* ijk, const float* phi, const float* vel, size_t count,
+                              float background )
+{
+    Oracle* o = (Oracle*)h;
+    std::memset( &o->cols, 0, sizeof( o->cols ) );
+    o->col_tslot.clear();
+    o->col_tphi.clear();
+    o->col_tvel.clear();
+    if( count == 0 ) return;
+    const int nx = o->nx, ny = o->ny, nz = o->nz;
+    const int tx = ( nx + 7 ) / 8, ty = ( ny + 7 ) / 8, tz = ( nz + 7 ) / 8;
+    const size_t ntv = (size_t)tx * ty * tz;
+    auto lin = [&]( int a, int b, int d ) { return (size_t)a + (size_t)tx * ( (size_t)b + (size_t)ty * d ); };
+    std::vector<uint8_t> hit( ntv, 0 );
+    for( size_t v = 0; v < count; ++v )
+    {
+        const int i = ijk[3 * v], j = ijk[3 * v + 1], k = ijk[3 * v + 2];
+        if( i < 0 || j < 0 || k < 0 || i >= nx || j >= ny || k >= nz ) continue;
+        hit[lin( i / 8, j / 8, k / 8 )] = 1;
+    }
+    o->col_tslot.assign( ntv, -1 );
+    int nslots = 0;
+    for( int d = 0; d < tz; ++d )
+        for( int b = 0; b < ty; ++b )
+            for( int a = 0; a < tx; ++a )
+            {
+                bool any = false;
+                for( int dd = d - 1; dd <= d + 1 && !any; ++dd )
+                    for( int bb = b - 1; bb <= b + 1 && !any; ++bb )
+                        for( int aa = a - 1; aa <= a + 1 && !any; ++aa )
+                            if( aa >= 0 && bb >= 0 && dd >= 0 && aa < tx && bb < ty && dd < tz && hit[lin( aa, bb, dd )] )
+                                any = true;
+                if( any ) o->col_tslot[lin( a, b, d )] = nslots++;
+            }
+    const float hsz = o->scale[0];
+    const float bg = background / hsz;
+    o->col_tphi.assign( (size_t)nslots * 512, bg );
+    if( vel ) o->col_tvel.assign( (size_t)nslots * 512 * 3, 0.f );
+    for( size_t v = 0; v < count; ++v )
+    {
+        const int i = ijk[3 * v], j = ijk[3 * v + 1], k = ijk[3 * v + 2];
+        if( i < 0 || j < 0 || k < 0 || i >= nx || j >= ny || k >= nz ) continue;
+        const size_t q = (size_t)o->col_tslot[lin( i / 8, j / 8, k / 8 )] * 512 + bora_collider_local( i, j, k );
+        o->col_tphi[q] = phi[v] / hsz;
+        if( vel )
+            for( int a = 0; a < 3; ++a ) o->col_tvel[3 * q + a] = vel[3 * v + a] / o->scale[a];
+    }
+    o->cols.tslot = o->col_tslot.data();
+    o->cols.tphi = o->col_tphi.data();
+    o->cols.tvel = vel ? o->col_tvel.data() : nullptr;
+    o->cols.tbg = bg;
+    o->cols.ttx = tx;
+    o->cols.tty = ty;
+}
 
 void ora_set_colliders( void* h, int n, const float* boxes, float band )
 {

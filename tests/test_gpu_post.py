@@ -305,3 +305,42 @@ def test_full_size_post_process_invariants(gpu):
     band[0, :, :] = band[-1, :, :] = band[:, 0, :] = band[:, -1, :] = band[:, :, 0] = band[:, :, -1] = False
     frac = np.mean(np.abs(mag[band] - 1.0) < 0.25)
     assert frac > 0.9, frac
+
+
+@pytest.mark.parametrize("name", ["swirl_padded_22", "bubble_32"])
+def test_vdb_export_matches_fieldcast(gpu, name):
+    """The device's sparse -> VDB leaves after a frame against FieldCast's conversions
+    restated in the oracle (oracle/fieldcast.py), bit for bit, on the device's own fields:
+    surface phi * dx with background * dx (and, for the water tank, the 3-cell border band's
+    Min(cell centre y - level, value)), velocity v * dx without the voxels below 1e-30."""
+    from oracle import fieldcast
+    sc, tank = make_case(name)
+    kw = {"enable_water_tank": 1} if tank else {}
+    sim = gpu.FlipSim.from_scene(sc, **kw)
+    assert sim.step(sc.dt) == 0
+    sim.post_process()
+    fi = sim.frame_info()
+    tiles = sim.tiles()
+    level = float(sim.params.wall_level)
+    for which in (gpu.VDB_SURFACE, gpu.VDB_VELOCITY):
+        dev = sim.export_vdb(which)
+        dx = np.float32(fi["scale"][0])
+        np.testing.assert_array_equal(dev["transform"], np.array([dx, *(fi["translate"] + dx * np.float32(0.5))],
+                                                                 np.float32))
+        if which == gpu.VDB_SURFACE:
+            assert dev["background"] == np.float32(10.0) * dx
+            ref = fieldcast.convert_surface(sim.field(gpu.FIELD_SURF), tiles, fi["nx"], fi["ny"], fi["nz"],
+                                            fi["translate"], fi["scale"], 10.0, tank, level)
+        else:
+            assert dev["background"] == 0.0
+            ref = fieldcast.convert_velocity(sim.field(gpu.FIELD_VELO), tiles, fi["nx"], fi["ny"], fi["nz"],
+                                             fi["scale"])
+        got = {tuple(int(v) for v in o): n for n, o in enumerate(dev["origins"])}
+        assert set(got) == set(ref), (which, sorted(set(got) ^ set(ref))[:5])
+        for origin, (mask, vals) in ref.items():
+            n = got[origin]
+            bits = np.unpackbits(dev["masks"][n].view(np.uint8), bitorder="little").astype(bool)
+            np.testing.assert_array_equal(bits, mask, err_msg=str(origin))
+            np.testing.assert_array_equal(dev["values"][n], vals, err_msg=str(origin))
+        if tank and which == gpu.VDB_SURFACE:
+            assert min(o[1] for o in got) < 0  # the band's leaves below the grid

@@ -10,6 +10,7 @@
 
 #include <atomic>
 #include <utility>
+#include <vector>
 
 // ---- per-device values computed on first use ------------------------------------------
 // Launch shapes and device attributes are queried once per device ordinal. Host threads
@@ -161,6 +162,20 @@ void bora_launch_surface_fields( const BoraGridDev& g, int ntiles, BoraTilesDev 
 void bora_launch_particle_attributes( const BoraGridDev& g, const int32_t* slot_of, size_t np, BoraParticlesDev p,
                                       const float* wx, const float* wy, const float* wz, const float* curvature,
                                       float3 scale, float dis, cudaStream_t st );
+
+// ---- sparse -> VDB leaf export (FieldCast convertSurfaceVDB / convertVelocityVDB) ------
+// leaf_ijk: 3 ints (voxel origin) per leaf; leaf_slot: its tile's slot or -1 (band leaf);
+// mask: 8 x 64 bits per leaf; val: 512 (surface) or 3 x 512 (velocity) floats per leaf.
+void bora_launch_vdb_surface( const BoraGridDev& g, const float* scale, const float* translate, int nleaves,
+                              const int32_t* leaf_ijk, const int32_t* leaf_slot, const float* surf, float bg, int tank,
+                              float level, uint64_t* mask, float* val, cudaStream_t st );
+void bora_launch_vdb_velocity( const BoraGridDev& g, const float* scale, int nleaves, const int32_t* leaf_ijk,
+                               const int32_t* leaf_slot, const float* vx, const float* vy, const float* vz,
+                               uint64_t* mask, float* val, cudaStream_t st );
+int bora_vdb_level_index( float level, float min_y, float dx );
+// tile coordinates (3 ints each) of the water tank's border band (FieldCast.h:398-440)
+void bora_vdb_band_tiles( const BoraGridDev& g, const float* scale, const float* translate, float level,
+                          std::vector<int32_t>& tiles );
 
 void bora_launch_to_soa( size_t n, const float* pos, const float* vel, int space, const float* translate,
                          const float* scale, BoraParticlesDev p, size_t offset, int32_t first_id, cudaStream_t st );

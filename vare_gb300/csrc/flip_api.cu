@@ -138,10 +138,12 @@ struct bora_flip_sim
     DevBuf sx, se, sr, sd0, sd1, sq, sz, sminv;
     DevBuf cell_count, cell_start;
     DevBuf col_phi, col_vel;  // collider signed distance / velocity per frame cell
+    DevBuf col_tslot, col_tnear, col_tphi, col_tvel;  // sparse collider: tile table, samples
 
     // multigrid hierarchy (mixed solver): per level type, code, r, z0, z1
     static constexpr int kMaxLevels = 16;
     DevBuf mg_type[kMaxLevels], mg_code[kMaxLevels], mg_r[kMaxLevels], mg_z0[kMaxLevels], mg_z1[kMaxLevels];
+    DevBuf vdb_leaf, vdb_mask, vdb_val;  // VDB leaf export: leaf origins + slots, masks, values
     DevBuf mg_mid;         // static image of the coarse levels' cluster kernel (mg_mid.cu), or empty
     bool mg_mid_on = false;
     BoraLevelDev levels[kMaxLevels] = {};
@@ -868,7 +870,8 @@ void for_each_buffer( bora_flip_sim* s, F&& f )
                       &s->pres, &s->vx, &s->vy, &s->vz, &s->cx, &s->cy, &s->cz, &s->flag, &s->code, &s->rhs, &s->sx,
                       &s->se, &s->sr, &s->sd0, &s->sd1, &s->sq, &s->sz, &s->sminv, &s->cell_count, &s->cell_start,
                       &s->ring, &s->partials, &s->done, &s->adj, &s->vkey, &s->key, &s->idx, &s->scan_scratch,
-                      &s->counters, &s->stage_in, &s->stage_out, &s->live_flag, &s->col_phi, &s->col_vel };
+                      &s->counters, &s->stage_in, &s->stage_out, &s->live_flag, &s->col_phi, &s->col_vel,
+                      &s->col_tslot, &s->col_tnear, &s->col_tphi, &s->col_tvel };
     for( DevBuf* b : all ) f( *b );
     for( int q = 0; q < 2; ++q )
     {
@@ -883,6 +886,7 @@ void for_each_buffer( bora_flip_sim* s, F&& f )
         f( s->mg_z0[l] ); f( s->mg_z1[l] );
     }
     f( s->mg_mid );
+    f( s->vdb_leaf ); f( s->vdb_mask ); f( s->vdb_val );
 }
 
 extern "C" {
@@ -1113,12 +1117,90 @@ int bora_flip_set_collider_field( bora_flip_handle s, const float* phi, const fl
     if( vel ) BORA_TRY( grow( s->col_vel, n * 12, false, s->st ) );
     c.fphi = nullptr;
     c.fvel = nullptr;
-    c.count = 0;  // replaces any boxes
+    c.tslot = nullptr;
+    c.count = 0;  // replaces any boxes or sparse collider
     BORA_TRY( cudaMemcpyAsync( s->col_phi.p, phi, n * 4, cudaMemcpyHostToDevice, s->st ) );
     if( vel ) BORA_TRY( cudaMemcpyAsync( s->col_vel.p, vel, n * 12, cudaMemcpyHostToDevice, s->st ) );
     BORA_TRY( cudaStreamSynchronize( s->st ) );  // the caller may free its buffers on return
     c.fphi = P<float>( s->col_phi );
     c.fvel = vel ? P<float>( s->col_vel ) : nullptr;
+    return BORA_OK;
+}
+
+int bora_flip_set_collider_voxels( bora_flip_handle s, const int32_t* ijk, const float* phi, const float* vel,
+                                   size_t count, float background )
+{
+    if( !s || ( count > 0 && ( !ijk || !phi ) ) || !std::isfinite( background ) ) return BORA_ERR_INVALID_ARG;
+    BoraColliderDev& c = s->g.cols;
+    if( count == 0 )
+    {
+        c.tslot = nullptr;
+        c.tnear = nullptr;
+        return BORA_OK;
+    }
+    const int nx = s->g.nx, ny = s->g.ny, nz = s->g.nz, tx = s->g.tx, ty = s->g.ty, tz = s->g.tz;
+    const size_t ntv = (size_t)tx * ty * tz;
+    auto tlin = [&]( int a, int b, int d ) { return (size_t)a + (size_t)tx * ( (size_t)b + (size_t)ty * d ); };
+    // SparseFrame::buildFromPoints over the active voxels (SparseFrame.cu:83-155): a tile is
+    // the collider's when an active voxel lies in it or in one of its 26 neighbours
+    std::vector<uint8_t> hit( ntv, 0 ), own( ntv, 0 ), near( ntv, 0 );
+    for( size_t v = 0; v < count; ++v )
+    {
+        const int i = ijk[3 * v], j = ijk[3 * v + 1], k = ijk[3 * v + 2];
+        if( i < 0 || j < 0 || k < 0 || i >= nx || j >= ny || k >= nz ) continue;  // outside the frame: never sampled
+        hit[tlin( i >> 3, j >> 3, k >> 3 )] = 1;
+    }
+    auto dilate = [&]( const std::vector<uint8_t>& in, std::vector<uint8_t>& out ) {
+        for( int d = 0; d < tz; ++d )
+            for( int b = 0; b < ty; ++b )
+                for( int a = 0; a < tx; ++a )
+                {
+                    if( !in[tlin( a, b, d )] ) continue;
+                    for( int dd = std::max( 0, d - 1 ); dd <= std::min( tz - 1, d + 1 ); ++dd )
+                        for( int bb = std::max( 0, b - 1 ); bb <= std::min( ty - 1, b + 1 ); ++bb )
+                            for( int aa = std::max( 0, a - 1 ); aa <= std::min( tx - 1, a + 1 ); ++aa )
+                                out[tlin( aa, bb, dd )] = 1;
+                }
+    };
+    dilate( hit, own );
+    dilate( own, near );
+    // slots in linear tile order; samples: phi / h and v / scale (CollisionSource.h:105-121),
+    // the background / h on the other cells of the collider's tiles
+    const float h = s->scale[0];
+    std::vector<int32_t> slot( ntv, -1 );
+    int nslots = 0;
+    for( size_t t = 0; t < ntv; ++t )
+        if( own[t] ) slot[t] = nslots++;
+    const float bg = background / h;
+    std::vector<float> tphi( (size_t)nslots * 512, bg ), tvel;
+    if( vel ) tvel.assign( (size_t)nslots * 512 * 3, 0.f );
+    for( size_t v = 0; v < count; ++v )
+    {
+        const int i = ijk[3 * v], j = ijk[3 * v + 1], k = ijk[3 * v + 2];
+        if( i < 0 || j < 0 || k < 0 || i >= nx || j >= ny || k >= nz ) continue;
+        const size_t q = (size_t)slot[tlin( i >> 3, j >> 3, k >> 3 )] * 512 + (size_t)bora_local( i, j, k );
+        tphi[q] = phi[v] / h;
+        if( vel )
+            for( int a = 0; a < 3; ++a ) tvel[3 * q + a] = vel[3 * v + a] / s->scale[a];
+    }
+    // all allocations first; a failure after the first copy leaves no collider at all
+    BORA_TRY( grow( s->col_tslot, ntv * 4, false, s->st ) );
+    BORA_TRY( grow( s->col_tnear, ntv, false, s->st ) );
+    BORA_TRY( grow( s->col_tphi, tphi.size() * 4 + 16, false, s->st ) );
+    if( vel ) BORA_TRY( grow( s->col_tvel, tvel.size() * 4 + 16, false, s->st ) );
+    std::memset( &c, 0, sizeof( c ) );  // replaces any boxes or per-cell field
+    BORA_TRY( cudaMemcpyAsync( s->col_tslot.p, slot.data(), ntv * 4, cudaMemcpyHostToDevice, s->st ) );
+    BORA_TRY( cudaMemcpyAsync( s->col_tnear.p, near.data(), ntv, cudaMemcpyHostToDevice, s->st ) );
+    BORA_TRY( cudaMemcpyAsync( s->col_tphi.p, tphi.data(), tphi.size() * 4, cudaMemcpyHostToDevice, s->st ) );
+    if( vel ) BORA_TRY( cudaMemcpyAsync( s->col_tvel.p, tvel.data(), tvel.size() * 4, cudaMemcpyHostToDevice, s->st ) );
+    BORA_TRY( cudaStreamSynchronize( s->st ) );  // the host vectors go out of scope
+    c.tslot = P<int32_t>( s->col_tslot );
+    c.tnear = P<uint8_t>( s->col_tnear );
+    c.tphi = P<float>( s->col_tphi );
+    c.tvel = vel ? P<float>( s->col_tvel ) : nullptr;
+    c.tbg = bg;
+    c.ttx = tx;
+    c.tty = ty;
     return BORA_OK;
 }
 
@@ -1380,6 +1462,111 @@ int bora_flip_get_tiles( bora_flip_handle s, int32_t* ijk, size_t cap_tiles )
         ijk[3 * t + 1] = ( lin[t] / s->g.tx ) % s->g.ty;
         ijk[3 * t + 2] = lin[t] / ( s->g.tx * s->g.ty );
     }
+    return BORA_OK;
+}
+
+// The surface field's background after post-processing (Rasterization::ReinitializeSurface,
+// Rasterization.cu:422), in voxel units.
+constexpr float kSurfaceBackground = 10.f;
+
+int bora_flip_export_vdb( bora_flip_handle s, int which, int32_t* origins, uint64_t* masks, float* values,
+                          size_t cap_leaves, size_t* nleaves, float* transform, float* background )
+{
+    if( !s || !nleaves || ( which != BORA_VDB_SURFACE && which != BORA_VDB_VELOCITY ) ) return BORA_ERR_INVALID_ARG;
+    *nleaves = 0;
+    const float dx = s->scale[0];
+    if( transform )  // FieldCast.h: linear transform of voxel size dx, translated by min + dx/2
+    {
+        transform[0] = dx;
+        for( int a = 0; a < 3; ++a ) transform[1 + a] = s->translate[a] + dx * 0.5f;
+    }
+    const float bg = which == BORA_VDB_SURFACE ? kSurfaceBackground : 0.f;
+    if( background ) *background = bg * dx;
+    // candidate leaves: the active tiles, then (surface, water tank) the band's other tiles
+    const size_t nt = (size_t)s->ntiles;
+    std::vector<int32_t> lin( nt );
+    if( nt )
+    {
+        BORA_TRY( cudaMemcpyAsync( lin.data(), s->tile_of.p, nt * 4, cudaMemcpyDeviceToHost, s->st ) );
+        BORA_TRY( cudaStreamSynchronize( s->st ) );
+    }
+    const int tx = s->g.tx, ty = s->g.ty, tz = s->g.tz;
+    std::vector<int32_t> leaf;  // per leaf: i, j, k origin, slot
+    leaf.reserve( nt * 4 );
+    for( size_t t = 0; t < nt; ++t )
+    {
+        leaf.push_back( 8 * ( lin[t] % tx ) );
+        leaf.push_back( 8 * ( ( lin[t] / tx ) % ty ) );
+        leaf.push_back( 8 * ( lin[t] / ( tx * ty ) ) );
+        leaf.push_back( (int32_t)t );
+    }
+    const bool tank = which == BORA_VDB_SURFACE && s->prm.enable_water_tank;
+    if( tank )
+    {
+        std::vector<int32_t> band;
+        bora_vdb_band_tiles( s->g, s->scale, s->translate, s->prm.wall_level, band );
+        std::vector<uint8_t> active( (size_t)tx * ty * tz, 0 );
+        for( size_t t = 0; t < nt; ++t ) active[(size_t)lin[t]] = 1;
+        for( size_t b = 0; b < band.size(); b += 3 )
+        {
+            const int ti = band[b], tj = band[b + 1], tk = band[b + 2];
+            const bool inside = ti >= 0 && tj >= 0 && tk >= 0 && ti < tx && tj < ty && tk < tz;
+            if( inside && active[( (size_t)tk * ty + tj ) * tx + ti] ) continue;
+            leaf.push_back( 8 * ti );
+            leaf.push_back( 8 * tj );
+            leaf.push_back( 8 * tk );
+            leaf.push_back( -1 );
+        }
+    }
+    const size_t nl = leaf.size() / 4;
+    if( nl == 0 ) return BORA_OK;
+    const size_t comps = which == BORA_VDB_SURFACE ? 1 : 3;
+    BORA_TRY( grow( s->vdb_leaf, nl * 16, false, s->st ) );
+    BORA_TRY( grow( s->vdb_mask, nl * 64, false, s->st ) );
+    BORA_TRY( grow( s->vdb_val, nl * 512 * comps * 4, false, s->st ) );
+    std::vector<int32_t> ijk( nl * 3 ), slot( nl );
+    for( size_t l = 0; l < nl; ++l )
+    {
+        for( int a = 0; a < 3; ++a ) ijk[3 * l + a] = leaf[4 * l + a];
+        slot[l] = leaf[4 * l + 3];
+    }
+    int32_t* d_ijk = P<int32_t>( s->vdb_leaf );
+    int32_t* d_slot = d_ijk + 3 * nl;
+    BORA_TRY( cudaMemcpyAsync( d_ijk, ijk.data(), nl * 12, cudaMemcpyHostToDevice, s->st ) );
+    BORA_TRY( cudaMemcpyAsync( d_slot, slot.data(), nl * 4, cudaMemcpyHostToDevice, s->st ) );
+    if( which == BORA_VDB_SURFACE )
+        bora_launch_vdb_surface( s->g, s->scale, s->translate, (int)nl, d_ijk, d_slot, P<float>( s->surf ), bg, tank ? 1 : 0,
+                                 s->prm.wall_level, P<uint64_t>( s->vdb_mask ), P<float>( s->vdb_val ), s->st );
+    else
+        bora_launch_vdb_velocity( s->g, s->scale, (int)nl, d_ijk, d_slot, P<float>( s->vx ), P<float>( s->vy ),
+                                  P<float>( s->vz ), P<uint64_t>( s->vdb_mask ), P<float>( s->vdb_val ), s->st );
+    s->stats.kernel_launches += 1;
+    BORA_TRYS( check_launch( s ) );
+    std::vector<uint64_t> m( nl * 8 );
+    BORA_TRY( cudaMemcpyAsync( m.data(), s->vdb_mask.p, nl * 64, cudaMemcpyDeviceToHost, s->st ) );
+    BORA_TRY( cudaStreamSynchronize( s->st ) );
+    // leaves without an active voxel are not written (OpenVDB creates no leaf for them)
+    std::vector<size_t> keep;
+    keep.reserve( nl );
+    for( size_t l = 0; l < nl; ++l )
+    {
+        uint64_t any = 0;
+        for( int w = 0; w < 8; ++w ) any |= m[8 * l + w];
+        if( any ) keep.push_back( l );
+    }
+    *nleaves = keep.size();
+    if( !origins ) return BORA_OK;
+    if( cap_leaves < keep.size() || !masks || !values ) return cap_leaves < keep.size() ? BORA_ERR_CAPACITY : BORA_ERR_INVALID_ARG;
+    const size_t per = 512 * comps;
+    for( size_t q = 0; q < keep.size(); ++q )
+    {
+        const size_t l = keep[q];
+        for( int a = 0; a < 3; ++a ) origins[3 * q + a] = ijk[3 * l + a];
+        for( int w = 0; w < 8; ++w ) masks[8 * q + w] = m[8 * l + w];
+        BORA_TRY( cudaMemcpyAsync( values + q * per, P<float>( s->vdb_val ) + l * per, per * 4, cudaMemcpyDeviceToHost,
+                                   s->st ) );
+    }
+    BORA_TRY( cudaStreamSynchronize( s->st ) );
     return BORA_OK;
 }
 

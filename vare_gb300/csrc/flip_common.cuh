@@ -50,9 +50,26 @@ struct BoraColliderDev
     BoraBoxDev box[BORA_MAX_COLLIDERS];
     const float* fphi;  // [nx*ny*nz] voxel units, or null
     const float* fvel;  // [3*nx*ny*nz] voxel units per second, or null (zero)
+    // sparse collider (CollisionSource::update from a level set's active voxels): the
+    // collider's own 8^3 tiles over the frame's tile grid
+    const int32_t* tslot;  // [tx*ty*tz] collider tile slot or -1, or null (no sparse collider)
+    const uint8_t* tnear;  // [tx*ty*tz] 1 where a collider tile lies within one tile
+    const float* tphi;     // [slots*512] signed distance, voxel units
+    const float* tvel;     // [slots*512*3] velocity, voxel units per second, or null (zero)
+    float tbg;             // the level set's background, voxel units
+    int ttx, tty;          // tile grid extents in x and y (for the lookup)
 };
 
-__host__ __device__ inline bool bora_col_active( const BoraColliderDev& s ) { return s.count > 0 || s.fphi != nullptr; }
+__host__ __device__ inline bool bora_col_active( const BoraColliderDev& s )
+{
+    return s.count > 0 || s.fphi != nullptr || s.tslot != nullptr;
+}
+
+// the sparse collider's slot of the tile holding cell (i,j,k), or -1
+__host__ __device__ inline int bora_col_tile_slot( const BoraColliderDev& s, int i, int j, int k )
+{
+    return s.tslot[(size_t)( i >> 3 ) + (size_t)s.ttx * ( (size_t)( j >> 3 ) + (size_t)s.tty * (size_t)( k >> 3 ) )];
+}
 
 // Grid constants shared by every kernel of one simulation.
 struct BoraGridDev
@@ -112,6 +129,12 @@ __device__ inline float bora_box_sdf( const BoraBoxDev& b, float px, float py, f
 
 __device__ inline float bora_col_phi_cell( const BoraColliderDev& s, int nx, int ny, int i, int j, int k, int* arg )
 {
+    if( s.tslot )
+    {
+        if( arg ) *arg = 0;
+        const int sl = bora_col_tile_slot( s, i, j, k );
+        return sl < 0 ? s.tbg : s.tphi[(size_t)sl * 512 + ( ( i & 7 ) | ( ( j & 7 ) << 3 ) | ( ( k & 7 ) << 6 ) )];
+    }
     if( s.fphi )
     {
         if( arg ) *arg = 0;
@@ -140,6 +163,21 @@ __device__ inline void bora_col_sample( const BoraColliderDev& s, int nx, int ny
     {
         out[0] = bora_col_phi_cell( s, nx, ny, i, j, k, &a );
         out[1] = out[2] = 0.f;
+        return;
+    }
+    if( s.tslot && which == 2 )
+    {
+        const int sl = bora_col_tile_slot( s, i, j, k );
+        const size_t c = (size_t)sl * 512 + ( ( i & 7 ) | ( ( j & 7 ) << 3 ) | ( ( k & 7 ) << 6 ) );
+        const bool have = sl >= 0 && s.tvel;
+        out[0] = have ? s.tvel[3 * c] : 0.f;
+        out[1] = have ? s.tvel[3 * c + 1] : 0.f;
+        out[2] = have ? s.tvel[3 * c + 2] : 0.f;
+        return;
+    }
+    if( s.tslot && bora_col_tile_slot( s, i, j, k ) < 0 )  // the gradient field's background
+    {
+        out[0] = out[1] = out[2] = 0.f;
         return;
     }
     if( which == 2 && s.fphi )

@@ -202,7 +202,21 @@ __device__ inline bool advance_particle( const BoraGridDev& g, const Sampler& sm
     // particle whose start is farther than 2 |v| dt + 2 cells from every box sees positive
     // collider values all step long. (RK2 moves with the grid velocity: no cull.)
     bool hasCols = bora_col_active( g.cols );
-    if( hasCols && !g.cols.fphi && g.advection != BORA_ADVECT_RK2 && inside_grid( g, px, py, pz ) )
+    if( hasCols && g.cols.tslot && g.advection != BORA_ADVECT_RK2 && inside_grid( g, px, py, pz ) )
+    {
+        // sparse collider: every sample outside its tiles is the (positive) background with
+        // a zero normal and velocity; a particle whose tile has no collider tile within one
+        // tile is 8 cells or more from every stored sample, and the samples it reads this
+        // step lie within |v| dt + 3 cells of its start
+        const float move = sqrtf( vx * vx + vy * vy + vz * vz ) * dt;
+        if( g.cols.tbg > 0.f && move < 5.f )
+        {
+            const int ti = bora_imin( bora_trunc( px ) >> 3, g.tx - 1 ), tj = bora_imin( bora_trunc( py ) >> 3, g.ty - 1 ),
+                      tk = bora_imin( bora_trunc( pz ) >> 3, g.tz - 1 );
+            if( !g.cols.tnear[(size_t)ti + (size_t)g.tx * ( (size_t)tj + (size_t)g.ty * tk )] ) hasCols = false;
+        }
+    }
+    else if( hasCols && !g.cols.fphi && g.advection != BORA_ADVECT_RK2 && inside_grid( g, px, py, pz ) )
     {
         const float reach = 2.f * sqrtf( vx * vx + vy * vy + vz * vz ) * dt + 2.f;
         hasCols = false;

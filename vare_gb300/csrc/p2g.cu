@@ -86,14 +86,18 @@ __global__ void __launch_bounds__( kP2GThreads, 2 ) k_p2g( const __grid_constant
             const float wx[2] = { fmaxf( 0.f, 1.f - fabsf( x - cx0 ) ), fmaxf( 0.f, 1.f - fabsf( x - cx1 ) ) };
             const float wy[2] = { fmaxf( 0.f, 1.f - fabsf( y - cy0 ) ), fmaxf( 0.f, 1.f - fabsf( y - cy1 ) ) };
             const float wz[2] = { fmaxf( 0.f, 1.f - fabsf( z - cz0 ) ), fmaxf( 0.f, 1.f - fabsf( z - cz1 ) ) };
+            // the weight rounds like the reference's; its products with the velocity are
+            // accumulated with fused multiply-adds (the sums' order differs from the
+            // reference's atomics in any case)
+            const float wxy[4] = { wx[0] * wy[0], wx[1] * wy[0], wx[0] * wy[1], wx[1] * wy[1] };
 #pragma unroll
             for( int cr = 0; cr < 8; ++cr )  // corner (a, b, c) = bits of cr
             {
-                const float w = wx[cr & 1] * wy[( cr >> 1 ) & 1] * wz[cr >> 2] + 1e-05f;
+                const float w = wxy[cr & 3] * wz[cr >> 2] + 1e-05f;
                 acc[cr][0] += w;
-                acc[cr][1] += w * vx;
-                acc[cr][2] += w * vy;
-                acc[cr][3] += w * vz;
+                acc[cr][1] = fmaf( w, vx, acc[cr][1] );
+                acc[cr][2] = fmaf( w, vy, acc[cr][2] );
+                acc[cr][3] = fmaf( w, vz, acc[cr][3] );
             }
         }
         const uint32_t n = q1 - q0;

@@ -27,6 +27,7 @@ ADVECT_EULER, ADVECT_RK2 = 0, 1
 STAGE_REBUILD, STAGE_P2G, STAGE_BUILD_SYSTEM, STAGE_SOLVE, STAGE_UPDATE_VELOCITY, STAGE_UPDATE_PARTICLES = range(6)
 POST_SPLAT, POST_TANK_SCAN, POST_REDISTANCE, POST_ATTRIBUTES = range(4)
 FIELD_MASS, FIELD_SURF, FIELD_PRES, FIELD_VELO, FIELD_COMP, FIELD_FLAG, FIELD_RHS, FIELD_CODE = range(8)
+VDB_SURFACE, VDB_VELOCITY = 0, 1
 KERNEL_CLASSES = ["bin", "tiles", "sort", "p2g", "rhs", "pcg_direction", "pcg_update", "refine", "velocity", "g2p",
                   "mg_vcycle", "post"]
 _FIELD_DTYPE = {FIELD_MASS: (np.float32, 1), FIELD_SURF: (np.float32, 1), FIELD_PRES: (np.float32, 1),
@@ -91,6 +92,7 @@ _SIGS = {
     "bora_flip_fill_water_tank": (ctypes.c_int, [_vp, _vp]),
     "bora_flip_set_collider_field": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_size_t]),
     "bora_flip_set_colliders": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_float]),
+    "bora_flip_set_collider_voxels": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_size_t, ctypes.c_float]),
     "bora_flip_step": (ctypes.c_int, [_vp, ctypes.c_float]),
     "bora_flip_frame": (ctypes.c_int, [_vp]),
     "bora_flip_run_stage": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_float]),
@@ -109,6 +111,8 @@ _SIGS = {
     "bora_flip_get_tiles": (ctypes.c_int, [_vp, _vp, ctypes.c_size_t]),
     "bora_flip_get_field": (ctypes.c_int, [_vp, ctypes.c_int, _vp, ctypes.c_size_t]),
     "bora_flip_set_field": (ctypes.c_int, [_vp, ctypes.c_int, _vp, ctypes.c_size_t]),
+    "bora_flip_export_vdb": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp, _vp, ctypes.c_size_t,
+                                            ctypes.POINTER(ctypes.c_size_t), _vp, _vp]),
     "bora_flip_get_stats": (ctypes.c_int, [_vp, ctypes.POINTER(Stats)]),
     "bora_flip_status_string": (ctypes.c_char_p, [ctypes.c_int]),
     "bora_flip_set_profiling": (ctypes.c_int, [_vp, ctypes.c_uint32]),
@@ -254,6 +258,15 @@ class FlipSim:
         vel = None if vel is None else np.ascontiguousarray(vel, np.float32).reshape(-1)
         _check(self.lib.bora_flip_set_collider_field(self.h, _ptr(phi), _ptr(vel), phi.size), "set_collider_field")
 
+    def set_collider_voxels(self, ijk, phi, vel=None, background: float = 0.0) -> None:
+        """Sparse collider from a level set's active voxels (bora_flip_set_collider_voxels):
+        ijk (N, 3) frame cells, phi (N,) world units, vel (N, 3) world units/s or None."""
+        ijk = np.ascontiguousarray(ijk, np.int32).reshape(-1, 3)
+        phi = np.ascontiguousarray(phi, np.float32).reshape(-1)
+        vel = None if vel is None else np.ascontiguousarray(vel, np.float32).reshape(-1, 3)
+        _check(self.lib.bora_flip_set_collider_voxels(self.h, _ptr(ijk), _ptr(phi), _ptr(vel), len(phi),
+                                                      float(background)), "set_collider_voxels")
+
     def fill_water_tank(self) -> int:
         """FLIPMethod::fillWaterTank: append the tank's particles; returns how many."""
         n = ctypes.c_size_t()
@@ -359,6 +372,25 @@ class FlipSim:
         dt, nc = _FIELD_DTYPE[which]
         data = np.ascontiguousarray(data, dt)
         _check(self.lib.bora_flip_set_field(self.h, which, _ptr(data), data.nbytes), "set_field")
+
+    def export_vdb(self, which: int) -> dict:
+        """FieldCast's sparse -> VDB conversion as OpenVDB leaf blocks (bora_flip_export_vdb):
+        origins (L, 3) int32, masks (L, 8) uint64, values (L, 512) or (L, 512, 3) float32,
+        the transform (voxel size, translate xyz) and the background value."""
+        n = ctypes.c_size_t(0)
+        _check(self.lib.bora_flip_export_vdb(self.h, which, None, None, None, 0, ctypes.byref(n), None, None),
+               "export_vdb")
+        L = n.value
+        comps = 1 if which == VDB_SURFACE else 3
+        origins = np.zeros((L, 3), np.int32)
+        masks = np.zeros((L, 8), np.uint64)
+        values = np.zeros((L, 512) if comps == 1 else (L, 512, 3), np.float32)
+        xform = np.zeros(4, np.float32)
+        bg = np.zeros(1, np.float32)
+        _check(self.lib.bora_flip_export_vdb(self.h, which, _ptr(origins), _ptr(masks), _ptr(values), L,
+                                             ctypes.byref(n), _ptr(xform), _ptr(bg)), "export_vdb")
+        return dict(origins=origins[:n.value], masks=masks[:n.value], values=values[:n.value], transform=xform,
+                    background=float(bg[0]))
 
     def stats(self) -> dict:
         s = Stats()
