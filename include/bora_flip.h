@@ -192,6 +192,17 @@ int bora_flip_set_collider_voxels( bora_flip_handle h, const int32_t* ijk, const
 /* FLIPMethod::advanceOneStep (FLIPMethod.cu:208-298) in voxel space. Returns
  * BORA_WARN_NOT_CONVERGED when the pressure solve stopped on its iteration caps. */
 int bora_flip_step( bora_flip_handle h, float dt );
+/* Several independent simulations one step each (FLIPMethod::advanceOneStep for every
+ * handle), with the pressure solve - almost all of a step's kernel launches - launched once
+ * per kernel for all of them: simulation k is row k of every launch, on the grid its own
+ * launch would use, with its own reductions and convergence, so each handle's result is the
+ * same as from bora_flip_step_batch with that handle alone. The other stages run per handle,
+ * back to back on the first handle's stream. Handles of the plain solver form (or whose
+ * multigrid hierarchy does not fit the batched coarse-level kernel) take a bora_flip_step of
+ * their own. status[k] receives handle k's step status; the handles must live on one
+ * device and be distinct. */
+int bora_flip_step_batch( bora_flip_handle* hs, int n, float dt, int* status );
+
 /* FLIPMethod::advanceOneFrame (FLIPMethod.cu:177-206): one step of params.dt, then (with
  * params.post_process) bora_flip_post_process. */
 int bora_flip_frame( bora_flip_handle h );

@@ -10,15 +10,17 @@
  *   - a scheduler thread admits queued requests in arrival order whenever a slot is free
  *     and the request's device-memory estimate fits in the budget next to the requests
  *     already running (a request that alone exceeds the budget fails);
- *   - every admitted request runs on its own CUDA stream, driven by its own host thread,
- *     so the device overlaps the kernels of all running requests; a request that arrives
- *     while others run starts as soon as a slot and memory free up (continuous
- *     batching, not a queue drained in rounds);
+ *   - a stepper thread advances all running requests together, one round at a time:
+ *     every running request takes one step per round, through bora_flip_step_batch, so the
+ *     pressure solve's kernels (almost all of a step's launches) run once per round for
+ *     all requests, each request on its own tiles and reductions; a request that arrives
+ *     while others run joins at the next round as soon as a slot and memory free up
+ *     (continuous batching, not a queue drained in rounds);
  *   - finished requests keep their final particles (and per-step latencies) until
  *     bora_serve_release.
  *
- * Each request runs the same deterministic kernels as bora_flip_step, so its result is
- * bit-identical whether it runs alone or in a mix.
+ * A request's launches and arithmetic in a batched step do not depend on the other
+ * requests, so its result is bit-identical whether it runs alone or in a mix.
  *
  * All functions return a bora_flip.h status code (BORA_OK = 0, negative = error).
  */
@@ -39,7 +41,7 @@ typedef struct bora_server* bora_serve_handle;
 typedef struct bora_serve_config
 {
     uint64_t hbm_budget_bytes; /* device memory the running requests may hold together */
-    int max_running;           /* running requests at most (host threads / streams) */
+    int max_running;           /* running requests at most (default 64) */
     int reserved;
 } bora_serve_config;
 

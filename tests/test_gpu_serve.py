@@ -21,9 +21,10 @@ def _requests():
 
 
 def _alone(sc, steps, **kw):
+    """The request run alone: its own simulation stepped in batches of one."""
     sim = flip.FlipSim.from_scene(sc, **kw)
     for _ in range(steps):
-        assert sim.step(sc.dt) >= 0
+        assert flip.step_batch([sim], sc.dt)[0] >= 0
     pos, vel, _, ids = sim.particles()
     o = np.argsort(ids)
     return pos[o], vel[o], ids[o]

@@ -251,6 +251,66 @@ int bora_mg_mid_vcycle( const BoraGridDev& g, const BoraLevelDev* levels, int nl
 void bora_mg_vcycle( const BoraGridDev& g, const BoraLevelDev* levels, int nlevels, BoraTilesDev t, const void* mid_image,
                      const float* r, float* z, BoraReduceDev red, int slot_rr, int slot_rz, int coarse_sweeps,
                      cudaStream_t st );
+// ---- batched solve: several simulations, one launch per kernel ---------------------------
+// A batched launch runs simulation blockIdx.y of the batch on the grid that its own
+// single-simulation launch would use (grid[], fixed by its tile count alone; blocks beyond
+// it return at once) and reduces into its own ring, so every simulation's arithmetic and
+// summation order are the same alone and in any batch. Arguments come from device arrays.
+enum BoraMemberGrid
+{
+    kGridDir = 0, kGridUpd, kGridCells, kGridResidual, kGridDown8, kGridDown4, kGridDown2, kGridUp8, kGridUp4, kGridUp2,
+    kGridCount
+};
+struct BoraMemberSolve
+{
+    int ntiles;
+    const int32_t* nbr;
+    const uint16_t* code;
+    const float* b;
+    float* pres;
+    BoraSolverDev sv;
+    BoraReduceDev red;
+    BoraLevelDev L[4];     // multigrid levels 0..3 (level 3: one cell per tile)
+    const __half* z3;      // level 3's correction, written by the coarse cluster kernel
+    int grid[kGridCount];  // this simulation's own grid per kernel
+};
+struct BoraMemberSlots  // ring slots of one batched launch sequence
+{
+    int active;                          // 0: this simulation sits the launch out
+    int dsel;                            // which search-direction buffer is the current one
+    int rz_new, rz_old, dq, a_rz, a_dq;  // direction (beta = rz_new / rz_old; pending alpha)
+    int rz_in, dq_in, rr_out;            // update (alpha = rz_in / dq_in), r.r out
+    int rr, rz;                          // V-cycle: the scale's r.r, r.z out
+    int n2, mx;                          // solve init / refinement residual: ||r||^2, max|r|
+};
+
+// The coarse cluster kernel of a batch: a simulation's descriptor (opaque, desc_bytes each;
+// 0 when its hierarchy does not fit the kernel), and one launch with one cluster per
+// simulation (all with the same cluster size; shared memory for the largest).
+size_t bora_mg_mid_desc_bytes();
+int bora_mg_mid_describe( const BoraGridDev& g, const BoraLevelDev* levels, int nlevels, BoraTilesDev t, int ntiles,
+                          const void* image, uint32_t* err, int sweeps, void* desc, size_t* smem, int* ctas );
+void bora_mg_mid_launch_batch( const void* descs, const BoraMemberSlots* slots, int n, int ctas, size_t smem,
+                               cudaStream_t st );
+// Batched launches of the solver kernels (projection.cu, multigrid.cu): n simulations in y,
+// grid x = the largest of their own grids for that kernel.
+void bora_launch_solve_init_batch( const BoraMemberSolve* ms, const BoraMemberSlots* sl, int n, int gx, cudaStream_t st );
+void bora_launch_pcg_direction_batch( const BoraMemberSolve* ms, const BoraMemberSlots* sl, int n, int gx,
+                                      cudaStream_t st );
+void bora_launch_refine_accumulate_batch( const BoraMemberSolve* ms, const BoraMemberSlots* sl, int n, int gx,
+                                          cudaStream_t st );
+void bora_launch_refine_residual_batch( const BoraMemberSolve* ms, const BoraMemberSlots* sl, int n, int gx,
+                                        cudaStream_t st );
+void bora_launch_write_pressure_batch( const BoraMemberSolve* ms, int n, int gx, cudaStream_t st );
+void bora_launch_pcg_update_noprec_batch( const BoraMemberSolve* ms, const BoraMemberSlots* sl, int n, int gx,
+                                          cudaStream_t st );
+// one fused V-cycle kernel (down or up) of level l (0, 1, 2) for the batch
+void bora_launch_mg_fused_batch( bool up, int l, const BoraMemberSolve* ms, const BoraMemberSlots* sl, int n, int gx,
+                                 cudaStream_t st );
+// this simulation's own grid per batched kernel (what its single launches use)
+void bora_member_grids( int ntiles, int* grid );
+void bora_projection_grids( int ntiles, int* grid );  // the kGridDir, kGridCells and kGridResidual entries
+
 // e += alpha d; r -= alpha q; r.r -> ring slot (alpha = rz / dq, or 0 when slot_rz < 0)
 void bora_launch_pcg_update_noprec( int ntiles, BoraSolverDev s, BoraReduceDev red, int slot_rz, int slot_dq,
                                     int slot_rr_out, cudaStream_t st );

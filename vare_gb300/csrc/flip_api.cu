@@ -8,6 +8,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <vector>
 
@@ -146,6 +147,7 @@ struct bora_flip_sim
     DevBuf vdb_leaf, vdb_mask, vdb_val;  // VDB leaf export: leaf origins + slots, masks, values
     DevBuf mg_mid;         // static image of the coarse levels' cluster kernel (mg_mid.cu), or empty
     bool mg_mid_on = false;
+    bool batching = false; // inside bora_flip_step_batch: hierarchies keep every level shape the batch needs
     BoraLevelDev levels[kMaxLevels] = {};
     int nlevels = 0;
 
@@ -527,7 +529,9 @@ int build_hierarchy( bora_flip_sim* s )
     {
         ex = half_up( ex ); ey = half_up( ey ); ez = half_up( ez );
         BORA_TRYS( add( 0, E, nt * (size_t)E * E * E, 0, 0, 0 ) );
-        if( s->levels[n - 1].ncells <= 512 ) { s->nlevels = n; return BORA_OK; }
+        // a batched step keeps the tiled levels 0-3 and at least one dense level below them
+        // (the shape of its launches), whatever the size
+        if( !s->batching && s->levels[n - 1].ncells <= 512 ) { s->nlevels = n; return BORA_OK; }
     }
     // level 3 has one cell per tile; its extent is the tile grid
     while( true )
@@ -1243,6 +1247,388 @@ int bora_flip_step( bora_flip_handle s, float dt )
     s->stats.steps++;
     s->stats.stage_ms[7] = std::chrono::duration<double, std::milli>( std::chrono::steady_clock::now() - t0 ).count();
     return solve;
+}
+
+// ---- batched steps ---------------------------------------------------------------------
+//
+// bora_flip_step_batch advances several simulations one step each. Their per-simulation
+// stages (tile rebuild and sort, P2G, system and multigrid set-up, velocity update, G2P)
+// run back to back on one stream; the pressure solve - all but a few of a step's launches -
+// runs every kernel once for all of them: simulation k of the batch is row blockIdx.y of
+// each launch, on the grid of its own single launch, reducing into its own ring (the
+// batched kernels in projection.cu, multigrid.cu and mg_mid.cu). Each simulation follows
+// stage_solve's control flow on its own (refinement passes, convergence checks one
+// iteration late, residual replacement), so its launches and arithmetic are the same
+// whether it runs alone or in a batch; a launch row of a simulation that is between passes
+// or finished returns at once.
+
+namespace {
+
+struct BatchMember
+{
+    bora_flip_sim* s = nullptr;
+    int row = 0;    // row of the batched launches
+    int index = 0;  // position in the caller's array
+    enum Phase { kStart, kInner, kRefine, kDone } phase = kStart;
+    double bnorm = 0, rnorm = 0, rmax = 0, dx = 1, target = 0;
+    int total_it = 0, passes = 0, it = 0, max_inner = 1, check = 1;
+    bool converged = false, inner_done = false;
+    int rz_prev = -1, dsel = 0, rz_cur = -1, rr_cur = -1, a_rz = -1, a_dq = -1;
+    int s_b2 = -1, s_bmax = -1, s_n2 = -1, s_mx = -1;
+    struct Check { int it, tick, slot; };
+    Check pend[bora_flip_sim::kChecks];
+    int npend = 0;
+
+    double mirror( int slot ) const { return ( (volatile double*)s->h_mirror )[slot]; }
+    // the check at the top of stage_solve's pass loop
+    void decide()
+    {
+        const bora_flip_params& p = s->prm;
+        const bool norm_ok = rnorm <= p.tolerance * bnorm;
+        const bool max_ok = rmax * dx <= p.div_tolerance;
+        if( bnorm == 0.0 || ( norm_ok && max_ok ) ) { converged = true; phase = kDone; return; }
+        if( passes >= std::max( 1, p.max_refinements ) ) { phase = kDone; return; }
+        target = norm_ok ? 0.1 * rnorm : std::max( p.inner_tolerance * rnorm, 0.25 * p.tolerance * bnorm );
+        phase = kStart;
+    }
+};
+
+struct BatchBuffers
+{
+    DevBuf ms, sl, mid;
+};
+
+int batch_solve( std::vector<BatchMember>& M, cudaStream_t st, BatchBuffers& bb, bora_flip_sim* host_of_events )
+{
+    const int n = (int)M.size();
+    // static per-simulation records: solver vectors, reductions, levels, own grids, and the
+    // coarse cluster kernel's descriptors
+    std::vector<BoraMemberSolve> ms( n );
+    const size_t dbytes = bora_mg_mid_desc_bytes();
+    std::vector<char> mid( dbytes * n );
+    int ctas = 0;
+    size_t smem = 0;
+    int gmax[kGridCount] = {};
+    for( int k = 0; k < n; ++k )
+    {
+        bora_flip_sim* s = M[k].s;
+        BoraMemberSolve& m = ms[k];
+        m.ntiles = s->ntiles;
+        m.nbr = P<int32_t>( s->nbr );
+        m.code = P<uint16_t>( s->code );
+        m.b = P<float>( s->rhs );
+        m.pres = P<float>( s->pres );
+        m.sv = s->solver();
+        m.red = s->reducer();
+        for( int l = 0; l < 4; ++l ) m.L[l] = s->levels[l];
+        m.z3 = s->levels[3].z0;
+        bora_member_grids( s->ntiles, m.grid );
+        for( int q = 0; q < kGridCount; ++q ) gmax[q] = std::max( gmax[q], m.grid[q] );
+        size_t sm = 0;
+        int c = 0;
+        if( !bora_mg_mid_describe( s->g, s->levels, s->nlevels, s->tiles(), s->ntiles, s->mg_mid.p,
+                                   P<uint32_t>( s->counters ) + 5, 16, mid.data() + dbytes * k, &sm, &c ) )
+            return BORA_ERR_INTERNAL;
+        if( ctas && c != ctas ) return BORA_ERR_INTERNAL;
+        ctas = c;
+        smem = std::max( smem, sm );
+    }
+    BORA_TRY( grow( bb.ms, sizeof( BoraMemberSolve ) * n, false, st ) );
+    BORA_TRY( grow( bb.sl, sizeof( BoraMemberSlots ) * n, false, st ) );
+    BORA_TRY( grow( bb.mid, dbytes * n, false, st ) );
+    BORA_TRY( cudaMemcpyAsync( bb.ms.p, ms.data(), sizeof( BoraMemberSolve ) * n, cudaMemcpyHostToDevice, st ) );
+    BORA_TRY( cudaMemcpyAsync( bb.mid.p, mid.data(), dbytes * n, cudaMemcpyHostToDevice, st ) );
+    const BoraMemberSolve* dms = P<BoraMemberSolve>( bb.ms );
+    const BoraMemberSlots* dsl = P<BoraMemberSlots>( bb.sl );
+    std::vector<BoraMemberSlots> sl( n );
+    uint64_t launches = 0;
+    // this launch group's slots; the copy is stream-ordered after every earlier launch that
+    // read the buffer
+    auto upload = [&]() -> int {
+        BORA_TRY( cudaMemcpyAsync( bb.sl.p, sl.data(), sizeof( BoraMemberSlots ) * n, cudaMemcpyHostToDevice, st ) );
+        return BORA_OK;
+    };
+    auto vcycle = [&]() {
+        for( int l = 0; l < 3; ++l ) bora_launch_mg_fused_batch( false, l, dms, dsl, n, gmax[kGridDown8 + l], st );
+        bora_mg_mid_launch_batch( bb.mid.p, dsl, n, ctas, smem, st );
+        for( int l = 2; l >= 0; --l ) bora_launch_mg_fused_batch( true, l, dms, dsl, n, gmax[kGridUp8 + l], st );
+        launches += 7;
+    };
+    // r = b, x = e = d = q = 0; ||b||^2, max|b|
+    for( int k = 0; k < n; ++k )
+    {
+        BatchMember& b = M[k];
+        b.s_b2 = b.s->slot();
+        b.s_bmax = b.s->slot();
+        sl[k] = BoraMemberSlots{};
+        sl[k].active = 1;
+        sl[k].n2 = b.s_b2;
+        sl[k].mx = b.s_bmax;
+        BORA_TRY( cudaMemsetAsync( P<uint32_t>( b.s->counters ) + 5, 0, 4, st ) );
+    }
+    BORA_TRYS( upload() );
+    bora_launch_solve_init_batch( dms, dsl, n, gmax[kGridCells], st );
+    ++launches;
+    BORA_TRYS( check_launch( nullptr ) );
+    BORA_TRY( cudaStreamSynchronize( st ) );
+    for( BatchMember& b : M )
+    {
+        b.dx = b.s->scale[0];
+        b.bnorm = std::sqrt( b.mirror( b.s_b2 ) );
+        b.rnorm = b.bnorm;
+        b.rmax = b.mirror( b.s_bmax );
+        b.max_inner = std::max( 1, b.s->prm.proj_iteration );
+        b.check = std::max( 1, b.s->prm.check_every );
+        b.decide();
+    }
+    int tick = 0;
+    cudaEvent_t* tev = host_of_events->ev_chk;
+    constexpr int kTicks = bora_flip_sim::kChecks;
+    for( ;; )
+    {
+        // passes that start: the first V-cycle z = M^-1 r after r.r
+        bool start = false;
+        for( int k = 0; k < n; ++k )
+        {
+            BatchMember& b = M[k];
+            sl[k] = BoraMemberSlots{};
+            if( b.phase != BatchMember::kStart ) continue;
+            b.rz_cur = b.s->slot();
+            b.rr_cur = b.s->slot();
+            sl[k].active = 1;
+            sl[k].rz_in = -1;
+            sl[k].dq_in = -1;
+            sl[k].rr_out = b.rr_cur;
+            sl[k].rr = b.rr_cur;
+            sl[k].rz = b.rz_cur;
+            b.phase = BatchMember::kInner;
+            b.it = 0;
+            b.npend = 0;
+            b.a_rz = b.a_dq = -1;
+            b.inner_done = false;
+            b.s->stats.mg_vcycle_launches = 7;
+            start = true;
+        }
+        if( start )
+        {
+            BORA_TRYS( upload() );
+            bora_launch_pcg_update_noprec_batch( dms, dsl, n, gmax[kGridUpd], st );
+            ++launches;
+            vcycle();
+        }
+        // one inner iteration for every simulation inside a pass
+        bool inner = false;
+        for( int k = 0; k < n; ++k )
+        {
+            BatchMember& b = M[k];
+            sl[k] = BoraMemberSlots{};
+            if( b.phase != BatchMember::kInner || b.inner_done || b.it >= b.max_inner ) continue;
+            const int s_dq = b.s->slot();
+            const int rz_new = b.s->slot(), rr_new = b.s->slot();
+            BoraMemberSlots& q = sl[k];
+            q.active = 1;
+            q.dsel = b.dsel;
+            q.rz_new = b.rz_cur; q.rz_old = b.rz_prev; q.dq = s_dq; q.a_rz = b.a_rz; q.a_dq = b.a_dq;
+            q.rz_in = b.rz_cur; q.dq_in = s_dq; q.rr_out = rr_new;
+            q.rr = rr_new; q.rz = rz_new;
+            b.dsel ^= 1;
+            b.a_rz = b.rz_cur;
+            b.a_dq = s_dq;
+            b.rz_prev = b.rz_cur;
+            b.rz_cur = rz_new;
+            b.rr_cur = rr_new;
+            ++b.it;
+            inner = true;
+        }
+        if( inner )
+        {
+            BORA_TRYS( upload() );
+            bora_launch_pcg_direction_batch( dms, dsl, n, gmax[kGridDir], st );
+            bora_launch_pcg_update_noprec_batch( dms, dsl, n, gmax[kGridUpd], st );
+            launches += 2;
+            vcycle();
+            BORA_TRYS( check_launch( nullptr ) );
+            BORA_TRY( cudaEventRecord( tev[tick % kTicks], st ) );
+            for( int k = 0; k < n; ++k )
+            {
+                if( !sl[k].active ) continue;
+                BatchMember& b = M[k];
+                if( b.it % b.check == 0 ) b.pend[b.npend++] = BatchMember::Check{ b.it, tick, b.rr_cur };
+                // the convergence check of stage_solve: iteration i is read once i + 1 is queued
+                while( b.npend > 0 && ( b.it - b.pend[0].it >= 1 || b.npend == kTicks || b.it >= b.max_inner ) )
+                {
+                    BORA_TRY( cudaEventSynchronize( tev[b.pend[0].tick % kTicks] ) );
+                    const double rr = b.mirror( b.pend[0].slot );
+                    for( int q = 1; q < b.npend; ++q ) b.pend[q - 1] = b.pend[q];
+                    --b.npend;
+                    if( !( rr > 0.0 ) || std::sqrt( rr ) <= b.target ) { b.inner_done = true; break; }
+                }
+            }
+            ++tick;
+        }
+        // passes that end: refinement (x += e; r = b - A x in double-float arithmetic)
+        bool refine = false;
+        for( int k = 0; k < n; ++k )
+        {
+            BatchMember& b = M[k];
+            sl[k] = BoraMemberSlots{};
+            if( b.phase != BatchMember::kInner || !( b.inner_done || b.it >= b.max_inner ) ) continue;
+            b.s_n2 = b.s->slot();
+            b.s_mx = b.s->slot();
+            sl[k].active = 1;
+            sl[k].dsel = b.dsel;
+            sl[k].a_rz = b.a_rz;
+            sl[k].a_dq = b.a_dq;
+            sl[k].n2 = b.s_n2;
+            sl[k].mx = b.s_mx;
+            b.phase = BatchMember::kRefine;
+            refine = true;
+        }
+        if( refine )
+        {
+            BORA_TRYS( upload() );
+            bora_launch_refine_accumulate_batch( dms, dsl, n, gmax[kGridCells], st );
+            bora_launch_refine_residual_batch( dms, dsl, n, gmax[kGridResidual], st );
+            launches += 2;
+            BORA_TRYS( check_launch( nullptr ) );
+            BORA_TRY( cudaStreamSynchronize( st ) );
+            for( BatchMember& b : M )
+            {
+                if( b.phase != BatchMember::kRefine ) continue;
+                b.total_it += b.it;
+                ++b.passes;
+                b.rnorm = std::sqrt( b.mirror( b.s_n2 ) );
+                b.rmax = b.mirror( b.s_mx );
+                if( !std::isfinite( b.rnorm ) ) { b.phase = BatchMember::kDone; continue; }
+                // continue the recurrence only while the refined and recursive residuals agree
+                const double rr_rec = b.mirror( b.rr_cur );
+                const double rec = rr_rec > 0.0 ? std::sqrt( rr_rec ) : 0.0;
+                if( !( rec > 0.0 ) || b.rnorm > 1.5 * rec ) b.rz_prev = -1;
+                b.decide();
+            }
+        }
+        bool any = false;
+        for( const BatchMember& b : M ) any = any || b.phase != BatchMember::kDone;
+        if( !any ) break;
+    }
+    bora_launch_write_pressure_batch( dms, n, gmax[kGridCells], st );
+    ++launches;
+    BORA_TRYS( check_launch( nullptr ) );
+    int status = BORA_OK;
+    for( BatchMember& b : M )
+    {
+        bora_flip_sim* s = b.s;
+        s->stats.kernel_launches += launches;
+        BORA_TRYS( read_counters( s, 5, 2 ) );
+        if( s->h_cnt[5] != 0 ) return BORA_ERR_INTERNAL;
+        s->stats.fluid_cells = (int32_t)s->h_cnt[6];
+        s->stats.solver_iterations = b.total_it;
+        s->stats.refinements = b.passes;
+        s->stats.residual_rel = b.bnorm > 0.0 ? b.rnorm / b.bnorm : 0.0;
+        s->stats.residual_max = b.rmax;
+        s->stats.residual_max_dx = b.rmax * b.dx;
+        s->stats.converged = b.converged ? 1 : 0;
+        s->last_status = b.converged ? BORA_OK : BORA_WARN_NOT_CONVERGED;
+        if( !b.converged ) status = BORA_WARN_NOT_CONVERGED;
+    }
+    return status;
+}
+
+}  // namespace
+
+int bora_flip_step_batch( bora_flip_handle* hs, int n, float dt, int* status )
+{
+    if( n < 0 || ( n > 0 && ( !hs || !status ) ) ) return BORA_ERR_INVALID_ARG;
+    if( n == 0 ) return BORA_OK;
+    int dev = -1;
+    for( int k = 0; k < n; ++k )
+    {
+        if( !hs[k] ) return BORA_ERR_INVALID_ARG;
+        for( int q = 0; q < k; ++q )
+            if( hs[q] == hs[k] ) return BORA_ERR_INVALID_ARG;
+        if( dev >= 0 && hs[k]->device != dev ) return BORA_ERR_INVALID_ARG;
+        dev = hs[k]->device;
+        status[k] = BORA_OK;
+    }
+    // the batch runs on the first simulation's stream; the others lend theirs back at the end
+    bora_flip_sim* h0 = hs[0];
+    cudaStream_t st = h0->st;
+    std::vector<cudaStream_t> own( n );
+    for( int k = 0; k < n; ++k )
+    {
+        own[k] = hs[k]->st;
+        if( k ) BORA_TRY( cudaStreamSynchronize( own[k] ) );
+    }
+    for( int k = 0; k < n; ++k ) hs[k]->st = st;
+    struct Restore
+    {
+        bora_flip_handle* hs;
+        std::vector<cudaStream_t>& own;
+        ~Restore()
+        {
+            for( size_t k = 0; k < own.size(); ++k ) { hs[k]->st = own[k]; hs[k]->batching = false; }
+        }
+    } restore{ hs, own };
+    const auto t0 = std::chrono::steady_clock::now();
+    BORA_TRY( cudaEventRecord( h0->ev_step[0], st ) );
+    // per-simulation stages before the solve; simulations the batched solve cannot take (the
+    // plain form, no tiles, a hierarchy the coarse cluster kernel does not fit) step on their
+    // own afterwards
+    std::vector<BatchMember> M;
+    std::vector<int> solo;
+    for( int k = 0; k < n; ++k )
+    {
+        bora_flip_sim* s = hs[k];
+        if( s->np == 0 ) continue;  // FLIPMethod.cu:179
+        if( s->prm.solver != BORA_SOLVER_MIXED ) { solo.push_back( k ); continue; }
+        s->batching = true;
+        if( !s->sorted ) status[k] = stage_rebuild( s );
+        if( status[k] >= 0 ) status[k] = stage_p2g( s );
+        if( status[k] >= 0 ) status[k] = stage_build_system( s );
+        if( status[k] < 0 ) continue;
+        if( s->ntiles <= 0 || !s->mg_mid_on ) { s->batching = false; solo.push_back( k ); continue; }
+        BatchMember b;
+        b.s = s;
+        b.row = (int)M.size();
+        b.index = k;
+        M.push_back( b );
+    }
+    if( !M.empty() )
+    {
+        static BatchBuffers bb_cache[64];  // per device: the batch's argument arrays
+        static std::mutex bb_mu;
+        std::lock_guard<std::mutex> lk( bb_mu );
+        BatchBuffers& bb = bb_cache[dev >= 0 && dev < 64 ? dev : 0];
+        const int solve = batch_solve( M, st, bb, h0 );
+        if( solve < 0 ) return solve;
+        for( BatchMember& b : M )
+        {
+            bora_flip_sim* s = b.s;
+            int stt = stage_update_velocity( s );
+            if( stt >= 0 ) stt = stage_update_particles( s, dt );
+            status[b.index] = stt < 0 ? stt : s->last_status;
+        }
+    }
+    BORA_TRY( cudaEventRecord( h0->ev_step[1], st ) );
+    BORA_TRY( cudaEventSynchronize( h0->ev_step[1] ) );
+    float gms = 0.f;
+    cudaEventElapsedTime( &gms, h0->ev_step[0], h0->ev_step[1] );
+    const double wall = std::chrono::duration<double, std::milli>( std::chrono::steady_clock::now() - t0 ).count();
+    for( BatchMember& b : M )
+    {
+        b.s->stats.gpu_ms = gms;
+        b.s->stats.steps++;
+        b.s->stats.stage_ms[7] = wall;
+        b.s->batching = false;
+    }
+    for( int k : solo )
+    {
+        hs[k]->st = own[k];
+        hs[k]->batching = false;
+        status[k] = bora_flip_step( hs[k], dt );
+        hs[k]->st = st;
+    }
+    return BORA_OK;
 }
 
 int bora_flip_frame( bora_flip_handle s )

@@ -33,6 +33,7 @@
 // bits select the fluid neighbours).
 #include <algorithm>
 #include <cooperative_groups.h>
+#include <cstring>
 
 #include <cuda_fp16.h>
 
@@ -79,6 +80,7 @@ struct MidDesc
     int ctas;
     int static_bytes;    // bytes of a CTA's static block (a multiple of 16)
     char* image;         // ctas static blocks, built by k_mg_mid_image
+    uint32_t* err;       // inconsistent stencil codes are recorded here
 };
 
 extern __shared__ __align__( 16 ) char g_mid_smem[];
@@ -311,9 +313,10 @@ __global__ void __launch_bounds__( kMidThreads ) k_mg_mid_image( const __grid_co
     for( int t = 0; t < d.n; ++t ) m.stage( t, blk );
 }
 
-__global__ void __launch_bounds__( kMidThreads, 1 ) k_mg_mid( const __grid_constant__ MidDesc d, uint32_t* err )
+__device__ __forceinline__ void mg_mid_body( const MidDesc& d )
 {
     __shared__ float wA[16], wB[16], wC[16];
+    uint32_t* err = d.err;
     Mid m{ d, cg::this_cluster(), 0u };
     m.me = m.cl.block_rank();
     const int tid = threadIdx.x;
@@ -433,6 +436,17 @@ __global__ void __launch_bounds__( kMidThreads, 1 ) k_mg_mid( const __grid_const
     m.barrier();  // no CTA leaves while another may still read its shared memory
 }
 
+__global__ void __launch_bounds__( kMidThreads, 1 ) k_mg_mid( const __grid_constant__ MidDesc d ) { mg_mid_body( d ); }
+
+// Batched: one cluster per simulation of the batch (all clusters of the same size).
+__global__ void __launch_bounds__( kMidThreads, 1 ) k_mg_mid_batch( const MidDesc* __restrict__ descs,
+                                                                    const BoraMemberSlots* __restrict__ sl )
+{
+    const unsigned c = blockIdx.x / cg::this_cluster().num_blocks();
+    if( !sl[c].active ) return;  // every CTA of the cluster returns: no barrier is pending
+    mg_mid_body( descs[c] );
+}
+
 // Cluster size: 16 CTAs where the device co-schedules such a cluster of this kernel with
 // the largest shared memory it may ask for, else 8; 0 when neither fits (the caller then
 // runs these levels itself). Queried once per device.
@@ -442,6 +456,8 @@ int mid_cluster_size()
     const int v = size.get( [] {
         cudaFuncSetAttribute( k_mg_mid, cudaFuncAttributeNonPortableClusterSizeAllowed, 1 );
         cudaFuncSetAttribute( k_mg_mid, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMidSmemMax );
+        cudaFuncSetAttribute( k_mg_mid_batch, cudaFuncAttributeNonPortableClusterSizeAllowed, 1 );
+        cudaFuncSetAttribute( k_mg_mid_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMidSmemMax );
         cudaGetLastError();
         auto fits = []( int ctas ) {
             cudaLaunchConfig_t cfg{};
@@ -561,6 +577,7 @@ int bora_mg_mid_vcycle( const BoraGridDev& g, const BoraLevelDev* levels, int nl
     if( !image || !mid_describe( g, levels, nlevels, t, ntiles, sweeps, d, smem ) ) return 0;
     if( !launch ) return 1;
     d.image = static_cast<char*>( const_cast<void*>( image ) );
+    d.err = err;
     cudaLaunchConfig_t cfg{};
     cfg.gridDim = dim3( d.ctas );
     cfg.blockDim = dim3( kMidThreads );
@@ -575,6 +592,43 @@ int bora_mg_mid_vcycle( const BoraGridDev& g, const BoraLevelDev* levels, int nl
     attr[1].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 2;
-    cudaLaunchKernelEx( &cfg, k_mg_mid, d, err );
+    cudaLaunchKernelEx( &cfg, k_mg_mid, d );
     return 1;
+}
+
+size_t bora_mg_mid_desc_bytes() { return sizeof( MidDesc ); }
+
+int bora_mg_mid_describe( const BoraGridDev& g, const BoraLevelDev* levels, int nlevels, BoraTilesDev t, int ntiles,
+                          const void* image, uint32_t* err, int sweeps, void* desc, size_t* smem, int* ctas )
+{
+    MidDesc d;
+    size_t sm = 0;
+    if( !image || !mid_describe( g, levels, nlevels, t, ntiles, sweeps, d, sm ) ) return 0;
+    d.image = static_cast<char*>( const_cast<void*>( image ) );
+    d.err = err;
+    std::memcpy( desc, &d, sizeof( d ) );
+    *smem = sm;
+    *ctas = d.ctas;
+    return 1;
+}
+
+void bora_mg_mid_launch_batch( const void* descs, const BoraMemberSlots* slots, int n, int ctas, size_t smem,
+                               cudaStream_t st )
+{
+    if( n <= 0 ) return;
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3( ctas * n );
+    cfg.blockDim = dim3( kMidThreads );
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[2];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = ctas;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[1].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 2;
+    cudaLaunchKernelEx( &cfg, k_mg_mid_batch, static_cast<const MidDesc*>( descs ), slots );
 }

@@ -836,10 +836,9 @@ struct RowZ
 };
 
 template <int E, bool L0>
-__global__ void __launch_bounds__( TileRegion<E>::NT, TileRegion<E>::MINB ) k_mg_down_fused( BoraLevelDev F, BoraLevelDev C,
-                                                                           BoraTilesDev t, int ntiles,
-                                                                           const float* __restrict__ r0, int slot_rr,
-                                                                           const double* __restrict__ ring )
+__device__ __forceinline__ void mg_down_fused_body( const BoraLevelDev& F, const BoraLevelDev& C, const BoraTilesDev& t,
+                                                    int ntiles, const float* __restrict__ r0, int slot_rr,
+                                                    const double* __restrict__ ring, int bid, int G )
 {
     using TR = TileRegion<E>;
     constexpr int R = TR::R, Q = TR::Q, H = TR::H, NT = TR::NT, E3 = TR::E3;
@@ -851,13 +850,13 @@ __global__ void __launch_bounds__( TileRegion<E>::NT, TileRegion<E>::MINB ) k_mg
     __shared__ int32_t nbb[2][27];
     __shared__ float wd[32];
     __shared__ float s_scale;
-    const int tid = threadIdx.x, G = gridDim.x;
+    const int tid = threadIdx.x;
     bora_pdl_trigger();
     init_wd( wd );
     if( tid < 27 )
     {
-        nbb[0][tid] = nbr_entry( t, blockIdx.x, ntiles, tid );
-        nbb[1][tid] = nbr_entry( t, blockIdx.x + G, ntiles, tid );
+        nbb[0][tid] = nbr_entry( t, bid, ntiles, tid );
+        nbb[1][tid] = nbr_entry( t, bid + G, ntiles, tid );
     }
     uint32_t am[TR::IA];
     int bh[TR::IB], ch[TR::IC], ch2[TR::IC];
@@ -902,7 +901,7 @@ __global__ void __launch_bounds__( TileRegion<E>::NT, TileRegion<E>::MINB ) k_mg
     };
     issue( nbb[0] );
     int n = 0;
-    for( int s = blockIdx.x; s < ntiles; s += G, ++n )
+    for( int s = bid; s < ntiles; s += G, ++n )
     {
         // stage tile s; the first sweep from zero is pointwise z1 = w r'/d
         if constexpr( kRows )
@@ -981,11 +980,33 @@ __global__ void __launch_bounds__( TileRegion<E>::NT, TileRegion<E>::MINB ) k_mg
 }
 
 template <int E, bool L0>
-__global__ void __launch_bounds__( TileRegion<E>::NT, TileRegion<E>::MINB ) k_mg_up_fused( BoraLevelDev F, const __half* __restrict__ ec,
-                                                                         BoraTilesDev t, int ntiles,
-                                                                         const float* __restrict__ r0, int slot_rr,
-                                                                         BoraReduceDev red, float* __restrict__ zout,
-                                                                         int slot_rz )
+__global__ void __launch_bounds__( TileRegion<E>::NT, TileRegion<E>::MINB ) k_mg_down_fused( BoraLevelDev F, BoraLevelDev C,
+                                                                           BoraTilesDev t, int ntiles,
+                                                                           const float* __restrict__ r0, int slot_rr,
+                                                                           const double* __restrict__ ring )
+{
+    mg_down_fused_body<E, L0>( F, C, t, ntiles, r0, slot_rr, ring, blockIdx.x, gridDim.x );
+}
+
+// Batched: simulation blockIdx.y, level l = 0, 1, 2 (E = 8, 4, 2) of its hierarchy.
+template <int E, bool L0>
+__global__ void __launch_bounds__( TileRegion<E>::NT, TileRegion<E>::MINB )
+    k_mg_down_fused_batch( const BoraMemberSolve* __restrict__ ms, const BoraMemberSlots* __restrict__ sl )
+{
+    constexpr int l = E == 8 ? 0 : ( E == 4 ? 1 : 2 );
+    const BoraMemberSolve& m = ms[blockIdx.y];
+    const BoraMemberSlots& q = sl[blockIdx.y];
+    const int G = m.grid[kGridDown8 + l];
+    if( !q.active || (int)blockIdx.x >= G ) return;
+    mg_down_fused_body<E, L0>( m.L[l], m.L[l + 1], BoraTilesDev{ nullptr, nullptr, m.nbr }, m.ntiles,
+                               L0 ? m.sv.r : nullptr, q.rr, m.red.ring, blockIdx.x, G );
+}
+
+template <int E, bool L0>
+__device__ __forceinline__ void mg_up_fused_body( const BoraLevelDev& F, const __half* __restrict__ ec, const BoraTilesDev& t,
+                                                  int ntiles, const float* __restrict__ r0, int slot_rr,
+                                                  const BoraReduceDev& red, float* __restrict__ zout, int slot_rz, int bid,
+                                                  int G )
 {
     using TR = TileRegion<E>;
     constexpr int R = TR::R, Q = TR::Q, H = TR::H, NT = TR::NT, E3 = TR::E3;
@@ -997,13 +1018,13 @@ __global__ void __launch_bounds__( TileRegion<E>::NT, TileRegion<E>::MINB ) k_mg
     __shared__ int32_t nbb[2][27];
     __shared__ float wd[32];
     __shared__ float s_scale;
-    const int tid = threadIdx.x, G = gridDim.x;
+    const int tid = threadIdx.x;
     bora_pdl_trigger();
     init_wd( wd );
     if( tid < 27 )
     {
-        nbb[0][tid] = nbr_entry( t, blockIdx.x, ntiles, tid );
-        nbb[1][tid] = nbr_entry( t, blockIdx.x + G, ntiles, tid );
+        nbb[0][tid] = nbr_entry( t, bid, ntiles, tid );
+        nbb[1][tid] = nbr_entry( t, bid + G, ntiles, tid );
     }
     uint32_t am[TR::IA];
     int bh[TR::IB], ch[TR::IC], ch2[TR::IC];
@@ -1065,7 +1086,7 @@ __global__ void __launch_bounds__( TileRegion<E>::NT, TileRegion<E>::MINB ) k_mg
     issue( nbb[0] );
     DF rz{ 0.f, 0.f };
     int n = 0;
-    for( int s = blockIdx.x; s < ntiles; s += G, ++n )
+    for( int s = bid; s < ntiles; s += G, ++n )
     {
         float trz = 0.f;  // this thread's r.z over its cells of the tile
         if constexpr( kRows )
@@ -1138,14 +1159,41 @@ __global__ void __launch_bounds__( TileRegion<E>::NT, TileRegion<E>::MINB ) k_mg
         if( tid < 27 ) nbb[n & 1][tid] = nb2;
         __syncthreads();  // the next tile's staging overwrites the shared arrays
     }
-    if( L0 ) reduce2_publish_warp( df_warp_sum( rz ), 0.0, 0, red, slot_rz, -1 );
+    if( L0 ) reduce2_publish_warp( df_warp_sum( rz ), 0.0, 0, red, slot_rz, -1, bid, G );
+}
+
+template <int E, bool L0>
+__global__ void __launch_bounds__( TileRegion<E>::NT, TileRegion<E>::MINB ) k_mg_up_fused( BoraLevelDev F, const __half* __restrict__ ec,
+                                                                         BoraTilesDev t, int ntiles,
+                                                                         const float* __restrict__ r0, int slot_rr,
+                                                                         BoraReduceDev red, float* __restrict__ zout,
+                                                                         int slot_rz )
+{
+    mg_up_fused_body<E, L0>( F, ec, t, ntiles, r0, slot_rr, red, zout, slot_rz, blockIdx.x, gridDim.x );
+}
+
+// Batched: simulation blockIdx.y; the coarser level's correction is its z1 after a fused
+// up kernel (levels 1 and 2 below levels 0 and 1), and level 3's z0 below level 2 (left
+// there by the coarse cluster kernel).
+template <int E, bool L0>
+__global__ void __launch_bounds__( TileRegion<E>::NT, TileRegion<E>::MINB )
+    k_mg_up_fused_batch( const BoraMemberSolve* __restrict__ ms, const BoraMemberSlots* __restrict__ sl )
+{
+    constexpr int l = E == 8 ? 0 : ( E == 4 ? 1 : 2 );
+    const BoraMemberSolve& m = ms[blockIdx.y];
+    const BoraMemberSlots& q = sl[blockIdx.y];
+    const int G = m.grid[kGridUp8 + l];
+    if( !q.active || (int)blockIdx.x >= G ) return;
+    const __half* ec = l < 2 ? m.L[l + 1].z1 : m.z3;
+    mg_up_fused_body<E, L0>( m.L[l], ec, BoraTilesDev{ nullptr, nullptr, m.nbr }, m.ntiles, L0 ? m.sv.r : nullptr, q.rr,
+                             m.red, L0 ? m.sv.z : nullptr, q.rz, blockIdx.x, G );
 }
 
 
 // PCG update without a preconditioner sweep: r -= alpha q; r.r (e += alpha d is applied by
 // the next direction kernel or the refinement step).
-__global__ void __launch_bounds__( 256 ) k_pcg_update_noprec( size_t ncells, BoraSolverDev sv, BoraReduceDev red,
-                                                              int slot_rz, int slot_dq, int slot_rr_out )
+__device__ __forceinline__ void pcg_update_noprec_body( size_t ncells, const BoraSolverDev& sv, const BoraReduceDev& red,
+                                                        int slot_rz, int slot_dq, int slot_rr_out, unsigned bid, unsigned G )
 {
     __shared__ float s_alpha;
     bora_pdl_trigger();
@@ -1157,7 +1205,7 @@ __global__ void __launch_bounds__( 256 ) k_pcg_update_noprec( size_t ncells, Bor
     const size_t n4 = ncells / 4;
     float4* __restrict__ r4 = reinterpret_cast<float4*>( sv.r );
     const float4* __restrict__ q4 = reinterpret_cast<const float4*>( sv.q );
-    for( size_t v = blockIdx.x * (size_t)blockDim.x + threadIdx.x; v < n4; v += (size_t)gridDim.x * blockDim.x )
+    for( size_t v = bid * (size_t)blockDim.x + threadIdx.x; v < n4; v += (size_t)G * blockDim.x )
     {
         float4 r = r4[v];
         const float4 q = q4[v];
@@ -1165,7 +1213,23 @@ __global__ void __launch_bounds__( 256 ) k_pcg_update_noprec( size_t ncells, Bor
         r4[v] = r;
         rr = df_add_f( rr, dot4( r, r ) );
     }
-    reduce2_publish_warp( df_warp_sum( rr ), 0.0, 0, red, slot_rr_out, -1 );
+    reduce2_publish_warp( df_warp_sum( rr ), 0.0, 0, red, slot_rr_out, -1, bid, G );
+}
+
+__global__ void __launch_bounds__( 256 ) k_pcg_update_noprec( size_t ncells, BoraSolverDev sv, BoraReduceDev red,
+                                                              int slot_rz, int slot_dq, int slot_rr_out )
+{
+    pcg_update_noprec_body( ncells, sv, red, slot_rz, slot_dq, slot_rr_out, blockIdx.x, gridDim.x );
+}
+
+__global__ void __launch_bounds__( 256 ) k_pcg_update_noprec_batch( const BoraMemberSolve* __restrict__ ms,
+                                                                    const BoraMemberSlots* __restrict__ sl )
+{
+    const BoraMemberSolve& m = ms[blockIdx.y];
+    const BoraMemberSlots& q = sl[blockIdx.y];
+    const unsigned G = (unsigned)m.grid[kGridUpd];
+    if( !q.active || blockIdx.x >= G ) return;
+    pcg_update_noprec_body( (size_t)m.ntiles * 512, m.sv, m.red, q.rz_in, q.dq_in, q.rr_out, blockIdx.x, G );
 }
 
 int sm_count()
@@ -1418,6 +1482,44 @@ void bora_mg_vcycle( const BoraGridDev& g, const BoraLevelDev* levels, int nleve
             k_mg_smooth_last<<<blocks_for( F.ncells ), 256, 0, st>>>( nav, F, r0, slot_rr, red, l == 0 ? z : nullptr,
                                                                       slot_rz );
         } );
+    }
+}
+
+void bora_member_grids( int ntiles, int* grid )
+{
+    bora_projection_grids( ntiles, grid );
+    grid[kGridUpd] = blocks_for( (size_t)std::max( ntiles, 0 ) * 512 / 4 );
+    static BoraPerDevice d8, d4, d2, u8, u4, u2;
+    grid[kGridDown8] = fused_grid( k_mg_down_fused<8, true>, TileRegion<8>::NT, ntiles, d8 );
+    grid[kGridDown4] = fused_grid( k_mg_down_fused<4, false>, TileRegion<4>::NT, ntiles, d4 );
+    grid[kGridDown2] = fused_grid( k_mg_down_fused<2, false>, TileRegion<2>::NT, ntiles, d2 );
+    grid[kGridUp8] = std::min( fused_grid( k_mg_up_fused<8, true>, TileRegion<8>::NT, ntiles, u8 ), kBoraMaxReduceBlocks );
+    grid[kGridUp4] = fused_grid( k_mg_up_fused<4, false>, TileRegion<4>::NT, ntiles, u4 );
+    grid[kGridUp2] = fused_grid( k_mg_up_fused<2, false>, TileRegion<2>::NT, ntiles, u2 );
+}
+
+void bora_launch_pcg_update_noprec_batch( const BoraMemberSolve* ms, const BoraMemberSlots* sl, int n, int gx,
+                                          cudaStream_t st )
+{
+    if( n > 0 && gx > 0 ) bora_launch_pdl( k_pcg_update_noprec_batch, dim3( gx, n ), dim3( 256 ), 0, st, ms, sl );
+}
+
+void bora_launch_mg_fused_batch( bool up, int l, const BoraMemberSolve* ms, const BoraMemberSlots* sl, int n, int gx,
+                                 cudaStream_t st )
+{
+    if( n <= 0 || gx <= 0 ) return;
+    const dim3 grid( gx, n );
+    if( !up )
+    {
+        if( l == 0 ) bora_launch_pdl( k_mg_down_fused_batch<8, true>, grid, dim3( TileRegion<8>::NT ), 0, st, ms, sl );
+        else if( l == 1 ) bora_launch_pdl( k_mg_down_fused_batch<4, false>, grid, dim3( TileRegion<4>::NT ), 0, st, ms, sl );
+        else bora_launch_pdl( k_mg_down_fused_batch<2, false>, grid, dim3( TileRegion<2>::NT ), 0, st, ms, sl );
+    }
+    else
+    {
+        if( l == 0 ) bora_launch_pdl( k_mg_up_fused_batch<8, true>, grid, dim3( TileRegion<8>::NT ), 0, st, ms, sl );
+        else if( l == 1 ) bora_launch_pdl( k_mg_up_fused_batch<4, false>, grid, dim3( TileRegion<4>::NT ), 0, st, ms, sl );
+        else bora_launch_pdl( k_mg_up_fused_batch<2, false>, grid, dim3( TileRegion<2>::NT ), 0, st, ms, sl );
     }
 }
 

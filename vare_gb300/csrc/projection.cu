@@ -468,11 +468,10 @@ __device__ inline size_t face_nbr( const int32_t* __restrict__ nbr, size_t cell,
 // sum.
 constexpr int kDirWarps = 4;
 
-__global__ void __launch_bounds__( 32 * kDirWarps ) k_pcg_direction( int ntiles, const int32_t* __restrict__ nbr,
-                                                                    const uint16_t* __restrict__ code, BoraSolverDev sv,
-                                                                    int dsel_in, BoraReduceDev red, int slot_rz_new,
-                                                                    int slot_rz_old, int slot_dq_out, int slot_a_rz,
-                                                                    int slot_a_dq )
+__device__ __forceinline__ void pcg_direction_body( int ntiles, const int32_t* __restrict__ nbr,
+                                                    const uint16_t* __restrict__ code, const BoraSolverDev& sv, int dsel_in,
+                                                    const BoraReduceDev& red, int slot_rz_new, int slot_rz_old,
+                                                    int slot_dq_out, int slot_a_rz, int slot_a_dq, unsigned bid, unsigned G )
 {
     __shared__ float s_beta, s_alpha;
     bora_pdl_trigger();
@@ -500,7 +499,7 @@ __global__ void __launch_bounds__( 32 * kDirWarps ) k_pcg_direction( int ntiles,
     };
     auto halo1 = [&]( int t, int c ) { return t < 0 ? 0.f : fmaf( beta, dold[(size_t)t * 512 + c], sv.z[(size_t)t * 512 + c] ); };
     DF pdq{ 0.f, 0.f };
-    for( int s = blockIdx.x * kDirWarps + ( threadIdx.x >> 5 ); s < ntiles; s += gridDim.x * kDirWarps )
+    for( int s = (int)bid * kDirWarps + ( threadIdx.x >> 5 ); s < ntiles; s += (int)G * kDirWarps )
     {
         const int32_t* __restrict__ nb = nbr + (size_t)s * 27;  // tile tables: not written by the solver chain
         const int smx = nb[bora_dir( -1, 0, 0 )], spx = nb[bora_dir( 1, 0, 0 )];
@@ -591,16 +590,39 @@ __global__ void __launch_bounds__( 32 * kDirWarps ) k_pcg_direction( int ntiles,
 #pragma unroll
         for( int i = 0; i < 8; ++i ) pdq = df_add_f( pdq, tdq[i] );
     }
-    reduce2_publish_warp( df_warp_sum( pdq ), 0.0, 0, red, slot_dq_out, -1 );
+    reduce2_publish_warp( df_warp_sum( pdq ), 0.0, 0, red, slot_dq_out, -1, bid, G );
+}
+
+__global__ void __launch_bounds__( 32 * kDirWarps ) k_pcg_direction( int ntiles, const int32_t* __restrict__ nbr,
+                                                                    const uint16_t* __restrict__ code, BoraSolverDev sv,
+                                                                    int dsel_in, BoraReduceDev red, int slot_rz_new,
+                                                                    int slot_rz_old, int slot_dq_out, int slot_a_rz,
+                                                                    int slot_a_dq )
+{
+    pcg_direction_body( ntiles, nbr, code, sv, dsel_in, red, slot_rz_new, slot_rz_old, slot_dq_out, slot_a_rz, slot_a_dq,
+                        blockIdx.x, gridDim.x );
+}
+
+// Batched: simulation blockIdx.y of the batch, on its own grid of m.grid[kGridDir] blocks.
+__global__ void __launch_bounds__( 32 * kDirWarps ) k_pcg_direction_batch( const BoraMemberSolve* __restrict__ ms,
+                                                                          const BoraMemberSlots* __restrict__ sl )
+{
+    const BoraMemberSolve& m = ms[blockIdx.y];
+    const BoraMemberSlots& q = sl[blockIdx.y];
+    const unsigned G = (unsigned)m.grid[kGridDir];
+    if( !q.active || blockIdx.x >= G ) return;
+    pcg_direction_body( m.ntiles, m.nbr, m.code, m.sv, q.dsel, m.red, q.rz_new, q.rz_old, q.dq, q.a_rz, q.a_dq,
+                        blockIdx.x, G );
 }
 
 // ---------------------------------------------------------------------------------
-__global__ void k_solve_init( size_t ncells, const float* __restrict__ b, BoraSolverDev sv, BoraReduceDev red,
-                              int slot_norm2, int slot_max )
+__device__ __forceinline__ void solve_init_body( size_t ncells, const float* __restrict__ b, const BoraSolverDev& sv,
+                                                 const BoraReduceDev& red, int slot_norm2, int slot_max, unsigned bid,
+                                                 unsigned G )
 {
     DF n2{ 0.f, 0.f };
     float mx = 0.f;
-    for( size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < ncells; i += (size_t)gridDim.x * blockDim.x )
+    for( size_t i = bid * (size_t)blockDim.x + threadIdx.x; i < ncells; i += (size_t)G * blockDim.x )
     {
         const float bv = b[i];
         sv.r[i] = bv;
@@ -612,20 +634,36 @@ __global__ void k_solve_init( size_t ncells, const float* __restrict__ b, BoraSo
         n2 = df_add( n2, df_prod( bv, bv ) );
         mx = fmaxf( mx, fabsf( bv ) );
     }
-    reduce2_publish_dfmax( n2, mx, red, slot_norm2, slot_max );
+    reduce2_publish_dfmax( n2, mx, red, slot_norm2, slot_max, bid, G );
+}
+
+__global__ void k_solve_init( size_t ncells, const float* __restrict__ b, BoraSolverDev sv, BoraReduceDev red,
+                              int slot_norm2, int slot_max )
+{
+    solve_init_body( ncells, b, sv, red, slot_norm2, slot_max, blockIdx.x, gridDim.x );
+}
+
+__global__ void k_solve_init_batch( const BoraMemberSolve* __restrict__ ms, const BoraMemberSlots* __restrict__ sl )
+{
+    const BoraMemberSolve& m = ms[blockIdx.y];
+    const BoraMemberSlots& q = sl[blockIdx.y];
+    const unsigned G = (unsigned)m.grid[kGridCells];
+    if( !q.active || blockIdx.x >= G ) return;
+    solve_init_body( (size_t)m.ntiles * 512, m.b, m.sv, m.red, q.n2, q.mx, blockIdx.x, G );
 }
 
 // x += e (+ the last update's pending alpha d), then clear e and q; the direction d is kept
 // (the next refinement pass continues the recurrence from it).
-__global__ void k_refine_accumulate( size_t ncells, const uint16_t* __restrict__ code, BoraSolverDev sv, int dsel,
-                                     const double* __restrict__ ring, int slot_a_rz, int slot_a_dq )
+__device__ __forceinline__ void refine_accumulate_body( size_t ncells, const uint16_t* __restrict__ code,
+                                                        const BoraSolverDev& sv, int dsel, const double* __restrict__ ring,
+                                                        int slot_a_rz, int slot_a_dq, unsigned bid, unsigned G )
 {
     __shared__ float s_alpha;
     if( threadIdx.x == 0 ) s_alpha = slot_a_rz < 0 ? 0.f : (float)( ring[slot_a_rz] / ring[slot_a_dq] );
     __syncthreads();
     const float alpha = s_alpha;
     const float* __restrict__ d = dsel ? sv.d[1] : sv.d[0];
-    for( size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < ncells; i += (size_t)gridDim.x * blockDim.x )
+    for( size_t i = bid * (size_t)blockDim.x + threadIdx.x; i < ncells; i += (size_t)G * blockDim.x )
     {
         const float e = slot_a_rz < 0 ? sv.e[i] : fmaf( alpha, d[i], sv.e[i] );
         if( code[i] & BORA_CODE_FLUID )
@@ -639,17 +677,32 @@ __global__ void k_refine_accumulate( size_t ncells, const uint16_t* __restrict__
     }
 }
 
+__global__ void k_refine_accumulate( size_t ncells, const uint16_t* __restrict__ code, BoraSolverDev sv, int dsel,
+                                     const double* __restrict__ ring, int slot_a_rz, int slot_a_dq )
+{
+    refine_accumulate_body( ncells, code, sv, dsel, ring, slot_a_rz, slot_a_dq, blockIdx.x, gridDim.x );
+}
+
+__global__ void k_refine_accumulate_batch( const BoraMemberSolve* __restrict__ ms, const BoraMemberSlots* __restrict__ sl )
+{
+    const BoraMemberSolve& m = ms[blockIdx.y];
+    const BoraMemberSlots& q = sl[blockIdx.y];
+    const unsigned G = (unsigned)m.grid[kGridCells];
+    if( !q.active || blockIdx.x >= G ) return;
+    refine_accumulate_body( (size_t)m.ntiles * 512, m.code, m.sv, q.dsel, m.red.ring, q.a_rz, q.a_dq, blockIdx.x, G );
+}
+
 // r = b - A x in double-float arithmetic (A from the stencil code, x the double-float
 // iterate); r stored in FP32, ||r||^2 and max|r| reduced. Streaming, one thread per cell.
 // GB300's FP64 pipe is narrow: in FP64 this kernel and the accumulation were bound by it.
-__global__ void __launch_bounds__( 256 ) k_refine_residual( size_t ncells, const int32_t* __restrict__ nbr,
-                                                            const float* __restrict__ b, const uint16_t* __restrict__ code,
-                                                            BoraSolverDev sv, BoraReduceDev red, int slot_norm2,
-                                                            int slot_max )
+__device__ __forceinline__ void refine_residual_body( size_t ncells, const int32_t* __restrict__ nbr,
+                                                      const float* __restrict__ b, const uint16_t* __restrict__ code,
+                                                      const BoraSolverDev& sv, const BoraReduceDev& red, int slot_norm2,
+                                                      int slot_max, unsigned bid, unsigned G )
 {
     DF n2{ 0.f, 0.f };
     float mx = 0.f;
-    for( size_t cell = blockIdx.x * (size_t)blockDim.x + threadIdx.x; cell < ncells; cell += (size_t)gridDim.x * blockDim.x )
+    for( size_t cell = bid * (size_t)blockDim.x + threadIdx.x; cell < ncells; cell += (size_t)G * blockDim.x )
     {
         const uint16_t cc = code[cell];
         if( !( cc & BORA_CODE_FLUID ) ) { sv.r[cell] = 0.f; continue; }
@@ -674,7 +727,25 @@ __global__ void __launch_bounds__( 256 ) k_refine_residual( size_t ncells, const
         n2 = df_add( n2, df_prod( rf, rf ) );
         mx = fmaxf( mx, fabsf( rf ) );
     }
-    reduce2_publish_dfmax( n2, mx, red, slot_norm2, slot_max );
+    reduce2_publish_dfmax( n2, mx, red, slot_norm2, slot_max, bid, G );
+}
+
+__global__ void __launch_bounds__( 256 ) k_refine_residual( size_t ncells, const int32_t* __restrict__ nbr,
+                                                            const float* __restrict__ b, const uint16_t* __restrict__ code,
+                                                            BoraSolverDev sv, BoraReduceDev red, int slot_norm2,
+                                                            int slot_max )
+{
+    refine_residual_body( ncells, nbr, b, code, sv, red, slot_norm2, slot_max, blockIdx.x, gridDim.x );
+}
+
+__global__ void __launch_bounds__( 256 ) k_refine_residual_batch( const BoraMemberSolve* __restrict__ ms,
+                                                                  const BoraMemberSlots* __restrict__ sl )
+{
+    const BoraMemberSolve& m = ms[blockIdx.y];
+    const BoraMemberSlots& q = sl[blockIdx.y];
+    const unsigned G = (unsigned)m.grid[kGridResidual];
+    if( !q.active || blockIdx.x >= G ) return;
+    refine_residual_body( (size_t)m.ntiles * 512, m.nbr, m.b, m.code, m.sv, m.red, q.n2, q.mx, blockIdx.x, G );
 }
 
 __global__ void k_write_pressure( size_t ncells, const uint16_t* __restrict__ code, const float2* __restrict__ x,
@@ -682,6 +753,16 @@ __global__ void k_write_pressure( size_t ncells, const uint16_t* __restrict__ co
 {
     for( size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < ncells; i += (size_t)gridDim.x * blockDim.x )
         pres[i] = ( code[i] & BORA_CODE_FLUID ) ? x[i].x + x[i].y : 0.f;
+}
+
+__global__ void k_write_pressure_batch( const BoraMemberSolve* __restrict__ ms )
+{
+    const BoraMemberSolve& m = ms[blockIdx.y];
+    const unsigned G = (unsigned)m.grid[kGridCells];
+    if( blockIdx.x >= G ) return;
+    const size_t ncells = (size_t)m.ntiles * 512;
+    for( size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < ncells; i += (size_t)G * blockDim.x )
+        m.pres[i] = ( m.code[i] & BORA_CODE_FLUID ) ? m.sv.x[i].x + m.sv.x[i].y : 0.f;
 }
 
 // ---------------------------------------------------------------------------------
@@ -830,20 +911,66 @@ void bora_launch_pcg_update( int ntiles, const uint16_t* code, BoraSolverDev s, 
                      slot_rr_out );
 }
 
-void bora_launch_pcg_direction( const BoraGridDev&, int ntiles, BoraTilesDev t, const uint16_t* code, BoraSolverDev s,
-                                int dsel_in, BoraReduceDev red, int slot_rz_new, int slot_rz_old, int slot_dq_out,
-                                int slot_a_rz, int slot_a_dq, cudaStream_t st )
+namespace {
+// Grid of the direction kernel: every warp gets the same number of tiles; at most
+// kBoraMaxReduceBlocks CTAs (partial sums capacity).
+int direction_grid( int ntiles )
 {
-    if( ntiles <= 0 ) return;
+    if( ntiles <= 0 ) return 0;
     static BoraPerDevice per_sm;
     const int b = per_sm.get( [] {
         int v = 0;
         return cudaOccupancyMaxActiveBlocksPerMultiprocessor( &v, k_pcg_direction, 32 * kDirWarps, 0 ) == cudaSuccess && v > 0 ? v : 1;
     } );
-    // every warp gets the same number of tiles; at most 152 x 16 CTAs (partial sums capacity)
     const int cap = std::max( 1, std::min( b * num_sms(), kBoraMaxReduceBlocks ) ) * kDirWarps;
     const int rounds = ( ntiles + cap - 1 ) / cap;
-    const int grid = std::max( 1, ( ntiles + kDirWarps * rounds - 1 ) / ( kDirWarps * rounds ) );
+    return std::max( 1, ( ntiles + kDirWarps * rounds - 1 ) / ( kDirWarps * rounds ) );
+}
+int residual_grid( size_t nc ) { return (int)std::max<size_t>( 1, std::min<size_t>( ( nc + 255 ) / 256, (size_t)num_sms() * 8 ) ); }
+}  // namespace
+
+void bora_projection_grids( int ntiles, int* grid )
+{
+    const size_t nc = (size_t)std::max( ntiles, 0 ) * 512;
+    grid[kGridDir] = direction_grid( ntiles );
+    grid[kGridCells] = grid_for( nc, 256 );
+    grid[kGridResidual] = residual_grid( nc );
+}
+
+void bora_launch_solve_init_batch( const BoraMemberSolve* ms, const BoraMemberSlots* sl, int n, int gx, cudaStream_t st )
+{
+    if( n > 0 && gx > 0 ) k_solve_init_batch<<<dim3( gx, n ), 256, 0, st>>>( ms, sl );
+}
+
+void bora_launch_pcg_direction_batch( const BoraMemberSolve* ms, const BoraMemberSlots* sl, int n, int gx,
+                                      cudaStream_t st )
+{
+    if( n > 0 && gx > 0 ) bora_launch_pdl( k_pcg_direction_batch, dim3( gx, n ), dim3( 32 * kDirWarps ), 0, st, ms, sl );
+}
+
+void bora_launch_refine_accumulate_batch( const BoraMemberSolve* ms, const BoraMemberSlots* sl, int n, int gx,
+                                          cudaStream_t st )
+{
+    if( n > 0 && gx > 0 ) k_refine_accumulate_batch<<<dim3( gx, n ), 256, 0, st>>>( ms, sl );
+}
+
+void bora_launch_refine_residual_batch( const BoraMemberSolve* ms, const BoraMemberSlots* sl, int n, int gx,
+                                        cudaStream_t st )
+{
+    if( n > 0 && gx > 0 ) k_refine_residual_batch<<<dim3( gx, n ), 256, 0, st>>>( ms, sl );
+}
+
+void bora_launch_write_pressure_batch( const BoraMemberSolve* ms, int n, int gx, cudaStream_t st )
+{
+    if( n > 0 && gx > 0 ) k_write_pressure_batch<<<dim3( gx, n ), 256, 0, st>>>( ms );
+}
+
+void bora_launch_pcg_direction( const BoraGridDev&, int ntiles, BoraTilesDev t, const uint16_t* code, BoraSolverDev s,
+                                int dsel_in, BoraReduceDev red, int slot_rz_new, int slot_rz_old, int slot_dq_out,
+                                int slot_a_rz, int slot_a_dq, cudaStream_t st )
+{
+    if( ntiles <= 0 ) return;
+    const int grid = direction_grid( ntiles );
     bora_launch_pdl( k_pcg_direction, grid, 32 * kDirWarps, 0, st, ntiles, (const int32_t*)t.nbr, code, s, dsel_in, red,
                      slot_rz_new, slot_rz_old, slot_dq_out, slot_a_rz, slot_a_dq );
 }
@@ -859,8 +986,7 @@ void bora_launch_refine_residual( const BoraGridDev&, int ntiles, BoraTilesDev t
                                   BoraSolverDev s, BoraReduceDev red, int slot_norm2, int slot_max, cudaStream_t st )
 {
     const size_t nc = (size_t)ntiles * 512;
-    const int nb = (int)std::max<size_t>( 1, std::min<size_t>( ( nc + 255 ) / 256, (size_t)num_sms() * 8 ) );
-    k_refine_residual<<<nb, 256, 0, st>>>( nc, t.nbr, b, code, s, red, slot_norm2, slot_max );
+    k_refine_residual<<<residual_grid( nc ), 256, 0, st>>>( nc, t.nbr, b, code, s, red, slot_norm2, slot_max );
 }
 
 void bora_launch_write_pressure( int ntiles, const uint16_t* code, const float2* x, float* pres, cudaStream_t st )

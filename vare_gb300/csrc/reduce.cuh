@@ -84,8 +84,11 @@ __device__ __forceinline__ double warp_max( double v )
 }
 
 // op1: 0 = sum, 1 = max for the second value. Slots < 0 are skipped. Inputs are the
-// per-warp totals (already reduced across the warp, valid in every lane).
-__device__ __forceinline__ void reduce2_publish_warp( double v0, double v1, int op1, BoraReduceDev red, int slot0, int slot1 )
+// per-warp totals (already reduced across the warp, valid in every lane). The block takes
+// part as block `bid` of `nblocks` (blockIdx.x of gridDim.x unless a batched launch runs
+// several simulations' blocks side by side in y).
+__device__ __forceinline__ void reduce2_publish_warp( double v0, double v1, int op1, BoraReduceDev red, int slot0, int slot1,
+                                                      unsigned bid, unsigned nblocks )
 {
     __shared__ double w0[32], w1[32];
     __shared__ bool last;
@@ -96,12 +99,12 @@ __device__ __forceinline__ void reduce2_publish_warp( double v0, double v1, int 
     {
         double a = 0.0, b = 0.0;
         for( int q = 0; q < nw; ++q ) { a += w0[q]; b = op1 ? fmax( b, w1[q] ) : b + w1[q]; }
-        red.partials[2 * (size_t)blockIdx.x] = a;
-        red.partials[2 * (size_t)blockIdx.x + 1] = b;
+        red.partials[2 * (size_t)bid] = a;
+        red.partials[2 * (size_t)bid + 1] = b;
         __threadfence();
         const int key = slot0 >= 0 ? slot0 : slot1;
         const unsigned prev = atomicAdd( &red.done[key % BORA_RING], 1u );
-        last = ( prev == gridDim.x - 1 );
+        last = ( prev == nblocks - 1 );
     }
     __syncthreads();
     if( !last ) return;
@@ -109,7 +112,7 @@ __device__ __forceinline__ void reduce2_publish_warp( double v0, double v1, int 
     // All threads of the last block: thread-strided partial sums in a fixed order
     // (independent loads, unrolled so that many are in flight), then a fixed-shape tree.
     double a = 0.0, b = 0.0;
-    const unsigned nb = gridDim.x, stride = blockDim.x;
+    const unsigned nb = nblocks, stride = blockDim.x;
 #pragma unroll 4
     for( unsigned q = threadIdx.x; q < nb; q += stride )
     {
@@ -138,18 +141,33 @@ __device__ __forceinline__ void reduce2_publish_warp( double v0, double v1, int 
     }
 }
 
+__device__ __forceinline__ void reduce2_publish_warp( double v0, double v1, int op1, BoraReduceDev red, int slot0, int slot1 )
+{
+    reduce2_publish_warp( v0, v1, op1, red, slot0, slot1, blockIdx.x, gridDim.x );
+}
+
 // Per-thread double-float sums (op1 = 0) or a float max in v1 (op1 = 1).
-__device__ __forceinline__ void reduce2_publish_df( DF v0, DF v1, BoraReduceDev red, int slot0, int slot1 )
+__device__ __forceinline__ void reduce2_publish_df( DF v0, DF v1, BoraReduceDev red, int slot0, int slot1,
+                                                    unsigned bid, unsigned nblocks )
 {
     const double a = df_warp_sum( v0 );
     const double b = df_warp_sum( v1 );
-    reduce2_publish_warp( a, b, 0, red, slot0, slot1 );
+    reduce2_publish_warp( a, b, 0, red, slot0, slot1, bid, nblocks );
 }
-__device__ __forceinline__ void reduce2_publish_dfmax( DF v0, float vmax, BoraReduceDev red, int slot0, int slot1 )
+__device__ __forceinline__ void reduce2_publish_df( DF v0, DF v1, BoraReduceDev red, int slot0, int slot1 )
+{
+    reduce2_publish_df( v0, v1, red, slot0, slot1, blockIdx.x, gridDim.x );
+}
+__device__ __forceinline__ void reduce2_publish_dfmax( DF v0, float vmax, BoraReduceDev red, int slot0, int slot1,
+                                                       unsigned bid, unsigned nblocks )
 {
     const double a = df_warp_sum( v0 );
     const double b = (double)warp_maxf( vmax );
-    reduce2_publish_warp( a, b, 1, red, slot0, slot1 );
+    reduce2_publish_warp( a, b, 1, red, slot0, slot1, bid, nblocks );
+}
+__device__ __forceinline__ void reduce2_publish_dfmax( DF v0, float vmax, BoraReduceDev red, int slot0, int slot1 )
+{
+    reduce2_publish_dfmax( v0, vmax, red, slot0, slot1, blockIdx.x, gridDim.x );
 }
 
 

@@ -1,8 +1,9 @@
 // Serving layer: continuous admission of independent FLIP simulations on one GPU under a
-// device-memory budget (include/bora_serve.h). Host code only: every admitted request is
-// a bora_flip handle with its own stream, advanced by its own host thread, so the device
-// overlaps the kernels of all running requests while the scheduler thread admits queued
-// requests as slots and memory free up.
+// device-memory budget (include/bora_serve.h). Host code only: a scheduler thread admits
+// queued requests as slots and memory free up; a stepper thread keeps every admitted
+// request as a bora_flip handle and advances all running requests together, one
+// bora_flip_step_batch per round (the pressure solve's kernels launched once for all of
+// them), taking newly admitted requests in between rounds.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -38,7 +39,6 @@ struct Request
     uint64_t nparticles = 0, estimate = 0, device_bytes = 0;
     Clock::time_point t_submit, t_admit, t_done;
     std::vector<float> step_ms;
-    std::thread worker;
 };
 
 double seconds( Clock::time_point a, Clock::time_point b ) { return std::chrono::duration<double>( b - a ).count(); }
@@ -68,11 +68,11 @@ struct bora_server
     uint64_t submitted = 0, admitted = 0, done = 0, failed = 0, particle_steps = 0, steps = 0;
     std::vector<float> step_ms;  // every step of every finished request
     bool stop = false;
-    std::thread scheduler;
-    std::vector<std::thread> retired;  // workers of released requests, joined at destroy
+    std::thread scheduler, stepper;
+    std::vector<Request*> starting;  // admitted, not yet taken by the stepper
 
-    void run_request( Request* r );
     void schedule();
+    void step_loop();
     void finish( Request* r, int status, bool ok );
 };
 
@@ -97,68 +97,156 @@ void bora_server::finish( Request* r, int status, bool ok )
     cv.notify_all();
 }
 
-void bora_server::run_request( Request* r )
+namespace {
+
+// A running request: its handle and what it has done so far.
+struct Live
 {
-    cudaSetDevice( device );
+    Request* r = nullptr;
+    bora_flip_handle h = nullptr;
+    uint64_t psteps = 0, peak = 0;
+};
+
+// Set up a request's simulation; BORA_OK or the failing call's status.
+int start_request( Request* r, bora_flip_handle* out )
+{
     bora_flip_handle h = nullptr;
     int st = bora_flip_create( &r->grid, &r->params, &h );
     if( st == BORA_OK && r->nboxes > 0 ) st = bora_flip_set_colliders( h, r->boxes.data(), r->nboxes, r->band );
-    if( st == BORA_OK )
-        st = bora_flip_set_particles( h, r->pos.data(), r->vel.data(), r->pos.size() / 3, r->space );
-    uint64_t psteps = 0, peak = 0;
-    for( int k = 0; st >= 0 && k < r->steps; ++k )
+    if( st == BORA_OK ) st = bora_flip_set_particles( h, r->pos.data(), r->vel.data(), r->pos.size() / 3, r->space );
+    if( st != BORA_OK && h ) { bora_flip_destroy( h ); h = nullptr; }
+    *out = h;
+    return st;
+}
+
+// The final particles in ascending id order (the result does not depend on the device order).
+int collect( Request* r, bora_flip_handle h, std::vector<float>& p2, std::vector<float>& v2, std::vector<int32_t>& i2 )
+{
+    size_t n = 0;
+    int st = bora_flip_num_particles( h, &n );
+    if( st != BORA_OK ) return st;
+    std::vector<float> pos( n * 3 ), vel( n * 3 );
+    std::vector<int32_t> ids( n );
+    size_t got = 0;
+    st = bora_flip_get_particles( h, pos.data(), vel.data(), nullptr, ids.data(), n, &got, r->space );
+    if( st != BORA_OK ) return st;
+    std::vector<size_t> ord( got );
+    for( size_t i = 0; i < got; ++i ) ord[i] = i;
+    std::sort( ord.begin(), ord.end(), [&]( size_t a, size_t b ) { return ids[a] < ids[b]; } );
+    p2.resize( got * 3 );
+    v2.resize( got * 3 );
+    i2.resize( got );
+    for( size_t i = 0; i < got; ++i )
     {
-        size_t n = 0;
-        bora_flip_num_particles( h, &n );
-        const Clock::time_point t0 = Clock::now();
-        const int s = bora_flip_step( h, r->dt );
-        const float ms = (float)( 1e3 * seconds( t0, Clock::now() ) );
-        if( s < 0 ) { st = s; break; }
-        psteps += n;
-        bora_flip_stats fs{};
-        bora_flip_get_stats( h, &fs );
-        peak = std::max<uint64_t>( peak, fs.device_bytes );
-        std::lock_guard<std::mutex> lk( mu );
-        r->step_ms.push_back( ms );
-        r->steps_done = k + 1;
-        r->nparticles = fs.num_particles;
-        r->device_bytes = peak;
+        std::memcpy( &p2[3 * i], &pos[3 * ord[i]], 12 );
+        std::memcpy( &v2[3 * i], &vel[3 * ord[i]], 12 );
+        i2[i] = ids[ord[i]];
     }
-    if( st >= 0 )
+    return BORA_OK;
+}
+
+}  // namespace
+
+void bora_server::step_loop()
+{
+    cudaSetDevice( device );
+    std::vector<Live> live;
+    for( ;; )
     {
-        size_t n = 0;
-        st = bora_flip_num_particles( h, &n );
-        if( st == BORA_OK )
+        std::vector<Request*> fresh;
+        bool stopping;
         {
-            std::vector<float> pos( n * 3 ), vel( n * 3 );
-            std::vector<int32_t> ids( n );
-            size_t got = 0;
-            st = bora_flip_get_particles( h, pos.data(), vel.data(), nullptr, ids.data(), n, &got, r->space );
-            if( st == BORA_OK )
+            std::unique_lock<std::mutex> lk( mu );
+            cv.wait( lk, [&] { return stop || !starting.empty() || !live.empty(); } );
+            fresh.swap( starting );
+            stopping = stop;
+        }
+        if( stopping )  // running requests are abandoned
+        {
+            for( Request* r : fresh ) finish( r, BORA_ERR_CAPACITY, false );
+            for( Live& l : live )
             {
-                // ascending ids: the result does not depend on the device order
-                std::vector<size_t> ord( got );
-                for( size_t i = 0; i < got; ++i ) ord[i] = i;
-                std::sort( ord.begin(), ord.end(), [&]( size_t a, size_t b ) { return ids[a] < ids[b]; } );
-                std::vector<float> p2( got * 3 ), v2( got * 3 );
-                std::vector<int32_t> i2( got );
-                for( size_t i = 0; i < got; ++i )
-                {
-                    std::memcpy( &p2[3 * i], &pos[3 * ord[i]], 12 );
-                    std::memcpy( &v2[3 * i], &vel[3 * ord[i]], 12 );
-                    i2[i] = ids[ord[i]];
-                }
+                bora_flip_destroy( l.h );
+                finish( l.r, BORA_ERR_CAPACITY, false );
+            }
+            return;
+        }
+        for( Request* r : fresh )
+        {
+            Live l;
+            l.r = r;
+            const int st = start_request( r, &l.h );
+            if( st != BORA_OK ) { finish( r, st, false ); continue; }
+            live.push_back( l );
+        }
+        if( live.empty() ) continue;
+        // one round: every running request with steps left advances one step; requests of
+        // equal dt share a batched step
+        std::vector<char> taken( live.size(), 0 ), bad( live.size(), 0 );
+        for( size_t a = 0; a < live.size(); ++a )
+            if( live[a].r->steps_done >= live[a].r->steps ) taken[a] = 1;  // finished (or zero steps)
+        for( size_t a = 0; a < live.size(); ++a )
+        {
+            if( taken[a] ) continue;
+            std::vector<size_t> grp;
+            for( size_t b = a; b < live.size(); ++b )
+                if( !taken[b] && live[b].r->dt == live[a].r->dt ) { grp.push_back( b ); taken[b] = 1; }
+            std::vector<bora_flip_handle> hs( grp.size() );
+            std::vector<size_t> n0( grp.size() );
+            for( size_t q = 0; q < grp.size(); ++q )
+            {
+                hs[q] = live[grp[q]].h;
+                bora_flip_num_particles( hs[q], &n0[q] );
+            }
+            std::vector<int> st( grp.size(), BORA_OK );
+            const Clock::time_point t0 = Clock::now();
+            const int bst = bora_flip_step_batch( hs.data(), (int)hs.size(), live[a].r->dt, st.data() );
+            const float ms = (float)( 1e3 * seconds( t0, Clock::now() ) );
+            for( size_t q = 0; q < grp.size(); ++q )
+            {
+                Live& l = live[grp[q]];
+                const int s = bst < 0 ? bst : st[q];
+                if( s < 0 ) { bad[grp[q]] = 1; std::lock_guard<std::mutex> lk( mu ); l.r->status = s; continue; }
+                l.psteps += n0[q];
+                bora_flip_stats fs{};
+                bora_flip_get_stats( l.h, &fs );
+                l.peak = std::max<uint64_t>( l.peak, fs.device_bytes );
                 std::lock_guard<std::mutex> lk( mu );
-                r->pos.swap( p2 );
-                r->vel.swap( v2 );
-                r->ids.swap( i2 );
-                r->nparticles = got;
-                particle_steps += psteps;
+                l.r->step_ms.push_back( ms );
+                l.r->steps_done += 1;
+                l.r->nparticles = fs.num_particles;
+                l.r->device_bytes = l.peak;
             }
         }
+        // retire finished and failed requests
+        std::vector<Live> keep;
+        for( size_t q = 0; q < live.size(); ++q )
+        {
+            Live& l = live[q];
+            if( bad[q] )
+            {
+                bora_flip_destroy( l.h );
+                finish( l.r, l.r->status, false );
+                continue;
+            }
+            if( l.r->steps_done < l.r->steps ) { keep.push_back( l ); continue; }
+            std::vector<float> p2, v2;
+            std::vector<int32_t> i2;
+            const int st = collect( l.r, l.h, p2, v2, i2 );
+            bora_flip_destroy( l.h );
+            if( st == BORA_OK )
+            {
+                std::lock_guard<std::mutex> lk( mu );
+                l.r->pos.swap( p2 );
+                l.r->vel.swap( v2 );
+                l.r->ids.swap( i2 );
+                l.r->nparticles = l.r->ids.size();
+                particle_steps += l.psteps;
+            }
+            finish( l.r, st, st == BORA_OK );
+        }
+        live.swap( keep );
     }
-    if( h ) bora_flip_destroy( h );
-    finish( r, st < 0 ? st : BORA_OK, st >= 0 );
 }
 
 void bora_server::schedule()
@@ -193,7 +281,8 @@ void bora_server::schedule()
         reserved += r->estimate;
         running_peak = std::max( running_peak, running );
         reserved_peak = std::max( reserved_peak, reserved );
-        r->worker = std::thread( [this, r] { run_request( r ); } );
+        starting.push_back( r );
+        cv.notify_all();
     }
     // stopping: queued requests are dropped
     while( !queue.empty() )
@@ -230,7 +319,7 @@ int bora_serve_default_config( bora_serve_config* out )
     if( !out ) return BORA_ERR_INVALID_ARG;
     std::memset( out, 0, sizeof( *out ) );
     out->hbm_budget_bytes = 120ull * 1000 * 1000 * 1000;
-    out->max_running = 16;
+    out->max_running = 64;
     return BORA_OK;
 }
 
@@ -249,6 +338,7 @@ int bora_serve_create( const bora_serve_config* cfg, bora_serve_handle* out )
     s->cfg = *cfg;
     cudaGetDevice( &s->device );
     s->scheduler = std::thread( [s] { s->schedule(); } );
+    s->stepper = std::thread( [s] { s->step_loop(); } );
     *out = s;
     return BORA_OK;
 }
@@ -262,10 +352,7 @@ int bora_serve_destroy( bora_serve_handle s )
     }
     s->cv.notify_all();
     if( s->scheduler.joinable() ) s->scheduler.join();
-    for( auto& kv : s->reqs )
-        if( kv.second->worker.joinable() ) kv.second->worker.join();
-    for( std::thread& t : s->retired )
-        if( t.joinable() ) t.join();
+    if( s->stepper.joinable() ) s->stepper.join();
     delete s;
     return BORA_OK;
 }
@@ -378,7 +465,6 @@ int bora_serve_release( bora_serve_handle s, uint64_t id )
     if( it == s->reqs.end() ) return BORA_ERR_INVALID_ARG;
     Request* r = it->second.get();
     if( r->state != BORA_REQ_DONE && r->state != BORA_REQ_FAILED ) return BORA_ERR_INVALID_ARG;
-    if( r->worker.joinable() ) s->retired.push_back( std::move( r->worker ) );
     s->reqs.erase( it );
     return BORA_OK;
 }

@@ -94,6 +94,7 @@ _SIGS = {
     "bora_flip_set_colliders": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_float]),
     "bora_flip_set_collider_voxels": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_size_t, ctypes.c_float]),
     "bora_flip_step": (ctypes.c_int, [_vp, ctypes.c_float]),
+    "bora_flip_step_batch": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_float, _vp]),
     "bora_flip_frame": (ctypes.c_int, [_vp]),
     "bora_flip_run_stage": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_float]),
     "bora_flip_post_process": (ctypes.c_int, [_vp]),
@@ -187,6 +188,17 @@ def scene_params(scene, **overrides) -> Params:
               proj_iteration=10000)
     kw.update(overrides)
     return default_params(**kw)
+
+
+def step_batch(sims, dt: float) -> list[int]:
+    """bora_flip_step_batch: one step of every simulation, the pressure solve batched."""
+    n = len(sims)
+    if n == 0:
+        return []
+    hs = (_vp * n)(*[s.h for s in sims])
+    st = np.zeros(n, np.int32)
+    _check(load().bora_flip_step_batch(ctypes.cast(hs, _vp), n, float(dt), _ptr(st)), "step_batch")
+    return [int(v) for v in st]
 
 
 class FlipSim:
