@@ -72,7 +72,8 @@ def parse():
     ap.add_argument("--workload", default="dam_sphere_256",
                     choices=["dam_sphere_256", "dam_break_64", "tank_1024", "serve_64"])
     ap.add_argument("--serve-requests", type=int, default=64)
-    ap.add_argument("--serve-slots", type=int, default=16)
+    ap.add_argument("--serve-slots", type=int, default=64)
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving-stream measurement of the default run")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-post", action="store_true", help="skip the post-processing measurement")
@@ -624,6 +625,14 @@ def run_ours(args, world, rank, local):
 
     post = None if args.no_post else post_measure(sim, sc, flip, args.post_reps, args.nvtx)
 
+    # the serving stream (64 uneven requests, Poisson arrivals) on the same GPU, after the timed steps
+    serve_res = None
+    if not args.no_serve and args.workload == "dam_sphere_256":
+        del sim
+        torch.cuda.empty_cache()
+        sim = None
+        serve_res = serve_stream(args, world, local, clocks_on=False)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         del sim
@@ -645,26 +654,24 @@ def run_ours(args, world, rank, local):
            "config": workload_config(sc, solver=args.solver if args.solver != "both" else "plain"), "roofline": roof,
            "cpu_baseline": cpu, "e2e": e2e,
            "gpu_launches": int(launches), "clocks": clk, "solver": meas["solver"], "step_roofline": meas["step_roofline"],
-           "mixed": mixed, "post_process": post}
+           "mixed": mixed, "post_process": post, "serve": serve_res}
     print(json.dumps(out), flush=True)
 
 
-def run_serve(args, world, rank, local):
+def serve_stream(args, world, local, clocks_on: bool = True) -> dict:
     """The serving stream: requests of uneven sizes arrive as a Poisson process at 20/s and
-    are admitted continuously under a 120 GB budget (mixed-precision solver); each rank
-    serves its own copy of the stream (replicas)."""
-    import torch
+    are admitted continuously under a 120 GB budget (mixed-precision solver); running
+    requests advance together in batched rounds (bora_flip_step_batch). Each rank serves its
+    own copy of the stream (replicas)."""
+    from vare_gb300 import flip, scenes, serve
 
-    from vare_gb300 import build, flip, scenes, serve
-
-    build.build()
-    torch.cuda.set_device(local)
     n = args.serve_requests
     reqs = [scenes.serving_request(r) for r in range(n)]
     arrivals = scenes.serving_arrivals(n, 20.0)
     srv = serve.Server(budget_bytes=120 * 10**9, max_running=args.serve_slots)
-    clocks = ClockSampler(local)
-    clocks.start()
+    clocks = ClockSampler(local) if clocks_on else None
+    if clocks:
+        clocks.start()
     barrier(world)
     t0 = time.perf_counter()
     ids = []
@@ -675,29 +682,45 @@ def run_serve(args, world, rank, local):
         ids.append(srv.submit(sc, steps, solver=flip.SOLVER_MIXED))
     srv.drain()
     t1 = time.perf_counter()
-    clk = clocks.stop()
+    clk = clocks.stop() if clocks else None
     st = srv.stats()
     info = [srv.poll(i) for i in ids]
     srv.close()
     span = allreduce_max(t1 - t0, world)
     total = allreduce_sum(float(st["particle_steps"]), world)
+    qs = sorted(x["queued_s"] for x in info)
+    return {"value": total / span, "unit": UNIT,
+            "step_ms_p50": st["step_ms_p50"], "step_ms_p99": st["step_ms_p99"], "step_ms_max": st["step_ms_max"],
+            "makespan_s": span, "requests": n, "done": st["done"], "failed": st["failed"],
+            "substeps": st["steps"], "particle_steps": st["particle_steps"], "running_peak": st["running_peak"],
+            "bytes_reserved_peak": st["bytes_reserved_peak"],
+            "queue_wait_s": {"p50": qs[len(qs) // 2], "p99": qs[min(len(qs) - 1, int(0.99 * (len(qs) - 1) + 0.5))]},
+            "config": {"workload": f"serve_{n}: per request cubic edge log-uniform in [32, 192] cells, fill 0.2-0.5, "
+                                   "50-400 substeps, dam break / sphere drop by parity, dt = 1/240, Poisson arrivals "
+                                   "at 20/s",
+                       "slots": args.serve_slots, "budget_bytes": 120 * 10**9,
+                       "stepping": "one stepper thread; all running requests advance together, one "
+                                   "bora_flip_step_batch per round (pressure-solve kernels launched once per round)",
+                       "parallelism": "replicas (each GPU serves its own stream)"},
+            "clocks": clk}
+
+
+def run_serve(args, world, rank, local):
+    import torch
+
+    from vare_gb300 import build
+
+    build.build()
+    torch.cuda.set_device(local)
+    res = serve_stream(args, world, local)
     if rank != 0:
         return
-    qs = sorted(x["queued_s"] for x in info)
+    n = args.serve_requests
     out = {"metric": f"particle-steps/s, serving stream of {n} FLIP requests (Poisson 20/s, edges 32-192, "
                      "mixed precision, 120 GB budget)",
-           "value": total / span, "unit": UNIT, "n_gpus": world, "higher_is_better": True, "scaling": "weak",
-           "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded dam-break / sphere-drop requests)",
-           "step_ms_p50": st["step_ms_p50"], "step_ms_p99": st["step_ms_p99"], "step_ms_max": st["step_ms_max"],
-           "makespan_s": span, "requests": n, "done": st["done"], "failed": st["failed"],
-           "substeps": st["steps"], "particle_steps": st["particle_steps"], "running_peak": st["running_peak"],
-           "bytes_reserved_peak": st["bytes_reserved_peak"],
-           "queue_wait_s": {"p50": qs[len(qs) // 2], "p99": qs[min(len(qs) - 1, int(0.99 * (len(qs) - 1) + 0.5))]},
-           "config": {"workload": "serve_64: per request cubic edge log-uniform in [32, 192] cells, fill 0.2-0.5, "
-                                  "50-400 substeps, dam break / sphere drop by parity, dt = 1/240",
-                      "slots": args.serve_slots, "budget_bytes": 120 * 10**9,
-                      "parallelism": "replicas (each GPU serves its own stream)"},
-           "clocks": clk}
+           "value": res["value"], "unit": UNIT, "n_gpus": world, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded dam-break / sphere-drop requests)"}
+    out.update({k: v for k, v in res.items() if k not in ("value", "unit")})
     print(json.dumps(out), flush=True)
 
 
