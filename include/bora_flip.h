@@ -109,7 +109,9 @@ typedef struct bora_flip_stats
     int32_t converged;
     int32_t mg_vcycle_launches;   /* kernel launches per V-cycle in the last solve (mixed form), else 0 */
     double stage_ms[8];           /* host wall time of the last step: rebuild, p2g, system, solve,
-                                     velocity, particles, -, total */
+                                     velocity, particles, -, total; after a batched step
+                                     (bora_flip_step_batch) the batch's: [0] the stages before
+                                     the solve, [3] the solve, [5] the stages after it, [7] total */
     double gpu_ms;                /* device time of the last step (CUDA events on the handle's stream) */
     uint64_t kernel_launches;     /* kernels launched by this handle since creation */
     uint64_t device_bytes;        /* device memory the handle holds */

@@ -47,7 +47,7 @@ def test_estimate_grows_with_particles_and_solver(lib):
 def test_default_config_and_invalid_arguments(lib):
     c = serve.ServeConfig()
     assert lib.bora_serve_default_config(ctypes.byref(c)) == 0
-    assert c.hbm_budget_bytes == 120 * 10**9 and c.max_running == 16
+    assert c.hbm_budget_bytes == 120 * 10**9 and c.max_running == 64
     h = ctypes.c_void_p()
     assert lib.bora_serve_create(None, ctypes.byref(h)) == -1
     c.max_running = 0

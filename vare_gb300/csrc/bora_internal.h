@@ -252,10 +252,12 @@ void bora_mg_vcycle( const BoraGridDev& g, const BoraLevelDev* levels, int nleve
                      const float* r, float* z, BoraReduceDev red, int slot_rr, int slot_rz, int coarse_sweeps,
                      cudaStream_t st );
 // ---- batched solve: several simulations, one launch per kernel ---------------------------
-// A batched launch runs simulation blockIdx.y of the batch on the grid that its own
-// single-simulation launch would use (grid[], fixed by its tile count alone; blocks beyond
-// it return at once) and reduces into its own ring, so every simulation's arithmetic and
-// summation order are the same alone and in any batch. Arguments come from device arrays.
+// A batched launch packs the blocks of the simulations taking part back to back into one
+// 1-D grid: simulation k owns blocks start[k] .. start[k+1] - 1, exactly the grid its own
+// single-simulation launch of that kernel would use (grid[], fixed by its tile count alone),
+// and no block when it sits the launch out. Each simulation reduces into its own ring, so
+// its block indices, grid size, arithmetic and summation order are the same alone and in
+// any batch, and no block of a batched launch idles. Arguments come from device arrays.
 enum BoraMemberGrid
 {
     kGridDir = 0, kGridUpd, kGridCells, kGridResidual, kGridDown8, kGridDown4, kGridDown2, kGridUp8, kGridUp4, kGridUp2,
@@ -283,30 +285,49 @@ struct BoraMemberSlots  // ring slots of one batched launch sequence
     int rr, rz;                          // V-cycle: the scale's r.r, r.z out
     int n2, mx;                          // solve init / refinement residual: ||r||^2, max|r|
 };
+struct BoraBatchLaunch
+{
+    const BoraMemberSolve* ms;
+    const BoraMemberSlots* sl;
+    const int* start;  // n + 1 block offsets of this launch (device memory)
+    int n;
+};
+#ifdef __CUDACC__
+// The simulation owning block b of a batched launch - the last k with start[k] <= b (the
+// ones before it that own no block share its offset) - and the block's index in its grid.
+__device__ __forceinline__ int bora_batch_member( const BoraBatchLaunch& L, unsigned b, unsigned* bid )
+{
+    int lo = 0, hi = L.n;
+    while( hi - lo > 1 )
+    {
+        const int mid = ( lo + hi ) >> 1;
+        if( (unsigned)__ldg( L.start + mid ) <= b ) lo = mid;
+        else hi = mid;
+    }
+    *bid = b - (unsigned)__ldg( L.start + lo );
+    return lo;
+}
+#endif
 
 // The coarse cluster kernel of a batch: a simulation's descriptor (opaque, desc_bytes each;
-// 0 when its hierarchy does not fit the kernel), and one launch with one cluster per
-// simulation (all with the same cluster size; shared memory for the largest).
+// 0 when its hierarchy does not fit the kernel), and one launch of `blocks` CTAs: one
+// cluster of `ctas` CTAs per simulation taking part (all of the same size; shared memory
+// for the largest).
 size_t bora_mg_mid_desc_bytes();
 int bora_mg_mid_describe( const BoraGridDev& g, const BoraLevelDev* levels, int nlevels, BoraTilesDev t, int ntiles,
                           const void* image, uint32_t* err, int sweeps, void* desc, size_t* smem, int* ctas );
-void bora_mg_mid_launch_batch( const void* descs, const BoraMemberSlots* slots, int n, int ctas, size_t smem,
+void bora_mg_mid_launch_batch( const void* descs, const BoraBatchLaunch& L, int blocks, int ctas, size_t smem,
                                cudaStream_t st );
-// Batched launches of the solver kernels (projection.cu, multigrid.cu): n simulations in y,
-// grid x = the largest of their own grids for that kernel.
-void bora_launch_solve_init_batch( const BoraMemberSolve* ms, const BoraMemberSlots* sl, int n, int gx, cudaStream_t st );
-void bora_launch_pcg_direction_batch( const BoraMemberSolve* ms, const BoraMemberSlots* sl, int n, int gx,
-                                      cudaStream_t st );
-void bora_launch_refine_accumulate_batch( const BoraMemberSolve* ms, const BoraMemberSlots* sl, int n, int gx,
-                                          cudaStream_t st );
-void bora_launch_refine_residual_batch( const BoraMemberSolve* ms, const BoraMemberSlots* sl, int n, int gx,
-                                        cudaStream_t st );
-void bora_launch_write_pressure_batch( const BoraMemberSolve* ms, int n, int gx, cudaStream_t st );
-void bora_launch_pcg_update_noprec_batch( const BoraMemberSolve* ms, const BoraMemberSlots* sl, int n, int gx,
-                                          cudaStream_t st );
+// Batched launches of the solver kernels (projection.cu, multigrid.cu) with `blocks` =
+// start[n] blocks in all.
+void bora_launch_solve_init_batch( const BoraBatchLaunch& L, int blocks, cudaStream_t st );
+void bora_launch_pcg_direction_batch( const BoraBatchLaunch& L, int blocks, cudaStream_t st );
+void bora_launch_refine_accumulate_batch( const BoraBatchLaunch& L, int blocks, cudaStream_t st );
+void bora_launch_refine_residual_batch( const BoraBatchLaunch& L, int blocks, cudaStream_t st );
+void bora_launch_write_pressure_batch( const BoraBatchLaunch& L, int blocks, cudaStream_t st );
+void bora_launch_pcg_update_noprec_batch( const BoraBatchLaunch& L, int blocks, cudaStream_t st );
 // one fused V-cycle kernel (down or up) of level l (0, 1, 2) for the batch
-void bora_launch_mg_fused_batch( bool up, int l, const BoraMemberSolve* ms, const BoraMemberSlots* sl, int n, int gx,
-                                 cudaStream_t st );
+void bora_launch_mg_fused_batch( bool up, int l, const BoraBatchLaunch& L, int blocks, cudaStream_t st );
 // this simulation's own grid per batched kernel (what its single launches use)
 void bora_member_grids( int ntiles, int* grid );
 void bora_projection_grids( int ntiles, int* grid );  // the kGridDir, kGridCells and kGridResidual entries

@@ -191,6 +191,7 @@ struct bora_flip_sim
 
     // device timing: per-step events (always) and opt-in per-kernel-class events
     cudaEvent_t ev_step[2] = { nullptr, nullptr };
+    cudaEvent_t ev_join = nullptr;  // batched steps: joins this handle's stream with the batch's
     uint32_t prof_mask = 0;
     double kt_ms[BORA_KERNEL_CLASSES] = {};
     uint64_t kt_n[BORA_KERNEL_CLASSES] = {};
@@ -410,11 +411,16 @@ int ensure_cells( bora_flip_sim* s, int ntiles )
 // Scalars the host reads back are written into mapped host memory by a one-warp kernel
 // rather than copied: a copy would queue behind a large export on the copy engines
 // (bora_flip_export_begin) and stall the step it should overlap.
-int read_counters( bora_flip_sim* s, int first, int count )
+int issue_counters( bora_flip_sim* s, int first, int count, cudaStream_t st )
 {
     s->stats.kernel_launches += 1;
-    k_to_host_u32<<<1, 32, 0, s->st>>>( P<uint32_t>( s->counters ) + first, s->d_cnt + first, count );
-    BORA_TRY( cudaGetLastError() );
+    k_to_host_u32<<<1, 32, 0, st>>>( P<uint32_t>( s->counters ) + first, s->d_cnt + first, count );
+    return cuda_status( cudaGetLastError() );
+}
+
+int read_counters( bora_flip_sim* s, int first, int count )
+{
+    BORA_TRYS( issue_counters( s, first, count, s->st ) );
     BORA_TRY( cudaStreamSynchronize( s->st ) );
     return BORA_OK;
 }
@@ -432,8 +438,10 @@ double read_ring( bora_flip_sim* s, int slot, int* status )
 // ---- stages --------------------------------------------------------------------------
 
 // SparseFrame::buildFromPoints (SparseFrame.cu:83-155): bin, activate, number the active
-// tiles, then counting-sort the particles by dual cell.
-int stage_rebuild( bora_flip_sim* s )
+// tiles, then counting-sort the particles by dual cell. Three parts around the two host
+// reads (the tile count, then the sort's totals), so that a batched step can issue each part
+// for all of its simulations before it waits.
+int rebuild_tiles( bora_flip_sim* s )
 {
     cudaStream_t st = s->st;
     BORA_TRY( cudaMemsetAsync( s->tile_flag.p, 0, s->ntv, st ) );
@@ -446,7 +454,13 @@ int stage_rebuild( bora_flip_sim* s )
                        P<uint32_t>( s->counters ) + 0, st );
     }
     BORA_TRYS( check_launch( s ) );
-    BORA_TRYS( read_counters( s, 0, 1 ) );
+    return issue_counters( s, 0, 1, st );
+}
+
+// after rebuild_tiles' tile count has reached the host
+int rebuild_sort( bora_flip_sim* s )
+{
+    cudaStream_t st = s->st;
     const int ntiles = (int)s->h_cnt[0];
     BORA_TRYS( ensure_cells( s, std::max( ntiles, 1 ) ) );
     s->ntiles = ntiles;
@@ -468,12 +482,26 @@ int stage_rebuild( bora_flip_sim* s )
         if( s->np ) bora_launch_order_bins( (size_t)ncell + 1, P<uint32_t>( s->cell_start ), P<uint32_t>( s->idx ), st );
     }
     BORA_TRYS( check_launch( s ) );
-    BORA_TRYS( read_counters( s, 1, 2 ) );
+    return issue_counters( s, 1, 2, st );
+}
+
+// after rebuild_sort's totals have reached the host
+int rebuild_finish( bora_flip_sim* s )
+{
     if( s->h_cnt[2] != 0 ) return BORA_ERR_INTERNAL;
     s->nsorted = s->h_cnt[1];  // live particles, addressed through idx in dual-cell order
     s->sorted = true;
-    s->stats.active_tiles = ntiles;
+    s->stats.active_tiles = s->ntiles;
     return BORA_OK;
+}
+
+int stage_rebuild( bora_flip_sim* s )
+{
+    BORA_TRYS( rebuild_tiles( s ) );
+    BORA_TRY( cudaStreamSynchronize( s->st ) );
+    BORA_TRYS( rebuild_sort( s ) );
+    BORA_TRY( cudaStreamSynchronize( s->st ) );
+    return rebuild_finish( s );
 }
 
 int stage_p2g( bora_flip_sim* s )
@@ -720,7 +748,9 @@ int stage_update_velocity( bora_flip_sim* s )
     return check_launch( s );
 }
 
-int stage_update_particles( bora_flip_sim* s, float dt )
+// G2P, advection and kills (FLIPMethod.cu:54-175) into the other particle buffer; the kill
+// count goes to the host. Two parts around the host read, as the rebuild.
+int g2p_issue( bora_flip_sim* s, float dt )
 {
     if( !s->sorted ) return BORA_ERR_INVALID_ARG;
     cudaStream_t st = s->st;
@@ -732,14 +762,25 @@ int stage_update_particles( bora_flip_sim* s, float dt )
                          P<uint32_t>( s->idx ), s->parts( nxt ), P<float>( s->adj ), dt, P<uint32_t>( s->counters ) + 3, st );
     }
     BORA_TRYS( check_launch( s ) );
-    BORA_TRYS( read_counters( s, 3, 1 ) );
-    s->cur = nxt;
+    return issue_counters( s, 3, 1, st );
+}
+
+int g2p_finish( bora_flip_sim* s )
+{
+    s->cur ^= 1;
     s->np = s->nsorted;
     s->sorted = false;
     s->stats.killed_last_step = s->h_cnt[3];
     s->nlive = s->np - s->h_cnt[3];
     s->stats.num_particles = s->nlive;
     return BORA_OK;
+}
+
+int stage_update_particles( bora_flip_sim* s, float dt )
+{
+    BORA_TRYS( g2p_issue( s, dt ) );
+    BORA_TRY( cudaStreamSynchronize( s->st ) );
+    return g2p_finish( s );
 }
 
 // ---- post-processing (FLIPMethod::postProcess, FLIPMethod.cu:300-405) --------------------
@@ -958,6 +999,7 @@ int bora_flip_create( const bora_grid_desc* grid, const bora_flip_params* params
     int st = cuda_status( cudaStreamCreateWithFlags( &s->st, cudaStreamNonBlocking ) );
     if( st == BORA_OK ) st = cuda_status( cudaEventCreate( &s->ev_step[0] ) );
     if( st == BORA_OK ) st = cuda_status( cudaEventCreate( &s->ev_step[1] ) );
+    if( st == BORA_OK ) st = cuda_status( cudaEventCreateWithFlags( &s->ev_join, cudaEventDisableTiming ) );
     if( st == BORA_OK ) st = cuda_status( cudaHostAlloc( (void**)&s->h_cnt, 64, cudaHostAllocMapped ) );
     if( st == BORA_OK ) st = cuda_status( cudaHostGetDevicePointer( (void**)&s->d_cnt, s->h_cnt, 0 ) );
     if( st == BORA_OK ) st = cuda_status( cudaHostAlloc( (void**)&s->h_ring, 64, cudaHostAllocMapped ) );
@@ -1002,6 +1044,7 @@ int bora_flip_destroy( bora_flip_handle s )
         if( s->ev_step[q] ) cudaEventDestroy( s->ev_step[q] );
     for( cudaEvent_t e : s->ev_chk )
         if( e ) cudaEventDestroy( e );
+    if( s->ev_join ) cudaEventDestroy( s->ev_join );
     if( s->h_cnt ) cudaFreeHost( s->h_cnt );
     if( s->h_ring ) cudaFreeHost( s->h_ring );
     if( s->h_mirror ) cudaFreeHost( s->h_mirror );
@@ -1253,8 +1296,9 @@ int bora_flip_step( bora_flip_handle s, float dt )
 //
 // bora_flip_step_batch advances several simulations one step each. Their per-simulation
 // stages (tile rebuild and sort, P2G, system and multigrid set-up, velocity update, G2P)
-// run back to back on one stream; the pressure solve - all but a few of a step's launches -
-// runs every kernel once for all of them: simulation k of the batch is row blockIdx.y of
+// run on each simulation's own stream, every part issued for all of them before the host
+// waits on any; the pressure solve - all but a few of a step's launches - runs every kernel
+// once for all of them: simulation k of the batch is row blockIdx.y of
 // each launch, on the grid of its own single launch, reducing into its own ring (the
 // batched kernels in projection.cu, multigrid.cu and mg_mid.cu). Each simulation follows
 // stage_solve's control flow on its own (refinement passes, convergence checks one
@@ -1308,7 +1352,6 @@ int batch_solve( std::vector<BatchMember>& M, cudaStream_t st, BatchBuffers& bb,
     std::vector<char> mid( dbytes * n );
     int ctas = 0;
     size_t smem = 0;
-    int gmax[kGridCount] = {};
     for( int k = 0; k < n; ++k )
     {
         bora_flip_sim* s = M[k].s;
@@ -1323,7 +1366,6 @@ int batch_solve( std::vector<BatchMember>& M, cudaStream_t st, BatchBuffers& bb,
         for( int l = 0; l < 4; ++l ) m.L[l] = s->levels[l];
         m.z3 = s->levels[3].z0;
         bora_member_grids( s->ntiles, m.grid );
-        for( int q = 0; q < kGridCount; ++q ) gmax[q] = std::max( gmax[q], m.grid[q] );
         size_t sm = 0;
         int c = 0;
         if( !bora_mg_mid_describe( s->g, s->levels, s->nlevels, s->tiles(), s->ntiles, s->mg_mid.p,
@@ -1333,25 +1375,46 @@ int batch_solve( std::vector<BatchMember>& M, cudaStream_t st, BatchBuffers& bb,
         ctas = c;
         smem = std::max( smem, sm );
     }
+    // a launch group's arguments: the slots, then per kernel (and the coarse cluster kernel)
+    // the n + 1 block offsets of the simulations taking part
+    constexpr int kRows = kGridCount + 1;
+    const size_t sl_bytes = sizeof( BoraMemberSlots ) * n;
+    const size_t grp_bytes = sl_bytes + sizeof( int ) * kRows * ( n + 1 );
     BORA_TRY( grow( bb.ms, sizeof( BoraMemberSolve ) * n, false, st ) );
-    BORA_TRY( grow( bb.sl, sizeof( BoraMemberSlots ) * n, false, st ) );
+    BORA_TRY( grow( bb.sl, grp_bytes, false, st ) );
     BORA_TRY( grow( bb.mid, dbytes * n, false, st ) );
     BORA_TRY( cudaMemcpyAsync( bb.ms.p, ms.data(), sizeof( BoraMemberSolve ) * n, cudaMemcpyHostToDevice, st ) );
     BORA_TRY( cudaMemcpyAsync( bb.mid.p, mid.data(), dbytes * n, cudaMemcpyHostToDevice, st ) );
     const BoraMemberSolve* dms = P<BoraMemberSolve>( bb.ms );
     const BoraMemberSlots* dsl = P<BoraMemberSlots>( bb.sl );
-    std::vector<BoraMemberSlots> sl( n );
+    const int* dstart = reinterpret_cast<const int*>( static_cast<const char*>( bb.sl.p ) + sl_bytes );
+    std::vector<char> grp( grp_bytes );
+    BoraMemberSlots* sl = reinterpret_cast<BoraMemberSlots*>( grp.data() );
+    int* start = reinterpret_cast<int*>( grp.data() + sl_bytes );
+    int blocks[kRows] = {};
     uint64_t launches = 0;
-    // this launch group's slots; the copy is stream-ordered after every earlier launch that
-    // read the buffer
+    // this launch group's arguments; the copy is stream-ordered after every earlier launch
+    // that read the buffer
     auto upload = [&]() -> int {
-        BORA_TRY( cudaMemcpyAsync( bb.sl.p, sl.data(), sizeof( BoraMemberSlots ) * n, cudaMemcpyHostToDevice, st ) );
+        for( int q = 0; q < kRows; ++q )
+        {
+            int acc = 0;
+            for( int k = 0; k < n; ++k )
+            {
+                start[q * ( n + 1 ) + k] = acc;
+                if( sl[k].active ) acc += q < kGridCount ? ms[k].grid[q] : ctas;
+            }
+            start[q * ( n + 1 ) + n] = acc;
+            blocks[q] = acc;
+        }
+        BORA_TRY( cudaMemcpyAsync( bb.sl.p, grp.data(), grp_bytes, cudaMemcpyHostToDevice, st ) );
         return BORA_OK;
     };
+    auto launch = [&]( int q ) { return BoraBatchLaunch{ dms, dsl, dstart + q * ( n + 1 ), n }; };
     auto vcycle = [&]() {
-        for( int l = 0; l < 3; ++l ) bora_launch_mg_fused_batch( false, l, dms, dsl, n, gmax[kGridDown8 + l], st );
-        bora_mg_mid_launch_batch( bb.mid.p, dsl, n, ctas, smem, st );
-        for( int l = 2; l >= 0; --l ) bora_launch_mg_fused_batch( true, l, dms, dsl, n, gmax[kGridUp8 + l], st );
+        for( int l = 0; l < 3; ++l ) bora_launch_mg_fused_batch( false, l, launch( kGridDown8 + l ), blocks[kGridDown8 + l], st );
+        bora_mg_mid_launch_batch( bb.mid.p, launch( kGridCount ), blocks[kGridCount], ctas, smem, st );
+        for( int l = 2; l >= 0; --l ) bora_launch_mg_fused_batch( true, l, launch( kGridUp8 + l ), blocks[kGridUp8 + l], st );
         launches += 7;
     };
     // r = b, x = e = d = q = 0; ||b||^2, max|b|
@@ -1367,7 +1430,7 @@ int batch_solve( std::vector<BatchMember>& M, cudaStream_t st, BatchBuffers& bb,
         BORA_TRY( cudaMemsetAsync( P<uint32_t>( b.s->counters ) + 5, 0, 4, st ) );
     }
     BORA_TRYS( upload() );
-    bora_launch_solve_init_batch( dms, dsl, n, gmax[kGridCells], st );
+    bora_launch_solve_init_batch( launch( kGridCells ), blocks[kGridCells], st );
     ++launches;
     BORA_TRYS( check_launch( nullptr ) );
     BORA_TRY( cudaStreamSynchronize( st ) );
@@ -1412,7 +1475,7 @@ int batch_solve( std::vector<BatchMember>& M, cudaStream_t st, BatchBuffers& bb,
         if( start )
         {
             BORA_TRYS( upload() );
-            bora_launch_pcg_update_noprec_batch( dms, dsl, n, gmax[kGridUpd], st );
+            bora_launch_pcg_update_noprec_batch( launch( kGridUpd ), blocks[kGridUpd], st );
             ++launches;
             vcycle();
         }
@@ -1443,8 +1506,8 @@ int batch_solve( std::vector<BatchMember>& M, cudaStream_t st, BatchBuffers& bb,
         if( inner )
         {
             BORA_TRYS( upload() );
-            bora_launch_pcg_direction_batch( dms, dsl, n, gmax[kGridDir], st );
-            bora_launch_pcg_update_noprec_batch( dms, dsl, n, gmax[kGridUpd], st );
+            bora_launch_pcg_direction_batch( launch( kGridDir ), blocks[kGridDir], st );
+            bora_launch_pcg_update_noprec_batch( launch( kGridUpd ), blocks[kGridUpd], st );
             launches += 2;
             vcycle();
             BORA_TRYS( check_launch( nullptr ) );
@@ -1487,8 +1550,8 @@ int batch_solve( std::vector<BatchMember>& M, cudaStream_t st, BatchBuffers& bb,
         if( refine )
         {
             BORA_TRYS( upload() );
-            bora_launch_refine_accumulate_batch( dms, dsl, n, gmax[kGridCells], st );
-            bora_launch_refine_residual_batch( dms, dsl, n, gmax[kGridResidual], st );
+            bora_launch_refine_accumulate_batch( launch( kGridCells ), blocks[kGridCells], st );
+            bora_launch_refine_residual_batch( launch( kGridResidual ), blocks[kGridResidual], st );
             launches += 2;
             BORA_TRYS( check_launch( nullptr ) );
             BORA_TRY( cudaStreamSynchronize( st ) );
@@ -1511,15 +1574,22 @@ int batch_solve( std::vector<BatchMember>& M, cudaStream_t st, BatchBuffers& bb,
         for( const BatchMember& b : M ) any = any || b.phase != BatchMember::kDone;
         if( !any ) break;
     }
-    bora_launch_write_pressure_batch( dms, n, gmax[kGridCells], st );
+    for( int k = 0; k < n; ++k )
+    {
+        sl[k] = BoraMemberSlots{};
+        sl[k].active = 1;
+    }
+    BORA_TRYS( upload() );
+    bora_launch_write_pressure_batch( launch( kGridCells ), blocks[kGridCells], st );
     ++launches;
     BORA_TRYS( check_launch( nullptr ) );
+    for( BatchMember& b : M ) BORA_TRYS( issue_counters( b.s, 5, 2, st ) );
+    BORA_TRY( cudaStreamSynchronize( st ) );
     int status = BORA_OK;
     for( BatchMember& b : M )
     {
         bora_flip_sim* s = b.s;
         s->stats.kernel_launches += launches;
-        BORA_TRYS( read_counters( s, 5, 2 ) );
         if( s->h_cnt[5] != 0 ) return BORA_ERR_INTERNAL;
         s->stats.fluid_cells = (int32_t)s->h_cnt[6];
         s->stats.solver_iterations = b.total_it;
@@ -1550,49 +1620,68 @@ int bora_flip_step_batch( bora_flip_handle* hs, int n, float dt, int* status )
         dev = hs[k]->device;
         status[k] = BORA_OK;
     }
-    // the batch runs on the first simulation's stream; the others lend theirs back at the end
-    bora_flip_sim* h0 = hs[0];
-    cudaStream_t st = h0->st;
-    std::vector<cudaStream_t> own( n );
-    for( int k = 0; k < n; ++k )
-    {
-        own[k] = hs[k]->st;
-        if( k ) BORA_TRY( cudaStreamSynchronize( own[k] ) );
-    }
-    for( int k = 0; k < n; ++k ) hs[k]->st = st;
     struct Restore
     {
         bora_flip_handle* hs;
-        std::vector<cudaStream_t>& own;
+        int n;
         ~Restore()
         {
-            for( size_t k = 0; k < own.size(); ++k ) { hs[k]->st = own[k]; hs[k]->batching = false; }
+            for( int k = 0; k < n; ++k ) hs[k]->batching = false;
         }
-    } restore{ hs, own };
+    } restore{ hs, n };
+    // the batched solve runs on the first simulation's stream; every simulation's own stages
+    // run on its own stream, so those of different simulations overlap on the device
+    bora_flip_sim* h0 = hs[0];
+    cudaStream_t st = h0->st;
     const auto t0 = std::chrono::steady_clock::now();
     BORA_TRY( cudaEventRecord( h0->ev_step[0], st ) );
-    // per-simulation stages before the solve; simulations the batched solve cannot take (the
-    // plain form, no tiles, a hierarchy the coarse cluster kernel does not fit) step on their
-    // own afterwards
-    std::vector<BatchMember> M;
-    std::vector<int> solo;
+    // simulations the batched solve cannot take (the plain form, no tiles, a hierarchy the
+    // coarse cluster kernel does not fit) step on their own afterwards
+    std::vector<int> pre, solo;
     for( int k = 0; k < n; ++k )
     {
         bora_flip_sim* s = hs[k];
         if( s->np == 0 ) continue;  // FLIPMethod.cu:179
         if( s->prm.solver != BORA_SOLVER_MIXED ) { solo.push_back( k ); continue; }
         s->batching = true;
-        if( !s->sorted ) status[k] = stage_rebuild( s );
+        pre.push_back( k );
+    }
+    // the stages before the solve, each part issued for every simulation before the host
+    // waits for any of them: tiles (-> tile count), sort (-> totals), P2G and the system
+    std::vector<char> rebuilt( n, 0 );
+    for( int k : pre )
+        if( !hs[k]->sorted ) { status[k] = rebuild_tiles( hs[k] ); rebuilt[k] = 1; }
+    for( int k : pre )
+        if( rebuilt[k] && status[k] >= 0 )
+        {
+            status[k] = cuda_status( cudaStreamSynchronize( hs[k]->st ) );
+            if( status[k] >= 0 ) status[k] = rebuild_sort( hs[k] );
+        }
+    std::vector<BatchMember> M;
+    for( int k : pre )
+    {
+        bora_flip_sim* s = hs[k];
+        if( rebuilt[k] && status[k] >= 0 )
+        {
+            status[k] = cuda_status( cudaStreamSynchronize( s->st ) );
+            if( status[k] >= 0 ) status[k] = rebuild_finish( s );
+        }
         if( status[k] >= 0 ) status[k] = stage_p2g( s );
         if( status[k] >= 0 ) status[k] = stage_build_system( s );
         if( status[k] < 0 ) continue;
         if( s->ntiles <= 0 || !s->mg_mid_on ) { s->batching = false; solo.push_back( k ); continue; }
+        if( s != h0 )
+        {
+            BORA_TRY( cudaEventRecord( s->ev_join, s->st ) );
+            BORA_TRY( cudaStreamWaitEvent( st, s->ev_join, 0 ) );
+        }
         BatchMember b;
         b.s = s;
         b.row = (int)M.size();
         b.index = k;
         M.push_back( b );
     }
+    const auto t1 = std::chrono::steady_clock::now();
     if( !M.empty() )
     {
         static BatchBuffers bb_cache[64];  // per device: the batch's argument arrays
@@ -1601,32 +1690,50 @@ int bora_flip_step_batch( bora_flip_handle* hs, int n, float dt, int* status )
         BatchBuffers& bb = bb_cache[dev >= 0 && dev < 64 ? dev : 0];
         const int solve = batch_solve( M, st, bb, h0 );
         if( solve < 0 ) return solve;
-        for( BatchMember& b : M )
-        {
-            bora_flip_sim* s = b.s;
-            int stt = stage_update_velocity( s );
-            if( stt >= 0 ) stt = stage_update_particles( s, dt );
-            status[b.index] = stt < 0 ? stt : s->last_status;
-        }
+    }
+    const auto t2 = std::chrono::steady_clock::now();
+    // the stages after the solve, back on each simulation's stream
+    if( !M.empty() ) BORA_TRY( cudaEventRecord( h0->ev_join, st ) );
+    for( BatchMember& b : M )
+    {
+        bora_flip_sim* s = b.s;
+        if( s != h0 ) BORA_TRY( cudaStreamWaitEvent( s->st, h0->ev_join, 0 ) );
+        int stt = stage_update_velocity( s );
+        if( stt >= 0 ) stt = g2p_issue( s, dt );
+        status[b.index] = stt;
+    }
+    for( BatchMember& b : M )
+    {
+        bora_flip_sim* s = b.s;
+        if( status[b.index] < 0 ) continue;
+        int stt = cuda_status( cudaStreamSynchronize( s->st ) );
+        if( stt >= 0 ) stt = g2p_finish( s );
+        status[b.index] = stt < 0 ? stt : s->last_status;
     }
     BORA_TRY( cudaEventRecord( h0->ev_step[1], st ) );
     BORA_TRY( cudaEventSynchronize( h0->ev_step[1] ) );
     float gms = 0.f;
     cudaEventElapsedTime( &gms, h0->ev_step[0], h0->ev_step[1] );
-    const double wall = std::chrono::duration<double, std::milli>( std::chrono::steady_clock::now() - t0 ).count();
+    const auto t3 = std::chrono::steady_clock::now();
+    auto ms = []( std::chrono::steady_clock::time_point x, std::chrono::steady_clock::time_point y ) {
+        return std::chrono::duration<double, std::milli>( y - x ).count();
+    };
     for( BatchMember& b : M )
     {
-        b.s->stats.gpu_ms = gms;
-        b.s->stats.steps++;
-        b.s->stats.stage_ms[7] = wall;
+        bora_flip_stats& o = b.s->stats;
+        o.gpu_ms = gms;
+        o.steps++;
+        for( double& v : o.stage_ms ) v = 0.0;
+        o.stage_ms[0] = ms( t0, t1 );  // the batch's stages before the solve
+        o.stage_ms[3] = ms( t1, t2 );  // the batched solve
+        o.stage_ms[5] = ms( t2, t3 );  // the stages after it
+        o.stage_ms[7] = ms( t0, t3 );
         b.s->batching = false;
     }
     for( int k : solo )
     {
-        hs[k]->st = own[k];
         hs[k]->batching = false;
         status[k] = bora_flip_step( hs[k], dt );
-        hs[k]->st = st;
     }
     return BORA_OK;
 }

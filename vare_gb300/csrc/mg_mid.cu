@@ -438,13 +438,13 @@ __device__ __forceinline__ void mg_mid_body( const MidDesc& d )
 
 __global__ void __launch_bounds__( kMidThreads, 1 ) k_mg_mid( const __grid_constant__ MidDesc d ) { mg_mid_body( d ); }
 
-// Batched: one cluster per simulation of the batch (all clusters of the same size).
+// Batched: one cluster per simulation taking part (all clusters of the same size; a
+// simulation's offset in the launch is a multiple of it, so a cluster is one simulation's).
 __global__ void __launch_bounds__( kMidThreads, 1 ) k_mg_mid_batch( const MidDesc* __restrict__ descs,
-                                                                    const BoraMemberSlots* __restrict__ sl )
+                                                                    const __grid_constant__ BoraBatchLaunch L )
 {
-    const unsigned c = blockIdx.x / cg::this_cluster().num_blocks();
-    if( !sl[c].active ) return;  // every CTA of the cluster returns: no barrier is pending
-    mg_mid_body( descs[c] );
+    unsigned bid;
+    mg_mid_body( descs[bora_batch_member( L, blockIdx.x, &bid )] );
 }
 
 // Cluster size: 16 CTAs where the device co-schedules such a cluster of this kernel with
@@ -612,12 +612,12 @@ int bora_mg_mid_describe( const BoraGridDev& g, const BoraLevelDev* levels, int 
     return 1;
 }
 
-void bora_mg_mid_launch_batch( const void* descs, const BoraMemberSlots* slots, int n, int ctas, size_t smem,
+void bora_mg_mid_launch_batch( const void* descs, const BoraBatchLaunch& L, int blocks, int ctas, size_t smem,
                                cudaStream_t st )
 {
-    if( n <= 0 ) return;
+    if( blocks <= 0 || ctas <= 0 || blocks % ctas ) return;
     cudaLaunchConfig_t cfg{};
-    cfg.gridDim = dim3( ctas * n );
+    cfg.gridDim = dim3( blocks );
     cfg.blockDim = dim3( kMidThreads );
     cfg.dynamicSmemBytes = smem;
     cfg.stream = st;
@@ -630,5 +630,5 @@ void bora_mg_mid_launch_batch( const void* descs, const BoraMemberSlots* slots, 
     attr[1].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 2;
-    cudaLaunchKernelEx( &cfg, k_mg_mid_batch, static_cast<const MidDesc*>( descs ), slots );
+    cudaLaunchKernelEx( &cfg, k_mg_mid_batch, static_cast<const MidDesc*>( descs ), L );
 }

@@ -988,18 +988,18 @@ __global__ void __launch_bounds__( TileRegion<E>::NT, TileRegion<E>::MINB ) k_mg
     mg_down_fused_body<E, L0>( F, C, t, ntiles, r0, slot_rr, ring, blockIdx.x, gridDim.x );
 }
 
-// Batched: simulation blockIdx.y, level l = 0, 1, 2 (E = 8, 4, 2) of its hierarchy.
+// Batched: level l = 0, 1, 2 (E = 8, 4, 2) of each simulation's hierarchy.
 template <int E, bool L0>
 __global__ void __launch_bounds__( TileRegion<E>::NT, TileRegion<E>::MINB )
-    k_mg_down_fused_batch( const BoraMemberSolve* __restrict__ ms, const BoraMemberSlots* __restrict__ sl )
+    k_mg_down_fused_batch( const __grid_constant__ BoraBatchLaunch L )
 {
     constexpr int l = E == 8 ? 0 : ( E == 4 ? 1 : 2 );
-    const BoraMemberSolve& m = ms[blockIdx.y];
-    const BoraMemberSlots& q = sl[blockIdx.y];
-    const int G = m.grid[kGridDown8 + l];
-    if( !q.active || (int)blockIdx.x >= G ) return;
+    unsigned bid;
+    const int k = bora_batch_member( L, blockIdx.x, &bid );
+    const BoraMemberSolve& m = L.ms[k];
+    const BoraMemberSlots& q = L.sl[k];
     mg_down_fused_body<E, L0>( m.L[l], m.L[l + 1], BoraTilesDev{ nullptr, nullptr, m.nbr }, m.ntiles,
-                               L0 ? m.sv.r : nullptr, q.rr, m.red.ring, blockIdx.x, G );
+                               L0 ? m.sv.r : nullptr, q.rr, m.red.ring, (int)bid, m.grid[kGridDown8 + l] );
 }
 
 template <int E, bool L0>
@@ -1172,21 +1172,21 @@ __global__ void __launch_bounds__( TileRegion<E>::NT, TileRegion<E>::MINB ) k_mg
     mg_up_fused_body<E, L0>( F, ec, t, ntiles, r0, slot_rr, red, zout, slot_rz, blockIdx.x, gridDim.x );
 }
 
-// Batched: simulation blockIdx.y; the coarser level's correction is its z1 after a fused
-// up kernel (levels 1 and 2 below levels 0 and 1), and level 3's z0 below level 2 (left
-// there by the coarse cluster kernel).
+// Batched: the coarser level's correction is its z1 after a fused up kernel (levels 1 and 2
+// below levels 0 and 1), and level 3's z0 below level 2 (left there by the coarse cluster
+// kernel).
 template <int E, bool L0>
 __global__ void __launch_bounds__( TileRegion<E>::NT, TileRegion<E>::MINB )
-    k_mg_up_fused_batch( const BoraMemberSolve* __restrict__ ms, const BoraMemberSlots* __restrict__ sl )
+    k_mg_up_fused_batch( const __grid_constant__ BoraBatchLaunch L )
 {
     constexpr int l = E == 8 ? 0 : ( E == 4 ? 1 : 2 );
-    const BoraMemberSolve& m = ms[blockIdx.y];
-    const BoraMemberSlots& q = sl[blockIdx.y];
-    const int G = m.grid[kGridUp8 + l];
-    if( !q.active || (int)blockIdx.x >= G ) return;
+    unsigned bid;
+    const int k = bora_batch_member( L, blockIdx.x, &bid );
+    const BoraMemberSolve& m = L.ms[k];
+    const BoraMemberSlots& q = L.sl[k];
     const __half* ec = l < 2 ? m.L[l + 1].z1 : m.z3;
     mg_up_fused_body<E, L0>( m.L[l], ec, BoraTilesDev{ nullptr, nullptr, m.nbr }, m.ntiles, L0 ? m.sv.r : nullptr, q.rr,
-                             m.red, L0 ? m.sv.z : nullptr, q.rz, blockIdx.x, G );
+                             m.red, L0 ? m.sv.z : nullptr, q.rz, (int)bid, m.grid[kGridUp8 + l] );
 }
 
 
@@ -1222,14 +1222,14 @@ __global__ void __launch_bounds__( 256 ) k_pcg_update_noprec( size_t ncells, Bor
     pcg_update_noprec_body( ncells, sv, red, slot_rz, slot_dq, slot_rr_out, blockIdx.x, gridDim.x );
 }
 
-__global__ void __launch_bounds__( 256 ) k_pcg_update_noprec_batch( const BoraMemberSolve* __restrict__ ms,
-                                                                    const BoraMemberSlots* __restrict__ sl )
+__global__ void __launch_bounds__( 256 ) k_pcg_update_noprec_batch( const __grid_constant__ BoraBatchLaunch L )
 {
-    const BoraMemberSolve& m = ms[blockIdx.y];
-    const BoraMemberSlots& q = sl[blockIdx.y];
-    const unsigned G = (unsigned)m.grid[kGridUpd];
-    if( !q.active || blockIdx.x >= G ) return;
-    pcg_update_noprec_body( (size_t)m.ntiles * 512, m.sv, m.red, q.rz_in, q.dq_in, q.rr_out, blockIdx.x, G );
+    unsigned bid;
+    const int k = bora_batch_member( L, blockIdx.x, &bid );
+    const BoraMemberSolve& m = L.ms[k];
+    const BoraMemberSlots& q = L.sl[k];
+    pcg_update_noprec_body( (size_t)m.ntiles * 512, m.sv, m.red, q.rz_in, q.dq_in, q.rr_out, bid,
+                            (unsigned)m.grid[kGridUpd] );
 }
 
 int sm_count()
@@ -1498,28 +1498,26 @@ void bora_member_grids( int ntiles, int* grid )
     grid[kGridUp2] = fused_grid( k_mg_up_fused<2, false>, TileRegion<2>::NT, ntiles, u2 );
 }
 
-void bora_launch_pcg_update_noprec_batch( const BoraMemberSolve* ms, const BoraMemberSlots* sl, int n, int gx,
-                                          cudaStream_t st )
+void bora_launch_pcg_update_noprec_batch( const BoraBatchLaunch& L, int blocks, cudaStream_t st )
 {
-    if( n > 0 && gx > 0 ) bora_launch_pdl( k_pcg_update_noprec_batch, dim3( gx, n ), dim3( 256 ), 0, st, ms, sl );
+    if( blocks > 0 ) bora_launch_pdl( k_pcg_update_noprec_batch, dim3( blocks ), dim3( 256 ), 0, st, L );
 }
 
-void bora_launch_mg_fused_batch( bool up, int l, const BoraMemberSolve* ms, const BoraMemberSlots* sl, int n, int gx,
-                                 cudaStream_t st )
+void bora_launch_mg_fused_batch( bool up, int l, const BoraBatchLaunch& L, int blocks, cudaStream_t st )
 {
-    if( n <= 0 || gx <= 0 ) return;
-    const dim3 grid( gx, n );
+    if( blocks <= 0 ) return;
+    const dim3 grid( blocks );
     if( !up )
     {
-        if( l == 0 ) bora_launch_pdl( k_mg_down_fused_batch<8, true>, grid, dim3( TileRegion<8>::NT ), 0, st, ms, sl );
-        else if( l == 1 ) bora_launch_pdl( k_mg_down_fused_batch<4, false>, grid, dim3( TileRegion<4>::NT ), 0, st, ms, sl );
-        else bora_launch_pdl( k_mg_down_fused_batch<2, false>, grid, dim3( TileRegion<2>::NT ), 0, st, ms, sl );
+        if( l == 0 ) bora_launch_pdl( k_mg_down_fused_batch<8, true>, grid, dim3( TileRegion<8>::NT ), 0, st, L );
+        else if( l == 1 ) bora_launch_pdl( k_mg_down_fused_batch<4, false>, grid, dim3( TileRegion<4>::NT ), 0, st, L );
+        else bora_launch_pdl( k_mg_down_fused_batch<2, false>, grid, dim3( TileRegion<2>::NT ), 0, st, L );
     }
     else
     {
-        if( l == 0 ) bora_launch_pdl( k_mg_up_fused_batch<8, true>, grid, dim3( TileRegion<8>::NT ), 0, st, ms, sl );
-        else if( l == 1 ) bora_launch_pdl( k_mg_up_fused_batch<4, false>, grid, dim3( TileRegion<4>::NT ), 0, st, ms, sl );
-        else bora_launch_pdl( k_mg_up_fused_batch<2, false>, grid, dim3( TileRegion<2>::NT ), 0, st, ms, sl );
+        if( l == 0 ) bora_launch_pdl( k_mg_up_fused_batch<8, true>, grid, dim3( TileRegion<8>::NT ), 0, st, L );
+        else if( l == 1 ) bora_launch_pdl( k_mg_up_fused_batch<4, false>, grid, dim3( TileRegion<4>::NT ), 0, st, L );
+        else bora_launch_pdl( k_mg_up_fused_batch<2, false>, grid, dim3( TileRegion<2>::NT ), 0, st, L );
     }
 }
 

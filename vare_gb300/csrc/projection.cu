@@ -603,16 +603,15 @@ __global__ void __launch_bounds__( 32 * kDirWarps ) k_pcg_direction( int ntiles,
                         blockIdx.x, gridDim.x );
 }
 
-// Batched: simulation blockIdx.y of the batch, on its own grid of m.grid[kGridDir] blocks.
-__global__ void __launch_bounds__( 32 * kDirWarps ) k_pcg_direction_batch( const BoraMemberSolve* __restrict__ ms,
-                                                                          const BoraMemberSlots* __restrict__ sl )
+// Batched: each simulation on its own grid of m.grid[kGridDir] blocks.
+__global__ void __launch_bounds__( 32 * kDirWarps ) k_pcg_direction_batch( const __grid_constant__ BoraBatchLaunch L )
 {
-    const BoraMemberSolve& m = ms[blockIdx.y];
-    const BoraMemberSlots& q = sl[blockIdx.y];
-    const unsigned G = (unsigned)m.grid[kGridDir];
-    if( !q.active || blockIdx.x >= G ) return;
-    pcg_direction_body( m.ntiles, m.nbr, m.code, m.sv, q.dsel, m.red, q.rz_new, q.rz_old, q.dq, q.a_rz, q.a_dq,
-                        blockIdx.x, G );
+    unsigned bid;
+    const int k = bora_batch_member( L, blockIdx.x, &bid );
+    const BoraMemberSolve& m = L.ms[k];
+    const BoraMemberSlots& q = L.sl[k];
+    pcg_direction_body( m.ntiles, m.nbr, m.code, m.sv, q.dsel, m.red, q.rz_new, q.rz_old, q.dq, q.a_rz, q.a_dq, bid,
+                        (unsigned)m.grid[kGridDir] );
 }
 
 // ---------------------------------------------------------------------------------
@@ -643,13 +642,13 @@ __global__ void k_solve_init( size_t ncells, const float* __restrict__ b, BoraSo
     solve_init_body( ncells, b, sv, red, slot_norm2, slot_max, blockIdx.x, gridDim.x );
 }
 
-__global__ void k_solve_init_batch( const BoraMemberSolve* __restrict__ ms, const BoraMemberSlots* __restrict__ sl )
+__global__ void k_solve_init_batch( const __grid_constant__ BoraBatchLaunch L )
 {
-    const BoraMemberSolve& m = ms[blockIdx.y];
-    const BoraMemberSlots& q = sl[blockIdx.y];
-    const unsigned G = (unsigned)m.grid[kGridCells];
-    if( !q.active || blockIdx.x >= G ) return;
-    solve_init_body( (size_t)m.ntiles * 512, m.b, m.sv, m.red, q.n2, q.mx, blockIdx.x, G );
+    unsigned bid;
+    const int k = bora_batch_member( L, blockIdx.x, &bid );
+    const BoraMemberSolve& m = L.ms[k];
+    const BoraMemberSlots& q = L.sl[k];
+    solve_init_body( (size_t)m.ntiles * 512, m.b, m.sv, m.red, q.n2, q.mx, bid, (unsigned)m.grid[kGridCells] );
 }
 
 // x += e (+ the last update's pending alpha d), then clear e and q; the direction d is kept
@@ -683,13 +682,14 @@ __global__ void k_refine_accumulate( size_t ncells, const uint16_t* __restrict__
     refine_accumulate_body( ncells, code, sv, dsel, ring, slot_a_rz, slot_a_dq, blockIdx.x, gridDim.x );
 }
 
-__global__ void k_refine_accumulate_batch( const BoraMemberSolve* __restrict__ ms, const BoraMemberSlots* __restrict__ sl )
+__global__ void k_refine_accumulate_batch( const __grid_constant__ BoraBatchLaunch L )
 {
-    const BoraMemberSolve& m = ms[blockIdx.y];
-    const BoraMemberSlots& q = sl[blockIdx.y];
-    const unsigned G = (unsigned)m.grid[kGridCells];
-    if( !q.active || blockIdx.x >= G ) return;
-    refine_accumulate_body( (size_t)m.ntiles * 512, m.code, m.sv, q.dsel, m.red.ring, q.a_rz, q.a_dq, blockIdx.x, G );
+    unsigned bid;
+    const int k = bora_batch_member( L, blockIdx.x, &bid );
+    const BoraMemberSolve& m = L.ms[k];
+    const BoraMemberSlots& q = L.sl[k];
+    refine_accumulate_body( (size_t)m.ntiles * 512, m.code, m.sv, q.dsel, m.red.ring, q.a_rz, q.a_dq, bid,
+                            (unsigned)m.grid[kGridCells] );
 }
 
 // r = b - A x in double-float arithmetic (A from the stencil code, x the double-float
@@ -738,14 +738,14 @@ __global__ void __launch_bounds__( 256 ) k_refine_residual( size_t ncells, const
     refine_residual_body( ncells, nbr, b, code, sv, red, slot_norm2, slot_max, blockIdx.x, gridDim.x );
 }
 
-__global__ void __launch_bounds__( 256 ) k_refine_residual_batch( const BoraMemberSolve* __restrict__ ms,
-                                                                  const BoraMemberSlots* __restrict__ sl )
+__global__ void __launch_bounds__( 256 ) k_refine_residual_batch( const __grid_constant__ BoraBatchLaunch L )
 {
-    const BoraMemberSolve& m = ms[blockIdx.y];
-    const BoraMemberSlots& q = sl[blockIdx.y];
-    const unsigned G = (unsigned)m.grid[kGridResidual];
-    if( !q.active || blockIdx.x >= G ) return;
-    refine_residual_body( (size_t)m.ntiles * 512, m.nbr, m.b, m.code, m.sv, m.red, q.n2, q.mx, blockIdx.x, G );
+    unsigned bid;
+    const int k = bora_batch_member( L, blockIdx.x, &bid );
+    const BoraMemberSolve& m = L.ms[k];
+    const BoraMemberSlots& q = L.sl[k];
+    refine_residual_body( (size_t)m.ntiles * 512, m.nbr, m.b, m.code, m.sv, m.red, q.n2, q.mx, bid,
+                          (unsigned)m.grid[kGridResidual] );
 }
 
 __global__ void k_write_pressure( size_t ncells, const uint16_t* __restrict__ code, const float2* __restrict__ x,
@@ -755,13 +755,13 @@ __global__ void k_write_pressure( size_t ncells, const uint16_t* __restrict__ co
         pres[i] = ( code[i] & BORA_CODE_FLUID ) ? x[i].x + x[i].y : 0.f;
 }
 
-__global__ void k_write_pressure_batch( const BoraMemberSolve* __restrict__ ms )
+__global__ void k_write_pressure_batch( const __grid_constant__ BoraBatchLaunch L )
 {
-    const BoraMemberSolve& m = ms[blockIdx.y];
+    unsigned bid;
+    const BoraMemberSolve& m = L.ms[bora_batch_member( L, blockIdx.x, &bid )];
     const unsigned G = (unsigned)m.grid[kGridCells];
-    if( blockIdx.x >= G ) return;
     const size_t ncells = (size_t)m.ntiles * 512;
-    for( size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < ncells; i += (size_t)G * blockDim.x )
+    for( size_t i = bid * (size_t)blockDim.x + threadIdx.x; i < ncells; i += (size_t)G * blockDim.x )
         m.pres[i] = ( m.code[i] & BORA_CODE_FLUID ) ? m.sv.x[i].x + m.sv.x[i].y : 0.f;
 }
 
@@ -937,32 +937,29 @@ void bora_projection_grids( int ntiles, int* grid )
     grid[kGridResidual] = residual_grid( nc );
 }
 
-void bora_launch_solve_init_batch( const BoraMemberSolve* ms, const BoraMemberSlots* sl, int n, int gx, cudaStream_t st )
+void bora_launch_solve_init_batch( const BoraBatchLaunch& L, int blocks, cudaStream_t st )
 {
-    if( n > 0 && gx > 0 ) k_solve_init_batch<<<dim3( gx, n ), 256, 0, st>>>( ms, sl );
+    if( blocks > 0 ) k_solve_init_batch<<<blocks, 256, 0, st>>>( L );
 }
 
-void bora_launch_pcg_direction_batch( const BoraMemberSolve* ms, const BoraMemberSlots* sl, int n, int gx,
-                                      cudaStream_t st )
+void bora_launch_pcg_direction_batch( const BoraBatchLaunch& L, int blocks, cudaStream_t st )
 {
-    if( n > 0 && gx > 0 ) bora_launch_pdl( k_pcg_direction_batch, dim3( gx, n ), dim3( 32 * kDirWarps ), 0, st, ms, sl );
+    if( blocks > 0 ) bora_launch_pdl( k_pcg_direction_batch, dim3( blocks ), dim3( 32 * kDirWarps ), 0, st, L );
 }
 
-void bora_launch_refine_accumulate_batch( const BoraMemberSolve* ms, const BoraMemberSlots* sl, int n, int gx,
-                                          cudaStream_t st )
+void bora_launch_refine_accumulate_batch( const BoraBatchLaunch& L, int blocks, cudaStream_t st )
 {
-    if( n > 0 && gx > 0 ) k_refine_accumulate_batch<<<dim3( gx, n ), 256, 0, st>>>( ms, sl );
+    if( blocks > 0 ) k_refine_accumulate_batch<<<blocks, 256, 0, st>>>( L );
 }
 
-void bora_launch_refine_residual_batch( const BoraMemberSolve* ms, const BoraMemberSlots* sl, int n, int gx,
-                                        cudaStream_t st )
+void bora_launch_refine_residual_batch( const BoraBatchLaunch& L, int blocks, cudaStream_t st )
 {
-    if( n > 0 && gx > 0 ) k_refine_residual_batch<<<dim3( gx, n ), 256, 0, st>>>( ms, sl );
+    if( blocks > 0 ) k_refine_residual_batch<<<blocks, 256, 0, st>>>( L );
 }
 
-void bora_launch_write_pressure_batch( const BoraMemberSolve* ms, int n, int gx, cudaStream_t st )
+void bora_launch_write_pressure_batch( const BoraBatchLaunch& L, int blocks, cudaStream_t st )
 {
-    if( n > 0 && gx > 0 ) k_write_pressure_batch<<<dim3( gx, n ), 256, 0, st>>>( ms );
+    if( blocks > 0 ) k_write_pressure_batch<<<blocks, 256, 0, st>>>( L );
 }
 
 void bora_launch_pcg_direction( const BoraGridDev&, int ntiles, BoraTilesDev t, const uint16_t* code, BoraSolverDev s,

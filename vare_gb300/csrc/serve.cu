@@ -1,9 +1,10 @@
 // Serving layer: continuous admission of independent FLIP simulations on one GPU under a
 // device-memory budget (include/bora_serve.h). Host code only: a scheduler thread admits
-// queued requests as slots and memory free up; a stepper thread keeps every admitted
-// request as a bora_flip handle and advances all running requests together, one
-// bora_flip_step_batch per round (the pressure solve's kernels launched once for all of
-// them), taking newly admitted requests in between rounds.
+// queued requests as slots and memory free up and sets up each one's bora_flip handle; a
+// stepper thread advances all running requests together, one bora_flip_step_batch per
+// round (the pressure solve's kernels launched once for all of them), taking newly set-up
+// requests in between rounds; a finisher thread orders finished requests' particles by id,
+// so neither set-up nor result handling holds up a round.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -36,6 +37,7 @@ struct Request
     int space = BORA_SPACE_VOXEL, steps = 0;
     float dt = 0.f;
     int state = BORA_REQ_QUEUED, status = BORA_OK, steps_done = 0;
+    bora_flip_handle h = nullptr;  // from set-up until the stepper has read the results back
     uint64_t nparticles = 0, estimate = 0, device_bytes = 0;
     Clock::time_point t_submit, t_admit, t_done;
     std::vector<float> step_ms;
@@ -68,17 +70,34 @@ struct bora_server
     uint64_t submitted = 0, admitted = 0, done = 0, failed = 0, particle_steps = 0, steps = 0;
     std::vector<float> step_ms;  // every step of every finished request
     bool stop = false;
-    std::thread scheduler, stepper;
-    std::vector<Request*> starting;  // admitted, not yet taken by the stepper
+    std::thread scheduler, stepper, finisher;
+    std::vector<Request*> starting;  // set up, not yet taken by the stepper
+    struct Finished
+    {
+        Request* r;
+        std::vector<float> pos, vel;
+        std::vector<int32_t> ids;
+        uint64_t psteps;
+        int status;
+    };
+    std::deque<Finished> finishing;  // read back, waiting for the finisher
+    bool stepper_done = false;
 
     void schedule();
     void step_loop();
+    void finish_loop();
     void finish( Request* r, int status, bool ok );
+    void finish_locked( Request* r, int status, bool ok );
 };
 
 void bora_server::finish( Request* r, int status, bool ok )
 {
     std::lock_guard<std::mutex> lk( mu );
+    finish_locked( r, status, ok );
+}
+
+void bora_server::finish_locked( Request* r, int status, bool ok )
+{
     r->state = ok ? BORA_REQ_DONE : BORA_REQ_FAILED;
     r->status = status;
     r->t_done = Clock::now();
@@ -119,33 +138,63 @@ int start_request( Request* r, bora_flip_handle* out )
     return st;
 }
 
-// The final particles in ascending id order (the result does not depend on the device order).
-int collect( Request* r, bora_flip_handle h, std::vector<float>& p2, std::vector<float>& v2, std::vector<int32_t>& i2 )
+// The final particles as the device holds them (any order).
+int read_back( bora_flip_handle h, int space, std::vector<float>& pos, std::vector<float>& vel, std::vector<int32_t>& ids )
 {
     size_t n = 0;
     int st = bora_flip_num_particles( h, &n );
     if( st != BORA_OK ) return st;
-    std::vector<float> pos( n * 3 ), vel( n * 3 );
-    std::vector<int32_t> ids( n );
+    pos.resize( n * 3 );
+    vel.resize( n * 3 );
+    ids.resize( n );
     size_t got = 0;
-    st = bora_flip_get_particles( h, pos.data(), vel.data(), nullptr, ids.data(), n, &got, r->space );
-    if( st != BORA_OK ) return st;
-    std::vector<size_t> ord( got );
-    for( size_t i = 0; i < got; ++i ) ord[i] = i;
-    std::sort( ord.begin(), ord.end(), [&]( size_t a, size_t b ) { return ids[a] < ids[b]; } );
-    p2.resize( got * 3 );
-    v2.resize( got * 3 );
-    i2.resize( got );
-    for( size_t i = 0; i < got; ++i )
-    {
-        std::memcpy( &p2[3 * i], &pos[3 * ord[i]], 12 );
-        std::memcpy( &v2[3 * i], &vel[3 * ord[i]], 12 );
-        i2[i] = ids[ord[i]];
-    }
-    return BORA_OK;
+    st = bora_flip_get_particles( h, pos.data(), vel.data(), nullptr, ids.data(), n, &got, space );
+    pos.resize( got * 3 );
+    vel.resize( got * 3 );
+    ids.resize( got );
+    return st;
 }
 
 }  // namespace
+
+// Results in ascending id order (the result does not depend on the device order).
+void bora_server::finish_loop()
+{
+    for( ;; )
+    {
+        Finished f;
+        {
+            std::unique_lock<std::mutex> lk( mu );
+            cv.wait( lk, [&] { return !finishing.empty() || stepper_done; } );
+            if( finishing.empty() ) return;
+            f = std::move( finishing.front() );
+            finishing.pop_front();
+        }
+        const size_t got = f.ids.size();
+        std::vector<size_t> ord( got );
+        for( size_t i = 0; i < got; ++i ) ord[i] = i;
+        std::sort( ord.begin(), ord.end(), [&]( size_t a, size_t b ) { return f.ids[a] < f.ids[b]; } );
+        std::vector<float> p2( got * 3 ), v2( got * 3 );
+        std::vector<int32_t> i2( got );
+        for( size_t i = 0; i < got; ++i )
+        {
+            std::memcpy( &p2[3 * i], &f.pos[3 * ord[i]], 12 );
+            std::memcpy( &v2[3 * i], &f.vel[3 * ord[i]], 12 );
+            i2[i] = f.ids[ord[i]];
+        }
+        std::lock_guard<std::mutex> lk( mu );
+        Request* r = f.r;
+        if( f.status == BORA_OK )
+        {
+            r->pos.swap( p2 );
+            r->vel.swap( v2 );
+            r->ids.swap( i2 );
+            r->nparticles = r->ids.size();
+            particle_steps += f.psteps;
+        }
+        finish_locked( r, f.status, f.status == BORA_OK );
+    }
+}
 
 void bora_server::step_loop()
 {
@@ -163,20 +212,27 @@ void bora_server::step_loop()
         }
         if( stopping )  // running requests are abandoned
         {
-            for( Request* r : fresh ) finish( r, BORA_ERR_CAPACITY, false );
+            for( Request* r : fresh )
+            {
+                bora_flip_destroy( r->h );
+                r->h = nullptr;
+                finish( r, BORA_ERR_CAPACITY, false );
+            }
             for( Live& l : live )
             {
                 bora_flip_destroy( l.h );
                 finish( l.r, BORA_ERR_CAPACITY, false );
             }
+            std::lock_guard<std::mutex> lk( mu );
+            stepper_done = true;
+            cv.notify_all();
             return;
         }
         for( Request* r : fresh )
         {
             Live l;
             l.r = r;
-            const int st = start_request( r, &l.h );
-            if( st != BORA_OK ) { finish( r, st, false ); continue; }
+            l.h = r->h;
             live.push_back( l );
         }
         if( live.empty() ) continue;
@@ -230,20 +286,15 @@ void bora_server::step_loop()
                 continue;
             }
             if( l.r->steps_done < l.r->steps ) { keep.push_back( l ); continue; }
-            std::vector<float> p2, v2;
-            std::vector<int32_t> i2;
-            const int st = collect( l.r, l.h, p2, v2, i2 );
+            Finished f;
+            f.r = l.r;
+            f.psteps = l.psteps;
+            f.status = read_back( l.h, l.r->space, f.pos, f.vel, f.ids );
             bora_flip_destroy( l.h );
-            if( st == BORA_OK )
-            {
-                std::lock_guard<std::mutex> lk( mu );
-                l.r->pos.swap( p2 );
-                l.r->vel.swap( v2 );
-                l.r->ids.swap( i2 );
-                l.r->nparticles = l.r->ids.size();
-                particle_steps += l.psteps;
-            }
-            finish( l.r, st, st == BORA_OK );
+            std::lock_guard<std::mutex> lk( mu );
+            l.r->h = nullptr;
+            finishing.push_back( std::move( f ) );
+            cv.notify_all();
         }
         live.swap( keep );
     }
@@ -281,6 +332,18 @@ void bora_server::schedule()
         reserved += r->estimate;
         running_peak = std::max( running_peak, running );
         reserved_peak = std::max( reserved_peak, reserved );
+        // the request's simulation is set up here, outside the lock, while rounds go on
+        lk.unlock();
+        bora_flip_handle h = nullptr;
+        const int st = start_request( r, &h );
+        lk.lock();
+        if( st == BORA_OK && stop ) { bora_flip_destroy( h ); h = nullptr; }
+        if( st != BORA_OK || stop )
+        {
+            finish_locked( r, st != BORA_OK ? st : BORA_ERR_CAPACITY, false );
+            continue;
+        }
+        r->h = h;
         starting.push_back( r );
         cv.notify_all();
     }
@@ -339,6 +402,7 @@ int bora_serve_create( const bora_serve_config* cfg, bora_serve_handle* out )
     cudaGetDevice( &s->device );
     s->scheduler = std::thread( [s] { s->schedule(); } );
     s->stepper = std::thread( [s] { s->step_loop(); } );
+    s->finisher = std::thread( [s] { s->finish_loop(); } );
     *out = s;
     return BORA_OK;
 }
@@ -353,6 +417,7 @@ int bora_serve_destroy( bora_serve_handle s )
     s->cv.notify_all();
     if( s->scheduler.joinable() ) s->scheduler.join();
     if( s->stepper.joinable() ) s->stepper.join();
+    if( s->finisher.joinable() ) s->finisher.join();
     delete s;
     return BORA_OK;
 }
