@@ -24,12 +24,12 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libbora_flip.so")
 
-SOURCES = ["scan.cu", "grid_build.cu", "p2g.cu", "projection.cu", "multigrid.cu", "mg_mid.cu", "g2p.cu", "surface.cu",
+SOURCES = ["scan.cu", "grid_build.cu", "p2g.cu", "projection.cu", "multigrid.cu", "mg_mid.cu", "mg_passes.cu", "g2p.cu", "surface.cu",
            "vdb_export.cu", "flip_api.cu", "serve.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
               "--expt-relaxed-constexpr", "-Xcudafe", "--diag_suppress=177"]
-CONTRACT = {"multigrid.cu", "mg_mid.cu"}  # translation units compiled with -fmad=true
+CONTRACT = {"multigrid.cu", "mg_mid.cu", "mg_passes.cu"}  # translation units compiled with -fmad=true
 
 
 def nvcc() -> str:

@@ -229,6 +229,17 @@ struct BoraLevelDev
     __half* z1;        // correction after prolongation + one sweep
 };
 
+// The tiled levels' passes of a V-cycle (mg_passes.cu): level l (E = 8, 4 or 2) pre-smoothed
+// and restricted into level l + 1's r (down), or prolonged from the coarser correction ec and
+// post-smoothed (up: level 0 into the PCG's z with r.z -> slot_rz, the others into z1).
+// scratch: an FP32 vector of level 0's size.
+int bora_mg_pass_grid( int E, int ntiles );
+void bora_mg_pass_down( const BoraLevelDev* levels, int l, const BoraTilesDev& t, int ntiles, const float* r0,
+                        float* scratch, const BoraReduceDev& red, int slot_rr, cudaStream_t st );
+void bora_mg_pass_up( const BoraLevelDev* levels, int l, const __half* ec, const BoraTilesDev& t, int ntiles,
+                      const float* r0, float* scratch, const BoraReduceDev& red, int slot_rr, float* z, int slot_rz,
+                      cudaStream_t st );
+
 // Cell types and stencil codes of level c from level c-1 (levels[0] = fine, given).
 // mid_image: the buffer for the coarse levels' cluster image (bora_mg_mid_image_bytes), or null
 void bora_mg_setup( const BoraGridDev& g, BoraLevelDev* levels, int nlevels, BoraTilesDev t, void* mid_image,
@@ -249,8 +260,8 @@ void bora_mg_mid_setup( const BoraGridDev& g, const BoraLevelDev* levels, int nl
 int bora_mg_mid_vcycle( const BoraGridDev& g, const BoraLevelDev* levels, int nlevels, BoraTilesDev t, int ntiles,
                         const void* image, uint32_t* err, int sweeps, cudaStream_t st, bool launch );
 void bora_mg_vcycle( const BoraGridDev& g, const BoraLevelDev* levels, int nlevels, BoraTilesDev t, const void* mid_image,
-                     const float* r, float* z, BoraReduceDev red, int slot_rr, int slot_rz, int coarse_sweeps,
-                     cudaStream_t st );
+                     const float* r, float* z, float* scratch, BoraReduceDev red, int slot_rr, int slot_rz,
+                     int coarse_sweeps, cudaStream_t st );
 // ---- batched solve: several simulations, one launch per kernel ---------------------------
 // A batched launch packs the blocks of the simulations taking part back to back into one
 // 1-D grid: simulation k owns blocks start[k] .. start[k+1] - 1, exactly the grid its own
@@ -260,7 +271,8 @@ void bora_mg_vcycle( const BoraGridDev& g, const BoraLevelDev* levels, int nleve
 // any batch, and no block of a batched launch idles. Arguments come from device arrays.
 enum BoraMemberGrid
 {
-    kGridDir = 0, kGridUpd, kGridCells, kGridResidual, kGridDown8, kGridDown4, kGridDown2, kGridUp8, kGridUp4, kGridUp2,
+    kGridDir = 0, kGridUpd, kGridCells, kGridResidual,
+    kGridPass0, kGridPass1, kGridPass2,  // the multigrid passes of levels 0, 1, 2 (mg_passes.cu)
     kGridCount
 };
 struct BoraMemberSolve
@@ -326,8 +338,8 @@ void bora_launch_refine_accumulate_batch( const BoraBatchLaunch& L, int blocks, 
 void bora_launch_refine_residual_batch( const BoraBatchLaunch& L, int blocks, cudaStream_t st );
 void bora_launch_write_pressure_batch( const BoraBatchLaunch& L, int blocks, cudaStream_t st );
 void bora_launch_pcg_update_noprec_batch( const BoraBatchLaunch& L, int blocks, cudaStream_t st );
-// one fused V-cycle kernel (down or up) of level l (0, 1, 2) for the batch
-void bora_launch_mg_fused_batch( bool up, int l, const BoraBatchLaunch& L, int blocks, cudaStream_t st );
+// pass `pass` (0, 1 down; 2, 3 up) of multigrid level l (0, 1, 2) for the batch
+void bora_launch_mg_pass_batch( int l, int pass, const BoraBatchLaunch& L, int blocks, cudaStream_t st );
 // this simulation's own grid per batched kernel (what its single launches use)
 void bora_member_grids( int ntiles, int* grid );
 void bora_projection_grids( int ntiles, int* grid );  // the kGridDir, kGridCells and kGridResidual entries

@@ -642,7 +642,8 @@ int stage_solve( bora_flip_sim* s )
         s->stats.mg_vcycle_launches = mixed ? vlaunch : 0;
         auto precondition = [&]( int rr_slot, int rz_slot ) {
             KTimer t( s, BORA_KERNEL_MG, vlaunch );
-            bora_mg_vcycle( s->g, s->levels, s->nlevels, s->tiles(), mid_img, sv.r, sv.z, red, rr_slot, rz_slot, 16, st );
+            bora_mg_vcycle( s->g, s->levels, s->nlevels, s->tiles(), mid_img, sv.r, sv.z, sv.minv, red, rr_slot, rz_slot, 16,
+                            st );
         };
         int rz_cur = s->slot(), rr_cur = s->slot();
         if( mixed )
@@ -1412,10 +1413,12 @@ int batch_solve( std::vector<BatchMember>& M, cudaStream_t st, BatchBuffers& bb,
     };
     auto launch = [&]( int q ) { return BoraBatchLaunch{ dms, dsl, dstart + q * ( n + 1 ), n }; };
     auto vcycle = [&]() {
-        for( int l = 0; l < 3; ++l ) bora_launch_mg_fused_batch( false, l, launch( kGridDown8 + l ), blocks[kGridDown8 + l], st );
+        for( int l = 0; l < 3; ++l )
+            for( int p = 0; p < 2; ++p ) bora_launch_mg_pass_batch( l, p, launch( kGridPass0 + l ), blocks[kGridPass0 + l], st );
         bora_mg_mid_launch_batch( bb.mid.p, launch( kGridCount ), blocks[kGridCount], ctas, smem, st );
-        for( int l = 2; l >= 0; --l ) bora_launch_mg_fused_batch( true, l, launch( kGridUp8 + l ), blocks[kGridUp8 + l], st );
-        launches += 7;
+        for( int l = 2; l >= 0; --l )
+            for( int p = 2; p < 4; ++p ) bora_launch_mg_pass_batch( l, p, launch( kGridPass0 + l ), blocks[kGridPass0 + l], st );
+        launches += 13;
     };
     // r = b, x = e = d = q = 0; ||b||^2, max|b|
     for( int k = 0; k < n; ++k )
@@ -1469,7 +1472,7 @@ int batch_solve( std::vector<BatchMember>& M, cudaStream_t st, BatchBuffers& bb,
             b.npend = 0;
             b.a_rz = b.a_dq = -1;
             b.inner_done = false;
-            b.s->stats.mg_vcycle_launches = 7;
+            b.s->stats.mg_vcycle_launches = 13;
             start = true;
         }
         if( start )

@@ -625,570 +625,8 @@ __global__ void __launch_bounds__( kTailThreads ) k_mg_tail( const __grid_consta
     }
 }
 
-// ---- fused per-tile kernels for tiled levels with E >= 2 ------------------------------
-//
-// Persistent CTAs walk the tiles; for each tile the CTA works on the tile plus a 2-cell
-// halo of its level, (E+4)^3 cells, staged in shared memory (cells in inactive tiles or
-// beyond the tile grid read as non-fluid, and non-fluid cells hold z = 0, so stencil sums
-// run over all six neighbours without branches). Every thread visits the same region
-// cells for every tile, so their tile direction and local index are computed once per
-// launch. The loads of the next tile are issued before the current tile's shared-memory
-// sweeps, and the neighbour table two tiles ahead, so that global latency stays off the
-// per-tile critical path. Down: two Jacobi sweeps from zero, the residual, and its
-// restriction to the tile's (E/2)^3 coarse cells. Up: prolongation of the coarse
-// correction, then two sweeps; on level 0 the result is unscaled into the FP32 z and r.z
-// is accumulated, coarser levels write their result to z1 (neighbouring CTAs still read
-// z0).
-
-template <int E>
-struct TileRegion
-{
-    static constexpr int LE = E == 8 ? 3 : ( E == 4 ? 2 : 1 );
-    static constexpr int R = E + 4;  // region edge (2-cell halo)
-    static constexpr int N = R * R * R;
-    static constexpr int Q = E + 2;  // inner region edge (1-cell halo)
-    static constexpr int NQ = Q * Q * Q;
-    static constexpr int E3 = E * E * E;
-    static constexpr int H = E / 2;
-    static constexpr int NT = E == 8 ? 256 : ( E == 4 ? 128 : 64 );  // threads per CTA
-    static constexpr int MINB = E == 8 ? 4 : 1024 / NT;                // resident CTAs per SM
-    static constexpr int IA = ( N + NT - 1 ) / NT;
-    static constexpr int IB = ( NQ + NT - 1 ) / NT;
-    static constexpr int IC = ( E3 + NT - 1 ) / NT;
-    static constexpr uint32_t kValid = 1u << 31, kInner = 1u << 30;
-    static constexpr uint32_t kCentre = 13;  // bora_dir( 0, 0, 0 )
-    // Region cell h: bits 0-8 local index in its tile, 9-14 parent's local index on the
-    // coarser level, 16-20 tile direction, kInner when inside the 1-cell-halo region.
-    __device__ static inline uint32_t region_map( int h )
-    {
-        if( h >= N ) return 0;
-        const int x = h % R, y = ( h / R ) % R, z = h / ( R * R );
-        const int a = x + E - 2, b = y + E - 2, c = z + E - 2;  // >= 0
-        const int la = a & ( E - 1 ), lb = b & ( E - 1 ), lc = c & ( E - 1 );
-        const uint32_t local = (uint32_t)( la + E * ( lb + E * lc ) );
-        const uint32_t parent = (uint32_t)( ( la >> 1 ) + H * ( ( lb >> 1 ) + H * ( lc >> 1 ) ) );
-        const uint32_t dir = (uint32_t)bora_dir( ( a >> LE ) - 1, ( b >> LE ) - 1, ( c >> LE ) - 1 );
-        const bool inner = x >= 1 && x <= R - 2 && y >= 1 && y <= R - 2 && z >= 1 && z <= R - 2;
-        return kValid | ( inner ? kInner : 0u ) | ( dir << 16 ) | ( parent << 9 ) | local;
-    }
-    __device__ static inline int qh( int h2 )  // region index of inner-region cell h2, or -1
-    {
-        if( h2 >= NQ ) return -1;
-        return ( h2 % Q + 1 ) + R * ( ( ( h2 / Q ) % Q + 1 ) + R * ( h2 / ( Q * Q ) + 1 ) );
-    }
-    __device__ static inline int th( int l )  // region index of tile cell l, or -1
-    {
-        if( l >= E3 ) return -1;
-        return ( l % E + 2 ) + R * ( ( ( l / E ) % E + 2 ) + R * ( l / ( E * E ) + 2 ) );
-    }
-    __device__ static inline int th2( int l )  // inner-region index of tile cell l
-    {
-        return ( l % E + 1 ) + Q * ( ( ( l / E ) % E + 1 ) + Q * ( l / ( E * E ) + 1 ) );
-    }
-    // slot of the region cell's tile for neighbour table nb, or -1
-    __device__ static inline int slot( const int32_t* nb, uint32_t m ) { return ( m & kValid ) ? nb[( m >> 16 ) & 31] : -1; }
-};
-
-// omega / diag for diag 0..15 (0 for diag 0: such cells keep z = 0): wd[0..15] with
-// kOmegaA, wd[16..31] with kOmegaB
-__device__ inline void init_wd( float* wd )
-{
-    const int d = threadIdx.x & 15;
-    if( threadIdx.x < 32 ) wd[threadIdx.x] = d ? ( threadIdx.x < 16 ? kOmegaA : kOmegaB ) / (float)d : 0.f;
-}
-
-// One damped Jacobi update of a cell from its six neighbours in the same array.
-template <int STRIDE_Y>
-__device__ inline float jacobi( const float* z, int h, uint16_t cc, float r, const float* wd )
-{
-    const float zc = z[h];
-    const float sum = ( z[h - 1] + z[h + 1] ) + ( z[h - STRIDE_Y] + z[h + STRIDE_Y] ) +
-                      ( z[h - STRIDE_Y * STRIDE_Y] + z[h + STRIDE_Y * STRIDE_Y] );
-    return ( cc & BORA_CODE_FLUID ) ? zc + wd[code_diag( cc )] * ( r - ( (float)code_diag( cc ) * zc - sum ) ) : 0.f;
-}
-
-// neighbour table entry tid (< 27) of tile s, or -1 past the last tile
-__device__ inline int32_t nbr_entry( const BoraTilesDev& t, int s, int ntiles, int tid )
-{
-    return s < ntiles ? t.nbr[(size_t)s * 27 + tid] : -1;
-}
-
-// Row-wise staging of the level-0 region (E = 8, 12^3 cells): one thread per region row
-// (12 cells along x: 2 from the -x neighbour tile, 8 from the middle tile, 2 from the +x
-// neighbour), loaded with vector loads (8 cells of a tile row are 16 B of codes and 32 B of
-// FP32 values, aligned) instead of one scalar load per cell.
-struct Row8
-{
-    int dl, dc, dr;  // tile directions of the row's three segments
-    uint32_t off;    // local index of the row's x = 0 cell in its tiles
-    uint32_t poff;   // local index of its parent on the 4^3 level
-    int h0;          // region index of the row's first cell
-    __device__ inline void init( int row )
-    {
-        const int b = row % 12, c = row / 12;
-        const int dy = b < 2 ? -1 : ( b >= 10 ? 1 : 0 ), dz = c < 2 ? -1 : ( c >= 10 ? 1 : 0 );
-        const int ly = ( b + 6 ) & 7, lz = ( c + 6 ) & 7;
-        dl = bora_dir( -1, dy, dz );
-        dc = bora_dir( 0, dy, dz );
-        dr = bora_dir( 1, dy, dz );
-        off = (uint32_t)( 8 * ly + 64 * lz );
-        poff = (uint32_t)( 4 * ( ly >> 1 ) + 16 * ( lz >> 1 ) );
-        h0 = 12 * row;
-    }
-};
-
-// The 12 codes and values of a row (segments left 2, middle 8, right 2 cells).
-struct RowData
-{
-    uint4 cm;          // middle codes
-    uint32_t cl, cr;   // left / right codes
-    float4 v0, v1;     // middle values
-    float2 vl, vr;     // left / right values
-    __device__ inline uint16_t code( int a ) const
-    {
-        if( a < 2 ) return (uint16_t)( cl >> ( 16 * a ) );
-        if( a >= 10 ) return (uint16_t)( cr >> ( 16 * ( a - 10 ) ) );
-        const int m = a - 2;
-        const uint32_t w = m < 2 ? cm.x : ( m < 4 ? cm.y : ( m < 6 ? cm.z : cm.w ) );
-        return (uint16_t)( w >> ( 16 * ( m & 1 ) ) );
-    }
-    __device__ inline float value( int a ) const
-    {
-        if( a < 2 ) return a == 0 ? vl.x : vl.y;
-        if( a >= 10 ) return a == 10 ? vr.x : vr.y;
-        const int m = a - 2;
-        const float4 v = m < 4 ? v0 : v1;
-        const int q = m & 3;
-        return q == 0 ? v.x : ( q == 1 ? v.y : ( q == 2 ? v.z : v.w ) );
-    }
-    // codes always; values only when with_val (zero otherwise)
-    __device__ inline void load( const int32_t* nb, const Row8& rw, const uint16_t* __restrict__ code,
-                                 const float* __restrict__ val, bool with_val )
-    {
-        const int sl = nb[rw.dl], sc = nb[rw.dc], sr = nb[rw.dr];
-        cm = make_uint4( 0u, 0u, 0u, 0u ); cl = cr = 0u;
-        v0 = v1 = make_float4( 0.f, 0.f, 0.f, 0.f ); vl = vr = make_float2( 0.f, 0.f );
-        if( sc >= 0 )
-        {
-            const size_t g = (size_t)sc * 512 + rw.off;
-            cm = *reinterpret_cast<const uint4*>( code + g );
-            if( with_val )
-            {
-                v0 = __ldg( reinterpret_cast<const float4*>( val + g ) );
-                v1 = __ldg( reinterpret_cast<const float4*>( val + g + 4 ) );
-            }
-        }
-        if( sl >= 0 )
-        {
-            const size_t g = (size_t)sl * 512 + rw.off + 6;
-            cl = *reinterpret_cast<const uint32_t*>( code + g );
-            if( with_val ) vl = __ldg( reinterpret_cast<const float2*>( val + g ) );
-        }
-        if( sr >= 0 )
-        {
-            const size_t g = (size_t)sr * 512 + rw.off;
-            cr = *reinterpret_cast<const uint32_t*>( code + g );
-            if( with_val ) vr = __ldg( reinterpret_cast<const float2*>( val + g ) );
-        }
-    }
-};
-
-// The FP16 correction z0 + P e of a level-0 row: z0 of the 12 cells and the parent value on
-// the 4^3 level (left cells have parent x 3, middle cells x / 2, right cells x 0).
-struct RowZ
-{
-    uint4 zm;
-    uint32_t zl, zr;
-    uint2 em;
-    uint32_t el, er;
-    __device__ inline void load( const int32_t* nb, const Row8& rw, const __half* __restrict__ z0,
-                                 const __half* __restrict__ ec )
-    {
-        const int sl = nb[rw.dl], sc = nb[rw.dc], sr = nb[rw.dr];
-        zm = make_uint4( 0u, 0u, 0u, 0u ); zl = zr = 0u;
-        em = make_uint2( 0u, 0u ); el = er = 0u;
-        if( sc >= 0 )
-        {
-            zm = *reinterpret_cast<const uint4*>( z0 + (size_t)sc * 512 + rw.off );
-            em = *reinterpret_cast<const uint2*>( ec + (size_t)sc * 64 + rw.poff );
-        }
-        if( sl >= 0 )
-        {
-            zl = *reinterpret_cast<const uint32_t*>( z0 + (size_t)sl * 512 + rw.off + 6 );
-            el = *reinterpret_cast<const uint16_t*>( ec + (size_t)sl * 64 + rw.poff + 3 );
-        }
-        if( sr >= 0 )
-        {
-            zr = *reinterpret_cast<const uint32_t*>( z0 + (size_t)sr * 512 + rw.off );
-            er = *reinterpret_cast<const uint16_t*>( ec + (size_t)sr * 64 + rw.poff );
-        }
-    }
-    __device__ static inline float h2f( uint32_t bits ) { return __half2float( __ushort_as_half( (unsigned short)bits ) ); }
-    __device__ inline float value( int a ) const  // z0 + P e of cell a
-    {
-        if( a < 2 ) return h2f( zl >> ( 16 * a ) ) + h2f( el );
-        if( a >= 10 ) return h2f( zr >> ( 16 * ( a - 10 ) ) ) + h2f( er );
-        const int m = a - 2;
-        const uint32_t w = m < 2 ? zm.x : ( m < 4 ? zm.y : ( m < 6 ? zm.z : zm.w ) );
-        const uint32_t e = m < 4 ? em.x : em.y;
-        return h2f( w >> ( 16 * ( m & 1 ) ) ) + h2f( e >> ( 16 * ( ( m >> 1 ) & 1 ) ) );
-    }
-};
-
-template <int E, bool L0>
-__device__ __forceinline__ void mg_down_fused_body( const BoraLevelDev& F, const BoraLevelDev& C, const BoraTilesDev& t,
-                                                    int ntiles, const float* __restrict__ r0, int slot_rr,
-                                                    const double* __restrict__ ring, int bid, int G )
-{
-    using TR = TileRegion<E>;
-    constexpr int R = TR::R, Q = TR::Q, H = TR::H, NT = TR::NT, E3 = TR::E3;
-    __shared__ __align__( 16 ) float rs[TR::N];
-    __shared__ __align__( 16 ) float z1[TR::N];
-    __shared__ __align__( 16 ) uint16_t cs[TR::N];
-    __shared__ float z2[TR::NQ];
-    __shared__ float res[E3];
-    __shared__ int32_t nbb[2][27];
-    __shared__ float wd[32];
-    __shared__ float s_scale;
-    const int tid = threadIdx.x;
-    bora_pdl_trigger();
-    init_wd( wd );
-    if( tid < 27 )
-    {
-        nbb[0][tid] = nbr_entry( t, bid, ntiles, tid );
-        nbb[1][tid] = nbr_entry( t, bid + G, ntiles, tid );
-    }
-    uint32_t am[TR::IA];
-    int bh[TR::IB], ch[TR::IC], ch2[TR::IC];
-#pragma unroll
-    for( int it = 0; it < TR::IA; ++it ) am[it] = TR::region_map( tid + it * NT );
-#pragma unroll
-    for( int it = 0; it < TR::IB; ++it ) bh[it] = TR::qh( tid + it * NT );
-#pragma unroll
-    for( int it = 0; it < TR::IC; ++it ) { ch[it] = TR::th( tid + it * NT ); ch2[it] = TR::th2( tid + it * NT ); }
-    bora_pdl_wait();  // the previous kernel's results are complete from here
-    if( tid == 0 ) s_scale = L0 ? scale_of( ring, slot_rr ) : 1.f;
-    __syncthreads();
-    const float sc = s_scale;
-    constexpr bool kRows = E == 8 && L0;  // row-wise vector staging of the level-0 region
-    uint16_t cv[kRows ? 1 : TR::IA];
-    float rv[kRows ? 1 : TR::IA];
-    Row8 rw;
-    RowData rd;
-    const bool has_row = kRows && tid < 144;
-    if( has_row ) rw.init( tid );
-    auto issue = [&]( const int32_t* nb ) {
-        if constexpr( kRows )
-        {
-            if( has_row ) rd.load( nb, rw, F.code, r0, true );
-        }
-        else
-        {
-#pragma unroll
-            for( int it = 0; it < TR::IA; ++it )
-            {
-                const int sl = TR::slot( nb, am[it] );
-                cv[it] = 0;
-                rv[it] = 0.f;
-                if( sl >= 0 )
-                {
-                    const uint32_t g = (uint32_t)sl * E3 + ( am[it] & 511u );
-                    cv[it] = F.code[g];
-                    rv[it] = L0 ? __ldg( r0 + g ) : __half2float( F.r[g] );
-                }
-            }
-        }
-    };
-    issue( nbb[0] );
-    int n = 0;
-    for( int s = bid; s < ntiles; s += G, ++n )
-    {
-        // stage tile s; the first sweep from zero is pointwise z1 = w r'/d
-        if constexpr( kRows )
-        {
-            if( has_row )
-            {
-#pragma unroll
-                for( int a = 0; a < 12; a += 2 )
-                {
-                    const uint16_t c0 = rd.code( a ), c1 = rd.code( a + 1 );
-                    const bool f0 = c0 & BORA_CODE_FLUID, f1 = c1 & BORA_CODE_FLUID;
-                    const float q0 = f0 ? rd.value( a ) * sc : 0.f, q1 = f1 ? rd.value( a + 1 ) * sc : 0.f;
-                    const int h = rw.h0 + a;
-                    *reinterpret_cast<uint32_t*>( &cs[h] ) = (uint32_t)c0 | ( (uint32_t)c1 << 16 );
-                    *reinterpret_cast<float2*>( &rs[h] ) = make_float2( q0, q1 );
-                    *reinterpret_cast<float2*>( &z1[h] ) =
-                        make_float2( f0 ? q0 * wd[code_diag( c0 )] : 0.f, f1 ? q1 * wd[code_diag( c1 )] : 0.f );
-                }
-            }
-        }
-        else
-        {
-#pragma unroll
-            for( int it = 0; it < TR::IA; ++it )
-            {
-                const int h = tid + it * NT;
-                if( h < TR::N )
-                {
-                    const uint16_t cc = cv[it];
-                    const bool fl = cc & BORA_CODE_FLUID;
-                    const float r = fl ? ( L0 ? rv[it] * sc : rv[it] ) : 0.f;
-                    cs[h] = cc;
-                    rs[h] = r;
-                    z1[h] = fl ? r * wd[code_diag( cc )] : 0.f;
-                }
-            }
-        }
-        const int32_t nb2 = tid < 27 ? nbr_entry( t, s + 2 * G, ntiles, tid ) : -1;
-        __syncthreads();
-        if( s + G < ntiles ) issue( nbb[( n + 1 ) & 1] );
-        // second sweep on the inner region
-#pragma unroll
-        for( int it = 0; it < TR::IB; ++it )
-        {
-            const int h = bh[it];
-            if( h >= 0 ) z2[tid + it * NT] = jacobi<R>( z1, h, cs[h], rs[h], wd + 16 );
-        }
-        __syncthreads();
-        // residual on the tile
-#pragma unroll
-        for( int it = 0; it < TR::IC; ++it )
-        {
-            const int h = ch[it];
-            if( h < 0 ) continue;
-            const int h2 = ch2[it], l = tid + it * NT;
-            const uint16_t cc = cs[h];
-            const float zc = z2[h2];
-            const float sum = ( z2[h2 - 1] + z2[h2 + 1] ) + ( z2[h2 - Q] + z2[h2 + Q] ) + ( z2[h2 - Q * Q] + z2[h2 + Q * Q] );
-            res[l] = ( cc & BORA_CODE_FLUID ) ? rs[h] - ( (float)code_diag( cc ) * zc - sum ) : 0.f;
-            F.z0[(size_t)s * E3 + l] = __float2half_rn( zc );
-        }
-        __syncthreads();
-        // restriction, r'_C = 4 * mean of the 8 children = 0.5 * sum (non-fluid children
-        // hold 0; the value of a non-fluid coarse cell is never read)
-        if( tid < H * H * H )
-        {
-            const int a = tid % H, b = ( tid / H ) % H, c = tid / ( H * H );
-            const int l = 2 * a + E * ( 2 * b + E * 2 * c );
-            const float sum = ( ( res[l] + res[l + 1] ) + ( res[l + E] + res[l + E + 1] ) ) +
-                              ( ( res[l + E * E] + res[l + E * E + 1] ) + ( res[l + E * E + E] + res[l + E * E + E + 1] ) );
-            C.r[(size_t)s * ( H * H * H ) + tid] = __float2half_rn( 0.5f * sum );
-        }
-        if( tid < 27 ) nbb[n & 1][tid] = nb2;  // tile s's table is no longer read
-        __syncthreads();
-    }
-}
-
-template <int E, bool L0>
-__global__ void __launch_bounds__( TileRegion<E>::NT, TileRegion<E>::MINB ) k_mg_down_fused( BoraLevelDev F, BoraLevelDev C,
-                                                                           BoraTilesDev t, int ntiles,
-                                                                           const float* __restrict__ r0, int slot_rr,
-                                                                           const double* __restrict__ ring )
-{
-    mg_down_fused_body<E, L0>( F, C, t, ntiles, r0, slot_rr, ring, blockIdx.x, gridDim.x );
-}
-
-// Batched: level l = 0, 1, 2 (E = 8, 4, 2) of each simulation's hierarchy.
-template <int E, bool L0>
-__global__ void __launch_bounds__( TileRegion<E>::NT, TileRegion<E>::MINB )
-    k_mg_down_fused_batch( const __grid_constant__ BoraBatchLaunch L )
-{
-    constexpr int l = E == 8 ? 0 : ( E == 4 ? 1 : 2 );
-    unsigned bid;
-    const int k = bora_batch_member( L, blockIdx.x, &bid );
-    const BoraMemberSolve& m = L.ms[k];
-    const BoraMemberSlots& q = L.sl[k];
-    mg_down_fused_body<E, L0>( m.L[l], m.L[l + 1], BoraTilesDev{ nullptr, nullptr, m.nbr }, m.ntiles,
-                               L0 ? m.sv.r : nullptr, q.rr, m.red.ring, (int)bid, m.grid[kGridDown8 + l] );
-}
-
-template <int E, bool L0>
-__device__ __forceinline__ void mg_up_fused_body( const BoraLevelDev& F, const __half* __restrict__ ec, const BoraTilesDev& t,
-                                                  int ntiles, const float* __restrict__ r0, int slot_rr,
-                                                  const BoraReduceDev& red, float* __restrict__ zout, int slot_rz, int bid,
-                                                  int G )
-{
-    using TR = TileRegion<E>;
-    constexpr int R = TR::R, Q = TR::Q, H = TR::H, NT = TR::NT, E3 = TR::E3;
-    __shared__ __align__( 16 ) float rs[TR::N];
-    __shared__ __align__( 16 ) float za[TR::N];
-    __shared__ __align__( 16 ) uint16_t cs[TR::N];
-    __shared__ float zb[TR::NQ];
-    __shared__ __align__( 16 ) float rraw[L0 ? E3 : 1];
-    __shared__ int32_t nbb[2][27];
-    __shared__ float wd[32];
-    __shared__ float s_scale;
-    const int tid = threadIdx.x;
-    bora_pdl_trigger();
-    init_wd( wd );
-    if( tid < 27 )
-    {
-        nbb[0][tid] = nbr_entry( t, bid, ntiles, tid );
-        nbb[1][tid] = nbr_entry( t, bid + G, ntiles, tid );
-    }
-    uint32_t am[TR::IA];
-    int bh[TR::IB], ch[TR::IC], ch2[TR::IC];
-#pragma unroll
-    for( int it = 0; it < TR::IA; ++it ) am[it] = TR::region_map( tid + it * NT );
-#pragma unroll
-    for( int it = 0; it < TR::IB; ++it ) bh[it] = TR::qh( tid + it * NT );
-#pragma unroll
-    for( int it = 0; it < TR::IC; ++it ) { ch[it] = TR::th( tid + it * NT ); ch2[it] = TR::th2( tid + it * NT ); }
-    bora_pdl_wait();  // the previous kernel's results are complete from here
-    if( tid == 0 ) s_scale = L0 ? scale_of( red.ring, slot_rr ) : 1.f;
-    __syncthreads();
-    const float sc = s_scale;
-    constexpr bool kRows = E == 8 && L0;  // row-wise vector staging of the level-0 region
-    uint16_t cv[kRows ? 1 : TR::IA];
-    float rv[kRows ? 1 : TR::IA], zv[kRows ? 1 : TR::IA];
-    Row8 rw;
-    RowData rd;
-    RowZ rzv;
-    const bool has_row = kRows && tid < 144;
-    bool inner_row = false, centre_row = false;
-    if( has_row )
-    {
-        rw.init( tid );
-        const int b = tid % 12, c = tid / 12;
-        inner_row = b >= 1 && b <= 10 && c >= 1 && c <= 10;
-        centre_row = b >= 2 && b <= 9 && c >= 2 && c <= 9;
-    }
-    auto issue = [&]( const int32_t* nb ) {
-        if constexpr( kRows )
-        {
-            if( has_row )
-            {
-                rd.load( nb, rw, F.code, r0, inner_row );
-                rzv.load( nb, rw, F.z0, ec );
-            }
-        }
-        else
-        {
-#pragma unroll
-            for( int it = 0; it < TR::IA; ++it )
-            {
-                const uint32_t m = am[it];
-                const int sl = TR::slot( nb, m );
-                cv[it] = 0;
-                rv[it] = 0.f;
-                zv[it] = 0.f;
-                if( sl >= 0 )
-                {
-                    const uint32_t g = (uint32_t)sl * E3 + ( m & 511u );
-                    cv[it] = F.code[g];
-                    // za = z0 + P e: the parent is the same tile's cell on the coarser level
-                    zv[it] = __half2float( F.z0[g] ) + __half2float( ec[(uint32_t)sl * ( H * H * H ) + ( ( m >> 9 ) & 63u )] );
-                    if( m & TR::kInner ) rv[it] = L0 ? __ldg( r0 + g ) : __half2float( F.r[g] );
-                }
-            }
-        }
-    };
-    issue( nbb[0] );
-    DF rz{ 0.f, 0.f };
-    int n = 0;
-    for( int s = bid; s < ntiles; s += G, ++n )
-    {
-        float trz = 0.f;  // this thread's r.z over its cells of the tile
-        if constexpr( kRows )
-        {
-            if( has_row )
-            {
-#pragma unroll
-                for( int a = 0; a < 12; a += 2 )
-                {
-                    const uint16_t c0 = rd.code( a ), c1 = rd.code( a + 1 );
-                    const bool f0 = c0 & BORA_CODE_FLUID, f1 = c1 & BORA_CODE_FLUID;
-                    const float v0 = rd.value( a ), v1 = rd.value( a + 1 );
-                    const int h = rw.h0 + a;
-                    *reinterpret_cast<uint32_t*>( &cs[h] ) = (uint32_t)c0 | ( (uint32_t)c1 << 16 );
-                    *reinterpret_cast<float2*>( &rs[h] ) = make_float2( f0 ? v0 * sc : 0.f, f1 ? v1 * sc : 0.f );
-                    *reinterpret_cast<float2*>( &za[h] ) = make_float2( f0 ? rzv.value( a ) : 0.f, f1 ? rzv.value( a + 1 ) : 0.f );
-                    if( centre_row && a >= 2 && a < 10 )
-                        *reinterpret_cast<float2*>( &rraw[rw.off + a - 2] ) = make_float2( v0, v1 );
-                }
-            }
-        }
-        else
-        {
-#pragma unroll
-            for( int it = 0; it < TR::IA; ++it )
-            {
-                const int h = tid + it * NT;
-                if( h < TR::N )
-                {
-                    const uint16_t cc = cv[it];
-                    const bool fl = cc & BORA_CODE_FLUID;
-                    cs[h] = cc;
-                    rs[h] = fl ? ( L0 ? rv[it] * sc : rv[it] ) : 0.f;
-                    za[h] = fl ? zv[it] : 0.f;
-                    if( L0 && ( ( am[it] >> 16 ) & 31u ) == TR::kCentre ) rraw[am[it] & 511u] = rv[it];
-                }
-            }
-        }
-        const int32_t nb2 = tid < 27 ? nbr_entry( t, s + 2 * G, ntiles, tid ) : -1;
-        __syncthreads();
-        if( s + G < ntiles ) issue( nbb[( n + 1 ) & 1] );
-#pragma unroll
-        for( int it = 0; it < TR::IB; ++it )
-        {
-            const int h = bh[it];
-            if( h >= 0 ) zb[tid + it * NT] = jacobi<R>( za, h, cs[h], rs[h], wd + 16 );
-        }
-        __syncthreads();
-#pragma unroll
-        for( int it = 0; it < TR::IC; ++it )
-        {
-            const int h = ch[it];
-            if( h < 0 ) continue;
-            const int h2 = ch2[it], l = tid + it * NT;
-            const uint16_t cc = cs[h];
-            const float zc = jacobi<Q>( zb, h2, cc, rs[h], wd );
-            const size_t g = (size_t)s * E3 + l;
-            if( L0 )
-            {
-                const float zf = zc / sc;  // undo the FP16 scaling of the residual
-                zout[g] = zf;
-                if( cc & BORA_CODE_FLUID ) trz = fmaf( rraw[l], zf, trz );
-            }
-            else
-            {
-                F.z1[g] = __float2half_rn( zc );
-            }
-        }
-        if( L0 ) rz = df_add_f( rz, trz );
-        if( tid < 27 ) nbb[n & 1][tid] = nb2;
-        __syncthreads();  // the next tile's staging overwrites the shared arrays
-    }
-    if( L0 ) reduce2_publish_warp( df_warp_sum( rz ), 0.0, 0, red, slot_rz, -1, bid, G );
-}
-
-template <int E, bool L0>
-__global__ void __launch_bounds__( TileRegion<E>::NT, TileRegion<E>::MINB ) k_mg_up_fused( BoraLevelDev F, const __half* __restrict__ ec,
-                                                                         BoraTilesDev t, int ntiles,
-                                                                         const float* __restrict__ r0, int slot_rr,
-                                                                         BoraReduceDev red, float* __restrict__ zout,
-                                                                         int slot_rz )
-{
-    mg_up_fused_body<E, L0>( F, ec, t, ntiles, r0, slot_rr, red, zout, slot_rz, blockIdx.x, gridDim.x );
-}
-
-// Batched: the coarser level's correction is its z1 after a fused up kernel (levels 1 and 2
-// below levels 0 and 1), and level 3's z0 below level 2 (left there by the coarse cluster
-// kernel).
-template <int E, bool L0>
-__global__ void __launch_bounds__( TileRegion<E>::NT, TileRegion<E>::MINB )
-    k_mg_up_fused_batch( const __grid_constant__ BoraBatchLaunch L )
-{
-    constexpr int l = E == 8 ? 0 : ( E == 4 ? 1 : 2 );
-    unsigned bid;
-    const int k = bora_batch_member( L, blockIdx.x, &bid );
-    const BoraMemberSolve& m = L.ms[k];
-    const BoraMemberSlots& q = L.sl[k];
-    const __half* ec = l < 2 ? m.L[l + 1].z1 : m.z3;
-    mg_up_fused_body<E, L0>( m.L[l], ec, BoraTilesDev{ nullptr, nullptr, m.nbr }, m.ntiles, L0 ? m.sv.r : nullptr, q.rr,
-                             m.red, L0 ? m.sv.z : nullptr, q.rz, (int)bid, m.grid[kGridUp8 + l] );
-}
-
+// ---- tiled levels with E >= 2 -----------------------------------------------------------
+// Levels 0, 1 and 2 (E = 8, 4, 2) run as stencil passes (mg_passes.cu).
 
 // PCG update without a preconditioner sweep: r -= alpha q; r.r (e += alpha d is applied by
 // the next direction kernel or the refinement step).
@@ -1246,38 +684,6 @@ int sm_count()
 int blocks_for( size_t n )
 {
     return (int)std::max<size_t>( 1, std::min<size_t>( ( n + 255 ) / 256, (size_t)sm_count() * 8 ) );
-}
-
-// Persistent grid for a fused kernel: as many CTAs as can be resident at once.
-template <class K>
-int fused_grid( K kernel, int nt, int ntiles, BoraPerDevice& per_sm )
-{
-    const int b = per_sm.get( [&] {
-        int v = 0;
-        return cudaOccupancyMaxActiveBlocksPerMultiprocessor( &v, kernel, nt, 0 ) == cudaSuccess && v > 0 ? v : 1;
-    } );
-    return std::max( 1, std::min( ntiles, b * sm_count() ) );
-}
-
-template <int E, bool L0>
-void launch_down_fused( const BoraLevelDev& F, const BoraLevelDev& C, BoraTilesDev t, int ntiles, const float* r0,
-                        int slot_rr, const double* ring, cudaStream_t st )
-{
-    static BoraPerDevice per_sm;
-    constexpr int NT = TileRegion<E>::NT;
-    const int grid = fused_grid( k_mg_down_fused<E, L0>, NT, ntiles, per_sm );
-    bora_launch_pdl( k_mg_down_fused<E, L0>, grid, NT, 0, st, F, C, t, ntiles, r0, slot_rr, ring );
-}
-
-template <int E, bool L0>
-void launch_up_fused( const BoraLevelDev& F, const __half* ec, BoraTilesDev t, int ntiles, const float* r0,
-                      int slot_rr, BoraReduceDev red, float* zout, int slot_rz, cudaStream_t st )
-{
-    static BoraPerDevice per_sm;
-    constexpr int NT = TileRegion<E>::NT;
-    int grid = fused_grid( k_mg_up_fused<E, L0>, NT, ntiles, per_sm );
-    if( L0 ) grid = std::min( grid, kBoraMaxReduceBlocks );  // partial sums capacity of the reduction
-    bora_launch_pdl( k_mg_up_fused<E, L0>, grid, NT, 0, st, F, ec, t, ntiles, r0, slot_rr, red, zout, slot_rz );
 }
 
 LevelNav nav_of( const BoraGridDev& g, const BoraLevelDev& L, BoraTilesDev t )
@@ -1340,7 +746,7 @@ int tail_start( const BoraLevelDev* levels, int nlevels )
     return first;
 }
 
-bool fused_level( const BoraLevelDev& L ) { return L.kind == 0 && L.E >= 2; }
+bool pass_level( const BoraLevelDev& L ) { return L.kind == 0 && L.E >= 2; }
 
 // CTAs of the tail cluster: 16 where the device can co-schedule such a cluster of this
 // kernel, else the portable 8.
@@ -1381,13 +787,13 @@ int bora_mg_vcycle_launches( const BoraGridDev& g, const BoraLevelDev* levels, i
                           : tail_start( levels, nlevels );
     const int stop = std::min( first, nlevels - 1 );
     int n = 1;  // the tail kernel, or the coarsest-level kernel
-    for( int l = 0; l < stop; ++l ) n += fused_level( levels[l] ) ? 2 : 4;
+    for( int l = 0; l < stop; ++l ) n += 4;
     return n;
 }
 
 void bora_mg_vcycle( const BoraGridDev& g, const BoraLevelDev* levels, int nlevels, BoraTilesDev t, const void* mid_image,
-                     const float* r, float* z, BoraReduceDev red, int slot_rr, int slot_rz, int coarse_sweeps,
-                     cudaStream_t st )
+                     const float* r, float* z, float* scratch, BoraReduceDev red, int slot_rr, int slot_rz,
+                     int coarse_sweeps, cudaStream_t st )
 {
     if( nlevels < 2 ) return;  // the caller always builds at least two levels
     if( levels[0].ncells == 0 ) return;
@@ -1404,11 +810,9 @@ void bora_mg_vcycle( const BoraGridDev& g, const BoraLevelDev* levels, int nleve
         const BoraLevelDev& F = levels[l];
         const BoraLevelDev& C = levels[l + 1];
         const float* r0 = l == 0 ? r : nullptr;
-        if( fused_level( F ) )
+        if( pass_level( F ) )
         {
-            if( F.E == 8 ) launch_down_fused<8, true>( F, C, t, ntiles, r0, slot_rr, red.ring, st );
-            else if( F.E == 4 ) launch_down_fused<4, false>( F, C, t, ntiles, r0, slot_rr, red.ring, st );
-            else launch_down_fused<2, false>( F, C, t, ntiles, r0, slot_rr, red.ring, st );
+            bora_mg_pass_down( levels, l, t, ntiles, r, scratch, red, slot_rr, st );
             continue;
         }
         with_nav( g, levels, nlevels, l, t, [&]( auto nav ) {
@@ -1466,14 +870,12 @@ void bora_mg_vcycle( const BoraGridDev& g, const BoraLevelDev* levels, int nleve
     {
         const BoraLevelDev& F = levels[l];
         const float* r0 = l == 0 ? r : nullptr;
-        if( fused_level( F ) )
+        if( pass_level( F ) )
         {
-            // a coarser level that went through the fused path left its result in z1
-            const bool cf = l + 1 < stop && fused_level( levels[l + 1] );
+            // a coarser level that ran its passes left its correction in z1, the others in z0
+            const bool cf = l + 1 < stop && pass_level( levels[l + 1] );
             const __half* ec = cf ? levels[l + 1].z1 : levels[l + 1].z0;
-            if( F.E == 8 ) launch_up_fused<8, true>( F, ec, t, ntiles, r0, slot_rr, red, z, slot_rz, st );
-            else if( F.E == 4 ) launch_up_fused<4, false>( F, ec, t, ntiles, r0, slot_rr, red, nullptr, slot_rz, st );
-            else launch_up_fused<2, false>( F, ec, t, ntiles, r0, slot_rr, red, nullptr, slot_rz, st );
+            bora_mg_pass_up( levels, l, ec, t, ntiles, r, scratch, red, slot_rr, z, slot_rz, st );
             continue;
         }
         with_nav( g, levels, nlevels, l, t, [&]( auto nav ) {
@@ -1489,13 +891,9 @@ void bora_member_grids( int ntiles, int* grid )
 {
     bora_projection_grids( ntiles, grid );
     grid[kGridUpd] = blocks_for( (size_t)std::max( ntiles, 0 ) * 512 / 4 );
-    static BoraPerDevice d8, d4, d2, u8, u4, u2;
-    grid[kGridDown8] = fused_grid( k_mg_down_fused<8, true>, TileRegion<8>::NT, ntiles, d8 );
-    grid[kGridDown4] = fused_grid( k_mg_down_fused<4, false>, TileRegion<4>::NT, ntiles, d4 );
-    grid[kGridDown2] = fused_grid( k_mg_down_fused<2, false>, TileRegion<2>::NT, ntiles, d2 );
-    grid[kGridUp8] = std::min( fused_grid( k_mg_up_fused<8, true>, TileRegion<8>::NT, ntiles, u8 ), kBoraMaxReduceBlocks );
-    grid[kGridUp4] = fused_grid( k_mg_up_fused<4, false>, TileRegion<4>::NT, ntiles, u4 );
-    grid[kGridUp2] = fused_grid( k_mg_up_fused<2, false>, TileRegion<2>::NT, ntiles, u2 );
+    grid[kGridPass0] = bora_mg_pass_grid( 8, ntiles );
+    grid[kGridPass1] = bora_mg_pass_grid( 4, ntiles );
+    grid[kGridPass2] = bora_mg_pass_grid( 2, ntiles );
 }
 
 void bora_launch_pcg_update_noprec_batch( const BoraBatchLaunch& L, int blocks, cudaStream_t st )
@@ -1503,23 +901,6 @@ void bora_launch_pcg_update_noprec_batch( const BoraBatchLaunch& L, int blocks, 
     if( blocks > 0 ) bora_launch_pdl( k_pcg_update_noprec_batch, dim3( blocks ), dim3( 256 ), 0, st, L );
 }
 
-void bora_launch_mg_fused_batch( bool up, int l, const BoraBatchLaunch& L, int blocks, cudaStream_t st )
-{
-    if( blocks <= 0 ) return;
-    const dim3 grid( blocks );
-    if( !up )
-    {
-        if( l == 0 ) bora_launch_pdl( k_mg_down_fused_batch<8, true>, grid, dim3( TileRegion<8>::NT ), 0, st, L );
-        else if( l == 1 ) bora_launch_pdl( k_mg_down_fused_batch<4, false>, grid, dim3( TileRegion<4>::NT ), 0, st, L );
-        else bora_launch_pdl( k_mg_down_fused_batch<2, false>, grid, dim3( TileRegion<2>::NT ), 0, st, L );
-    }
-    else
-    {
-        if( l == 0 ) bora_launch_pdl( k_mg_up_fused_batch<8, true>, grid, dim3( TileRegion<8>::NT ), 0, st, L );
-        else if( l == 1 ) bora_launch_pdl( k_mg_up_fused_batch<4, false>, grid, dim3( TileRegion<4>::NT ), 0, st, L );
-        else bora_launch_pdl( k_mg_up_fused_batch<2, false>, grid, dim3( TileRegion<2>::NT ), 0, st, L );
-    }
-}
 
 void bora_launch_pcg_update_noprec( int ntiles, BoraSolverDev s, BoraReduceDev red, int slot_rz, int slot_dq,
                                     int slot_rr_out, cudaStream_t st )
