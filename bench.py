@@ -609,6 +609,10 @@ def run_ours(args, world, rank, local):
                  "p99_ms": mm["p99_ms"], "roofline": mm["roofline"], "step_roofline": mm["step_roofline"],
                  "gpu_launches": mm["launches"],
                  "solver": mm["solver"], "speedup_over_plain": mm["value"] / value,
+                 "launch_shapes": [{"group": ["L0", "L1", "L2", "L0 batch", "L1 batch", "L2 batch"][g], "size_class": c,
+                                    "shape": ([2, 4, 8] if g % 3 == 0 else [64, 128, 256, 512])[v] if v >= 0 else None,
+                                    "median_ms": m}
+                                   for g, d, c, v, m in flip.tune_table() if d == local],
                  "config": "same scene; geometric-multigrid-preconditioned CG, V(2,2) damped Jacobi, FP16 level "
                            "storage with FP32 arithmetic, FP64-accurate dots and norms, double-float iterative refinement"}
 

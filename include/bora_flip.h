@@ -315,6 +315,20 @@ int bora_flip_set_profiling( bora_flip_handle h, uint32_t class_mask );
 int bora_flip_get_kernel_times( bora_flip_handle h, double* ms, uint64_t* launches, int n );
 const char* bora_flip_status_string( int status );
 
+/* Launch-shape autotuner (process-wide; no counterpart in the reference). Kernels with
+ * several launch shapes that compute the same bits (the multigrid passes of levels 0-2:
+ * tiles and threads per block) are timed in every shape on their first launches per
+ * device and size class (floor(log2 tiles)), single simulations and batches apart; the
+ * fastest median is kept. Tuning never changes a result. mode 1 = tune (the default),
+ * 0 = the default shapes everywhere. With the environment variable BORA_TUNE_FILE set,
+ * the table is read from that file on first use and written back when an entry is
+ * decided. */
+int bora_flip_set_tuning( int mode );
+/* The table as text, one line per entry: "group device size_class shape median_ms"
+ * (shape -1: still measuring). *len = its length; cap = 0 asks for the length only;
+ * BORA_ERR_CAPACITY when cap cannot hold the text and its terminating zero. */
+int bora_flip_tune_table( char* buf, size_t cap, size_t* len );
+
 /* ---- device building blocks ------------------------------------------------------- */
 
 /* Exclusive prefix sum of n uint32 counts in device memory: d_out[i] = sum_{j<i} d_in[j];

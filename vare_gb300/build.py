@@ -25,7 +25,7 @@ OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libbora_flip.so")
 
 SOURCES = ["scan.cu", "grid_build.cu", "p2g.cu", "projection.cu", "multigrid.cu", "mg_mid.cu", "mg_passes.cu", "g2p.cu", "surface.cu",
-           "vdb_export.cu", "flip_api.cu", "serve.cu"]
+           "vdb_export.cu", "tune.cu", "flip_api.cu", "serve.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
               "--expt-relaxed-constexpr", "-Xcudafe", "--diag_suppress=177"]

@@ -233,12 +233,42 @@ struct BoraLevelDev
 // and restricted into level l + 1's r (down), or prolonged from the coarser correction ec and
 // post-smoothed (up: level 0 into the PCG's z with r.z -> slot_rz, the others into z1).
 // scratch: an FP32 vector of level 0's size.
-int bora_mg_pass_grid( int E, int ntiles );
+int bora_mg_pass_grid( int E, int ntiles, int v );  // v < 0: level 0's fixed up-2 shape
 void bora_mg_pass_down( const BoraLevelDev* levels, int l, const BoraTilesDev& t, int ntiles, const float* r0,
                         float* scratch, const BoraReduceDev& red, int slot_rr, cudaStream_t st );
 void bora_mg_pass_up( const BoraLevelDev* levels, int l, const __half* ec, const BoraTilesDev& t, int ntiles,
                       const float* r0, float* scratch, const BoraReduceDev& red, int slot_rr, float* z, int slot_rz,
                       cudaStream_t st );
+
+// ---- launch-shape autotuner (tune.cu) ------------------------------------------------------
+// Kernel groups with interchangeable launch shapes (bit-identical results): the multigrid
+// passes of levels 0, 1, 2, for single simulations and for batches.
+enum BoraTuneGroup
+{
+    kBoraTuneL0 = 0, kBoraTuneL1, kBoraTuneL2, kBoraTuneL0Batch, kBoraTuneL1Batch, kBoraTuneL2Batch, kBoraTuneGroups
+};
+struct BoraTunePick
+{
+    int variant;  // the launch shape to use
+    bool timed;   // still measuring: time this launch (BoraTuneTimer)
+};
+int bora_tune_variants( int group );
+int bora_tune_default( int group );
+BoraTunePick bora_tune_pick( int group, int units );  // units: the work's size (tiles)
+// Brackets the launches of a pick with events on the stream while the group is measured.
+struct BoraTuneTimer
+{
+    bool timed;
+    int group, units, variant;
+    cudaStream_t st;
+    cudaEvent_t a = nullptr;
+    BoraTuneTimer( const BoraTunePick& p, int group, int units, cudaStream_t st );
+    ~BoraTuneTimer();
+    BoraTuneTimer( const BoraTuneTimer& ) = delete;
+    BoraTuneTimer& operator=( const BoraTuneTimer& ) = delete;
+};
+// Fold the timings of completed launches into the table (call after a stream synchronize).
+void bora_tune_resolve();
 
 // Cell types and stencil codes of level c from level c-1 (levels[0] = fine, given).
 // mid_image: the buffer for the coarse levels' cluster image (bora_mg_mid_image_bytes), or null
@@ -272,7 +302,8 @@ void bora_mg_vcycle( const BoraGridDev& g, const BoraLevelDev* levels, int nleve
 enum BoraMemberGrid
 {
     kGridDir = 0, kGridUpd, kGridCells, kGridResidual,
-    kGridPass0, kGridPass1, kGridPass2,  // the multigrid passes of levels 0, 1, 2 (mg_passes.cu)
+    kGridPass0, kGridPass0R, kGridPass1, kGridPass2,  // the multigrid passes of levels 0, 1, 2 (mg_passes.cu);
+                                                      // 0R: level 0's up 2, which reduces r.z
     kGridCount
 };
 struct BoraMemberSolve
@@ -338,10 +369,12 @@ void bora_launch_refine_accumulate_batch( const BoraBatchLaunch& L, int blocks, 
 void bora_launch_refine_residual_batch( const BoraBatchLaunch& L, int blocks, cudaStream_t st );
 void bora_launch_write_pressure_batch( const BoraBatchLaunch& L, int blocks, cudaStream_t st );
 void bora_launch_pcg_update_noprec_batch( const BoraBatchLaunch& L, int blocks, cudaStream_t st );
-// pass `pass` (0, 1 down; 2, 3 up) of multigrid level l (0, 1, 2) for the batch
-void bora_launch_mg_pass_batch( int l, int pass, const BoraBatchLaunch& L, int blocks, cudaStream_t st );
-// this simulation's own grid per batched kernel (what its single launches use)
-void bora_member_grids( int ntiles, int* grid );
+// pass `pass` (0, 1 down; 2, 3 up) of multigrid level l (0, 1, 2) for the batch, launch
+// shape v (level 0's up 2 has a fixed shape)
+void bora_launch_mg_pass_batch( int l, int pass, int v, const BoraBatchLaunch& L, int blocks, cudaStream_t st );
+// this simulation's own grid per batched kernel (what its single launches use), with the
+// multigrid passes of levels 0, 1, 2 in launch shapes v[0..2]
+void bora_member_grids( int ntiles, int* grid, const int* v );
 void bora_projection_grids( int ntiles, int* grid );  // the kGridDir, kGridCells and kGridResidual entries
 
 // e += alpha d; r -= alpha q; r.r -> ring slot (alpha = rz / dq, or 0 when slot_rz < 0)

@@ -1288,6 +1288,7 @@ int bora_flip_step( bora_flip_handle s, float dt )
     cudaEventElapsedTime( &gms, s->ev_step[0], s->ev_step[1] );
     s->stats.gpu_ms = gms;
     s->prof_resolve();
+    bora_tune_resolve();
     s->stats.steps++;
     s->stats.stage_ms[7] = std::chrono::duration<double, std::milli>( std::chrono::steady_clock::now() - t0 ).count();
     return solve;
@@ -1353,6 +1354,18 @@ int batch_solve( std::vector<BatchMember>& M, cudaStream_t st, BatchBuffers& bb,
     std::vector<char> mid( dbytes * n );
     int ctas = 0;
     size_t smem = 0;
+    // the launch shapes of the multigrid passes for this batch (the autotuner's choice for
+    // the batch's total size; every shape gives the same results)
+    int total_tiles = 0;
+    for( int k = 0; k < n; ++k ) total_tiles += M[k].s->ntiles;
+    const int tgroup[3] = { kBoraTuneL0Batch, kBoraTuneL1Batch, kBoraTuneL2Batch };
+    BoraTunePick tpick[3];
+    int tv[3];
+    for( int l = 0; l < 3; ++l )
+    {
+        tpick[l] = bora_tune_pick( tgroup[l], total_tiles );
+        tv[l] = tpick[l].variant;
+    }
     for( int k = 0; k < n; ++k )
     {
         bora_flip_sim* s = M[k].s;
@@ -1366,7 +1379,7 @@ int batch_solve( std::vector<BatchMember>& M, cudaStream_t st, BatchBuffers& bb,
         m.red = s->reducer();
         for( int l = 0; l < 4; ++l ) m.L[l] = s->levels[l];
         m.z3 = s->levels[3].z0;
-        bora_member_grids( s->ntiles, m.grid );
+        bora_member_grids( s->ntiles, m.grid, tv );
         size_t sm = 0;
         int c = 0;
         if( !bora_mg_mid_describe( s->g, s->levels, s->nlevels, s->tiles(), s->ntiles, s->mg_mid.p,
@@ -1412,12 +1425,20 @@ int batch_solve( std::vector<BatchMember>& M, cudaStream_t st, BatchBuffers& bb,
         return BORA_OK;
     };
     auto launch = [&]( int q ) { return BoraBatchLaunch{ dms, dsl, dstart + q * ( n + 1 ), n }; };
+    const int lgrid[3] = { kGridPass0, kGridPass1, kGridPass2 };
     auto vcycle = [&]() {
         for( int l = 0; l < 3; ++l )
-            for( int p = 0; p < 2; ++p ) bora_launch_mg_pass_batch( l, p, launch( kGridPass0 + l ), blocks[kGridPass0 + l], st );
+        {
+            BoraTuneTimer timer( tpick[l], tgroup[l], total_tiles, st );  // times the level's two down passes
+            for( int p = 0; p < 2; ++p ) bora_launch_mg_pass_batch( l, p, tv[l], launch( lgrid[l] ), blocks[lgrid[l]], st );
+        }
         bora_mg_mid_launch_batch( bb.mid.p, launch( kGridCount ), blocks[kGridCount], ctas, smem, st );
         for( int l = 2; l >= 0; --l )
-            for( int p = 2; p < 4; ++p ) bora_launch_mg_pass_batch( l, p, launch( kGridPass0 + l ), blocks[kGridPass0 + l], st );
+            for( int p = 2; p < 4; ++p )
+            {
+                const int q = l == 0 && p == 3 ? kGridPass0R : lgrid[l];
+                bora_launch_mg_pass_batch( l, p, tv[l], launch( q ), blocks[q], st );
+            }
         launches += 13;
     };
     // r = b, x = e = d = q = 0; ||b||^2, max|b|
@@ -1717,6 +1738,7 @@ int bora_flip_step_batch( bora_flip_handle* hs, int n, float dt, int* status )
     BORA_TRY( cudaEventSynchronize( h0->ev_step[1] ) );
     float gms = 0.f;
     cudaEventElapsedTime( &gms, h0->ev_step[0], h0->ev_step[1] );
+    bora_tune_resolve();
     const auto t3 = std::chrono::steady_clock::now();
     auto ms = []( std::chrono::steady_clock::time_point x, std::chrono::steady_clock::time_point y ) {
         return std::chrono::duration<double, std::milli>( y - x ).count();

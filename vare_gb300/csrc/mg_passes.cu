@@ -23,6 +23,7 @@
 // neighbours come from other lanes by shuffles, and the lanes of the tile's faces load the face
 // rows of the six neighbour tiles. Levels 1 and 2 run one thread per cell.
 #include <algorithm>
+#include <type_traits>
 
 #include "bora_internal.h"
 #include "reduce.cuh"
@@ -31,8 +32,11 @@ namespace {
 
 constexpr float kOmegaA = 0.5687f;  // the Chebyshev pair of the smoothers (multigrid.cu)
 constexpr float kOmegaB = 1.6902f;
-constexpr int kPassWarps = 4;       // level 0: tiles in flight per block (one per warp)
-constexpr int kFlatThreads = 256;   // levels 1 and 2: cells per block and round
+// launch shapes (the autotuner picks one per size class; the results do not depend on it):
+// level 0 tiles (warps) per block, levels 1 and 2 threads (cells) per block
+constexpr int kPassWarpsOf[3] = { 2, 4, 8 };
+constexpr int kFlatThreadsOf[4] = { 64, 128, 256, 512 };
+constexpr int kReduceWarps = 4;  // level 0's up 2 sums r.z over its blocks: its shape is fixed
 constexpr unsigned kAll = 0xffffffffu;
 
 __device__ __forceinline__ int cdiag( uint16_t c ) { return ( c >> 8 ) & 15; }
@@ -231,8 +235,8 @@ struct Pass0Args
     int slot_rr, slot_rz;
 };
 
-// pass P of level 0: 0 = down 1, 1 = down 2, 2 = up 1, 3 = up 2
-template <int P>
+// pass P of level 0: 0 = down 1, 1 = down 2, 2 = up 1, 3 = up 2; W tiles (warps) per block
+template <int W, int P>
 __device__ __forceinline__ void pass0_body( const Pass0Args& a, unsigned bid, unsigned G )
 {
     __shared__ float w[32];
@@ -240,7 +244,7 @@ __device__ __forceinline__ void pass0_body( const Pass0Args& a, unsigned bid, un
     bora_pdl_trigger();
     init_weights( w );
     const int lane = threadIdx.x & 31, j = lane & 7, kq = lane >> 3;
-    const int stride = (int)G * kPassWarps;
+    const int stride = (int)G * W;
     // what no kernel of the solve writes - the tile's face neighbours and the rows' codes - is
     // read a tile ahead, the first tile's before the dependency wait
     int nfn[6] = { -1, -1, -1, -1, -1, -1 };
@@ -254,7 +258,7 @@ __device__ __forceinline__ void pass0_body( const Pass0Args& a, unsigned bid, un
         cwA = *reinterpret_cast<const uint4*>( a.F.code + (size_t)t * 512 + 8 * lane );
         cwB = *reinterpret_cast<const uint4*>( a.F.code + (size_t)t * 512 + 256 + 8 * lane );
     };
-    int s = (int)bid * kPassWarps + ( threadIdx.x >> 5 );
+    int s = (int)bid * W + ( threadIdx.x >> 5 );
     fetch( s );
     bora_pdl_wait();  // the previous kernel's results are complete from here
     if( threadIdx.x == 0 ) s_sc = scale_from( a.red.ring, a.slot_rr );
@@ -384,14 +388,14 @@ __device__ __forceinline__ void pass0_body( const Pass0Args& a, unsigned bid, un
     if constexpr( P == 3 ) reduce2_publish_warp( df_warp_sum( rz ), 0.0, 0, a.red, a.slot_rz, -1, bid, G );
 }
 
-template <int P>
-__global__ void __launch_bounds__( 32 * kPassWarps ) k_mg_pass0( const __grid_constant__ Pass0Args a )
+template <int W, int P>
+__global__ void __launch_bounds__( 32 * W, 16 / W ) k_mg_pass0( const __grid_constant__ Pass0Args a )
 {
-    pass0_body<P>( a, blockIdx.x, gridDim.x );
+    pass0_body<W, P>( a, blockIdx.x, gridDim.x );
 }
 
-template <int P>
-__global__ void __launch_bounds__( 32 * kPassWarps ) k_mg_pass0_batch( const __grid_constant__ BoraBatchLaunch L )
+template <int W, int P>
+__global__ void __launch_bounds__( 32 * W, 16 / W ) k_mg_pass0_batch( const __grid_constant__ BoraBatchLaunch L )
 {
     unsigned bid;
     const int k = bora_batch_member( L, blockIdx.x, &bid );
@@ -408,7 +412,7 @@ __global__ void __launch_bounds__( 32 * kPassWarps ) k_mg_pass0_batch( const __g
     a.red = m.red;
     a.slot_rr = q.rr;
     a.slot_rz = q.rz;
-    pass0_body<P>( a, bid, (unsigned)m.grid[kGridPass0] );
+    pass0_body<W, P>( a, bid, (unsigned)m.grid[P == 3 ? kGridPass0R : kGridPass0] );
 }
 
 // ---- levels 1 and 2: one thread per cell --------------------------------------------------
@@ -427,17 +431,17 @@ struct PassFArgs
 // per thread (the grid covers every cell once; a block holds whole tiles). What no kernel of
 // the solve writes - the cell's code, its neighbours' indices and codes - is read before the
 // dependency wait, so that it overlaps the previous kernel.
-template <int E, int P>
+template <int E, int P, int T>
 __device__ __forceinline__ void passf_body( const PassFArgs& a, unsigned bid )
 {
     constexpr int E3 = E * E * E, H = E / 2, H3 = H * H * H;
     constexpr bool kCodes = P == 0 || P == 2;  // the neighbours' values need their codes
     __shared__ float w[32];
-    __shared__ float res[kFlatThreads];
+    __shared__ float res[T];
     bora_pdl_trigger();
     init_weights( w );
     const size_t ncells = (size_t)a.ntiles * E3;
-    const size_t base = (size_t)bid * kFlatThreads, g = base + threadIdx.x;
+    const size_t base = (size_t)bid * T, g = base + threadIdx.x;
     const bool live = g < ncells;
     const BoraLevelDev& F = a.F;
     int s = 0, x = 0, y = 0, z = 0;
@@ -499,7 +503,7 @@ __device__ __forceinline__ void passf_body( const PassFArgs& a, unsigned bid )
         // restriction of the block's tiles
         res[threadIdx.x] = out;
         __syncthreads();
-        constexpr int kParents = kFlatThreads / 8;
+        constexpr int kParents = T / 8;
         if( threadIdx.x < kParents )
         {
             const int p = threadIdx.x, tl = p / H3, pl = p % H3;
@@ -516,14 +520,14 @@ __device__ __forceinline__ void passf_body( const PassFArgs& a, unsigned bid )
     }
 }
 
-template <int E, int P>
-__global__ void __launch_bounds__( kFlatThreads ) k_mg_passf( const __grid_constant__ PassFArgs a )
+template <int E, int P, int T>
+__global__ void __launch_bounds__( T ) k_mg_passf( const __grid_constant__ PassFArgs a )
 {
-    passf_body<E, P>( a, blockIdx.x );
+    passf_body<E, P, T>( a, blockIdx.x );
 }
 
-template <int E, int P>
-__global__ void __launch_bounds__( kFlatThreads ) k_mg_passf_batch( const __grid_constant__ BoraBatchLaunch L )
+template <int E, int P, int T>
+__global__ void __launch_bounds__( T ) k_mg_passf_batch( const __grid_constant__ BoraBatchLaunch L )
 {
     constexpr int l = E == 4 ? 1 : 2;
     unsigned bid;
@@ -536,7 +540,7 @@ __global__ void __launch_bounds__( kFlatThreads ) k_mg_passf_batch( const __grid
     a.C = m.L[l + 1];
     a.ec = l == 1 ? m.L[2].z1 : m.z3;
     a.scratch = m.sv.minv;
-    passf_body<E, P>( a, bid );
+    passf_body<E, P, T>( a, bid );
 }
 
 int num_sms_pass()
@@ -551,101 +555,137 @@ int num_sms_pass()
 }
 
 template <int E, int P>
-void launch_passf( const PassFArgs& a, cudaStream_t st )
+void launch_passf( const PassFArgs& a, int v, cudaStream_t st )
 {
-    const int g = bora_mg_pass_grid( E, a.ntiles );
-    if( g > 0 ) bora_launch_pdl( k_mg_passf<E, P>, dim3( g ), dim3( kFlatThreads ), 0, st, a );
+    const int g = bora_mg_pass_grid( E, a.ntiles, v );
+    if( g <= 0 ) return;
+    switch( v )
+    {
+    case 0: bora_launch_pdl( k_mg_passf<E, P, 64>, dim3( g ), dim3( 64 ), 0, st, a ); break;
+    case 1: bora_launch_pdl( k_mg_passf<E, P, 128>, dim3( g ), dim3( 128 ), 0, st, a ); break;
+    case 2: bora_launch_pdl( k_mg_passf<E, P, 256>, dim3( g ), dim3( 256 ), 0, st, a ); break;
+    default: bora_launch_pdl( k_mg_passf<E, P, 512>, dim3( g ), dim3( 512 ), 0, st, a ); break;
+    }
 }
 
 template <int P>
-void launch_pass0( const Pass0Args& a, cudaStream_t st )
+void launch_pass0( const Pass0Args& a, int v, cudaStream_t st )
 {
-    const int g = bora_mg_pass_grid( 8, a.ntiles );
-    if( g > 0 ) bora_launch_pdl( k_mg_pass0<P>, dim3( g ), dim3( 32 * kPassWarps ), 0, st, a );
+    const int g = bora_mg_pass_grid( 8, a.ntiles, v );
+    if( g <= 0 ) return;
+    switch( v )
+    {
+    case 0: bora_launch_pdl( k_mg_pass0<2, P>, dim3( g ), dim3( 64 ), 0, st, a ); break;
+    case 1: bora_launch_pdl( k_mg_pass0<4, P>, dim3( g ), dim3( 128 ), 0, st, a ); break;
+    default: bora_launch_pdl( k_mg_pass0<8, P>, dim3( g ), dim3( 256 ), 0, st, a ); break;
+    }
 }
 
 }  // namespace
 
-// Grid of the passes of a level with E cells per tile edge: level 0 as many blocks as make
-// equal rounds of warps over the tiles with up to 8 blocks per SM (the up 2 pass reduces over
-// them: at most kBoraMaxReduceBlocks); levels 1 and 2 one thread per cell.
-int bora_mg_pass_grid( int E, int ntiles )
+// Grid of the passes of a level with E cells per tile edge in launch shape v: level 0 as many
+// blocks as make equal rounds of warps over the tiles with up to 16 warps per SM (the up 2 pass,
+// shape kReduceWarps, reduces over them: at most kBoraMaxReduceBlocks); levels 1 and 2 one
+// thread per cell.
+int bora_mg_pass_grid( int E, int ntiles, int v )
 {
     if( ntiles <= 0 ) return 0;
     const int sms = num_sms_pass();
     if( E == 8 )
     {
-        const int cap = std::max( 1, std::min( 8 * sms, kBoraMaxReduceBlocks ) ) * kPassWarps;
+        const int W = v < 0 ? kReduceWarps : kPassWarpsOf[std::min( v, 2 )];
+        const int cap = std::max( 1, std::min( 32 / W * sms, kBoraMaxReduceBlocks ) ) * W;
         const int rounds = ( ntiles + cap - 1 ) / cap;
-        return std::max( 1, ( ntiles + kPassWarps * rounds - 1 ) / ( kPassWarps * rounds ) );
+        return std::max( 1, ( ntiles + W * rounds - 1 ) / ( W * rounds ) );
     }
+    const int T = kFlatThreadsOf[std::min( std::max( v, 0 ), 3 )];
     const size_t n = (size_t)ntiles * E * E * E;
-    return (int)( ( n + kFlatThreads - 1 ) / kFlatThreads );
+    return (int)( ( n + T - 1 ) / T );
 }
 
 void bora_mg_pass_down( const BoraLevelDev* levels, int l, const BoraTilesDev& t, int ntiles, const float* r0,
                         float* scratch, const BoraReduceDev& red, int slot_rr, cudaStream_t st )
 {
+    const int group = l == 0 ? kBoraTuneL0 : ( l == 1 ? kBoraTuneL1 : kBoraTuneL2 );
+    const BoraTunePick pick = bora_tune_pick( group, ntiles );
+    BoraTuneTimer timer( pick, group, ntiles, st );  // times the level's two down passes
+    const int v = pick.variant;
     if( levels[l].E == 8 )
     {
         Pass0Args a{};
         a.ntiles = ntiles; a.nbr = t.nbr; a.F = levels[0]; a.C = levels[1]; a.r0 = r0; a.scratch = scratch;
         a.red = red; a.slot_rr = slot_rr; a.slot_rz = -1;
-        launch_pass0<0>( a, st );
-        launch_pass0<1>( a, st );
+        launch_pass0<0>( a, v, st );
+        launch_pass0<1>( a, v, st );
         return;
     }
     PassFArgs a{};
     a.ntiles = ntiles; a.nbr = t.nbr; a.F = levels[l]; a.C = levels[l + 1]; a.scratch = scratch;
-    if( levels[l].E == 4 ) { launch_passf<4, 0>( a, st ); launch_passf<4, 1>( a, st ); }
-    else { launch_passf<2, 0>( a, st ); launch_passf<2, 1>( a, st ); }
+    if( levels[l].E == 4 ) { launch_passf<4, 0>( a, v, st ); launch_passf<4, 1>( a, v, st ); }
+    else { launch_passf<2, 0>( a, v, st ); launch_passf<2, 1>( a, v, st ); }
 }
 
 void bora_mg_pass_up( const BoraLevelDev* levels, int l, const __half* ec, const BoraTilesDev& t, int ntiles,
                       const float* r0, float* scratch, const BoraReduceDev& red, int slot_rr, float* z, int slot_rz,
                       cudaStream_t st )
 {
+    const int group = l == 0 ? kBoraTuneL0 : ( l == 1 ? kBoraTuneL1 : kBoraTuneL2 );
+    const int v = bora_tune_pick( group, ntiles ).variant;
     if( levels[l].E == 8 )
     {
         Pass0Args a{};
         a.ntiles = ntiles; a.nbr = t.nbr; a.F = levels[0]; a.C = levels[1]; a.C.z1 = const_cast<__half*>( ec );
         a.r0 = r0; a.scratch = scratch; a.zout = z; a.red = red; a.slot_rr = slot_rr; a.slot_rz = slot_rz;
-        launch_pass0<2>( a, st );
-        launch_pass0<3>( a, st );
+        launch_pass0<2>( a, v, st );
+        // r.z: the fixed shape
+        const int g = bora_mg_pass_grid( 8, ntiles, -1 );
+        if( g > 0 ) bora_launch_pdl( k_mg_pass0<kReduceWarps, 3>, dim3( g ), dim3( 32 * kReduceWarps ), 0, st, a );
         return;
     }
     PassFArgs a{};
     a.ntiles = ntiles; a.nbr = t.nbr; a.F = levels[l]; a.C = levels[l + 1]; a.ec = ec; a.scratch = scratch;
-    if( levels[l].E == 4 ) { launch_passf<4, 2>( a, st ); launch_passf<4, 3>( a, st ); }
-    else { launch_passf<2, 2>( a, st ); launch_passf<2, 3>( a, st ); }
+    if( levels[l].E == 4 ) { launch_passf<4, 2>( a, v, st ); launch_passf<4, 3>( a, v, st ); }
+    else { launch_passf<2, 2>( a, v, st ); launch_passf<2, 3>( a, v, st ); }
 }
 
-void bora_launch_mg_pass_batch( int l, int pass, const BoraBatchLaunch& L, int blocks, cudaStream_t st )
+void bora_launch_mg_pass_batch( int l, int pass, int v, const BoraBatchLaunch& L, int blocks, cudaStream_t st )
 {
     if( blocks <= 0 ) return;
     const dim3 grid( blocks );
     if( l == 0 )
     {
-        const dim3 blk( 32 * kPassWarps );
-        if( pass == 0 ) bora_launch_pdl( k_mg_pass0_batch<0>, grid, blk, 0, st, L );
-        else if( pass == 1 ) bora_launch_pdl( k_mg_pass0_batch<1>, grid, blk, 0, st, L );
-        else if( pass == 2 ) bora_launch_pdl( k_mg_pass0_batch<2>, grid, blk, 0, st, L );
-        else bora_launch_pdl( k_mg_pass0_batch<3>, grid, blk, 0, st, L );
+        if( pass == 3 )
+        {
+            bora_launch_pdl( k_mg_pass0_batch<kReduceWarps, 3>, grid, dim3( 32 * kReduceWarps ), 0, st, L );
+            return;
+        }
+        const int W = kPassWarpsOf[std::min( std::max( v, 0 ), 2 )];
+        const dim3 blk( 32 * W );
+        auto go = [&]( auto k0, auto k1, auto k2 ) {
+            if( pass == 0 ) bora_launch_pdl( k0, grid, blk, 0, st, L );
+            else if( pass == 1 ) bora_launch_pdl( k1, grid, blk, 0, st, L );
+            else bora_launch_pdl( k2, grid, blk, 0, st, L );
+        };
+        if( W == 2 ) go( k_mg_pass0_batch<2, 0>, k_mg_pass0_batch<2, 1>, k_mg_pass0_batch<2, 2> );
+        else if( W == 4 ) go( k_mg_pass0_batch<4, 0>, k_mg_pass0_batch<4, 1>, k_mg_pass0_batch<4, 2> );
+        else go( k_mg_pass0_batch<8, 0>, k_mg_pass0_batch<8, 1>, k_mg_pass0_batch<8, 2> );
         return;
     }
-    const dim3 blk( kFlatThreads );
-    if( l == 1 )
-    {
-        if( pass == 0 ) bora_launch_pdl( k_mg_passf_batch<4, 0>, grid, blk, 0, st, L );
-        else if( pass == 1 ) bora_launch_pdl( k_mg_passf_batch<4, 1>, grid, blk, 0, st, L );
-        else if( pass == 2 ) bora_launch_pdl( k_mg_passf_batch<4, 2>, grid, blk, 0, st, L );
-        else bora_launch_pdl( k_mg_passf_batch<4, 3>, grid, blk, 0, st, L );
-    }
-    else
-    {
-        if( pass == 0 ) bora_launch_pdl( k_mg_passf_batch<2, 0>, grid, blk, 0, st, L );
-        else if( pass == 1 ) bora_launch_pdl( k_mg_passf_batch<2, 1>, grid, blk, 0, st, L );
-        else if( pass == 2 ) bora_launch_pdl( k_mg_passf_batch<2, 2>, grid, blk, 0, st, L );
-        else bora_launch_pdl( k_mg_passf_batch<2, 3>, grid, blk, 0, st, L );
-    }
+    const int T = kFlatThreadsOf[std::min( std::max( v, 0 ), 3 )];
+    auto flat = [&]( auto tag ) {
+        constexpr int E = decltype( tag )::value;
+        auto go = [&]( auto k0, auto k1, auto k2, auto k3 ) {
+            const dim3 blk( T );
+            if( pass == 0 ) bora_launch_pdl( k0, grid, blk, 0, st, L );
+            else if( pass == 1 ) bora_launch_pdl( k1, grid, blk, 0, st, L );
+            else if( pass == 2 ) bora_launch_pdl( k2, grid, blk, 0, st, L );
+            else bora_launch_pdl( k3, grid, blk, 0, st, L );
+        };
+        if( T == 64 ) go( k_mg_passf_batch<E, 0, 64>, k_mg_passf_batch<E, 1, 64>, k_mg_passf_batch<E, 2, 64>, k_mg_passf_batch<E, 3, 64> );
+        else if( T == 128 ) go( k_mg_passf_batch<E, 0, 128>, k_mg_passf_batch<E, 1, 128>, k_mg_passf_batch<E, 2, 128>, k_mg_passf_batch<E, 3, 128> );
+        else if( T == 256 ) go( k_mg_passf_batch<E, 0, 256>, k_mg_passf_batch<E, 1, 256>, k_mg_passf_batch<E, 2, 256>, k_mg_passf_batch<E, 3, 256> );
+        else go( k_mg_passf_batch<E, 0, 512>, k_mg_passf_batch<E, 1, 512>, k_mg_passf_batch<E, 2, 512>, k_mg_passf_batch<E, 3, 512> );
+    };
+    if( l == 1 ) flat( std::integral_constant<int, 4>{} );
+    else flat( std::integral_constant<int, 2>{} );
 }

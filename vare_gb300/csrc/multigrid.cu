@@ -887,13 +887,14 @@ void bora_mg_vcycle( const BoraGridDev& g, const BoraLevelDev* levels, int nleve
     }
 }
 
-void bora_member_grids( int ntiles, int* grid )
+void bora_member_grids( int ntiles, int* grid, const int* v )
 {
     bora_projection_grids( ntiles, grid );
     grid[kGridUpd] = blocks_for( (size_t)std::max( ntiles, 0 ) * 512 / 4 );
-    grid[kGridPass0] = bora_mg_pass_grid( 8, ntiles );
-    grid[kGridPass1] = bora_mg_pass_grid( 4, ntiles );
-    grid[kGridPass2] = bora_mg_pass_grid( 2, ntiles );
+    grid[kGridPass0] = bora_mg_pass_grid( 8, ntiles, v[0] );
+    grid[kGridPass0R] = bora_mg_pass_grid( 8, ntiles, -1 );
+    grid[kGridPass1] = bora_mg_pass_grid( 4, ntiles, v[1] );
+    grid[kGridPass2] = bora_mg_pass_grid( 2, ntiles, v[2] );
 }
 
 void bora_launch_pcg_update_noprec_batch( const BoraBatchLaunch& L, int blocks, cudaStream_t st )

@@ -118,6 +118,8 @@ _SIGS = {
     "bora_flip_status_string": (ctypes.c_char_p, [ctypes.c_int]),
     "bora_flip_set_profiling": (ctypes.c_int, [_vp, ctypes.c_uint32]),
     "bora_flip_get_kernel_times": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int]),
+    "bora_flip_set_tuning": (ctypes.c_int, [ctypes.c_int]),
+    "bora_flip_tune_table": (ctypes.c_int, [_vp, ctypes.c_size_t, _vp]),
     "bora_scan_u32": (ctypes.c_int, [_vp, _vp, ctypes.c_size_t, _vp, _vp]),
     "bora_scan_u32_noalloc": (ctypes.c_int, [_vp, _vp, ctypes.c_size_t, _vp, _vp]),
 }
@@ -188,6 +190,25 @@ def scene_params(scene, **overrides) -> Params:
               proj_iteration=10000)
     kw.update(overrides)
     return default_params(**kw)
+
+
+def set_tuning(on: bool) -> None:
+    """bora_flip_set_tuning: the launch-shape autotuner on (default) or off."""
+    _check(load().bora_flip_set_tuning(1 if on else 0), "set_tuning")
+
+
+def tune_table() -> list[tuple[int, int, int, int, float]]:
+    """bora_flip_tune_table: (group, device, size class, chosen shape or -1, median ms) rows."""
+    lib = load()
+    n = ctypes.c_size_t(0)
+    _check(lib.bora_flip_tune_table(None, 0, ctypes.byref(n)), "tune_table")
+    buf = ctypes.create_string_buffer(n.value + 1)
+    _check(lib.bora_flip_tune_table(buf, n.value + 1, ctypes.byref(n)), "tune_table")
+    rows = []
+    for line in buf.value.decode().splitlines():
+        g, d, c, v, m = line.split()
+        rows.append((int(g), int(d), int(c), int(v), float(m)))
+    return rows
 
 
 def step_batch(sims, dt: float) -> list[int]:
