@@ -86,6 +86,7 @@ def parse():
                     help="skip the parity report (one step of each solver form against the oracle's FP64 "
                          "projection from the state the timed steps left)")
     ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--no-persistent", action="store_true", help="skip the persistent plain-PCG measurement")
     ap.add_argument("--solver", default="both", choices=["both", "plain", "mixed"],
                     help="plain only / mixed only (profiling runs); the default times both")
     return ap.parse_args()
@@ -598,6 +599,21 @@ def run_ours(args, world, rank, local):
                "how": "host wall time of bora_flip_set_particles (pinned host -> device) + bora_flip_step + "
                       "bora_flip_get_particles (device -> pinned host) per step"}
 
+    # the plain form with each refinement pass's inner PCG in one cooperative launch
+    # (bounded grid barriers between the phases; bora_flip_params.persistent = 1)
+    persistent = None
+    if args.solver != "mixed" and not args.no_persistent:
+        del sim
+        torch.cuda.empty_cache()
+        sim = flip.FlipSim.from_scene(sc, solver=flip.SOLVER_PLAIN, persistent=1)
+        pm = timed_steps(sim, sc, args, world, flip, local, False, ALG_BYTES)
+        persistent = {"value": pm["value"], "unit": UNIT, "ms_per_step": pm["ms_per_step"], "p50_ms": pm["p50_ms"],
+                      "p99_ms": pm["p99_ms"], "gpu_launches": pm["launches"],
+                      "iterations_per_step": pm["solver"]["iterations_per_step"],
+                      "config": "same scene and stop rule; each refinement pass's inner PCG (first update, then "
+                                "direction and update per iteration) in one cooperative launch whose phases meet at "
+                                "grid barriers with bounded waits, convergence checked on the device"}
+
     # mixed-precision form on the same scene: MG-preconditioned CG, FP16 V-cycle storage
     mixed = None
     if not args.no_mixed:
@@ -658,7 +674,7 @@ def run_ours(args, world, rank, local):
            "config": workload_config(sc, solver=args.solver if args.solver != "both" else "plain"), "roofline": roof,
            "cpu_baseline": cpu, "e2e": e2e,
            "gpu_launches": int(launches), "clocks": clk, "solver": meas["solver"], "step_roofline": meas["step_roofline"],
-           "mixed": mixed, "post_process": post, "serve": serve_res}
+           "plain_persistent": persistent, "mixed": mixed, "post_process": post, "serve": serve_res}
     print(json.dumps(out), flush=True)
 
 

@@ -92,6 +92,10 @@ typedef struct bora_flip_params
                                 velocity field, per substep */
     int post_process;        /* 1: bora_flip_frame post-processes after the step, as
                                 FLIPMethod::advanceOneFrame does (FLIPMethod.cu:177-206) */
+    int persistent;          /* 0: one launch per PCG phase, convergence read back by the host
+                                (check_every); 1: the plain form runs each refinement pass's inner
+                                PCG in one cooperative launch whose phases meet at bounded grid
+                                barriers and which checks convergence itself */
 } bora_flip_params;
 
 typedef struct bora_flip_stats
@@ -314,6 +318,15 @@ int bora_flip_set_profiling( bora_flip_handle h, uint32_t class_mask );
 /* Accumulated device milliseconds and launch counts per kernel class (n <= 16 entries). */
 int bora_flip_get_kernel_times( bora_flip_handle h, double* ms, uint64_t* launches, int n );
 const char* bora_flip_status_string( int status );
+
+/* Fault injection for tests of the error paths (no counterpart in the reference).
+ * BORA_FAULT_BARRIER: the next solves' grid barriers (persistent plain PCG) wait for one
+ * block more than they launch, so every wait runs out after a short limit, the kernel
+ * returns, and the step returns BORA_ERR_INTERNAL with the handle still usable.
+ * BORA_FAULT_NONE clears it. */
+#define BORA_FAULT_NONE 0
+#define BORA_FAULT_BARRIER 1
+int bora_flip_set_fault( bora_flip_handle h, int fault );
 
 /* Launch-shape autotuner (process-wide; no counterpart in the reference). Kernels with
  * several launch shapes that compute the same bits (the multigrid passes of levels 0-2:

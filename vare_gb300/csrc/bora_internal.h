@@ -200,6 +200,17 @@ void bora_launch_solve_init( int ntiles, const float* b, const uint16_t* code, B
 void bora_launch_pcg_update( int ntiles, const uint16_t* code, BoraSolverDev s, BoraReduceDev red, int slot_rz_in,
                              int slot_dq_in, int slot_rz_out, int slot_rr_out, cudaStream_t st );
 // d' = z + beta d; q = A d'; dq -> ring slot (beta = rz_new / rz_old, or 0 when slot_rz_old < 0)
+// One refinement pass of the plain form's inner PCG in one cooperative launch with bounded
+// grid barriers (projection.cu). Outputs: ring slots slot_a_rz / slot_a_dq (the last
+// update's alpha, whose e += alpha d is pending), slot_rr (the last r.r), *iters. bar: two
+// zeroed words; part: 3 * bora_pcg_persistent_grid() doubles. never_release: every barrier
+// wait runs out (a test of the error path). Returns 0, or -1 when the launch is refused.
+#define BORA_REDUCE_ERR_BARRIER 0x100u  // a grid barrier wait ran out
+int bora_pcg_persistent_grid();
+int bora_launch_pcg_persistent( int ntiles, const int32_t* nbr, const uint16_t* code, BoraSolverDev s, BoraReduceDev red,
+                                int dsel, int slot_rz_prev, int max_inner, double target, int slot_a_rz, int slot_a_dq,
+                                int slot_rr, uint32_t* iters, unsigned* bar, double* part, bool never_release,
+                                cudaStream_t st );
 void bora_launch_pcg_direction( const BoraGridDev& g, int ntiles, BoraTilesDev t, const uint16_t* code, BoraSolverDev s,
                                 int dsel_in, BoraReduceDev red, int slot_rz_new, int slot_rz_old, int slot_dq_out,
                                 int slot_a_rz, int slot_a_dq, cudaStream_t st );

@@ -153,6 +153,8 @@ struct bora_flip_sim
 
     // reductions
     DevBuf ring, partials, done;
+    DevBuf gbar;     // the persistent solver's grid barrier: count, generation
+    int fault = 0;   // BORA_FAULT_*
     int next_slot = 0;
 
     // particles
@@ -402,7 +404,8 @@ int ensure_cells( bora_flip_sim* s, int ntiles )
     BORA_TRY( grow( s->cell_start, ( nc + 2 ) * 4, false, s->st ) );
     BORA_TRY( grow( s->tile_of, cap * 4, false, s->st ) );
     BORA_TRY( grow( s->nbr, cap * 27 * 4, false, s->st ) );
-    BORA_TRY( grow( s->partials, ( std::max<size_t>( cap, kBoraMaxReduceBlocks ) + 16 ) * 2 * 8, false, s->st ) );
+    // two values per block for the reductions; three for the persistent solver's
+    BORA_TRY( grow( s->partials, ( std::max<size_t>( cap, kBoraMaxReduceBlocks ) + 16 ) * 3 * 8, false, s->st ) );
     BORA_TRYS( ensure_scan_scratch( s, std::max( nc + 2, s->ntv ) ) );
     s->cap_tiles = cap;
     return BORA_OK;
@@ -646,7 +649,31 @@ int stage_solve( bora_flip_sim* s )
                             st );
         };
         int rz_cur = s->slot(), rr_cur = s->slot();
-        if( mixed )
+        int it = 0;
+        int a_rz = -1, a_dq = -1;  // alpha of the last update, whose e += alpha d is still pending
+        if( !mixed && p.persistent && bora_pcg_persistent_grid() > 0 )
+        {
+            // the whole pass in one cooperative launch (convergence checked on the device)
+            const int s_a_rz = s->slot(), s_a_dq = s->slot();
+            BORA_TRY( cudaMemsetAsync( P<uint32_t>( s->counters ) + 8, 0, 4, st ) );
+            {
+                KTimer t( s, BORA_KERNEL_PCG_UPDATE, 1 );
+                if( bora_launch_pcg_persistent( s->ntiles, P<int32_t>( s->nbr ), code, sv, red, dsel, rz_prev, max_inner, target,
+                                                s_a_rz, s_a_dq, rr_cur, P<uint32_t>( s->counters ) + 8,
+                                                P<unsigned>( s->gbar ), P<double>( s->partials ),
+                                                s->fault == BORA_FAULT_BARRIER, st ) != 0 )
+                    return BORA_ERR_CUDA;
+            }
+            BORA_TRYS( check_launch( s ) );
+            BORA_TRYS( read_counters( s, 5, 4 ) );
+            if( s->h_cnt[5] & BORA_REDUCE_ERR_BARRIER ) return BORA_ERR_INTERNAL;
+            it = (int)s->h_cnt[8];
+            dsel ^= it & 1;
+            a_rz = s_a_rz;
+            a_dq = s_a_dq;
+            rz_prev = s_a_rz;
+        }
+        else if( mixed )
         {
             { KTimer t( s, BORA_KERNEL_PCG_UPDATE, 1 ); bora_launch_pcg_update_noprec( s->ntiles, sv, red, -1, -1, rr_cur, st ); }
             precondition( rr_cur, rz_cur );
@@ -663,9 +690,7 @@ int stage_solve( bora_flip_sim* s )
         struct Check { int it, q, slot; };
         Check pend[bora_flip_sim::kChecks];
         int npend = 0, nchk = 0;
-        bool done = false;
-        int it = 0;
-        int a_rz = -1, a_dq = -1;  // alpha of the last update, whose e += alpha d is still pending
+        bool done = a_rz >= 0;  // the persistent pass has run
         while( it < max_inner && !done )
         {
             const int s_dq = s->slot();
@@ -917,7 +942,7 @@ void for_each_buffer( bora_flip_sim* s, F&& f )
                       &s->se, &s->sr, &s->sd0, &s->sd1, &s->sq, &s->sz, &s->sminv, &s->cell_count, &s->cell_start,
                       &s->ring, &s->partials, &s->done, &s->adj, &s->vkey, &s->key, &s->idx, &s->scan_scratch,
                       &s->counters, &s->stage_in, &s->stage_out, &s->live_flag, &s->col_phi, &s->col_vel,
-                      &s->col_tslot, &s->col_tnear, &s->col_tphi, &s->col_tvel };
+                      &s->col_tslot, &s->col_tnear, &s->col_tphi, &s->col_tvel, &s->gbar };
     for( DevBuf* b : all ) f( *b );
     for( int q = 0; q < 2; ++q )
     {
@@ -963,6 +988,7 @@ int bora_flip_default_params( bora_flip_params* o )
     o->check_every = 1;
     o->advection = BORA_ADVECT_EULER;
     o->post_process = 1;
+    o->persistent = 0;
     return BORA_OK;
 }
 
@@ -973,6 +999,7 @@ static int validate_params( const bora_flip_params* p )
     if( p->solver != BORA_SOLVER_PLAIN && p->solver != BORA_SOLVER_MIXED ) return BORA_ERR_INVALID_ARG;
     if( p->advection != BORA_ADVECT_EULER && p->advection != BORA_ADVECT_RK2 ) return BORA_ERR_INVALID_ARG;
     if( !( p->voxel_size > 0.f ) || !( p->tolerance > 0.0 ) ) return BORA_ERR_INVALID_ARG;
+    if( p->persistent != 0 && p->persistent != 1 ) return BORA_ERR_INVALID_ARG;
     return BORA_OK;
 }
 
@@ -1016,6 +1043,7 @@ int bora_flip_create( const bora_grid_desc* grid, const bora_flip_params* params
     if( st == BORA_OK ) st = cuda_status( grow( s->counters, 64, false, s->st ) );
     if( st == BORA_OK ) st = cuda_status( grow( s->ring, BORA_RING * 8, false, s->st ) );
     if( st == BORA_OK ) st = cuda_status( grow( s->done, BORA_RING * 4, false, s->st ) );
+    if( st == BORA_OK ) st = cuda_status( grow( s->gbar, 16, false, s->st ) );
     if( st == BORA_OK ) st = cuda_status( cudaMemsetAsync( s->done.p, 0, BORA_RING * 4, s->st ) );
     if( st == BORA_OK ) st = cuda_status( cudaMemsetAsync( s->ring.p, 0, BORA_RING * 8, s->st ) );
     if( st == BORA_OK ) st = ensure_cells( s, 1 );
@@ -2166,6 +2194,13 @@ int bora_flip_get_stats( bora_flip_handle s, bora_flip_stats* o )
     uint64_t bytes = 0;
     for_each_buffer( s, [&]( DevBuf& b ) { bytes += b.bytes; } );
     o->device_bytes = bytes;
+    return BORA_OK;
+}
+
+int bora_flip_set_fault( bora_flip_handle s, int fault )
+{
+    if( !s || ( fault != BORA_FAULT_NONE && fault != BORA_FAULT_BARRIER ) ) return BORA_ERR_INVALID_ARG;
+    s->fault = fault;
     return BORA_OK;
 }
 

@@ -281,23 +281,16 @@ constexpr int kWarps = 4;  // 4 x 5.9 KB of buffers per CTA; five CTAs per SM at
 }  // namespace micsweep
 constexpr int kUpdWarps = micsweep::kWarps;
 
-__global__ void __launch_bounds__( 32 * kUpdWarps, 5 ) k_pcg_update( int ntiles, BoraSolverDev sv, BoraReduceDev red,
-                                                                  int slot_rz_in, int slot_dq_in, int slot_rz_out,
-                                                                  int slot_rr_out )
+// The update of the warp's tiles first, first + tstride, ...: r -= alpha q, z = M^-1 r; r.z and
+// r.r accumulated into prz, prr. sv_w, sp_w: the warp's two sweep buffers (kBuf floats each,
+// zeroed before the first call; the sweeps keep their guard cells zero).
+__device__ __forceinline__ void pcg_update_tiles( int ntiles, const BoraSolverDev& sv, float alpha, int first, int tstride,
+                                                  float* sv_w, float* sp_w, DF& prz, DF& prr )
 {
     using namespace micsweep;
-    __shared__ __align__( 16 ) float sval[kUpdWarps][kBuf];
-    __shared__ __align__( 16 ) float spiv[kUpdWarps][kBuf];
-    __shared__ float s_alpha;
-    bora_pdl_trigger();
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    float* const V = sval[w] + kGuard;  // tile cell (i, j, k) at V[i + 8 j + kPlane k]
-    float* const P = spiv[w] + kGuard;
-    for( int q = lane; q < kBuf; q += 32 ) { sval[w][q] = 0.f; spiv[w][q] = 0.f; }
-    bora_pdl_wait();  // the previous kernel's results are complete from here
-    if( threadIdx.x == 0 ) s_alpha = slot_rz_in < 0 ? 0.f : (float)( red.ring[slot_rz_in] / red.ring[slot_dq_in] );
-    __syncthreads();
-    const float alpha = s_alpha;
+    const int lane = threadIdx.x & 31;
+    float* const V = sv_w + kGuard;  // tile cell (i, j, k) at V[i + 8 j + kPlane k]
+    float* const P = sp_w + kGuard;
     const int j = lane & 7, kq = lane >> 3, sA = j + kq;  // plane offset of row A; row B: sA + 4
     const bool has_ym = j > 0, has_yp = j < 7, has_zmA = kq > 0, has_zpB = kq < 3;
     // cell of row A at step u: VA + u (row B: VB + u)
@@ -349,8 +342,6 @@ __global__ void __launch_bounds__( 32 * kUpdWarps, 5 ) k_pcg_update( int ntiles,
             asm volatile( "cp.async.bulk.prefetch.L2.global [%0], 2048;" ::"l"( src ) : "memory" );
         }
     };
-    DF prz{ 0.f, 0.f }, prr{ 0.f, 0.f };
-    const int tstride = gridDim.x * kUpdWarps;
     // the next tile's r, q and pivots are loaded into registers before this tile's sweeps
     float4 rn[4], qn[4], mn[4];
     auto load_tile = [&]( int s ) {
@@ -364,8 +355,8 @@ __global__ void __launch_bounds__( 32 * kUpdWarps, 5 ) k_pcg_update( int ntiles,
             mn[m] = m4[o];
         }
     };
-    load_tile( blockIdx.x * kUpdWarps + w );
-    for( int s = blockIdx.x * kUpdWarps + w; s < ntiles; s += tstride )
+    load_tile( first );
+    for( int s = first; s < ntiles; s += tstride )
     {
         const size_t b4 = (size_t)s * 128 + lane;
         float4 r[4];
@@ -430,6 +421,24 @@ __global__ void __launch_bounds__( 32 * kUpdWarps, 5 ) k_pcg_update( int ntiles,
         }
         __syncwarp();
     }
+}
+
+__global__ void __launch_bounds__( 32 * kUpdWarps, 5 ) k_pcg_update( int ntiles, BoraSolverDev sv, BoraReduceDev red,
+                                                                  int slot_rz_in, int slot_dq_in, int slot_rz_out,
+                                                                  int slot_rr_out )
+{
+    using namespace micsweep;
+    __shared__ __align__( 16 ) float sval[kUpdWarps][kBuf];
+    __shared__ __align__( 16 ) float spiv[kUpdWarps][kBuf];
+    __shared__ float s_alpha;
+    bora_pdl_trigger();
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for( int q = lane; q < kBuf; q += 32 ) { sval[w][q] = 0.f; spiv[w][q] = 0.f; }
+    bora_pdl_wait();  // the previous kernel's results are complete from here
+    if( threadIdx.x == 0 ) s_alpha = slot_rz_in < 0 ? 0.f : (float)( red.ring[slot_rz_in] / red.ring[slot_dq_in] );
+    __syncthreads();
+    DF prz{ 0.f, 0.f }, prr{ 0.f, 0.f };
+    pcg_update_tiles( ntiles, sv, s_alpha, blockIdx.x * kUpdWarps + w, gridDim.x * kUpdWarps, sval[w], spiv[w], prz, prr );
     reduce2_publish_df( prz, prr, red, slot_rz_out, slot_rr_out );
 }
 
@@ -468,22 +477,12 @@ __device__ inline size_t face_nbr( const int32_t* __restrict__ nbr, size_t cell,
 // sum.
 constexpr int kDirWarps = 4;
 
-__device__ __forceinline__ void pcg_direction_body( int ntiles, const int32_t* __restrict__ nbr,
-                                                    const uint16_t* __restrict__ code, const BoraSolverDev& sv, int dsel_in,
-                                                    const BoraReduceDev& red, int slot_rz_new, int slot_rz_old,
-                                                    int slot_dq_out, int slot_a_rz, int slot_a_dq, unsigned bid, unsigned G )
+// The direction step of the warp's tiles bid * kDirWarps + warp, then every G * kDirWarps:
+// returns the thread's d'.q. upd_e: the previous update's e += alpha d is still pending.
+__device__ __forceinline__ DF pcg_direction_tiles( int ntiles, const int32_t* __restrict__ nbr,
+                                                   const uint16_t* __restrict__ code, const BoraSolverDev& sv, int dsel_in,
+                                                   float beta, float alpha, bool upd_e, unsigned bid, unsigned G )
 {
-    __shared__ float s_beta, s_alpha;
-    bora_pdl_trigger();
-    bora_pdl_wait();  // the previous kernel's results (ring, z, d, e) are complete from here
-    if( threadIdx.x == 0 )
-    {
-        s_beta = slot_rz_old < 0 ? 0.f : (float)( red.ring[slot_rz_new] / red.ring[slot_rz_old] );
-        s_alpha = slot_a_rz < 0 ? 0.f : (float)( red.ring[slot_a_rz] / red.ring[slot_a_dq] );
-    }
-    __syncthreads();
-    const float beta = s_beta, alpha = s_alpha;
-    const bool upd_e = slot_a_rz >= 0;  // the previous update's e += alpha d is still pending
     const float* __restrict__ dold = dsel_in ? sv.d[1] : sv.d[0];  // selects keep sv out of local memory
     float* __restrict__ dnew = dsel_in ? sv.d[0] : sv.d[1];
     const int lane = threadIdx.x & 31, j = lane & 7, kq = lane >> 3;
@@ -590,6 +589,24 @@ __device__ __forceinline__ void pcg_direction_body( int ntiles, const int32_t* _
 #pragma unroll
         for( int i = 0; i < 8; ++i ) pdq = df_add_f( pdq, tdq[i] );
     }
+    return pdq;
+}
+
+__device__ __forceinline__ void pcg_direction_body( int ntiles, const int32_t* __restrict__ nbr,
+                                                    const uint16_t* __restrict__ code, const BoraSolverDev& sv, int dsel_in,
+                                                    const BoraReduceDev& red, int slot_rz_new, int slot_rz_old,
+                                                    int slot_dq_out, int slot_a_rz, int slot_a_dq, unsigned bid, unsigned G )
+{
+    __shared__ float s_beta, s_alpha;
+    bora_pdl_trigger();
+    bora_pdl_wait();  // the previous kernel's results (ring, z, d, e) are complete from here
+    if( threadIdx.x == 0 )
+    {
+        s_beta = slot_rz_old < 0 ? 0.f : (float)( red.ring[slot_rz_new] / red.ring[slot_rz_old] );
+        s_alpha = slot_a_rz < 0 ? 0.f : (float)( red.ring[slot_a_rz] / red.ring[slot_a_dq] );
+    }
+    __syncthreads();
+    const DF pdq = pcg_direction_tiles( ntiles, nbr, code, sv, dsel_in, s_beta, s_alpha, slot_a_rz >= 0, bid, G );
     reduce2_publish_warp( df_warp_sum( pdq ), 0.0, 0, red, slot_dq_out, -1, bid, G );
 }
 
@@ -612,6 +629,171 @@ __global__ void __launch_bounds__( 32 * kDirWarps ) k_pcg_direction_batch( const
     const BoraMemberSlots& q = L.sl[k];
     pcg_direction_body( m.ntiles, m.nbr, m.code, m.sv, q.dsel, m.red, q.rz_new, q.rz_old, q.dq, q.a_rz, q.a_dq, bid,
                         (unsigned)m.grid[kGridDir] );
+}
+
+// ---------------------------------------------------------------------------------
+// Persistent plain PCG: one cooperative launch runs a refinement pass's inner iterations -
+// the first update (z = M^-1 r), then direction and update per iteration - with a grid-wide
+// barrier after each phase instead of a kernel boundary. The phases are the kernels' own tile
+// loops; a phase's sums are formed per block (warps in a fixed order), stored, and after the
+// barrier every block adds all blocks' values in the same fixed order, so each block holds
+// the same bits without a second barrier. The pass stops after the update whose ||r|| reaches
+// the target (checked in the kernel, the same in every block) or after max_inner iterations.
+//
+// Every barrier wait is bounded: a block that has spun `limit` times, or that sees another
+// block's error, sets BORA_REDUCE_ERR_BARRIER in the error word and returns; every other block
+// then runs out of its own waits and returns too, and the host reports BORA_ERR_INTERNAL.
+struct PcgPersistArgs
+{
+    int ntiles;
+    const int32_t* nbr;
+    const uint16_t* code;
+    BoraSolverDev sv;
+    BoraReduceDev red;
+    int dsel;                  // the current search-direction buffer
+    int slot_rz_prev;          // r.z before the last update of the previous pass, or -1 (restart)
+    int max_inner;
+    double target;             // stop once ||r|| <= target
+    int slot_a_rz, slot_a_dq;  // out: the last update's alpha = a_rz / a_dq (its e += alpha d is pending)
+    int slot_rr;               // out: the last r.r
+    uint32_t* iters;           // out: iterations run
+    unsigned* bar;             // barrier count and generation (zeroed before the launch)
+    unsigned expect;           // blocks a barrier waits for (gridDim.x)
+    unsigned limit;            // spins per barrier wait
+    double* part;              // 3 * gridDim.x block sums
+};
+
+__device__ __forceinline__ bool grid_barrier( const PcgPersistArgs& a )
+{
+    __shared__ int s_ok;
+    __syncthreads();
+    if( threadIdx.x == 0 )
+    {
+        volatile unsigned* gen = a.bar + 1;
+        volatile uint32_t* err = a.red.err;
+        int ok = 1;
+        const unsigned g = *gen;
+        __threadfence();
+        if( atomicAdd( a.bar, 1u ) == a.expect - 1 )
+        {
+            atomicExch( a.bar, 0u );
+            __threadfence();
+            atomicAdd( a.bar + 1, 1u );
+        }
+        else
+        {
+            for( unsigned n = 0; *gen == g; ++n )
+            {
+                if( n >= a.limit || *err )
+                {
+                    atomicOr( a.red.err, (uint32_t)BORA_REDUCE_ERR_BARRIER );
+                    ok = 0;
+                    break;
+                }
+                __nanosleep( 128 );
+            }
+        }
+        __threadfence();
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+// The block's total of v (valid in every lane of every warp), stored at part[blockIdx.x].
+__device__ __forceinline__ void block_sum_store( double v, double* part )
+{
+    __shared__ double w[32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if( lane == 0 ) w[wid] = v;
+    __syncthreads();
+    if( threadIdx.x == 0 )
+    {
+        double t = 0.0;
+        for( int q = 0; q < nw; ++q ) t += w[q];
+        part[blockIdx.x] = t;
+    }
+    __syncthreads();  // w is reused by the next call
+}
+
+// The sum of part[0 .. nb) in a fixed order (the first warp: lane-strided, then a fixed
+// shuffle tree), returned in every thread.
+__device__ __forceinline__ double grid_sum( const double* part, unsigned nb )
+{
+    __shared__ double s_total;
+    if( threadIdx.x < 32 )
+    {
+        double t = 0.0;
+        for( unsigned q = threadIdx.x; q < nb; q += 32 ) t += __ldcg( part + q );
+        t = warp_sum( t );
+        if( threadIdx.x == 0 ) s_total = t;
+    }
+    __syncthreads();
+    const double v = s_total;
+    __syncthreads();
+    return v;
+}
+
+__global__ void __launch_bounds__( 32 * kUpdWarps, 3 ) k_pcg_persistent( const __grid_constant__ PcgPersistArgs a )
+{
+    using namespace micsweep;
+    static_assert( kUpdWarps == kDirWarps, "both phases run one tile per warp" );
+    __shared__ __align__( 16 ) float sval[kUpdWarps][kBuf];
+    __shared__ __align__( 16 ) float spiv[kUpdWarps][kBuf];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for( int q = lane; q < kBuf; q += 32 ) { sval[w][q] = 0.f; spiv[w][q] = 0.f; }
+    __syncwarp();
+    const unsigned G = gridDim.x;
+    double* const pd = a.part;                // d'.q
+    double* const pz = a.part + G;            // r.z
+    double* const pr = a.part + 2 * (size_t)G;  // r.r
+    const int first = blockIdx.x * kUpdWarps + w, stride = G * kUpdWarps;
+    double rz_prev = a.slot_rz_prev >= 0 ? a.red.ring[a.slot_rz_prev] : -1.0;
+    // the pass's first update: z = M^-1 r (alpha 0)
+    DF prz{ 0.f, 0.f }, prr{ 0.f, 0.f };
+    pcg_update_tiles( a.ntiles, a.sv, 0.f, first, stride, sval[w], spiv[w], prz, prr );
+    block_sum_store( df_warp_sum( prz ), pz );
+    block_sum_store( df_warp_sum( prr ), pr );
+    if( !grid_barrier( a ) ) return;
+    double rz = grid_sum( pz, G ), rr = grid_sum( pr, G );
+    double a_rz = -1.0, a_dq = 1.0;
+    int dsel = a.dsel, it = 0;
+    while( it < a.max_inner )
+    {
+        const float beta = rz_prev < 0.0 ? 0.f : (float)( rz / rz_prev );
+        const float alpha_e = a_rz < 0.0 ? 0.f : (float)( a_rz / a_dq );
+        const DF pdq = pcg_direction_tiles( a.ntiles, a.nbr, a.code, a.sv, dsel, beta, alpha_e, a_rz >= 0.0, blockIdx.x, G );
+        block_sum_store( df_warp_sum( pdq ), pd );
+        if( !grid_barrier( a ) ) return;
+        const double dq = grid_sum( pd, G );
+        dsel ^= 1;
+        prz = DF{ 0.f, 0.f };
+        prr = DF{ 0.f, 0.f };
+        pcg_update_tiles( a.ntiles, a.sv, (float)( rz / dq ), first, stride, sval[w], spiv[w], prz, prr );
+        block_sum_store( df_warp_sum( prz ), pz );
+        block_sum_store( df_warp_sum( prr ), pr );
+        if( !grid_barrier( a ) ) return;
+        a_rz = rz;
+        a_dq = dq;
+        rz_prev = rz;
+        rz = grid_sum( pz, G );
+        rr = grid_sum( pr, G );
+        ++it;
+        if( !( rr > 0.0 ) || sqrt( rr ) <= a.target ) break;
+    }
+    if( blockIdx.x == 0 && threadIdx.x == 0 )
+    {
+        a.red.ring[a.slot_a_rz] = a_rz;
+        a.red.ring[a.slot_a_dq] = a_dq;
+        a.red.ring[a.slot_rr] = rr;
+        if( a.red.mirror )
+        {
+            a.red.mirror[a.slot_a_rz] = a_rz;
+            a.red.mirror[a.slot_a_dq] = a_dq;
+            a.red.mirror[a.slot_rr] = rr;
+        }
+        *a.iters = (uint32_t)it;
+    }
 }
 
 // ---------------------------------------------------------------------------------
@@ -960,6 +1142,40 @@ void bora_launch_refine_residual_batch( const BoraBatchLaunch& L, int blocks, cu
 void bora_launch_write_pressure_batch( const BoraBatchLaunch& L, int blocks, cudaStream_t st )
 {
     if( blocks > 0 ) k_write_pressure_batch<<<blocks, 256, 0, st>>>( L );
+}
+
+int bora_pcg_persistent_grid()
+{
+    static BoraPerDevice per_sm;
+    const int b = per_sm.get( [] {
+        int v = 0;
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor( &v, k_pcg_persistent, 32 * kUpdWarps, 0 ) == cudaSuccess ? v : 0;
+    } );
+    return std::min( b * num_sms(), kBoraMaxReduceBlocks );
+}
+
+int bora_launch_pcg_persistent( int ntiles, const int32_t* nbr, const uint16_t* code, BoraSolverDev s, BoraReduceDev red,
+                                int dsel, int slot_rz_prev, int max_inner, double target, int slot_a_rz, int slot_a_dq,
+                                int slot_rr, uint32_t* iters, unsigned* bar, double* part, bool never_release,
+                                cudaStream_t st )
+{
+    const int grid = bora_pcg_persistent_grid();
+    if( grid <= 0 ) return -1;
+    PcgPersistArgs a{};
+    a.ntiles = ntiles; a.nbr = nbr; a.code = code; a.sv = s; a.red = red;
+    a.dsel = dsel; a.slot_rz_prev = slot_rz_prev; a.max_inner = max_inner; a.target = target;
+    a.slot_a_rz = slot_a_rz; a.slot_a_dq = slot_a_dq; a.slot_rr = slot_rr; a.iters = iters;
+    a.bar = bar; a.part = part;
+    // a barrier that waits for one block more than there are never releases: every wait runs
+    // out (fault injection for tests), after a short limit
+    a.expect = (unsigned)grid + ( never_release ? 1u : 0u );
+    a.limit = never_release ? ( 1u << 12 ) : ( 1u << 22 );
+    if( cudaMemsetAsync( bar, 0, 2 * sizeof( unsigned ), st ) != cudaSuccess ) return -1;
+    void* args[] = { &a };
+    return cudaLaunchCooperativeKernel( (const void*)k_pcg_persistent, dim3( grid ), dim3( 32 * kUpdWarps ), args, 0, st ) ==
+                   cudaSuccess
+               ? 0
+               : -1;
 }
 
 void bora_launch_pcg_direction( const BoraGridDev&, int ntiles, BoraTilesDev t, const uint16_t* code, BoraSolverDev s,

@@ -23,6 +23,7 @@ BORA_OK = 0
 BORA_WARN_NOT_CONVERGED = 1
 SPACE_WORLD, SPACE_VOXEL = 0, 1
 SOLVER_PLAIN, SOLVER_MIXED = 0, 1
+FAULT_NONE, FAULT_BARRIER = 0, 1
 ADVECT_EULER, ADVECT_RK2 = 0, 1
 STAGE_REBUILD, STAGE_P2G, STAGE_BUILD_SYSTEM, STAGE_SOLVE, STAGE_UPDATE_VELOCITY, STAGE_UPDATE_PARTICLES = range(6)
 POST_SPLAT, POST_TANK_SCAN, POST_REDISTANCE, POST_ATTRIBUTES = range(4)
@@ -55,7 +56,7 @@ class Params(ctypes.Structure):
                 ("redist_iteration", ctypes.c_int), ("solver", ctypes.c_int), ("tolerance", ctypes.c_double),
                 ("div_tolerance", ctypes.c_double), ("inner_tolerance", ctypes.c_double),
                 ("max_refinements", ctypes.c_int), ("check_every", ctypes.c_int), ("advection", ctypes.c_int),
-                ("post_process", ctypes.c_int)]
+                ("post_process", ctypes.c_int), ("persistent", ctypes.c_int)]
 
 
 class Stats(ctypes.Structure):
@@ -119,6 +120,7 @@ _SIGS = {
     "bora_flip_set_profiling": (ctypes.c_int, [_vp, ctypes.c_uint32]),
     "bora_flip_get_kernel_times": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int]),
     "bora_flip_set_tuning": (ctypes.c_int, [ctypes.c_int]),
+    "bora_flip_set_fault": (ctypes.c_int, [_vp, ctypes.c_int]),
     "bora_flip_tune_table": (ctypes.c_int, [_vp, ctypes.c_size_t, _vp]),
     "bora_scan_u32": (ctypes.c_int, [_vp, _vp, ctypes.c_size_t, _vp, _vp]),
     "bora_scan_u32_noalloc": (ctypes.c_int, [_vp, _vp, ctypes.c_size_t, _vp, _vp]),
@@ -429,6 +431,10 @@ class FlipSim:
         s = Stats()
         _check(self.lib.bora_flip_get_stats(self.h, ctypes.byref(s)), "get_stats")
         return s.as_dict()
+
+    def set_fault(self, fault: int) -> None:
+        """bora_flip_set_fault: inject a fault into the next solves (tests of the error paths)."""
+        _check(self.lib.bora_flip_set_fault(self.h, int(fault)), "bora_flip_set_fault")
 
     def set_profiling(self, class_mask: int) -> None:
         _check(self.lib.bora_flip_set_profiling(self.h, class_mask), "set_profiling")
