@@ -243,10 +243,13 @@ struct BoraLevelDev
 // The tiled levels' passes of a V-cycle (mg_passes.cu): level l (E = 8, 4 or 2) pre-smoothed
 // and restricted into level l + 1's r (down), or prolonged from the coarser correction ec and
 // post-smoothed (up: level 0 into the PCG's z with r.z -> slot_rz, the others into z1).
-// scratch: an FP32 vector of level 0's size.
+// scratch: an FP32 vector of level 0's size. Level 0's down passes first apply the PCG's
+// residual update r -= alpha q, alpha = ring[slot_rz_in] / ring[slot_dq_in] (none when
+// slot_rz_in < 0), and sum the updated r.r into slot_rr_out; slot_rr gives the scale.
 int bora_mg_pass_grid( int E, int ntiles, int v );  // v < 0: level 0's fixed up-2 shape
-void bora_mg_pass_down( const BoraLevelDev* levels, int l, const BoraTilesDev& t, int ntiles, const float* r0,
-                        float* scratch, const BoraReduceDev& red, int slot_rr, cudaStream_t st );
+void bora_mg_pass_down( const BoraLevelDev* levels, int l, const BoraTilesDev& t, int ntiles, float* r0, const float* q,
+                        float* scratch, const BoraReduceDev& red, int slot_rr, int slot_rz_in, int slot_dq_in,
+                        int slot_rr_out, cudaStream_t st );
 void bora_mg_pass_up( const BoraLevelDev* levels, int l, const __half* ec, const BoraTilesDev& t, int ntiles,
                       const float* r0, float* scratch, const BoraReduceDev& red, int slot_rr, float* z, int slot_rz,
                       cudaStream_t st );
@@ -285,7 +288,9 @@ void bora_tune_resolve();
 // mid_image: the buffer for the coarse levels' cluster image (bora_mg_mid_image_bytes), or null
 void bora_mg_setup( const BoraGridDev& g, BoraLevelDev* levels, int nlevels, BoraTilesDev t, void* mid_image,
                     uint32_t* err, cudaStream_t st );
-// One V-cycle: z = M^-1 r (FP32 in and out, FP16 inside); r.z -> ring slot (FP64-accurate).
+// One preconditioned PCG update: r -= alpha q (alpha = ring[slot_rz_in] / ring[slot_dq_in],
+// none when slot_rz_in < 0), r.r -> slot_rr_out, then one V-cycle z = M^-1 r (FP32 in and out,
+// FP16 inside, scaled by 1 / sqrt(ring[slot_scale])); r.z -> slot_rz (FP64-accurate).
 // Kernel launches of one bora_mg_vcycle call for this hierarchy.
 int bora_mg_vcycle_launches( const BoraGridDev& g, const BoraLevelDev* levels, int nlevels, BoraTilesDev t,
                              const void* mid_image );
@@ -301,8 +306,8 @@ void bora_mg_mid_setup( const BoraGridDev& g, const BoraLevelDev* levels, int nl
 int bora_mg_mid_vcycle( const BoraGridDev& g, const BoraLevelDev* levels, int nlevels, BoraTilesDev t, int ntiles,
                         const void* image, uint32_t* err, int sweeps, cudaStream_t st, bool launch );
 void bora_mg_vcycle( const BoraGridDev& g, const BoraLevelDev* levels, int nlevels, BoraTilesDev t, const void* mid_image,
-                     const float* r, float* z, float* scratch, BoraReduceDev red, int slot_rr, int slot_rz,
-                     int coarse_sweeps, cudaStream_t st );
+                     float* r, const float* q, float* z, float* scratch, BoraReduceDev red, int slot_rz_in,
+                     int slot_dq_in, int slot_rr_out, int slot_scale, int slot_rz, int coarse_sweeps, cudaStream_t st );
 // ---- batched solve: several simulations, one launch per kernel ---------------------------
 // A batched launch packs the blocks of the simulations taking part back to back into one
 // 1-D grid: simulation k owns blocks start[k] .. start[k+1] - 1, exactly the grid its own

@@ -631,6 +631,7 @@ int stage_solve( bora_flip_sim* s )
     // pass ends by replacing the recursive FP32 residual with the refined one, keeps the last
     // direction d and r.z, and the next pass carries on from them instead of restarting.
     int rz_prev = -1, dsel = 0;
+    int scale_slot = s_b2;  // the latest residual norm the host has: ||b|| (r = b), then each refinement's
     for( ;; )
     {
         const bool norm_ok = rnorm <= p.tolerance * bnorm;
@@ -643,10 +644,12 @@ int stage_solve( bora_flip_sim* s )
         const void* mid_img = s->mg_mid_on ? s->mg_mid.p : nullptr;
         const int vlaunch = mixed ? bora_mg_vcycle_launches( s->g, s->levels, s->nlevels, s->tiles(), mid_img ) : 0;
         s->stats.mg_vcycle_launches = mixed ? vlaunch : 0;
-        auto precondition = [&]( int rr_slot, int rz_slot ) {
+        // the mixed form's update r -= alpha q (alpha = rz_in / dq_in) and r.r run inside the
+        // V-cycle's first passes, which scale the FP16 levels by the last known residual norm
+        auto precondition = [&]( int rz_in, int dq_in, int rr_out, int scale, int rz_out ) {
             KTimer t( s, BORA_KERNEL_MG, vlaunch );
-            bora_mg_vcycle( s->g, s->levels, s->nlevels, s->tiles(), mid_img, sv.r, sv.z, sv.minv, red, rr_slot, rz_slot, 16,
-                            st );
+            bora_mg_vcycle( s->g, s->levels, s->nlevels, s->tiles(), mid_img, sv.r, sv.q, sv.z, sv.minv, red, rz_in, dq_in,
+                            rr_out, scale, rz_out, 16, st );
         };
         int rz_cur = s->slot(), rr_cur = s->slot();
         int it = 0;
@@ -675,8 +678,7 @@ int stage_solve( bora_flip_sim* s )
         }
         else if( mixed )
         {
-            { KTimer t( s, BORA_KERNEL_PCG_UPDATE, 1 ); bora_launch_pcg_update_noprec( s->ntiles, sv, red, -1, -1, rr_cur, st ); }
-            precondition( rr_cur, rz_cur );
+            precondition( -1, -1, rr_cur, scale_slot, rz_cur );
         }
         else
         {
@@ -702,8 +704,7 @@ int stage_solve( bora_flip_sim* s )
             const int rz_new = s->slot(), rr_new = s->slot();
             if( mixed )
             {
-                { KTimer t( s, BORA_KERNEL_PCG_UPDATE, 1 ); bora_launch_pcg_update_noprec( s->ntiles, sv, red, rz_cur, s_dq, rr_new, st ); }
-                precondition( rr_new, rz_new );
+                precondition( rz_cur, s_dq, rr_new, rr_cur, rz_new );
             }
             else
             {
@@ -742,6 +743,7 @@ int stage_solve( bora_flip_sim* s )
         }
         BORA_TRYS( check_launch( s ) );
         rnorm = std::sqrt( read_ring( s, s_n2, &status ) );
+        scale_slot = s_n2;
         BORA_TRYS( status );
         rmax = read_ring( s, s_mx, &status );
         BORA_TRYS( status );
@@ -1458,7 +1460,12 @@ int batch_solve( std::vector<BatchMember>& M, cudaStream_t st, BatchBuffers& bb,
         for( int l = 0; l < 3; ++l )
         {
             BoraTuneTimer timer( tpick[l], tgroup[l], total_tiles, st );  // times the level's two down passes
-            for( int p = 0; p < 2; ++p ) bora_launch_mg_pass_batch( l, p, tv[l], launch( lgrid[l] ), blocks[lgrid[l]], st );
+            for( int p = 0; p < 2; ++p )
+            {
+                // level 0's down 1 and up 2 reduce over their blocks: the fixed shape's grid
+                const int q = l == 0 && p == 0 ? kGridPass0R : lgrid[l];
+                bora_launch_mg_pass_batch( l, p, tv[l], launch( q ), blocks[q], st );
+            }
         }
         bora_mg_mid_launch_batch( bb.mid.p, launch( kGridCount ), blocks[kGridCount], ctas, smem, st );
         for( int l = 2; l >= 0; --l )
@@ -1501,7 +1508,8 @@ int batch_solve( std::vector<BatchMember>& M, cudaStream_t st, BatchBuffers& bb,
     constexpr int kTicks = bora_flip_sim::kChecks;
     for( ;; )
     {
-        // passes that start: the first V-cycle z = M^-1 r after r.r
+        // passes that start: the first V-cycle z = M^-1 r with r.r (no residual update; scaled
+        // by ||b|| on the first pass, by the refined ||r|| after)
         bool start = false;
         for( int k = 0; k < n; ++k )
         {
@@ -1514,7 +1522,7 @@ int batch_solve( std::vector<BatchMember>& M, cudaStream_t st, BatchBuffers& bb,
             sl[k].rz_in = -1;
             sl[k].dq_in = -1;
             sl[k].rr_out = b.rr_cur;
-            sl[k].rr = b.rr_cur;
+            sl[k].rr = b.passes == 0 ? b.s_b2 : b.s_n2;
             sl[k].rz = b.rz_cur;
             b.phase = BatchMember::kInner;
             b.it = 0;
@@ -1527,8 +1535,6 @@ int batch_solve( std::vector<BatchMember>& M, cudaStream_t st, BatchBuffers& bb,
         if( start )
         {
             BORA_TRYS( upload() );
-            bora_launch_pcg_update_noprec_batch( launch( kGridUpd ), blocks[kGridUpd], st );
-            ++launches;
             vcycle();
         }
         // one inner iteration for every simulation inside a pass
@@ -1545,7 +1551,7 @@ int batch_solve( std::vector<BatchMember>& M, cudaStream_t st, BatchBuffers& bb,
             q.dsel = b.dsel;
             q.rz_new = b.rz_cur; q.rz_old = b.rz_prev; q.dq = s_dq; q.a_rz = b.a_rz; q.a_dq = b.a_dq;
             q.rz_in = b.rz_cur; q.dq_in = s_dq; q.rr_out = rr_new;
-            q.rr = rr_new; q.rz = rz_new;
+            q.rr = b.rr_cur; q.rz = rz_new;  // the V-cycle's scale: the previous r.r
             b.dsel ^= 1;
             b.a_rz = b.rz_cur;
             b.a_dq = s_dq;
@@ -1559,9 +1565,8 @@ int batch_solve( std::vector<BatchMember>& M, cudaStream_t st, BatchBuffers& bb,
         {
             BORA_TRYS( upload() );
             bora_launch_pcg_direction_batch( launch( kGridDir ), blocks[kGridDir], st );
-            bora_launch_pcg_update_noprec_batch( launch( kGridUpd ), blocks[kGridUpd], st );
-            launches += 2;
-            vcycle();
+            ++launches;
+            vcycle();  // with the residual update
             BORA_TRYS( check_launch( nullptr ) );
             BORA_TRY( cudaEventRecord( tev[tick % kTicks], st ) );
             for( int k = 0; k < n; ++k )

@@ -325,6 +325,17 @@ __global__ void __launch_bounds__( kG2PThreads, 4 ) k_g2p( const __grid_constant
         if( tid < 27 ) nb[tid] = t.nbr[(size_t)s * 27 + tid];
         const int vt = t.tile_of[s];
         const int ti = vt % g.tx, tj = ( vt / g.tx ) % g.ty, tk = vt / ( g.tx * g.ty );
+        // the thread's particles are loaded one ahead: the first before the staging, each
+        // next one while the current one is advanced
+        const uint32_t q0 = start[(size_t)s * BORA_TILE_CELLS], q1 = start[(size_t)( s + 1 ) * BORA_TILE_CELLS];
+        uint32_t pin = 0;
+        float pxn = 0.f, pyn = 0.f, pzn = 0.f, vxn = 0.f, vyn = 0.f, vzn = 0.f;
+        auto fetch = [&]( uint32_t q ) {
+            pin = idx[q];
+            pxn = src.px[pin]; pyn = src.py[pin]; pzn = src.pz[pin];
+            vxn = src.vx[pin]; vyn = src.vy[pin]; vzn = src.vz[pin];
+        };
+        if( q0 + tid < q1 ) fetch( q0 + tid );
         __syncthreads();
         for( int h = tid; h < kStageCells; h += kG2PThreads )
         {
@@ -341,12 +352,12 @@ __global__ void __launch_bounds__( kG2PThreads, 4 ) k_g2p( const __grid_constant
             fb[h] = vb;
         }
         __syncthreads();
-        const uint32_t q0 = start[(size_t)s * BORA_TILE_CELLS], q1 = start[(size_t)( s + 1 ) * BORA_TILE_CELLS];
         for( uint32_t q = q0 + tid; q < q1; q += kG2PThreads )
         {
-            const uint32_t pi = idx[q];
-            float px = src.px[pi], py = src.py[pi], pz = src.pz[pi];
-            float vx = src.vx[pi], vy = src.vy[pi], vz = src.vz[pi];
+            const uint32_t pi = pin;
+            float px = pxn, py = pyn, pz = pzn;
+            float vx = vxn, vy = vyn, vz = vzn;
+            if( q + kG2PThreads < q1 ) fetch( q + kG2PThreads );
             StagedSampler smp{ {}, fa, fb };
             smp.l.setup( g, ti, tj, tk, px, py, pz );
             adj[q] = smp.surf_min();  // surf background 10 (FLIPMethod.cu:30)

@@ -11,12 +11,19 @@
 //           neighbours' za).                                                    zb -> scratch
 //   up 2    z = S_A(zb) (the neighbours' zb); level 0 unscales into the FP32 z of the PCG and
 //           sums r.z, the other levels store FP16 z1 for the finer level's up 1
-// where r' = r / ||r|| on level 0 (the FP16 levels hold scaled values) and r on the others,
+// where r' = r * sc on level 0 (sc = 1 / ||r|| of the latest residual whose norm is known: it
+// keeps the FP16 levels' values O(1), and the V-cycle is linear in r, so any scale serves) and r
+// on the others,
 // S_w(v) = v + (w / d) (r' - (d v - sum of the neighbours' v)) on fluid cells and 0 elsewhere,
 // neighbour sums in the order ((x- + x+) + (y- + y+)) + (z- + z+), and the 8 children summed as
 // ((x pairs) + (y pairs)) + (z pairs). Every cell is computed once per pass; the scratch is
 // the FP32 cell vector that the plain form keeps its preconditioner pivots in (the mixed form
 // has none), used by one pass pair at a time.
+//
+// Level 0's down passes also apply the PCG's residual update r -= alpha q (alpha = rz / dq of the
+// last direction): down 1 forms the updated residual of its cells and of the face cells it reads,
+// without storing it, and sums r.r over the grid (the convergence check); down 2, which reads no
+// neighbour's r, stores it. This takes the update kernel out of every iteration.
 //
 // Level 0 runs one warp per tile: a lane owns the x-rows (j, k) and (j, k + 4) of the tile as
 // 16-byte vectors (lane = j + 8 k), its x neighbours are in its registers, the y and z
@@ -108,10 +115,12 @@ __device__ __forceinline__ uint32_t pack2( float a, float b )
 
 // the fields a pass reads at its neighbours, for 8 cells of a row or one cell of tile slot t
 // (cell index c in the tile; t < 0 gives zeros)
-struct FieldZ1  // down 1: the first sweep's z1 = w_A r' / d
+struct FieldZ1  // down 1: the first sweep's z1 = w_A r' / d of the updated residual r - alpha q
 {
     const uint16_t* code;
     const float* r0;
+    const float* q;  // null: no update
+    float alpha;
     float sc;
     const float* w;
     __device__ void row( int t, int c, float* v ) const
@@ -122,6 +131,13 @@ struct FieldZ1  // down 1: the first sweep's z1 = w_A r' / d
         float rr[8];
         codes8( code, g, cc );
         f32x8( r0, g, rr );
+        if( q )
+        {
+            float qq[8];
+            f32x8( q, g, qq );
+#pragma unroll
+            for( int i = 0; i < 8; ++i ) rr[i] = fmaf( -alpha, qq[i], rr[i] );
+        }
 #pragma unroll
         for( int i = 0; i < 8; ++i ) v[i] = cfluid( cc[i] ) ? ( rr[i] * sc ) * w[cdiag( cc[i] )] : 0.f;
     }
@@ -130,7 +146,8 @@ struct FieldZ1  // down 1: the first sweep's z1 = w_A r' / d
         if( t < 0 ) return 0.f;
         const size_t g = (size_t)t * 512 + c;
         const uint16_t cc = code[g];
-        return cfluid( cc ) ? ( r0[g] * sc ) * w[cdiag( cc )] : 0.f;
+        const float r = q ? fmaf( -alpha, q[g], r0[g] ) : r0[g];
+        return cfluid( cc ) ? ( r * sc ) * w[cdiag( cc )] : 0.f;
     }
 };
 
@@ -228,11 +245,15 @@ struct Pass0Args
     const int32_t* nbr;
     BoraLevelDev F;       // level 0
     BoraLevelDev C;       // level 1 (down 2 writes its r; up 1 reads its z1)
-    const float* r0;      // the PCG residual
+    float* r0;            // the PCG residual (down 2 stores its update)
+    const float* q;       // the PCG's A d (the update's direction term)
     float* scratch;       // FP32 per cell
     float* zout;          // up 2: the PCG's z
     BoraReduceDev red;
-    int slot_rr, slot_rz;
+    int slot_rr;          // the scale's r.r
+    int slot_rz;          // up 2: r.z out
+    int slot_rz_in, slot_dq_in;  // down 1, 2: alpha = rz_in / dq_in (slot_rz_in < 0: no update)
+    int slot_rr_out;      // down 1: r.r of the updated residual out
 };
 
 // pass P of level 0: 0 = down 1, 1 = down 2, 2 = up 1, 3 = up 2; W tiles (warps) per block
@@ -260,10 +281,16 @@ __device__ __forceinline__ void pass0_body( const Pass0Args& a, unsigned bid, un
     };
     int s = (int)bid * W + ( threadIdx.x >> 5 );
     fetch( s );
+    __shared__ float s_alpha;
     bora_pdl_wait();  // the previous kernel's results are complete from here
-    if( threadIdx.x == 0 ) s_sc = scale_from( a.red.ring, a.slot_rr );
+    if( threadIdx.x == 0 )
+    {
+        s_sc = scale_from( a.red.ring, a.slot_rr );
+        s_alpha = a.slot_rz_in < 0 ? 0.f : (float)( a.red.ring[a.slot_rz_in] / a.red.ring[a.slot_dq_in] );
+    }
     __syncthreads();
-    const float sc = s_sc;
+    const float sc = s_sc, alpha = s_alpha;
+    const bool upd = ( P == 0 || P == 1 ) && a.slot_rz_in >= 0;  // down 1, 2 apply r -= alpha q
     DF rz{ 0.f, 0.f };
     for( ; s < a.ntiles; s += stride )
     {
@@ -285,6 +312,30 @@ __device__ __forceinline__ void pass0_body( const Pass0Args& a, unsigned bid, un
         float rA[8], rB[8];  // r' on fluid cells
         f32x8( a.r0, gA, rA );
         f32x8( a.r0, gB, rB );
+        if( upd )
+        {
+            float qA[8], qB[8];
+            f32x8( a.q, gA, qA );
+            f32x8( a.q, gB, qB );
+#pragma unroll
+            for( int i = 0; i < 8; ++i )
+            {
+                rA[i] = fmaf( -alpha, qA[i], rA[i] );
+                rB[i] = fmaf( -alpha, qB[i], rB[i] );
+            }
+            if constexpr( P == 1 )
+            {
+                st_f32x8( a.r0, gA, rA );
+                st_f32x8( a.r0, gB, rB );
+            }
+        }
+        if constexpr( P == 0 )
+        {
+            float t = 0.f;
+#pragma unroll
+            for( int i = 0; i < 8; ++i ) { t = fmaf( rA[i], rA[i], t ); t = fmaf( rB[i], rB[i], t ); }
+            rz = df_add_f( rz, t );  // down 1: r.r of the updated residual
+        }
 #pragma unroll
         for( int i = 0; i < 8; ++i )
         {
@@ -300,7 +351,7 @@ __device__ __forceinline__ void pass0_body( const Pass0Args& a, unsigned bid, un
                 vA[i] = cfluid( cA[i] ) ? rA[i] * w[cdiag( cA[i] )] : 0.f;
                 vB[i] = cfluid( cB[i] ) ? rB[i] * w[cdiag( cB[i] )] : 0.f;
             }
-            row_sums( FieldZ1{ a.F.code, a.r0, sc, w }, nf, lane, vA, vB, sA, sB );
+            row_sums( FieldZ1{ a.F.code, a.r0, upd ? a.q : nullptr, alpha, sc, w }, nf, lane, vA, vB, sA, sB );
 #pragma unroll
             for( int i = 0; i < 8; ++i )
             {
@@ -386,6 +437,7 @@ __device__ __forceinline__ void pass0_body( const Pass0Args& a, unsigned bid, un
         }
     }
     if constexpr( P == 3 ) reduce2_publish_warp( df_warp_sum( rz ), 0.0, 0, a.red, a.slot_rz, -1, bid, G );
+    if constexpr( P == 0 ) reduce2_publish_warp( df_warp_sum( rz ), 0.0, 0, a.red, a.slot_rr_out, -1, bid, G );
 }
 
 template <int W, int P>
@@ -407,12 +459,16 @@ __global__ void __launch_bounds__( 32 * W, 16 / W ) k_mg_pass0_batch( const __gr
     a.F = m.L[0];
     a.C = m.L[1];
     a.r0 = m.sv.r;
+    a.q = m.sv.q;
     a.scratch = m.sv.minv;
     a.zout = m.sv.z;
     a.red = m.red;
     a.slot_rr = q.rr;
     a.slot_rz = q.rz;
-    pass0_body<W, P>( a, bid, (unsigned)m.grid[P == 3 ? kGridPass0R : kGridPass0] );
+    a.slot_rz_in = q.rz_in;
+    a.slot_dq_in = q.dq_in;
+    a.slot_rr_out = q.rr_out;
+    pass0_body<W, P>( a, bid, (unsigned)m.grid[P == 0 || P == 3 ? kGridPass0R : kGridPass0] );
 }
 
 // ---- levels 1 and 2: one thread per cell --------------------------------------------------
@@ -603,8 +659,9 @@ int bora_mg_pass_grid( int E, int ntiles, int v )
     return (int)( ( n + T - 1 ) / T );
 }
 
-void bora_mg_pass_down( const BoraLevelDev* levels, int l, const BoraTilesDev& t, int ntiles, const float* r0,
-                        float* scratch, const BoraReduceDev& red, int slot_rr, cudaStream_t st )
+void bora_mg_pass_down( const BoraLevelDev* levels, int l, const BoraTilesDev& t, int ntiles, float* r0, const float* q,
+                        float* scratch, const BoraReduceDev& red, int slot_rr, int slot_rz_in, int slot_dq_in,
+                        int slot_rr_out, cudaStream_t st )
 {
     const int group = l == 0 ? kBoraTuneL0 : ( l == 1 ? kBoraTuneL1 : kBoraTuneL2 );
     const BoraTunePick pick = bora_tune_pick( group, ntiles );
@@ -613,9 +670,12 @@ void bora_mg_pass_down( const BoraLevelDev* levels, int l, const BoraTilesDev& t
     if( levels[l].E == 8 )
     {
         Pass0Args a{};
-        a.ntiles = ntiles; a.nbr = t.nbr; a.F = levels[0]; a.C = levels[1]; a.r0 = r0; a.scratch = scratch;
+        a.ntiles = ntiles; a.nbr = t.nbr; a.F = levels[0]; a.C = levels[1]; a.r0 = r0; a.q = q; a.scratch = scratch;
         a.red = red; a.slot_rr = slot_rr; a.slot_rz = -1;
-        launch_pass0<0>( a, v, st );
+        a.slot_rz_in = slot_rz_in; a.slot_dq_in = slot_dq_in; a.slot_rr_out = slot_rr_out;
+        // down 1 sums r.r over its blocks: the fixed shape
+        const int g = bora_mg_pass_grid( 8, ntiles, -1 );
+        if( g > 0 ) bora_launch_pdl( k_mg_pass0<kReduceWarps, 0>, dim3( g ), dim3( 32 * kReduceWarps ), 0, st, a );
         launch_pass0<1>( a, v, st );
         return;
     }
@@ -635,7 +695,8 @@ void bora_mg_pass_up( const BoraLevelDev* levels, int l, const __half* ec, const
     {
         Pass0Args a{};
         a.ntiles = ntiles; a.nbr = t.nbr; a.F = levels[0]; a.C = levels[1]; a.C.z1 = const_cast<__half*>( ec );
-        a.r0 = r0; a.scratch = scratch; a.zout = z; a.red = red; a.slot_rr = slot_rr; a.slot_rz = slot_rz;
+        a.r0 = const_cast<float*>( r0 ); a.scratch = scratch; a.zout = z; a.red = red; a.slot_rr = slot_rr; a.slot_rz = slot_rz;
+        a.slot_rz_in = -1; a.slot_dq_in = -1; a.slot_rr_out = -1;
         launch_pass0<2>( a, v, st );
         // r.z: the fixed shape
         const int g = bora_mg_pass_grid( 8, ntiles, -1 );
@@ -654,9 +715,11 @@ void bora_launch_mg_pass_batch( int l, int pass, int v, const BoraBatchLaunch& L
     const dim3 grid( blocks );
     if( l == 0 )
     {
-        if( pass == 3 )
+        // down 1 and up 2 reduce over their blocks: the fixed shape
+        if( pass == 0 || pass == 3 )
         {
-            bora_launch_pdl( k_mg_pass0_batch<kReduceWarps, 3>, grid, dim3( 32 * kReduceWarps ), 0, st, L );
+            if( pass == 0 ) bora_launch_pdl( k_mg_pass0_batch<kReduceWarps, 0>, grid, dim3( 32 * kReduceWarps ), 0, st, L );
+            else bora_launch_pdl( k_mg_pass0_batch<kReduceWarps, 3>, grid, dim3( 32 * kReduceWarps ), 0, st, L );
             return;
         }
         const int W = kPassWarpsOf[std::min( std::max( v, 0 ), 2 )];

@@ -788,12 +788,13 @@ int bora_mg_vcycle_launches( const BoraGridDev& g, const BoraLevelDev* levels, i
     const int stop = std::min( first, nlevels - 1 );
     int n = 1;  // the tail kernel, or the coarsest-level kernel
     for( int l = 0; l < stop; ++l ) n += 4;
+    if( !( stop > 0 && pass_level( levels[0] ) ) ) n += 1;  // the residual update on its own
     return n;
 }
 
 void bora_mg_vcycle( const BoraGridDev& g, const BoraLevelDev* levels, int nlevels, BoraTilesDev t, const void* mid_image,
-                     const float* r, float* z, float* scratch, BoraReduceDev red, int slot_rr, int slot_rz,
-                     int coarse_sweeps, cudaStream_t st )
+                     float* r, const float* q, float* z, float* scratch, BoraReduceDev red, int slot_rz_in,
+                     int slot_dq_in, int slot_rr_out, int slot_scale, int slot_rz, int coarse_sweeps, cudaStream_t st )
 {
     if( nlevels < 2 ) return;  // the caller always builds at least two levels
     if( levels[0].ncells == 0 ) return;
@@ -804,6 +805,17 @@ void bora_mg_vcycle( const BoraGridDev& g, const BoraLevelDev* levels, int nleve
     const bool mid = bora_mg_mid_vcycle( g, levels, nlevels, t, ntiles, mid_image, red.err, coarse_sweeps, st, false ) != 0;
     const int first = mid ? 3 : tail_start( levels, nlevels );  // levels [first, last] run in one kernel
     const int stop = std::min( first, last );                     // levels [0, stop) restrict/prolong here
+    // the residual update runs in level 0's down passes; when level 0 itself is in the tail
+    // kernel, it runs first on its own, and the V-cycle is scaled by its r.r
+    int slot_rr = slot_scale;
+    if( !( stop > 0 && pass_level( levels[0] ) ) )
+    {
+        BoraSolverDev sv{};
+        sv.r = r;
+        sv.q = const_cast<float*>( q );
+        bora_launch_pcg_update_noprec( ntiles, sv, red, slot_rz_in, slot_dq_in, slot_rr_out, st );
+        slot_rr = slot_rr_out;
+    }
     // down: pre-smooth and restrict
     for( int l = 0; l < stop; ++l )
     {
@@ -812,7 +824,7 @@ void bora_mg_vcycle( const BoraGridDev& g, const BoraLevelDev* levels, int nleve
         const float* r0 = l == 0 ? r : nullptr;
         if( pass_level( F ) )
         {
-            bora_mg_pass_down( levels, l, t, ntiles, r, scratch, red, slot_rr, st );
+            bora_mg_pass_down( levels, l, t, ntiles, r, q, scratch, red, slot_rr, slot_rz_in, slot_dq_in, slot_rr_out, st );
             continue;
         }
         with_nav( g, levels, nlevels, l, t, [&]( auto nav ) {
