@@ -59,8 +59,10 @@ ALG_BYTES = {
     "pcg_direction": (26, 0), "pcg_update": (20, 0), "refine": (30, 0), "velocity": (33, 0), "g2p": (28, 64),
     "mg_vcycle": (23, 0),
 }
-# Mixed form: the PCG update has no preconditioner sweep (read r, q; write r: 12 B/cell).
-ALG_BYTES_MIXED = dict(ALG_BYTES, pcg_update=(12, 0))
+# Mixed form: the PCG update has no preconditioner sweep (read r, q; write r: 12 B/cell) and
+# runs inside the V-cycle's first passes, so a V-cycle moves 23 + 12 B per fine cell (the
+# separate update kernel remains only for hierarchies whose level 0 is in the tail kernel).
+ALG_BYTES_MIXED = dict(ALG_BYTES, pcg_update=(12, 0), mg_vcycle=(35, 0))
 
 
 def parse():
