@@ -200,13 +200,18 @@ int bora_flip_set_collider_voxels( bora_flip_handle h, const int32_t* ijk, const
 int bora_flip_step( bora_flip_handle h, float dt );
 /* Several independent simulations one step each (FLIPMethod::advanceOneStep for every
  * handle), with the pressure solve - almost all of a step's kernel launches - launched once
- * per kernel for all of them: simulation k is row k of every launch, on the grid its own
- * launch would use, with its own reductions and convergence, so each handle's result is the
- * same as from bora_flip_step_batch with that handle alone. The other stages run per handle,
- * back to back on the first handle's stream. Handles of the plain solver form (or whose
- * multigrid hierarchy does not fit the batched coarse-level kernel) take a bora_flip_step of
- * their own. status[k] receives handle k's step status; the handles must live on one
- * device and be distinct. */
+ * per kernel for all of them: the blocks of the simulations taking part are packed back to
+ * back in each launch, simulation k running exactly the blocks of its own launch with its
+ * own reductions and convergence, so each handle's result is the same as from
+ * bora_flip_step_batch with that handle alone, whatever else is in the batch. The other
+ * stages run on each handle's own stream, every part issued for all handles before the host
+ * waits on any. A batched step keeps the multigrid levels 0-3 and one dense level in every
+ * hierarchy, so a scene with fewer than 512 active tiles solves on more levels than in
+ * bora_flip_step (from 512 tiles up the two give the same bits). Handles of the plain solver
+ * form (or whose hierarchy does not fit the batched coarse-level kernel) take a
+ * bora_flip_step of their own. status[k] receives handle k's step status; the handles must
+ * live on one device and be distinct. After the call, stage_ms of the batched handles holds
+ * the batch's phase times. */
 int bora_flip_step_batch( bora_flip_handle* hs, int n, float dt, int* status );
 
 /* FLIPMethod::advanceOneFrame (FLIPMethod.cu:177-206): one step of params.dt, then (with

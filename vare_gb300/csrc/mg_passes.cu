@@ -291,7 +291,7 @@ __device__ __forceinline__ void pass0_body( const Pass0Args& a, unsigned bid, un
     __syncthreads();
     const float sc = s_sc, alpha = s_alpha;
     const bool upd = ( P == 0 || P == 1 ) && a.slot_rz_in >= 0;  // down 1, 2 apply r -= alpha q
-    DF rz{ 0.f, 0.f };
+    DF acc{ 0.f, 0.f };  // down 1: r.r of the updated residual; up 2: r.z
     for( ; s < a.ntiles; s += stride )
     {
         int nf[6];
@@ -334,7 +334,7 @@ __device__ __forceinline__ void pass0_body( const Pass0Args& a, unsigned bid, un
             float t = 0.f;
 #pragma unroll
             for( int i = 0; i < 8; ++i ) { t = fmaf( rA[i], rA[i], t ); t = fmaf( rB[i], rB[i], t ); }
-            rz = df_add_f( rz, t );  // down 1: r.r of the updated residual
+            acc = df_add_f( acc, t );
         }
 #pragma unroll
         for( int i = 0; i < 8; ++i )
@@ -433,11 +433,11 @@ __device__ __forceinline__ void pass0_body( const Pass0Args& a, unsigned bid, un
             }
             st_f32x8( a.zout, gA, vA );
             st_f32x8( a.zout, gB, vB );
-            rz = df_add_f( rz, trz );
+            acc = df_add_f( acc, trz );
         }
     }
-    if constexpr( P == 3 ) reduce2_publish_warp( df_warp_sum( rz ), 0.0, 0, a.red, a.slot_rz, -1, bid, G );
-    if constexpr( P == 0 ) reduce2_publish_warp( df_warp_sum( rz ), 0.0, 0, a.red, a.slot_rr_out, -1, bid, G );
+    if constexpr( P == 3 ) reduce2_publish_warp( df_warp_sum( acc ), 0.0, 0, a.red, a.slot_rz, -1, bid, G );
+    if constexpr( P == 0 ) reduce2_publish_warp( df_warp_sum( acc ), 0.0, 0, a.red, a.slot_rr_out, -1, bid, G );
 }
 
 template <int W, int P>
