@@ -531,63 +531,68 @@ __device__ __forceinline__ DF pcg_direction_tiles( int ntiles, const int32_t* __
                 reinterpret_cast<float4*>( sv.e + g )[1] = e1;
             }
         }
-        // neighbour-tile cells: x ends of both rows; the y face row of lanes j = 0 / 7 (both
-        // rows); the z face row of row A at k = 0 (-z) and of row B at k = 7 (+z)
+        // neighbour-tile cells: x ends of both rows; the y face row of lanes j = 0 / 7 (row A
+        // here, row B after row A's stencil); the z face row of row A at k = 0 (-z) and of row
+        // B at k = 7 (+z)
         const float xmA = halo1( smx, 8 * lane + 7 ), xpA = halo1( spx, 8 * lane );
         const float xmB = halo1( smx, 256 + 8 * lane + 7 ), xpB = halo1( spx, 256 + 8 * lane );
-        float yhA[8], yhB[8], zh[8];
+        const int yt = j == 0 ? smy : ( j == 7 ? spy : -1 );
+        const int yc = 8 * ( lane - j ) + ( j == 0 ? 56 : 0 );  // row (7 or 0, kq) of the neighbour tile
+        float yh[8], zh[8];
+        halo8( yt, yc, yh );
         {
-            const int yt = j == 0 ? smy : ( j == 7 ? spy : -1 );
-            const int yc = 8 * ( lane - j ) + ( j == 0 ? 56 : 0 );  // row (7 or 0, kq) of the neighbour tile
-            halo8( yt, yc, yhA );
-            halo8( yt, yc + 256, yhB );
             const int zt = kq == 0 ? smz : ( kq == 3 ? spz : -1 );
             const int zc = 8 * j + ( kq == 0 ? 448 : 0 );  // row (j, 7) or (j, 0) of the neighbour tile
             halo8( zt, zc, zh );
         }
-        float qA[8], qB[8];
-        float tdq[8];
+        // q = A d' and d'.q, row A then row B (both rows' d' feed the z shuffles)
+        float q[8], tA[8];
 #pragma unroll
         for( int i = 0; i < 8; ++i )
         {
-            // y neighbours (lanes j -+ 1), z neighbours (lanes -+ 8, across the two rows)
             float ymA = __shfl_up_sync( kAll, dA[i], 1 ), ypA = __shfl_down_sync( kAll, dA[i], 1 );
-            float ymB = __shfl_up_sync( kAll, dB[i], 1 ), ypB = __shfl_down_sync( kAll, dB[i], 1 );
-            if( j == 0 ) { ymA = yhA[i]; ymB = yhB[i]; }
-            if( j == 7 ) { ypA = yhA[i]; ypB = yhB[i]; }
+            if( j == 0 ) ymA = yh[i];
+            if( j == 7 ) ypA = yh[i];
             float zmA = __shfl_up_sync( kAll, dA[i], 8 );
             if( kq == 0 ) zmA = zh[i];
             const float zpA = __shfl_sync( kAll, kq == 0 ? dB[i] : dA[i], ( lane + 8 ) & 31 );
-            const float zmB = __shfl_sync( kAll, kq == 3 ? dA[i] : dB[i], ( lane + 24 ) & 31 );
-            float zpB = __shfl_down_sync( kAll, dB[i], 8 );
-            if( kq == 3 ) zpB = zh[i];
             const float xmA_ = i > 0 ? dA[i > 0 ? i - 1 : 0] : xmA, xpA_ = i < 7 ? dA[i < 7 ? i + 1 : 7] : xpA;
-            const float xmB_ = i > 0 ? dB[i > 0 ? i - 1 : 0] : xmB, xpB_ = i < 7 ? dB[i < 7 ? i + 1 : 7] : xpB;
-            qA[i] = 0.f;
-            qB[i] = 0.f;
-            float t = 0.f;
+            q[i] = 0.f;
+            tA[i] = 0.f;
             if( cA[i] & BORA_CODE_FLUID )
             {
                 float acc = 0.f;
                 acc += xmA_; acc += xpA_; acc += ymA; acc += ypA; acc += zmA; acc += zpA;
-                qA[i] = fmaf( (float)code_diag( cA[i] ), dA[i], -acc );
-                t = fmaf( dA[i], qA[i], t );
+                q[i] = fmaf( (float)code_diag( cA[i] ), dA[i], -acc );
+                tA[i] = fmaf( dA[i], q[i], 0.f );
             }
+        }
+        reinterpret_cast<float4*>( sv.q + gA )[0] = make_float4( q[0], q[1], q[2], q[3] );
+        reinterpret_cast<float4*>( sv.q + gA )[1] = make_float4( q[4], q[5], q[6], q[7] );
+        halo8( yt, yc + 256, yh );
+#pragma unroll
+        for( int i = 0; i < 8; ++i )
+        {
+            float ymB = __shfl_up_sync( kAll, dB[i], 1 ), ypB = __shfl_down_sync( kAll, dB[i], 1 );
+            if( j == 0 ) ymB = yh[i];
+            if( j == 7 ) ypB = yh[i];
+            const float zmB = __shfl_sync( kAll, kq == 3 ? dA[i] : dB[i], ( lane + 24 ) & 31 );
+            float zpB = __shfl_down_sync( kAll, dB[i], 8 );
+            if( kq == 3 ) zpB = zh[i];
+            const float xmB_ = i > 0 ? dB[i > 0 ? i - 1 : 0] : xmB, xpB_ = i < 7 ? dB[i < 7 ? i + 1 : 7] : xpB;
+            q[i] = 0.f;
+            float t = tA[i];
             if( cB[i] & BORA_CODE_FLUID )
             {
                 float acc = 0.f;
                 acc += xmB_; acc += xpB_; acc += ymB; acc += ypB; acc += zmB; acc += zpB;
-                qB[i] = fmaf( (float)code_diag( cB[i] ), dB[i], -acc );
-                t = fmaf( dB[i], qB[i], t );
+                q[i] = fmaf( (float)code_diag( cB[i] ), dB[i], -acc );
+                t = fmaf( dB[i], q[i], t );
             }
-            tdq[i] = t;
+            pdq = df_add_f( pdq, t );
         }
-        reinterpret_cast<float4*>( sv.q + gA )[0] = make_float4( qA[0], qA[1], qA[2], qA[3] );
-        reinterpret_cast<float4*>( sv.q + gA )[1] = make_float4( qA[4], qA[5], qA[6], qA[7] );
-        reinterpret_cast<float4*>( sv.q + gB )[0] = make_float4( qB[0], qB[1], qB[2], qB[3] );
-        reinterpret_cast<float4*>( sv.q + gB )[1] = make_float4( qB[4], qB[5], qB[6], qB[7] );
-#pragma unroll
-        for( int i = 0; i < 8; ++i ) pdq = df_add_f( pdq, tdq[i] );
+        reinterpret_cast<float4*>( sv.q + gB )[0] = make_float4( q[0], q[1], q[2], q[3] );
+        reinterpret_cast<float4*>( sv.q + gB )[1] = make_float4( q[4], q[5], q[6], q[7] );
     }
     return pdq;
 }
@@ -610,7 +615,7 @@ __device__ __forceinline__ void pcg_direction_body( int ntiles, const int32_t* _
     reduce2_publish_warp( df_warp_sum( pdq ), 0.0, 0, red, slot_dq_out, -1, bid, G );
 }
 
-__global__ void __launch_bounds__( 32 * kDirWarps ) k_pcg_direction( int ntiles, const int32_t* __restrict__ nbr,
+__global__ void __launch_bounds__( 32 * kDirWarps, 7 ) k_pcg_direction( int ntiles, const int32_t* __restrict__ nbr,
                                                                     const uint16_t* __restrict__ code, BoraSolverDev sv,
                                                                     int dsel_in, BoraReduceDev red, int slot_rz_new,
                                                                     int slot_rz_old, int slot_dq_out, int slot_a_rz,
