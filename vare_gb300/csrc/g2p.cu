@@ -13,8 +13,9 @@
 namespace {
 
 // Grid values of a tile and its high-side halo layer, (8+1)^3 cells, staged in shared
-// memory as two float4 per cell: (comp, surf) and (velo, 0). Cells of inactive tiles hold
-// the field backgrounds (0, and 10 for surf: FLIPMethod.cu:30).
+// memory as two float4 per cell: (comp.x, comp.y, velo.x, velo.y) and (comp.z, velo.z, surf,
+// 0), so that the lerps of both vector fields read two float4 per corner. Cells of inactive
+// tiles hold the field backgrounds (0, and 10 for surf: FLIPMethod.cu:30).
 constexpr int kG2PThreads = 256;
 constexpr int kStageEdge = BORA_TILE + 1;
 constexpr int kStageCells = kStageEdge * kStageEdge * kStageEdge;
@@ -46,22 +47,28 @@ struct StagedLerp
         return make_float4( a.x * ( 1.f - t ) + b.x * t, a.y * ( 1.f - t ) + b.y * t, a.z * ( 1.f - t ) + b.z * t,
                             a.w * ( 1.f - t ) + b.w * t );
     }
-    __device__ inline float4 lerp( const float4* f ) const
-    {
-        const float4 c00 = mix( f[base + off( 0 )], f[base + off( 1 )], x );
-        const float4 c01 = mix( f[base + off( 2 )], f[base + off( 3 )], x );
-        const float4 c10 = mix( f[base + off( 4 )], f[base + off( 5 )], x );
-        const float4 c11 = mix( f[base + off( 6 )], f[base + off( 7 )], x );
-        return mix( mix( c00, c10, y ), mix( c01, c11, y ), z );
-    }
     __device__ static inline float fminf_ref( float a, float b ) { return a < b ? a : b; }  // MathUtils.h:174
-    __device__ inline float lerp_min_w( const float4* f ) const
+    // comp and velo lerped from the staged cells (comp.xy and velo.xy from fa, comp.z and
+    // velo.z from fb), and lerpMin of surf; the corners' mix order and the min order are
+    // SparseField's
+    __device__ inline void sample( const float4* fa, const float4* fb, float4& comp, float4& velo, float& smin ) const
     {
-        float v = fminf_ref( f[base + off( 0 )].w, f[base + off( 1 )].w );
-        v = fminf_ref( v, fminf_ref( f[base + off( 2 )].w, f[base + off( 3 )].w ) );
-        v = fminf_ref( v, fminf_ref( f[base + off( 4 )].w, f[base + off( 5 )].w ) );
-        v = fminf_ref( v, fminf_ref( f[base + off( 6 )].w, f[base + off( 7 )].w ) );
-        return v;
+        auto lerp = [&]( const float4* f ) {
+            const float4 c00 = mix( f[base + off( 0 )], f[base + off( 1 )], x );
+            const float4 c01 = mix( f[base + off( 2 )], f[base + off( 3 )], x );
+            const float4 c10 = mix( f[base + off( 4 )], f[base + off( 5 )], x );
+            const float4 c11 = mix( f[base + off( 6 )], f[base + off( 7 )], x );
+            return mix( mix( c00, c10, y ), mix( c01, c11, y ), z );
+        };
+        const float4 A = lerp( fa ), B = lerp( fb );
+        comp = make_float4( A.x, A.y, B.x, 0.f );
+        velo = make_float4( A.z, A.w, B.y, 0.f );
+        auto w = [&]( int q ) { return fb[base + off( q )].z; };
+        float v = fminf_ref( w( 0 ), w( 1 ) );
+        v = fminf_ref( v, fminf_ref( w( 2 ), w( 3 ) ) );
+        v = fminf_ref( v, fminf_ref( w( 4 ), w( 5 ) ) );
+        v = fminf_ref( v, fminf_ref( w( 6 ), w( 7 ) ) );
+        smin = v;
     }
 };
 
@@ -167,19 +174,17 @@ __device__ inline float4 comp_at( const BoraGridDev& g, const int32_t* slot_of, 
     return l.comp();
 }
 
-// FLIPMethod::updateParticles for one particle (FLIPMethod.cu:60-170); `smp` has been set
-// up at the particle's position and gives the interpolated grid values. With the RK2
-// option each substep moves the particle by the midpoint rule in the grid velocity field
+// FLIPMethod::updateParticles for one particle (FLIPMethod.cu:60-170); gn and go are the
+// grid's projected and pre-projection velocities lerped at the particle's position. With the
+// RK2 option each substep moves the particle by the midpoint rule in the grid velocity field
 // instead of by its own velocity; everything else is unchanged.
-template <class Sampler>
-__device__ inline bool advance_particle( const BoraGridDev& g, const Sampler& smp, const int32_t* slot_of,
+__device__ inline bool advance_particle( const BoraGridDev& g, float4 gn, float4 go, const int32_t* slot_of,
                                          const BoraCellsDev& c, float& px, float& py, float& pz, float& vx, float& vy,
                                          float& vz, float dt )
 {
     const float lx = (float)g.nx + 0.5f, lz = (float)g.nz + 0.5f;
     const float wall = g.voxel_wall;
     {
-        const float4 gn = smp.comp(), go = smp.velo();
         vx += gn.x - go.x; vy += gn.y - go.y; vz += gn.z - go.z;
         vx = vx * 0.95f + gn.x * 0.05f;
         vy = vy * 0.95f + gn.y * 0.05f;
@@ -270,16 +275,6 @@ __device__ inline bool advance_particle( const BoraGridDev& g, const Sampler& sm
     return kill;
 }
 
-struct StagedSampler
-{
-    StagedLerp l;
-    const float4* fa;
-    const float4* fb;
-    __device__ inline float4 comp() const { return l.lerp( fa ); }
-    __device__ inline float4 velo() const { return l.lerp( fb ); }
-    __device__ inline float surf_min() const { return l.lerp_min_w( fa ); }
-};
-
 // One CTA per tile: stage the tile's grid values, then advance the particles of the
 // tile's dual cells (a contiguous range of the sorted order). The CTA after the last tile
 // advances the sort's outside bin through the tile table.
@@ -289,15 +284,16 @@ __global__ void __launch_bounds__( kG2PThreads, 4 ) k_g2p( const __grid_constant
                                                        BoraParticlesDev dst, float* __restrict__ adj, float dt,
                                                        uint32_t* __restrict__ nkilled )
 {
-    __shared__ float4 fa[kStageCells];  // comp, surf
-    __shared__ float4 fb[kStageCells];  // velo, 0
+    __shared__ float4 fa[kStageCells];  // comp.x, comp.y, velo.x, velo.y
+    __shared__ float4 fb[kStageCells];  // comp.z, velo.z, surf, 0
     __shared__ int32_t nb[27];
     const int s = blockIdx.x, tid = threadIdx.x;
     uint32_t kills = 0;
-    auto finish = [&]( uint32_t q, uint32_t pi, float px, float py, float pz, float vx, float vy, float vz, bool kill ) {
+    auto finish = [&]( uint32_t q, uint32_t pi, int32_t id, float px, float py, float pz, float vx, float vy, float vz,
+                       bool kill ) {
         dst.px[q] = px; dst.py[q] = py; dst.pz[q] = pz;
         dst.vx[q] = vx; dst.vy[q] = vy; dst.vz[q] = vz;
-        dst.id[q] = kill ? -1 : src.id[pi];
+        dst.id[q] = kill ? -1 : id;
         if( dst.vort )  // post-processing attributes ride along (FLIPMethod.cu:295-296)
         {
             dst.vort[q] = src.vort[pi];
@@ -316,8 +312,8 @@ __global__ void __launch_bounds__( kG2PThreads, 4 ) k_g2p( const __grid_constant
             GlobalLerp smp{ g, t.slot_of, c };
             smp.setup( px, py, pz );
             adj[q] = smp.surf_min();
-            const bool kill = advance_particle( g, smp, t.slot_of, c, px, py, pz, vx, vy, vz, dt );
-            finish( q, pi, px, py, pz, vx, vy, vz, kill );
+            const bool kill = advance_particle( g, smp.comp(), smp.velo(), t.slot_of, c, px, py, pz, vx, vy, vz, dt );
+            finish( q, pi, src.id[pi], px, py, pz, vx, vy, vz, kill );
         }
     }
     else
@@ -325,28 +321,35 @@ __global__ void __launch_bounds__( kG2PThreads, 4 ) k_g2p( const __grid_constant
         if( tid < 27 ) nb[tid] = t.nbr[(size_t)s * 27 + tid];
         const int vt = t.tile_of[s];
         const int ti = vt % g.tx, tj = ( vt / g.tx ) % g.ty, tk = vt / ( g.tx * g.ty );
-        // the thread's particles are loaded one ahead: the first before the staging, each
-        // next one while the current one is advanced
+        // the thread's particles are loaded one ahead and their sorted-order indices two ahead:
+        // the first particle and the second index before the staging, then each next particle
+        // (from an index that has arrived) while the current one is advanced
         const uint32_t q0 = start[(size_t)s * BORA_TILE_CELLS], q1 = start[(size_t)( s + 1 ) * BORA_TILE_CELLS];
-        uint32_t pin = 0;
+        uint32_t pin = 0, pin2 = 0;
+        int32_t idn = 0;
         float pxn = 0.f, pyn = 0.f, pzn = 0.f, vxn = 0.f, vyn = 0.f, vzn = 0.f;
-        auto fetch = [&]( uint32_t q ) {
-            pin = idx[q];
-            pxn = src.px[pin]; pyn = src.py[pin]; pzn = src.pz[pin];
-            vxn = src.vx[pin]; vyn = src.vy[pin]; vzn = src.vz[pin];
+        auto fetch = [&]( uint32_t pi ) {
+            pxn = src.px[pi]; pyn = src.py[pi]; pzn = src.pz[pi];
+            vxn = src.vx[pi]; vyn = src.vy[pi]; vzn = src.vz[pi];
+            idn = src.id[pi];
         };
-        if( q0 + tid < q1 ) fetch( q0 + tid );
+        if( q0 + tid < q1 )
+        {
+            pin = idx[q0 + tid];
+            fetch( pin );
+        }
+        if( q0 + tid + kG2PThreads < q1 ) pin2 = idx[q0 + tid + kG2PThreads];
         __syncthreads();
         for( int h = tid; h < kStageCells; h += kG2PThreads )
         {
             const int a = h % kStageEdge, b = ( h / kStageEdge ) % kStageEdge, cz = h / ( kStageEdge * kStageEdge );
             const int ns = nb[bora_dir( a >> 3, b >> 3, cz >> 3 )];
-            float4 va = make_float4( 0.f, 0.f, 0.f, 10.f ), vb = make_float4( 0.f, 0.f, 0.f, 0.f );
+            float4 va = make_float4( 0.f, 0.f, 0.f, 0.f ), vb = make_float4( 0.f, 0.f, 10.f, 0.f );
             if( ns >= 0 )
             {
                 const size_t q = (size_t)ns * BORA_TILE_CELLS + (size_t)bora_local( a, b, cz );
-                va = make_float4( c.cx[q], c.cy[q], c.cz[q], c.surf[q] );
-                vb = make_float4( c.vx[q], c.vy[q], c.vz[q], 0.f );
+                va = make_float4( c.cx[q], c.cy[q], c.vx[q], c.vy[q] );
+                vb = make_float4( c.cz[q], c.vz[q], c.surf[q], 0.f );
             }
             fa[h] = va;
             fb[h] = vb;
@@ -355,14 +358,23 @@ __global__ void __launch_bounds__( kG2PThreads, 4 ) k_g2p( const __grid_constant
         for( uint32_t q = q0 + tid; q < q1; q += kG2PThreads )
         {
             const uint32_t pi = pin;
+            const int32_t id = idn;
             float px = pxn, py = pyn, pz = pzn;
             float vx = vxn, vy = vyn, vz = vzn;
-            if( q + kG2PThreads < q1 ) fetch( q + kG2PThreads );
-            StagedSampler smp{ {}, fa, fb };
-            smp.l.setup( g, ti, tj, tk, px, py, pz );
-            adj[q] = smp.surf_min();  // surf background 10 (FLIPMethod.cu:30)
-            const bool kill = advance_particle( g, smp, t.slot_of, c, px, py, pz, vx, vy, vz, dt );
-            finish( q, pi, px, py, pz, vx, vy, vz, kill );
+            if( q + kG2PThreads < q1 )
+            {
+                pin = pin2;
+                fetch( pin );
+                if( q + 2 * kG2PThreads < q1 ) pin2 = idx[q + 2 * kG2PThreads];
+            }
+            StagedLerp l;
+            l.setup( g, ti, tj, tk, px, py, pz );
+            float4 gn, go;
+            float smin;
+            l.sample( fa, fb, gn, go, smin );
+            adj[q] = smin;  // surf background 10 (FLIPMethod.cu:30)
+            const bool kill = advance_particle( g, gn, go, t.slot_of, c, px, py, pz, vx, vy, vz, dt );
+            finish( q, pi, id, px, py, pz, vx, vy, vz, kill );
         }
     }
     // one atomic per warp
