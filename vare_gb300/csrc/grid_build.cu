@@ -191,6 +191,16 @@ __global__ void k_scatter( size_t n, const uint32_t* __restrict__ key, const uin
 // arrival order; this makes the order - and so every floating-point sum over a bin - a
 // function of the input only. Bins larger than `max_bin` (possible only for the bin of
 // particles outside the grid) keep their arrival order.
+// Batcher's odd-even merge sort (Knuth, TAOCP vol. 3, 5.3.4) on 16 inputs: comparator pairs
+// (a, b), a < b, in the order applied.
+constexpr int kSortNet16 = 63;
+__constant__ const int8_t kNet16[2 * kSortNet16] = {
+    0, 1, 2, 3, 0, 2, 1, 3, 1, 2, 4, 5, 6, 7, 4, 6, 5, 7, 5, 6, 0, 4, 2, 6, 2, 4, 1, 5, 3, 7, 3, 5,
+    1, 2, 3, 4, 5, 6, 8, 9, 10, 11, 8, 10, 9, 11, 9, 10, 12, 13, 14, 15, 12, 14, 13, 15, 13, 14, 8, 12, 10, 14,
+    10, 12, 9, 13, 11, 15, 11, 13, 9, 10, 11, 12, 13, 14, 0, 8, 4, 12, 4, 8, 2, 10, 6, 14, 6, 10, 2, 4, 6, 8,
+    10, 12, 1, 9, 5, 13, 5, 9, 3, 11, 7, 15, 7, 11, 3, 5, 7, 9, 11, 13, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12,
+    13, 14 };
+
 __global__ void k_order_bins( size_t nbins, const uint32_t* __restrict__ start, uint32_t* __restrict__ idx,
                               uint32_t max_bin )
 {
@@ -209,16 +219,16 @@ __global__ void k_order_bins( size_t nbins, const uint32_t* __restrict__ start, 
 #pragma unroll
             for( int a = 1; a < kReg; ++a ) sorted = sorted && v[a - 1] < v[a];  // padding sorts last
             if( sorted ) continue;
-            // odd-even transposition network (indices are distinct)
+            // Batcher's odd-even merge sorting network for 16 inputs (63 comparators; indices
+            // are distinct)
 #pragma unroll
-            for( int pass = 0; pass < kReg; ++pass )
-#pragma unroll
-                for( int a = pass & 1; a + 1 < kReg; a += 2 )
-                {
-                    const uint32_t lo = min( v[a], v[a + 1] ), hi = max( v[a], v[a + 1] );
-                    v[a] = lo;
-                    v[a + 1] = hi;
-                }
+            for( int c = 0; c < kSortNet16; ++c )
+            {
+                const int a = kNet16[2 * c], b = kNet16[2 * c + 1];
+                const uint32_t lo = min( v[a], v[b] ), hi = max( v[a], v[b] );
+                v[a] = lo;
+                v[b] = hi;
+            }
 #pragma unroll
             for( int a = 0; a < kReg; ++a )
                 if( a < (int)n ) idx[q0 + a] = v[a];
