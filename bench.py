@@ -44,19 +44,20 @@ UNIT = "particle-steps/s"
 #   pcg_update:    read r, q (8) + M^-1 (4); write r, z (8)                   -> 20 B/cell
 #   p2g:           per particle read idx (4) + pos, vel (24); per cell read dual-cell
 #                  starts (4), write mass, count, velocity (20) + flag (1)      -> 25 B/cell, 28 B/particle
-#   g2p:           per particle idx (4), read pos, vel, id (28), write (28), adjacency (4);
-#                  per cell read velo, comp, count (28)                          -> 28 B/cell, 64 B/particle
+#   g2p:           per particle idx (4), read pos, vel, id (28), write (28), adjacency (4), the next
+#                  rebuild's sort key (4); per cell read velo, comp, count (28)  -> 28 B/cell, 68 B/particle
 #   velocity:      read flag (1), pres (4), velo (12); write pres (4), comp (12)  -> 33 B/cell
 #   rhs:           read flag (1), velo (12); write b (4), code (2); MIC read code (2), write M (4) -> 25 B/cell
 #   refine:        per pass read x (8), e (4), b (4), code (2); write x (8), r (4) -> 30 B/cell
 #   sort:          per particle read vkey (4), write key (4), read key (4), write idx (4); per cell scan 12 B
-#   bin:           per particle read id + pos (16), write vkey (4)
+#   bin:           per particle read id + pos (16), write vkey (4); only after the particles changed
+#                  between steps (G2P bins the particles it writes)
 #   mg_vcycle:     level 0 down: read r (4), code (2); write z0 (2), coarse r (0.25); level 0 up:
 #                  read r (4), code (2), z0 (2), coarse z (0.25); write z (4) -> 20.5 B per fine
 #                  cell, plus the coarser levels (1/8 of that per level)       -> 23 B/cell
 ALG_BYTES = {
     "bin": (0, 20), "tiles": (0, 0), "sort": (12, 16), "p2g": (25, 28), "rhs": (25, 0),
-    "pcg_direction": (26, 0), "pcg_update": (20, 0), "refine": (30, 0), "velocity": (33, 0), "g2p": (28, 64),
+    "pcg_direction": (26, 0), "pcg_update": (20, 0), "refine": (30, 0), "velocity": (33, 0), "g2p": (28, 68),
     "mg_vcycle": (23, 0),
 }
 # Mixed form: the PCG update has no preconditioner sweep (read r, q; write r: 12 B/cell) and

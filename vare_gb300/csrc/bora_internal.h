@@ -147,7 +147,7 @@ void bora_launch_rhs( const BoraGridDev& g, int ntiles, BoraTilesDev t, BoraCell
 void bora_launch_vel_update( const BoraGridDev& g, int ntiles, BoraTilesDev t, BoraCellsDev c, cudaStream_t st );
 void bora_launch_g2p( const BoraGridDev& g, int ntiles, size_t nsorted, BoraTilesDev t, const uint32_t* start, BoraCellsDev c,
                       BoraParticlesDev src, const uint32_t* idx, BoraParticlesDev dst, float* adj, float dt,
-                      uint32_t* nkilled, cudaStream_t st );
+                      uint32_t* nkilled, uint32_t* vkey, uint8_t* tile_flag, cudaStream_t st );
 // ---- post-processing (FLIPMethod::postProcess) ------------------------------------------
 void bora_launch_splat( const BoraGridDev& g, int ntiles, BoraTilesDev t, const uint32_t* start, const uint32_t* idx,
                         BoraParticlesDev p, BoraCellsDev c, cudaStream_t st );

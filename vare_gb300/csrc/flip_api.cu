@@ -176,6 +176,7 @@ struct bora_flip_sim
     int cur = 0;
     int32_t next_id = 0;
     bool sorted = false;   // idx/cell_start describe the current buffer
+    bool keys_valid = false;  // vkey and tile_flag bin the current buffer (written by the last G2P)
 
     // scratch and staging
     DevBuf scan_scratch, counters, stage_in, stage_out, live_flag;
@@ -447,9 +448,14 @@ double read_ring( bora_flip_sim* s, int slot, int* status )
 int rebuild_tiles( bora_flip_sim* s )
 {
     cudaStream_t st = s->st;
-    BORA_TRY( cudaMemsetAsync( s->tile_flag.p, 0, s->ntv, st ) );
     BORA_TRY( cudaMemsetAsync( s->counters.p, 0, 8 * 4, st ) );
-    if( s->np ) { KTimer t( s, BORA_KERNEL_BIN, 1 ); bora_launch_bin( s->g, s->parts( s->cur ), s->np, P<uint32_t>( s->vkey ), P<uint8_t>( s->tile_flag ), st ); }
+    // the last G2P binned the particles it wrote, unless they have changed since
+    if( !s->keys_valid )
+    {
+        BORA_TRY( cudaMemsetAsync( s->tile_flag.p, 0, s->ntv, st ) );
+        if( s->np ) { KTimer t( s, BORA_KERNEL_BIN, 1 ); bora_launch_bin( s->g, s->parts( s->cur ), s->np, P<uint32_t>( s->vkey ), P<uint8_t>( s->tile_flag ), st ); }
+    }
+    s->keys_valid = false;
     {
         KTimer t( s, BORA_KERNEL_TILES, 4 );
         bora_launch_activate( s->g, P<uint8_t>( s->tile_flag ), P<uint32_t>( s->tile_act ), st );
@@ -783,11 +789,13 @@ int g2p_issue( bora_flip_sim* s, float dt )
     if( !s->sorted ) return BORA_ERR_INVALID_ARG;
     cudaStream_t st = s->st;
     BORA_TRY( cudaMemsetAsync( P<uint32_t>( s->counters ) + 3, 0, 4, st ) );
+    BORA_TRY( cudaMemsetAsync( s->tile_flag.p, 0, s->ntv, st ) );  // G2P bins what it writes for the next rebuild
     const int nxt = s->cur ^ 1;
     {
         KTimer t( s, BORA_KERNEL_G2P, s->nsorted > 0 );
         bora_launch_g2p( s->g, s->ntiles, s->nsorted, s->tiles(), P<uint32_t>( s->cell_start ), s->cells(), s->parts( s->cur ),
-                         P<uint32_t>( s->idx ), s->parts( nxt ), P<float>( s->adj ), dt, P<uint32_t>( s->counters ) + 3, st );
+                         P<uint32_t>( s->idx ), s->parts( nxt ), P<float>( s->adj ), dt, P<uint32_t>( s->counters ) + 3,
+                         P<uint32_t>( s->vkey ), P<uint8_t>( s->tile_flag ), st );
     }
     BORA_TRYS( check_launch( s ) );
     return issue_counters( s, 3, 1, st );
@@ -798,6 +806,7 @@ int g2p_finish( bora_flip_sim* s )
     s->cur ^= 1;
     s->np = s->nsorted;
     s->sorted = false;
+    s->keys_valid = true;
     s->stats.killed_last_step = s->h_cnt[3];
     s->nlive = s->np - s->h_cnt[3];
     s->stats.num_particles = s->nlive;
@@ -928,6 +937,7 @@ int add_particles( bora_flip_sim* s, const float* pos, const float* vel, size_t 
     s->nlive += n;
     s->next_id += (int32_t)n;
     s->sorted = false;
+    s->keys_valid = false;
     s->stats.num_particles = s->nlive;
     return BORA_OK;
 }
@@ -1091,6 +1101,7 @@ int bora_flip_set_params( bora_flip_handle s, const bora_flip_params* p )
     s->prm = *p;
     apply_params( s );
     s->sorted = false;  // the water tank's rows change the activation
+    s->keys_valid = false;
     return BORA_OK;
 }
 
@@ -1137,6 +1148,7 @@ int bora_flip_fill_water_tank( bora_flip_handle s, size_t* added )
     s->nlive += n;
     s->next_id += (int32_t)n;
     s->sorted = false;
+    s->keys_valid = false;
     s->stats.num_particles = s->nlive;
     if( added ) *added = n;
     return BORA_OK;
@@ -1149,6 +1161,7 @@ int bora_flip_clear_particles( bora_flip_handle s )
     s->nlive = 0;
     s->next_id = 0;
     s->sorted = false;
+    s->keys_valid = false;
     s->attrs = false;
     s->stats.num_particles = 0;
     return BORA_OK;

@@ -100,6 +100,38 @@ __host__ __device__ inline int bora_local( int i, int j, int k ) { return ( i & 
 // Neighbour direction index 0..26 of an offset in {-1,0,1}^3.
 __host__ __device__ inline int bora_dir( int dx, int dy, int dz ) { return ( dx + 1 ) + 3 * ( dy + 1 ) + 9 * ( dz + 1 ); }
 
+// The rebuild's binning rule for one particle (SparseFrame::buildFromPoints,
+// SparseFrame.cu:101-103 at tile edge 8): a live particle activates its tile
+// (max(int(p)/8, 0), clamped to the table) and gets the key virtual tile * 512 + local index
+// of its dual cell (the base cell max(int(p - 0.5), 0) of the P2G stencil, Rasterization.cu:
+// 139-141); killed particles get BORA_DEAD_KEY, live ones outside the grid (Grid::inside,
+// Grid.h:408-417) BORA_DEAD_KEY - 1 (they still activate their clamped tile).
+__device__ inline void bora_bin_tile( int tx, int ty, int tz, float x, float y, float z, int& ti, int& tj, int& tk )
+{
+    ti = bora_imin( bora_imax( bora_trunc( x ) / BORA_TILE, 0 ), tx - 1 );
+    tj = bora_imin( bora_imax( bora_trunc( y ) / BORA_TILE, 0 ), ty - 1 );
+    tk = bora_imin( bora_imax( bora_trunc( z ) / BORA_TILE, 0 ), tz - 1 );
+}
+__device__ inline uint32_t bora_bin_live_key( int nx, int ny, int nz, int tx, int ty, float x, float y, float z )
+{
+    if( x < 0.f || x > (float)nx || y < 0.f || y > (float)ny || z < 0.f || z > (float)nz ) return BORA_DEAD_KEY - 1;
+    const int di = bora_imax( bora_trunc( x - 0.5f ), 0 );
+    const int dj = bora_imax( bora_trunc( y - 0.5f ), 0 );
+    const int dk = bora_imax( bora_trunc( z - 0.5f ), 0 );
+    const uint32_t vt = (uint32_t)( ( (size_t)( dk >> 3 ) * ty + ( dj >> 3 ) ) * tx + ( di >> 3 ) );
+    return vt * BORA_TILE_CELLS + (uint32_t)bora_local( di, dj, dk );
+}
+// both parts, the tile flag stored in tile_flag
+__device__ inline uint32_t bora_bin_key( int nx, int ny, int nz, int tx, int ty, int tz, int32_t id, float x, float y,
+                                         float z, uint8_t* __restrict__ tile_flag )
+{
+    if( id < 0 ) return BORA_DEAD_KEY;
+    int ti, tj, tk;
+    bora_bin_tile( tx, ty, tz, x, y, z, ti, tj, tk );
+    tile_flag[( (size_t)tk * ty + tj ) * tx + ti] = 1;
+    return bora_bin_live_key( nx, ny, nz, tx, ty, x, y, z );
+}
+
 // ---- analytic box colliders sampled at cell centres -------------------------------
 // The reference samples an OpenVDB level set into sparse fields and lerps the samples
 // (base/header/CollisionSource.h:66-150). Colliders here are analytic boxes: cell-centre

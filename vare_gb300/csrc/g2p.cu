@@ -6,7 +6,10 @@
 // Particles are visited in dual-cell order through the sort permutation and written
 // to the other particle buffer in that order, so the particle store stays spatially
 // sorted and each warp's trilinear reads hit the same few cells. Killed particles are
-// written with id -1 and dropped by the next step's counting sort.
+// written with id -1 and dropped by the next step's counting sort. Each written particle
+// is also binned for the next rebuild (its sort key and tile flag, the rule of k_bin), so
+// that the next step need not read the particles again to bin them; a tile's CTA marks the
+// flags of the 27 tiles around its own in shared memory and stores each marked one once.
 #include "bora_internal.h"
 #include "../../include/bora_flip.h"
 
@@ -282,18 +285,32 @@ __global__ void __launch_bounds__( kG2PThreads, 4 ) k_g2p( const __grid_constant
                                                        uint32_t nsorted, const uint32_t* __restrict__ start, BoraCellsDev c,
                                                        BoraParticlesDev src, const uint32_t* __restrict__ idx,
                                                        BoraParticlesDev dst, float* __restrict__ adj, float dt,
-                                                       uint32_t* __restrict__ nkilled )
+                                                       uint32_t* __restrict__ nkilled, uint32_t* __restrict__ vkey,
+                                                       uint8_t* __restrict__ tile_flag )
 {
     __shared__ float4 fa[kStageCells];  // comp.x, comp.y, velo.x, velo.y
     __shared__ float4 fb[kStageCells];  // comp.z, velo.z, surf, 0
     __shared__ int32_t nb[27];
+    __shared__ uint8_t near_flag[27];  // activation flags of the tiles around the CTA's own
     const int s = blockIdx.x, tid = threadIdx.x;
     uint32_t kills = 0;
+    int cti = -8, ctj = -8, ctk = -8;  // the CTA's tile (far from every tile: no shared flags)
     auto finish = [&]( uint32_t q, uint32_t pi, int32_t id, float px, float py, float pz, float vx, float vy, float vz,
                        bool kill ) {
         dst.px[q] = px; dst.py[q] = py; dst.pz[q] = pz;
         dst.vx[q] = vx; dst.vy[q] = vy; dst.vz[q] = vz;
         dst.id[q] = kill ? -1 : id;
+        uint32_t key = BORA_DEAD_KEY;
+        if( !kill && id >= 0 )
+        {
+            int ti, tj, tk;
+            bora_bin_tile( g.tx, g.ty, g.tz, px, py, pz, ti, tj, tk );
+            const int dx = ti - cti, dy = tj - ctj, dz = tk - ctk;
+            if( dx >= -1 && dx <= 1 && dy >= -1 && dy <= 1 && dz >= -1 && dz <= 1 ) near_flag[bora_dir( dx, dy, dz )] = 1;
+            else tile_flag[( (size_t)tk * g.ty + tj ) * g.tx + ti] = 1;
+            key = bora_bin_live_key( g.nx, g.ny, g.nz, g.tx, g.ty, px, py, pz );
+        }
+        vkey[q] = key;
         if( dst.vort )  // post-processing attributes ride along (FLIPMethod.cu:295-296)
         {
             dst.vort[q] = src.vort[pi];
@@ -319,8 +336,10 @@ __global__ void __launch_bounds__( kG2PThreads, 4 ) k_g2p( const __grid_constant
     else
     {
         if( tid < 27 ) nb[tid] = t.nbr[(size_t)s * 27 + tid];
+        if( tid < 27 ) near_flag[tid] = 0;
         const int vt = t.tile_of[s];
         const int ti = vt % g.tx, tj = ( vt / g.tx ) % g.ty, tk = vt / ( g.tx * g.ty );
+        cti = ti; ctj = tj; ctk = tk;
         // the thread's particles are loaded one ahead and their sorted-order indices two ahead:
         // the first particle and the second index before the staging, then each next particle
         // (from an index that has arrived) while the current one is advanced
@@ -376,6 +395,12 @@ __global__ void __launch_bounds__( kG2PThreads, 4 ) k_g2p( const __grid_constant
             const bool kill = advance_particle( g, gn, go, t.slot_of, c, px, py, pz, vx, vy, vz, dt );
             finish( q, pi, id, px, py, pz, vx, vy, vz, kill );
         }
+        __syncthreads();
+        if( tid < 27 && near_flag[tid] )  // a marked tile is a clamped particle tile: inside the table
+        {
+            const int i = cti + tid % 3 - 1, j = ctj + ( tid / 3 ) % 3 - 1, k = ctk + tid / 9 - 1;
+            tile_flag[( (size_t)k * g.ty + j ) * g.tx + i] = 1;
+        }
     }
     // one atomic per warp
     for( int o = 16; o > 0; o >>= 1 ) kills += __shfl_xor_sync( 0xffffffffu, kills, o );
@@ -386,8 +411,9 @@ __global__ void __launch_bounds__( kG2PThreads, 4 ) k_g2p( const __grid_constant
 
 void bora_launch_g2p( const BoraGridDev& g, int ntiles, size_t nsorted, BoraTilesDev t, const uint32_t* start, BoraCellsDev c,
                       BoraParticlesDev src, const uint32_t* idx, BoraParticlesDev dst, float* adj, float dt,
-                      uint32_t* nkilled, cudaStream_t st )
+                      uint32_t* nkilled, uint32_t* vkey, uint8_t* tile_flag, cudaStream_t st )
 {
     if( nsorted == 0 ) return;
-    k_g2p<<<ntiles + 1, kG2PThreads, 0, st>>>( g, t, ntiles, (uint32_t)nsorted, start, c, src, idx, dst, adj, dt, nkilled );
+    k_g2p<<<ntiles + 1, kG2PThreads, 0, st>>>( g, t, ntiles, (uint32_t)nsorted, start, c, src, idx, dst, adj, dt, nkilled,
+                                               vkey, tile_flag );
 }

@@ -22,28 +22,10 @@ inline int grid_for( size_t n, int threads = kThreads )
     return (int)( b < 152 * 16 ? ( b > 0 ? b : 1 ) : 152 * 16 );  // grid-stride loops: 16 blocks per SM
 }
 
-// Grid::inside (base/header/Grid.h:408-417)
-__device__ inline bool inside_grid( const BoraGridDev& g, float x, float y, float z )
-{
-    return !( x < 0.f || x > (float)g.nx || y < 0.f || y > (float)g.ny || z < 0.f || z > (float)g.nz );
-}
-
 __device__ inline uint32_t bin_one( const BoraGridDev& g, int32_t id, float x, float y, float z,
                                     uint8_t* __restrict__ tile_flag )
 {
-    if( id < 0 ) return BORA_DEAD_KEY;
-    // activation tile: SparseFrame.cu:101-103 at tile edge 8, clamped to the table
-    const int ti = bora_imin( bora_imax( bora_trunc( x ) / BORA_TILE, 0 ), g.tx - 1 );
-    const int tj = bora_imin( bora_imax( bora_trunc( y ) / BORA_TILE, 0 ), g.ty - 1 );
-    const int tk = bora_imin( bora_imax( bora_trunc( z ) / BORA_TILE, 0 ), g.tz - 1 );
-    tile_flag[( (size_t)tk * g.ty + tj ) * g.tx + ti] = 1;
-    if( !inside_grid( g, x, y, z ) ) return BORA_DEAD_KEY - 1;
-    // dual cell = base of the P2G stencil (Rasterization.cu:139-141); <= n-1 inside
-    const int di = bora_imax( bora_trunc( x - 0.5f ), 0 );
-    const int dj = bora_imax( bora_trunc( y - 0.5f ), 0 );
-    const int dk = bora_imax( bora_trunc( z - 0.5f ), 0 );
-    const uint32_t vt = (uint32_t)( ( (size_t)( dk >> 3 ) * g.ty + ( dj >> 3 ) ) * g.tx + ( di >> 3 ) );
-    return vt * BORA_TILE_CELLS + (uint32_t)bora_local( di, dj, dk );
+    return bora_bin_key( g.nx, g.ny, g.nz, g.tx, g.ty, g.tz, id, x, y, z, tile_flag );
 }
 
 // Four particles per thread with 16-byte loads and stores (the arrays are 256-byte
