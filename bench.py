@@ -73,7 +73,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="dam_sphere_256",
-                    choices=["dam_sphere_256", "dam_break_64", "tank_1024", "serve_64"])
+                    choices=["dam_sphere_256", "dam_sphere_160", "dam_break_64", "tank_1024", "serve_64"],
+                    help="dam_sphere_160: the 256^3 scene at 160^3, for profiler captures")
     ap.add_argument("--serve-requests", type=int, default=64)
     ap.add_argument("--serve-slots", type=int, default=64)
     ap.add_argument("--no-serve", action="store_true", help="skip the serving-stream measurement of the default run")
@@ -99,6 +100,8 @@ def make_scene(name):
     from vare_gb300 import scenes
     if name == "tank_1024":
         return scenes.config3()
+    if name == "dam_sphere_160":
+        return scenes.dam_sphere(160)
     return scenes.config1() if name == "dam_sphere_256" else scenes.config0()
 
 

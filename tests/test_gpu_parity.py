@@ -438,6 +438,33 @@ def test_tank_scene_matches_oracle(gpu, oracle_lib, solver):
     assert rel_err(g[1], o[1]) <= TOL
 
 
+def test_emission_between_steps_matches_oracle(gpu, oracle_lib):
+    """Particles emitted between steps (FLIPMethod::newParticle, FLIPMethod.h:75-99) join the
+    next step. G2P bins only the particles it writes, so the rebuild after an emission must bin
+    the particles again; the oracle gets the same particles appended with the same ids (the
+    device hands ids out in order of addition)."""
+    sc = scenes.small(24, seed=5)
+    sim = gpu.FlipSim.from_scene(sc, **tight())
+    ora = oracle_lib.Oracle(sc, block=8, solver="fp64", tol=1e-13, threads=1)
+    assert sim.step(sc.dt) == 0
+    ora.step(sc.dt)
+    n0, m = sc.pos.shape[0], 500
+    rng = np.random.default_rng(3)
+    new = (rng.random((m, 3)) * [6.0, 4.0, 6.0] + [9.0, 14.0, 9.0]).astype(np.float32)  # voxel space
+    newv = np.tile(np.float32([0.0, -2.0, 0.0]), (m, 1))
+    sim.add_particles(new, newv, space=gpu.SPACE_VOXEL)
+    p, v, _, ids = ora.particles()
+    ora.set_particles(np.concatenate([p, new]), np.concatenate([v, newv]),
+                      np.concatenate([ids, np.arange(n0, n0 + m, dtype=np.int32)]))
+    for _ in range(2):
+        assert sim.step(sc.dt) == 0
+        ora.step(sc.dt)
+    g = by_id(*sim.particles())
+    o = by_id(*ora.particles())
+    np.testing.assert_array_equal(g[3], o[3])
+    assert rel_err(g[0], o[0]) <= TOL and rel_err(g[1], o[1]) <= TOL
+
+
 def test_water_tank_matches_oracle(gpu, oracle_lib):
     """FLIPMethod::fillWaterTank on the device (bit-exact particles, in the reference's
     order) and steps with the tank on: its tile rows stay active, the damping band acts."""

@@ -64,6 +64,7 @@ __global__ void __launch_bounds__( 512 ) k_rhs( BoraGridDev g, BoraTilesDev t, B
     int ti, tj, tk;
     tile_coords( g, t.tile_of[s], ti, tj, tk );
     __syncthreads();
+#pragma unroll 2
     for( int h = threadIdx.x; h < HL::N; h += blockDim.x )
     {
         const long long gi = halo_index<1>( g, nb, ti, tj, tk, h );
@@ -970,6 +971,9 @@ __global__ void __launch_bounds__( 512 ) k_vel_update( BoraGridDev g, BoraTilesD
     int ti, tj, tk;
     tile_coords( g, t.tile_of[s], ti, tj, tk );
     __syncthreads();
+    // the pressure is read with the flag, not after it (every active cell holds a pressure,
+    // 0 off the fluid), so that a cell's two loads are in flight together
+#pragma unroll 4
     for( int h = threadIdx.x; h < H2::N; h += blockDim.x )
     {
         const long long gi = halo_index<2>( g, nb, ti, tj, tk, h );
@@ -977,8 +981,9 @@ __global__ void __launch_bounds__( 512 ) k_vel_update( BoraGridDev g, BoraTilesD
         else
         {
             const uint8_t f = c.flag[gi];
+            const float pr = c.pres[gi];
             sf[h] = f;
-            sp[h] = f == BORA_FLUID ? c.pres[gi] : 0.f;
+            sp[h] = f == BORA_FLUID ? pr : 0.f;
         }
     }
     __syncthreads();
