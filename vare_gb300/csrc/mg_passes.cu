@@ -18,7 +18,9 @@
 // neighbour sums in the order ((x- + x+) + (y- + y+)) + (z- + z+), and the 8 children summed as
 // ((x pairs) + (y pairs)) + (z pairs). Every cell is computed once per pass; the scratch is
 // the FP32 cell vector that the plain form keeps its preconditioner pivots in (the mixed form
-// has none), used by one pass pair at a time.
+// has none), used by one pass pair at a time: level 0 stores its z2 and zb there in FP16 (half
+// the bytes of the pass pair's store and reads; the residual of down 2 is then formed from the
+// same FP16 values that z0 keeps), levels 1 and 2 in FP32.
 //
 // Level 0's down passes also apply the PCG's residual update r -= alpha q (alpha = rz / dq of the
 // last direction): down 1 forms the updated residual of its cells and of the face cells it reads,
@@ -161,6 +163,22 @@ struct FieldF32  // down 2 and up 2: a scratch value
     }
     __device__ float one( int t, int c ) const { return t < 0 ? 0.f : v[(size_t)t * 512 + c]; }
 };
+
+struct FieldF16  // down 2 and up 2 (level 0): a scratch value stored in FP16
+{
+    const __half* v;
+    __device__ void row( int t, int c, float* o ) const
+    {
+        if( t < 0 ) { for( int i = 0; i < 8; ++i ) o[i] = 0.f; return; }
+        f16x8( v, (size_t)t * 512 + c, o );
+    }
+    __device__ float one( int t, int c ) const { return t < 0 ? 0.f : __half2float( v[(size_t)t * 512 + c] ); }
+};
+
+__device__ __forceinline__ void st_f16x8( __half* __restrict__ p, size_t g, const float* v )
+{
+    *reinterpret_cast<uint4*>( p + g ) = make_uint4( pack2( v[0], v[1] ), pack2( v[2], v[3] ), pack2( v[4], v[5] ), pack2( v[6], v[7] ) );
+}
 
 struct FieldZa  // up 1: za = z0 + e(parent) on fluid cells
 {
@@ -358,14 +376,14 @@ __device__ __forceinline__ void pass0_body( const Pass0Args& a, unsigned bid, un
                 vA[i] = sweep( vA[i], rA[i], cA[i], sA[i], w + 16 );
                 vB[i] = sweep( vB[i], rB[i], cB[i], sB[i], w + 16 );
             }
-            st_f32x8( a.scratch, gA, vA );
-            st_f32x8( a.scratch, gB, vB );
+            st_f16x8( reinterpret_cast<__half*>( a.scratch ), gA, vA );
+            st_f16x8( reinterpret_cast<__half*>( a.scratch ), gB, vB );
         }
         else if constexpr( P == 1 )
         {
-            f32x8( a.scratch, gA, vA );
-            f32x8( a.scratch, gB, vB );
-            row_sums( FieldF32{ a.scratch }, nf, lane, vA, vB, sA, sB );
+            f16x8( reinterpret_cast<const __half*>( a.scratch ), gA, vA );
+            f16x8( reinterpret_cast<const __half*>( a.scratch ), gB, vB );
+            row_sums( FieldF16{ reinterpret_cast<const __half*>( a.scratch ) }, nf, lane, vA, vB, sA, sB );
             float qA[8], qB[8];  // residuals
 #pragma unroll
             for( int i = 0; i < 8; ++i )
@@ -410,14 +428,14 @@ __device__ __forceinline__ void pass0_body( const Pass0Args& a, unsigned bid, un
                 vA[i] = sweep( vA[i], rA[i], cA[i], sA[i], w + 16 );
                 vB[i] = sweep( vB[i], rB[i], cB[i], sB[i], w + 16 );
             }
-            st_f32x8( a.scratch, gA, vA );
-            st_f32x8( a.scratch, gB, vB );
+            st_f16x8( reinterpret_cast<__half*>( a.scratch ), gA, vA );
+            st_f16x8( reinterpret_cast<__half*>( a.scratch ), gB, vB );
         }
         else
         {
-            f32x8( a.scratch, gA, vA );
-            f32x8( a.scratch, gB, vB );
-            row_sums( FieldF32{ a.scratch }, nf, lane, vA, vB, sA, sB );
+            f16x8( reinterpret_cast<const __half*>( a.scratch ), gA, vA );
+            f16x8( reinterpret_cast<const __half*>( a.scratch ), gB, vB );
+            row_sums( FieldF16{ reinterpret_cast<const __half*>( a.scratch ) }, nf, lane, vA, vB, sA, sB );
             float rawA[8], rawB[8];
             f32x8( a.r0, gA, rawA );
             f32x8( a.r0, gB, rawB );
