@@ -180,7 +180,9 @@ __device__ inline float4 comp_at( const BoraGridDev& g, const int32_t* slot_of, 
 // FLIPMethod::updateParticles for one particle (FLIPMethod.cu:60-170); gn and go are the
 // grid's projected and pre-projection velocities lerped at the particle's position. With the
 // RK2 option each substep moves the particle by the midpoint rule in the grid velocity field
-// instead of by its own velocity; everything else is unchanged.
+// instead of by its own velocity; everything else is unchanged. kAll = false compiles the
+// common case alone: no water tank, no colliders, Euler advection (the caller checks).
+template <bool kAll>
 __device__ inline bool advance_particle( const BoraGridDev& g, float4 gn, float4 go, const int32_t* slot_of,
                                          const BoraCellsDev& c, float& px, float& py, float& pz, float& vx, float& vy,
                                          float& vz, float dt )
@@ -193,7 +195,7 @@ __device__ inline bool advance_particle( const BoraGridDev& g, float4 gn, float4
         vy = vy * 0.95f + gn.y * 0.05f;
         vz = vz * 0.95f + gn.z * 0.05f;
     }
-    if( g.enable_tank && py <= wall )
+    if( kAll && g.enable_tank && py <= wall )
     {
         const float band = g.damping_band;
         float w = 1.f;
@@ -209,7 +211,7 @@ __device__ inline bool advance_particle( const BoraGridDev& g, float4 gn, float4
     // within sqrt(3) cells, and a box distance changes by at most the distance moved. So a
     // particle whose start is farther than 2 |v| dt + 2 cells from every box sees positive
     // collider values all step long. (RK2 moves with the grid velocity: no cull.)
-    bool hasCols = bora_col_active( g.cols );
+    bool hasCols = kAll && bora_col_active( g.cols );
     if( hasCols && g.cols.tslot && g.advection != BORA_ADVECT_RK2 && inside_grid( g, px, py, pz ) )
     {
         // sparse collider: every sample outside its tiles is the (positive) background with
@@ -244,7 +246,7 @@ __device__ inline bool advance_particle( const BoraGridDev& g, float4 gn, float4
         bool col = false;
         for( int it = 0; it < iter; ++it )
         {
-            if( g.advection == BORA_ADVECT_RK2 )
+            if( kAll && g.advection == BORA_ADVECT_RK2 )
             {
                 const float h = 0.5f * sub_dt;
                 const float4 k1 = comp_at( g, slot_of, c, px, py, pz );
@@ -280,8 +282,11 @@ __device__ inline bool advance_particle( const BoraGridDev& g, float4 gn, float4
 
 // One CTA per tile: stage the tile's grid values, then advance the particles of the
 // tile's dual cells (a contiguous range of the sorted order). The CTA after the last tile
-// advances the sort's outside bin through the tile table.
-__global__ void __launch_bounds__( kG2PThreads, 4 ) k_g2p( const __grid_constant__ BoraGridDev g, BoraTilesDev t, int ntiles,
+// advances the sort's outside bin through the tile table. The common-case kernel (kAll =
+// false) needs 80 registers without spills and runs three CTAs per SM; the one with the
+// collider, water-tank and RK2 paths runs four at 64 registers.
+template <bool kAll>
+__global__ void __launch_bounds__( kG2PThreads, kAll ? 4 : 3 ) k_g2p( const __grid_constant__ BoraGridDev g, BoraTilesDev t, int ntiles,
                                                        uint32_t nsorted, const uint32_t* __restrict__ start, BoraCellsDev c,
                                                        BoraParticlesDev src, const uint32_t* __restrict__ idx,
                                                        BoraParticlesDev dst, float* __restrict__ adj, float dt,
@@ -329,7 +334,7 @@ __global__ void __launch_bounds__( kG2PThreads, 4 ) k_g2p( const __grid_constant
             GlobalLerp smp{ g, t.slot_of, c };
             smp.setup( px, py, pz );
             adj[q] = smp.surf_min();
-            const bool kill = advance_particle( g, smp.comp(), smp.velo(), t.slot_of, c, px, py, pz, vx, vy, vz, dt );
+            const bool kill = advance_particle<kAll>( g, smp.comp(), smp.velo(), t.slot_of, c, px, py, pz, vx, vy, vz, dt );
             finish( q, pi, src.id[pi], px, py, pz, vx, vy, vz, kill );
         }
     }
@@ -392,7 +397,7 @@ __global__ void __launch_bounds__( kG2PThreads, 4 ) k_g2p( const __grid_constant
             float smin;
             l.sample( fa, fb, gn, go, smin );
             adj[q] = smin;  // surf background 10 (FLIPMethod.cu:30)
-            const bool kill = advance_particle( g, gn, go, t.slot_of, c, px, py, pz, vx, vy, vz, dt );
+            const bool kill = advance_particle<kAll>( g, gn, go, t.slot_of, c, px, py, pz, vx, vy, vz, dt );
             finish( q, pi, id, px, py, pz, vx, vy, vz, kill );
         }
         __syncthreads();
@@ -414,6 +419,12 @@ void bora_launch_g2p( const BoraGridDev& g, int ntiles, size_t nsorted, BoraTile
                       uint32_t* nkilled, uint32_t* vkey, uint8_t* tile_flag, cudaStream_t st )
 {
     if( nsorted == 0 ) return;
-    k_g2p<<<ntiles + 1, kG2PThreads, 0, st>>>( g, t, ntiles, (uint32_t)nsorted, start, c, src, idx, dst, adj, dt, nkilled,
-                                               vkey, tile_flag );
+    // the common case (no water tank, no colliders, Euler advection) in a kernel without the
+    // code of the others
+    if( g.enable_tank || bora_col_active( g.cols ) || g.advection == BORA_ADVECT_RK2 )
+        k_g2p<true><<<ntiles + 1, kG2PThreads, 0, st>>>( g, t, ntiles, (uint32_t)nsorted, start, c, src, idx, dst, adj, dt,
+                                                         nkilled, vkey, tile_flag );
+    else
+        k_g2p<false><<<ntiles + 1, kG2PThreads, 0, st>>>( g, t, ntiles, (uint32_t)nsorted, start, c, src, idx, dst, adj,
+                                                          dt, nkilled, vkey, tile_flag );
 }

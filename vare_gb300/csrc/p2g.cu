@@ -25,13 +25,13 @@ __device__ __noinline__ float3 col_velocity( const BoraGridDev* g, float x, floa
     return make_float3( cv[0], cv[1], cv[2] );
 }
 
-// One CTA per tile. Each thread owns a dual cell of the tile (then, in a second round, of
-// the tile's low-side halo), reads its particles once in bin order (fixed by k_order_bins)
-// and keeps the 8 corner sums of m, m*v in registers. Every (cell, source dual cell) pair of
+// One CTA per tile. The threads take the tile's 512 dual cells, then the 217 of its low-side
+// halo, one at a time; each reads its dual cell's particles once in bin order (fixed by
+// k_order_bins) and keeps the 8 corner sums of m, m*v in registers. Every (cell, source dual cell) pair of
 // the tile is produced by exactly one thread and parked in shared memory; each cell then
 // adds its 8 sources with a fixed tree, so the result is reproducible. Halo dual cells
 // are recomputed by every tile that needs them instead of being exchanged.
-constexpr int kP2GThreads = 512;
+constexpr int kP2GThreads = 384;  // two CTAs per SM at 80 registers (the 729 dual cells in two rounds)
 constexpr int kP2GHalo = 217;  // 9^3 - 8^3 dual cells with a -1 tile-local coordinate
 constexpr size_t kP2GSmem = 8 * 4 * 512 * sizeof( float ) + 8 * 512 * sizeof( uint32_t );
 
@@ -48,19 +48,19 @@ __global__ void __launch_bounds__( kP2GThreads, 2 ) k_p2g( const __grid_constant
     const int vt = t.tile_of[s];
     const int ti = vt % g.tx, tj = ( vt / g.tx ) % g.ty, tk = vt / ( g.tx * g.ty );
     __syncthreads();
-    for( int round = 0; round < 2; ++round )
+    for( int item = tid; item < 512 + kP2GHalo; item += kP2GThreads )
     {
         int di, dj, dk;  // tile-local dual-cell coordinates in [-1, 7]
-        if( round == 0 )
+        if( item < 512 )
         {
-            di = tid & 7; dj = ( tid >> 3 ) & 7; dk = tid >> 6;
+            di = item & 7; dj = ( item >> 3 ) & 7; dk = item >> 6;
         }
         else
         {
-            if( tid >= kP2GHalo ) break;
-            if( tid < 81 ) { di = tid % 9 - 1; dj = tid / 9 - 1; dk = -1; }
-            else if( tid < 153 ) { const int u = tid - 81; di = u % 9 - 1; dj = -1; dk = u / 9; }
-            else { const int u = tid - 153; di = -1; dj = u & 7; dk = u >> 3; }
+            const int hh = item - 512;
+            if( hh < 81 ) { di = hh % 9 - 1; dj = hh / 9 - 1; dk = -1; }
+            else if( hh < 153 ) { const int u = hh - 81; di = u % 9 - 1; dj = -1; dk = u / 9; }
+            else { const int u = hh - 153; di = -1; dj = u & 7; dk = u >> 3; }
         }
         const int ns = nb[bora_dir( di < 0 ? -1 : 0, dj < 0 ? -1 : 0, dk < 0 ? -1 : 0 )];
         uint32_t q0 = 0, q1 = 0;
@@ -118,52 +118,54 @@ __global__ void __launch_bounds__( kP2GThreads, 2 ) k_p2g( const __grid_constant
     }
     __syncthreads();
     // per cell: fixed tree over the 8 source dual cells
-    const int l = tid;
-    auto tree = [&]( int v ) {
-        const float* q = part + v * 512 + l;
-        return ( ( q[0 * 2048] + q[1 * 2048] ) + ( q[2 * 2048] + q[3 * 2048] ) ) +
-               ( ( q[4 * 2048] + q[5 * 2048] ) + ( q[6 * 2048] + q[7 * 2048] ) );
-    };
-    const float m = tree( 0 ), mx = tree( 1 ), my = tree( 2 ), mz = tree( 3 );
-    uint32_t cnt = 0;
+    for( int l = tid; l < BORA_TILE_CELLS; l += kP2GThreads )
+    {
+        auto tree = [&]( int v ) {
+            const float* q = part + v * 512 + l;
+            return ( ( q[0 * 2048] + q[1 * 2048] ) + ( q[2 * 2048] + q[3 * 2048] ) ) +
+                   ( ( q[4 * 2048] + q[5 * 2048] ) + ( q[6 * 2048] + q[7 * 2048] ) );
+        };
+        const float m = tree( 0 ), mx = tree( 1 ), my = tree( 2 ), mz = tree( 3 );
+        uint32_t cnt = 0;
 #pragma unroll
-    for( int o = 0; o < 8; ++o ) cnt += pcnt[o * 512 + l];
-    const size_t cell = (size_t)s * BORA_TILE_CELLS + l;
-    const int i = ti * BORA_TILE + ( l & 7 ), j = tj * BORA_TILE + ( ( l >> 3 ) & 7 ), k = tk * BORA_TILE + ( l >> 6 );
-    if( !( i < g.nx && j < g.ny && k < g.nz ) )
-    {
-        c.flag[cell] = BORA_MASKED;
-        c.mass[cell] = 0.f; c.surf[cell] = 0.f;
-        c.vx[cell] = 0.f; c.vy[cell] = 0.f; c.vz[cell] = 0.f;
-        return;
+        for( int o = 0; o < 8; ++o ) cnt += pcnt[o * 512 + l];
+        const size_t cell = (size_t)s * BORA_TILE_CELLS + l;
+        const int i = ti * BORA_TILE + ( l & 7 ), j = tj * BORA_TILE + ( ( l >> 3 ) & 7 ), k = tk * BORA_TILE + ( l >> 6 );
+        if( !( i < g.nx && j < g.ny && k < g.nz ) )
+        {
+            c.flag[cell] = BORA_MASKED;
+            c.mass[cell] = 0.f; c.surf[cell] = 0.f;
+            c.vx[cell] = 0.f; c.vy[cell] = 0.f; c.vz[cell] = 0.f;
+            continue;
+        }
+        const float ccx = (float)i + .5f, ccy = (float)j + .5f, ccz = (float)k + .5f;
+        float vx = 0.f, vy = 0.f, vz = 0.f, mass = 0.f;
+        if( m > 0.f )
+        {
+            mass = m;
+            vx = mx / m;
+            vy = my / m;
+            vz = mz / m;
+        }
+        // flags and collider velocity (FLIPMethod.cu:244-260)
+        uint8_t f;
+        const float phi = bora_col_phi( g, ccx, ccy, ccz );
+        if( m > 0.f ) f = BORA_FLUID;
+        else f = phi < 0.f ? BORA_SOLID : BORA_AIR;
+        if( phi < 0.f )
+        {
+            const float3 cv = col_velocity( &g, ccx, ccy, ccz );
+            vx += cv.x * g.col_vel_scale;
+            vy += cv.y * g.col_vel_scale;
+            vz += cv.z * g.col_vel_scale;
+        }
+        c.flag[cell] = f;
+        c.mass[cell] = mass;
+        c.surf[cell] = (float)cnt;
+        c.vx[cell] = vx;
+        c.vy[cell] = vy;
+        c.vz[cell] = vz;
     }
-    const float ccx = (float)i + .5f, ccy = (float)j + .5f, ccz = (float)k + .5f;
-    float vx = 0.f, vy = 0.f, vz = 0.f, mass = 0.f;
-    if( m > 0.f )
-    {
-        mass = m;
-        vx = mx / m;
-        vy = my / m;
-        vz = mz / m;
-    }
-    // flags and collider velocity (FLIPMethod.cu:244-260)
-    uint8_t f;
-    const float phi = bora_col_phi( g, ccx, ccy, ccz );
-    if( m > 0.f ) f = BORA_FLUID;
-    else f = phi < 0.f ? BORA_SOLID : BORA_AIR;
-    if( phi < 0.f )
-    {
-        const float3 cv = col_velocity( &g, ccx, ccy, ccz );
-        vx += cv.x * g.col_vel_scale;
-        vy += cv.y * g.col_vel_scale;
-        vz += cv.z * g.col_vel_scale;
-    }
-    c.flag[cell] = f;
-    c.mass[cell] = mass;
-    c.surf[cell] = (float)cnt;
-    c.vx[cell] = vx;
-    c.vy[cell] = vy;
-    c.vz[cell] = vz;
 }
 
 }  // namespace
