@@ -412,7 +412,10 @@ def run_reference(args, world, rank):
 
 def timed_steps(sim, sc, args, world, flip, local, sample_clocks, alg=ALG_BYTES):
     """W warm-up steps (every kernel class timed, to find the dominant one), then K timed
-    steps with only the dominant class bracketed by events. Returns the measurements."""
+    steps with the dominant class's launches bracketed by events, a few of them per step
+    (every n-th bracket: an event record ends the programmatic overlap of the kernels around it,
+    so bracketing all of a step's ~380 PCG launches would slow the step it measures). Returns
+    the measurements."""
     import numpy as np
     import torch
 
@@ -423,7 +426,10 @@ def timed_steps(sim, sc, args, world, flip, local, sample_clocks, alg=ALG_BYTES)
     classes = flip.KERNEL_CLASSES
     dom = int(np.argmax(ms[:len(classes)]))
     share = {c: float(ms[i]) for i, c in enumerate(classes)}
+    # the warm-up's mean launches per step (its first step, from rest, solves little) set the stride
+    every = max(1, int(float(n[dom]) / max(1, args.warmup)) // 4)
     sim.set_profiling(1 << dom)
+    sim.set_profiling_sampling(every)
     clocks = ClockSampler(local) if sample_clocks else None
     if clocks:
         clocks.start()
@@ -448,6 +454,7 @@ def timed_steps(sim, sc, args, world, flip, local, sample_clocks, alg=ALG_BYTES)
     clk = clocks.stop() if clocks else None
     launches = sim.stats()["kernel_launches"] - launches0
     kms, kn = sim.kernel_times()
+    sim.set_profiling_sampling(1)
     my_time = sum(step_ms) / 1e3
     t_max = allreduce_max(my_time, world)
     total_ps = allreduce_sum(float(particle_steps), world)
@@ -468,7 +475,8 @@ def timed_steps(sim, sc, args, world, flip, local, sample_clocks, alg=ALG_BYTES)
             else "fallback 6.8 TB/s",
             "alg_bytes_per_launch": bytes_per_launch, "avg_launch_ms": avg_launch_ms,
             "kernels_per_launch": (sim.stats()["mg_vcycle_launches"] if name == "mg_vcycle" else 1),
-            "launches_per_step": float(kn[dom]) / args.steps, "active_cells": ncells,
+            "launches_per_step": float(kn[dom]) * every / args.steps, "timed_launches": int(kn[dom]),
+            "timed_every": every, "active_cells": ncells,
             "share_of_warmup_device_time": {c: round(v / max(1e-9, sum(share.values())), 4)
                                             for c, v in share.items()}}
     if tnote:

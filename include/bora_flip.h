@@ -320,6 +320,11 @@ int bora_flip_get_stats( bora_flip_handle h, bora_flip_stats* out );
 /* Record CUDA events around every launch of the kernel classes in `class_mask` (bit c =
  * class c) and accumulate their device time; setting a mask resets the totals. */
 int bora_flip_set_profiling( bora_flip_handle h, uint32_t class_mask );
+/* Time only one in `every` brackets of each profiled class (1, the default: all). A bracket
+ * records an event on the handle's stream before and after the class's kernels, which ends the
+ * programmatic overlap of a kernel with its neighbours in the solver chain; sampling keeps most
+ * brackets of a long step free of it. The launch counts then count the timed brackets. */
+int bora_flip_set_profiling_sampling( bora_flip_handle h, uint32_t every );
 /* Accumulated device milliseconds and launch counts per kernel class (n <= 16 entries). */
 int bora_flip_get_kernel_times( bora_flip_handle h, double* ms, uint64_t* launches, int n );
 const char* bora_flip_status_string( int status );

@@ -196,6 +196,8 @@ struct bora_flip_sim
     cudaEvent_t ev_step[2] = { nullptr, nullptr };
     cudaEvent_t ev_join = nullptr;  // batched steps: joins this handle's stream with the batch's
     uint32_t prof_mask = 0;
+    uint32_t prof_every = 1;                       // time one bracket in prof_every per class
+    uint32_t prof_seen[BORA_KERNEL_CLASSES] = {};  // brackets of each class since the mask was set
     double kt_ms[BORA_KERNEL_CLASSES] = {};
     uint64_t kt_n[BORA_KERNEL_CLASSES] = {};
     struct Pending { int cls; cudaEvent_t a, b; };
@@ -288,7 +290,7 @@ struct KTimer
     KTimer( bora_flip_sim* sim, int c, int nkernels ) : s( sim ), cls( c )
     {
         s->stats.kernel_launches += (uint64_t)nkernels;
-        if( ( s->prof_mask >> cls ) & 1u )
+        if( ( ( s->prof_mask >> cls ) & 1u ) && s->prof_seen[cls]++ % s->prof_every == 0 )
         {
             a = s->take_event();
             cudaEventRecord( a, s->st );
@@ -2228,7 +2230,15 @@ int bora_flip_set_profiling( bora_flip_handle s, uint32_t mask )
     BORA_TRY( cudaStreamSynchronize( s->st ) );
     s->prof_resolve();
     s->prof_mask = mask;
-    for( int c = 0; c < BORA_KERNEL_CLASSES; ++c ) { s->kt_ms[c] = 0.0; s->kt_n[c] = 0; }
+    for( int c = 0; c < BORA_KERNEL_CLASSES; ++c ) { s->kt_ms[c] = 0.0; s->kt_n[c] = 0; s->prof_seen[c] = 0; }
+    return BORA_OK;
+}
+
+int bora_flip_set_profiling_sampling( bora_flip_handle s, uint32_t every )
+{
+    if( !s || every == 0 ) return BORA_ERR_INVALID_ARG;
+    s->prof_every = every;
+    for( int c = 0; c < BORA_KERNEL_CLASSES; ++c ) s->prof_seen[c] = 0;
     return BORA_OK;
 }
 

@@ -118,6 +118,7 @@ _SIGS = {
     "bora_flip_get_stats": (ctypes.c_int, [_vp, ctypes.POINTER(Stats)]),
     "bora_flip_status_string": (ctypes.c_char_p, [ctypes.c_int]),
     "bora_flip_set_profiling": (ctypes.c_int, [_vp, ctypes.c_uint32]),
+    "bora_flip_set_profiling_sampling": (ctypes.c_int, [_vp, ctypes.c_uint32]),
     "bora_flip_get_kernel_times": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int]),
     "bora_flip_set_tuning": (ctypes.c_int, [ctypes.c_int]),
     "bora_flip_set_fault": (ctypes.c_int, [_vp, ctypes.c_int]),
@@ -438,6 +439,10 @@ class FlipSim:
 
     def set_profiling(self, class_mask: int) -> None:
         _check(self.lib.bora_flip_set_profiling(self.h, class_mask), "set_profiling")
+
+    def set_profiling_sampling(self, every: int) -> None:
+        """Time one in `every` brackets of each profiled kernel class (1: all)."""
+        _check(self.lib.bora_flip_set_profiling_sampling(self.h, every), "set_profiling_sampling")
 
     def kernel_times(self):
         ms = np.zeros(16, np.float64)
