@@ -96,6 +96,13 @@ typedef struct bora_flip_params
                                 (check_every); 1: the plain form runs each refinement pass's inner
                                 PCG in one cooperative launch whose phases meet at bounded grid
                                 barriers and which checks convergence itself */
+    int warm_start;          /* 0: every pressure solve starts from p = 0, as the reference's does
+                                (its pressure field is re-created with the frame each step,
+                                FLIPMethod.cu:28-33, FluidProjection.cu:265); 1: from the last
+                                step's pressure in the cells whose tiles were active then (0
+                                elsewhere, and wherever that start is no closer to the solution
+                                than p = 0); the stop rule is the same. Batched steps
+                                (bora_flip_step_batch) take such simulations on their own */
 } bora_flip_params;
 
 typedef struct bora_flip_stats

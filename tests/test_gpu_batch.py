@@ -95,3 +95,22 @@ def test_batch_mixed_with_plain_and_empty(gpu):
     assert empty.num_particles == 0
     for u, v in zip(_by_id(plain), _by_id(ref)):
         np.testing.assert_array_equal(u, v)
+
+
+def test_warm_start_member_steps_on_its_own(gpu):
+    """A simulation with the warm start (params.warm_start) is taken out of the batched solve and
+    stepped on its own: in a batch it gives the bits of bora_flip_step, and the others still
+    give the bits they have alone."""
+    scs = _mix()[:2]
+    dt = scs[0].dt
+    mix = [flip.FlipSim.from_scene(scs[0], solver=flip.SOLVER_MIXED, warm_start=1),
+           flip.FlipSim.from_scene(scs[1], solver=flip.SOLVER_MIXED)]
+    warm = flip.FlipSim.from_scene(scs[0], solver=flip.SOLVER_MIXED, warm_start=1)
+    cold = flip.FlipSim.from_scene(scs[1], solver=flip.SOLVER_MIXED)
+    for _ in range(3):
+        assert flip.step_batch(mix, dt) == [0, 0]
+        assert warm.step(dt) == 0
+        assert flip.step_batch([cold], dt) == [0]
+    for m, alone in zip(mix, (warm, cold)):
+        for a, b, name in zip(_by_id(m), _by_id(alone), ("pos", "vel", "adj", "ids")):
+            np.testing.assert_array_equal(a, b, err_msg=name)

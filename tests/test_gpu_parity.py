@@ -465,6 +465,30 @@ def test_emission_between_steps_matches_oracle(gpu, oracle_lib):
     assert rel_err(g[0], o[0]) <= TOL and rel_err(g[1], o[1]) <= TOL
 
 
+@pytest.mark.parametrize("solver", ["plain", "mixed"])
+def test_warm_start_matches_oracle(gpu, oracle_lib, solver):
+    """params.warm_start: each solve starts from the last step's pressure (the reference's starts
+    from 0). Steps still match the oracle's (cold, FP64) steps, with fewer PCG iterations in
+    all than the same steps started cold."""
+    sc = scenes.small(32, seed=13)
+    form = gpu.SOLVER_PLAIN if solver == "plain" else gpu.SOLVER_MIXED
+    warm = gpu.FlipSim.from_scene(sc, **tight(solver=form, warm_start=1))
+    cold = gpu.FlipSim.from_scene(sc, **tight(solver=form))
+    ora = oracle_lib.Oracle(sc, block=8, solver="fp64", tol=1e-13, threads=1)
+    iters = {"warm": 0, "cold": 0}
+    for n in range(5):
+        assert warm.step(sc.dt) == 0 and cold.step(sc.dt) == 0
+        ora.step(sc.dt)
+        if n > 0:  # the first solve has no earlier pressure
+            iters["warm"] += warm.stats()["solver_iterations"]
+            iters["cold"] += cold.stats()["solver_iterations"]
+    g = by_id(*warm.particles())
+    o = by_id(*ora.particles())
+    np.testing.assert_array_equal(g[3], o[3])
+    assert rel_err(g[0], o[0]) <= TOL and rel_err(g[1], o[1]) <= TOL
+    assert iters["warm"] < iters["cold"], iters
+
+
 def test_water_tank_matches_oracle(gpu, oracle_lib):
     """FLIPMethod::fillWaterTank on the device (bit-exact particles, in the reference's
     order) and steps with the tank on: its tile rows stay active, the damping band acts."""

@@ -215,6 +215,9 @@ void bora_launch_pcg_direction( const BoraGridDev& g, int ntiles, BoraTilesDev t
                                 int dsel_in, BoraReduceDev red, int slot_rz_new, int slot_rz_old, int slot_dq_out,
                                 int slot_a_rz, int slot_a_dq, cudaStream_t st );
 // x += e (FP64); e = 0; d = 0; q = 0
+// x = the last step's pressure on fluid cells, read through the previous tile table (the warm start)
+void bora_launch_solve_warm( int ntiles, const uint16_t* code, const int32_t* tile_of, const int32_t* slot_prev,
+                             const float* pres, BoraSolverDev s, cudaStream_t st );
 void bora_launch_refine_accumulate( int ntiles, const uint16_t* code, BoraSolverDev s, int dsel, const double* ring,
                                     int slot_a_rz, int slot_a_dq, cudaStream_t st );
 // r = b - A x in FP64 (stored FP32); ||r||^2 and max|r| -> ring slots

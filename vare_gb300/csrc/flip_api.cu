@@ -131,6 +131,7 @@ struct bora_flip_sim
 
     // tiles
     DevBuf tile_flag, tile_act, tile_excl, slot_of, tile_of, nbr;
+    DevBuf slot_prev;  // the tile table of the last solve's pressure (warm start)
     int ntiles = 0;
     size_t cap_tiles = 0;
 
@@ -177,6 +178,8 @@ struct bora_flip_sim
     int32_t next_id = 0;
     bool sorted = false;   // idx/cell_start describe the current buffer
     bool keys_valid = false;  // vkey and tile_flag bin the current buffer (written by the last G2P)
+    bool pres_valid = false;  // pres holds the last solve's pressure over the current tiles
+    bool warm_ready = false;  // slot_prev is the tile table of pres (warm start of the next solve)
 
     // scratch and staging
     DevBuf scan_scratch, counters, stage_in, stage_out, live_flag;
@@ -392,6 +395,7 @@ int ensure_scan_scratch( bora_flip_sim* s, size_t n )
 int ensure_cells( bora_flip_sim* s, int ntiles )
 {
     if( (size_t)ntiles <= s->cap_tiles && s->cap_tiles ) return BORA_OK;
+    s->warm_ready = false;  // the cell fields are re-allocated: the last pressure is gone
     const size_t cap = std::max<size_t>( (size_t)ntiles, s->cap_tiles + s->cap_tiles / 2 );
     const size_t nc = cap * BORA_TILE_CELLS;
     DevBuf* f4[] = { &s->mass, &s->surf, &s->pres, &s->vx, &s->vy, &s->vz, &s->cx, &s->cy, &s->cz, &s->rhs,
@@ -451,6 +455,14 @@ int rebuild_tiles( bora_flip_sim* s )
 {
     cudaStream_t st = s->st;
     BORA_TRY( cudaMemsetAsync( s->counters.p, 0, 8 * 4, st ) );
+    // the warm start reads the last pressure through the tile table it was solved on
+    s->warm_ready = false;
+    if( s->prm.warm_start && s->pres_valid )
+    {
+        BORA_TRY( cudaMemcpyAsync( s->slot_prev.p, s->slot_of.p, s->ntv * 4, cudaMemcpyDeviceToDevice, st ) );
+        s->warm_ready = true;
+    }
+    s->pres_valid = false;
     // the last G2P binned the particles it wrote, unless they have changed since
     if( !s->keys_valid )
     {
@@ -640,6 +652,36 @@ int stage_solve( bora_flip_sim* s )
     // direction d and r.z, and the next pass carries on from them instead of restarting.
     int rz_prev = -1, dsel = 0;
     int scale_slot = s_b2;  // the latest residual norm the host has: ||b|| (r = b), then each refinement's
+    if( s->warm_ready )
+    {
+        // warm start: x = the last step's pressure, r = b - A x; kept only if closer than x = 0
+        s->warm_ready = false;
+        const int w_n2 = s->slot(), w_mx = s->slot();
+        {
+            KTimer t( s, BORA_KERNEL_REFINE, 2 );
+            bora_launch_solve_warm( s->ntiles, code, P<int32_t>( s->tile_of ), P<int32_t>( s->slot_prev ),
+                                    P<float>( s->pres ), sv, st );
+            bora_launch_refine_residual( s->g, s->ntiles, s->tiles(), b, code, sv, red, w_n2, w_mx, st );
+        }
+        BORA_TRYS( check_launch( s ) );
+        const double wnorm = std::sqrt( read_ring( s, w_n2, &status ) );
+        BORA_TRYS( status );
+        const double wmax = read_ring( s, w_mx, &status );
+        BORA_TRYS( status );
+        if( wnorm < rnorm )
+        {
+            rnorm = wnorm;
+            rmax = wmax;
+            scale_slot = w_n2;
+        }
+        else
+        {
+            const int c_b2 = s->slot(), c_bmax = s->slot();  // back to x = 0, r = b
+            { KTimer t( s, BORA_KERNEL_REFINE, 1 ); bora_launch_solve_init( s->ntiles, b, code, sv, red, c_b2, c_bmax, st ); }
+            BORA_TRYS( check_launch( s ) );
+            scale_slot = c_b2;
+        }
+    }
     for( ;; )
     {
         const bool norm_ok = rnorm <= p.tolerance * bnorm;
@@ -781,7 +823,9 @@ int stage_update_velocity( bora_flip_sim* s )
 {
     KTimer t( s, BORA_KERNEL_VELOCITY, s->ntiles > 0 );
     bora_launch_vel_update( s->g, s->ntiles, s->tiles(), s->cells(), s->st );
-    return check_launch( s );
+    const int st = check_launch( s );
+    s->pres_valid = st == BORA_OK;  // the solve's pressure (and the air cells' means) over the current tiles
+    return st;
 }
 
 // G2P, advection and kills (FLIPMethod.cu:54-175) into the other particle buffer; the kill
@@ -913,6 +957,7 @@ int post_process( bora_flip_sim* s )
     BORA_TRYS( post_tank_scan( s ) );
     BORA_TRYS( post_redistance( s ) );
     BORA_TRYS( post_attributes( s ) );
+    s->warm_ready = false;  // the post-processing stages use pres as scratch and clear it
     return BORA_OK;
 }
 
@@ -940,6 +985,7 @@ int add_particles( bora_flip_sim* s, const float* pos, const float* vel, size_t 
     s->next_id += (int32_t)n;
     s->sorted = false;
     s->keys_valid = false;
+    s->pres_valid = false;
     s->stats.num_particles = s->nlive;
     return BORA_OK;
 }
@@ -1003,6 +1049,7 @@ int bora_flip_default_params( bora_flip_params* o )
     o->advection = BORA_ADVECT_EULER;
     o->post_process = 1;
     o->persistent = 0;
+    o->warm_start = 0;
     return BORA_OK;
 }
 
@@ -1014,6 +1061,7 @@ static int validate_params( const bora_flip_params* p )
     if( p->advection != BORA_ADVECT_EULER && p->advection != BORA_ADVECT_RK2 ) return BORA_ERR_INVALID_ARG;
     if( !( p->voxel_size > 0.f ) || !( p->tolerance > 0.0 ) ) return BORA_ERR_INVALID_ARG;
     if( p->persistent != 0 && p->persistent != 1 ) return BORA_ERR_INVALID_ARG;
+    if( p->warm_start != 0 && p->warm_start != 1 ) return BORA_ERR_INVALID_ARG;
     return BORA_OK;
 }
 
@@ -1054,6 +1102,7 @@ int bora_flip_create( const bora_grid_desc* grid, const bora_flip_params* params
     if( st == BORA_OK ) st = cuda_status( grow( s->tile_act, s->ntv * 4, false, s->st ) );
     if( st == BORA_OK ) st = cuda_status( grow( s->tile_excl, s->ntv * 4, false, s->st ) );
     if( st == BORA_OK ) st = cuda_status( grow( s->slot_of, s->ntv * 4, false, s->st ) );
+    if( st == BORA_OK ) st = cuda_status( grow( s->slot_prev, s->ntv * 4, false, s->st ) );
     if( st == BORA_OK ) st = cuda_status( grow( s->counters, 64, false, s->st ) );
     if( st == BORA_OK ) st = cuda_status( grow( s->ring, BORA_RING * 8, false, s->st ) );
     if( st == BORA_OK ) st = cuda_status( grow( s->done, BORA_RING * 4, false, s->st ) );
@@ -1104,6 +1153,7 @@ int bora_flip_set_params( bora_flip_handle s, const bora_flip_params* p )
     apply_params( s );
     s->sorted = false;  // the water tank's rows change the activation
     s->keys_valid = false;
+    s->pres_valid = false;
     return BORA_OK;
 }
 
@@ -1151,6 +1201,7 @@ int bora_flip_fill_water_tank( bora_flip_handle s, size_t* added )
     s->next_id += (int32_t)n;
     s->sorted = false;
     s->keys_valid = false;
+    s->pres_valid = false;
     s->stats.num_particles = s->nlive;
     if( added ) *added = n;
     return BORA_OK;
@@ -1164,6 +1215,7 @@ int bora_flip_clear_particles( bora_flip_handle s )
     s->next_id = 0;
     s->sorted = false;
     s->keys_valid = false;
+    s->pres_valid = false;
     s->attrs = false;
     s->stats.num_particles = 0;
     return BORA_OK;
@@ -1707,14 +1759,14 @@ int bora_flip_step_batch( bora_flip_handle* hs, int n, float dt, int* status )
     cudaStream_t st = h0->st;
     const auto t0 = std::chrono::steady_clock::now();
     BORA_TRY( cudaEventRecord( h0->ev_step[0], st ) );
-    // simulations the batched solve cannot take (the plain form, no tiles, a hierarchy the
-    // coarse cluster kernel does not fit) step on their own afterwards
+    // simulations the batched solve cannot take (the plain form, the warm start, no tiles, a
+    // hierarchy the coarse cluster kernel does not fit) step on their own afterwards
     std::vector<int> pre, solo;
     for( int k = 0; k < n; ++k )
     {
         bora_flip_sim* s = hs[k];
         if( s->np == 0 ) continue;  // FLIPMethod.cu:179
-        if( s->prm.solver != BORA_SOLVER_MIXED ) { solo.push_back( k ); continue; }
+        if( s->prm.solver != BORA_SOLVER_MIXED || s->prm.warm_start ) { solo.push_back( k ); continue; }
         s->batching = true;
         pre.push_back( k );
     }
@@ -1842,6 +1894,8 @@ int bora_flip_run_post_stage( bora_flip_handle s, int stage )
         case BORA_POST_ATTRIBUTES: st = post_attributes( s ); break;
         default: return BORA_ERR_INVALID_ARG;
     }
+    s->warm_ready = false;  // post-processing uses pres as scratch
+    s->pres_valid = false;
     BORA_TRYS( st );
     BORA_TRY( cudaStreamSynchronize( s->st ) );
     s->prof_resolve();

@@ -824,6 +824,23 @@ __device__ __forceinline__ void solve_init_body( size_t ncells, const float* __r
     reduce2_publish_dfmax( n2, mx, red, slot_norm2, slot_max, bid, G );
 }
 
+// The warm start of a solve: x = the last step's pressure on fluid cells whose tile was active
+// then (slot_prev: the previous tile table, virtual tile -> slot), 0 elsewhere.
+__global__ void k_solve_warm( size_t ncells, const uint16_t* __restrict__ code, const int32_t* __restrict__ tile_of,
+                              const int32_t* __restrict__ slot_prev, const float* __restrict__ pres, float2* __restrict__ x )
+{
+    for( size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < ncells; i += (size_t)gridDim.x * blockDim.x )
+    {
+        float v = 0.f;
+        if( code[i] & BORA_CODE_FLUID )
+        {
+            const int os = slot_prev[tile_of[i >> 9]];
+            if( os >= 0 ) v = pres[(size_t)os * BORA_TILE_CELLS + ( i & ( BORA_TILE_CELLS - 1 ) )];
+        }
+        x[i] = make_float2( v, 0.f );
+    }
+}
+
 __global__ void k_solve_init( size_t ncells, const float* __restrict__ b, BoraSolverDev sv, BoraReduceDev red,
                               int slot_norm2, int slot_max )
 {
@@ -1196,6 +1213,13 @@ void bora_launch_pcg_direction( const BoraGridDev&, int ntiles, BoraTilesDev t, 
     const int grid = direction_grid( ntiles );
     bora_launch_pdl( k_pcg_direction, grid, 32 * kDirWarps, 0, st, ntiles, (const int32_t*)t.nbr, code, s, dsel_in, red,
                      slot_rz_new, slot_rz_old, slot_dq_out, slot_a_rz, slot_a_dq );
+}
+
+void bora_launch_solve_warm( int ntiles, const uint16_t* code, const int32_t* tile_of, const int32_t* slot_prev,
+                             const float* pres, BoraSolverDev s, cudaStream_t st )
+{
+    const size_t nc = (size_t)ntiles * 512;
+    if( nc ) k_solve_warm<<<grid_for( nc, 256 ), 256, 0, st>>>( nc, code, tile_of, slot_prev, pres, s.x );
 }
 
 void bora_launch_refine_accumulate( int ntiles, const uint16_t* code, BoraSolverDev s, int dsel, const double* ring,

@@ -56,7 +56,7 @@ class Params(ctypes.Structure):
                 ("redist_iteration", ctypes.c_int), ("solver", ctypes.c_int), ("tolerance", ctypes.c_double),
                 ("div_tolerance", ctypes.c_double), ("inner_tolerance", ctypes.c_double),
                 ("max_refinements", ctypes.c_int), ("check_every", ctypes.c_int), ("advection", ctypes.c_int),
-                ("post_process", ctypes.c_int), ("persistent", ctypes.c_int)]
+                ("post_process", ctypes.c_int), ("persistent", ctypes.c_int), ("warm_start", ctypes.c_int)]
 
 
 class Stats(ctypes.Structure):
