@@ -91,6 +91,8 @@ def parse():
                          "projection from the state the timed steps left)")
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-persistent", action="store_true", help="skip the persistent plain-PCG measurement")
+    ap.add_argument("--no-warm", action="store_true",
+                    help="skip the warm-start measurements (each solve started from the last step's pressure)")
     ap.add_argument("--solver", default="both", choices=["both", "plain", "mixed"],
                     help="plain only / mixed only (profiling runs); the default times both")
     return ap.parse_args()
@@ -524,6 +526,32 @@ def parity_report(flip, sc, sim, forms: dict) -> dict:
     return out
 
 
+def warm_parity(flip, sc, sim) -> dict:
+    """One warm-started step of `sim` (its solve starts from its last pressure) against the
+    oracle's step from the same particles (FP64 projection from p = 0): the errors of
+    parity_report."""
+    import numpy as np
+
+    from oracle import parity as OP
+    pos, vel, _, ids = sim.particles()
+    o = np.argsort(ids)
+    state = OP.with_state(sc, pos[o], vel[o])
+    del pos, vel, ids
+    ora = OP.oracle_step(state)
+    status = sim.step(sc.dt)
+    st = sim.stats()
+    pos, vel, _, ids = sim.particles()
+    o = np.argsort(ids, kind="stable")
+    fi = sim.frame_info()
+    dev = dict(status=status, stats=st, tiles=sim.tiles(), pres=sim.field(flip.FIELD_PRES),
+               comp=sim.field(flip.FIELD_COMP), nx=fi["nx"], ny=fi["ny"], nz=fi["nz"],
+               pos=pos[o], vel=vel[o], ids=ids[o])
+    e = OP.compare(dev, ora)
+    e["how"] = ("one warm-started device step from the state after the timed steps vs the oracle's step from the "
+                "same particles with its FP64 projection (CG to 1e-12, from p = 0); max|device - oracle| / max|oracle|")
+    return e
+
+
 def post_measure(sim, sc, flip, reps: int = 5, nvtx: bool = False) -> dict:
     """FLIPMethod::postProcess on the state the timed steps left (one frame's surface
     pipeline): host wall time of bora_flip_post_process (synchronous; it includes the
@@ -659,6 +687,28 @@ def run_ours(args, world, rank, local):
 
     post = None if args.no_post else post_measure(sim, sc, flip, args.post_reps, args.nvtx)
 
+    # both forms again with the warm start (bora_flip_params.warm_start = 1): each solve starts
+    # from the last step's pressure instead of from 0 as the reference's does; same stop rule
+    warm = None
+    if not args.no_warm and args.workload == "dam_sphere_256":
+        warm = {}
+        cold_mixed = value if args.solver == "mixed" else (mixed["value"] if mixed else None)
+        forms = {"plain": (flip.SOLVER_PLAIN, ALG_BYTES, value if args.solver != "mixed" else None),
+                 "mixed": (flip.SOLVER_MIXED, ALG_BYTES_MIXED, cold_mixed)}
+        if args.solver != "both":
+            forms = {args.solver: forms[args.solver]}
+        for name, (solver, alg, cold) in forms.items():
+            del sim
+            torch.cuda.empty_cache()
+            sim = flip.FlipSim.from_scene(sc, solver=solver, warm_start=1)
+            wm = timed_steps(sim, sc, args, world, flip, local, False, alg)
+            warm[name] = {"value": wm["value"], "unit": UNIT, "ms_per_step": wm["ms_per_step"], "p50_ms": wm["p50_ms"],
+                          "p99_ms": wm["p99_ms"], "iterations_per_step": wm["solver"]["iterations_per_step"],
+                          "all_converged": wm["solver"]["all_converged"],
+                          "speedup_over_cold_start": (wm["value"] / cold) if cold else None}
+            if not args.no_parity:
+                warm[name]["parity"] = warm_parity(flip, sc, sim)
+
     # the serving stream (64 uneven requests, Poisson arrivals) on the same GPU, after the timed steps
     serve_res = None
     if not args.no_serve and args.workload == "dam_sphere_256":
@@ -688,7 +738,8 @@ def run_ours(args, world, rank, local):
            "config": workload_config(sc, solver=args.solver if args.solver != "both" else "plain"), "roofline": roof,
            "cpu_baseline": cpu, "e2e": e2e,
            "gpu_launches": int(launches), "clocks": clk, "solver": meas["solver"], "step_roofline": meas["step_roofline"],
-           "plain_persistent": persistent, "mixed": mixed, "post_process": post, "serve": serve_res}
+           "plain_persistent": persistent, "mixed": mixed, "warm_start": warm, "post_process": post,
+           "serve": serve_res}
     print(json.dumps(out), flush=True)
 
 
