@@ -265,3 +265,27 @@ def test_direction_shuffle_schedule_matches_stencil():
                         acc = F(acc + v)
                     got[l] = F(F(diag[l]) * dd[L][i] - acc)
     np.testing.assert_array_equal(got, ref)
+
+
+def test_p2g_dual_cells_each_taken_once():
+    """k_p2g (p2g.cu) hands its threads the tile's 512 dual cells, then the 217 of its low-side
+    halo, by item number: restated here, the items cover the 9^3 dual cells of tile-local
+    coordinates -1..7 exactly once."""
+    seen = set()
+    for item in range(512 + 217):
+        if item < 512:
+            d = (item & 7, (item >> 3) & 7, item >> 6)
+        else:
+            hh = item - 512
+            if hh < 81:
+                d = (hh % 9 - 1, hh // 9 - 1, -1)
+            elif hh < 153:
+                u = hh - 81
+                d = (u % 9 - 1, -1, u // 9)
+            else:
+                u = hh - 153
+                d = (-1, u & 7, u >> 3)
+        assert all(-1 <= c <= 7 for c in d)
+        assert d not in seen
+        seen.add(d)
+    assert len(seen) == 9 ** 3
