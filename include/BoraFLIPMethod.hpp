@@ -91,6 +91,7 @@ class FLIPMethod
         double tolerance = 1e-6;
         double divTolerance = 1e-5;
         int advection = BORA_ADVECT_EULER;
+        bool warmStart = false;  // start each pressure solve from the last step's pressure (bora_flip_params.warm_start)
     } params;
 
     FLIPMethod() = default;
@@ -251,6 +252,7 @@ class FLIPMethod
         p.tolerance = params.tolerance;
         p.div_tolerance = params.divTolerance;
         p.advection = params.advection;
+        p.warm_start = params.warmStart ? 1 : 0;
         return p;
     }
 
