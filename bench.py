@@ -456,6 +456,7 @@ def timed_steps(sim, sc, args, world, flip, local, sample_clocks, alg=ALG_BYTES)
     clk = clocks.stop() if clocks else None
     launches = sim.stats()["kernel_launches"] - launches0
     kms, kn = sim.kernel_times()
+    sim.set_profiling(0)  # untimed from here: the end-to-end steps that follow record no events
     sim.set_profiling_sampling(1)
     my_time = sum(step_ms) / 1e3
     t_max = allreduce_max(my_time, world)
