@@ -371,10 +371,11 @@ uint64_t bora_serve_estimate_bytes( const bora_grid_desc* grid, size_t n, int so
     // plus the multigrid levels for the mixed form
     const uint64_t cells = std::max<uint64_t>( 512, 3 * (uint64_t)n / 8 );
     const uint64_t per_cell = 4 * 9 + 1 + 2 + 4 + 8 + 4 * 7 + 8 + 8 + ( solver == BORA_SOLVER_MIXED ? 12 : 0 );
-    // virtual tile tables
+    // virtual tile tables: activation flag (1 B), activation, its scan, the slot table and the
+    // previous step's slot table (4 B each)
     const uint64_t tiles = (uint64_t)( ( grid->nx + 8 ) / 8 + 1 ) * ( ( grid->ny + 8 ) / 8 + 1 ) * ( ( grid->nz + 8 ) / 8 + 1 );
     // geometric buffer growth keeps up to 1.5x slack
-    return ( 3 * ( (uint64_t)n * per_particle + cells * per_cell ) ) / 2 + tiles * 16 + ( 16ull << 20 );
+    return ( 3 * ( (uint64_t)n * per_particle + cells * per_cell ) ) / 2 + tiles * 20 + ( 16ull << 20 );
 }
 
 int bora_serve_default_config( bora_serve_config* out )
